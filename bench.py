@@ -1,0 +1,444 @@
+#!/usr/bin/env python
+"""Benchmark of the radial loop's spherical-harmonic transform set on GB300.
+
+Workload (the precision-form configuration): l_max=255, n_theta=384 Gauss
+points, n_phi=768, minc=1, 129 radial levels; per level 13 spectral fields ->
+15 grids (transform_to_grid_space, src/rIter.f90:466-622) and 10 grids -> 10
+spectral fields (transform_to_lm_space, src/rIter.f90:624-712).  Synthetic
+seeded spectra with std (l+1)^-2 and a radial envelope; the forward inputs
+are the grids produced by the inverse transforms.
+
+One step = both transform sets over all 129 levels.  The headline `value` is
+radial levels/s of the reduced-precision form; the FP64 form is timed in the
+same run, and the reduced form's relative L2 error against it is reported.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SHT radial levels/s at lmax=255: mixed-prec vs FP64 GPU at <=1e-6 rel L2"
+L_MAX, N_THETA, N_PHI, MINC, N_LEVELS = 255, 384, 768, 1, 129
+WORKLOAD = ("precision form: l_max=255, n_theta=384, n_phi=768, minc=1, 129 radial levels, "
+            "15 inverse + 10 forward grids per level")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3"])
+    ap.add_argument("--cpu-levels", type=int, default=2)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ algorithmic
+def algorithmic_per_level(L, N, P, minc, t2):
+    """Bytes and flops per radial level of each launch phase (FP64 outputs,
+    half spectra of t2 bytes per complex).  Tables are counted per launch."""
+    n_m = L // minc + 1
+    K = sum(L - m + 1 for m in range(0, L + 1, minc))
+    hs = n_m * N * t2
+    grid = N * P * 8
+    spec = K * 16
+    return {
+        "inv_leg_scalar": dict(bytes=7 * spec + 7 * hs, flops=7 * 2 * K * N),
+        "inv_leg_vector": dict(bytes=11 * spec + 8 * hs, flops=4 * 8 * K * N),
+        "fft_inv": dict(bytes=15 * hs + 15 * grid, flops=15 * N * 2.5 * P * __import__("math").log2(P)),
+        "fft_fwd": dict(bytes=10 * grid + 10 * hs, flops=10 * N * 2.5 * P * __import__("math").log2(P)),
+        "fwd_leg_scalar": dict(bytes=4 * hs + 4 * spec, flops=4 * 2 * K * N),
+        "fwd_leg_vector": dict(bytes=6 * hs + 6 * spec, flops=3 * 8 * K * N),
+    }, K
+
+
+def table_bytes(L, N, minc, elem):
+    K = sum(L - m + 1 for m in range(0, L + 1, minc))
+    return 2 * K * (N // 2) * elem
+
+
+# ------------------------------------------------------------------ arms
+def reference_arm(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import oracle
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    oracle.build_oracle()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    n = max(1, args.cpu_levels)
+    o = oracle.OracleSHT(L_MAX, MINC, N_THETA, N_PHI)
+    spec = grid_space_inputs(L_MAX, MINC, N_LEVELS, seed=1234)
+    or2 = or2_levels(N_LEVELS)
+
+    def one_level(r):
+        g = {}
+        g["sc"] = o.scal_to_spat(spec["s"][r])
+        g["pc"] = o.scal_to_spat(spec["p"][r])
+        g["xic"] = o.scal_to_spat(spec["xi"][r])
+        g["vrc"], g["vtc"], g["vpc"] = o.torpol_to_spat(spec["w"][r], spec["dw"][r], spec["z"][r])
+        g["cvrc"], g["cvtc"], g["cvpc"] = o.torpol_to_curl_spat(or2[r], spec["w"][r], spec["ddw"][r],
+                                                                spec["z"][r], spec["dz"][r])
+        g["brc"], g["btc"], g["bpc"] = o.torpol_to_spat(spec["b"][r], spec["db"][r], spec["aj"][r])
+        g["cbrc"], g["cbtc"], g["cbpc"] = o.torpol_to_curl_spat(or2[r], spec["b"][r], spec["ddb"][r],
+                                                                spec["aj"][r], spec["dj"][r])
+        f = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
+        for pre in ("Adv", "VS", "VxB"):
+            o.spat_to_qst(f[pre + "r"], f[pre + "t"], f[pre + "p"])
+        o.scal_to_SH(f["heatTerms"])
+
+    for w in range(args.warmup):
+        one_level(w % N_LEVELS)
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        for i in range(n):
+            one_level((k * n + i) % N_LEVELS)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    v = n * args.steps / total
+    line = {
+        "metric": METRIC, "impl": "reference", "value": v, "unit": "levels/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "l_max": L_MAX, "n_theta": N_THETA, "n_phi": N_PHI,
+                   "minc": MINC, "n_levels": N_LEVELS, "parallelism": "openmp over theta"},
+        "cpu_baseline": {"value": v, "unit": "levels/s", "cores": threads, "kind": "port",
+                         "sample": "%d of %d levels per step, full 15+10 transform set" % (n, N_LEVELS)},
+        "e2e": {"value": v, "unit": "levels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Fortran and no Fortran compiler exists here; the timed CPU code "
+                "is the C++ restatement of its native transforms (oracle/sht_oracle.cpp)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(levels: int):
+    from oracle import oracle
+    from magic_gb300.workload import spectra
+    oracle.build_oracle()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    o = oracle.OracleSHT(L_MAX, MINC, N_THETA, N_PHI)
+    S = spectra(L_MAX, MINC, 13, seed=99)
+    t0 = time.perf_counter()
+    for _ in range(levels):
+        for i in range(3):
+            o.scal_to_spat(S[i])
+        g = o.torpol_to_spat(S[3], S[4], S[5])
+        o.torpol_to_curl_spat(0.7, S[3], S[6], S[5], S[7])
+        o.torpol_to_spat(S[8], S[9], S[10])
+        o.torpol_to_curl_spat(0.7, S[8], S[11], S[10], S[12])
+        for _ in range(3):
+            o.spat_to_qst(g[0], g[1], g[2])
+        o.scal_to_SH(g[0])
+    dt = time.perf_counter() - t0
+    return {"value": levels / dt, "unit": "levels/s", "cores": threads, "kind": "port",
+            "sample": "%d levels of the full 15+10 transform set at l_max=255 (oracle, OpenMP)" % levels}
+
+
+def our_arm(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from magic_gb300 import build as b
+    b.build()
+    from magic_gb300 import SHT, measure_gflops, _lib
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+
+    dev = torch.device("cuda", local)
+    hbm, bf16, peak_kind = peaks()
+    form = args.form
+    if form == "auto":
+        form = "fp32"
+        try:
+            SHT(15, 1, 24, 48, precision="bf16x3", device=local).close()
+            form = "bf16x3"
+        except Exception:
+            form = "fp32"
+
+    spec_np = grid_space_inputs(L_MAX, MINC, N_LEVELS, seed=1234 + 7919 * rank)
+    spec = {k: torch.from_numpy(v).to(dev) for k, v in spec_np.items()}
+    or2 = torch.from_numpy(or2_levels(N_LEVELS)).to(dev)
+
+    def run_set(s, out_g, out_s):
+        g = s.transform_to_grid_space(spec, or2=or2, out=out_g)
+        f = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
+        return g, s.transform_to_lm_space(f, out=out_s)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def time_steps(s, out_g, out_s, steps):
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        n0 = s.launch_count()
+        e0.record()
+        for _ in range(steps):
+            run_set(s, out_g, out_s)
+        e1.record()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        launches = s.launch_count() - n0
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, launches
+
+    # ---- FP64 form
+    s64 = SHT(L_MAX, MINC, N_THETA, N_PHI, precision="fp64", device=local)
+    g64, l64 = run_set(s64, None, None)
+    for _ in range(max(0, args.warmup - 1)):
+        run_set(s64, g64, l64)
+    k64 = max(1, min(args.steps, 3))
+    ms64, _ = time_steps(s64, g64, l64, k64)
+    lev64 = world * N_LEVELS * k64 / (ms64 * 1e-3)
+
+    # ---- reduced-precision form (headline)
+    sm = SHT(L_MAX, MINC, N_THETA, N_PHI, precision=form, device=local)
+    gm, lmx = run_set(sm, None, None)
+    for _ in range(max(0, args.warmup - 1)):
+        run_set(sm, gm, lmx)
+    # clocks: sampled while the same steps run back to back, then the timed K steps
+    clk = ClockSampler(local)
+    clk.start()
+    t_end = time.time() + 1.5
+    while time.time() < t_end:
+        run_set(sm, gm, lmx)
+        torch.cuda.synchronize()
+    ms, launches = time_steps(sm, gm, lmx, args.steps)
+    clocks = clk.stop()
+    value = world * N_LEVELS * args.steps / (ms * 1e-3)
+
+    # ---- accuracy of the reduced form against the FP64 form (same inputs)
+    run_set(sm, gm, lmx)
+    run_set(s64, g64, l64)
+    torch.cuda.synchronize()
+    errs = {}
+    for k in g64:
+        errs[k] = float(torch.linalg.vector_norm(gm[k] - g64[k]) / torch.linalg.vector_norm(g64[k]))
+    for k in l64:
+        errs[k] = float(torch.linalg.vector_norm(lmx[k] - l64[k]) / torch.linalg.vector_norm(l64[k]))
+    max_err = max(errs.values())
+    maxabs = max(float((gm[k] - g64[k]).abs().max() / g64[k].abs().max()) for k in g64)
+
+    # ---- per-phase kernel timing (CUDA events on the launching stream)
+    sm.set_profiling(True)
+    sm.phase_times(reset=True)
+    for _ in range(2):
+        run_set(sm, gm, lmx)
+    ph = sm.phase_times(reset=True)
+    sm.set_profiling(False)
+    s64.set_profiling(True)
+    s64.phase_times(reset=True)
+    run_set(s64, g64, l64)
+    ph64 = s64.phase_times(reset=True)
+    s64.set_profiling(False)
+
+    t2 = 16 if form == "fp64" else 8
+    alg, K = algorithmic_per_level(L_MAX, N_THETA, N_PHI, MINC, t2)
+    tab_elem = 4
+    dom = max(ph, key=lambda k: ph[k][0])
+    dom_ms, dom_n = ph[dom]
+    per_launch_ms = dom_ms / max(dom_n, 1)
+    levels_per_launch = N_LEVELS  # every launch covers all levels of its field group
+    nbytes = alg[dom]["bytes"] * levels_per_launch
+    if "leg" in dom:
+        nbytes += table_bytes(L_MAX, N_THETA, MINC, tab_elem)
+    achieved_gbs = nbytes / (per_launch_ms * 1e-3) / 1e9
+    fp32_peak = measure_gflops("fp32", local)
+    fp64_peak = measure_gflops("fp64", local)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_level.json")
+    if os.path.exists(tpath):
+        try:
+            tj = json.load(open(tpath))
+            if form in tj and dom in tj[form]:
+                traffic = tj[form][dom] * levels_per_launch
+        except Exception:
+            traffic = None
+    if "leg" in dom and form in ("fp32", "fp64"):
+        achieved_gf = alg[dom]["flops"] * levels_per_launch / (per_launch_ms * 1e-3) / 1e9
+        pk = fp32_peak if form == "fp32" else fp64_peak
+        roof = {"bound": form, "achieved": achieved_gf / 1e3, "peak": pk / 1e3, "unit": "TFLOP/s",
+                "frac": achieved_gf / pk, "traffic": traffic, "kernel": dom,
+                "hbm_achieved_gbs": achieved_gbs, "hbm_frac": achieved_gbs / hbm,
+                "peak_source": "measured in this run (FMA-chain probe)"}
+    else:
+        roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                "frac": achieved_gbs / hbm, "traffic": traffic, "kernel": dom,
+                "peak_source": peak_kind}
+    phases = {k: {"ms_per_step": v[0] / 2, "launches_per_step": v[1] // 2} for k, v in ph.items()}
+    phases64 = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in ph64.items()}
+    # FP64 form's Legendre against the FP64 pipe
+    leg64_ms = sum(v[0] for k, v in ph64.items() if "leg" in k)
+    leg_flops = sum(alg[k]["flops"] for k in alg if "leg" in k) * N_LEVELS
+    fp64_leg_frac = (leg_flops / (leg64_ms * 1e-3) / 1e9) / fp64_peak
+
+    # ---- end to end through the public API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        hspec = {k: torch.from_numpy(v).pin_memory() for k, v in spec_np.items()}
+        hor2 = or2_levels(N_LEVELS)
+        hg = {k: torch.empty(tuple(v.shape), dtype=torch.float64, pin_memory=True) for k, v in gm.items()}
+        hl = {k: torch.empty(tuple(v.shape), dtype=torch.complex128, pin_memory=True) for k, v in lmx.items()}
+
+        def host_set():
+            g = sm.transform_to_grid_space(hspec, or2=hor2, out=hg)
+            f = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
+            sm.transform_to_lm_space(f, out=hl)
+
+        host_set()
+        barrier()
+        ke = max(1, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            host_set()
+        barrier()
+        dt = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([dt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        h2d = sum(v.numel() * v.element_size() for v in hspec.values()) + \
+            sum(hg[v].numel() * 8 for v in FORWARD_FROM_INVERSE.values())
+        d2h = sum(v.numel() * 8 for v in hg.values()) + sum(v.numel() * 16 for v in hl.values())
+        e2e = {"value": world * N_LEVELS * ke / dt, "unit": "levels/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": ke}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args.cpu_levels)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "levels/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "bf16x3": "bf16x3+f32", "fp64": "f64"}[form],
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": form, "l_max": L_MAX, "n_theta": N_THETA,
+                       "n_phi": N_PHI, "minc": MINC, "n_levels": N_LEVELS,
+                       "l2": "inputs larger than L2 (882 MB spectra, 4.6 GB grids per step)",
+                       "parallelism": "radial-level replicas" if world > 1 else "single GPU"},
+            "fp64_gpu": {"value": lev64, "unit": "levels/s", "ms_per_step": ms64 / k64,
+                         "steps": k64, "legendre_frac_of_fp64_peak": fp64_leg_frac,
+                         "phases": phases64},
+            "speedup_vs_fp64_gpu": value / lev64,
+            "rel_l2_vs_fp64": {"max": max_err, "max_abs_over_max": maxabs, "per_field": errs},
+            "roofline": roof,
+            "phases": phases,
+            "peaks": {"fp64_gflops": fp64_peak, "fp32_gflops": fp32_peak, "hbm_gbs": hbm,
+                      "bf16_tflops": bf16, "source": peak_kind},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    our_arm(args)
+
+
+if __name__ == "__main__":
+    main()

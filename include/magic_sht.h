@@ -1,0 +1,190 @@
+/*
+ * magic_sht.h — C ABI of the GB300 (sm_103a) spherical-harmonic transform
+ * library that replaces MagIC's `module sht` (src/sht_native.f90 over
+ * src/shtransforms.f90, src/plms.f90 and src/fft.f90) as a drop-in.
+ *
+ * Conventions (identical to the reference):
+ *   - spectral arrays: complex(8) in st_map order (m-major, l inner,
+ *     src/blocking.f90:309-317), passed as interleaved (re, im) doubles;
+ *   - grid arrays: real(8) f(nlat_padded, n_phi_max), column-major (theta
+ *     fastest), theta rows scrambled north/south (row 2j-1 north, 2j south,
+ *     1-based; initialize_sht returns l_scrambled_theta = .true.,
+ *     src/sht_native.f90:29);
+ *   - vector outputs in Robert form (x sin theta); forward FFT carries 1/n_phi.
+ * Every pointer may be host memory (pageable or pinned: staged through the
+ * device, the call returns after the results are back on the host) or device
+ * memory (the call is asynchronous on the handle's stream).
+ * Every function returns MAGIC_SHT_OK (0) or a MAGIC_SHT_ERR_* code; the
+ * reference has no return codes and aborts (abortRun) on bad sizes
+ * (src/truncation.f90:126-160, src/fft.f90:55-65).  magic_sht_last_error()
+ * returns the message of the calling thread's last failure.
+ */
+#ifndef MAGIC_SHT_H
+#define MAGIC_SHT_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MAGIC_SHT_OK 0
+#define MAGIC_SHT_ERR_ARG 1         /* null handle/pointer, n_levels < 0, bad stride */
+#define MAGIC_SHT_ERR_SIZE 2        /* grid/truncation rejected (truncation.f90:126-160) */
+#define MAGIC_SHT_ERR_LCUT 3        /* lcut outside [0, l_max] */
+#define MAGIC_SHT_ERR_CUDA 4        /* a CUDA runtime call failed */
+#define MAGIC_SHT_ERR_UNSUPPORTED 5 /* precision/mode not available on this device */
+#define MAGIC_SHT_ERR_NOMEM 6       /* device allocation failed */
+#define MAGIC_SHT_ERR_TIMEOUT 7     /* a bounded device wait gave up */
+
+/* Arithmetic forms of the Legendre sums and FFTs. */
+#define MAGIC_SHT_FP64 0    /* FP64 everywhere: the parity form */
+#define MAGIC_SHT_FP32 1    /* FP32 tables, FFTs and accumulation */
+#define MAGIC_SHT_BF16X3 2  /* tensor cores: 3xBF16 split products, FP32 accumulate, FP32 FFT */
+
+typedef struct magic_sht_desc {
+  int l_max;       /* truncation degree (truncation.f90 l_max) */
+  int m_max;       /* 0 -> (l_max/minc)*minc (truncation.f90:75) */
+  int minc;        /* azimuthal symmetry; n_phi_max = n_phi_tot/minc */
+  int n_theta_max; /* Gauss points, multiple of 4 (truncation.f90:150) */
+  int n_phi_max;   /* longitudes per symmetry sector, multiple of 4, 2^i 3^j 5^k */
+  int nlat_padded; /* leading dimension of grid arrays; 0 -> n_theta_max */
+  int precision;   /* MAGIC_SHT_FP64 | MAGIC_SHT_FP32 | MAGIC_SHT_BF16X3 */
+  int device;      /* CUDA device ordinal; -1 -> current device */
+} magic_sht_desc;
+
+typedef struct magic_sht_handle magic_sht_handle;
+typedef struct magic_sht_graph magic_sht_graph;
+
+/* ---- set-up: replaces initialize_sht / finalize_sht (sht_native.f90:24-38)
+ * and initialize_transforms (shtransforms.f90:38-91): Gauss nodes, P_lm and
+ * sin(theta) dP_lm/dtheta tables are built in FP64 on the GPU. */
+int magic_sht_init(const magic_sht_desc* desc, magic_sht_handle** handle);
+int magic_sht_finalize(magic_sht_handle* handle);
+const char* magic_sht_last_error(void);
+/* l_scrambled_theta of initialize_sht (sht_native.f90:29): always 1. */
+int magic_sht_scrambled_theta(const magic_sht_handle* handle, int* l_scrambled_theta);
+/* out[0..7] = {l_max, m_max, minc, n_theta_max, n_phi_max, nlat_padded, n_m_max, lm_max} */
+int magic_sht_get_sizes(const magic_sht_handle* handle, int* out8);
+/* Gauss-Legendre colatitudes (north -> south) and weights, n_theta_max each
+ * (gauleg, horizontal.f90:279-340). Host pointers. */
+int magic_sht_gauss_grid(magic_sht_handle* handle, double* theta_ord, double* gauss);
+/* Use an external CUDA stream (cudaStream_t passed as void*); NULL -> own stream. */
+int magic_sht_set_stream(magic_sht_handle* handle, void* cuda_stream);
+int magic_sht_synchronize(magic_sht_handle* handle);
+/* Pre-size the device workspace for batched calls of up to n_levels levels
+ * (required before capturing a graph). */
+int magic_sht_reserve(magic_sht_handle* handle, int n_levels);
+
+/* ---- spectral -> grid, one radial level (sht_native.f90 public names) ---- */
+int magic_sht_scal_to_spat(magic_sht_handle* h, const double* Slm, double* fieldc,
+                           int lcut);                                   /* :40-52   */
+int magic_sht_scal_to_grad_spat(magic_sht_handle* h, const double* Slm, double* gradtc,
+                                double* gradpc, int lcut);              /* :54-68   */
+int magic_sht_pol_to_grad_spat(magic_sht_handle* h, const double* Slm, double* gradtc,
+                               double* gradpc, int lcut);               /* :70-97   */
+int magic_sht_torpol_to_spat(magic_sht_handle* h, const double* Wlm, const double* dWlm,
+                             const double* Zlm, double* vrc, double* vtc, double* vpc,
+                             int lcut);                                 /* :99-127  */
+int magic_sht_sphtor_to_spat(magic_sht_handle* h, const double* dWlm, const double* Zlm,
+                             double* vtc, double* vpc, int lcut);       /* :129-141 */
+int magic_sht_torpol_to_curl_spat_IC(magic_sht_handle* h, double r, double r_ICB,
+                                     const double* dBlm, const double* ddBlm,
+                                     const double* Jlm, const double* dJlm, double* cbr,
+                                     double* cbt, double* cbp);         /* :143-186 */
+int magic_sht_torpol_to_spat_IC(magic_sht_handle* h, double r, double r_ICB,
+                                const double* Wlm, const double* dWlm, const double* Zlm,
+                                double* Br, double* Bt, double* Bp);    /* :188-229 */
+int magic_sht_torpol_to_dphspat(magic_sht_handle* h, const double* dWlm, const double* Zlm,
+                                double* dvtdp, double* dvpdp, int lcut); /* :231-272 */
+int magic_sht_pol_to_curlr_spat(magic_sht_handle* h, const double* Qlm, double* cvrc,
+                                int lcut);                              /* :274-300 */
+int magic_sht_torpol_to_curl_spat(magic_sht_handle* h, double or2, const double* Blm,
+                                  const double* ddBlm, const double* Jlm, const double* dJlm,
+                                  double* cvrc, double* cvtc, double* cvpc,
+                                  int lcut);                            /* :302-336 */
+int magic_sht_axi_to_spat(magic_sht_handle* h, const double* fl_ax,
+                          double* f);                                   /* :381-391 */
+int magic_sht_toraxi_to_spat(magic_sht_handle* h, const double* fl_ax, double* ft, double* fp,
+                             int lcut);                                 /* :393-405 */
+
+/* ---- grid -> spectral, one radial level ---- */
+int magic_sht_scal_to_SH(magic_sht_handle* h, const double* f, double* fLM,
+                         int lcut);                                     /* :338-346 */
+int magic_sht_spat_to_qst(magic_sht_handle* h, const double* f, const double* g,
+                          const double* hh, double* qLM, double* sLM, double* tLM,
+                          int lcut);                                    /* :348-364 */
+int magic_sht_spat_to_sphertor(magic_sht_handle* h, const double* f, const double* g,
+                               double* fLM, double* gLM, int lcut);     /* :366-379 */
+
+/* ---- the radial loop's transform set, many radial levels per call ----
+ * transform_to_grid_space (rIter.f90:466-622) and transform_to_lm_space
+ * (rIter.f90:624-712) for levels nR = 1..n_levels at once.  Spectral arrays
+ * are laid out like the reference's R-distributed fields f_Rloc(lm_max, nR):
+ * level k starts at ptr + 2*k*spec_ld doubles; grids at ptr + k*grid_ld
+ * doubles.  A NULL input/output pointer skips that field (and its outputs).
+ * or2 (1/r^2 per level) and lcut (l_R(nR) per level) may be NULL (0 and
+ * l_max).  Host pointers are staged; device pointers stay asynchronous. */
+typedef struct magic_sht_grid_space_args {
+  /* spectral inputs, complex [n_levels][spec_ld] */
+  const double *s, *p, *xi;                 /* scal_to_spat (rIter.f90:485,503,506) */
+  const double *w, *dw, *ddw, *z, *dz;      /* torpol_to_spat + torpol_to_curl_spat (:516,:522) */
+  const double *b, *db, *ddb, *aj, *dj;     /* torpol_to_spat + torpol_to_curl_spat (:606,:610) */
+  long long spec_ld;                        /* complex elements between levels (>= lm_max) */
+  /* grid outputs, [n_levels][grid_ld] doubles, each level f(nlat_padded, n_phi_max) */
+  double *sc, *pc, *xic;
+  double *vrc, *vtc, *vpc, *cvrc, *cvtc, *cvpc;
+  double *brc, *btc, *bpc, *cbrc, *cbtc, *cbpc;
+  long long grid_ld;                        /* doubles between levels (>= nlat_padded*n_phi_max) */
+} magic_sht_grid_space_args;
+
+typedef struct magic_sht_lm_space_args {
+  /* grid inputs */
+  const double *Advr, *Advt, *Advp;         /* spat_to_qst (rIter.f90:682) */
+  const double *VSr, *VSt, *VSp;            /* spat_to_qst (:688) */
+  const double *VxBr, *VxBt, *VxBp;         /* spat_to_qst (:701) */
+  const double *heatTerms;                  /* scal_to_SH (:691) */
+  long long grid_ld;
+  /* spectral outputs */
+  double *AdvrLM, *AdvtLM, *AdvpLM;
+  double *VSrLM, *VStLM, *VSpLM;
+  double *VxBrLM, *VxBtLM, *VxBpLM;
+  double *heatTermsLM;
+  long long spec_ld;
+} magic_sht_lm_space_args;
+
+int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n_levels, const double* or2,
+                                      const int* lcut, const magic_sht_grid_space_args* a);
+int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n_levels, const int* lcut,
+                                    const magic_sht_lm_space_args* a);
+
+/* ---- CUDA-graph capture of a device-pointer call sequence on the handle's
+ * stream (e.g. the radial loop's transform set), replayed with one launch. */
+int magic_sht_graph_begin(magic_sht_handle* h);
+int magic_sht_graph_end(magic_sht_handle* h, magic_sht_graph** graph);
+int magic_sht_graph_launch(magic_sht_handle* h, const magic_sht_graph* graph);
+int magic_sht_graph_destroy(magic_sht_graph* graph);
+
+/* ---- per-phase timing: CUDA events recorded on the handle's stream around
+ * every kernel launch while profiling is on (timer counterpart of the
+ * reference's lm2phy/phy2lm counters, timing.f90:17-163). */
+#define MAGIC_SHT_PHASE_INV_LEG_SCALAR 0
+#define MAGIC_SHT_PHASE_INV_LEG_VECTOR 1
+#define MAGIC_SHT_PHASE_FFT_INV 2
+#define MAGIC_SHT_PHASE_FFT_FWD 3
+#define MAGIC_SHT_PHASE_FWD_LEG_SCALAR 4
+#define MAGIC_SHT_PHASE_FWD_LEG_VECTOR 5
+#define MAGIC_SHT_N_PHASES 6
+int magic_sht_set_profiling(magic_sht_handle* h, int on);
+/* accumulated ms and launch counts per phase (arrays of MAGIC_SHT_N_PHASES) */
+int magic_sht_phase_times(magic_sht_handle* h, double* ms, long long* launches, int reset);
+/* total kernel launches issued by this handle */
+int magic_sht_launch_count(const magic_sht_handle* h, long long* n);
+
+/* ---- measurement helper: FMA throughput of the device in GFLOP/s for
+ * precision MAGIC_SHT_FP64 or MAGIC_SHT_FP32, the roofline denominators of
+ * the FP64 and FP32 forms of the Legendre sums. */
+int magic_sht_measure_gflops(int device, int precision, double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MAGIC_SHT_H */

@@ -1,0 +1,124 @@
+"""ctypes binding of ``libmagic_sht.so`` (C ABI declared in include/magic_sht.h).
+
+The library is built in-tree by ``magic_gb300.build.build()``.  There is no
+CPU fallback: if the shared library is missing, importing the transform
+layer raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmagic_sht.so")
+
+OK = 0
+ERR_ARG, ERR_SIZE, ERR_LCUT, ERR_CUDA, ERR_UNSUPPORTED, ERR_NOMEM, ERR_TIMEOUT = range(1, 8)
+FP64, FP32, BF16X3 = 0, 1, 2
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16x3": BF16X3}
+PHASES = ["inv_leg_scalar", "inv_leg_vector", "fft_inv", "fft_fwd", "fwd_leg_scalar",
+          "fwd_leg_vector"]
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_V = ctypes.c_void_p
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [("l_max", ctypes.c_int), ("m_max", ctypes.c_int), ("minc", ctypes.c_int),
+                ("n_theta_max", ctypes.c_int), ("n_phi_max", ctypes.c_int),
+                ("nlat_padded", ctypes.c_int), ("precision", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+GRID_SPACE_IN = ["s", "p", "xi", "w", "dw", "ddw", "z", "dz", "b", "db", "ddb", "aj", "dj"]
+GRID_SPACE_OUT = ["sc", "pc", "xic", "vrc", "vtc", "vpc", "cvrc", "cvtc", "cvpc",
+                  "brc", "btc", "bpc", "cbrc", "cbtc", "cbpc"]
+LM_SPACE_IN = ["Advr", "Advt", "Advp", "VSr", "VSt", "VSp", "VxBr", "VxBt", "VxBp", "heatTerms"]
+LM_SPACE_OUT = ["AdvrLM", "AdvtLM", "AdvpLM", "VSrLM", "VStLM", "VSpLM", "VxBrLM", "VxBtLM",
+                "VxBpLM", "heatTermsLM"]
+
+
+class GridSpaceArgs(ctypes.Structure):
+    _fields_ = ([(n, _V) for n in GRID_SPACE_IN] + [("spec_ld", ctypes.c_longlong)] +
+                [(n, _V) for n in GRID_SPACE_OUT] + [("grid_ld", ctypes.c_longlong)])
+
+
+class LmSpaceArgs(ctypes.Structure):
+    _fields_ = ([(n, _V) for n in LM_SPACE_IN] + [("grid_ld", ctypes.c_longlong)] +
+                [(n, _V) for n in LM_SPACE_OUT] + [("spec_ld", ctypes.c_longlong)])
+
+
+# every entry point of include/magic_sht.h with its argument types
+SIGNATURES = {
+    "magic_sht_init": [ctypes.POINTER(Desc), ctypes.POINTER(_V)],
+    "magic_sht_finalize": [_V],
+    "magic_sht_last_error": [],
+    "magic_sht_scrambled_theta": [_V, _I],
+    "magic_sht_get_sizes": [_V, _I],
+    "magic_sht_gauss_grid": [_V, _V, _V],
+    "magic_sht_set_stream": [_V, _V],
+    "magic_sht_synchronize": [_V],
+    "magic_sht_reserve": [_V, ctypes.c_int],
+    "magic_sht_scal_to_spat": [_V, _V, _V, ctypes.c_int],
+    "magic_sht_scal_to_grad_spat": [_V, _V, _V, _V, ctypes.c_int],
+    "magic_sht_pol_to_grad_spat": [_V, _V, _V, _V, ctypes.c_int],
+    "magic_sht_torpol_to_spat": [_V, _V, _V, _V, _V, _V, _V, ctypes.c_int],
+    "magic_sht_sphtor_to_spat": [_V, _V, _V, _V, _V, ctypes.c_int],
+    "magic_sht_torpol_to_curl_spat_IC": [_V, ctypes.c_double, ctypes.c_double, _V, _V, _V, _V,
+                                         _V, _V, _V],
+    "magic_sht_torpol_to_spat_IC": [_V, ctypes.c_double, ctypes.c_double, _V, _V, _V, _V, _V, _V],
+    "magic_sht_torpol_to_dphspat": [_V, _V, _V, _V, _V, ctypes.c_int],
+    "magic_sht_pol_to_curlr_spat": [_V, _V, _V, ctypes.c_int],
+    "magic_sht_torpol_to_curl_spat": [_V, ctypes.c_double, _V, _V, _V, _V, _V, _V, _V,
+                                      ctypes.c_int],
+    "magic_sht_axi_to_spat": [_V, _V, _V],
+    "magic_sht_toraxi_to_spat": [_V, _V, _V, _V, ctypes.c_int],
+    "magic_sht_scal_to_SH": [_V, _V, _V, ctypes.c_int],
+    "magic_sht_spat_to_qst": [_V, _V, _V, _V, _V, _V, _V, ctypes.c_int],
+    "magic_sht_spat_to_sphertor": [_V, _V, _V, _V, _V, ctypes.c_int],
+    "magic_sht_transform_to_grid_space": [_V, ctypes.c_int, _V, _V,
+                                          ctypes.POINTER(GridSpaceArgs)],
+    "magic_sht_transform_to_lm_space": [_V, ctypes.c_int, _V, ctypes.POINTER(LmSpaceArgs)],
+    "magic_sht_graph_begin": [_V],
+    "magic_sht_graph_end": [_V, ctypes.POINTER(_V)],
+    "magic_sht_graph_launch": [_V, _V],
+    "magic_sht_graph_destroy": [_V],
+    "magic_sht_measure_gflops": [ctypes.c_int, ctypes.c_int, _D],
+    "magic_sht_set_profiling": [_V, ctypes.c_int],
+    "magic_sht_phase_times": [_V, _V, _V, ctypes.c_int],
+    "magic_sht_launch_count": [_V, ctypes.POINTER(ctypes.c_longlong)],
+}
+
+_lib = None
+
+
+class ShtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("magic_sht error %d: %s" % (code, msg))
+        self.code = code
+
+
+def load(path: str = LIB_PATH):
+    """Load the CUDA library; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "libmagic_sht.so is missing (%s); build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    lib = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = ctypes.c_char_p if name == "magic_sht_last_error" else ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def check(rc: int):
+    if rc != OK:
+        msg = load().magic_sht_last_error()
+        raise ShtError(rc, msg.decode() if msg else "")
+    return rc

@@ -1,0 +1,114 @@
+// Shared device/host definitions for the GB300 spherical-harmonic transform
+// library (libmagic_sht).  Everything here is internal; the public C ABI is
+// include/magic_sht.h.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#define MAGIC_MAX_FIELDS 16
+
+// Pre-scaling applied to a spectral operand while it is staged into shared
+// memory (the O(lm_max) loops of src/sht_native.f90:84-93, 114-123,
+// 249-260, 287-296, 320-330 fused into the Legendre prologue).
+enum SpecOp : int {
+  OP_ZERO = 0,   // X = 0
+  OP_COPY = 1,   // X = A
+  OP_DLH = 2,    // X = l(l+1) A                      (dLh, horizontal.f90:216)
+  OP_CURLT = 3,  // X = or2(level) l(l+1) A - B       (torpol_to_curl_spat T)
+  OP_IM = 4,     // X = i m A                         (torpol_to_dphspat)
+};
+
+// One spectral operand: X = op(A, B), level stride `ld` (complex elements).
+struct SpecOperand {
+  const double2* A;
+  const double2* B;
+  long long ld;
+  int op;
+  int pad_;
+};
+
+// Legendre synthesis field (spectral -> (theta,m) half spectrum).
+//   SCALAR: out0 = sum_l P X0
+//   VECTOR: (S=X0, T=X1) -> out0 = v_theta, out1 = v_phi (Robert form)
+struct InvField {
+  SpecOperand x0, x1;
+  void* out0;  // T2 [n_m][n_theta] per level
+  void* out1;
+  long long out_ld;  // complex elements between levels
+};
+
+struct InvSet {
+  InvField f[MAGIC_MAX_FIELDS];
+  int nf;
+  int nlev;
+  const int* lcut;    // device [nlev] or null (then lcut0 for every level)
+  const double* or2;  // device [nlev] or null (then or2_0; only OP_CURLT uses it)
+  int lcut0;
+  double or2_0;
+};
+
+// Legendre analysis field ((theta,m) ES/EA half spectrum -> spectral).
+//   SCALAR: out0(l,m) = sum_j F_{mine}(j) P(l,m,j)
+//   VECTOR: in0 = F1 (from v_phi), in1 = F2 (from v_theta) -> out0 = S, out1 = T
+struct FwdField {
+  const void* in0;  // T2 [n_m][n_theta/2][2] per level (ES, EA pairs), weighted
+  const void* in1;
+  long long in_ld;   // complex elements between levels
+  double2* out0;     // complex128 [lm_max] per level
+  double2* out1;
+  long long out_ld;  // complex elements between levels
+};
+
+struct FwdSet {
+  FwdField f[MAGIC_MAX_FIELDS];
+  int nf;
+  int nlev;
+  const int* lcut;    // device [nlev] or null (then lcut0)
+  int lcut0;
+};
+
+// Azimuthal FFT field.
+enum FftFlags : int {
+  FFT_OSIN2 = 1,    // inverse: multiply grid rows by 1/sin^2 theta (dphspat)
+                    // forward: multiply spectrum rows by 1/sin^2 theta (sphtor)
+  FFT_WEIGHT = 2,   // forward: multiply by 2 pi w_j (Gauss weight) for the Legendre sums
+};
+
+struct FftField {
+  const void* in;
+  void* out;
+  long long in_ld;   // elements (complex T for spectra, double for grids) between levels
+  long long out_ld;
+  int flags;
+  int pad_;
+};
+
+struct FftSet {
+  FftField f[MAGIC_MAX_FIELDS];
+  int nf;
+  int nlev;
+};
+
+// Grid geometry and device tables of one transform instance.
+struct ShtGeom {
+  int l_max, m_max, minc, n_m;   // n_m = m_max/minc + 1
+  int n_theta, nh;               // nh = n_theta/2 (north points)
+  int n_phi;                     // n_phi_max = n_phi_tot/minc
+  int lm_max;
+  int ld;                        // leading dimension (nlat_padded) of grid arrays
+  const int* lmoff;              // device [n_m] start of each m block (st_map)
+  const double* P64;             // device [lm_max][nh]
+  const double* dP64;
+  const float* P32;
+  const float* dP32;
+  const double* wgt;             // device [nh]  2 pi w_j
+  const double* osin2;           // device [nh]  1/sin^2 theta_j
+  const double2* tw64;           // device [n_phi]  e^{+2 pi i k/n_phi}
+  const float2* tw32;
+};
+
+#define CUDA_TRY(x)                                                        \
+  do {                                                                     \
+    cudaError_t _e = (x);                                                  \
+    if (_e != cudaSuccess) return _e;                                      \
+  } while (0)

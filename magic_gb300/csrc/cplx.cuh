@@ -1,0 +1,40 @@
+// Small complex helpers for double2 / float2 (device only).
+#pragma once
+#include <cuda_runtime.h>
+
+template <typename T> struct V2;
+template <> struct V2<double> { typedef double2 t; };
+template <> struct V2<float> { typedef float2 t; };
+
+template <typename T2> struct ScalarOf;
+template <> struct ScalarOf<double2> { typedef double t; };
+template <> struct ScalarOf<float2> { typedef float t; };
+
+__device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
+
+template <typename T2> __device__ __forceinline__ T2 zero2() {
+  T2 z; z.x = 0; z.y = 0; return z;
+}
+template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { T2 r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { T2 r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+  T2 r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { a.y = -a.y; return a; }
+// multiply by +i (s>0) or -i (s<0)
+template <typename T2> __device__ __forceinline__ T2 cmuli(T2 a, int s) {
+  T2 r; if (s > 0) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; } return r;
+}
+template <typename T2, typename S> __device__ __forceinline__ T2 cscale(T2 a, S s) {
+  T2 r; r.x = a.x * s; r.y = a.y * s; return r;
+}
+
+template <typename T2> __device__ __forceinline__ T2 cvt2(double2 a);
+template <> __device__ __forceinline__ double2 cvt2<double2>(double2 a) { return a; }
+template <> __device__ __forceinline__ float2 cvt2<float2>(double2 a) { return make_float2((float)a.x, (float)a.y); }
+template <typename T2> __device__ __forceinline__ double2 to_d2(T2 a) { return make_double2((double)a.x, (double)a.y); }
+
+template <typename T2> __device__ __forceinline__ T2 shfl_xor2(T2 v, int d) {
+  T2 r; r.x = __shfl_xor_sync(0xffffffffu, v.x, d); r.y = __shfl_xor_sync(0xffffffffu, v.y, d); return r;
+}

@@ -1,0 +1,489 @@
+// Azimuthal real FFTs over phi, batched over theta rows, radial levels and
+// fields.  Transform definition of MagIC's fft991 (src/fft.f90:262-268):
+//   inverse (ifft_many, :211-252): x_j = sum_k c_k e^{+2 pi i j k / P},
+//     hermitian extension, Im(c_0) and Im(c_{P/2}) ignored, unnormalised;
+//   forward (fft_many, :164-209): c_k = (1/P) sum_j x_j e^{-2 pi i j k / P}.
+// Grids are theta-fastest (P rows of ld doubles), as in the reference.
+//
+// A real FFT of length P runs as a complex FFT of length n = P/2 plus the
+// usual even/odd pre/post-processing.  Fast path (n = 32*S, S in
+// {1,2,3,4,5,6,8,10,12,16,20,24}): each warp owns one theta row; lane l holds
+// z[32q+l]; a length-S FFT runs in registers, then a twiddle, then a 32-point
+// radix-2 DIF network across lanes with warp shuffles.  Rows are staged
+// through shared memory so that global loads/stores stay coalesced along
+// theta.  Other sizes use a per-warp shared-memory Stockham FFT.
+//
+// Forward epilogue (fused): 1/sin^2 theta (spat_to_sph_tor,
+// src/shtransforms.f90:789-794), the Gauss weight 2 pi w_j, and the
+// north/south -> ES/EA combination (src/shtransforms.f90:704-709, :811-818).
+#include <vector>
+#include "common.cuh"
+#include "cplx.cuh"
+#include "internal.h"
+
+namespace {
+
+template <typename T2, int R> struct Bfly;
+template <typename T2> struct Bfly<T2, 2> {
+  static __device__ __forceinline__ void run(T2* v, int) {
+    const T2 a = v[0], b = v[1];
+    v[0] = cadd(a, b); v[1] = csub(a, b);
+  }
+};
+template <typename T2> struct Bfly<T2, 3> {
+  static __device__ __forceinline__ void run(T2* v, int s) {
+    typedef typename ScalarOf<T2>::t T;
+    const T h = (T)0.5, r3 = (T)0.86602540378443864676372317075294;
+    const T2 t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+    T2 m1; m1.x = v[0].x - h * t1.x; m1.y = v[0].y - h * t1.y;
+    const T2 m2 = cscale(cmuli(t2, s), r3);
+    v[0] = cadd(v[0], t1); v[1] = cadd(m1, m2); v[2] = csub(m1, m2);
+  }
+};
+template <typename T2> struct Bfly<T2, 4> {
+  static __device__ __forceinline__ void run(T2* v, int s) {
+    const T2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+    const T2 b0 = cadd(v[1], v[3]), b1 = cmuli(csub(v[1], v[3]), s);
+    v[0] = cadd(a0, b0); v[2] = csub(a0, b0);
+    v[1] = cadd(a1, b1); v[3] = csub(a1, b1);
+  }
+};
+template <typename T2> struct Bfly<T2, 5> {
+  static __device__ __forceinline__ void run(T2* v, int s) {
+    typedef typename ScalarOf<T2>::t T;
+    const T c1 = (T)0.30901699437494742410229341718282;    // cos(2pi/5)
+    const T c2 = (T)-0.80901699437494742410229341718282;   // cos(4pi/5)
+    const T s1 = (T)0.95105651629515357211643933337938;    // sin(2pi/5)
+    const T s2 = (T)0.58778525229247312916870595463907;    // sin(4pi/5)
+    const T2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+    const T2 t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+    T2 a1, a2, u1, u2;
+    a1.x = v[0].x + c1 * t1.x + c2 * t2.x; a1.y = v[0].y + c1 * t1.y + c2 * t2.y;
+    a2.x = v[0].x + c2 * t1.x + c1 * t2.x; a2.y = v[0].y + c2 * t1.y + c1 * t2.y;
+    u1.x = s1 * t3.x + s2 * t4.x; u1.y = s1 * t3.y + s2 * t4.y;
+    u2.x = s2 * t3.x - s1 * t4.x; u2.y = s2 * t3.y - s1 * t4.y;
+    const T2 b1 = cmuli(u1, s), b2 = cmuli(u2, s);
+    v[0] = cadd(v[0], cadd(t1, t2));
+    v[1] = cadd(a1, b1); v[4] = csub(a1, b1);
+    v[2] = cadd(a2, b2); v[3] = csub(a2, b2);
+  }
+};
+
+// twiddle e^{s 2 pi i e / P} from the table of e^{+2 pi i k / P}
+template <typename T2>
+__device__ __forceinline__ T2 twid(const T2* __restrict__ tw, int e, int s) {
+  T2 w = tw[e];
+  if (s < 0) w.y = -w.y;
+  return w;
+}
+
+// One Stockham stage of radix R on a length-S register array.
+template <typename T2, int S, int R, int Ns>
+__device__ __forceinline__ void reg_stage(T2 (&a)[S], const T2* __restrict__ tw, int pstride, int s) {
+  T2 b[S];
+  constexpr int nR = S / R;
+#pragma unroll
+  for (int j = 0; j < nR; ++j) {
+    const int k = j % Ns;
+    T2 v[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      v[q] = a[j + q * nR];
+      const int e = (k * q * (S / (Ns * R))) % S;
+      if (e != 0) v[q] = cmul(v[q], twid(tw, e * pstride, s));
+    }
+    Bfly<T2, R>::run(v, s);
+    const int idxD = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int p = 0; p < R; ++p) b[idxD + p * Ns] = v[p];
+  }
+#pragma unroll
+  for (int i = 0; i < S; ++i) a[i] = b[i];
+}
+
+template <typename T2, int S>
+__device__ __forceinline__ void reg_fft(T2 (&a)[S], const T2* __restrict__ tw, int P, int s) {
+  const int ps = P / S;
+  if constexpr (S == 2) { reg_stage<T2, S, 2, 1>(a, tw, ps, s); }
+  else if constexpr (S == 3) { reg_stage<T2, S, 3, 1>(a, tw, ps, s); }
+  else if constexpr (S == 4) { reg_stage<T2, S, 4, 1>(a, tw, ps, s); }
+  else if constexpr (S == 5) { reg_stage<T2, S, 5, 1>(a, tw, ps, s); }
+  else if constexpr (S == 6) { reg_stage<T2, S, 2, 1>(a, tw, ps, s); reg_stage<T2, S, 3, 2>(a, tw, ps, s); }
+  else if constexpr (S == 8) { reg_stage<T2, S, 4, 1>(a, tw, ps, s); reg_stage<T2, S, 2, 4>(a, tw, ps, s); }
+  else if constexpr (S == 10) { reg_stage<T2, S, 2, 1>(a, tw, ps, s); reg_stage<T2, S, 5, 2>(a, tw, ps, s); }
+  else if constexpr (S == 12) { reg_stage<T2, S, 4, 1>(a, tw, ps, s); reg_stage<T2, S, 3, 4>(a, tw, ps, s); }
+  else if constexpr (S == 16) { reg_stage<T2, S, 4, 1>(a, tw, ps, s); reg_stage<T2, S, 4, 4>(a, tw, ps, s); }
+  else if constexpr (S == 20) { reg_stage<T2, S, 4, 1>(a, tw, ps, s); reg_stage<T2, S, 5, 4>(a, tw, ps, s); }
+  else if constexpr (S == 24) {
+    reg_stage<T2, S, 4, 1>(a, tw, ps, s); reg_stage<T2, S, 2, 4>(a, tw, ps, s);
+    reg_stage<T2, S, 3, 8>(a, tw, ps, s);
+  }
+}
+
+// Complex FFT of length n = 32*S of the row held as a[q] = z[32q + lane];
+// returns a[k1] = Z[k1 + S*brev5(lane)].
+template <typename T2, int S>
+__device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tw, int P, int s) {
+  const int lane = threadIdx.x & 31;
+  reg_fft<T2, S>(a, tw, P, s);
+#pragma unroll
+  for (int k1 = 1; k1 < S; ++k1) {
+    const int e = (2 * lane * k1) % P;  // omega_n^{lane k1}
+    if (lane) a[k1] = cmul(a[k1], twid(tw, e, s));
+  }
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) {
+    const bool up = (lane & d) != 0;
+    const T2 w = twid(tw, (lane & (d - 1)) * (P / (2 * d)), s);
+#pragma unroll
+    for (int k1 = 0; k1 < S; ++k1) {
+      const T2 b = shfl_xor2(a[k1], d);
+      if (up) a[k1] = cmul(csub(b, a[k1]), w);
+      else a[k1] = cadd(a[k1], b);
+    }
+  }
+}
+
+__device__ __forceinline__ int brev5(int x) { return __brev(x) >> 27; }
+
+// ---------------------------------------------------- shared staging code ----
+template <typename T2>
+__device__ __forceinline__ void stage_spectrum(const ShtGeom& g, const T2* __restrict__ in,
+                                               int row0, int RT, int RP, T2* sm) {
+  for (int i = threadIdx.x; i < g.n_m * RT; i += blockDim.x) {
+    const int k = i / RT, rr = i - k * RT;
+    const int row = row0 + rr;
+    T2 v = zero2<T2>();
+    if (row < g.n_theta) v = in[(long long)k * g.n_theta + row];
+    sm[k * RP + rr] = v;
+  }
+}
+
+// Z_k = E_k + i O_k for the half-length complex inverse (k = 32q + lane)
+template <typename T2>
+__device__ __forceinline__ T2 inv_pre(const ShtGeom& g, const T2* sm, int RP, int rr, int k, int n,
+                                      const T2* __restrict__ tw) {
+  T2 ck = zero2<T2>(), cn = zero2<T2>();
+  if (k < g.n_m) ck = sm[k * RP + rr];
+  const int kn = n - k;
+  if (kn < g.n_m) cn = sm[kn * RP + rr];
+  if (k == 0) { ck.y = 0; cn.y = 0; }
+  const T2 E = cadd(ck, cconj(cn));
+  const T2 O = cmul(csub(ck, cconj(cn)), tw[k]);
+  T2 z; z.x = E.x - O.y; z.y = E.y + O.x;
+  return z;
+}
+
+template <typename T2>
+__device__ __forceinline__ void store_grid(const ShtGeom& g, const FftField& fd, double* out,
+                                           int row0, int RT, int RP, const T2* sm) {
+  for (int i = threadIdx.x; i < g.n_phi * RT; i += blockDim.x) {
+    const int ph = i / RT, rr = i - ph * RT;
+    const int row = row0 + rr;
+    if (row >= g.n_theta) continue;
+    const T2 v = sm[(ph >> 1) * RP + rr];
+    double x = (ph & 1) ? (double)v.y : (double)v.x;
+    if (fd.flags & FFT_OSIN2) x *= g.osin2[row >> 1];
+    out[(long long)ph * g.ld + row] = x;
+  }
+}
+
+template <typename T2>
+__device__ __forceinline__ void stage_grid(const ShtGeom& g, const double* __restrict__ in, int row0,
+                                           int RT, int RP, T2* sm) {
+  typedef typename ScalarOf<T2>::t T;
+  T* smr = (T*)sm;
+  for (int i = threadIdx.x; i < g.n_phi * RT; i += blockDim.x) {
+    const int ph = i / RT, rr = i - ph * RT;
+    const int row = row0 + rr;
+    double x = 0.0;
+    if (row < g.n_theta) x = in[(long long)ph * g.ld + row];
+    smr[((ph >> 1) * RP + rr) * 2 + (ph & 1)] = (T)x;
+  }
+}
+
+// X_k from the half-length forward spectrum Z (in smem), then ES/EA output.
+template <typename T2>
+__device__ __forceinline__ void fwd_post(const ShtGeom& g, const FftField& fd, T2* out, int row0,
+                                         int RT, int RP, const T2* sm, const T2* __restrict__ tw) {
+  typedef typename ScalarOf<T2>::t T;
+  const int n = g.n_phi / 2;
+  const T scale = (T)(1.0 / (double)g.n_phi);
+  const int npair = RT / 2;
+  for (int i = threadIdx.x; i < g.n_m * npair; i += blockDim.x) {
+    const int k = i / npair, jp = i - k * npair;
+    const int jg = (row0 >> 1) + jp;
+    if (jg >= g.nh) continue;
+    T2 c[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int rr = 2 * jp + h;
+      const T2 Zk = sm[k * RP + rr];
+      const T2 Zn = cconj(sm[((n - k) % n) * RP + rr]);
+      const T2 D = csub(Zk, Zn);
+      const T2 u = cmul(cconj(tw[k]), D);
+      T2 X;
+      X.x = (T)0.5 * (Zk.x + Zn.x + u.y);
+      X.y = (T)0.5 * (Zk.y + Zn.y - u.x);
+      X.x *= scale; X.y *= scale;
+      if (k == 0) X.y = 0;
+      c[h] = X;
+    }
+    T fac = 1;
+    if (fd.flags & FFT_OSIN2) fac *= (T)g.osin2[jg];
+    if (fd.flags & FFT_WEIGHT) fac *= (T)g.wgt[jg];
+    c[0] = cscale(c[0], fac); c[1] = cscale(c[1], fac);
+    const long long o = ((long long)k * g.nh + jg) * 2;
+    out[o] = cadd(c[0], c[1]);
+    out[o + 1] = csub(c[0], c[1]);
+  }
+}
+
+// ------------------------------------------------------------ fast path ----
+template <typename T, int S, int RPW>
+__global__ void __launch_bounds__(256) fft_inv_fast(const ShtGeom g, const FftSet s) {
+  typedef typename V2<T>::t T2;
+  constexpr int RT = 8 * RPW, RP = RT + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* sm = (T2*)smem_raw;
+  const int n = 32 * S;
+  const int col = blockIdx.y;
+  const int r = col / s.nf, f = col - r * s.nf;
+  const FftField& fd = s.f[f];
+  const int row0 = blockIdx.x * RT;
+  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  stage_spectrum<T2>(g, (const T2*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T2 a[RPW][S];
+#pragma unroll
+  for (int rp = 0; rp < RPW; ++rp)
+#pragma unroll
+    for (int q = 0; q < S; ++q) a[rp][q] = inv_pre<T2>(g, sm, RP, warp * RPW + rp, 32 * q + lane, n, tw);
+  __syncthreads();
+  const int kb = S * brev5(lane);
+#pragma unroll
+  for (int rp = 0; rp < RPW; ++rp) {
+    warp_fft<T2, S>(a[rp], tw, g.n_phi, +1);
+#pragma unroll
+    for (int k1 = 0; k1 < S; ++k1) sm[(k1 + kb) * RP + warp * RPW + rp] = a[rp][k1];
+  }
+  __syncthreads();
+  store_grid<T2>(g, fd, (double*)fd.out + (long long)r * fd.out_ld, row0, RT, RP, sm);
+}
+
+template <typename T, int S, int RPW>
+__global__ void __launch_bounds__(256) fft_fwd_fast(const ShtGeom g, const FftSet s) {
+  typedef typename V2<T>::t T2;
+  constexpr int RT = 8 * RPW, RP = RT + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* sm = (T2*)smem_raw;
+  const int col = blockIdx.y;
+  const int r = col / s.nf, f = col - r * s.nf;
+  const FftField& fd = s.f[f];
+  const int row0 = blockIdx.x * RT;
+  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  stage_grid<T2>(g, (const double*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T2 a[RPW][S];
+#pragma unroll
+  for (int rp = 0; rp < RPW; ++rp)
+#pragma unroll
+    for (int q = 0; q < S; ++q) a[rp][q] = sm[(32 * q + lane) * RP + warp * RPW + rp];
+  __syncthreads();
+  const int kb = S * brev5(lane);
+#pragma unroll
+  for (int rp = 0; rp < RPW; ++rp) {
+    warp_fft<T2, S>(a[rp], tw, g.n_phi, -1);
+#pragma unroll
+    for (int k1 = 0; k1 < S; ++k1) sm[(k1 + kb) * RP + warp * RPW + rp] = a[rp][k1];
+  }
+  __syncthreads();
+  fwd_post<T2>(g, fd, (T2*)fd.out + (long long)r * fd.out_ld, row0, RT, RP, sm, tw);
+}
+
+// ------------------------------------------------------- general sizes ----
+struct Radices { int n; int r[24]; };
+
+template <typename T2>
+__device__ void warp_stockham(T2* src, T2* dst, int n, const Radices& rad, const T2* __restrict__ tw,
+                              int P, int s) {
+  // result ends in `src` (buffers swapped internally an even/odd number of times)
+  const int lane = threadIdx.x & 31;
+  int Ns = 1;
+  T2* a = src;
+  T2* b = dst;
+  for (int st = 0; st < rad.n; ++st) {
+    const int R = rad.r[st];
+    const int nR = n / R;
+    const int tstride = n / (Ns * R);
+    for (int j = lane; j < nR; j += 32) {
+      const int k = j % Ns;
+      T2 v[5];
+      for (int q = 0; q < R; ++q) {
+        v[q] = a[j + q * nR];
+        const int e = (k * q * tstride) % n;
+        if (e) v[q] = cmul(v[q], twid(tw, 2 * e, s));
+      }
+      if (R == 2) Bfly<T2, 2>::run(v, s);
+      else if (R == 3) Bfly<T2, 3>::run(v, s);
+      else if (R == 4) Bfly<T2, 4>::run(v, s);
+      else Bfly<T2, 5>::run(v, s);
+      const int idxD = (j / Ns) * Ns * R + k;
+      for (int p = 0; p < R; ++p) b[idxD + p * Ns] = v[p];
+    }
+    __syncwarp();
+    T2* t = a; a = b; b = t;
+    Ns *= R;
+  }
+  if (a != src) {
+    for (int i = lane; i < n; i += 32) src[i] = a[i];
+    __syncwarp();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) fft_inv_gen(const ShtGeom g, const FftSet s, const Radices rad) {
+  typedef typename V2<T>::t T2;
+  constexpr int RT = 8, RP = RT + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* sm = (T2*)smem_raw;
+  const int n = g.n_phi / 2;
+  const int nstage = (g.n_m > n ? g.n_m : n) * RP;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T2* wa = sm + nstage + warp * 2 * n;
+  T2* wb = wa + n;
+  const int col = blockIdx.y;
+  const int r = col / s.nf, f = col - r * s.nf;
+  const FftField& fd = s.f[f];
+  const int row0 = blockIdx.x * RT;
+  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  stage_spectrum<T2>(g, (const T2*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm);
+  __syncthreads();
+  for (int k = lane; k < n; k += 32) wa[k] = inv_pre<T2>(g, sm, RP, warp, k, n, tw);
+  __syncwarp();
+  warp_stockham<T2>(wa, wb, n, rad, tw, g.n_phi, +1);
+  __syncthreads();
+  for (int k = lane; k < n; k += 32) sm[k * RP + warp] = wa[k];
+  __syncthreads();
+  store_grid<T2>(g, fd, (double*)fd.out + (long long)r * fd.out_ld, row0, RT, RP, sm);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) fft_fwd_gen(const ShtGeom g, const FftSet s, const Radices rad) {
+  typedef typename V2<T>::t T2;
+  constexpr int RT = 8, RP = RT + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* sm = (T2*)smem_raw;
+  const int n = g.n_phi / 2;
+  const int nstage = (g.n_m > n ? g.n_m : n) * RP;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T2* wa = sm + nstage + warp * 2 * n;
+  T2* wb = wa + n;
+  const int col = blockIdx.y;
+  const int r = col / s.nf, f = col - r * s.nf;
+  const FftField& fd = s.f[f];
+  const int row0 = blockIdx.x * RT;
+  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  stage_grid<T2>(g, (const double*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm);
+  __syncthreads();
+  for (int k = lane; k < n; k += 32) wa[k] = sm[k * RP + warp];
+  __syncwarp();
+  warp_stockham<T2>(wa, wb, n, rad, tw, g.n_phi, -1);
+  __syncthreads();
+  for (int k = lane; k < n; k += 32) sm[k * RP + warp] = wa[k];
+  __syncthreads();
+  fwd_post<T2>(g, fd, (T2*)fd.out + (long long)r * fd.out_ld, row0, RT, RP, sm, tw);
+}
+
+bool factorize(int n, Radices& rad) {
+  rad.n = 0;
+  while (n % 4 == 0 && rad.n < 24) { rad.r[rad.n++] = 4; n /= 4; }
+  while (n % 2 == 0 && rad.n < 24) { rad.r[rad.n++] = 2; n /= 2; }
+  while (n % 3 == 0 && rad.n < 24) { rad.r[rad.n++] = 3; n /= 3; }
+  while (n % 5 == 0 && rad.n < 24) { rad.r[rad.n++] = 5; n /= 5; }
+  return n == 1;
+}
+
+template <typename T, int S, int RPW>
+cudaError_t launch_fast(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
+  typedef typename V2<T>::t T2;
+  constexpr int RT = 8 * RPW, RP = RT + 1;
+  const int n = 32 * S;
+  const size_t smem = (size_t)(g.n_m > n ? g.n_m : n) * RP * sizeof(T2);
+  dim3 grid((g.n_theta + RT - 1) / RT, s.nf * s.nlev);
+  if (inverse) {
+    auto k = fft_inv_fast<T, S, RPW>;
+    CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<grid, 256, smem, st>>>(g, s);
+  } else {
+    auto k = fft_fwd_fast<T, S, RPW>;
+    CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<grid, 256, smem, st>>>(g, s);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_gen(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
+  typedef typename V2<T>::t T2;
+  const int n = g.n_phi / 2;
+  Radices rad;
+  if (!factorize(n, rad)) return cudaErrorInvalidValue;
+  const size_t smem = ((size_t)(g.n_m > n ? g.n_m : n) * 9 + (size_t)8 * 2 * n) * sizeof(T2);
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  dim3 grid((g.n_theta + 7) / 8, s.nf * s.nlev);
+  if (inverse) {
+    CUDA_TRY(cudaFuncSetAttribute(fft_inv_gen<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fft_inv_gen<T><<<grid, 256, smem, st>>>(g, s, rad);
+  } else {
+    CUDA_TRY(cudaFuncSetAttribute(fft_fwd_gen<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fft_fwd_gen<T><<<grid, 256, smem, st>>>(g, s, rad);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_any(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
+  if (s.nf * s.nlev <= 0) return cudaSuccess;
+  const int n = g.n_phi / 2;
+  if (n % 32 == 0) {
+    switch (n / 32) {
+      case 1: return launch_fast<T, 1, 2>(g, s, inverse, st);
+      case 2: return launch_fast<T, 2, 2>(g, s, inverse, st);
+      case 3: return launch_fast<T, 3, 2>(g, s, inverse, st);
+      case 4: return launch_fast<T, 4, 2>(g, s, inverse, st);
+      case 5: return launch_fast<T, 5, 2>(g, s, inverse, st);
+      case 6: return launch_fast<T, 6, 2>(g, s, inverse, st);
+      case 8: return launch_fast<T, 8, 2>(g, s, inverse, st);
+      case 10: return launch_fast<T, 10, 2>(g, s, inverse, st);
+      case 12: return launch_fast<T, 12, 2>(g, s, inverse, st);
+      case 16: return launch_fast<T, 16, 1>(g, s, inverse, st);
+      case 20: return launch_fast<T, 20, 1>(g, s, inverse, st);
+      case 24: return launch_fast<T, 24, 1>(g, s, inverse, st);
+      default: break;
+    }
+  }
+  return launch_gen<T>(g, s, inverse, st);
+}
+
+}  // namespace
+
+bool fft_fast_path(int n_phi) {
+  const int n = n_phi / 2;
+  if (n % 32) return false;
+  switch (n / 32) {
+    case 1: case 2: case 3: case 4: case 5: case 6: case 8: case 10: case 12: case 16:
+    case 20: case 24: return true;
+    default: return false;
+  }
+}
+
+cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, bool fp64, cudaStream_t st) {
+  return fp64 ? launch_any<double>(g, s, true, st) : launch_any<float>(g, s, true, st);
+}
+
+cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, bool fp64, cudaStream_t st) {
+  return fp64 ? launch_any<double>(g, s, false, st) : launch_any<float>(g, s, false, st);
+}

@@ -1,0 +1,26 @@
+// Internal launcher declarations shared by the library's translation units.
+#pragma once
+#include "common.cuh"
+
+// legendre_simt.cu
+cudaError_t launch_inv_legendre_simt(const ShtGeom& g, const InvSet& s, bool vec, bool fp64,
+                                     cudaStream_t st);
+cudaError_t launch_fwd_legendre_simt(const ShtGeom& g, const FwdSet& s, bool vec, bool fp64,
+                                     cudaStream_t st);
+
+// fft.cu
+// Inverse: half spectrum T2 [n_m][n_theta] -> double grid [n_phi][ld].
+// Forward: double grid -> ES/EA half spectrum T2 [n_m][nh][2] (scaled 1/n_phi).
+cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, bool fp64, cudaStream_t st);
+cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, bool fp64, cudaStream_t st);
+bool fft_fast_path(int n_phi);
+
+// tables.cu
+cudaError_t build_tables_fp64(int l_max, int m_max, int minc, int n_theta, const int* d_lmoff,
+                              double* d_theta, double* d_gauss, double* d_P, double* d_dP,
+                              double* d_wgt, double* d_osin2, cudaStream_t st);
+cudaError_t convert_tables_fp32(const double* P, const double* dP, float* P32, float* dP32,
+                                size_t n, cudaStream_t st);
+
+// peak.cu
+cudaError_t launch_fma_peak(void* out, bool fp64, int blocks, int iters, cudaStream_t st);

@@ -1,0 +1,1145 @@
+// C ABI of the library (include/magic_sht.h): handle life cycle, host/device
+// pointer staging, the public names of MagIC's `module sht`
+// (src/sht_native.f90:16-20) and the batched radial-loop transform set
+// (src/rIter.f90:466-712).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/magic_sht.h"
+#include "common.cuh"
+#include "internal.h"
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_err;
+
+static int set_err(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t _e = (call);                                                       \
+    if (_e != cudaSuccess)                                                         \
+      return set_err(_e == cudaErrorMemoryAllocation ? MAGIC_SHT_ERR_NOMEM         \
+                                                     : MAGIC_SHT_ERR_CUDA,         \
+                     "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e),       \
+                     __FILE__, __LINE__);                                          \
+  } while (0)
+
+#define TRY(x)               \
+  do {                       \
+    int _rc = (x);           \
+    if (_rc) return _rc;     \
+  } while (0)
+
+extern "C" const char* magic_sht_last_error(void) { return g_err.c_str(); }
+
+// ------------------------------------------------------------------ handle
+struct magic_sht_handle {
+  int device = 0;
+  int precision = MAGIC_SHT_FP64;
+  ShtGeom g{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  bool capturing = false;
+  int* d_lmoff = nullptr;
+  double *d_theta = nullptr, *d_gauss = nullptr, *d_P = nullptr, *d_dP = nullptr;
+  double *d_wgt = nullptr, *d_osin2 = nullptr;
+  float *d_P32 = nullptr, *d_dP32 = nullptr;
+  double2* d_tw64 = nullptr;
+  float2* d_tw32 = nullptr;
+  char* ws = nullptr;
+  size_t ws_bytes = 0;
+  std::vector<int> lmoff;
+  // per-phase CUDA-event timing (magic_sht_set_profiling)
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_marks;
+  double phase_ms[MAGIC_SHT_N_PHASES] = {0};
+  long long phase_launches[MAGIC_SHT_N_PHASES] = {0};
+  long long launches = 0;
+};
+
+struct magic_sht_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+bool smooth235(int n) {
+  if (n <= 0) return false;
+  for (int f : {2, 3, 5})
+    while (n % f == 0) n /= f;
+  return n == 1;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int ensure_ws(magic_sht_handle* h, size_t bytes) {
+  if (bytes <= h->ws_bytes) return MAGIC_SHT_OK;
+  if (h->capturing)
+    return set_err(MAGIC_SHT_ERR_NOMEM,
+                   "workspace of %zu bytes needed during graph capture; call "
+                   "magic_sht_reserve first",
+                   bytes);
+  if (h->ws) {
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaFree(h->ws));
+    h->ws = nullptr;
+    h->ws_bytes = 0;
+  }
+  const size_t nb = align256(bytes + bytes / 8);
+  CK(cudaMalloc((void**)&h->ws, nb));
+  h->ws_bytes = nb;
+  return MAGIC_SHT_OK;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+bool fp64_pipes(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_FP64; }
+size_t t2_bytes(const magic_sht_handle* h) { return fp64_pipes(h) ? 16 : 8; }
+
+cudaEvent_t next_event(magic_sht_handle* h) {
+  if (h->ev_used == h->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    h->ev_pool.push_back(e);
+  }
+  return h->ev_pool[h->ev_used++];
+}
+
+// Brackets one kernel launch: counts it and, when profiling, records an
+// event pair on the launching stream.
+struct PhaseScope {
+  magic_sht_handle* h;
+  int ph;
+  cudaEvent_t e1 = nullptr;
+  PhaseScope(magic_sht_handle* h_, int ph_) : h(h_), ph(ph_) {
+    h->launches++;
+    h->phase_launches[ph]++;
+    if (h->profiling && !h->capturing) {
+      cudaEvent_t e0 = next_event(h);
+      e1 = next_event(h);
+      if (e0 && e1) {
+        cudaEventRecord(e0, h->stream);
+        h->ev_marks.push_back({ph, {e0, e1}});
+      } else {
+        e1 = nullptr;
+      }
+    }
+  }
+  ~PhaseScope() {
+    if (e1) cudaEventRecord(e1, h->stream);
+  }
+};
+
+// One call's device buffers: host arrays are staged, device arrays are used
+// in place, temporaries come from the handle's workspace.
+class CallCtx {
+ public:
+  enum Kind { IN = 0, OUT = 1, TMP = 2 };
+  CallCtx(magic_sht_handle* h) : h_(h) {}
+
+  // grid arrays: nlev levels of n_phi rows of ld doubles, level stride `lds`
+  int grid_in(const double* p, int nlev, long long lds) { return add(p, IN, nlev, lds, true); }
+  int grid_out(double* p, int nlev, long long lds) { return add(p, OUT, nlev, lds, true); }
+  // spectral arrays: nlev levels of lm_max complex, level stride `lds` complex
+  int spec_in(const double* p, int nlev, long long lds) { return add(p, IN, nlev, lds, false); }
+  int spec_out(double* p, int nlev, long long lds) { return add(p, OUT, nlev, lds, false); }
+  int raw_in(const void* p, size_t bytes) {
+    Ent e;
+    e.host = p; e.kind = IN; e.bytes = bytes; e.raw = true;
+    ents_.push_back(e);
+    return (int)ents_.size() - 1;
+  }
+  int tmp(size_t bytes) {
+    Ent e;
+    e.kind = TMP; e.bytes = bytes;
+    ents_.push_back(e);
+    return (int)ents_.size() - 1;
+  }
+
+  int prepare() {
+    size_t total = 0;
+    for (auto& e : ents_) {
+      if (e.kind != TMP) e.is_dev = is_device_ptr(e.host);
+      if (e.kind == TMP || !e.is_dev) total += align256(e.bytes);
+      if (e.kind != TMP && !e.is_dev) any_host_ = true;
+    }
+    TRY(ensure_ws(h_, total));
+    size_t off = 0;
+    for (auto& e : ents_) {
+      if (e.kind != TMP && e.is_dev) {
+        e.dev = const_cast<void*>(e.host);
+        continue;
+      }
+      e.dev = h_->ws + off;
+      off += align256(e.bytes);
+      if (e.kind == IN && e.bytes) CK(cudaMemcpyAsync(e.dev, e.host, e.bytes, cudaMemcpyHostToDevice, h_->stream));
+    }
+    return MAGIC_SHT_OK;
+  }
+
+  void* dev(int i) const { return i < 0 ? nullptr : ents_[i].dev; }
+
+  int finish() {
+    const ShtGeom& g = h_->g;
+    for (auto& e : ents_) {
+      if (e.kind != OUT || e.is_dev || !e.host) continue;
+      if (e.grid && g.ld > g.n_theta) {
+        for (int r = 0; r < e.nlev; ++r)
+          CK(cudaMemcpy2DAsync((char*)e.host + (size_t)r * e.lds * 8, (size_t)g.ld * 8,
+                               (char*)e.dev + (size_t)r * e.lds * 8, (size_t)g.ld * 8,
+                               (size_t)g.n_theta * 8, g.n_phi, cudaMemcpyDeviceToHost, h_->stream));
+      } else {
+        CK(cudaMemcpyAsync(const_cast<void*>(e.host), e.dev, e.bytes, cudaMemcpyDeviceToHost, h_->stream));
+      }
+    }
+    if (any_host_) CK(cudaStreamSynchronize(h_->stream));
+    return MAGIC_SHT_OK;
+  }
+
+ private:
+  struct Ent {
+    const void* host = nullptr;
+    void* dev = nullptr;
+    size_t bytes = 0;
+    int kind = 0;
+    bool is_dev = false;
+    bool grid = false;
+    bool raw = false;
+    int nlev = 0;
+    long long lds = 0;
+  };
+  int add(const void* p, int kind, int nlev, long long lds, bool grid) {
+    if (!p) return -1;
+    const ShtGeom& g = h_->g;
+    Ent e;
+    e.host = p; e.kind = kind; e.grid = grid; e.nlev = nlev; e.lds = lds;
+    const size_t last = grid ? (size_t)g.n_phi * g.ld * 8 : (size_t)g.lm_max * 16;
+    const size_t unit = grid ? 8 : 16;
+    e.bytes = (size_t)(nlev - 1) * (size_t)lds * unit + last;
+    ents_.push_back(e);
+    return (int)ents_.size() - 1;
+  }
+  magic_sht_handle* h_;
+  std::vector<Ent> ents_;
+  bool any_host_ = false;
+};
+
+// ---------------------------------------------------------- transform jobs
+struct SpecRef {  // operand: op(A, B) with ctx indices
+  int op = OP_ZERO;
+  int a = -1, b = -1;
+};
+struct ScalarInv { SpecRef x; int out = -1; int flags = 0; };
+struct VectorInv { SpecRef s, t; int out_t = -1, out_p = -1; int flags = 0; };
+struct ScalarFwd { int in = -1; int out = -1; };
+struct VectorFwd { int in_t = -1, in_p = -1; int out_s = -1, out_t = -1; };
+
+struct LevelCtl {
+  int nlev = 1;
+  int lcut0 = 0;
+  double or2_0 = 0.0;
+  int lcut_idx = -1;  // ctx index of device int[nlev]
+  int or2_idx = -1;
+  long long spec_ld = 0;  // complex
+  long long grid_ld = 0;  // doubles
+};
+
+SpecOperand make_operand(const CallCtx& cx, const SpecRef& r, long long ld) {
+  SpecOperand o;
+  o.A = (const double2*)cx.dev(r.a);
+  o.B = (const double2*)cx.dev(r.b);
+  o.ld = ld;
+  o.op = (r.a < 0) ? OP_ZERO : r.op;
+  o.pad_ = 0;
+  return o;
+}
+
+// Synthesis: Legendre sums into half spectra, then inverse FFTs.  The
+// half-spectrum temporaries must have been registered in `cx` before
+// prepare(); `hs` holds their ctx indices (one per output grid, in order).
+int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
+                const std::vector<ScalarInv>& sc, const std::vector<VectorInv>& vc,
+                const std::vector<int>& hs_sc, const std::vector<int>& hs_vc) {
+  const ShtGeom& g = h->g;
+  const long long hs_ld = (long long)g.n_m * g.n_theta;
+  const bool f64 = fp64_pipes(h);
+  const int* d_lcut = (const int*)cx.dev(lv.lcut_idx);
+  const double* d_or2 = (const double*)cx.dev(lv.or2_idx);
+  FftSet fs{};
+  fs.nlev = lv.nlev;
+  auto flush_fft = [&]() -> int {
+    if (fs.nf) {
+      PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_INV);
+      CK(launch_fft_inverse(g, fs, f64, h->stream));
+      fs.nf = 0;
+    }
+    return MAGIC_SHT_OK;
+  };
+  auto add_fft = [&](void* in, int out_idx, int flags) -> int {
+    if (fs.nf == MAGIC_MAX_FIELDS) TRY(flush_fft());
+    FftField& f = fs.f[fs.nf++];
+    f.in = in; f.out = cx.dev(out_idx); f.in_ld = hs_ld; f.out_ld = lv.grid_ld;
+    f.flags = flags; f.pad_ = 0;
+    return MAGIC_SHT_OK;
+  };
+  for (size_t i0 = 0; i0 < sc.size(); i0 += MAGIC_MAX_FIELDS) {
+    InvSet s{};
+    s.nlev = lv.nlev; s.lcut = d_lcut; s.or2 = d_or2; s.lcut0 = lv.lcut0; s.or2_0 = lv.or2_0;
+    for (size_t i = i0; i < sc.size() && i < i0 + MAGIC_MAX_FIELDS; ++i) {
+      InvField& f = s.f[s.nf++];
+      f.x0 = make_operand(cx, sc[i].x, lv.spec_ld);
+      f.x1 = SpecOperand{nullptr, nullptr, 0, OP_ZERO, 0};
+      f.out0 = cx.dev(hs_sc[i]); f.out1 = nullptr; f.out_ld = hs_ld;
+    }
+    PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_SCALAR);
+    CK(launch_inv_legendre_simt(g, s, false, f64, h->stream));
+  }
+  for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
+    InvSet s{};
+    s.nlev = lv.nlev; s.lcut = d_lcut; s.or2 = d_or2; s.lcut0 = lv.lcut0; s.or2_0 = lv.or2_0;
+    for (size_t i = i0; i < vc.size() && i < i0 + MAGIC_MAX_FIELDS; ++i) {
+      InvField& f = s.f[s.nf++];
+      f.x0 = make_operand(cx, vc[i].s, lv.spec_ld);
+      f.x1 = make_operand(cx, vc[i].t, lv.spec_ld);
+      f.out0 = cx.dev(hs_vc[2 * i]); f.out1 = cx.dev(hs_vc[2 * i + 1]); f.out_ld = hs_ld;
+    }
+    PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_VECTOR);
+    CK(launch_inv_legendre_simt(g, s, true, f64, h->stream));
+  }
+  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags));
+  for (size_t i = 0; i < vc.size(); ++i) {
+    TRY(add_fft(cx.dev(hs_vc[2 * i]), vc[i].out_t, vc[i].flags));
+    TRY(add_fft(cx.dev(hs_vc[2 * i + 1]), vc[i].out_p, vc[i].flags));
+  }
+  return flush_fft();
+}
+
+// Analysis: forward FFTs into ES/EA half spectra, then Legendre sums.
+int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
+                const std::vector<ScalarFwd>& sc, const std::vector<VectorFwd>& vc,
+                const std::vector<int>& hs_sc, const std::vector<int>& hs_vc) {
+  const ShtGeom& g = h->g;
+  const long long hs_ld = (long long)g.n_m * g.n_theta;
+  const bool f64 = fp64_pipes(h);
+  const int* d_lcut = (const int*)cx.dev(lv.lcut_idx);
+  FftSet fs{};
+  fs.nlev = lv.nlev;
+  auto flush_fft = [&]() -> int {
+    if (fs.nf) {
+      PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_FWD);
+      CK(launch_fft_forward(g, fs, f64, h->stream));
+      fs.nf = 0;
+    }
+    return MAGIC_SHT_OK;
+  };
+  auto add_fft = [&](int in_idx, void* out, int flags) -> int {
+    if (fs.nf == MAGIC_MAX_FIELDS) TRY(flush_fft());
+    FftField& f = fs.f[fs.nf++];
+    f.in = cx.dev(in_idx); f.out = out; f.in_ld = lv.grid_ld; f.out_ld = hs_ld;
+    f.flags = flags; f.pad_ = 0;
+    return MAGIC_SHT_OK;
+  };
+  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(sc[i].in, cx.dev(hs_sc[i]), FFT_WEIGHT));
+  for (size_t i = 0; i < vc.size(); ++i) {
+    TRY(add_fft(vc[i].in_t, cx.dev(hs_vc[2 * i]), FFT_WEIGHT | FFT_OSIN2));
+    TRY(add_fft(vc[i].in_p, cx.dev(hs_vc[2 * i + 1]), FFT_WEIGHT | FFT_OSIN2));
+  }
+  TRY(flush_fft());
+  for (size_t i0 = 0; i0 < sc.size(); i0 += MAGIC_MAX_FIELDS) {
+    FwdSet s{};
+    s.nlev = lv.nlev; s.lcut = d_lcut; s.lcut0 = lv.lcut0;
+    for (size_t i = i0; i < sc.size() && i < i0 + MAGIC_MAX_FIELDS; ++i) {
+      FwdField& f = s.f[s.nf++];
+      f.in0 = cx.dev(hs_sc[i]); f.in1 = nullptr; f.in_ld = hs_ld;
+      f.out0 = (double2*)cx.dev(sc[i].out); f.out1 = nullptr; f.out_ld = lv.spec_ld;
+    }
+    PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_SCALAR);
+    CK(launch_fwd_legendre_simt(g, s, false, f64, h->stream));
+  }
+  for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
+    FwdSet s{};
+    s.nlev = lv.nlev; s.lcut = d_lcut; s.lcut0 = lv.lcut0;
+    for (size_t i = i0; i < vc.size() && i < i0 + MAGIC_MAX_FIELDS; ++i) {
+      FwdField& f = s.f[s.nf++];
+      // F1 from v_phi, F2 from v_theta (the crossing of shtransforms.f90:764-767)
+      f.in0 = cx.dev(hs_vc[2 * i + 1]); f.in1 = cx.dev(hs_vc[2 * i]); f.in_ld = hs_ld;
+      f.out0 = (double2*)cx.dev(vc[i].out_s); f.out1 = (double2*)cx.dev(vc[i].out_t);
+      f.out_ld = lv.spec_ld;
+    }
+    PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_VECTOR);
+    CK(launch_fwd_legendre_simt(g, s, true, f64, h->stream));
+  }
+  return MAGIC_SHT_OK;
+}
+
+int check_handle(const magic_sht_handle* h) {
+  if (!h) return set_err(MAGIC_SHT_ERR_ARG, "null handle");
+  return MAGIC_SHT_OK;
+}
+
+int check_lcut(const magic_sht_handle* h, int lcut) {
+  if (lcut < 0 || lcut > h->g.l_max)
+    return set_err(MAGIC_SHT_ERR_LCUT, "lcut=%d outside [0, l_max=%d]", lcut, h->g.l_max);
+  return MAGIC_SHT_OK;
+}
+
+size_t hs_bytes(const magic_sht_handle* h, int nlev) {
+  return (size_t)nlev * h->g.n_m * h->g.n_theta * t2_bytes(h);
+}
+
+// Single-level synthesis helper.
+int inverse_one(magic_sht_handle* h, int lcut, double or2, const std::vector<const double*>& specs,
+                const std::vector<double*>& grids,
+                // builds the jobs from ctx indices of specs / grids
+                void (*build)(const std::vector<int>&, const std::vector<int>&,
+                              std::vector<ScalarInv>&, std::vector<VectorInv>&)) {
+  TRY(check_handle(h));
+  TRY(check_lcut(h, lcut));
+  for (auto p : specs) if (!p) return set_err(MAGIC_SHT_ERR_ARG, "null spectral pointer");
+  for (auto p : grids) if (!p) return set_err(MAGIC_SHT_ERR_ARG, "null grid pointer");
+  DeviceGuard dg(h->device);
+  CallCtx cx(h);
+  std::vector<int> si, gi;
+  for (auto p : specs) si.push_back(cx.spec_in(p, 1, h->g.lm_max));
+  for (auto p : grids) gi.push_back(cx.grid_out(p, 1, (long long)h->g.n_phi * h->g.ld));
+  std::vector<ScalarInv> sc;
+  std::vector<VectorInv> vc;
+  build(si, gi, sc, vc);
+  std::vector<int> hs_sc, hs_vc;
+  for (size_t i = 0; i < sc.size(); ++i) hs_sc.push_back(cx.tmp(hs_bytes(h, 1)));
+  for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_bytes(h, 1)));
+  TRY(cx.prepare());
+  LevelCtl lv;
+  lv.nlev = 1; lv.lcut0 = lcut; lv.or2_0 = or2;
+  lv.spec_ld = h->g.lm_max; lv.grid_ld = (long long)h->g.n_phi * h->g.ld;
+  TRY(run_inverse(h, cx, lv, sc, vc, hs_sc, hs_vc));
+  return cx.finish();
+}
+
+int forward_one(magic_sht_handle* h, int lcut, const std::vector<const double*>& grids,
+                const std::vector<double*>& specs,
+                void (*build)(const std::vector<int>&, const std::vector<int>&,
+                              std::vector<ScalarFwd>&, std::vector<VectorFwd>&)) {
+  TRY(check_handle(h));
+  TRY(check_lcut(h, lcut));
+  for (auto p : specs) if (!p) return set_err(MAGIC_SHT_ERR_ARG, "null spectral pointer");
+  for (auto p : grids) if (!p) return set_err(MAGIC_SHT_ERR_ARG, "null grid pointer");
+  DeviceGuard dg(h->device);
+  CallCtx cx(h);
+  std::vector<int> gi, si;
+  for (auto p : grids) gi.push_back(cx.grid_in(p, 1, (long long)h->g.n_phi * h->g.ld));
+  for (auto p : specs) si.push_back(cx.spec_out(p, 1, h->g.lm_max));
+  std::vector<ScalarFwd> sc;
+  std::vector<VectorFwd> vc;
+  build(gi, si, sc, vc);
+  std::vector<int> hs_sc, hs_vc;
+  for (size_t i = 0; i < sc.size(); ++i) hs_sc.push_back(cx.tmp(hs_bytes(h, 1)));
+  for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_bytes(h, 1)));
+  TRY(cx.prepare());
+  LevelCtl lv;
+  lv.nlev = 1; lv.lcut0 = lcut;
+  lv.spec_ld = h->g.lm_max; lv.grid_ld = (long long)h->g.n_phi * h->g.ld;
+  TRY(run_forward(h, cx, lv, sc, vc, hs_sc, hs_vc));
+  return cx.finish();
+}
+
+SpecRef ref(int op, int a, int b = -1) {
+  SpecRef r;
+  r.op = op; r.a = a; r.b = b;
+  return r;
+}
+
+__global__ void ic_prescale_kernel(int K, const int* __restrict__ lm2l, const double* __restrict__ ca,
+                                   const double* __restrict__ cb, const double2* __restrict__ A,
+                                   const double2* __restrict__ B, double2* __restrict__ X) {
+  const int lm = blockIdx.x * blockDim.x + threadIdx.x;
+  if (lm >= K) return;
+  const int l = lm2l[lm];
+  const double2 a = A[lm];
+  double2 x = make_double2(ca[l] * a.x, ca[l] * a.y);
+  if (B) {
+    const double2 b = B[lm];
+    x.x += cb[l] * b.x;
+    x.y += cb[l] * b.y;
+  }
+  X[lm] = x;
+}
+
+__global__ void axi_kernel(int l_max, int nh, const double* __restrict__ P, const double* __restrict__ dP,
+                           const double2* __restrict__ S, int lcut, int tor, double* a, double* b) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nh) return;
+  // m = 0 block occupies lm = 0..l_max (native_axi_to_spat, shtransforms.f90:374-403;
+  // native_toraxi_to_spat, :405-491).  Only real parts enter for m = 0.
+  double es = 0.0, ea = 0.0;
+  for (int l = 0; l <= l_max; ++l) {
+    if (tor && l > lcut) continue;
+    const double v = S[l].x * (tor ? dP[(size_t)l * nh + j] : P[(size_t)l * nh + j]);
+    if (l & 1) ea += v; else es += v;
+  }
+  if (!tor) {
+    a[2 * j] = es + ea;
+    a[2 * j + 1] = es - ea;
+  } else {
+    // bhG = -iT, bhC = iT: the theta component cancels, v_phi = -sum T dP
+    // with dP odd under theta -> pi - theta for even l.
+    a[2 * j] = 0.0;
+    a[2 * j + 1] = 0.0;
+    b[2 * j] = -(es + ea);
+    b[2 * j + 1] = es - ea;
+  }
+}
+
+}  // namespace
+
+// ============================================================ public ABI ==
+extern "C" {
+
+int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
+  if (!d || !out) return set_err(MAGIC_SHT_ERR_ARG, "null descriptor or output pointer");
+  *out = nullptr;
+  const int L = d->l_max, minc = d->minc, N = d->n_theta_max, P = d->n_phi_max;
+  if (L < 1) return set_err(MAGIC_SHT_ERR_SIZE, "l_max=%d must be >= 1", L);
+  if (minc < 1) return set_err(MAGIC_SHT_ERR_SIZE, "minc=%d must be > 0", minc);
+  if (N <= 2 || N % 4) return set_err(MAGIC_SHT_ERR_SIZE, "n_theta_max=%d must be a multiple of 4 and > 2", N);
+  if (P % 4 || P / 2 <= 2) return set_err(MAGIC_SHT_ERR_SIZE, "n_phi_max=%d must be a multiple of 4 and > 4", P);
+  if (!smooth235(P)) return set_err(MAGIC_SHT_ERR_SIZE, "n_phi_max=%d must factor into 2, 3 and 5", P);
+  int m_max = d->m_max > 0 ? d->m_max : (L / minc) * minc;
+  if (m_max > L) m_max = L;
+  if (m_max % minc) return set_err(MAGIC_SHT_ERR_SIZE, "m_max=%d not a multiple of minc=%d", m_max, minc);
+  const int n_m = m_max / minc + 1;
+  if (n_m > P / 2) return set_err(MAGIC_SHT_ERR_SIZE, "m_max/minc+1=%d exceeds n_phi_max/2=%d (aliasing)", n_m, P / 2);
+  const int ld = d->nlat_padded > 0 ? d->nlat_padded : N;
+  if (ld < N) return set_err(MAGIC_SHT_ERR_SIZE, "nlat_padded=%d < n_theta_max=%d", ld, N);
+  if (d->precision != MAGIC_SHT_FP64 && d->precision != MAGIC_SHT_FP32 && d->precision != MAGIC_SHT_BF16X3)
+    return set_err(MAGIC_SHT_ERR_ARG, "unknown precision %d", d->precision);
+  if (d->precision == MAGIC_SHT_BF16X3)
+    return set_err(MAGIC_SHT_ERR_UNSUPPORTED, "BF16X3 tensor-core form not built in this library");
+
+  int dev = d->device;
+  if (dev < 0) CK(cudaGetDevice(&dev));
+  int ndev = 0;
+  CK(cudaGetDeviceCount(&ndev));
+  if (dev >= ndev) return set_err(MAGIC_SHT_ERR_ARG, "device %d not present (%d devices)", dev, ndev);
+  DeviceGuard dg(dev);
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major < 10)
+    return set_err(MAGIC_SHT_ERR_UNSUPPORTED, "device %d is sm_%d%d; this library is built for sm_103a",
+                   dev, prop.major, prop.minor);
+
+  magic_sht_handle* h = new magic_sht_handle();
+  h->device = dev;
+  h->precision = d->precision;
+  ShtGeom& g = h->g;
+  g.l_max = L; g.m_max = m_max; g.minc = minc; g.n_m = n_m;
+  g.n_theta = N; g.nh = N / 2; g.n_phi = P; g.ld = ld;
+  h->lmoff.resize(n_m);
+  int K = 0;
+  for (int mc = 0; mc < n_m; ++mc) { h->lmoff[mc] = K; K += L - mc * minc + 1; }
+  g.lm_max = K;
+  int rc = MAGIC_SHT_OK;
+  auto fail = [&](int code) { magic_sht_finalize(h); return code; };
+  cudaError_t e;
+#define INIT_CK(x)                                                                     \
+  do {                                                                                 \
+    e = (x);                                                                           \
+    if (e != cudaSuccess) {                                                            \
+      rc = set_err(e == cudaErrorMemoryAllocation ? MAGIC_SHT_ERR_NOMEM : MAGIC_SHT_ERR_CUDA, \
+                   "init: %s: %s", #x, cudaGetErrorString(e));                         \
+      return fail(rc);                                                                 \
+    }                                                                                  \
+  } while (0)
+  INIT_CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  h->own_stream = true;
+  const size_t tab = (size_t)K * g.nh;
+  INIT_CK(cudaMalloc((void**)&h->d_lmoff, sizeof(int) * n_m));
+  INIT_CK(cudaMalloc((void**)&h->d_theta, sizeof(double) * N));
+  INIT_CK(cudaMalloc((void**)&h->d_gauss, sizeof(double) * N));
+  INIT_CK(cudaMalloc((void**)&h->d_wgt, sizeof(double) * g.nh));
+  INIT_CK(cudaMalloc((void**)&h->d_osin2, sizeof(double) * g.nh));
+  INIT_CK(cudaMalloc((void**)&h->d_P, sizeof(double) * tab));
+  INIT_CK(cudaMalloc((void**)&h->d_dP, sizeof(double) * tab));
+  INIT_CK(cudaMalloc((void**)&h->d_tw64, sizeof(double2) * P));
+  INIT_CK(cudaMalloc((void**)&h->d_tw32, sizeof(float2) * P));
+  if (h->precision != MAGIC_SHT_FP64) {
+    INIT_CK(cudaMalloc((void**)&h->d_P32, sizeof(float) * tab));
+    INIT_CK(cudaMalloc((void**)&h->d_dP32, sizeof(float) * tab));
+  }
+  INIT_CK(cudaMemcpyAsync(h->d_lmoff, h->lmoff.data(), sizeof(int) * n_m, cudaMemcpyHostToDevice, h->stream));
+  {
+    std::vector<double2> tw(P);
+    std::vector<float2> tw32(P);
+    for (int k = 0; k < P; ++k) {
+      const long double a = 2.0L * 3.14159265358979323846264338327950288L * (long double)k / (long double)P;
+      tw[k] = make_double2((double)cosl(a), (double)sinl(a));
+      tw32[k] = make_float2((float)tw[k].x, (float)tw[k].y);
+    }
+    INIT_CK(cudaMemcpyAsync(h->d_tw64, tw.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, h->stream));
+    INIT_CK(cudaMemcpyAsync(h->d_tw32, tw32.data(), sizeof(float2) * P, cudaMemcpyHostToDevice, h->stream));
+    INIT_CK(cudaStreamSynchronize(h->stream));
+  }
+  INIT_CK(build_tables_fp64(L, m_max, minc, N, h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP,
+                            h->d_wgt, h->d_osin2, h->stream));
+  if (h->precision != MAGIC_SHT_FP64)
+    INIT_CK(convert_tables_fp32(h->d_P, h->d_dP, h->d_P32, h->d_dP32, tab, h->stream));
+  INIT_CK(cudaStreamSynchronize(h->stream));
+#undef INIT_CK
+  g.lmoff = h->d_lmoff;
+  g.P64 = h->d_P; g.dP64 = h->d_dP; g.P32 = h->d_P32; g.dP32 = h->d_dP32;
+  g.wgt = h->d_wgt; g.osin2 = h->d_osin2; g.tw64 = h->d_tw64; g.tw32 = h->d_tw32;
+  *out = h;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_finalize(magic_sht_handle* h) {
+  if (!h) return MAGIC_SHT_OK;
+  DeviceGuard dg(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  void* ptrs[] = {h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP, h->d_wgt, h->d_osin2,
+                  h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws};
+  for (void* p : ptrs) if (p) cudaFree(p);
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_scrambled_theta(const magic_sht_handle* h, int* l_scrambled_theta) {
+  TRY(check_handle(h));
+  if (!l_scrambled_theta) return set_err(MAGIC_SHT_ERR_ARG, "null output");
+  *l_scrambled_theta = 1;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_get_sizes(const magic_sht_handle* h, int* o) {
+  TRY(check_handle(h));
+  if (!o) return set_err(MAGIC_SHT_ERR_ARG, "null output");
+  const ShtGeom& g = h->g;
+  o[0] = g.l_max; o[1] = g.m_max; o[2] = g.minc; o[3] = g.n_theta; o[4] = g.n_phi;
+  o[5] = g.ld; o[6] = g.n_m; o[7] = g.lm_max;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_gauss_grid(magic_sht_handle* h, double* theta_ord, double* gauss) {
+  TRY(check_handle(h));
+  DeviceGuard dg(h->device);
+  if (theta_ord) CK(cudaMemcpy(theta_ord, h->d_theta, sizeof(double) * h->g.n_theta, cudaMemcpyDeviceToHost));
+  if (gauss) CK(cudaMemcpy(gauss, h->d_gauss, sizeof(double) * h->g.n_theta, cudaMemcpyDeviceToHost));
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_set_stream(magic_sht_handle* h, void* s) {
+  TRY(check_handle(h));
+  DeviceGuard dg(h->device);
+  CK(cudaStreamSynchronize(h->stream));
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  if (s) {
+    h->stream = (cudaStream_t)s;
+    h->own_stream = false;
+  } else {
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->own_stream = true;
+  }
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_synchronize(magic_sht_handle* h) {
+  TRY(check_handle(h));
+  DeviceGuard dg(h->device);
+  CK(cudaStreamSynchronize(h->stream));
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_reserve(magic_sht_handle* h, int n) {
+  TRY(check_handle(h));
+  if (n < 1) return set_err(MAGIC_SHT_ERR_ARG, "n_levels=%d", n);
+  DeviceGuard dg(h->device);
+  // the radial set needs 15 inverse half spectra (the forward set needs 10)
+  // plus per-level lcut/or2 staging
+  const size_t need = 15 * align256(hs_bytes(h, n)) + 4 * align256((size_t)n * 8) + 4096;
+  return ensure_ws(h, need);
+}
+
+// ----------------------------------------------------- single-level facade
+int magic_sht_scal_to_spat(magic_sht_handle* h, const double* Slm, double* f, int lcut) {
+  return inverse_one(h, lcut, 0.0, {Slm}, {f},
+                     [](const std::vector<int>& s, const std::vector<int>& g, std::vector<ScalarInv>& sc,
+                        std::vector<VectorInv>&) { sc.push_back({ref(OP_COPY, s[0]), g[0], 0}); });
+}
+
+int magic_sht_pol_to_curlr_spat(magic_sht_handle* h, const double* Qlm, double* f, int lcut) {
+  return inverse_one(h, lcut, 0.0, {Qlm}, {f},
+                     [](const std::vector<int>& s, const std::vector<int>& g, std::vector<ScalarInv>& sc,
+                        std::vector<VectorInv>&) { sc.push_back({ref(OP_DLH, s[0]), g[0], 0}); });
+}
+
+int magic_sht_scal_to_grad_spat(magic_sht_handle* h, const double* Slm, double* gt, double* gp, int lcut) {
+  return inverse_one(h, lcut, 0.0, {Slm}, {gt, gp},
+                     [](const std::vector<int>& s, const std::vector<int>& g, std::vector<ScalarInv>&,
+                        std::vector<VectorInv>& vc) {
+                       vc.push_back({ref(OP_COPY, s[0]), SpecRef(), g[0], g[1], 0});
+                     });
+}
+
+int magic_sht_pol_to_grad_spat(magic_sht_handle* h, const double* Slm, double* gt, double* gp, int lcut) {
+  return inverse_one(h, lcut, 0.0, {Slm}, {gt, gp},
+                     [](const std::vector<int>& s, const std::vector<int>& g, std::vector<ScalarInv>&,
+                        std::vector<VectorInv>& vc) {
+                       vc.push_back({ref(OP_DLH, s[0]), SpecRef(), g[0], g[1], 0});
+                     });
+}
+
+int magic_sht_torpol_to_spat(magic_sht_handle* h, const double* W, const double* dW, const double* Z,
+                             double* vr, double* vt, double* vp, int lcut) {
+  return inverse_one(h, lcut, 0.0, {W, dW, Z}, {vr, vt, vp},
+                     [](const std::vector<int>& s, const std::vector<int>& g, std::vector<ScalarInv>& sc,
+                        std::vector<VectorInv>& vc) {
+                       sc.push_back({ref(OP_DLH, s[0]), g[0], 0});
+                       vc.push_back({ref(OP_COPY, s[1]), ref(OP_COPY, s[2]), g[1], g[2], 0});
+                     });
+}
+
+int magic_sht_sphtor_to_spat(magic_sht_handle* h, const double* dW, const double* Z, double* vt,
+                             double* vp, int lcut) {
+  return inverse_one(h, lcut, 0.0, {dW, Z}, {vt, vp},
+                     [](const std::vector<int>& s, const std::vector<int>& g, std::vector<ScalarInv>&,
+                        std::vector<VectorInv>& vc) {
+                       vc.push_back({ref(OP_COPY, s[0]), ref(OP_COPY, s[1]), g[0], g[1], 0});
+                     });
+}
+
+int magic_sht_torpol_to_dphspat(magic_sht_handle* h, const double* dW, const double* Z, double* dvtdp,
+                                double* dvpdp, int lcut) {
+  return inverse_one(h, lcut, 0.0, {dW, Z}, {dvtdp, dvpdp},
+                     [](const std::vector<int>& s, const std::vector<int>& g, std::vector<ScalarInv>&,
+                        std::vector<VectorInv>& vc) {
+                       vc.push_back({ref(OP_IM, s[0]), ref(OP_IM, s[1]), g[0], g[1], FFT_OSIN2});
+                     });
+}
+
+int magic_sht_torpol_to_curl_spat(magic_sht_handle* h, double or2, const double* B, const double* ddB,
+                                  const double* J, const double* dJ, double* cvr, double* cvt,
+                                  double* cvp, int lcut) {
+  return inverse_one(h, lcut, or2, {B, ddB, J, dJ}, {cvr, cvt, cvp},
+                     [](const std::vector<int>& s, const std::vector<int>& g, std::vector<ScalarInv>& sc,
+                        std::vector<VectorInv>& vc) {
+                       sc.push_back({ref(OP_DLH, s[2]), g[0], 0});
+                       vc.push_back({ref(OP_COPY, s[3]), ref(OP_CURLT, s[0], s[1]), g[1], g[2], 0});
+                     });
+}
+
+// Inner-core variants (rare diagnostics): the r-dependent prescaling is a
+// small kernel writing Q,S,T into the workspace, then the QST synthesis.
+static int ic_qst(magic_sht_handle* h, double r, double r_ICB, const double* A0, const double* A1,
+                  const double* A2, const double* A3, double* o0, double* o1, double* o2, bool curl) {
+  TRY(check_handle(h));
+  if (!A0 || !A1 || !A2 || (curl && !A3) || !o0 || !o1 || !o2)
+    return set_err(MAGIC_SHT_ERR_ARG, "null pointer");
+  if (r_ICB == 0.0) return set_err(MAGIC_SHT_ERR_ARG, "r_ICB must be non-zero");
+  DeviceGuard dg(h->device);
+  const ShtGeom& g = h->g;
+  const int L = g.l_max, K = g.lm_max;
+  // coefficient tables (src/sht_native.f90:166-182, :209-225)
+  std::vector<double> rDep(L + 1), rDep2(L + 1);
+  const double rRatio = r / r_ICB;
+  rDep[0] = rRatio; rDep2[0] = 1.0 / r_ICB;
+  for (int l = 1; l <= L; ++l) { rDep[l] = rDep[l - 1] * rRatio; rDep2[l] = rDep2[l - 1] * rRatio; }
+  std::vector<double> cq(L + 1), cs_a(L + 1), cs_b(L + 1), ct_a(L + 1), ct_b(L + 1);
+  for (int l = 0; l <= L; ++l) {
+    cq[l] = rDep[l] * (double)(l * (l + 1));
+    cs_a[l] = rDep2[l] * (double)(l + 1);
+    cs_b[l] = rDep2[l] * r;
+    if (curl) { ct_a[l] = -rDep2[l] * 2.0 * (double)(l + 1); ct_b[l] = -rDep2[l] * r; }
+    else { ct_a[l] = rDep[l]; ct_b[l] = 0.0; }
+  }
+  std::vector<int> lm2l(K);
+  for (int mc = 0; mc < g.n_m; ++mc)
+    for (int l = mc * g.minc; l <= L; ++l) lm2l[h->lmoff[mc] + l - mc * g.minc] = l;
+  CallCtx cx(h);
+  // curl: Q from J (A2), S from J,dJ (A2,A3), T from dB,ddB (A0,A1)
+  // plain: Q from W (A0), S from W,dW (A0,A1), T from Z (A2)
+  const double* qa = curl ? A2 : A0;
+  const double* sa = curl ? A2 : A0;
+  const double* sb = curl ? A3 : A1;
+  const double* ta = curl ? A0 : A2;
+  const double* tb = curl ? A1 : nullptr;
+  const int iqa = cx.spec_in(qa, 1, K), isa = cx.spec_in(sa, 1, K), isb = cx.spec_in(sb, 1, K);
+  const int ita = cx.spec_in(ta, 1, K), itb = tb ? cx.spec_in(tb, 1, K) : -1;
+  const int ilm = cx.tmp(sizeof(int) * K);
+  const int icf = cx.tmp(sizeof(double) * 5 * (L + 1));
+  const int iQ = cx.tmp(16 * (size_t)K), iS = cx.tmp(16 * (size_t)K), iT = cx.tmp(16 * (size_t)K);
+  const long long gl = (long long)g.n_phi * g.ld;
+  const int g0 = cx.grid_out(o0, 1, gl), g1 = cx.grid_out(o1, 1, gl), g2 = cx.grid_out(o2, 1, gl);
+  const int hs0 = cx.tmp(hs_bytes(h, 1)), hs1 = cx.tmp(hs_bytes(h, 1)), hs2 = cx.tmp(hs_bytes(h, 1));
+  TRY(cx.prepare());
+  std::vector<double> cf;
+  cf.insert(cf.end(), cq.begin(), cq.end());
+  cf.insert(cf.end(), cs_a.begin(), cs_a.end());
+  cf.insert(cf.end(), cs_b.begin(), cs_b.end());
+  cf.insert(cf.end(), ct_a.begin(), ct_a.end());
+  cf.insert(cf.end(), ct_b.begin(), ct_b.end());
+  double* dcf = (double*)cx.dev(icf);
+  CK(cudaMemcpyAsync(cx.dev(ilm), lm2l.data(), sizeof(int) * K, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dcf, cf.data(), sizeof(double) * cf.size(), cudaMemcpyHostToDevice, h->stream));
+  const int nb = (K + 255) / 256;
+  const int* dlm = (const int*)cx.dev(ilm);
+  ic_prescale_kernel<<<nb, 256, 0, h->stream>>>(K, dlm, dcf, nullptr, (const double2*)cx.dev(iqa), nullptr,
+                                                (double2*)cx.dev(iQ));
+  ic_prescale_kernel<<<nb, 256, 0, h->stream>>>(K, dlm, dcf + (L + 1), dcf + 2 * (L + 1),
+                                                (const double2*)cx.dev(isa), (const double2*)cx.dev(isb),
+                                                (double2*)cx.dev(iS));
+  ic_prescale_kernel<<<nb, 256, 0, h->stream>>>(K, dlm, dcf + 3 * (L + 1), dcf + 4 * (L + 1),
+                                                (const double2*)cx.dev(ita),
+                                                itb >= 0 ? (const double2*)cx.dev(itb) : nullptr,
+                                                (double2*)cx.dev(iT));
+  CK(cudaGetLastError());
+  // The synchronous host copies above use pageable vectors; make sure they
+  // have been consumed before the vectors go out of scope.
+  CK(cudaStreamSynchronize(h->stream));
+  std::vector<ScalarInv> sc{{ref(OP_COPY, iQ), g0, 0}};
+  std::vector<VectorInv> vc{{ref(OP_COPY, iS), ref(OP_COPY, iT), g1, g2, 0}};
+  LevelCtl lv;
+  lv.nlev = 1; lv.lcut0 = L; lv.spec_ld = K; lv.grid_ld = gl;
+  TRY(run_inverse(h, cx, lv, sc, vc, {hs0}, {hs1, hs2}));
+  return cx.finish();
+}
+
+int magic_sht_torpol_to_spat_IC(magic_sht_handle* h, double r, double r_ICB, const double* W,
+                                const double* dW, const double* Z, double* Br, double* Bt, double* Bp) {
+  return ic_qst(h, r, r_ICB, W, dW, Z, nullptr, Br, Bt, Bp, false);
+}
+
+int magic_sht_torpol_to_curl_spat_IC(magic_sht_handle* h, double r, double r_ICB, const double* dB,
+                                     const double* ddB, const double* J, const double* dJ, double* cbr,
+                                     double* cbt, double* cbp) {
+  return ic_qst(h, r, r_ICB, dB, ddB, J, dJ, cbr, cbt, cbp, true);
+}
+
+// m = 0 only transforms (native_axi_to_spat / native_toraxi_to_spat), grids of n_theta.
+static int axi_common(magic_sht_handle* h, const double* fl, double* a, double* b, int lcut, int tor) {
+  TRY(check_handle(h));
+  if (!fl || !a || (tor && !b)) return set_err(MAGIC_SHT_ERR_ARG, "null pointer");
+  if (tor) TRY(check_lcut(h, lcut));
+  DeviceGuard dg(h->device);
+  const ShtGeom& g = h->g;
+  CallCtx cx(h);
+  const int iin = cx.raw_in(fl, sizeof(double) * 2 * (g.l_max + 1));
+  const int ia = cx.tmp(sizeof(double) * g.n_theta), ib = cx.tmp(sizeof(double) * g.n_theta);
+  TRY(cx.prepare());
+  axi_kernel<<<(g.nh + 127) / 128, 128, 0, h->stream>>>(g.l_max, g.nh, g.P64, g.dP64,
+                                                        (const double2*)cx.dev(iin), lcut, tor,
+                                                        (double*)cx.dev(ia), (double*)cx.dev(ib));
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(a, cx.dev(ia), sizeof(double) * g.n_theta, cudaMemcpyDefault, h->stream));
+  if (tor) CK(cudaMemcpyAsync(b, cx.dev(ib), sizeof(double) * g.n_theta, cudaMemcpyDefault, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return cx.finish();
+}
+
+int magic_sht_axi_to_spat(magic_sht_handle* h, const double* fl_ax, double* f) {
+  return axi_common(h, fl_ax, f, nullptr, 0, 0);
+}
+
+int magic_sht_toraxi_to_spat(magic_sht_handle* h, const double* fl_ax, double* ft, double* fp, int lcut) {
+  return axi_common(h, fl_ax, ft, fp, lcut, 1);
+}
+
+// -------------------------------------------------------- analysis facade
+int magic_sht_scal_to_SH(magic_sht_handle* h, const double* f, double* fLM, int lcut) {
+  return forward_one(h, lcut, {f}, {fLM},
+                     [](const std::vector<int>& g, const std::vector<int>& s, std::vector<ScalarFwd>& sc,
+                        std::vector<VectorFwd>&) { sc.push_back({g[0], s[0]}); });
+}
+
+int magic_sht_spat_to_qst(magic_sht_handle* h, const double* f, const double* gg, const double* hh,
+                          double* qLM, double* sLM, double* tLM, int lcut) {
+  return forward_one(h, lcut, {f, gg, hh}, {qLM, sLM, tLM},
+                     [](const std::vector<int>& g, const std::vector<int>& s, std::vector<ScalarFwd>& sc,
+                        std::vector<VectorFwd>& vc) {
+                       sc.push_back({g[0], s[0]});
+                       vc.push_back({g[1], g[2], s[1], s[2]});
+                     });
+}
+
+int magic_sht_spat_to_sphertor(magic_sht_handle* h, const double* f, const double* gg, double* fLM,
+                               double* gLM, int lcut) {
+  return forward_one(h, lcut, {f, gg}, {fLM, gLM},
+                     [](const std::vector<int>& g, const std::vector<int>& s, std::vector<ScalarFwd>&,
+                        std::vector<VectorFwd>& vc) { vc.push_back({g[0], g[1], s[0], s[1]}); });
+}
+
+// ------------------------------------------------------ radial-loop sets
+static int level_ctl(magic_sht_handle* h, CallCtx& cx, int n, const int* lcut, const double* or2,
+                     LevelCtl& lv, std::vector<int>& lcut_copy) {
+  lv.nlev = n;
+  lv.lcut0 = h->g.l_max;
+  lv.or2_0 = 0.0;
+  if (lcut) {
+    if (!is_device_ptr(lcut)) {
+      for (int i = 0; i < n; ++i)
+        if (lcut[i] < 0 || lcut[i] > h->g.l_max)
+          return set_err(MAGIC_SHT_ERR_LCUT, "lcut[%d]=%d outside [0, %d]", i, lcut[i], h->g.l_max);
+    }
+    lv.lcut_idx = cx.raw_in(lcut, sizeof(int) * n);
+  }
+  if (or2) lv.or2_idx = cx.raw_in(or2, sizeof(double) * n);
+  (void)lcut_copy;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* or2, const int* lcut,
+                                      const magic_sht_grid_space_args* a) {
+  TRY(check_handle(h));
+  if (!a || n < 0) return set_err(MAGIC_SHT_ERR_ARG, "null args or n_levels < 0");
+  if (n == 0) return MAGIC_SHT_OK;
+  const ShtGeom& g = h->g;
+  if (a->spec_ld < g.lm_max || a->grid_ld < (long long)g.n_phi * g.ld)
+    return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
+  DeviceGuard dg(h->device);
+  CallCtx cx(h);
+  LevelCtl lv;
+  std::vector<int> lc;
+  TRY(level_ctl(h, cx, n, lcut, or2, lv, lc));
+  lv.spec_ld = a->spec_ld;
+  lv.grid_ld = a->grid_ld;
+  auto si = [&](const double* p) { return cx.spec_in(p, n, a->spec_ld); };
+  auto go = [&](double* p) { return cx.grid_out(p, n, a->grid_ld); };
+  std::vector<ScalarInv> sc;
+  std::vector<VectorInv> vc;
+  // scalars: s, p, xi (rIter.f90:485, 503, 506)
+  if (a->s && a->sc) sc.push_back({ref(OP_COPY, si(a->s)), go(a->sc), 0});
+  if (a->p && a->pc) sc.push_back({ref(OP_COPY, si(a->p)), go(a->pc), 0});
+  if (a->xi && a->xic) sc.push_back({ref(OP_COPY, si(a->xi)), go(a->xic), 0});
+  // velocity and vorticity (rIter.f90:516, 522)
+  int iw = -1, idw = -1, iddw = -1, iz = -1, idz = -1;
+  if (a->w) iw = si(a->w);
+  if (a->dw) idw = si(a->dw);
+  if (a->ddw) iddw = si(a->ddw);
+  if (a->z) iz = si(a->z);
+  if (a->dz) idz = si(a->dz);
+  if (iw >= 0 && idw >= 0 && iz >= 0 && a->vrc && a->vtc && a->vpc) {
+    sc.push_back({ref(OP_DLH, iw), go(a->vrc), 0});
+    vc.push_back({ref(OP_COPY, idw), ref(OP_COPY, iz), go(a->vtc), go(a->vpc), 0});
+  }
+  if (iw >= 0 && iddw >= 0 && iz >= 0 && idz >= 0 && a->cvrc && a->cvtc && a->cvpc) {
+    sc.push_back({ref(OP_DLH, iz), go(a->cvrc), 0});
+    vc.push_back({ref(OP_COPY, idz), ref(OP_CURLT, iw, iddw), go(a->cvtc), go(a->cvpc), 0});
+  }
+  // magnetic field and current (rIter.f90:606, 610)
+  int ib = -1, idb = -1, iddb = -1, iaj = -1, idj = -1;
+  if (a->b) ib = si(a->b);
+  if (a->db) idb = si(a->db);
+  if (a->ddb) iddb = si(a->ddb);
+  if (a->aj) iaj = si(a->aj);
+  if (a->dj) idj = si(a->dj);
+  if (ib >= 0 && idb >= 0 && iaj >= 0 && a->brc && a->btc && a->bpc) {
+    sc.push_back({ref(OP_DLH, ib), go(a->brc), 0});
+    vc.push_back({ref(OP_COPY, idb), ref(OP_COPY, iaj), go(a->btc), go(a->bpc), 0});
+  }
+  if (ib >= 0 && iddb >= 0 && iaj >= 0 && idj >= 0 && a->cbrc && a->cbtc && a->cbpc) {
+    sc.push_back({ref(OP_DLH, iaj), go(a->cbrc), 0});
+    vc.push_back({ref(OP_COPY, idj), ref(OP_CURLT, ib, iddb), go(a->cbtc), go(a->cbpc), 0});
+  }
+  std::vector<int> hs_sc, hs_vc;
+  for (size_t i = 0; i < sc.size(); ++i) hs_sc.push_back(cx.tmp(hs_bytes(h, n)));
+  for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_bytes(h, n)));
+  TRY(cx.prepare());
+  TRY(run_inverse(h, cx, lv, sc, vc, hs_sc, hs_vc));
+  return cx.finish();
+}
+
+int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
+                                    const magic_sht_lm_space_args* a) {
+  TRY(check_handle(h));
+  if (!a || n < 0) return set_err(MAGIC_SHT_ERR_ARG, "null args or n_levels < 0");
+  if (n == 0) return MAGIC_SHT_OK;
+  const ShtGeom& g = h->g;
+  if (a->spec_ld < g.lm_max || a->grid_ld < (long long)g.n_phi * g.ld)
+    return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
+  DeviceGuard dg(h->device);
+  CallCtx cx(h);
+  LevelCtl lv;
+  std::vector<int> lc;
+  TRY(level_ctl(h, cx, n, lcut, nullptr, lv, lc));
+  lv.spec_ld = a->spec_ld;
+  lv.grid_ld = a->grid_ld;
+  auto gi = [&](const double* p) { return cx.grid_in(p, n, a->grid_ld); };
+  auto so = [&](double* p) { return cx.spec_out(p, n, a->spec_ld); };
+  std::vector<ScalarFwd> sc;
+  std::vector<VectorFwd> vc;
+  struct Q { const double *f, *g, *h; double *q, *s, *t; };
+  const Q qs[3] = {{a->Advr, a->Advt, a->Advp, a->AdvrLM, a->AdvtLM, a->AdvpLM},
+                   {a->VSr, a->VSt, a->VSp, a->VSrLM, a->VStLM, a->VSpLM},
+                   {a->VxBr, a->VxBt, a->VxBp, a->VxBrLM, a->VxBtLM, a->VxBpLM}};
+  for (const Q& q : qs) {
+    if (q.f && q.q) sc.push_back({gi(q.f), so(q.q)});
+    if (q.g && q.h && q.s && q.t) vc.push_back({gi(q.g), gi(q.h), so(q.s), so(q.t)});
+  }
+  if (a->heatTerms && a->heatTermsLM) sc.push_back({gi(a->heatTerms), so(a->heatTermsLM)});
+  std::vector<int> hs_sc, hs_vc;
+  for (size_t i = 0; i < sc.size(); ++i) hs_sc.push_back(cx.tmp(hs_bytes(h, n)));
+  for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_bytes(h, n)));
+  TRY(cx.prepare());
+  TRY(run_forward(h, cx, lv, sc, vc, hs_sc, hs_vc));
+  return cx.finish();
+}
+
+// ------------------------------------------------------------ graphs
+int magic_sht_graph_begin(magic_sht_handle* h) {
+  TRY(check_handle(h));
+  if (h->capturing) return set_err(MAGIC_SHT_ERR_ARG, "capture already active");
+  DeviceGuard dg(h->device);
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  h->capturing = true;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_graph_end(magic_sht_handle* h, magic_sht_graph** out) {
+  TRY(check_handle(h));
+  if (!out) return set_err(MAGIC_SHT_ERR_ARG, "null output");
+  if (!h->capturing) return set_err(MAGIC_SHT_ERR_ARG, "no capture active");
+  DeviceGuard dg(h->device);
+  h->capturing = false;
+  magic_sht_graph* gr = new magic_sht_graph();
+  cudaError_t e = cudaStreamEndCapture(h->stream, &gr->graph);
+  if (e != cudaSuccess) {
+    delete gr;
+    return set_err(MAGIC_SHT_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+  }
+  e = cudaGraphInstantiate(&gr->exec, gr->graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(gr->graph);
+    delete gr;
+    return set_err(MAGIC_SHT_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  }
+  *out = gr;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_graph_launch(magic_sht_handle* h, const magic_sht_graph* gr) {
+  TRY(check_handle(h));
+  if (!gr) return set_err(MAGIC_SHT_ERR_ARG, "null graph");
+  DeviceGuard dg(h->device);
+  CK(cudaGraphLaunch(gr->exec, h->stream));
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_graph_destroy(magic_sht_graph* gr) {
+  if (!gr) return MAGIC_SHT_OK;
+  if (gr->exec) cudaGraphExecDestroy(gr->exec);
+  if (gr->graph) cudaGraphDestroy(gr->graph);
+  delete gr;
+  return MAGIC_SHT_OK;
+}
+
+// ------------------------------------------------------------ profiling
+int magic_sht_set_profiling(magic_sht_handle* h, int on) {
+  TRY(check_handle(h));
+  h->profiling = on != 0;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_phase_times(magic_sht_handle* h, double* ms, long long* launches, int reset) {
+  TRY(check_handle(h));
+  DeviceGuard dg(h->device);
+  CK(cudaStreamSynchronize(h->stream));
+  for (auto& m : h->ev_marks) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, m.second.first, m.second.second));
+    h->phase_ms[m.first] += t;
+  }
+  h->ev_marks.clear();
+  h->ev_used = 0;
+  for (int i = 0; i < MAGIC_SHT_N_PHASES; ++i) {
+    if (ms) ms[i] = h->phase_ms[i];
+    if (launches) launches[i] = h->phase_launches[i];
+    if (reset) { h->phase_ms[i] = 0.0; h->phase_launches[i] = 0; }
+  }
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_launch_count(const magic_sht_handle* h, long long* n) {
+  TRY(check_handle(h));
+  if (!n) return set_err(MAGIC_SHT_ERR_ARG, "null output");
+  *n = h->launches;
+  return MAGIC_SHT_OK;
+}
+
+// ------------------------------------------------------------ measurement
+int magic_sht_measure_gflops(int device, int precision, double* gflops) {
+  if (!gflops) return set_err(MAGIC_SHT_ERR_ARG, "null output");
+  if (precision != MAGIC_SHT_FP64 && precision != MAGIC_SHT_FP32)
+    return set_err(MAGIC_SHT_ERR_ARG, "precision must be MAGIC_SHT_FP64 or MAGIC_SHT_FP32");
+  const bool f64 = precision == MAGIC_SHT_FP64;
+  if (device < 0) CK(cudaGetDevice(&device));
+  DeviceGuard dg(device);
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device));
+  const int blocks = prop.multiProcessorCount * 8;
+  const int iters = f64 ? 256 : 4096;
+  double* d = nullptr;
+  CK(cudaMalloc((void**)&d, sizeof(double) * (blocks + 1)));
+  cudaStream_t st;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  for (int w = 0; w < 2; ++w) CK(launch_fma_peak(d, f64, blocks, iters, st));
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    CK(cudaEventRecord(e0, st));
+    CK(launch_fma_peak(d, f64, blocks, iters, st));
+    CK(cudaEventRecord(e1, st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) best = ms;
+  }
+  const double flops = (double)blocks * 256.0 * iters * 16 * 8 * 2;
+  *gflops = flops / (best * 1e-3) / 1e9;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  cudaFree(d);
+  return MAGIC_SHT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,397 @@
+"""Host-side mirror of MagIC's ``module sht`` (src/sht_native.f90:16-20) over
+the GB300 CUDA library.
+
+Arrays follow the reference layouts:
+  * spectral: complex128, shape (lm_max,) in st_map order (m-major, l inner);
+    batched: (n_levels, lm_max) like the R-distributed ``f_Rloc(lm_max, nR)``;
+  * grid: float64, shape (n_phi_max, nlat_padded) in C order, i.e. Fortran
+    ``f(nlat_padded, n_phi_max)`` with theta fastest and the theta rows
+    scrambled north/south (row 2j north, 2j+1 south); batched:
+    (n_levels, n_phi_max, nlat_padded).
+Inputs may be numpy arrays (host memory: the call stages them through the
+GPU and returns numpy results) or CUDA torch tensors (device memory: the call
+runs asynchronously on the current torch stream and returns CUDA tensors).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+
+def prime_decomposition(nlon: int) -> int:
+    """Closest 2^i 3^j 5^k >= nlon (src/truncation.f90:162-192)."""
+    best, dist_min = nlon, 100.0
+    for i in range(13):
+        for j in range(7):
+            for k in range(7):
+                res = 2 ** i * 3 ** j * 5 ** k
+                dist = res - nlon
+                if 0 <= dist < dist_min:
+                    best, dist_min = res, dist
+    return best
+
+
+def truncation(l_max: int, nalias: int = 20, minc: int = 1) -> Dict[str, int]:
+    """Grid sizes from l_max (src/truncation.f90:50-124, the l_max /= 0 branch)."""
+    n_theta = (30 * l_max) // nalias
+    n_phi_tot = prime_decomposition(2 * n_theta)
+    n_phi_max = n_phi_tot // minc
+    n_theta = n_phi_tot // 2
+    m_max = min((l_max // minc) * minc, l_max)
+    n_m_max = m_max // minc + 1
+    lm_max = sum(l_max - m + 1 for m in range(0, m_max + 1, minc))
+    return dict(n_theta_max=n_theta, n_phi_tot=n_phi_tot, n_phi_max=n_phi_max, m_max=m_max,
+                n_m_max=n_m_max, lm_max=lm_max)
+
+
+def _torch():
+    try:
+        import torch
+        return torch
+    except Exception:  # pragma: no cover
+        return None
+
+
+def _is_torch(x) -> bool:
+    t = _torch()
+    return t is not None and isinstance(x, t.Tensor)
+
+
+class SHT:
+    """One transform instance (grid + truncation), the drop-in for ``module sht``."""
+
+    def __init__(self, l_max: int, minc: int = 1, n_theta_max: Optional[int] = None,
+                 n_phi_max: Optional[int] = None, m_max: int = 0, nlat_padded: int = 0,
+                 precision: str = "fp64", device: int = -1):
+        if n_theta_max is None or n_phi_max is None:
+            tr = truncation(l_max, minc=minc)
+            n_theta_max = n_theta_max or tr["n_theta_max"]
+            n_phi_max = n_phi_max or tr["n_phi_max"]
+        self._lib = _lib.load()
+        d = _lib.Desc(l_max, m_max, minc, n_theta_max, n_phi_max, nlat_padded,
+                      _lib.PRECISIONS[precision], device)
+        h = ctypes.c_void_p()
+        check(self._lib.magic_sht_init(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        sz = (ctypes.c_int * 8)()
+        check(self._lib.magic_sht_get_sizes(h, sz))
+        (self.l_max, self.m_max, self.minc, self.n_theta_max, self.n_phi_max,
+         self.nlat_padded, self.n_m_max, self.lm_max) = list(sz)
+        self.precision = precision
+        self.lm2l = np.array([l for m in range(0, self.m_max + 1, self.minc)
+                              for l in range(m, self.l_max + 1)], dtype=np.int64)
+        self.lm2m = np.array([m for m in range(0, self.m_max + 1, self.minc)
+                              for l in range(m, self.l_max + 1)], dtype=np.int64)
+        self._stream = None
+        self._device = None
+
+    # ---------------------------------------------------------------- life
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.magic_sht_finalize(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initialize_sht(self) -> bool:
+        """l_scrambled_theta of the reference (src/sht_native.f90:24-32)."""
+        v = ctypes.c_int()
+        check(self._lib.magic_sht_scrambled_theta(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
+    def gauss_grid(self):
+        th = np.zeros(self.n_theta_max)
+        w = np.zeros(self.n_theta_max)
+        check(self._lib.magic_sht_gauss_grid(self._h, th.ctypes.data, w.ctypes.data))
+        return th, w
+
+    def synchronize(self):
+        check(self._lib.magic_sht_synchronize(self._h))
+
+    def reserve(self, n_levels: int):
+        check(self._lib.magic_sht_reserve(self._h, int(n_levels)))
+
+    def set_stream(self, stream_ptr: Optional[int]):
+        check(self._lib.magic_sht_set_stream(self._h, stream_ptr))
+        self._stream = stream_ptr
+
+    # ------------------------------------------------------------- helpers
+    def _bind_torch_stream(self):
+        torch = _torch()
+        s = torch.cuda.current_stream().cuda_stream
+        if s != self._stream:
+            self.set_stream(s)
+
+    def _spec_in(self, x, n=None):
+        if _is_torch(x):
+            torch = _torch()
+            assert x.dtype == torch.complex128, "spectral tensors: complex128"
+            x = x.contiguous()
+            if x.is_cuda:
+                self._bind_torch_stream()
+            return x, x.data_ptr()
+        a = np.ascontiguousarray(x, dtype=np.complex128)
+        return a, a.ctypes.data
+
+    def _grid_in(self, x):
+        if _is_torch(x):
+            torch = _torch()
+            assert x.dtype == torch.float64, "grid tensors: float64"
+            x = x.contiguous()
+            if x.is_cuda:
+                self._bind_torch_stream()
+            return x, x.data_ptr()
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        return a, a.ctypes.data
+
+    def _new(self, like, shape, complex_=False):
+        if _is_torch(like):
+            torch = _torch()
+            dt = torch.complex128 if complex_ else torch.float64
+            if like.is_cuda:
+                t = torch.zeros(shape, dtype=dt, device=like.device)
+            else:
+                t = torch.zeros(shape, dtype=dt, pin_memory=True)
+            return t, t.data_ptr()
+        a = np.zeros(shape, dtype=np.complex128 if complex_ else np.float64)
+        return a, a.ctypes.data
+
+    def _grid(self, like, n=None):
+        shape = (self.n_phi_max, self.nlat_padded) if n is None else (n, self.n_phi_max, self.nlat_padded)
+        return self._new(like, shape)
+
+    def _spec(self, like, n=None):
+        shape = (self.lm_max,) if n is None else (n, self.lm_max)
+        return self._new(like, shape, complex_=True)
+
+    def _lc(self, lcut):
+        return self.l_max if lcut is None else int(lcut)
+
+    # ------------------------------------- spectral -> grid (one level)
+    def scal_to_spat(self, Slm, lcut=None):
+        S, ps = self._spec_in(Slm)
+        f, pf = self._grid(S)
+        check(self._lib.magic_sht_scal_to_spat(self._h, ps, pf, self._lc(lcut)))
+        return f
+
+    def scal_to_grad_spat(self, Slm, lcut=None):
+        S, ps = self._spec_in(Slm)
+        a, pa = self._grid(S)
+        b, pb = self._grid(S)
+        check(self._lib.magic_sht_scal_to_grad_spat(self._h, ps, pa, pb, self._lc(lcut)))
+        return a, b
+
+    def pol_to_grad_spat(self, Slm, lcut=None):
+        S, ps = self._spec_in(Slm)
+        a, pa = self._grid(S)
+        b, pb = self._grid(S)
+        check(self._lib.magic_sht_pol_to_grad_spat(self._h, ps, pa, pb, self._lc(lcut)))
+        return a, b
+
+    def torpol_to_spat(self, Wlm, dWlm, Zlm, lcut=None):
+        (W, pw), (dW, pdw), (Z, pz) = self._spec_in(Wlm), self._spec_in(dWlm), self._spec_in(Zlm)
+        a, pa = self._grid(W)
+        b, pb = self._grid(W)
+        c, pc = self._grid(W)
+        check(self._lib.magic_sht_torpol_to_spat(self._h, pw, pdw, pz, pa, pb, pc, self._lc(lcut)))
+        return a, b, c
+
+    def sphtor_to_spat(self, dWlm, Zlm, lcut=None):
+        (dW, pdw), (Z, pz) = self._spec_in(dWlm), self._spec_in(Zlm)
+        a, pa = self._grid(dW)
+        b, pb = self._grid(dW)
+        check(self._lib.magic_sht_sphtor_to_spat(self._h, pdw, pz, pa, pb, self._lc(lcut)))
+        return a, b
+
+    def torpol_to_curl_spat_IC(self, r, r_ICB, dBlm, ddBlm, Jlm, dJlm):
+        ins = [self._spec_in(x) for x in (dBlm, ddBlm, Jlm, dJlm)]
+        outs = [self._grid(ins[0][0]) for _ in range(3)]
+        check(self._lib.magic_sht_torpol_to_curl_spat_IC(self._h, float(r), float(r_ICB),
+                                                        *[p for _, p in ins], *[p for _, p in outs]))
+        return tuple(o for o, _ in outs)
+
+    def torpol_to_spat_IC(self, r, r_ICB, Wlm, dWlm, Zlm):
+        ins = [self._spec_in(x) for x in (Wlm, dWlm, Zlm)]
+        outs = [self._grid(ins[0][0]) for _ in range(3)]
+        check(self._lib.magic_sht_torpol_to_spat_IC(self._h, float(r), float(r_ICB),
+                                                   *[p for _, p in ins], *[p for _, p in outs]))
+        return tuple(o for o, _ in outs)
+
+    def torpol_to_dphspat(self, dWlm, Zlm, lcut=None):
+        (dW, pdw), (Z, pz) = self._spec_in(dWlm), self._spec_in(Zlm)
+        a, pa = self._grid(dW)
+        b, pb = self._grid(dW)
+        check(self._lib.magic_sht_torpol_to_dphspat(self._h, pdw, pz, pa, pb, self._lc(lcut)))
+        return a, b
+
+    def pol_to_curlr_spat(self, Qlm, lcut=None):
+        Q, pq = self._spec_in(Qlm)
+        f, pf = self._grid(Q)
+        check(self._lib.magic_sht_pol_to_curlr_spat(self._h, pq, pf, self._lc(lcut)))
+        return f
+
+    def torpol_to_curl_spat(self, or2, Blm, ddBlm, Jlm, dJlm, lcut=None):
+        ins = [self._spec_in(x) for x in (Blm, ddBlm, Jlm, dJlm)]
+        outs = [self._grid(ins[0][0]) for _ in range(3)]
+        check(self._lib.magic_sht_torpol_to_curl_spat(self._h, float(or2), *[p for _, p in ins],
+                                                     *[p for _, p in outs], self._lc(lcut)))
+        return tuple(o for o, _ in outs)
+
+    def axi_to_spat(self, fl_ax):
+        F, pf = self._spec_in(fl_ax)
+        out, po = self._new(F, (self.n_theta_max,))
+        check(self._lib.magic_sht_axi_to_spat(self._h, pf, po))
+        return out
+
+    def toraxi_to_spat(self, fl_ax, lcut=None):
+        F, pf = self._spec_in(fl_ax)
+        a, pa = self._new(F, (self.n_theta_max,))
+        b, pb = self._new(F, (self.n_theta_max,))
+        check(self._lib.magic_sht_toraxi_to_spat(self._h, pf, pa, pb, self._lc(lcut)))
+        return a, b
+
+    # ------------------------------------- grid -> spectral (one level)
+    def scal_to_SH(self, f, lcut=None):
+        F, pf = self._grid_in(f)
+        o, po = self._spec(F)
+        check(self._lib.magic_sht_scal_to_SH(self._h, pf, po, self._lc(lcut)))
+        return o
+
+    def spat_to_qst(self, f, g, h, lcut=None):
+        ins = [self._grid_in(x) for x in (f, g, h)]
+        outs = [self._spec(ins[0][0]) for _ in range(3)]
+        check(self._lib.magic_sht_spat_to_qst(self._h, *[p for _, p in ins], *[p for _, p in outs],
+                                             self._lc(lcut)))
+        return tuple(o for o, _ in outs)
+
+    def spat_to_sphertor(self, f, g, lcut=None):
+        ins = [self._grid_in(x) for x in (f, g)]
+        outs = [self._spec(ins[0][0]) for _ in range(2)]
+        check(self._lib.magic_sht_spat_to_sphertor(self._h, *[p for _, p in ins],
+                                                  *[p for _, p in outs], self._lc(lcut)))
+        return tuple(o for o, _ in outs)
+
+    # ------------------------------------- the radial loop's transform set
+    def _levels(self, arr, n, lcut):
+        lc = None
+        if lcut is not None:
+            if _is_torch(arr):
+                torch = _torch()
+                lc = torch.as_tensor(lcut, dtype=torch.int32, device=arr.device).contiguous()
+                return lc, lc.data_ptr()
+            lc = np.ascontiguousarray(lcut, dtype=np.int32)
+            assert lc.shape == (n,)
+            return lc, lc.ctypes.data
+        return None, None
+
+    def transform_to_grid_space(self, spec: dict, or2=None, lcut=None, out: Optional[dict] = None):
+        """rIter.f90:466-622 for many radial levels; `spec` maps the names of
+        _lib.GRID_SPACE_IN to (n_levels, lm_max) arrays; returns the grid dict."""
+        keys = [k for k in _lib.GRID_SPACE_IN if spec.get(k) is not None]
+        first = spec[keys[0]]
+        n = int(first.shape[0])
+        a = _lib.GridSpaceArgs()
+        keep = []
+        for k in keys:
+            arr, p = self._spec_in(spec[k])
+            assert tuple(arr.shape) == (n, self.lm_max), k
+            keep.append(arr)
+            setattr(a, k, p)
+        a.spec_ld = self.lm_max
+        produced = {
+            "sc": "s", "pc": "p", "xic": "xi",
+            "vrc": "w", "vtc": "w", "vpc": "w", "cvrc": "ddw", "cvtc": "ddw", "cvpc": "ddw",
+            "brc": "b", "btc": "b", "bpc": "b", "cbrc": "ddb", "cbtc": "ddb", "cbpc": "ddb",
+        }
+        outs = {} if out is None else dict(out)
+        for k in _lib.GRID_SPACE_OUT:
+            if spec.get(produced[k]) is None:
+                continue
+            if k not in outs:
+                outs[k], _ = self._grid(first, n)
+            setattr(a, k, outs[k].data_ptr() if _is_torch(outs[k]) else outs[k].ctypes.data)
+        a.grid_ld = self.n_phi_max * self.nlat_padded
+        or2_arr, por2 = (None, None)
+        if or2 is not None:
+            if _is_torch(first):
+                torch = _torch()
+                or2_arr = torch.as_tensor(or2, dtype=torch.float64, device=first.device).contiguous()
+                por2 = or2_arr.data_ptr()
+            else:
+                or2_arr = np.ascontiguousarray(or2, dtype=np.float64)
+                por2 = or2_arr.ctypes.data
+        lc_arr, plc = self._levels(first, n, lcut)
+        check(self._lib.magic_sht_transform_to_grid_space(self._h, n, por2, plc, ctypes.byref(a)))
+        return outs
+
+    def transform_to_lm_space(self, grids: dict, lcut=None, out: Optional[dict] = None):
+        """rIter.f90:624-712 for many radial levels."""
+        keys = [k for k in _lib.LM_SPACE_IN if grids.get(k) is not None]
+        first = grids[keys[0]]
+        n = int(first.shape[0])
+        a = _lib.LmSpaceArgs()
+        keep = []
+        for k in keys:
+            arr, p = self._grid_in(grids[k])
+            keep.append(arr)
+            setattr(a, k, p)
+        a.grid_ld = self.n_phi_max * self.nlat_padded
+        outs = {} if out is None else dict(out)
+        for kin, kout in zip(_lib.LM_SPACE_IN, _lib.LM_SPACE_OUT):
+            if grids.get(kin) is None:
+                continue
+            if kout not in outs:
+                outs[kout], _ = self._spec(first, n)
+            setattr(a, kout, outs[kout].data_ptr() if _is_torch(outs[kout]) else outs[kout].ctypes.data)
+        a.spec_ld = self.lm_max
+        lc_arr, plc = self._levels(first, n, lcut)
+        check(self._lib.magic_sht_transform_to_lm_space(self._h, n, plc, ctypes.byref(a)))
+        return outs
+
+    # ---------------------------------------------------------- profiling
+    def set_profiling(self, on: bool):
+        check(self._lib.magic_sht_set_profiling(self._h, 1 if on else 0))
+
+    def phase_times(self, reset: bool = True):
+        n = len(_lib.PHASES)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_longlong * n)()
+        check(self._lib.magic_sht_phase_times(self._h, ms, cnt, 1 if reset else 0))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(_lib.PHASES)}
+
+    def launch_count(self) -> int:
+        v = ctypes.c_longlong()
+        check(self._lib.magic_sht_launch_count(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    # ------------------------------------------------------------- graphs
+    def graph_begin(self):
+        check(self._lib.magic_sht_graph_begin(self._h))
+
+    def graph_end(self):
+        g = ctypes.c_void_p()
+        check(self._lib.magic_sht_graph_end(self._h, ctypes.byref(g)))
+        return g
+
+    def graph_launch(self, g):
+        check(self._lib.magic_sht_graph_launch(self._h, g))
+
+    def graph_destroy(self, g):
+        check(self._lib.magic_sht_graph_destroy(g))
+
+
+def measure_gflops(precision: str = "fp64", device: int = 0) -> float:
+    """FMA throughput of the device (GFLOP/s) for "fp64" or "fp32"."""
+    lib = _lib.load()
+    v = ctypes.c_double()
+    check(lib.magic_sht_measure_gflops(int(device), _lib.PRECISIONS[precision], ctypes.byref(v)))
+    return float(v.value)

@@ -1,0 +1,263 @@
+"""GPU parity: every public transform of the CUDA library (through the C ABI)
+against the oracle on the same seeded inputs, and against the committed
+golden vectors.  FP64 form: relative L2 and max error <= 1e-12.  FP32 form:
+<= 2e-6 relative L2."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2, rel_max
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+TOL64 = 1e-12
+
+GRIDS = [  # (l_max, minc, n_theta, n_phi_max)
+    (15, 1, 24, 48),      # generic Stockham FFT path (n = 24)
+    (31, 1, 48, 96),      # fast path S=1... (n = 48 -> generic), small
+    (64, 4, 96, 48),      # minc = 4 like the reference sample boussBenchSat
+    (63, 1, 96, 192),     # fast path S=3
+    (64, 1, 96, 192),     # C0 grid
+    (42, 2, 64, 128),     # fast path S=2 with minc=2
+    (128, 1, 192, 384),   # C1 grid, fast path S=6
+]
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__ as g
+    g.build()
+
+
+def make(L, minc, N, P, prec="fp64", nlat=0):
+    from magic_gb300 import SHT
+    return SHT(L, minc, N, P, precision=prec, nlat_padded=nlat, device=0)
+
+
+def spec(o, n, seed):
+    from magic_gb300.workload import spectra
+    return spectra(o.l_max, o.minc, n, seed, m_max=o.m_max)
+
+
+def close(a, b, tol=TOL64):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    e2, em = rel_l2(a, b), rel_max(a, b)
+    assert e2 <= tol and em <= 10 * tol, (e2, em)
+    return e2
+
+
+@pytest.mark.parametrize("grid", GRIDS)
+def test_inverse_routines_match_oracle(built, oracle_mod, torch, grid):
+    L, minc, N, P = grid
+    s = make(*grid)
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    S = spec(o, 4, seed=L + minc)
+    for lcut in (L, max(L - 5, 1)):
+        close(s.scal_to_spat(S[0], lcut), o.scal_to_spat(S[0], lcut))
+        close(s.pol_to_curlr_spat(S[1], lcut), o.pol_to_curlr_spat(S[1], lcut))
+        close(np.array(s.scal_to_grad_spat(S[0], lcut)), np.array(o.scal_to_grad_spat(S[0], lcut)))
+        close(np.array(s.pol_to_grad_spat(S[2], lcut)), np.array(o.pol_to_grad_spat(S[2], lcut)))
+        close(np.array(s.torpol_to_spat(S[0], S[1], S[2], lcut)),
+              np.array(o.torpol_to_spat(S[0], S[1], S[2], lcut)))
+        close(np.array(s.sphtor_to_spat(S[1], S[2], lcut)), np.array(o.sphtor_to_spat(S[1], S[2], lcut)))
+        close(np.array(s.torpol_to_dphspat(S[1], S[2], lcut)),
+              np.array(o.torpol_to_dphspat(S[1], S[2], lcut)))
+        close(np.array(s.torpol_to_curl_spat(0.83, S[0], S[3], S[1], S[2], lcut)),
+              np.array(o.torpol_to_curl_spat(0.83, S[0], S[3], S[1], S[2], lcut)))
+    close(np.array(s.torpol_to_spat_IC(0.3, 0.35, S[0], S[1], S[2])),
+          np.array(o.torpol_to_spat_IC(0.3, 0.35, S[0], S[1], S[2])))
+    close(np.array(s.torpol_to_curl_spat_IC(0.2, 0.35, S[0], S[1], S[2], S[3])),
+          np.array(o.torpol_to_curl_spat_IC(0.2, 0.35, S[0], S[1], S[2], S[3])))
+    close(s.axi_to_spat(S[0][: L + 1]), o.axi_to_spat(S[0][: L + 1]))
+    close(np.array(s.toraxi_to_spat(S[1][: L + 1], L - 2)), np.array(o.toraxi_to_spat(S[1][: L + 1], L - 2)))
+
+
+@pytest.mark.parametrize("grid", GRIDS)
+def test_forward_routines_match_oracle(built, oracle_mod, torch, grid):
+    L, minc, N, P = grid
+    s = make(*grid)
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    rng = np.random.default_rng(L)
+    f, g, h = (rng.standard_normal((P, N)) for _ in range(3))
+    for lcut in (L, max(L - 7, 1)):
+        close(s.scal_to_SH(f, lcut), o.scal_to_SH(f, lcut))
+        close(np.array(s.spat_to_qst(f, g, h, lcut)), np.array(o.spat_to_qst(f, g, h, lcut)))
+        close(np.array(s.spat_to_sphertor(g, h, lcut)), np.array(o.spat_to_sphertor(g, h, lcut)))
+
+
+def test_golden_vectors_on_gpu(built, torch):
+    g = np.load(os.path.join(GOLD, "oracle_small.npz"))
+    s = make(15, 1, 24, 48)
+    S = g["s15_in"]
+    close(s.scal_to_spat(S[0]), g["s15_scal"])
+    close(s.scal_to_spat(S[0], 11), g["s15_scal_lcut11"])
+    close(np.array(s.torpol_to_spat(S[0], S[1], S[2])), g["s15_qst"])
+    close(np.array(s.torpol_to_curl_spat(0.7, S[0], S[3], S[1], S[2])), g["s15_curl"])
+    close(np.array(s.sphtor_to_spat(S[1], S[2])), g["s15_sphtor"])
+    close(np.array(s.scal_to_grad_spat(S[0])), g["s15_grad"])
+    close(np.array(s.torpol_to_dphspat(S[1], S[2])), g["s15_dph"])
+    q = g["s15_qst"]
+    close(np.array(s.spat_to_qst(q[0], q[1], q[2])), g["s15_fwd_qst"])
+    close(s.scal_to_SH(q[0], 11), g["s15_fwd_sh_lcut11"])
+    cp = np.load(os.path.join(GOLD, "checkpoint_spectra.npz"))
+    L, minc, N, P = [int(x) for x in g["cp_dims"]]
+    s = make(L, minc, N, P)
+    w, z, sc = cp["wpol"][2], cp["ztor"][2], cp["entropy"][2]
+    close(s.scal_to_spat(sc), g["cp_scal"])
+    close(np.array(s.torpol_to_spat(w, w, z)), g["cp_qst"])
+    qq = g["cp_qst"]
+    close(np.array(s.spat_to_qst(qq[0], qq[1], qq[2])), g["cp_fwd_qst"])
+
+
+def _radial_set_ref(o, spec_in, or2, lcut):
+    n = spec_in["w"].shape[0]
+    out = {k: [] for k in ("sc", "pc", "xic", "vrc", "vtc", "vpc", "cvrc", "cvtc", "cvpc",
+                           "brc", "btc", "bpc", "cbrc", "cbtc", "cbpc")}
+    for r in range(n):
+        lc = int(lcut[r])
+        out["sc"].append(o.scal_to_spat(spec_in["s"][r], lc))
+        out["pc"].append(o.scal_to_spat(spec_in["p"][r], lc))
+        out["xic"].append(o.scal_to_spat(spec_in["xi"][r], lc))
+        for k, v in zip(("vrc", "vtc", "vpc"),
+                        o.torpol_to_spat(spec_in["w"][r], spec_in["dw"][r], spec_in["z"][r], lc)):
+            out[k].append(v)
+        for k, v in zip(("cvrc", "cvtc", "cvpc"),
+                        o.torpol_to_curl_spat(or2[r], spec_in["w"][r], spec_in["ddw"][r], spec_in["z"][r],
+                                              spec_in["dz"][r], lc)):
+            out[k].append(v)
+        for k, v in zip(("brc", "btc", "bpc"),
+                        o.torpol_to_spat(spec_in["b"][r], spec_in["db"][r], spec_in["aj"][r], lc)):
+            out[k].append(v)
+        for k, v in zip(("cbrc", "cbtc", "cbpc"),
+                        o.torpol_to_curl_spat(or2[r], spec_in["b"][r], spec_in["ddb"][r], spec_in["aj"][r],
+                                              spec_in["dj"][r], lc)):
+            out[k].append(v)
+    return {k: np.array(v) for k, v in out.items()}
+
+
+@pytest.mark.parametrize("grid", [(31, 1, 48, 96), (64, 4, 96, 48), (63, 1, 96, 192)])
+@pytest.mark.parametrize("device_ptrs", [False, True])
+def test_radial_loop_set_matches_oracle(built, oracle_mod, torch, grid, device_ptrs):
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    L, minc, N, P = grid
+    n = 5
+    s = make(*grid)
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    spec_in = grid_space_inputs(L, minc, n, seed=42)
+    or2 = or2_levels(n)
+    lcut = np.array([L, L - 1, L, max(L - 9, 1), L], dtype=np.int32)
+    ref = _radial_set_ref(o, spec_in, or2, lcut)
+    if device_ptrs:
+        din = {k: torch.from_numpy(v).cuda() for k, v in spec_in.items()}
+        got = s.transform_to_grid_space(din, or2=or2, lcut=lcut)
+        torch.cuda.synchronize()
+        got = {k: v.cpu().numpy() for k, v in got.items()}
+    else:
+        got = s.transform_to_grid_space(spec_in, or2=or2, lcut=lcut)
+    for k in ref:
+        close(got[k], ref[k])
+    # grid -> spectral on the same levels
+    fwd_in = {k: got[v] for k, v in FORWARD_FROM_INVERSE.items()}
+    if device_ptrs:
+        lm = s.transform_to_lm_space({k: torch.from_numpy(v).cuda() for k, v in fwd_in.items()}, lcut=lcut)
+        torch.cuda.synchronize()
+        lm = {k: v.cpu().numpy() for k, v in lm.items()}
+    else:
+        lm = s.transform_to_lm_space(fwd_in, lcut=lcut)
+    for r in range(n):
+        lc = int(lcut[r])
+        for pre in ("Adv", "VS", "VxB"):
+            q, ss, t = o.spat_to_qst(fwd_in[pre + "r"][r], fwd_in[pre + "t"][r], fwd_in[pre + "p"][r], lc)
+            close(lm[pre + "rLM"][r], q)
+            close(lm[pre + "tLM"][r], ss)
+            close(lm[pre + "pLM"][r], t)
+        close(lm["heatTermsLM"][r], o.scal_to_SH(fwd_in["heatTerms"][r], lc))
+
+
+def test_padded_grids(built, oracle_mod, torch):
+    L, minc, N, P = 31, 1, 48, 96
+    s = make(L, minc, N, P, nlat=52)
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    S = spec(o, 3, 1)
+    vr, vt, vp = s.torpol_to_spat(S[0], S[1], S[2])
+    assert vr.shape == (P, 52)
+    rr = o.torpol_to_spat(S[0], S[1], S[2])
+    close(np.array([vr[:, :N], vt[:, :N], vp[:, :N]]), np.array(rr))
+    g = np.zeros((P, 52))
+    g[:, :N] = rr[0]
+    close(s.scal_to_SH(g), o.scal_to_SH(rr[0]))
+
+
+def test_round_trip_identity_full_size(built, torch):
+    """Size-independent property at the precision-form grid (l_max=255)."""
+    from magic_gb300.workload import spectra
+    s = make(255, 1, 384, 768)
+    S = spectra(255, 1, 3, seed=77)
+    S[:, 0] = 0
+    ell = s.lm2l
+    d = [torch.from_numpy(x).cuda() for x in S]
+    q, ss, t = s.spat_to_qst(*s.torpol_to_spat(d[0], d[1], d[2]))
+    torch.cuda.synchronize()
+    assert rel_l2(q.cpu().numpy(), ell * (ell + 1) * S[0]) < 1e-12
+    assert rel_l2(ss.cpu().numpy(), S[1]) < 1e-12
+    assert rel_l2(t.cpu().numpy(), S[2]) < 1e-12
+    f = s.scal_to_spat(d[0])
+    back = s.scal_to_SH(f)
+    torch.cuda.synchronize()
+    assert rel_l2(back.cpu().numpy(), S[0]) < 1e-12
+
+
+def test_fp32_form(built, oracle_mod, torch):
+    L, minc, N, P = 63, 1, 96, 192
+    s = make(L, minc, N, P, prec="fp32")
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    S = spec(o, 3, 5)
+    for a, b in zip(s.torpol_to_spat(S[0], S[1], S[2]), o.torpol_to_spat(S[0], S[1], S[2])):
+        assert rel_l2(a, b) < 2e-6
+    g = o.torpol_to_spat(S[0], S[1], S[2])
+    for a, b in zip(s.spat_to_qst(*g), o.spat_to_qst(*g)):
+        assert rel_l2(a, b) < 2e-6
+
+
+def test_graph_replay_matches_direct(built, torch):
+    from magic_gb300.workload import grid_space_inputs, or2_levels
+    L, minc, N, P, n = 63, 1, 96, 192, 6
+    s = make(L, minc, N, P)
+    spec_in = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(L, minc, n, seed=3).items()}
+    or2 = torch.from_numpy(or2_levels(n)).cuda()
+    ref = s.transform_to_grid_space(spec_in, or2=or2)
+    torch.cuda.synchronize()
+    out = {k: torch.zeros_like(v) for k, v in ref.items()}
+    s.reserve(n)
+    s.synchronize()
+    s.graph_begin()
+    s.transform_to_grid_space(spec_in, or2=or2, out=out)
+    gr = s.graph_end()
+    s.graph_launch(gr)
+    s.synchronize()
+    for k in ref:
+        assert torch.equal(out[k], ref[k]), k
+    s.graph_destroy(gr)
+
+
+def test_error_codes(built, torch):
+    from magic_gb300._lib import ShtError
+    s = make(31, 1, 48, 96)
+    S = np.zeros(s.lm_max, complex)
+    with pytest.raises(ShtError) as e:
+        s.scal_to_spat(S, 40)
+    assert e.value.code == 3
+    with pytest.raises(ShtError) as e:
+        s.scal_to_spat(S, -1)
+    assert e.value.code == 3
