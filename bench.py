@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--cpu-levels", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--levels", type=int, default=N_LEVELS, help="radial levels (profiling cases)")
+    ap.add_argument("--only-reduced", action="store_true", help="skip the FP64 form (profiling)")
+    ap.add_argument("--clock-seconds", type=float, default=1.5,
+                    help="back-to-back steps sampled for clocks before the timed steps")
     return ap.parse_args()
 
 
@@ -221,6 +225,8 @@ def cpu_baseline(levels: int):
 
 
 def our_arm(args):
+    global N_LEVELS
+    N_LEVELS = args.levels
     import numpy as np
     import torch
     import torch.distributed as dist
@@ -278,12 +284,13 @@ def our_arm(args):
 
     # ---- FP64 form
     s64 = SHT(L_MAX, MINC, N_THETA, N_PHI, precision="fp64", device=local)
-    g64, l64 = run_set(s64, None, None)
-    for _ in range(max(0, args.warmup - 1)):
-        run_set(s64, g64, l64)
     k64 = max(1, min(args.steps, 3))
-    ms64, _ = time_steps(s64, g64, l64, k64)
-    lev64 = world * N_LEVELS * k64 / (ms64 * 1e-3)
+    if not args.only_reduced:
+        g64, l64 = run_set(s64, None, None)
+        for _ in range(max(0, args.warmup - 1)):
+            run_set(s64, g64, l64)
+        ms64, _ = time_steps(s64, g64, l64, k64)
+        lev64 = world * N_LEVELS * k64 / (ms64 * 1e-3)
 
     # ---- reduced-precision form (headline)
     sm = SHT(L_MAX, MINC, N_THETA, N_PHI, precision=form, device=local)
@@ -293,7 +300,7 @@ def our_arm(args):
     # clocks: sampled while the same steps run back to back, then the timed K steps
     clk = ClockSampler(local)
     clk.start()
-    t_end = time.time() + 1.5
+    t_end = time.time() + args.clock_seconds
     while time.time() < t_end:
         run_set(sm, gm, lmx)
         torch.cuda.synchronize()
@@ -301,6 +308,10 @@ def our_arm(args):
     clocks = clk.stop()
     value = world * N_LEVELS * args.steps / (ms * 1e-3)
 
+    if args.only_reduced:
+        print(json.dumps({"form": form, "value": value, "ms_per_step": ms / args.steps,
+                          "levels": N_LEVELS}), flush=True)
+        return
     # ---- accuracy of the reduced form against the FP64 form (same inputs)
     run_set(sm, gm, lmx)
     run_set(s64, g64, l64)

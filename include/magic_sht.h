@@ -67,7 +67,8 @@ int magic_sht_get_sizes(const magic_sht_handle* handle, int* out8);
 /* Gauss-Legendre colatitudes (north -> south) and weights, n_theta_max each
  * (gauleg, horizontal.f90:279-340). Host pointers. */
 int magic_sht_gauss_grid(magic_sht_handle* handle, double* theta_ord, double* gauss);
-/* Use an external CUDA stream (cudaStream_t passed as void*); NULL -> own stream. */
+/* Run on an external CUDA stream (cudaStream_t passed as void*); NULL selects
+ * the legacy default stream.  The handle starts on a stream of its own. */
 int magic_sht_set_stream(magic_sht_handle* handle, void* cuda_stream);
 int magic_sht_synchronize(magic_sht_handle* handle);
 /* Pre-size the device workspace for batched calls of up to n_levels levels

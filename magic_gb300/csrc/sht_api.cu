@@ -668,16 +668,14 @@ int magic_sht_gauss_grid(magic_sht_handle* h, double* theta_ord, double* gauss) 
 
 int magic_sht_set_stream(magic_sht_handle* h, void* s) {
   TRY(check_handle(h));
+  if (h->capturing) return set_err(MAGIC_SHT_ERR_ARG, "cannot change the stream during capture");
   DeviceGuard dg(h->device);
   CK(cudaStreamSynchronize(h->stream));
   if (h->own_stream) cudaStreamDestroy(h->stream);
-  if (s) {
-    h->stream = (cudaStream_t)s;
-    h->own_stream = false;
-  } else {
-    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-    h->own_stream = true;
-  }
+  // NULL selects the legacy default stream (the CUDA convention), so the
+  // library orders with every other default-stream user.
+  h->stream = (cudaStream_t)s;
+  h->own_stream = false;
   return MAGIC_SHT_OK;
 }
 
@@ -1026,6 +1024,8 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
 int magic_sht_graph_begin(magic_sht_handle* h) {
   TRY(check_handle(h));
   if (h->capturing) return set_err(MAGIC_SHT_ERR_ARG, "capture already active");
+  if (h->stream == nullptr)
+    return set_err(MAGIC_SHT_ERR_ARG, "graph capture needs a non-default stream (magic_sht_set_stream)");
   DeviceGuard dg(h->device);
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   h->capturing = true;

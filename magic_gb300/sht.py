@@ -87,7 +87,7 @@ class SHT:
                               for l in range(m, self.l_max + 1)], dtype=np.int64)
         self.lm2m = np.array([m for m in range(0, self.m_max + 1, self.minc)
                               for l in range(m, self.l_max + 1)], dtype=np.int64)
-        self._stream = None
+        self._stream = -1  # the handle's own stream until bound to torch's
         self._device = None
 
     # ---------------------------------------------------------------- life

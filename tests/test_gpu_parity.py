@@ -240,12 +240,14 @@ def test_graph_replay_matches_direct(built, torch):
     torch.cuda.synchronize()
     out = {k: torch.zeros_like(v) for k, v in ref.items()}
     s.reserve(n)
-    s.synchronize()
-    s.graph_begin()
-    s.transform_to_grid_space(spec_in, or2=or2, out=out)
-    gr = s.graph_end()
-    s.graph_launch(gr)
-    s.synchronize()
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):  # capture needs a non-default stream
+        s.graph_begin()
+        s.transform_to_grid_space(spec_in, or2=or2, out=out)
+        gr = s.graph_end()
+        s.graph_launch(gr)
+        s.synchronize()
     for k in ref:
         assert torch.equal(out[k], ref[k]), k
     s.graph_destroy(gr)
