@@ -375,6 +375,9 @@ class SHT:
 
     # ------------------------------------------------------------- graphs
     def graph_begin(self):
+        """Start capturing on the current torch stream (must not be the default stream)."""
+        if _torch() is not None and _torch().cuda.is_available():
+            self._bind_torch_stream()
         check(self._lib.magic_sht_graph_begin(self._h))
 
     def graph_end(self):
