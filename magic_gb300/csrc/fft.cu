@@ -120,31 +120,208 @@ __device__ __forceinline__ void reg_fft(T2 (&a)[S], const T2* __restrict__ tw, i
   }
 }
 
-// Complex FFT of length n = 32*S of the row held as a[q] = z[32q + lane];
-// returns a[k1] = Z[k1 + S*brev5(lane)].
+// Complex FFT of length n = 32*S held by one warp, four-step with the
+// 32-point radix-2 DIF across lanes first and the length-S DFT in registers
+// last:  input a[q] = z[S*lane + q],  output a[k2] = Z[brev5(lane) + 32*k2].
+// Outputs of one register are therefore 32 consecutive indices across the
+// warp, which keeps the shared-memory write-back free of bank conflicts.
+__device__ __forceinline__ int brev5(int x) { return __brev(x) >> 27; }
+
 template <typename T2, int S>
 __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tw, int P, int s) {
   const int lane = threadIdx.x & 31;
-  reg_fft<T2, S>(a, tw, P, s);
-#pragma unroll
-  for (int k1 = 1; k1 < S; ++k1) {
-    const int e = (2 * lane * k1) % P;  // omega_n^{lane k1}
-    if (lane) a[k1] = cmul(a[k1], twid(tw, e, s));
-  }
 #pragma unroll
   for (int d = 16; d >= 1; d >>= 1) {
     const bool up = (lane & d) != 0;
     const T2 w = twid(tw, (lane & (d - 1)) * (P / (2 * d)), s);
 #pragma unroll
-    for (int k1 = 0; k1 < S; ++k1) {
-      const T2 b = shfl_xor2(a[k1], d);
-      if (up) a[k1] = cmul(csub(b, a[k1]), w);
-      else a[k1] = cadd(a[k1], b);
+    for (int q = 0; q < S; ++q) {
+      const T2 b = shfl_xor2(a[q], d);
+      if (up) a[q] = cmul(csub(b, a[q]), w);
+      else a[q] = cadd(a[q], b);
+    }
+  }
+  const int k1 = brev5(lane);
+#pragma unroll
+  for (int q = 1; q < S; ++q) {
+    if (k1) a[q] = cmul(a[q], twid(tw, (2 * q * k1) % P, s));  // omega_n^{q k1}
+  }
+  reg_fft<T2, S>(a, tw, P, s);
+}
+
+// shared-memory position of input index k (digit swap k = S*i1 + q -> q*32 + i1)
+template <int S>
+__device__ __forceinline__ int pin(int k) { return (k % S) * 32 + k / S; }
+
+// ------------------------------------------------------------ fast path ----
+// One CTA = RT consecutive theta rows of one (level, field) column; 8 warps,
+// each owning RT/8 rows in turn.  Shared memory holds the RT rows with an
+// odd pitch KP = n+1 so that row-parallel and index-parallel accesses both
+// spread over the banks.
+template <typename T, int S, int RT>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1)) fft_inv_fast(const ShtGeom g, const FftSet s) {
+  typedef typename V2<T>::t T2;
+  constexpr int n = 32 * S, KP = n + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* sm = (T2*)smem_raw;
+  const int col = blockIdx.y;
+  const int r = col / s.nf, f = col - r * s.nf;
+  const FftField& fd = s.f[f];
+  const int row0 = blockIdx.x * RT;
+  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  const T2* __restrict__ in = (const T2*)fd.in + (long long)r * fd.in_ld;
+  const int n_m = g.n_m;
+  // two consecutive rows per thread (16 B for FP32 half spectra); n_theta is even
+  constexpr int RT2 = RT / 2;
+#pragma unroll (sizeof(T) == 4 ? 8 : 2)
+  for (int i = threadIdx.x; i < n_m * RT2; i += 256) {
+    const int k = i / RT2, rr = 2 * (i - k * RT2);
+    const int row = row0 + rr;
+    T2 v0 = zero2<T2>(), v1 = zero2<T2>();
+    if (row < g.n_theta) {
+      const T2* p = in + (long long)k * g.n_theta + row;
+      v0 = p[0];
+      v1 = p[1];
+    }
+    sm[rr * KP + pin<S>(k)] = v0;
+    sm[(rr + 1) * KP + pin<S>(k)] = v1;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int rr = warp; rr < RT; rr += 8) {
+    T2* row = sm + rr * KP;
+    T2 a[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) {
+      const int k = S * lane + q;
+      T2 ck = zero2<T2>(), cn = zero2<T2>();
+      if (k < n_m) ck = row[pin<S>(k)];
+      const int kn = n - k;
+      if (kn < n_m) cn = row[pin<S>(kn)];
+      if (k == 0) { ck.y = 0; cn.y = 0; }
+      const T2 E = cadd(ck, cconj(cn));
+      const T2 O = cmul(csub(ck, cconj(cn)), tw[k]);
+      a[q].x = E.x - O.y;
+      a[q].y = E.y + O.x;
+    }
+    __syncwarp();
+    warp_fft<T2, S>(a, tw, g.n_phi, +1);
+    const int k1 = brev5(lane);
+#pragma unroll
+    for (int k2 = 0; k2 < S; ++k2) row[k1 + 32 * k2] = a[k2];  // z_j = x_{2j} + i x_{2j+1}
+    __syncwarp();
+  }
+  __syncthreads();
+  double* out = (double*)fd.out + (long long)r * fd.out_ld;
+  const bool osin = (fd.flags & FFT_OSIN2) != 0;
+  const bool vec = (g.ld % 2) == 0;  // 16-byte stores of two rows need an even pitch
+#pragma unroll (sizeof(T) == 4 ? 8 : 2)
+  for (int i = threadIdx.x; i < g.n_phi * RT2; i += 256) {
+    const int ph = i / RT2, rr = 2 * (i - ph * RT2);
+    const int rowg = row0 + rr;
+    if (rowg >= g.n_theta) continue;
+    const T2 v0 = sm[rr * KP + (ph >> 1)];
+    const T2 v1 = sm[(rr + 1) * KP + (ph >> 1)];
+    double x0 = (ph & 1) ? (double)v0.y : (double)v0.x;
+    double x1 = (ph & 1) ? (double)v1.y : (double)v1.x;
+    if (osin) {
+      const double o = g.osin2[rowg >> 1];  // rows 2j and 2j+1 share theta_j
+      x0 *= o;
+      x1 *= o;
+    }
+    double* dst = out + (long long)ph * g.ld + rowg;
+    if (vec) {
+      *reinterpret_cast<double2*>(dst) = make_double2(x0, x1);
+    } else {
+      dst[0] = x0;
+      dst[1] = x1;
     }
   }
 }
 
-__device__ __forceinline__ int brev5(int x) { return __brev(x) >> 27; }
+template <typename T, int S, int RT>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1)) fft_fwd_fast(const ShtGeom g, const FftSet s) {
+  typedef typename V2<T>::t T2;
+  constexpr int n = 32 * S, KP = n + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* sm = (T2*)smem_raw;
+  T* smr = (T*)smem_raw;
+  const int col = blockIdx.y;
+  const int r = col / s.nf, f = col - r * s.nf;
+  const FftField& fd = s.f[f];
+  const int row0 = blockIdx.x * RT;
+  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  const double* __restrict__ in = (const double*)fd.in + (long long)r * fd.in_ld;
+  constexpr int RT2 = RT / 2;
+  const bool vec = (g.ld % 2) == 0;
+#pragma unroll (sizeof(T) == 4 ? 8 : 2)
+  for (int i = threadIdx.x; i < g.n_phi * RT2; i += 256) {
+    const int ph = i / RT2, rr = 2 * (i - ph * RT2);
+    const int row = row0 + rr;
+    double x0 = 0.0, x1 = 0.0;
+    if (row < g.n_theta) {
+      const double* src = in + (long long)ph * g.ld + row;
+      if (vec) {
+        const double2 v = *reinterpret_cast<const double2*>(src);
+        x0 = v.x;
+        x1 = v.y;
+      } else {
+        x0 = src[0];
+        x1 = src[1];
+      }
+    }
+    const int pj = pin<S>(ph >> 1);
+    smr[2 * (rr * KP + pj) + (ph & 1)] = (T)x0;
+    smr[2 * ((rr + 1) * KP + pj) + (ph & 1)] = (T)x1;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int rr = warp; rr < RT; rr += 8) {
+    T2* row = sm + rr * KP;
+    T2 a[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) a[q] = row[q * 32 + lane];  // = z[S*lane + q]
+    __syncwarp();
+    warp_fft<T2, S>(a, tw, g.n_phi, -1);
+    const int k1 = brev5(lane);
+#pragma unroll
+    for (int k2 = 0; k2 < S; ++k2) row[k1 + 32 * k2] = a[k2];
+    __syncwarp();
+  }
+  __syncthreads();
+  // X_k = (Z_k + conj Z_{n-k})/2 - i e^{-2 pi i k/P} (Z_k - conj Z_{n-k})/2, then ES/EA
+  typedef T Tt;
+  const Tt scale = (Tt)(1.0 / (double)g.n_phi);
+  constexpr int npair = RT / 2;
+  T2* out = (T2*)fd.out + (long long)r * fd.out_ld;
+  for (int i = threadIdx.x; i < g.n_m * npair; i += 256) {
+    const int k = i / npair, jp = i - k * npair;
+    const int jg = (row0 >> 1) + jp;
+    if (jg >= g.nh) continue;
+    T2 c[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const T2* row = sm + (2 * jp + h) * KP;
+      const T2 Zk = row[k];
+      const T2 Zn = cconj(row[(n - k) % n]);
+      const T2 D = csub(Zk, Zn);
+      const T2 u = cmul(cconj(tw[k]), D);
+      T2 X;
+      X.x = (Tt)0.5 * (Zk.x + Zn.x + u.y) * scale;
+      X.y = (Tt)0.5 * (Zk.y + Zn.y - u.x) * scale;
+      if (k == 0) X.y = 0;
+      c[h] = X;
+    }
+    Tt fac = 1;
+    if (fd.flags & FFT_OSIN2) fac *= (Tt)g.osin2[jg];
+    if (fd.flags & FFT_WEIGHT) fac *= (Tt)g.wgt[jg];
+    c[0] = cscale(c[0], fac);
+    c[1] = cscale(c[1], fac);
+    const long long o = ((long long)k * g.nh + jg) * 2;
+    out[o] = cadd(c[0], c[1]);
+    out[o + 1] = csub(c[0], c[1]);
+  }
+}
 
 // ---------------------------------------------------- shared staging code ----
 template <typename T2>
@@ -237,70 +414,6 @@ __device__ __forceinline__ void fwd_post(const ShtGeom& g, const FftField& fd, T
     out[o] = cadd(c[0], c[1]);
     out[o + 1] = csub(c[0], c[1]);
   }
-}
-
-// ------------------------------------------------------------ fast path ----
-template <typename T, int S, int RPW>
-__global__ void __launch_bounds__(256) fft_inv_fast(const ShtGeom g, const FftSet s) {
-  typedef typename V2<T>::t T2;
-  constexpr int RT = 8 * RPW, RP = RT + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T2* sm = (T2*)smem_raw;
-  const int n = 32 * S;
-  const int col = blockIdx.y;
-  const int r = col / s.nf, f = col - r * s.nf;
-  const FftField& fd = s.f[f];
-  const int row0 = blockIdx.x * RT;
-  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
-  stage_spectrum<T2>(g, (const T2*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm);
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T2 a[RPW][S];
-#pragma unroll
-  for (int rp = 0; rp < RPW; ++rp)
-#pragma unroll
-    for (int q = 0; q < S; ++q) a[rp][q] = inv_pre<T2>(g, sm, RP, warp * RPW + rp, 32 * q + lane, n, tw);
-  __syncthreads();
-  const int kb = S * brev5(lane);
-#pragma unroll
-  for (int rp = 0; rp < RPW; ++rp) {
-    warp_fft<T2, S>(a[rp], tw, g.n_phi, +1);
-#pragma unroll
-    for (int k1 = 0; k1 < S; ++k1) sm[(k1 + kb) * RP + warp * RPW + rp] = a[rp][k1];
-  }
-  __syncthreads();
-  store_grid<T2>(g, fd, (double*)fd.out + (long long)r * fd.out_ld, row0, RT, RP, sm);
-}
-
-template <typename T, int S, int RPW>
-__global__ void __launch_bounds__(256) fft_fwd_fast(const ShtGeom g, const FftSet s) {
-  typedef typename V2<T>::t T2;
-  constexpr int RT = 8 * RPW, RP = RT + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T2* sm = (T2*)smem_raw;
-  const int col = blockIdx.y;
-  const int r = col / s.nf, f = col - r * s.nf;
-  const FftField& fd = s.f[f];
-  const int row0 = blockIdx.x * RT;
-  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
-  stage_grid<T2>(g, (const double*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm);
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T2 a[RPW][S];
-#pragma unroll
-  for (int rp = 0; rp < RPW; ++rp)
-#pragma unroll
-    for (int q = 0; q < S; ++q) a[rp][q] = sm[(32 * q + lane) * RP + warp * RPW + rp];
-  __syncthreads();
-  const int kb = S * brev5(lane);
-#pragma unroll
-  for (int rp = 0; rp < RPW; ++rp) {
-    warp_fft<T2, S>(a[rp], tw, g.n_phi, -1);
-#pragma unroll
-    for (int k1 = 0; k1 < S; ++k1) sm[(k1 + kb) * RP + warp * RPW + rp] = a[rp][k1];
-  }
-  __syncthreads();
-  fwd_post<T2>(g, fd, (T2*)fd.out + (long long)r * fd.out_ld, row0, RT, RP, sm, tw);
 }
 
 // ------------------------------------------------------- general sizes ----
@@ -406,19 +519,20 @@ bool factorize(int n, Radices& rad) {
   return n == 1;
 }
 
-template <typename T, int S, int RPW>
+template <typename T, int S>
 cudaError_t launch_fast(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
   typedef typename V2<T>::t T2;
-  constexpr int RT = 8 * RPW, RP = RT + 1;
-  const int n = 32 * S;
-  const size_t smem = (size_t)(g.n_m > n ? g.n_m : n) * RP * sizeof(T2);
+  constexpr int n = 32 * S;
+  // 16 rows per CTA; 8 rows where 16 would leave one CTA per SM
+  constexpr int RT = (sizeof(T2) * 16 * (n + 1) > 100 * 1024) ? 8 : 16;
+  const size_t smem = (size_t)RT * (n + 1) * sizeof(T2);
   dim3 grid((g.n_theta + RT - 1) / RT, s.nf * s.nlev);
   if (inverse) {
-    auto k = fft_inv_fast<T, S, RPW>;
+    auto k = fft_inv_fast<T, S, RT>;
     CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k<<<grid, 256, smem, st>>>(g, s);
   } else {
-    auto k = fft_fwd_fast<T, S, RPW>;
+    auto k = fft_fwd_fast<T, S, RT>;
     CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k<<<grid, 256, smem, st>>>(g, s);
   }
@@ -450,18 +564,18 @@ cudaError_t launch_any(const ShtGeom& g, const FftSet& s, bool inverse, cudaStre
   const int n = g.n_phi / 2;
   if (n % 32 == 0) {
     switch (n / 32) {
-      case 1: return launch_fast<T, 1, 2>(g, s, inverse, st);
-      case 2: return launch_fast<T, 2, 2>(g, s, inverse, st);
-      case 3: return launch_fast<T, 3, 2>(g, s, inverse, st);
-      case 4: return launch_fast<T, 4, 2>(g, s, inverse, st);
-      case 5: return launch_fast<T, 5, 2>(g, s, inverse, st);
-      case 6: return launch_fast<T, 6, 2>(g, s, inverse, st);
-      case 8: return launch_fast<T, 8, 2>(g, s, inverse, st);
-      case 10: return launch_fast<T, 10, 2>(g, s, inverse, st);
-      case 12: return launch_fast<T, 12, 2>(g, s, inverse, st);
-      case 16: return launch_fast<T, 16, 1>(g, s, inverse, st);
-      case 20: return launch_fast<T, 20, 1>(g, s, inverse, st);
-      case 24: return launch_fast<T, 24, 1>(g, s, inverse, st);
+      case 1: return launch_fast<T, 1>(g, s, inverse, st);
+      case 2: return launch_fast<T, 2>(g, s, inverse, st);
+      case 3: return launch_fast<T, 3>(g, s, inverse, st);
+      case 4: return launch_fast<T, 4>(g, s, inverse, st);
+      case 5: return launch_fast<T, 5>(g, s, inverse, st);
+      case 6: return launch_fast<T, 6>(g, s, inverse, st);
+      case 8: return launch_fast<T, 8>(g, s, inverse, st);
+      case 10: return launch_fast<T, 10>(g, s, inverse, st);
+      case 12: return launch_fast<T, 12>(g, s, inverse, st);
+      case 16: return launch_fast<T, 16>(g, s, inverse, st);
+      case 20: return launch_fast<T, 20>(g, s, inverse, st);
+      case 24: return launch_fast<T, 24>(g, s, inverse, st);
       default: break;
     }
   }
