@@ -185,6 +185,11 @@ int magic_sht_launch_count(const magic_sht_handle* h, long long* n);
  * the FP64 and FP32 forms of the Legendre sums. */
 int magic_sht_measure_gflops(int device, int precision, double* gflops);
 
+/* ---- diagnostics: one tcgen05 (tensor-core) GEMM D = A B^T with M=128,
+ * N = n (32/64/128/256), K = 64*kchunks (1 or 2) on bf16-exact inputs,
+ * checked on the host; returns the max error relative to max |D|. */
+int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err);
+
 #ifdef __cplusplus
 }
 #endif

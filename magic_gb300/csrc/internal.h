@@ -24,3 +24,7 @@ cudaError_t convert_tables_fp32(const double* P, const double* dP, float* P32, f
 
 // peak.cu
 cudaError_t launch_fma_peak(void* out, bool fp64, int blocks, int iters, cudaStream_t st);
+
+// legendre_tc.cu
+cudaError_t launch_tc_selftest(int n, int kchunks, const float* A, const float* B, float* D, int* err,
+                               cudaStream_t st);

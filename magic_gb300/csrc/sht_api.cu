@@ -1103,6 +1103,53 @@ int magic_sht_launch_count(const magic_sht_handle* h, long long* n) {
   return MAGIC_SHT_OK;
 }
 
+// ------------------------------------------------------------ self-test
+int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err) {
+  if (!max_rel_err) return set_err(MAGIC_SHT_ERR_ARG, "null output");
+  if (!(n == 32 || n == 64 || n == 128 || n == 256) || kchunks < 1 || kchunks > 2)
+    return set_err(MAGIC_SHT_ERR_ARG, "n must be 32/64/128/256 and kchunks 1 or 2");
+  if (device < 0) CK(cudaGetDevice(&device));
+  DeviceGuard dg(device);
+  const int K = 64 * kchunks;
+  std::vector<float> A((size_t)128 * K), B((size_t)n * K), D((size_t)128 * n);
+  unsigned s = 12345u;
+  auto rnd = [&]() {  // small integers times powers of two: exact in bf16
+    s = s * 1664525u + 1013904223u;
+    const int v = (int)((s >> 9) % 255) - 127;
+    const int e = (int)((s >> 20) % 7) - 3;
+    return std::ldexp((float)v, e);
+  };
+  for (auto& x : A) x = rnd();
+  for (auto& x : B) x = rnd();
+  float *dA = nullptr, *dB = nullptr, *dD = nullptr;
+  int* derr = nullptr;
+  CK(cudaMalloc((void**)&dA, A.size() * 4));
+  CK(cudaMalloc((void**)&dB, B.size() * 4));
+  CK(cudaMalloc((void**)&dD, D.size() * 4));
+  CK(cudaMalloc((void**)&derr, 4));
+  CK(cudaMemcpy(dA, A.data(), A.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dB, B.data(), B.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemset(dD, 0, D.size() * 4));
+  CK(cudaMemset(derr, 0, 4));
+  CK(launch_tc_selftest(n, kchunks, dA, dB, dD, derr, 0));
+  CK(cudaDeviceSynchronize());
+  int herr = 0;
+  CK(cudaMemcpy(D.data(), dD, D.size() * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost));
+  cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(derr);
+  if (herr) return set_err(MAGIC_SHT_ERR_TIMEOUT, "tcgen05 self-test: MMA completion wait gave up");
+  double worst = 0.0, scale = 0.0;
+  for (int i = 0; i < 128; ++i)
+    for (int j = 0; j < n; ++j) {
+      double ref = 0.0;
+      for (int k = 0; k < K; ++k) ref += (double)A[(size_t)i * K + k] * (double)B[(size_t)j * K + k];
+      worst = std::fmax(worst, std::fabs(ref - (double)D[(size_t)i * n + j]));
+      scale = std::fmax(scale, std::fabs(ref));
+    }
+  *max_rel_err = worst / (scale > 0 ? scale : 1.0);
+  return MAGIC_SHT_OK;
+}
+
 // ------------------------------------------------------------ measurement
 int magic_sht_measure_gflops(int device, int precision, double* gflops) {
   if (!gflops) return set_err(MAGIC_SHT_ERR_ARG, "null output");

@@ -1,0 +1,28 @@
+"""tcgen05 tensor-core GEMM self-test through the C ABI: one M=128 MMA chain
+with bf16 operands in 128-byte-swizzled shared memory and the accumulator in
+tensor memory must reproduce A B^T exactly (bf16-exact inputs, sums well
+inside fp32)."""
+import ctypes
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import __graft_entry__ as g
+    g.build()
+    from magic_gb300 import _lib
+    return _lib.load()
+
+
+@pytest.mark.parametrize("n,kc", [(128, 1), (64, 1), (32, 1), (256, 2), (128, 2)])
+def test_tc_gemm_exact(lib, n, kc):
+    from magic_gb300._lib import check
+    v = ctypes.c_double()
+    check(lib.magic_sht_tc_selftest(0, n, kc, ctypes.byref(v)))
+    assert v.value < 1e-6, v.value
