@@ -177,6 +177,9 @@ int magic_sht_graph_destroy(magic_sht_graph* graph);
 int magic_sht_set_profiling(magic_sht_handle* h, int on);
 /* accumulated ms and launch counts per phase (arrays of MAGIC_SHT_N_PHASES) */
 int magic_sht_phase_times(magic_sht_handle* h, double* ms, long long* launches, int reset);
+/* MAGIC_SHT_ERR_TIMEOUT if a bounded device wait of an earlier kernel gave
+ * up (synchronizes the handle's stream); clear != 0 resets the flag. */
+int magic_sht_device_status(magic_sht_handle* h, int clear);
 /* total kernel launches issued by this handle */
 int magic_sht_launch_count(const magic_sht_handle* h, long long* n);
 

@@ -88,6 +88,7 @@ SIGNATURES = {
     "magic_sht_set_profiling": [_V, ctypes.c_int],
     "magic_sht_phase_times": [_V, _V, _V, ctypes.c_int],
     "magic_sht_launch_count": [_V, ctypes.POINTER(ctypes.c_longlong)],
+    "magic_sht_device_status": [_V, ctypes.c_int],
     "magic_sht_tc_selftest": [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D],
 }
 

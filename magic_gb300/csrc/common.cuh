@@ -107,6 +107,29 @@ struct ShtGeom {
   const float2* tw32;
 };
 
+// Pre-split (3xBF16) and pre-tiled Legendre tables of the tensor-core form.
+// Every block is the exact shared-memory image of one 128-row x 64-column
+// K-major operand tile with the 128-byte swizzle (16 KB).
+//   synthesis block  (m, theta tile tt, table tb, parity p, l' chunk c, split s):
+//     rows = 128 northern colatitudes, columns = 64 degrees l = m + p + 2 l'
+//   analysis block   (m, parity p, l' tile lt, table tb, theta chunk c, split s):
+//     rows = 128 degrees l = m + p + 2 l', columns = 64 northern colatitudes
+// Rows are scaled by powers of two (scale tables hold the inverse factors).
+struct TcTables {
+  const unsigned char* inv_img;
+  const long long* inv_blk0;  // [n_m] first synthesis block of each m
+  const float* inv_scale;     // [2][n_m][ntt*128]
+  const unsigned char* fwd_img;
+  const long long* fwd_blk0;  // [n_m]
+  const float* fwd_scale;     // [2][lm_max]
+  int* err;                   // device error word (bounded waits that gave up)
+  int ntt;                    // theta tiles of 128 northern points
+  int nlt;                    // l' tiles of 128 rows per parity
+  int ncj;                    // theta chunks of 64 (analysis K)
+};
+
+__host__ __device__ inline int tc_nch(int n_l) { return ((n_l + 1) / 2 + 63) / 64; }
+
 #define CUDA_TRY(x)                                                        \
   do {                                                                     \
     cudaError_t _e = (x);                                                  \

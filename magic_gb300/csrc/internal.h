@@ -1,5 +1,6 @@
 // Internal launcher declarations shared by the library's translation units.
 #pragma once
+#include <vector>
 #include "common.cuh"
 
 // legendre_simt.cu
@@ -28,3 +29,11 @@ cudaError_t launch_fma_peak(void* out, bool fp64, int blocks, int iters, cudaStr
 // legendre_tc.cu
 cudaError_t launch_tc_selftest(int n, int kchunks, const float* A, const float* B, float* D, int* err,
                                cudaStream_t st);
+void tc_table_layout(const ShtGeom& g, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
+                     std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks);
+cudaError_t build_tc_images(const ShtGeom& g, const TcTables& t, unsigned char* inv_img, float* inv_scale,
+                            unsigned char* fwd_img, float* fwd_scale, cudaStream_t st);
+cudaError_t launch_inv_legendre_tc(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
+                                   cudaStream_t st);
+cudaError_t launch_fwd_legendre_tc(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
+                                   cudaStream_t st);

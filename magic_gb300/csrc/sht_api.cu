@@ -58,6 +58,15 @@ struct magic_sht_handle {
   float *d_P32 = nullptr, *d_dP32 = nullptr;
   double2* d_tw64 = nullptr;
   float2* d_tw32 = nullptr;
+  // tensor-core form: pre-split table images
+  TcTables tct{};
+  unsigned char* d_inv_img = nullptr;
+  unsigned char* d_fwd_img = nullptr;
+  long long* d_inv_blk0 = nullptr;
+  long long* d_fwd_blk0 = nullptr;
+  float* d_inv_scale = nullptr;
+  float* d_fwd_scale = nullptr;
+  int* d_err = nullptr;
   char* ws = nullptr;
   size_t ws_bytes = 0;
   std::vector<int> lmoff;
@@ -329,7 +338,8 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = cx.dev(hs_sc[i]); f.out1 = nullptr; f.out_ld = hs_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_SCALAR);
-    CK(launch_inv_legendre_simt(g, s, false, f64, h->stream));
+    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, false, h->tct, h->stream));
+    else CK(launch_inv_legendre_simt(g, s, false, f64, h->stream));
   }
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
     InvSet s{};
@@ -341,7 +351,8 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = cx.dev(hs_vc[2 * i]); f.out1 = cx.dev(hs_vc[2 * i + 1]); f.out_ld = hs_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_VECTOR);
-    CK(launch_inv_legendre_simt(g, s, true, f64, h->stream));
+    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, true, h->tct, h->stream));
+    else CK(launch_inv_legendre_simt(g, s, true, f64, h->stream));
   }
   for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags));
   for (size_t i = 0; i < vc.size(); ++i) {
@@ -391,7 +402,8 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = (double2*)cx.dev(sc[i].out); f.out1 = nullptr; f.out_ld = lv.spec_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_SCALAR);
-    CK(launch_fwd_legendre_simt(g, s, false, f64, h->stream));
+    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_fwd_legendre_tc(g, s, false, h->tct, h->stream));
+    else CK(launch_fwd_legendre_simt(g, s, false, f64, h->stream));
   }
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
     FwdSet s{};
@@ -404,7 +416,8 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out_ld = lv.spec_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_VECTOR);
-    CK(launch_fwd_legendre_simt(g, s, true, f64, h->stream));
+    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_fwd_legendre_tc(g, s, true, h->tct, h->stream));
+    else CK(launch_fwd_legendre_simt(g, s, true, f64, h->stream));
   }
   return MAGIC_SHT_OK;
 }
@@ -550,8 +563,6 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   if (ld < N) return set_err(MAGIC_SHT_ERR_SIZE, "nlat_padded=%d < n_theta_max=%d", ld, N);
   if (d->precision != MAGIC_SHT_FP64 && d->precision != MAGIC_SHT_FP32 && d->precision != MAGIC_SHT_BF16X3)
     return set_err(MAGIC_SHT_ERR_ARG, "unknown precision %d", d->precision);
-  if (d->precision == MAGIC_SHT_BF16X3)
-    return set_err(MAGIC_SHT_ERR_UNSUPPORTED, "BF16X3 tensor-core form not built in this library");
 
   int dev = d->device;
   if (dev < 0) CK(cudaGetDevice(&dev));
@@ -599,10 +610,12 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   INIT_CK(cudaMalloc((void**)&h->d_dP, sizeof(double) * tab));
   INIT_CK(cudaMalloc((void**)&h->d_tw64, sizeof(double2) * P));
   INIT_CK(cudaMalloc((void**)&h->d_tw32, sizeof(float2) * P));
-  if (h->precision != MAGIC_SHT_FP64) {
+  if (h->precision == MAGIC_SHT_FP32) {
     INIT_CK(cudaMalloc((void**)&h->d_P32, sizeof(float) * tab));
     INIT_CK(cudaMalloc((void**)&h->d_dP32, sizeof(float) * tab));
   }
+  INIT_CK(cudaMalloc((void**)&h->d_err, sizeof(int)));
+  INIT_CK(cudaMemset(h->d_err, 0, sizeof(int)));
   INIT_CK(cudaMemcpyAsync(h->d_lmoff, h->lmoff.data(), sizeof(int) * n_m, cudaMemcpyHostToDevice, h->stream));
   {
     std::vector<double2> tw(P);
@@ -618,13 +631,36 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   }
   INIT_CK(build_tables_fp64(L, m_max, minc, N, h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP,
                             h->d_wgt, h->d_osin2, h->stream));
-  if (h->precision != MAGIC_SHT_FP64)
+  if (h->precision == MAGIC_SHT_FP32)
     INIT_CK(convert_tables_fp32(h->d_P, h->d_dP, h->d_P32, h->d_dP32, tab, h->stream));
   INIT_CK(cudaStreamSynchronize(h->stream));
-#undef INIT_CK
   g.lmoff = h->d_lmoff;
   g.P64 = h->d_P; g.dP64 = h->d_dP; g.P32 = h->d_P32; g.dP32 = h->d_dP32;
   g.wgt = h->d_wgt; g.osin2 = h->d_osin2; g.tw64 = h->d_tw64; g.tw32 = h->d_tw32;
+  if (h->precision == MAGIC_SHT_BF16X3) {
+    if (prop.major != 10)
+      return fail(set_err(MAGIC_SHT_ERR_UNSUPPORTED, "the tensor-core form needs tcgen05 (sm_10x)"));
+    TcTables& t = h->tct;
+    std::vector<long long> ib, fb;
+    long long ninv = 0, nfwd = 0;
+    tc_table_layout(g, &t.ntt, &t.nlt, &t.ncj, ib, fb, &ninv, &nfwd);
+    INIT_CK(cudaMalloc((void**)&h->d_inv_img, (size_t)ninv * 16384));
+    INIT_CK(cudaMalloc((void**)&h->d_fwd_img, (size_t)nfwd * 16384));
+    INIT_CK(cudaMalloc((void**)&h->d_inv_blk0, sizeof(long long) * n_m));
+    INIT_CK(cudaMalloc((void**)&h->d_fwd_blk0, sizeof(long long) * n_m));
+    INIT_CK(cudaMalloc((void**)&h->d_inv_scale, sizeof(float) * 2 * n_m * t.ntt * 128));
+    INIT_CK(cudaMalloc((void**)&h->d_fwd_scale, sizeof(float) * 2 * (size_t)K));
+    INIT_CK(cudaMemcpy(h->d_inv_blk0, ib.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
+    INIT_CK(cudaMemcpy(h->d_fwd_blk0, fb.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
+    INIT_CK(cudaMemset(h->d_fwd_scale, 0, sizeof(float) * 2 * (size_t)K));
+    t.inv_img = h->d_inv_img; t.fwd_img = h->d_fwd_img;
+    t.inv_blk0 = h->d_inv_blk0; t.fwd_blk0 = h->d_fwd_blk0;
+    t.inv_scale = h->d_inv_scale; t.fwd_scale = h->d_fwd_scale;
+    t.err = h->d_err;
+    INIT_CK(build_tc_images(g, t, h->d_inv_img, h->d_inv_scale, h->d_fwd_img, h->d_fwd_scale, h->stream));
+    INIT_CK(cudaStreamSynchronize(h->stream));
+  }
+#undef INIT_CK
   *out = h;
   return MAGIC_SHT_OK;
 }
@@ -634,7 +670,8 @@ int magic_sht_finalize(magic_sht_handle* h) {
   DeviceGuard dg(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ptrs[] = {h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP, h->d_wgt, h->d_osin2,
-                  h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws};
+                  h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws, h->d_inv_img, h->d_fwd_img,
+                  h->d_inv_blk0, h->d_fwd_blk0, h->d_inv_scale, h->d_fwd_scale, h->d_err};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -1093,6 +1130,17 @@ int magic_sht_phase_times(magic_sht_handle* h, double* ms, long long* launches, 
     if (launches) launches[i] = h->phase_launches[i];
     if (reset) { h->phase_ms[i] = 0.0; h->phase_launches[i] = 0; }
   }
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_device_status(magic_sht_handle* h, int clear) {
+  TRY(check_handle(h));
+  DeviceGuard dg(h->device);
+  int v = 0;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (clear) CK(cudaMemset(h->d_err, 0, sizeof(int)));
+  if (v) return set_err(MAGIC_SHT_ERR_TIMEOUT, "a bounded device wait gave up in a tensor-core kernel");
   return MAGIC_SHT_OK;
 }
 

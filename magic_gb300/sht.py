@@ -368,6 +368,10 @@ class SHT:
         check(self._lib.magic_sht_phase_times(self._h, ms, cnt, 1 if reset else 0))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(_lib.PHASES)}
 
+    def device_status(self, clear: bool = True):
+        """Raise if a bounded device wait of an earlier tensor-core kernel gave up."""
+        check(self._lib.magic_sht_device_status(self._h, 1 if clear else 0))
+
     def launch_count(self) -> int:
         v = ctypes.c_longlong()
         check(self._lib.magic_sht_launch_count(self._h, ctypes.byref(v)))

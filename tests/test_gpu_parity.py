@@ -263,3 +263,23 @@ def test_error_codes(built, torch):
     with pytest.raises(ShtError) as e:
         s.scal_to_spat(S, -1)
     assert e.value.code == 3
+
+
+@pytest.mark.parametrize("grid", [(63, 1, 96, 192), (64, 4, 96, 48), (128, 1, 192, 384)])
+def test_bf16x3_form_matches_oracle(built, oracle_mod, torch, grid):
+    """Tensor-core form (3xBF16 split products, FP32 accumulation, FP32 FFT):
+    relative L2 against the FP64 oracle within 2e-6 on well-conditioned outputs."""
+    L, minc, N, P = grid
+    s = make(L, minc, N, P, prec="bf16x3")
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    S = spec(o, 4, 17)
+    for a, b in zip(s.torpol_to_spat(S[0], S[1], S[2]), o.torpol_to_spat(S[0], S[1], S[2])):
+        assert rel_l2(a, b) < 2e-6
+    assert rel_l2(s.scal_to_spat(S[3], L - 3), o.scal_to_spat(S[3], L - 3)) < 2e-6
+    for a, b in zip(s.sphtor_to_spat(S[1], S[2]), o.sphtor_to_spat(S[1], S[2])):
+        assert rel_l2(a, b) < 2e-6
+    g = o.torpol_to_spat(S[0], S[1], S[2])
+    for a, b in zip(s.spat_to_qst(*g), o.spat_to_qst(*g)):
+        assert rel_l2(a, b) < 2e-6
+    assert rel_l2(s.scal_to_SH(g[0], L - 2), o.scal_to_SH(g[0], L - 2)) < 2e-6
+    s.device_status()
