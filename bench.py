@@ -316,6 +316,7 @@ def our_arm(args):
     run_set(sm, gm, lmx)
     run_set(s64, g64, l64)
     torch.cuda.synchronize()
+    sm.device_status()
     errs = {}
     for k in g64:
         errs[k] = float(torch.linalg.vector_norm(gm[k] - g64[k]) / torch.linalg.vector_norm(g64[k]))

@@ -502,10 +502,13 @@ __global__ void build_inv_img_kernel(const ShtGeom g, TcTables t, unsigned char*
   double mx = 0.0;
   if (valid)
     for (int l = 0; l < n_l; ++l) mx = fmax(mx, fabs(tab[(size_t)(lm0 + l) * g.nh + j]));
+  // Rows whose largest |P| is below 1e-250 contribute nothing at FP32
+  // precision; they are stored as zeros (their 2^-e factor would overflow).
   int e = 0;
-  if (mx > 0.0) frexp(mx, &e);
-  scale[((size_t)tb * g.n_m + mc) * NHP + j] = ldexpf(1.0f, e);
-  const double inv = ldexp(1.0, -e);
+  const bool live = mx > 1e-250;
+  if (live) frexp(mx, &e);
+  scale[((size_t)tb * g.n_m + mc) * NHP + j] = live ? ldexpf(1.0f, e) : 0.0f;
+  const double inv = live ? ldexp(1.0, -e) : 0.0;
   const int nch = tc_nch(n_l);
   const int tt = j / 128, row = j % 128;
   for (int p = 0; p < 2; ++p)
@@ -537,9 +540,10 @@ __global__ void build_fwd_img_kernel(const ShtGeom g, TcTables t, unsigned char*
   if (valid)
     for (int j = 0; j < g.nh; ++j) mx = fmax(mx, fabs(tab[(size_t)(lm0 + loff) * g.nh + j]));
   int e = 0;
-  if (mx > 0.0) frexp(mx, &e);
-  if (valid) scale[(size_t)tb * g.lm_max + lm0 + loff] = ldexpf(1.0f, e);
-  const double inv = ldexp(1.0, -e);
+  const bool live = mx > 1e-250;
+  if (live) frexp(mx, &e);
+  if (valid) scale[(size_t)tb * g.lm_max + lm0 + loff] = live ? ldexpf(1.0f, e) : 0.0f;
+  const double inv = live ? ldexp(1.0, -e) : 0.0;
   const int lt = lpad / 128, row = lpad % 128;
   for (int j = 0; j < t.ncj * 64; ++j) {
     const double v = (valid && j < g.nh) ? tab[(size_t)(lm0 + loff) * g.nh + j] * inv : 0.0;

@@ -283,3 +283,30 @@ def test_bf16x3_form_matches_oracle(built, oracle_mod, torch, grid):
         assert rel_l2(a, b) < 2e-6
     assert rel_l2(s.scal_to_SH(g[0], L - 2), o.scal_to_SH(g[0], L - 2)) < 2e-6
     s.device_status()
+
+
+def test_bf16x3_full_size_levels(built, torch):
+    """Precision-form grid (l_max=255, 384 x 768): the tensor-core form against
+    the FP64 form on 3 radial levels of the full transform set; every output
+    finite and within 2e-6 relative L2 except the ill-conditioned spheroidal
+    part of the vorticity-derived pair."""
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    n = 3
+    s64 = make(255, 1, 384, 768)
+    sbf = make(255, 1, 384, 768, prec="bf16x3")
+    spec_in = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(255, 1, n, seed=5).items()}
+    or2 = torch.from_numpy(or2_levels(n)).cuda()
+    g64 = s64.transform_to_grid_space(spec_in, or2=or2)
+    gbf = sbf.transform_to_grid_space(spec_in, or2=or2)
+    l64 = s64.transform_to_lm_space({k: g64[v] for k, v in FORWARD_FROM_INVERSE.items()})
+    lbf = sbf.transform_to_lm_space({k: g64[v] for k, v in FORWARD_FROM_INVERSE.items()})
+    torch.cuda.synchronize()
+    sbf.device_status()
+    for k in g64:
+        assert torch.isfinite(gbf[k]).all(), k
+        e = float(torch.linalg.vector_norm(gbf[k] - g64[k]) / torch.linalg.vector_norm(g64[k]))
+        assert e < 2e-6, (k, e)
+    for k in l64:
+        assert torch.isfinite(lbf[k]).all(), k
+        e = float(torch.linalg.vector_norm(lbf[k] - l64[k]) / torch.linalg.vector_norm(l64[k]))
+        assert e < (1e-3 if k == "VStLM" else 2e-6), (k, e)
