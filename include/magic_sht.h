@@ -107,6 +107,28 @@ int magic_sht_axi_to_spat(magic_sht_handle* h, const double* fl_ax,
 int magic_sht_toraxi_to_spat(magic_sht_handle* h, const double* fl_ax, double* ft, double* fp,
                              int lcut);                                 /* :393-405 */
 
+/* Allocation-free variant of magic_sht_scal_to_spat.  It has no counterpart
+ * in the reference.  It is meant for callers that must not allocate device
+ * memory while they run: applications whose free GPU memory is owned by a
+ * pool allocator (a raw cudaMalloc there fails or fragments the pool), and
+ * time-critical loops where cudaMalloc/cudaFree would stall on their
+ * implicit device synchronization.  The ordinary entry points may grow the
+ * handle's workspace with cudaMalloc; this one calls no allocating routine:
+ * its only scratch (the (theta, m) half spectrum) is a static 4 MiB device
+ * array that every GPU loading the library holds until the process exits.
+ *   - Slm and fieldc must be device pointers (MAGIC_SHT_ERR_ARG otherwise);
+ *     the call is asynchronous on the handle's stream.
+ *   - Limit: n_m_max * n_theta_max * 16 bytes (FP64 form; 8 bytes for the
+ *     other forms) must not exceed 4 MiB, else MAGIC_SHT_ERR_SIZE; e.g.
+ *     l_max=255 with 384 Gauss points uses 1.5 MiB.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - Every call shares the one array, which keeps the last call's contents
+ *     (each call overwrites all of it before reading it); calls that overlap
+ *     on the GPU (other streams, other handles on the same device) race. */
+int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double* Slm, double* fieldc, int lcut);
+
 /* ---- grid -> spectral, one radial level ---- */
 int magic_sht_scal_to_SH(magic_sht_handle* h, const double* f, double* fLM,
                          int lcut);                                     /* :338-346 */

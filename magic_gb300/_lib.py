@@ -61,6 +61,7 @@ SIGNATURES = {
     "magic_sht_synchronize": [_V],
     "magic_sht_reserve": [_V, ctypes.c_int],
     "magic_sht_scal_to_spat": [_V, _V, _V, ctypes.c_int],
+    "magic_sht_scal_to_spat_noalloc": [_V, _V, _V, ctypes.c_int],
     "magic_sht_scal_to_grad_spat": [_V, _V, _V, _V, ctypes.c_int],
     "magic_sht_pol_to_grad_spat": [_V, _V, _V, _V, ctypes.c_int],
     "magic_sht_torpol_to_spat": [_V, _V, _V, _V, _V, _V, _V, ctypes.c_int],

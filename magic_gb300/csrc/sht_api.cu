@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1238,3 +1239,78 @@ int magic_sht_measure_gflops(int device, int precision, double* gflops) {
 }
 
 }  // extern "C"
+
+// ============================================== allocation-free scal_to_spat
+// A variant of magic_sht_scal_to_spat for callers that must not allocate
+// device memory while they run: the (theta, m) half spectrum between the
+// Legendre sums and the inverse FFT lives in this file-scope array instead
+// of the handle's workspace.  Every GPU that loads the library holds the
+// array until the process exits.
+#define MAGIC_SHT_NOALLOC_SCRATCH_BYTES (4u << 20)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MAGIC_SHT_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on `dev` (which must be current).  In
+// host code the symbol names a host-side stand-in, so the address is looked
+// up once per device and cached.
+int noalloc_scratch(int dev, void** out) {
+  if (dev < 0 || dev >= kMaxDevices) return set_err(MAGIC_SHT_ERR_ARG, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return set_err(MAGIC_SHT_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed: %s",
+                     cudaGetErrorString(e));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return MAGIC_SHT_OK;
+}
+}  // namespace
+
+extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double* Slm, double* fieldc,
+                                              int lcut) {
+  TRY(check_handle(h));
+  TRY(check_lcut(h, lcut));
+  if (!Slm || !fieldc) return set_err(MAGIC_SHT_ERR_ARG, "null pointer");
+  DeviceGuard dg(h->device);
+  if (!is_device_ptr(Slm) || !is_device_ptr(fieldc))
+    return set_err(MAGIC_SHT_ERR_ARG,
+                   "scal_to_spat_noalloc takes device pointers only (host arrays would need staging buffers)");
+  const ShtGeom& g = h->g;
+  const size_t need = (size_t)g.n_m * g.n_theta * t2_bytes(h);
+  if (need > MAGIC_SHT_NOALLOC_SCRATCH_BYTES)
+    return set_err(MAGIC_SHT_ERR_SIZE,
+                   "half spectrum of %zu bytes (n_m_max=%d x n_theta_max=%d) exceeds the %u-byte static "
+                   "scratch of scal_to_spat_noalloc",
+                   need, g.n_m, g.n_theta, MAGIC_SHT_NOALLOC_SCRATCH_BYTES);
+  void* scratch = nullptr;
+  TRY(noalloc_scratch(h->device, &scratch));
+  const long long hs_ld = (long long)g.n_m * g.n_theta;
+  InvSet s{};
+  s.nf = 1;
+  s.nlev = 1;
+  s.lcut0 = lcut;
+  s.f[0].x0 = SpecOperand{(const double2*)Slm, nullptr, (long long)g.lm_max, OP_COPY, 0};
+  s.f[0].x1 = SpecOperand{nullptr, nullptr, 0, OP_ZERO, 0};
+  s.f[0].out0 = scratch;
+  s.f[0].out1 = nullptr;
+  s.f[0].out_ld = hs_ld;
+  if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, false, h->tct, h->stream));
+  else CK(launch_inv_legendre_simt(g, s, false, fp64_pipes(h), h->stream));
+  FftSet fs{};
+  fs.nf = 1;
+  fs.nlev = 1;
+  fs.f[0].in = scratch;
+  fs.f[0].out = fieldc;
+  fs.f[0].in_ld = hs_ld;
+  fs.f[0].out_ld = (long long)g.n_phi * g.ld;
+  fs.f[0].flags = 0;
+  CK(launch_fft_inverse(g, fs, fp64_pipes(h), h->stream));
+  return MAGIC_SHT_OK;
+}
