@@ -72,6 +72,11 @@ enum FftFlags : int {
   FFT_OSIN2 = 1,    // inverse: multiply grid rows by 1/sin^2 theta (dphspat)
                     // forward: multiply spectrum rows by 1/sin^2 theta (sphtor)
   FFT_WEIGHT = 2,   // forward: multiply by 2 pi w_j (Gauss weight) for the Legendre sums
+  // inverse input in the parity-separated layout of the tensor-core synthesis:
+  // per m, parity p = 0,1: E_p[nh] (and F_p[nh] with FFT_IN_EF); rows are
+  // N = E_0 + E_1, S = F_0 - F_1 (F = E with FFT_IN_E)
+  FFT_IN_E = 4,
+  FFT_IN_EF = 8,
 };
 
 struct FftField {

@@ -38,3 +38,31 @@ template <typename T2> __device__ __forceinline__ double2 to_d2(T2 a) { return m
 template <typename T2> __device__ __forceinline__ T2 shfl_xor2(T2 v, int d) {
   T2 r; r.x = __shfl_xor_sync(0xffffffffu, v.x, d); r.y = __shfl_xor_sync(0xffffffffu, v.y, d); return r;
 }
+
+// FP64 <-> FP32 conversions with integer instructions only (the FP64 pipe of
+// GB300 is narrow; these conversions run on the integer/FP32 pipes).
+// d2f: round to nearest even, magnitudes below 2^-126 flush to zero, no
+// overflow handling (transform data stays far inside the FP32 range).
+__device__ __forceinline__ float d2f_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int hi = (unsigned int)(b >> 32), lo = (unsigned int)b;
+  const int e = (int)((hi >> 20) & 0x7FF);
+  const unsigned int sign = hi & 0x80000000u;
+  if (e < 1023 - 126) return __uint_as_float(sign);
+  const unsigned int mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  unsigned int f = sign | ((unsigned int)(e - 1023 + 127) << 23) | mant;
+  const unsigned int rbit = (lo >> 28) & 1u;
+  const unsigned int sticky = (lo & 0x0FFFFFFFu) != 0u;
+  if (rbit && (sticky || (mant & 1u))) f += 1u;
+  return __uint_as_float(f);
+}
+// exact widening (normal numbers and zero; FP32 subnormals flush to zero)
+__device__ __forceinline__ double f2d_int(float x) {
+  const unsigned int u = __float_as_uint(x);
+  const unsigned int e = (u >> 23) & 0xFFu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)sign);
+  const unsigned long long bits = sign | ((unsigned long long)(e - 127 + 1023) << 52) |
+                                  ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}

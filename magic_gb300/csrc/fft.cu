@@ -171,6 +171,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
   const T2* __restrict__ in = (const T2*)fd.in + (long long)r * fd.in_ld;
   const int n_m = g.n_m;
+  const bool in_parity = (fd.flags & (FFT_IN_E | FFT_IN_EF)) != 0;
+  const bool has_f = (fd.flags & FFT_IN_EF) != 0;
+  const long long per_p = has_f ? 2LL * g.nh : (long long)g.nh;
   // two consecutive rows per thread (16 B for FP32 half spectra); n_theta is even
   constexpr int RT2 = RT / 2;
 #pragma unroll (sizeof(T) == 4 ? 8 : 2)
@@ -179,9 +182,19 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
     const int row = row0 + rr;
     T2 v0 = zero2<T2>(), v1 = zero2<T2>();
     if (row < g.n_theta) {
-      const T2* p = in + (long long)k * g.n_theta + row;
-      v0 = p[0];
-      v1 = p[1];
+      if (in_parity) {
+        const int jg = row >> 1;
+        const T2* b0 = in + (long long)k * 2 * per_p;
+        const T2* b1 = b0 + per_p;
+        const T2 e0 = b0[jg], e1 = b1[jg];
+        const T2 f0 = has_f ? b0[g.nh + jg] : e0, f1 = has_f ? b1[g.nh + jg] : e1;
+        v0 = cadd(e0, e1);
+        v1 = csub(f0, f1);
+      } else {
+        const T2* p = in + (long long)k * g.n_theta + row;
+        v0 = p[0];
+        v1 = p[1];
+      }
     }
     sm[rr * KP + pin<S>(k)] = v0;
     sm[(rr + 1) * KP + pin<S>(k)] = v1;
@@ -326,12 +339,25 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
 // ---------------------------------------------------- shared staging code ----
 template <typename T2>
 __device__ __forceinline__ void stage_spectrum(const ShtGeom& g, const T2* __restrict__ in,
-                                               int row0, int RT, int RP, T2* sm) {
+                                               int row0, int RT, int RP, T2* sm, int flags) {
+  const bool in_parity = (flags & (FFT_IN_E | FFT_IN_EF)) != 0;
+  const bool has_f = (flags & FFT_IN_EF) != 0;
+  const long long per_p = has_f ? 2LL * g.nh : (long long)g.nh;
   for (int i = threadIdx.x; i < g.n_m * RT; i += blockDim.x) {
     const int k = i / RT, rr = i - k * RT;
     const int row = row0 + rr;
     T2 v = zero2<T2>();
-    if (row < g.n_theta) v = in[(long long)k * g.n_theta + row];
+    if (row < g.n_theta) {
+      if (in_parity) {
+        const int jg = row >> 1;
+        const T2* b0 = in + (long long)k * 2 * per_p;
+        const T2* b1 = b0 + per_p;
+        if ((row & 1) == 0) v = cadd(b0[jg], b1[jg]);
+        else v = has_f ? csub(b0[g.nh + jg], b1[g.nh + jg]) : csub(b0[jg], b1[jg]);
+      } else {
+        v = in[(long long)k * g.n_theta + row];
+      }
+    }
     sm[k * RP + rr] = v;
   }
 }
@@ -472,7 +498,7 @@ __global__ void __launch_bounds__(256) fft_inv_gen(const ShtGeom g, const FftSet
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
   const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
-  stage_spectrum<T2>(g, (const T2*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm);
+  stage_spectrum<T2>(g, (const T2*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm, fd.flags);
   __syncthreads();
   for (int k = lane; k < n; k += 32) wa[k] = inv_pre<T2>(g, sm, RP, warp, k, n, tw);
   __syncwarp();

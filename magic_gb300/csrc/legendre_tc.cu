@@ -9,6 +9,7 @@
 #include "common.cuh"
 #include "internal.h"
 #include "tc_ptx.cuh"
+#include "cplx.cuh"
 
 namespace {
 
@@ -113,67 +114,90 @@ cudaError_t launch_tc_selftest(int n, int kchunks, const float* A, const float* 
 namespace {
 
 constexpr int TC_THREADS = 128;
-constexpr uint32_t TC_IDESC = tc::idesc_bf16(128, 128);
-__constant__ int kSplitPairs[6][2] = {{0, 0}, {0, 1}, {1, 0}, {0, 2}, {1, 1}, {2, 0}};
 
 __device__ __forceinline__ unsigned char* align1024(unsigned char* p) {
   return (unsigned char*)(((uintptr_t)p + 1023) & ~(uintptr_t)1023);
 }
 
-__device__ __forceinline__ double2 tc_load_operand(const SpecOperand& o, int r, int lm, int l, int m,
-                                                   double or2) {
-  if (o.op == OP_ZERO || o.A == nullptr) return make_double2(0.0, 0.0);
-  const long long base = (long long)r * o.ld + lm;
-  const double2 a = o.A[base];
-  switch (o.op) {
-    case OP_COPY: return a;
-    case OP_DLH: { const double d = (double)(l * (l + 1)); return make_double2(d * a.x, d * a.y); }
-    case OP_CURLT: {
-      const double2 b = o.B[base];
-      const double d = or2 * (double)(l * (l + 1));
-      return make_double2(d * a.x - b.x, d * a.y - b.y);
-    }
-    case OP_IM: { const double dm = (double)m; return make_double2(-dm * a.y, dm * a.x); }
-    default: return make_double2(0.0, 0.0);
-  }
-}
-
 // 8 values -> three 16-byte chunks (hi, mid, lo) at the swizzled position
-__device__ __forceinline__ void store_split8(unsigned char* tile0, uint32_t off, const float (&v)[8]) {
+__device__ __forceinline__ void store_split8(unsigned char* tile0, uint32_t off, const float (&v)[8],
+                                             uint32_t tile_bytes) {
   __nv_bfloat16 h[8], md[8], lo[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) tc::split3(v[i], h[i], md[i], lo[i]);
   *(uint4*)(tile0 + off) = *(const uint4*)h;
-  *(uint4*)(tile0 + 16384 + off) = *(const uint4*)md;
-  *(uint4*)(tile0 + 2 * 16384 + off) = *(const uint4*)lo;
+  *(uint4*)(tile0 + tile_bytes + off) = *(const uint4*)md;
+  *(uint4*)(tile0 + 2 * tile_bytes + off) = *(const uint4*)lo;
 }
 
 __device__ __forceinline__ void tc_record_error(int* err) {
   if (err) atomicExch(err, 1);
 }
 
+// Synthesis, one (m, parity, theta tile, column tile) per CTA.  The CTA
+// writes, for each output field, E_p = U + W and F_p = U - W where U holds the
+// P-terms and W the dP-terms of its parity (scalar fields: E_p only); the
+// inverse FFT forms the north/south rows N = E_0 + E_1, S = F_0 - F_1
+// (P is even and sin(theta) dP/dtheta odd under theta -> pi - theta for
+// even l-m).  Accumulators: hi*hi and the five cross products apart, so the
+// large partial sums take one rounding per k-step.
 template <bool VEC>
-__global__ void __launch_bounds__(TC_THREADS, 1) inv_leg_tc(const ShtGeom g, const InvSet s, const TcTables t) {
+__global__ void __launch_bounds__(TC_THREADS, 2) inv_leg_tc(const ShtGeom g, const InvSet s, const TcTables t) {
   constexpr int NT = VEC ? 2 : 1;
-  constexpr uint32_t TMEM_COLS = VEC ? 512 : 256;
+  constexpr int NC = 64;                       // real columns per CTA
+  constexpr int BT = NC * 128;                 // bytes of one B split tile
+  constexpr uint32_t TMEM_COLS = NT * 2 * NC;  // (table) x (hi, cross)
+  constexpr uint32_t IDESC = tc::idesc_bf16(128, NC);
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t barA, barM;
+  __shared__ uint64_t barA0, barA1, barF0, barM;
   __shared__ uint32_t tmem_base;
   unsigned char* base = align1024(smem_raw);
-  unsigned char* sA = base;                        // [NT][3] x 16 KB
-  unsigned char* sB = sA + NT * 3 * 16384;         // [3] x 16 KB
+  unsigned char* sA0 = base;                   // slot 0: NT x 16 KB
+  unsigned char* sA1 = sA0 + NT * 16384;       // slot 1
+  unsigned char* sB = sA1 + NT * 16384;        // 3 x BT
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int tt = blockIdx.x, ct = blockIdx.y, mc = blockIdx.z;
+  const int tt = blockIdx.x, ct = blockIdx.y;
+  const int mc = blockIdx.z >> 1, p = blockIdx.z & 1;
   const int m = mc * g.minc;
   const int n_l = g.l_max - m + 1;
   const int lm0 = g.lmoff[mc];
   const int nch = tc_nch(n_l);
-  const int npair = s.nf * s.nlev;                 // columns groups (level, field)
-  const int ncplx = npair * (VEC ? 2 : 1);         // complex source columns
-  if (ct * 64 >= ncplx) return;
+  const int nlp = (n_l + 1 - p) / 2;
+  const int nchp = (nlp + 63) / 64;
+  const int npair = s.nf * s.nlev;
+  const int ncplx = npair * (VEC ? 2 : 1);
+  if (ct * (NC / 2) >= ncplx) return;
+  const int jl = 32 * warp + lane;
+  const int jg = tt * 128 + jl;
+  // output element (field f, level r, parity p, E/F) of this thread's colatitude
+  auto out_ptr = [&](void* base_ptr, int r, int f, int ef) -> float2* {
+    const long long per_p = VEC ? 2LL * g.nh : (long long)g.nh;
+    return (float2*)base_ptr + (long long)r * s.f[f].out_ld + ((long long)mc * 2 + p) * per_p +
+           (long long)ef * g.nh + jg;
+  };
+  if (nlp == 0) {  // m = l_max, odd parity: nothing to sum, contribute zeros
+    if (jg < g.nh)
+      for (int q = 0; q < NC / 2; ++q) {
+        const int cq = ct * (NC / 2) + q;
+        if (cq >= ncplx) break;
+        if (!VEC) {
+          const int r = cq / s.nf, f = cq - r * s.nf;
+          *out_ptr(s.f[f].out0, r, f, 0) = make_float2(0.f, 0.f);
+        } else if ((cq & 1) == 0) {
+          const int pair = cq >> 1, r = pair / s.nf, f = pair - r * s.nf;
+          for (int ef = 0; ef < 2; ++ef) {
+            *out_ptr(s.f[f].out0, r, f, ef) = make_float2(0.f, 0.f);
+            *out_ptr(s.f[f].out1, r, f, ef) = make_float2(0.f, 0.f);
+          }
+        }
+      }
+    return;
+  }
 
   if (tid == 0) {
-    tc::mbar_init(&barA, 1);
+    tc::mbar_init(&barA0, 1);
+    tc::mbar_init(&barA1, 1);
+    tc::mbar_init(&barF0, 1);
     tc::mbar_init(&barM, 1);
     tc::fence_mbar_init();
   }
@@ -185,138 +209,161 @@ __global__ void __launch_bounds__(TC_THREADS, 1) inv_leg_tc(const ShtGeom g, con
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_base;
-
+  uint32_t ph_a0 = 0, ph_a1 = 0, ph_f0 = 0;
   bool ok = true;
-  int stage = 0;
-  for (int p = 0; p < 2; ++p) {
-    const int nlp = (n_l + 1 - p) / 2;
-    const int nchp = (nlp + 63) / 64;
-    for (int c = 0; c < nchp; ++c, ++stage) {
-      if (stage > 0 && !tc::mbar_wait(&barM, (stage - 1) & 1)) ok = false;
-      if (!__syncthreads_and(ok)) { ok = false; break; }
-      if (tid == 0) {
-        tc::mbar_expect_tx(&barA, NT * 3 * 16384);
-        for (int tb = 0; tb < NT; ++tb)
-          for (int sp = 0; sp < 3; ++sp) {
-            const long long blk = t.inv_blk0[mc] + ((((long long)tt * 2 + tb) * 2 + p) * nch + c) * 3 + sp;
-            tc::bulk_g2s(sA + (tb * 3 + sp) * 16384, t.inv_img + blk * 16384, 16384, &barA);
-          }
-      }
-      // data operand: 64 complex columns x 64 degrees of parity p
-      for (int u = tid; u < 64 * 8; u += TC_THREADS) {
-        const int ql = u >> 3, kg = u & 7;
-        const int q = ct * 64 + ql;
-        float re[8], im[8];
-        if (q < ncplx) {
-          const int pair = VEC ? (q >> 1) : q;
-          const int r = pair / s.nf, f = pair - r * s.nf;
-          const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
-          const double o2 = s.or2 ? s.or2[r] : s.or2_0;
-          const SpecOperand& op = (VEC && (q & 1)) ? s.f[f].x1 : s.f[f].x0;
+  auto issue_split = [&](int c, int sp, unsigned char* slot, uint64_t* bar) {
+    tc::mbar_expect_tx(bar, NT * 16384);
+    for (int tb = 0; tb < NT; ++tb) {
+      const long long blk = t.inv_blk0[mc] + ((((long long)tt * 2 + tb) * 2 + p) * nch + c) * 3 + sp;
+      tc::bulk_g2s(slot + tb * 16384, t.inv_img + blk * 16384, 16384, bar);
+    }
+  };
+  for (int c = 0; c < nchp; ++c) {
+    if (c > 0 && !tc::mbar_wait(&barM, (c - 1) & 1)) ok = false;
+    if (!__syncthreads_and(ok)) { ok = false; break; }
+    if (tid == 0) {
+      issue_split(c, 0, sA0, &barA0);
+      issue_split(c, 1, sA1, &barA1);
+    }
+    // data operand: 32 complex columns x 64 degrees of parity p
+    for (int u = tid; u < (NC / 2) * 8; u += TC_THREADS) {
+      const int ql = u >> 3, kg = u & 7;
+      const int q = ct * (NC / 2) + ql;
+      float re[8], im[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) { re[i] = 0.f; im[i] = 0.f; }
+      if (q < ncplx) {
+        const int pair = VEC ? (q >> 1) : q;
+        const int r = pair / s.nf, f = pair - r * s.nf;
+        const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+        const SpecOperand& op = (VEC && (q & 1)) ? s.f[f].x1 : s.f[f].x0;
+        if (op.op != OP_ZERO && op.A != nullptr) {
+          const float o2 = (op.op == OP_CURLT) ? d2f_int(s.or2 ? s.or2[r] : s.or2_0) : 0.f;
+          const double2* A = op.A + (long long)r * op.ld;
+          const double2* B = op.B ? op.B + (long long)r * op.ld : nullptr;
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const int lp = 64 * c + 8 * kg + i;
-            const int l = m + p + 2 * lp;
-            double2 x = make_double2(0.0, 0.0);
-            if (l <= lc) x = tc_load_operand(op, r, lm0 + l - m, l, m, o2);
-            re[i] = (float)x.x;
-            im[i] = (float)x.y;
-          }
-        } else {
-#pragma unroll
-          for (int i = 0; i < 8; ++i) { re[i] = 0.f; im[i] = 0.f; }
-        }
-        store_split8(sB, tc::sw128_offset(2 * ql, 8 * kg), re);
-        store_split8(sB, tc::sw128_offset(2 * ql + 1, 8 * kg), im);
-      }
-      tc::fence_proxy_async_smem();
-      tc::tc_fence_before();
-      __syncthreads();
-      if (tid == 0) {
-        if (!tc::mbar_wait(&barA, stage & 1)) {
-          ok = false;
-        } else {
-          tc::tc_fence_after();
-          for (int ks = 0; ks < 4; ++ks)
-            for (int tb = 0; tb < NT; ++tb) {
-              const uint32_t d = tmem + (uint32_t)((tb * 2 + p) * 128);
-              for (int pr = 0; pr < 6; ++pr) {
-                const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA + (tb * 3 + kSplitPairs[pr][0]) * 16384) + ks * 32);
-                const uint64_t bd = tc::sw128_desc(tc::smem_u32(sB + kSplitPairs[pr][1] * 16384) + ks * 32);
-                tc::mma_bf16(d, ad, bd, TC_IDESC, (c | ks | pr) ? 1u : 0u);
+            const int l = m + p + 2 * (64 * c + 8 * kg + i);
+            if (l <= lc) {
+              const double2 a = A[lm0 + l - m];
+              float ar = d2f_int(a.x), ai = d2f_int(a.y);
+              switch (op.op) {
+                case OP_DLH: { const float d = (float)(l * (l + 1)); ar *= d; ai *= d; break; }
+                case OP_CURLT: {
+                  const double2 b = B[lm0 + l - m];
+                  const float d = o2 * (float)(l * (l + 1));
+                  ar = fmaf(d, ar, -d2f_int(b.x));
+                  ai = fmaf(d, ai, -d2f_int(b.y));
+                  break;
+                }
+                case OP_IM: { const float dm = (float)m, t0 = ar; ar = -dm * ai; ai = dm * t0; break; }
+                default: break;
               }
+              re[i] = ar;
+              im[i] = ai;
             }
+          }
         }
-        tc::mma_commit(&barM);  // arrives also when nothing was issued
       }
+      store_split8(sB, tc::sw128_offset(2 * ql, 8 * kg), re, BT);
+      store_split8(sB, tc::sw128_offset(2 * ql + 1, 8 * kg), im, BT);
     }
-    if (!ok) break;
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      bool good = tc::mbar_wait(&barA0, ph_a0);
+      ph_a0 ^= 1;
+      tc::tc_fence_after();
+      if (good) {
+        for (int ks = 0; ks < 4; ++ks)
+          for (int tb = 0; tb < NT; ++tb) {
+            const uint32_t hi = tmem + (uint32_t)((tb * 2 + 0) * NC), cr = tmem + (uint32_t)((tb * 2 + 1) * NC);
+            const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA0 + tb * 16384) + ks * 32);
+            const uint32_t first = (c | ks) ? 1u : 0u;
+            tc::mma_bf16(hi, ad, tc::sw128_desc(tc::smem_u32(sB) + ks * 32), IDESC, first);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(sB + BT) + ks * 32), IDESC, first);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(sB + 2 * BT) + ks * 32), IDESC, 1u);
+          }
+      }
+      tc::mma_commit(&barF0);
+      good = good && tc::mbar_wait(&barA1, ph_a1);
+      ph_a1 ^= 1;
+      tc::tc_fence_after();
+      if (good) {
+        for (int ks = 0; ks < 4; ++ks)
+          for (int tb = 0; tb < NT; ++tb) {
+            const uint32_t cr = tmem + (uint32_t)((tb * 2 + 1) * NC);
+            const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA1 + tb * 16384) + ks * 32);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(sB) + ks * 32), IDESC, 1u);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(sB + BT) + ks * 32), IDESC, 1u);
+          }
+      }
+      good = good && tc::mbar_wait(&barF0, ph_f0);  // slot 0 free again
+      ph_f0 ^= 1;
+      if (good) issue_split(c, 2, sA0, &barA0);
+      good = good && tc::mbar_wait(&barA0, ph_a0);
+      ph_a0 ^= 1;
+      tc::tc_fence_after();
+      if (good) {
+        for (int ks = 0; ks < 4; ++ks)
+          for (int tb = 0; tb < NT; ++tb) {
+            const uint32_t cr = tmem + (uint32_t)((tb * 2 + 1) * NC);
+            const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA0 + tb * 16384) + ks * 32);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(sB) + ks * 32), IDESC, 1u);
+          }
+      }
+      if (!good) ok = false;
+      tc::mma_commit(&barM);
+    }
   }
-  if (stage > 0 && !tc::mbar_wait(&barM, (stage - 1) & 1)) ok = false;
+  if (nchp > 0 && !tc::mbar_wait(&barM, (nchp - 1) & 1)) ok = false;
   ok = __syncthreads_and(ok);
   tc::tc_fence_after();
   if (!ok) {
     if (tid == 0) tc_record_error(t.err);
   } else {
-    const int jl = 32 * warp + lane;
-    const int jg = tt * 128 + jl;
     const int NHP = t.ntt * 128;
     const float sP = t.inv_scale[(size_t)mc * NHP + jg];
     const float sdP = VEC ? t.inv_scale[((size_t)g.n_m + mc) * NHP + jg] : 0.f;
-    const bool odd_ok = n_l >= 2;
     const uint32_t lane_off = (uint32_t)(32 * warp) << 16;
     const float dm = (float)m;
-    for (int cc0 = 0; cc0 < 128; cc0 += 32) {
-      float Pe[32], Po[32];
-      tc::tmem_ld32(tmem + lane_off + 0 * 128 + cc0, Pe);
-      tc::tmem_ld32(tmem + lane_off + 1 * 128 + cc0, Po);
-      if (!odd_ok)
+    for (int cc0 = 0; cc0 < NC; cc0 += 32) {
+      float P[32], X[32];
+      tc::tmem_ld32(tmem + lane_off + 0 * NC + cc0, P);
+      tc::tmem_ld32(tmem + lane_off + 1 * NC + cc0, X);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) Po[i] = 0.f;
+      for (int i = 0; i < 32; ++i) P[i] = (P[i] + X[i]) * sP;
       if (!VEC) {
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          const int cq = ct * 64 + cc0 / 2 + q;
+          const int cq = ct * (NC / 2) + cc0 / 2 + q;
           if (cq >= ncplx || jg >= g.nh) continue;
           const int r = cq / s.nf, f = cq - r * s.nf;
-          const float2 es = make_float2(Pe[2 * q] * sP, Pe[2 * q + 1] * sP);
-          const float2 ea = make_float2(Po[2 * q] * sP, Po[2 * q + 1] * sP);
-          float2* o = (float2*)s.f[f].out0 + (long long)r * s.f[f].out_ld + (long long)mc * g.n_theta + 2 * jg;
-          o[0] = make_float2(es.x + ea.x, es.y + ea.y);
-          o[1] = make_float2(es.x - ea.x, es.y - ea.y);
+          *out_ptr(s.f[f].out0, r, f, 0) = make_float2(P[2 * q], P[2 * q + 1]);
         }
       } else {
-        float De[32], Do[32];
-        tc::tmem_ld32(tmem + lane_off + 2 * 128 + cc0, De);
-        tc::tmem_ld32(tmem + lane_off + 3 * 128 + cc0, Do);
-        if (!odd_ok)
+        float D[32];
+        tc::tmem_ld32(tmem + lane_off + 2 * NC + cc0, D);
+        tc::tmem_ld32(tmem + lane_off + 3 * NC + cc0, X);
 #pragma unroll
-          for (int i = 0; i < 32; ++i) Do[i] = 0.f;
+        for (int i = 0; i < 32; ++i) D[i] = (D[i] + X[i]) * sdP;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const int pair = ct * 32 + cc0 / 4 + q;
+          const int pair = ct * (NC / 4) + cc0 / 4 + q;
           if (pair >= npair || jg >= g.nh) continue;
           const int r = pair / s.nf, f = pair - r * s.nf;
-          // C = sum S P, B = sum T P, A = sum S dP, D = sum T dP (even/odd)
-          const float Cer = Pe[4 * q] * sP, Cei = Pe[4 * q + 1] * sP;
-          const float Ber = Pe[4 * q + 2] * sP, Bei = Pe[4 * q + 3] * sP;
-          const float Cor = Po[4 * q] * sP, Coi = Po[4 * q + 1] * sP;
-          const float Bor = Po[4 * q + 2] * sP, Boi = Po[4 * q + 3] * sP;
-          const float Aer = De[4 * q] * sdP, Aei = De[4 * q + 1] * sdP;
-          const float Der = De[4 * q + 2] * sdP, Dei = De[4 * q + 3] * sdP;
-          const float Aor = Do[4 * q] * sdP, Aoi = Do[4 * q + 1] * sdP;
-          const float Dor = Do[4 * q + 2] * sdP, Doi = Do[4 * q + 3] * sdP;
-          const float bNr = Ber + Bor, bNi = Bei + Boi, bSr = Ber - Bor, bSi = Bei - Boi;
-          const float cNr = Cer + Cor, cNi = Cei + Coi, cSr = Cer - Cor, cSi = Cei - Coi;
-          const float2 vtN = make_float2(Aer + Aor - dm * bNi, Aei + Aoi + dm * bNr);
-          const float2 vtS = make_float2(Aor - Aer - dm * bSi, Aoi - Aei + dm * bSr);
-          const float2 vpN = make_float2(-dm * cNi - (Der + Dor), dm * cNr - (Dei + Doi));
-          const float2 vpS = make_float2(-dm * cSi + (Der - Dor), dm * cSr + (Dei - Doi));
-          const long long o = (long long)r * s.f[f].out_ld + (long long)mc * g.n_theta + 2 * jg;
-          float2* o0 = (float2*)s.f[f].out0 + o;
-          float2* o1 = (float2*)s.f[f].out1 + o;
-          o0[0] = vtN; o0[1] = vtS;
-          o1[0] = vpN; o1[1] = vpS;
+          // C = sum S P, B = sum T P (columns S, T of the pair against P);
+          // A = sum S dP, D = sum T dP (against dP)
+          const float Cr = P[4 * q], Ci = P[4 * q + 1], Br = P[4 * q + 2], Bi = P[4 * q + 3];
+          const float Ar = D[4 * q], Ai = D[4 * q + 1], Dr = D[4 * q + 2], Di = D[4 * q + 3];
+          // v_theta: U = i m B, W = A;   v_phi: U = i m C, W = -D
+          const float2 Ut = make_float2(-dm * Bi, dm * Br), Wt = make_float2(Ar, Ai);
+          const float2 Up = make_float2(-dm * Ci, dm * Cr), Wp = make_float2(-Dr, -Di);
+          *out_ptr(s.f[f].out0, r, f, 0) = make_float2(Ut.x + Wt.x, Ut.y + Wt.y);
+          *out_ptr(s.f[f].out0, r, f, 1) = make_float2(Ut.x - Wt.x, Ut.y - Wt.y);
+          *out_ptr(s.f[f].out1, r, f, 0) = make_float2(Up.x + Wp.x, Up.y + Wp.y);
+          *out_ptr(s.f[f].out1, r, f, 1) = make_float2(Up.x - Wp.x, Up.y - Wp.y);
         }
       }
     }
@@ -326,16 +373,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) inv_leg_tc(const ShtGeom g, con
   if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
 }
 
+// Analysis, one (m, parity, l' tile, column tile) per CTA.  P x (ES or EA of
+// the same parity) and, for vector fields, dP x (the other one); hi*hi and
+// cross products in separate accumulators; table splits through a 2-slot
+// ring as in the synthesis.
 template <bool VEC>
-__global__ void __launch_bounds__(TC_THREADS, 1) fwd_leg_tc(const ShtGeom g, const FwdSet s, const TcTables t) {
+__global__ void __launch_bounds__(TC_THREADS, 2) fwd_leg_tc(const ShtGeom g, const FwdSet s, const TcTables t) {
   constexpr int NT = VEC ? 2 : 1;
-  constexpr uint32_t TMEM_COLS = VEC ? 256 : 128;
+  constexpr int NC = VEC ? 64 : 128;
+  constexpr int BT = NC * 128;
+  constexpr uint32_t TMEM_COLS = NT * 2 * NC;  // 256
+  constexpr uint32_t IDESC = tc::idesc_bf16(128, NC);
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t barA, barM;
+  __shared__ uint64_t barA0, barA1, barF0, barM;
   __shared__ uint32_t tmem_base;
   unsigned char* base = align1024(smem_raw);
-  unsigned char* sA = base;                      // [NT][3] x 16 KB
-  unsigned char* sB = sA + NT * 3 * 16384;       // [NT][3] x 16 KB (mine, other)
+  unsigned char* sA0 = base;
+  unsigned char* sA1 = sA0 + NT * 16384;
+  unsigned char* sB = sA1 + NT * 16384;        // [NT][3] x BT (mine, other)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ct = blockIdx.x, lt = blockIdx.y;
   const int mc = blockIdx.z >> 1, p = blockIdx.z & 1;
@@ -345,10 +400,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fwd_leg_tc(const ShtGeom g, con
   const int lm0 = g.lmoff[mc];
   const int npair = s.nf * s.nlev;
   const int ncplx = npair * (VEC ? 2 : 1);
-  if (lt * 128 >= nlp || ct * 64 >= ncplx) return;
+  if (lt * 128 >= nlp || ct * (NC / 2) >= ncplx) return;
 
   if (tid == 0) {
-    tc::mbar_init(&barA, 1);
+    tc::mbar_init(&barA0, 1);
+    tc::mbar_init(&barA1, 1);
+    tc::mbar_init(&barF0, 1);
     tc::mbar_init(&barM, 1);
     tc::fence_mbar_init();
   }
@@ -360,25 +417,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fwd_leg_tc(const ShtGeom g, con
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_base;
-  const int mine = p, other = p ^ 1;  // 0 = ES, 1 = EA
-
+  const int mine = p;  // 0 = ES, 1 = EA
+  uint32_t ph_a0 = 0, ph_a1 = 0, ph_f0 = 0;
   bool ok = true;
-  int stage = 0;
-  for (int c = 0; c < t.ncj; ++c, ++stage) {
-    if (stage > 0 && !tc::mbar_wait(&barM, (stage - 1) & 1)) ok = false;
+  auto issue_split = [&](int c, int sp, unsigned char* slot, uint64_t* bar) {
+    tc::mbar_expect_tx(bar, NT * 16384);
+    for (int tb = 0; tb < NT; ++tb) {
+      const long long blk = t.fwd_blk0[mc] + ((((long long)p * t.nlt + lt) * 2 + tb) * t.ncj + c) * 3 + sp;
+      tc::bulk_g2s(slot + tb * 16384, t.fwd_img + blk * 16384, 16384, bar);
+    }
+  };
+  for (int c = 0; c < t.ncj; ++c) {
+    if (c > 0 && !tc::mbar_wait(&barM, (c - 1) & 1)) ok = false;
     if (!__syncthreads_and(ok)) { ok = false; break; }
     if (tid == 0) {
-      tc::mbar_expect_tx(&barA, NT * 3 * 16384);
-      for (int tb = 0; tb < NT; ++tb)
-        for (int sp = 0; sp < 3; ++sp) {
-          const long long blk =
-              t.fwd_blk0[mc] + ((((long long)p * t.nlt + lt) * 2 + tb) * t.ncj + c) * 3 + sp;
-          tc::bulk_g2s(sA + (tb * 3 + sp) * 16384, t.fwd_img + blk * 16384, 16384, &barA);
-        }
+      issue_split(c, 0, sA0, &barA0);
+      issue_split(c, 1, sA1, &barA1);
     }
-    for (int u = tid; u < 64 * 8; u += TC_THREADS) {
+    for (int u = tid; u < (NC / 2) * 8; u += TC_THREADS) {
       const int ql = u >> 3, kg = u & 7;
-      const int q = ct * 64 + ql;
+      const int q = ct * (NC / 2) + ql;
       float mr[8], mi[8], orr[8], oi[8];
 #pragma unroll
       for (int i = 0; i < 8; ++i) { mr[i] = mi[i] = orr[i] = oi[i] = 0.f; }
@@ -391,45 +449,72 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fwd_leg_tc(const ShtGeom g, con
         for (int i = 0; i < 8; ++i) {
           const int j = 64 * c + 8 * kg + i;
           if (j < g.nh) {
-            const float4 v = *(const float4*)(src + 2 * j);  // (ES, EA) of colatitude j
-            const float2 es = make_float2(v.x, v.y), ea = make_float2(v.z, v.w);
-            const float2 a = mine ? ea : es, b = mine ? es : ea;
-            mr[i] = a.x; mi[i] = a.y; orr[i] = b.x; oi[i] = b.y;
+            const float4 v = *(const float4*)(src + 2 * j);  // (ES, EA) at colatitude j
+            if (mine == 0) { mr[i] = v.x; mi[i] = v.y; orr[i] = v.z; oi[i] = v.w; }
+            else { mr[i] = v.z; mi[i] = v.w; orr[i] = v.x; oi[i] = v.y; }
           }
         }
       }
-      store_split8(sB, tc::sw128_offset(2 * ql, 8 * kg), mr);
-      store_split8(sB, tc::sw128_offset(2 * ql + 1, 8 * kg), mi);
+      store_split8(sB, tc::sw128_offset(2 * ql, 8 * kg), mr, BT);
+      store_split8(sB, tc::sw128_offset(2 * ql + 1, 8 * kg), mi, BT);
       if (VEC) {
-        store_split8(sB + 3 * 16384, tc::sw128_offset(2 * ql, 8 * kg), orr);
-        store_split8(sB + 3 * 16384, tc::sw128_offset(2 * ql + 1, 8 * kg), oi);
+        store_split8(sB + 3 * BT, tc::sw128_offset(2 * ql, 8 * kg), orr, BT);
+        store_split8(sB + 3 * BT, tc::sw128_offset(2 * ql + 1, 8 * kg), oi, BT);
       }
     }
-    (void)other;
     tc::fence_proxy_async_smem();
     tc::tc_fence_before();
     __syncthreads();
     if (tid == 0) {
-      if (!tc::mbar_wait(&barA, stage & 1)) {
-        ok = false;
-      } else {
-        tc::tc_fence_after();
+      bool good = tc::mbar_wait(&barA0, ph_a0);
+      ph_a0 ^= 1;
+      tc::tc_fence_after();
+      if (good) {
         for (int ks = 0; ks < 4; ++ks)
-          for (int tb = 0; tb < NT; ++tb) {
-            // P x mine -> D0,  dP x other -> D1
-            const uint32_t d = tmem + (uint32_t)(tb * 128);
-            for (int pr = 0; pr < 6; ++pr) {
-              const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA + (tb * 3 + kSplitPairs[pr][0]) * 16384) + ks * 32);
-              const uint64_t bd =
-                  tc::sw128_desc(tc::smem_u32(sB + (tb * 3 + kSplitPairs[pr][1]) * 16384) + ks * 32);
-              tc::mma_bf16(d, ad, bd, TC_IDESC, (c | ks | pr) ? 1u : 0u);
-            }
+          for (int tb = 0; tb < NT; ++tb) {  // tb 0: P x mine, tb 1: dP x other
+            const uint32_t hi = tmem + (uint32_t)((tb * 2 + 0) * NC), cr = tmem + (uint32_t)((tb * 2 + 1) * NC);
+            const unsigned char* b = sB + tb * 3 * BT;
+            const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA0 + tb * 16384) + ks * 32);
+            const uint32_t first = (c | ks) ? 1u : 0u;
+            tc::mma_bf16(hi, ad, tc::sw128_desc(tc::smem_u32(b) + ks * 32), IDESC, first);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(b + BT) + ks * 32), IDESC, first);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(b + 2 * BT) + ks * 32), IDESC, 1u);
           }
       }
+      tc::mma_commit(&barF0);
+      good = good && tc::mbar_wait(&barA1, ph_a1);
+      ph_a1 ^= 1;
+      tc::tc_fence_after();
+      if (good) {
+        for (int ks = 0; ks < 4; ++ks)
+          for (int tb = 0; tb < NT; ++tb) {
+            const uint32_t cr = tmem + (uint32_t)((tb * 2 + 1) * NC);
+            const unsigned char* b = sB + tb * 3 * BT;
+            const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA1 + tb * 16384) + ks * 32);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(b) + ks * 32), IDESC, 1u);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(b + BT) + ks * 32), IDESC, 1u);
+          }
+      }
+      good = good && tc::mbar_wait(&barF0, ph_f0);
+      ph_f0 ^= 1;
+      if (good) issue_split(c, 2, sA0, &barA0);
+      good = good && tc::mbar_wait(&barA0, ph_a0);
+      ph_a0 ^= 1;
+      tc::tc_fence_after();
+      if (good) {
+        for (int ks = 0; ks < 4; ++ks)
+          for (int tb = 0; tb < NT; ++tb) {
+            const uint32_t cr = tmem + (uint32_t)((tb * 2 + 1) * NC);
+            const unsigned char* b = sB + tb * 3 * BT;
+            const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA0 + tb * 16384) + ks * 32);
+            tc::mma_bf16(cr, ad, tc::sw128_desc(tc::smem_u32(b) + ks * 32), IDESC, 1u);
+          }
+      }
+      if (!good) ok = false;
       tc::mma_commit(&barM);
     }
   }
-  if (stage > 0 && !tc::mbar_wait(&barM, (stage - 1) & 1)) ok = false;
+  if (t.ncj > 0 && !tc::mbar_wait(&barM, (t.ncj - 1) & 1)) ok = false;
   ok = __syncthreads_and(ok);
   tc::tc_fence_after();
   if (!ok) {
@@ -443,38 +528,42 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fwd_leg_tc(const ShtGeom g, con
     const float sP = valid ? t.fwd_scale[lm] : 0.f;
     const float sdP = (VEC && valid) ? t.fwd_scale[(size_t)g.lm_max + lm] : 0.f;
     const uint32_t lane_off = (uint32_t)(32 * warp) << 16;
-    const double dm = (double)m;
-    const double inv_ll = l > 0 ? 1.0 / (double)(l * (l + 1)) : 1.0;
-    for (int cc0 = 0; cc0 < 128; cc0 += 32) {
-      float D0[32];
-      tc::tmem_ld32(tmem + lane_off + cc0, D0);
+    const float dm = (float)m;
+    const float inv_ll = l > 0 ? 1.0f / (float)(l * (l + 1)) : 1.0f;
+    for (int cc0 = 0; cc0 < NC; cc0 += 32) {
+      float D0[32], X[32];
+      tc::tmem_ld32(tmem + lane_off + 0 * NC + cc0, D0);
+      tc::tmem_ld32(tmem + lane_off + 1 * NC + cc0, X);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) D0[i] = (D0[i] + X[i]) * sP;
       if (!VEC) {
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          const int cq = ct * 64 + cc0 / 2 + q;
+          const int cq = ct * (NC / 2) + cc0 / 2 + q;
           if (cq >= ncplx || !valid) continue;
           const int r = cq / s.nf, f = cq - r * s.nf;
           const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
-          const double2 v = (l <= lc) ? make_double2((double)(D0[2 * q] * sP), (double)(D0[2 * q + 1] * sP))
+          const double2 v = (l <= lc) ? make_double2(f2d_int(D0[2 * q]), f2d_int(D0[2 * q + 1]))
                                       : make_double2(0.0, 0.0);
           s.f[f].out0[(long long)r * s.f[f].out_ld + lm] = v;
         }
       } else {
         float D1[32];
-        tc::tmem_ld32(tmem + lane_off + 128 + cc0, D1);
+        tc::tmem_ld32(tmem + lane_off + 2 * NC + cc0, D1);
+        tc::tmem_ld32(tmem + lane_off + 3 * NC + cc0, X);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) D1[i] = (D1[i] + X[i]) * sdP;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const int pair = ct * 32 + cc0 / 4 + q;
+          const int pair = ct * (NC / 4) + cc0 / 4 + q;
           if (pair >= npair || !valid) continue;
           const int r = pair / s.nf, f = pair - r * s.nf;
           const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
           // A = sum F1_mine P, D = sum F2_mine P, C = sum F1_other dP, B = sum F2_other dP
-          const double Ar = D0[4 * q] * sP, Ai = D0[4 * q + 1] * sP;
-          const double Dr = D0[4 * q + 2] * sP, Di = D0[4 * q + 3] * sP;
-          const double Cr = D1[4 * q] * sdP, Ci = D1[4 * q + 1] * sdP;
-          const double Br = D1[4 * q + 2] * sdP, Bi = D1[4 * q + 3] * sdP;
-          double2 Sv = make_double2((dm * Ai + Br) * inv_ll, (-dm * Ar + Bi) * inv_ll);
-          double2 Tv = make_double2((-Cr + dm * Di) * inv_ll, (-Ci - dm * Dr) * inv_ll);
+          const float Ar = D0[4 * q], Ai = D0[4 * q + 1], Dr = D0[4 * q + 2], Di = D0[4 * q + 3];
+          const float Cr = D1[4 * q], Ci = D1[4 * q + 1], Br = D1[4 * q + 2], Bi = D1[4 * q + 3];
+          double2 Sv = make_double2(f2d_int((dm * Ai + Br) * inv_ll), f2d_int((-dm * Ar + Bi) * inv_ll));
+          double2 Tv = make_double2(f2d_int((-Cr + dm * Di) * inv_ll), f2d_int((-Ci - dm * Dr) * inv_ll));
           if (l > lc) { Sv = make_double2(0.0, 0.0); Tv = Sv; }
           const long long o = (long long)r * s.f[f].out_ld + lm;
           s.f[f].out0[o] = Sv;
@@ -560,9 +649,9 @@ template <bool VEC>
 cudaError_t launch_inv_tc_t(const ShtGeom& g, const InvSet& s, const TcTables& t, cudaStream_t st) {
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
-  const size_t smem = 1024 + (size_t)((VEC ? 2 : 1) * 3 + 3) * 16384;
+  const size_t smem = 1024 + (size_t)(VEC ? 2 : 1) * 2 * 16384 + 3 * 64 * 128;
   CUDA_TRY(cudaFuncSetAttribute(inv_leg_tc<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid(t.ntt, (ncplx + 63) / 64, g.n_m);
+  dim3 grid(t.ntt, (ncplx + 31) / 32, g.n_m * 2);
   inv_leg_tc<VEC><<<grid, TC_THREADS, smem, st>>>(g, s, t);
   return cudaGetLastError();
 }
@@ -571,9 +660,10 @@ template <bool VEC>
 cudaError_t launch_fwd_tc_t(const ShtGeom& g, const FwdSet& s, const TcTables& t, cudaStream_t st) {
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
-  const size_t smem = 1024 + (size_t)((VEC ? 2 : 1) * 6) * 16384;
+  constexpr int NC = VEC ? 64 : 128;
+  const size_t smem = 1024 + (size_t)(VEC ? 2 : 1) * 2 * 16384 + (size_t)(VEC ? 2 : 1) * 3 * NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tc<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((ncplx + 63) / 64, t.nlt, g.n_m * 2);
+  dim3 grid((ncplx + NC / 2 - 1) / (NC / 2), t.nlt, g.n_m * 2);
   fwd_leg_tc<VEC><<<grid, TC_THREADS, smem, st>>>(g, s, t);
   return cudaGetLastError();
 }

@@ -143,6 +143,20 @@ bool is_device_ptr(const void* p) {
 bool fp64_pipes(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_FP64; }
 size_t t2_bytes(const magic_sht_handle* h) { return fp64_pipes(h) ? 16 : 8; }
 
+size_t hs_bytes(const magic_sht_handle* h, int nlev) {
+  return (size_t)nlev * h->g.n_m * h->g.n_theta * t2_bytes(h);
+}
+
+// Synthesis half spectra of a vector component in the tensor-core form hold
+// E and F for both parities: twice the entries of the N/S layout.
+bool tc_form(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_BF16X3; }
+size_t hs_inv_bytes(const magic_sht_handle* h, int nlev, bool vec) {
+  return hs_bytes(h, nlev) * ((vec && tc_form(h)) ? 2 : 1);
+}
+long long hs_inv_ld(const magic_sht_handle* h, bool vec) {
+  return (long long)h->g.n_m * h->g.n_theta * ((vec && tc_form(h)) ? 2 : 1);
+}
+
 cudaEvent_t next_event(magic_sht_handle* h) {
   if (h->ev_used == h->ev_pool.size()) {
     cudaEvent_t e;
@@ -308,7 +322,8 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
                 const std::vector<ScalarInv>& sc, const std::vector<VectorInv>& vc,
                 const std::vector<int>& hs_sc, const std::vector<int>& hs_vc) {
   const ShtGeom& g = h->g;
-  const long long hs_ld = (long long)g.n_m * g.n_theta;
+  const long long hs_ld = hs_inv_ld(h, false), hs_ld_v = hs_inv_ld(h, true);
+  const int flag_s = tc_form(h) ? FFT_IN_E : 0, flag_v = tc_form(h) ? FFT_IN_EF : 0;
   const bool f64 = fp64_pipes(h);
   const int* d_lcut = (const int*)cx.dev(lv.lcut_idx);
   const double* d_or2 = (const double*)cx.dev(lv.or2_idx);
@@ -322,10 +337,10 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     }
     return MAGIC_SHT_OK;
   };
-  auto add_fft = [&](void* in, int out_idx, int flags) -> int {
+  auto add_fft = [&](void* in, int out_idx, int flags, long long in_ld) -> int {
     if (fs.nf == MAGIC_MAX_FIELDS) TRY(flush_fft());
     FftField& f = fs.f[fs.nf++];
-    f.in = in; f.out = cx.dev(out_idx); f.in_ld = hs_ld; f.out_ld = lv.grid_ld;
+    f.in = in; f.out = cx.dev(out_idx); f.in_ld = in_ld; f.out_ld = lv.grid_ld;
     f.flags = flags; f.pad_ = 0;
     return MAGIC_SHT_OK;
   };
@@ -349,16 +364,16 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       InvField& f = s.f[s.nf++];
       f.x0 = make_operand(cx, vc[i].s, lv.spec_ld);
       f.x1 = make_operand(cx, vc[i].t, lv.spec_ld);
-      f.out0 = cx.dev(hs_vc[2 * i]); f.out1 = cx.dev(hs_vc[2 * i + 1]); f.out_ld = hs_ld;
+      f.out0 = cx.dev(hs_vc[2 * i]); f.out1 = cx.dev(hs_vc[2 * i + 1]); f.out_ld = hs_ld_v;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_VECTOR);
     if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, true, h->tct, h->stream));
     else CK(launch_inv_legendre_simt(g, s, true, f64, h->stream));
   }
-  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags));
+  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
   for (size_t i = 0; i < vc.size(); ++i) {
-    TRY(add_fft(cx.dev(hs_vc[2 * i]), vc[i].out_t, vc[i].flags));
-    TRY(add_fft(cx.dev(hs_vc[2 * i + 1]), vc[i].out_p, vc[i].flags));
+    TRY(add_fft(cx.dev(hs_vc[2 * i]), vc[i].out_t, vc[i].flags | flag_v, hs_ld_v));
+    TRY(add_fft(cx.dev(hs_vc[2 * i + 1]), vc[i].out_p, vc[i].flags | flag_v, hs_ld_v));
   }
   return flush_fft();
 }
@@ -434,9 +449,7 @@ int check_lcut(const magic_sht_handle* h, int lcut) {
   return MAGIC_SHT_OK;
 }
 
-size_t hs_bytes(const magic_sht_handle* h, int nlev) {
-  return (size_t)nlev * h->g.n_m * h->g.n_theta * t2_bytes(h);
-}
+
 
 // Single-level synthesis helper.
 int inverse_one(magic_sht_handle* h, int lcut, double or2, const std::vector<const double*>& specs,
@@ -458,7 +471,7 @@ int inverse_one(magic_sht_handle* h, int lcut, double or2, const std::vector<con
   build(si, gi, sc, vc);
   std::vector<int> hs_sc, hs_vc;
   for (size_t i = 0; i < sc.size(); ++i) hs_sc.push_back(cx.tmp(hs_bytes(h, 1)));
-  for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_bytes(h, 1)));
+  for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_inv_bytes(h, 1, true)));
   TRY(cx.prepare());
   LevelCtl lv;
   lv.nlev = 1; lv.lcut0 = lcut; lv.or2_0 = or2;
@@ -730,7 +743,7 @@ int magic_sht_reserve(magic_sht_handle* h, int n) {
   DeviceGuard dg(h->device);
   // the radial set needs 15 inverse half spectra (the forward set needs 10)
   // plus per-level lcut/or2 staging
-  const size_t need = 15 * align256(hs_bytes(h, n)) + 4 * align256((size_t)n * 8) + 4096;
+  const size_t need = (tc_form(h) ? 23 : 15) * align256(hs_bytes(h, n)) + 4 * align256((size_t)n * 8) + 4096;
   return ensure_ws(h, need);
 }
 
@@ -844,7 +857,7 @@ static int ic_qst(magic_sht_handle* h, double r, double r_ICB, const double* A0,
   const int iQ = cx.tmp(16 * (size_t)K), iS = cx.tmp(16 * (size_t)K), iT = cx.tmp(16 * (size_t)K);
   const long long gl = (long long)g.n_phi * g.ld;
   const int g0 = cx.grid_out(o0, 1, gl), g1 = cx.grid_out(o1, 1, gl), g2 = cx.grid_out(o2, 1, gl);
-  const int hs0 = cx.tmp(hs_bytes(h, 1)), hs1 = cx.tmp(hs_bytes(h, 1)), hs2 = cx.tmp(hs_bytes(h, 1));
+  const int hs0 = cx.tmp(hs_bytes(h, 1)), hs1 = cx.tmp(hs_inv_bytes(h, 1, true)), hs2 = cx.tmp(hs_inv_bytes(h, 1, true));
   TRY(cx.prepare());
   std::vector<double> cf;
   cf.insert(cf.end(), cq.begin(), cq.end());
@@ -1016,7 +1029,7 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
   }
   std::vector<int> hs_sc, hs_vc;
   for (size_t i = 0; i < sc.size(); ++i) hs_sc.push_back(cx.tmp(hs_bytes(h, n)));
-  for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_bytes(h, n)));
+  for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_inv_bytes(h, n, true)));
   TRY(cx.prepare());
   TRY(run_inverse(h, cx, lv, sc, vc, hs_sc, hs_vc));
   return cx.finish();
@@ -1310,7 +1323,7 @@ extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double*
   fs.f[0].out = fieldc;
   fs.f[0].in_ld = hs_ld;
   fs.f[0].out_ld = (long long)g.n_phi * g.ld;
-  fs.f[0].flags = 0;
+  fs.f[0].flags = tc_form(h) ? FFT_IN_E : 0;  // parity-separated synthesis output
   CK(launch_fft_inverse(g, fs, fp64_pipes(h), h->stream));
   return MAGIC_SHT_OK;
 }
