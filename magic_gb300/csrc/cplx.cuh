@@ -30,10 +30,6 @@ template <typename T2, typename S> __device__ __forceinline__ T2 cscale(T2 a, S 
   T2 r; r.x = a.x * s; r.y = a.y * s; return r;
 }
 
-template <typename T2> __device__ __forceinline__ T2 cvt2(double2 a);
-template <> __device__ __forceinline__ double2 cvt2<double2>(double2 a) { return a; }
-template <> __device__ __forceinline__ float2 cvt2<float2>(double2 a) { return make_float2((float)a.x, (float)a.y); }
-template <typename T2> __device__ __forceinline__ double2 to_d2(T2 a) { return make_double2((double)a.x, (double)a.y); }
 
 template <typename T2> __device__ __forceinline__ T2 shfl_xor2(T2 v, int d) {
   T2 r; r.x = __shfl_xor_sync(0xffffffffu, v.x, d); r.y = __shfl_xor_sync(0xffffffffu, v.y, d); return r;
@@ -41,8 +37,8 @@ template <typename T2> __device__ __forceinline__ T2 shfl_xor2(T2 v, int d) {
 
 // FP64 <-> FP32 conversions with integer instructions only (the FP64 pipe of
 // GB300 is narrow; these conversions run on the integer/FP32 pipes).
-// d2f: round to nearest even, magnitudes below 2^-126 flush to zero, no
-// overflow handling (transform data stays far inside the FP32 range).
+// d2f: round to nearest even; magnitudes below 2^-126 flush to zero, beyond
+// the FP32 range give +-Inf, NaN stays NaN.
 __device__ __forceinline__ float d2f_int(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned int hi = (unsigned int)(b >> 32), lo = (unsigned int)b;
@@ -50,19 +46,38 @@ __device__ __forceinline__ float d2f_int(double x) {
   const unsigned int sign = hi & 0x80000000u;
   if (e < 1023 - 126) return __uint_as_float(sign);
   const unsigned int mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  if (e > 1023 + 127) {
+    const bool nan = e == 0x7FF && ((hi & 0xFFFFFu) | lo) != 0u;
+    return __uint_as_float(sign | 0x7F800000u | (nan ? 0x400000u : 0u));
+  }
   unsigned int f = sign | ((unsigned int)(e - 1023 + 127) << 23) | mant;
   const unsigned int rbit = (lo >> 28) & 1u;
   const unsigned int sticky = (lo & 0x0FFFFFFFu) != 0u;
-  if (rbit && (sticky || (mant & 1u))) f += 1u;
+  if (rbit && (sticky || (mant & 1u))) f += 1u;  // a carry may round up to Inf: correct
   return __uint_as_float(f);
 }
-// exact widening (normal numbers and zero; FP32 subnormals flush to zero)
+// exact widening (normal numbers, zero, Inf and NaN; FP32 subnormals flush to zero)
 __device__ __forceinline__ double f2d_int(float x) {
   const unsigned int u = __float_as_uint(x);
   const unsigned int e = (u >> 23) & 0xFFu;
   const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
   if (e == 0) return __longlong_as_double((long long)sign);
-  const unsigned long long bits = sign | ((unsigned long long)(e - 127 + 1023) << 52) |
-                                  ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  const unsigned long long ed = e == 0xFFu ? 0x7FFull : (unsigned long long)(e - 127 + 1023);
+  const unsigned long long bits = sign | (ed << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
   return __longlong_as_double((long long)bits);
 }
+
+// Conversions between a transform's working type T and the FP64 of the
+// grids and spectra: identity for double, integer-only for float.
+template <typename T> __device__ __forceinline__ double to_f64(T x);
+template <> __device__ __forceinline__ double to_f64<double>(double x) { return x; }
+template <> __device__ __forceinline__ double to_f64<float>(float x) { return f2d_int(x); }
+template <typename T> __device__ __forceinline__ T from_f64(double x);
+template <> __device__ __forceinline__ double from_f64<double>(double x) { return x; }
+template <> __device__ __forceinline__ float from_f64<float>(double x) { return d2f_int(x); }
+
+template <typename T2> __device__ __forceinline__ T2 cvt2(double2 a);
+template <> __device__ __forceinline__ double2 cvt2<double2>(double2 a) { return a; }
+template <> __device__ __forceinline__ float2 cvt2<float2>(double2 a) { return make_float2(d2f_int(a.x), d2f_int(a.y)); }
+__device__ __forceinline__ double2 to_d2(double2 a) { return a; }
+__device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(f2d_int(a.x), f2d_int(a.y)); }

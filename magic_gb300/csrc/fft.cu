@@ -235,19 +235,19 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
     if (rowg >= g.n_theta) continue;
     const T2 v0 = sm[rr * KP + (ph >> 1)];
     const T2 v1 = sm[(rr + 1) * KP + (ph >> 1)];
-    double x0 = (ph & 1) ? (double)v0.y : (double)v0.x;
-    double x1 = (ph & 1) ? (double)v1.y : (double)v1.x;
+    T x0 = (ph & 1) ? v0.y : v0.x;
+    T x1 = (ph & 1) ? v1.y : v1.x;
     if (osin) {
-      const double o = g.osin2[rowg >> 1];  // rows 2j and 2j+1 share theta_j
+      const T o = from_f64<T>(g.osin2[rowg >> 1]);  // rows 2j and 2j+1 share theta_j
       x0 *= o;
       x1 *= o;
     }
     double* dst = out + (long long)ph * g.ld + rowg;
     if (vec) {
-      *reinterpret_cast<double2*>(dst) = make_double2(x0, x1);
+      *reinterpret_cast<double2*>(dst) = make_double2(to_f64<T>(x0), to_f64<T>(x1));
     } else {
-      dst[0] = x0;
-      dst[1] = x1;
+      dst[0] = to_f64<T>(x0);
+      dst[1] = to_f64<T>(x1);
     }
   }
 }
@@ -326,8 +326,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
       c[h] = X;
     }
     Tt fac = 1;
-    if (fd.flags & FFT_OSIN2) fac *= (Tt)g.osin2[jg];
-    if (fd.flags & FFT_WEIGHT) fac *= (Tt)g.wgt[jg];
+    if (fd.flags & FFT_OSIN2) fac *= from_f64<Tt>(g.osin2[jg]);
+    if (fd.flags & FFT_WEIGHT) fac *= from_f64<Tt>(g.wgt[jg]);
     c[0] = cscale(c[0], fac);
     c[1] = cscale(c[1], fac);
     const long long o = ((long long)k * g.nh + jg) * 2;
@@ -384,10 +384,11 @@ __device__ __forceinline__ void store_grid(const ShtGeom& g, const FftField& fd,
     const int ph = i / RT, rr = i - ph * RT;
     const int row = row0 + rr;
     if (row >= g.n_theta) continue;
+    typedef typename ScalarOf<T2>::t T;
     const T2 v = sm[(ph >> 1) * RP + rr];
-    double x = (ph & 1) ? (double)v.y : (double)v.x;
-    if (fd.flags & FFT_OSIN2) x *= g.osin2[row >> 1];
-    out[(long long)ph * g.ld + row] = x;
+    T x = (ph & 1) ? v.y : v.x;
+    if (fd.flags & FFT_OSIN2) x *= from_f64<T>(g.osin2[row >> 1]);
+    out[(long long)ph * g.ld + row] = to_f64<T>(x);
   }
 }
 
@@ -433,8 +434,8 @@ __device__ __forceinline__ void fwd_post(const ShtGeom& g, const FftField& fd, T
       c[h] = X;
     }
     T fac = 1;
-    if (fd.flags & FFT_OSIN2) fac *= (T)g.osin2[jg];
-    if (fd.flags & FFT_WEIGHT) fac *= (T)g.wgt[jg];
+    if (fd.flags & FFT_OSIN2) fac *= from_f64<T>(g.osin2[jg]);
+    if (fd.flags & FFT_WEIGHT) fac *= from_f64<T>(g.wgt[jg]);
     c[0] = cscale(c[0], fac); c[1] = cscale(c[1], fac);
     const long long o = ((long long)k * g.nh + jg) * 2;
     out[o] = cadd(c[0], c[1]);

@@ -37,3 +37,9 @@ cudaError_t launch_inv_legendre_tc(const ShtGeom& g, const InvSet& s, bool vec, 
                                    cudaStream_t st);
 cudaError_t launch_fwd_legendre_tc(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
                                    cudaStream_t st);
+// legendre_tcp.cu (pack kernels + persistent, warp-specialized tensor-core kernels)
+size_t tcp_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool vec, bool inverse);
+cudaError_t launch_inv_legendre_tcp(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
+                                    unsigned char* bimg, cudaStream_t st);
+cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
+                                    unsigned char* bimg, cudaStream_t st);

@@ -10,6 +10,7 @@
 #include "internal.h"
 #include "tc_ptx.cuh"
 #include "cplx.cuh"
+#include "tc_build.cuh"
 
 namespace {
 
@@ -119,17 +120,6 @@ __device__ __forceinline__ unsigned char* align1024(unsigned char* p) {
   return (unsigned char*)(((uintptr_t)p + 1023) & ~(uintptr_t)1023);
 }
 
-// 8 values -> three 16-byte chunks (hi, mid, lo) at the swizzled position
-__device__ __forceinline__ void store_split8(unsigned char* tile0, uint32_t off, const float (&v)[8],
-                                             uint32_t tile_bytes) {
-  __nv_bfloat16 h[8], md[8], lo[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) tc::split3(v[i], h[i], md[i], lo[i]);
-  *(uint4*)(tile0 + off) = *(const uint4*)h;
-  *(uint4*)(tile0 + tile_bytes + off) = *(const uint4*)md;
-  *(uint4*)(tile0 + 2 * tile_bytes + off) = *(const uint4*)lo;
-}
-
 __device__ __forceinline__ void tc_record_error(int* err) {
   if (err) atomicExch(err, 1);
 }
@@ -226,48 +216,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) inv_leg_tc(const ShtGeom g, con
       issue_split(c, 1, sA1, &barA1);
     }
     // data operand: 32 complex columns x 64 degrees of parity p
-    for (int u = tid; u < (NC / 2) * 8; u += TC_THREADS) {
-      const int ql = u >> 3, kg = u & 7;
-      const int q = ct * (NC / 2) + ql;
-      float re[8], im[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) { re[i] = 0.f; im[i] = 0.f; }
-      if (q < ncplx) {
-        const int pair = VEC ? (q >> 1) : q;
-        const int r = pair / s.nf, f = pair - r * s.nf;
-        const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
-        const SpecOperand& op = (VEC && (q & 1)) ? s.f[f].x1 : s.f[f].x0;
-        if (op.op != OP_ZERO && op.A != nullptr) {
-          const float o2 = (op.op == OP_CURLT) ? d2f_int(s.or2 ? s.or2[r] : s.or2_0) : 0.f;
-          const double2* A = op.A + (long long)r * op.ld;
-          const double2* B = op.B ? op.B + (long long)r * op.ld : nullptr;
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int l = m + p + 2 * (64 * c + 8 * kg + i);
-            if (l <= lc) {
-              const double2 a = A[lm0 + l - m];
-              float ar = d2f_int(a.x), ai = d2f_int(a.y);
-              switch (op.op) {
-                case OP_DLH: { const float d = (float)(l * (l + 1)); ar *= d; ai *= d; break; }
-                case OP_CURLT: {
-                  const double2 b = B[lm0 + l - m];
-                  const float d = o2 * (float)(l * (l + 1));
-                  ar = fmaf(d, ar, -d2f_int(b.x));
-                  ai = fmaf(d, ai, -d2f_int(b.y));
-                  break;
-                }
-                case OP_IM: { const float dm = (float)m, t0 = ar; ar = -dm * ai; ai = dm * t0; break; }
-                default: break;
-              }
-              re[i] = ar;
-              im[i] = ai;
-            }
-          }
-        }
-      }
-      store_split8(sB, tc::sw128_offset(2 * ql, 8 * kg), re, BT);
-      store_split8(sB, tc::sw128_offset(2 * ql + 1, 8 * kg), im, BT);
-    }
+    inv_build_tile<VEC, NC, 4>(g, s, sB, ct, ncplx, m, lm0, p, c, warp, TC_THREADS / 32, lane);
     tc::fence_proxy_async_smem();
     tc::tc_fence_before();
     __syncthreads();
@@ -434,34 +383,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) fwd_leg_tc(const ShtGeom g, con
       issue_split(c, 0, sA0, &barA0);
       issue_split(c, 1, sA1, &barA1);
     }
-    for (int u = tid; u < (NC / 2) * 8; u += TC_THREADS) {
-      const int ql = u >> 3, kg = u & 7;
-      const int q = ct * (NC / 2) + ql;
-      float mr[8], mi[8], orr[8], oi[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) { mr[i] = mi[i] = orr[i] = oi[i] = 0.f; }
-      if (q < ncplx) {
-        const int pair = VEC ? (q >> 1) : q;
-        const int r = pair / s.nf, f = pair - r * s.nf;
-        const float2* src = (const float2*)((VEC && (q & 1)) ? s.f[f].in1 : s.f[f].in0) +
-                            (long long)r * s.f[f].in_ld + (long long)mc * g.nh * 2;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int j = 64 * c + 8 * kg + i;
-          if (j < g.nh) {
-            const float4 v = *(const float4*)(src + 2 * j);  // (ES, EA) at colatitude j
-            if (mine == 0) { mr[i] = v.x; mi[i] = v.y; orr[i] = v.z; oi[i] = v.w; }
-            else { mr[i] = v.z; mi[i] = v.w; orr[i] = v.x; oi[i] = v.y; }
-          }
-        }
-      }
-      store_split8(sB, tc::sw128_offset(2 * ql, 8 * kg), mr, BT);
-      store_split8(sB, tc::sw128_offset(2 * ql + 1, 8 * kg), mi, BT);
-      if (VEC) {
-        store_split8(sB + 3 * BT, tc::sw128_offset(2 * ql, 8 * kg), orr, BT);
-        store_split8(sB + 3 * BT, tc::sw128_offset(2 * ql + 1, 8 * kg), oi, BT);
-      }
-    }
+    fwd_build_tile<VEC, NC, 4>(g, s, sB, ct, ncplx, mc, mine, c, warp, TC_THREADS / 32, lane);
     tc::fence_proxy_async_smem();
     tc::tc_fence_before();
     __syncthreads();

@@ -1,0 +1,607 @@
+// Persistent, warp-specialized tensor-core Legendre sums (3xBF16 split
+// products, fp32 accumulation in tensor memory) for the radial loop's
+// batched transforms.
+//
+// Two kernels per transform:
+//  1. a pack kernel splits the data operand once into 3xBF16 tiles in the
+//     exact shared-memory image of the MMA's K-major, 128-byte-swizzled
+//     operand (synthesis: spectra with their operator applied, one image per
+//     (m, parity, 64-degree chunk, column tile); analysis: the ES and EA half
+//     spectra, one image pair per (m, 64-colatitude chunk, column tile)).
+//     It runs at full occupancy and writes each tile with one bulk copy.
+//  2. one persistent CTA per SM walks a static list of output tiles
+//        synthesis tile = (m, parity, 128 colatitudes, column tile)
+//        analysis tile  = (m, parity, 128 degrees of that parity, column tile)
+//     with three roles:
+//        warp 0      bulk-copy loader of table tiles (A ring) and data tiles (B ring)
+//        warp 1      tcgen05.mma issuer (one thread)
+//        warps 2..9  epilogue: two warps per TMEM lane quadrant, each draining
+//                    half of the columns of one of two accumulator sets while
+//                    the next tile accumulates in the other
+// Hand-offs use full/empty mbarriers; every wait is bounded and a wait that
+// gives up sets the device error word.  The MMA sequence per accumulator is
+// that of legendre_tc.cu: hi*hi and the five cross products accumulate apart.
+#include <cuda_bf16.h>
+#include "common.cuh"
+#include "cplx.cuh"
+#include "internal.h"
+#include "tc_ptx.cuh"
+#include "tc_build.cuh"
+
+namespace {
+
+constexpr int kThreads = 320;     // 10 warps
+constexpr int kEpiThreads = 256;  // warps 2..9
+constexpr int kPackThreads = 256;
+
+__device__ __forceinline__ unsigned char* align1k(unsigned char* p) {
+  return (unsigned char*)(((uintptr_t)p + 1023) & ~(uintptr_t)1023);
+}
+
+// consumer waits for "full" with the round's parity, producer waits for
+// "empty" with the opposite parity (an empty ring passes at once)
+__device__ __forceinline__ bool wait_full(uint64_t* bar, uint32_t use, uint32_t ring) {
+  return tc::mbar_wait(bar, (use / ring) & 1u);
+}
+__device__ __forceinline__ bool wait_empty(uint64_t* bar, uint32_t use, uint32_t ring) {
+  return tc::mbar_wait(bar, ((use / ring) & 1u) ^ 1u);
+}
+
+// The loader's last copies (one per ring slot) have landed: nothing writes
+// shared memory after the CTA exits, also when a consumer gave up early.
+template <int N>
+__device__ __forceinline__ void drain_copies(uint64_t* full, uint32_t use) {
+  for (uint32_t u = use > N ? use - N : 0; u < use; ++u) wait_full(&full[u % N], u, N);
+}
+
+// Issue the MMAs of one table split `sp` against the three data splits.
+template <int NT, int NC>
+__device__ __forceinline__ void issue_split(uint32_t acc, const unsigned char* A, const unsigned char* B,
+                                            int sp, bool first_chunk, uint32_t bstride_tb) {
+  constexpr int BT = NC * 128;
+  constexpr uint32_t IDESC = tc::idesc_bf16(128, NC);
+  for (int ks = 0; ks < 4; ++ks)
+    for (int tb = 0; tb < NT; ++tb) {
+      const uint32_t hi = acc + (uint32_t)((tb * 2 + 0) * NC), cr = acc + (uint32_t)((tb * 2 + 1) * NC);
+      const uint64_t ad = tc::sw128_desc(tc::smem_u32(A + tb * 16384) + ks * 32);
+      const unsigned char* b = B + tb * bstride_tb;
+      const uint64_t b0 = tc::sw128_desc(tc::smem_u32(b) + ks * 32);
+      const uint64_t b1 = tc::sw128_desc(tc::smem_u32(b + BT) + ks * 32);
+      const uint64_t b2 = tc::sw128_desc(tc::smem_u32(b + 2 * BT) + ks * 32);
+      const uint32_t first = (!first_chunk || ks) ? 1u : 0u;
+      if (sp == 0) {
+        tc::mma_bf16(hi, ad, b0, IDESC, first);
+        tc::mma_bf16(cr, ad, b1, IDESC, first);
+        tc::mma_bf16(cr, ad, b2, IDESC, 1u);
+      } else if (sp == 1) {
+        tc::mma_bf16(cr, ad, b0, IDESC, 1u);
+        tc::mma_bf16(cr, ad, b1, IDESC, 1u);
+      } else {
+        tc::mma_bf16(cr, ad, b0, IDESC, 1u);
+      }
+    }
+}
+
+// ------------------------------------------------------------------ packing
+// Synthesis data images: [pc = bpc0[m] + p*nch + c][ct] tiles of 3 splits.
+template <bool VEC>
+__global__ void __launch_bounds__(kPackThreads) pack_inv_kernel(const ShtGeom g, const InvSet s, const TcTables t,
+                                                               unsigned char* __restrict__ bimg, int nct) {
+  constexpr int NC = VEC ? 64 : 128;
+  constexpr uint32_t BSZ = 3u * NC * 128u;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* buf = align1k(smem_raw);
+  const int ct = blockIdx.x, mc = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m = mc * g.minc, lm0 = g.lmoff[mc];
+  const int nch = tc_nch(g.l_max - m + 1);
+  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
+  const long long pc0 = t.bpc0[mc];
+  for (int i = 0; i < 2 * nch; ++i) {
+    unsigned char* B = buf + (i & 1) * BSZ;
+    if (i >= 2) {  // the copy that last read this buffer has finished reading it
+      if (threadIdx.x == 0) tc::bulk_wait_read<1>();
+      __syncthreads();
+    }
+    inv_build_tile<VEC, NC, 4>(g, s, B, ct, ncplx, m, lm0, i / nch, i % nch, warp, kPackThreads / 32, lane);
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc::bulk_s2g(bimg + ((pc0 + i) * nct + ct) * (long long)BSZ, B, BSZ);
+      tc::bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) tc::bulk_wait<0>();
+}
+
+// Analysis data images: [m][c][ct] pairs (ES tile, EA tile) of 3 splits each.
+template <bool VEC>
+__global__ void __launch_bounds__(kPackThreads) pack_fwd_kernel(const ShtGeom g, const FwdSet s, const TcTables t,
+                                                               unsigned char* __restrict__ bimg, int nct) {
+  constexpr int NC = VEC ? 64 : 128;
+  constexpr uint32_t PSZ = 2u * 3u * NC * 128u;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* buf = align1k(smem_raw);
+  const int ct = blockIdx.x, mc = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
+  for (int c = 0; c < t.ncj; ++c) {
+    unsigned char* B = buf + (c & 1) * PSZ;
+    if (c >= 2) {
+      if (threadIdx.x == 0) tc::bulk_wait_read<1>();
+      __syncthreads();
+    }
+    fwd_build_tile<VEC, NC, 4, true>(g, s, B, ct, ncplx, mc, 0, c, warp, kPackThreads / 32, lane);
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc::bulk_s2g(bimg + (((long long)mc * t.ncj + c) * nct + ct) * (long long)PSZ, B, PSZ);
+      tc::bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) tc::bulk_wait<0>();
+}
+
+// ------------------------------------------------------------ synthesis
+struct InvTile {
+  int mc, p, tt, ct, nch, nchp, nlp;
+  __device__ void decode(const ShtGeom& g, const TcTables& t, int nct, int ix) {
+    ct = ix % nct;
+    int rest = ix / nct;
+    tt = rest % t.ntt;
+    rest /= t.ntt;
+    p = rest & 1;
+    mc = rest >> 1;
+    const int n_l = g.l_max - mc * g.minc + 1;
+    nch = tc_nch(n_l);
+    nlp = (n_l + 1 - p) / 2;
+    nchp = (nlp + 63) / 64;
+  }
+};
+
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, const InvSet s, const TcTables t,
+                                                           const unsigned char* __restrict__ bimg, int nct) {
+  constexpr int NT = VEC ? 2 : 1;
+  constexpr int NC = VEC ? 64 : 128;
+  constexpr int NA = VEC ? 3 : 4;
+  constexpr int NB = 2;
+  constexpr int BT = NC * 128;
+  constexpr int ASZ = NT * 16384;
+  constexpr int BSZ = 3 * BT;
+  constexpr uint32_t ACC = NT * 2 * NC;  // one accumulator set (256 columns)
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[2], acc_empty[2], fin;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_fail;
+  unsigned char* base = align1k(smem_raw);
+  unsigned char* sA = base;
+  unsigned char* sB = sA + NA * ASZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int npair = s.nf * s.nlev;
+  const int ncplx = npair * (VEC ? 2 : 1);
+  const int ntiles = nct * t.ntt * 2 * g.n_m;
+
+  if (tid == 0) {
+    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], 1); }
+    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
+    for (int i = 0; i < 2; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
+    tc::mbar_init(&fin, 1);
+    s_fail = 0;
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_base, 512);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  bool ok = true;
+  InvTile T;
+
+  if (warp == 0) {
+    if (lane == 0) {  // ---------------------------------------- loader
+      uint32_t a_use = 0, b_use = 0;
+      for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+        T.decode(g, t, nct, ix);
+        if (T.nlp == 0 || T.ct * (NC / 2) >= ncplx) continue;
+        for (int c = 0; c < T.nchp && ok; ++c) {
+          const uint32_t bslot = b_use % NB;
+          if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
+          tc::mbar_expect_tx(&b_full[bslot], BSZ);
+          tc::bulk_g2s(sB + bslot * BSZ, bimg + ((t.bpc0[T.mc] + T.p * T.nch + c) * nct + T.ct) * (long long)BSZ,
+                       BSZ, &b_full[bslot]);
+          ++b_use;
+          for (int sp = 0; sp < 3; ++sp, ++a_use) {
+            const uint32_t slot = a_use % NA;
+            if (!wait_empty(&a_empty[slot], a_use, NA)) { ok = false; break; }
+            tc::mbar_expect_tx(&a_full[slot], ASZ);
+            for (int tb = 0; tb < NT; ++tb) {
+              const long long blk =
+                  t.inv_blk0[T.mc] + ((((long long)T.tt * 2 + tb) * 2 + T.p) * T.nch + c) * 3 + sp;
+              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.inv_img + blk * 16384, 16384, &a_full[slot]);
+            }
+          }
+        }
+      }
+      drain_copies<NA>(a_full, a_use);
+      drain_copies<NB>(b_full, b_use);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // ---------------------------------------- MMA issuer
+      uint32_t a_use = 0, b_use = 0, acc_use = 0;
+      for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+        T.decode(g, t, nct, ix);
+        if (T.nlp == 0 || T.ct * (NC / 2) >= ncplx) continue;
+        const uint32_t abuf = acc_use & 1u;
+        if (!wait_empty(&acc_empty[abuf], acc_use, 2)) { ok = false; break; }
+        tc::tc_fence_after();
+        const uint32_t acc = tmem + abuf * ACC;
+        for (int c = 0; c < T.nchp && ok; ++c, ++b_use) {
+          const uint32_t bslot = b_use % NB;
+          if (!wait_full(&b_full[bslot], b_use, NB)) { ok = false; break; }
+          for (int sp = 0; sp < 3; ++sp, ++a_use) {
+            const uint32_t slot = a_use % NA;
+            if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
+            tc::tc_fence_after();
+            issue_split<NT, NC>(acc, sA + slot * ASZ, sB + bslot * BSZ, sp, c == 0, 0);
+            tc::mma_commit(&a_empty[slot]);
+          }
+          tc::mma_commit(&b_empty[bslot]);
+        }
+        tc::mma_commit(&acc_full[abuf]);
+        ++acc_use;
+      }
+      // every MMA issued above has finished before tensor memory is released
+      tc::mma_commit(&fin);
+      if (!tc::mbar_wait(&fin, 0)) ok = false;
+    }
+  } else {  // ------------------------------------------------------ epilogue
+    const int q4 = warp & 3, half = (warp - 2) >> 2;
+    const int jl = 32 * q4 + lane;
+    const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
+    const int NHP = t.ntt * 128;
+    uint32_t acc_use = 0;
+    for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+      T.decode(g, t, nct, ix);
+      if (T.ct * (NC / 2) >= ncplx) continue;
+      const int jg = T.tt * 128 + jl;
+      const long long per_p = VEC ? 2LL * g.nh : (long long)g.nh;
+      auto optr = [&](void* bp, int r, int f, int ef) -> float2* {
+        return (float2*)bp + (long long)r * s.f[f].out_ld + ((long long)T.mc * 2 + T.p) * per_p +
+               (long long)ef * g.nh + jg;
+      };
+      if (T.nlp == 0) {  // odd parity of m = l_max: zeros
+        if (jg < g.nh)
+          for (int q = half * (NC / 4); q < (half + 1) * (NC / 4); ++q) {
+            const int cq = T.ct * (NC / 2) + q;
+            if (cq >= ncplx) break;
+            if (!VEC) {
+              const int r = cq / s.nf, f = cq - r * s.nf;
+              *optr(s.f[f].out0, r, f, 0) = make_float2(0.f, 0.f);
+            } else if ((cq & 1) == 0) {
+              const int pr = cq >> 1, r = pr / s.nf, f = pr - r * s.nf;
+              for (int ef = 0; ef < 2; ++ef) {
+                *optr(s.f[f].out0, r, f, ef) = make_float2(0.f, 0.f);
+                *optr(s.f[f].out1, r, f, ef) = make_float2(0.f, 0.f);
+              }
+            }
+          }
+        continue;
+      }
+      const uint32_t abuf = acc_use & 1u;
+      if (!wait_full(&acc_full[abuf], acc_use, 2)) { ok = false; break; }
+      tc::tc_fence_after();
+      const uint32_t acc = tmem + abuf * ACC + lane_off;
+      const float sP = t.inv_scale[(size_t)T.mc * NHP + jg];
+      const float sdP = VEC ? t.inv_scale[((size_t)g.n_m + T.mc) * NHP + jg] : 0.f;
+      const float dm = (float)(T.mc * g.minc);
+      for (int cc0 = half * (NC / 2); cc0 < (half + 1) * (NC / 2); cc0 += 32) {
+        float P[32], X[32];
+        tc::tmem_ld32(acc + 0 * NC + cc0, P);
+        tc::tmem_ld32(acc + 1 * NC + cc0, X);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) P[i] = (P[i] + X[i]) * sP;
+        if (!VEC) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int cq = T.ct * (NC / 2) + cc0 / 2 + q;
+            if (cq >= ncplx || jg >= g.nh) continue;
+            const int r = cq / s.nf, f = cq - r * s.nf;
+            *optr(s.f[f].out0, r, f, 0) = make_float2(P[2 * q], P[2 * q + 1]);
+          }
+        } else {
+          float D[32];
+          tc::tmem_ld32(acc + 2 * NC + cc0, D);
+          tc::tmem_ld32(acc + 3 * NC + cc0, X);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) D[i] = (D[i] + X[i]) * sdP;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int pr = T.ct * (NC / 4) + cc0 / 4 + q;
+            if (pr >= npair || jg >= g.nh) continue;
+            const int r = pr / s.nf, f = pr - r * s.nf;
+            // C = sum S P, B = sum T P; A = sum S dP, D = sum T dP
+            const float Cr = P[4 * q], Ci = P[4 * q + 1], Br = P[4 * q + 2], Bi = P[4 * q + 3];
+            const float Ar = D[4 * q], Ai = D[4 * q + 1], Dr = D[4 * q + 2], Di = D[4 * q + 3];
+            // v_theta: U = i m B, W = A;   v_phi: U = i m C, W = -D
+            const float2 Ut = make_float2(-dm * Bi, dm * Br), Wt = make_float2(Ar, Ai);
+            const float2 Up = make_float2(-dm * Ci, dm * Cr), Wp = make_float2(-Dr, -Di);
+            *optr(s.f[f].out0, r, f, 0) = make_float2(Ut.x + Wt.x, Ut.y + Wt.y);
+            *optr(s.f[f].out0, r, f, 1) = make_float2(Ut.x - Wt.x, Ut.y - Wt.y);
+            *optr(s.f[f].out1, r, f, 0) = make_float2(Up.x + Wp.x, Up.y + Wp.y);
+            *optr(s.f[f].out1, r, f, 1) = make_float2(Up.x - Wp.x, Up.y - Wp.y);
+          }
+        }
+      }
+      tc::tc_fence_before();
+      tc::mbar_arrive(&acc_empty[abuf]);
+      ++acc_use;
+    }
+  }
+  if (!ok) atomicExch(&s_fail, 1);
+  tc::tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+// ------------------------------------------------------------ analysis
+struct FwdTile {
+  int mc, p, lt, ct, nlp;
+  __device__ void decode(const ShtGeom& g, const TcTables& t, int nct, int ix) {
+    ct = ix % nct;
+    int rest = ix / nct;
+    lt = rest % t.nlt;
+    rest /= t.nlt;
+    p = rest & 1;
+    mc = rest >> 1;
+    const int n_l = g.l_max - mc * g.minc + 1;
+    nlp = (n_l + 1 - p) / 2;
+  }
+};
+
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, const FwdSet s, const TcTables t,
+                                                           const unsigned char* __restrict__ bimg, int nct) {
+  constexpr int NT = VEC ? 2 : 1;
+  constexpr int NC = VEC ? 64 : 128;
+  constexpr int NA = VEC ? 3 : 4;
+  constexpr int NB = 2;
+  constexpr int BT = NC * 128;
+  constexpr int TS = 3 * BT;        // one data operand (3 splits)
+  constexpr int ASZ = NT * 16384;
+  constexpr int BSZ = NT * TS;      // mine (and other)
+  constexpr uint32_t ACC = NT * 2 * NC;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[2], acc_empty[2], fin;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_fail;
+  unsigned char* base = align1k(smem_raw);
+  unsigned char* sA = base;
+  unsigned char* sB = sA + NA * ASZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int npair = s.nf * s.nlev;
+  const int ncplx = npair * (VEC ? 2 : 1);
+  const int ntiles = nct * t.nlt * 2 * g.n_m;
+
+  if (tid == 0) {
+    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], 1); }
+    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
+    for (int i = 0; i < 2; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
+    tc::mbar_init(&fin, 1);
+    s_fail = 0;
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_base, 512);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  bool ok = true;
+  FwdTile T;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t a_use = 0, b_use = 0;
+      for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+        T.decode(g, t, nct, ix);
+        if (T.lt * 128 >= T.nlp || T.ct * (NC / 2) >= ncplx) continue;
+        for (int c = 0; c < t.ncj && ok; ++c) {
+          const uint32_t bslot = b_use % NB;
+          if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
+          tc::mbar_expect_tx(&b_full[bslot], BSZ);
+          const unsigned char* img = bimg + (((long long)T.mc * t.ncj + c) * nct + T.ct) * (2LL * TS);
+          tc::bulk_g2s(sB + bslot * BSZ, img + T.p * TS, TS, &b_full[bslot]);              // mine
+          if (VEC) tc::bulk_g2s(sB + bslot * BSZ + TS, img + (1 - T.p) * TS, TS, &b_full[bslot]);  // other
+          ++b_use;
+          for (int sp = 0; sp < 3; ++sp, ++a_use) {
+            const uint32_t slot = a_use % NA;
+            if (!wait_empty(&a_empty[slot], a_use, NA)) { ok = false; break; }
+            tc::mbar_expect_tx(&a_full[slot], ASZ);
+            for (int tb = 0; tb < NT; ++tb) {
+              const long long blk =
+                  t.fwd_blk0[T.mc] + ((((long long)T.p * t.nlt + T.lt) * 2 + tb) * t.ncj + c) * 3 + sp;
+              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.fwd_img + blk * 16384, 16384, &a_full[slot]);
+            }
+          }
+        }
+      }
+      drain_copies<NA>(a_full, a_use);
+      drain_copies<NB>(b_full, b_use);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      uint32_t a_use = 0, b_use = 0, acc_use = 0;
+      for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+        T.decode(g, t, nct, ix);
+        if (T.lt * 128 >= T.nlp || T.ct * (NC / 2) >= ncplx) continue;
+        const uint32_t abuf = acc_use & 1u;
+        if (!wait_empty(&acc_empty[abuf], acc_use, 2)) { ok = false; break; }
+        tc::tc_fence_after();
+        const uint32_t acc = tmem + abuf * ACC;
+        for (int c = 0; c < t.ncj && ok; ++c, ++b_use) {
+          const uint32_t bslot = b_use % NB;
+          if (!wait_full(&b_full[bslot], b_use, NB)) { ok = false; break; }
+          for (int sp = 0; sp < 3; ++sp, ++a_use) {
+            const uint32_t slot = a_use % NA;
+            if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
+            tc::tc_fence_after();
+            issue_split<NT, NC>(acc, sA + slot * ASZ, sB + bslot * BSZ, sp, c == 0, TS);
+            tc::mma_commit(&a_empty[slot]);
+          }
+          tc::mma_commit(&b_empty[bslot]);
+        }
+        tc::mma_commit(&acc_full[abuf]);
+        ++acc_use;
+      }
+      tc::mma_commit(&fin);
+      if (!tc::mbar_wait(&fin, 0)) ok = false;
+    }
+  } else {
+    const int q4 = warp & 3, half = (warp - 2) >> 2;
+    const int lr = 32 * q4 + lane;
+    const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
+    uint32_t acc_use = 0;
+    for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+      T.decode(g, t, nct, ix);
+      if (T.lt * 128 >= T.nlp || T.ct * (NC / 2) >= ncplx) continue;
+      const uint32_t abuf = acc_use & 1u;
+      if (!wait_full(&acc_full[abuf], acc_use, 2)) { ok = false; break; }
+      tc::tc_fence_after();
+      const uint32_t acc = tmem + abuf * ACC + lane_off;
+      const int m = T.mc * g.minc;
+      const int lp = T.lt * 128 + lr;
+      const int l = m + T.p + 2 * lp;
+      const bool valid = lp < T.nlp;
+      const int lm = g.lmoff[T.mc] + l - m;
+      const float sP = valid ? t.fwd_scale[lm] : 0.f;
+      const float sdP = (VEC && valid) ? t.fwd_scale[(size_t)g.lm_max + lm] : 0.f;
+      const float dm = (float)m;
+      const float inv_ll = l > 0 ? 1.0f / (float)(l * (l + 1)) : 1.0f;
+      for (int cc0 = half * (NC / 2); cc0 < (half + 1) * (NC / 2); cc0 += 32) {
+        float D0[32], X[32];
+        tc::tmem_ld32(acc + 0 * NC + cc0, D0);
+        tc::tmem_ld32(acc + 1 * NC + cc0, X);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) D0[i] = (D0[i] + X[i]) * sP;
+        if (!VEC) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int cq = T.ct * (NC / 2) + cc0 / 2 + q;
+            if (cq >= ncplx || !valid) continue;
+            const int r = cq / s.nf, f = cq - r * s.nf;
+            const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+            const double2 v = (l <= lc) ? make_double2(f2d_int(D0[2 * q]), f2d_int(D0[2 * q + 1]))
+                                        : make_double2(0.0, 0.0);
+            s.f[f].out0[(long long)r * s.f[f].out_ld + lm] = v;
+          }
+        } else {
+          float D1[32];
+          tc::tmem_ld32(acc + 2 * NC + cc0, D1);
+          tc::tmem_ld32(acc + 3 * NC + cc0, X);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) D1[i] = (D1[i] + X[i]) * sdP;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int pr = T.ct * (NC / 4) + cc0 / 4 + q;
+            if (pr >= npair || !valid) continue;
+            const int r = pr / s.nf, f = pr - r * s.nf;
+            const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+            // A = sum F1_mine P, D = sum F2_mine P, C = sum F1_other dP, B = sum F2_other dP
+            const float Ar = D0[4 * q], Ai = D0[4 * q + 1], Dr = D0[4 * q + 2], Di = D0[4 * q + 3];
+            const float Cr = D1[4 * q], Ci = D1[4 * q + 1], Br = D1[4 * q + 2], Bi = D1[4 * q + 3];
+            double2 Sv = make_double2(f2d_int((dm * Ai + Br) * inv_ll), f2d_int((-dm * Ar + Bi) * inv_ll));
+            double2 Tv = make_double2(f2d_int((-Cr + dm * Di) * inv_ll), f2d_int((-Ci - dm * Dr) * inv_ll));
+            if (l > lc) { Sv = make_double2(0.0, 0.0); Tv = Sv; }
+            const long long o = (long long)r * s.f[f].out_ld + lm;
+            s.f[f].out0[o] = Sv;
+            s.f[f].out1[o] = Tv;
+          }
+        }
+      }
+      tc::tc_fence_before();
+      tc::mbar_arrive(&acc_empty[abuf]);
+      ++acc_use;
+    }
+  }
+  if (!ok) atomicExch(&s_fail, 1);
+  tc::tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 148;
+  }
+  return n;
+}
+
+template <bool VEC>
+cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, unsigned char* bimg,
+                         cudaStream_t st) {
+  constexpr int NT = VEC ? 2 : 1, NC = VEC ? 64 : 128, NA = VEC ? 3 : 4;
+  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
+  if (ncplx <= 0) return cudaSuccess;
+  const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
+  const size_t psmem = 1024 + 2 * 3 * (size_t)NC * 128;
+  CUDA_TRY(cudaFuncSetAttribute(pack_inv_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  pack_inv_kernel<VEC><<<dim3(nct, g.n_m), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  CUDA_TRY(cudaGetLastError());
+  const size_t smem = 1024 + (size_t)NA * NT * 16384 + 2 * 3 * (size_t)NC * 128;
+  CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
+  const int grid = (int)std::min<long long>(ntiles, num_sms());
+  inv_leg_tcp<VEC><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
+  return cudaGetLastError();
+}
+
+template <bool VEC>
+cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, unsigned char* bimg,
+                         cudaStream_t st) {
+  constexpr int NT = VEC ? 2 : 1, NC = VEC ? 64 : 128, NA = VEC ? 3 : 4;
+  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
+  if (ncplx <= 0) return cudaSuccess;
+  const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
+  const size_t psmem = 1024 + 2 * 2 * 3 * (size_t)NC * 128;
+  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  pack_fwd_kernel<VEC><<<dim3(nct, g.n_m), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  CUDA_TRY(cudaGetLastError());
+  const size_t smem = 1024 + (size_t)NA * NT * 16384 + 2 * (size_t)NT * 3 * NC * 128;
+  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
+  const int grid = (int)std::min<long long>(ntiles, num_sms());
+  fwd_leg_tcp<VEC><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t tcp_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool vec, bool inverse) {
+  const int NC = vec ? 64 : 128;
+  const long long nct = (ncplx + NC / 2 - 1) / (NC / 2);
+  const long long tile = 3LL * NC * 128;
+  if (inverse) return (size_t)(t.npc * nct * tile);
+  return (size_t)((long long)g.n_m * t.ncj * nct * 2 * tile);
+}
+
+cudaError_t launch_inv_legendre_tcp(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
+                                    unsigned char* bimg, cudaStream_t st) {
+  return vec ? launch_inv_p<true>(g, s, t, bimg, st) : launch_inv_p<false>(g, s, t, bimg, st);
+}
+
+cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
+                                    unsigned char* bimg, cudaStream_t st) {
+  return vec ? launch_fwd_p<true>(g, s, t, bimg, st) : launch_fwd_p<false>(g, s, t, bimg, st);
+}

@@ -2,10 +2,13 @@
 // pointer staging, the public names of MagIC's `module sht`
 // (src/sht_native.f90:16-20) and the batched radial-loop transform set
 // (src/rIter.f90:466-712).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -65,12 +68,21 @@ struct magic_sht_handle {
   unsigned char* d_fwd_img = nullptr;
   long long* d_inv_blk0 = nullptr;
   long long* d_fwd_blk0 = nullptr;
+  long long* d_bpc0 = nullptr;
+  unsigned char* d_bimg = nullptr;  // data-operand images of the persistent tensor-core kernels
+  size_t bimg_bytes = 0;
   float* d_inv_scale = nullptr;
   float* d_fwd_scale = nullptr;
   int* d_err = nullptr;
+  bool tc_persistent = true;  // MAGIC_SHT_TC_KERNEL=tiled selects the one-tile-per-CTA kernels
   char* ws = nullptr;
   size_t ws_bytes = 0;
   std::vector<int> lmoff;
+  // host-buffer pipeline of the batched calls: two staging slots, two copy streams
+  char* stage = nullptr;
+  size_t stage_bytes = 0;
+  cudaStream_t cpy_in = nullptr, cpy_out = nullptr;
+  cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
   // per-phase CUDA-event timing (magic_sht_set_profiling)
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -150,6 +162,43 @@ size_t hs_bytes(const magic_sht_handle* h, int nlev) {
 // Synthesis half spectra of a vector component in the tensor-core form hold
 // E and F for both parities: twice the entries of the N/S layout.
 bool tc_form(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_BF16X3; }
+// data-operand images of the persistent tensor-core kernels (grown like the workspace)
+int ensure_bimg(magic_sht_handle* h, size_t bytes) {
+  if (bytes <= h->bimg_bytes) return MAGIC_SHT_OK;
+  if (h->capturing)
+    return set_err(MAGIC_SHT_ERR_NOMEM,
+                   "tensor-core data images of %zu bytes needed during graph capture; call "
+                   "magic_sht_reserve first",
+                   bytes);
+  if (h->d_bimg) {
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaFree(h->d_bimg));
+    h->d_bimg = nullptr;
+    h->bimg_bytes = 0;
+  }
+  const size_t nb = align256(bytes);
+  CK(cudaMalloc((void**)&h->d_bimg, nb));
+  h->bimg_bytes = nb;
+  return MAGIC_SHT_OK;
+}
+int inv_tc(magic_sht_handle* h, const ShtGeom& g, const InvSet& s, bool vec) {
+  if (!h->tc_persistent) {
+    CK(launch_inv_legendre_tc(g, s, vec, h->tct, h->stream));
+    return MAGIC_SHT_OK;
+  }
+  TRY(ensure_bimg(h, tcp_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), vec, true)));
+  CK(launch_inv_legendre_tcp(g, s, vec, h->tct, h->d_bimg, h->stream));
+  return MAGIC_SHT_OK;
+}
+int fwd_tc(magic_sht_handle* h, const ShtGeom& g, const FwdSet& s, bool vec) {
+  if (!h->tc_persistent) {
+    CK(launch_fwd_legendre_tc(g, s, vec, h->tct, h->stream));
+    return MAGIC_SHT_OK;
+  }
+  TRY(ensure_bimg(h, tcp_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), vec, false)));
+  CK(launch_fwd_legendre_tcp(g, s, vec, h->tct, h->d_bimg, h->stream));
+  return MAGIC_SHT_OK;
+}
 size_t hs_inv_bytes(const magic_sht_handle* h, int nlev, bool vec) {
   return hs_bytes(h, nlev) * ((vec && tc_form(h)) ? 2 : 1);
 }
@@ -354,7 +403,7 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = cx.dev(hs_sc[i]); f.out1 = nullptr; f.out_ld = hs_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_SCALAR);
-    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, false, h->tct, h->stream));
+    if (h->precision == MAGIC_SHT_BF16X3) TRY(inv_tc(h, g, s, false));
     else CK(launch_inv_legendre_simt(g, s, false, f64, h->stream));
   }
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
@@ -367,7 +416,7 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = cx.dev(hs_vc[2 * i]); f.out1 = cx.dev(hs_vc[2 * i + 1]); f.out_ld = hs_ld_v;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_VECTOR);
-    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, true, h->tct, h->stream));
+    if (h->precision == MAGIC_SHT_BF16X3) TRY(inv_tc(h, g, s, true));
     else CK(launch_inv_legendre_simt(g, s, true, f64, h->stream));
   }
   for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
@@ -418,7 +467,7 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = (double2*)cx.dev(sc[i].out); f.out1 = nullptr; f.out_ld = lv.spec_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_SCALAR);
-    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_fwd_legendre_tc(g, s, false, h->tct, h->stream));
+    if (h->precision == MAGIC_SHT_BF16X3) TRY(fwd_tc(h, g, s, false));
     else CK(launch_fwd_legendre_simt(g, s, false, f64, h->stream));
   }
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
@@ -432,7 +481,7 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out_ld = lv.spec_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_VECTOR);
-    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_fwd_legendre_tc(g, s, true, h->tct, h->stream));
+    if (h->precision == MAGIC_SHT_BF16X3) TRY(fwd_tc(h, g, s, true));
     else CK(launch_fwd_legendre_simt(g, s, true, f64, h->stream));
   }
   return MAGIC_SHT_OK;
@@ -654,6 +703,8 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   if (h->precision == MAGIC_SHT_BF16X3) {
     if (prop.major != 10)
       return fail(set_err(MAGIC_SHT_ERR_UNSUPPORTED, "the tensor-core form needs tcgen05 (sm_10x)"));
+    const char* kern = getenv("MAGIC_SHT_TC_KERNEL");
+    h->tc_persistent = !(kern && strcmp(kern, "tiled") == 0);
     TcTables& t = h->tct;
     std::vector<long long> ib, fb;
     long long ninv = 0, nfwd = 0;
@@ -666,6 +717,15 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     INIT_CK(cudaMalloc((void**)&h->d_fwd_scale, sizeof(float) * 2 * (size_t)K));
     INIT_CK(cudaMemcpy(h->d_inv_blk0, ib.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
     INIT_CK(cudaMemcpy(h->d_fwd_blk0, fb.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
+    std::vector<long long> pc(n_m);
+    t.npc = 0;
+    for (int mc = 0; mc < n_m; ++mc) {
+      pc[mc] = t.npc;
+      t.npc += 2LL * tc_nch(L - mc * minc + 1);
+    }
+    INIT_CK(cudaMalloc((void**)&h->d_bpc0, sizeof(long long) * n_m));
+    INIT_CK(cudaMemcpy(h->d_bpc0, pc.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
+    t.bpc0 = h->d_bpc0;
     INIT_CK(cudaMemset(h->d_fwd_scale, 0, sizeof(float) * 2 * (size_t)K));
     t.inv_img = h->d_inv_img; t.fwd_img = h->d_fwd_img;
     t.inv_blk0 = h->d_inv_blk0; t.fwd_blk0 = h->d_fwd_blk0;
@@ -685,9 +745,18 @@ int magic_sht_finalize(magic_sht_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ptrs[] = {h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP, h->d_wgt, h->d_osin2,
                   h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws, h->d_inv_img, h->d_fwd_img,
-                  h->d_inv_blk0, h->d_fwd_blk0, h->d_inv_scale, h->d_fwd_scale, h->d_err};
+                  h->d_inv_blk0, h->d_fwd_blk0, h->d_inv_scale, h->d_fwd_scale, h->d_err,
+                  h->d_bpc0, h->d_bimg};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  if (h->stage) cudaFree(h->stage);
+  for (int i = 0; i < 2; ++i) {
+    if (h->ev_in[i]) cudaEventDestroy(h->ev_in[i]);
+    if (h->ev_comp[i]) cudaEventDestroy(h->ev_comp[i]);
+    if (h->ev_out[i]) cudaEventDestroy(h->ev_out[i]);
+  }
+  if (h->cpy_in) cudaStreamDestroy(h->cpy_in);
+  if (h->cpy_out) cudaStreamDestroy(h->cpy_out);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return MAGIC_SHT_OK;
@@ -744,7 +813,18 @@ int magic_sht_reserve(magic_sht_handle* h, int n) {
   // the radial set needs 15 inverse half spectra (the forward set needs 10)
   // plus per-level lcut/or2 staging
   const size_t need = (tc_form(h) ? 23 : 15) * align256(hs_bytes(h, n)) + 4 * align256((size_t)n * 8) + 4096;
-  return ensure_ws(h, need);
+  TRY(ensure_ws(h, need));
+  if (tc_form(h) && h->tc_persistent) {
+    // data images of the radial set's largest tensor-core launch (7 scalar + 4 vector
+    // syntheses, 1 scalar + 3 vector analyses per level)
+    const ShtGeom& g = h->g;
+    size_t b = tcp_data_bytes(g, h->tct, 7 * n, false, true);
+    b = std::max(b, tcp_data_bytes(g, h->tct, 4 * n * 2, true, true));
+    b = std::max(b, tcp_data_bytes(g, h->tct, n, false, false));
+    b = std::max(b, tcp_data_bytes(g, h->tct, 3 * n * 2, true, false));
+    TRY(ensure_bimg(h, b));
+  }
+  return MAGIC_SHT_OK;
 }
 
 // ----------------------------------------------------- single-level facade
@@ -955,6 +1035,87 @@ int magic_sht_spat_to_sphertor(magic_sht_handle* h, const double* f, const doubl
                         std::vector<VectorFwd>& vc) { vc.push_back({g[0], g[1], s[0], s[1]}); });
 }
 
+// ------------------------------------------- host-buffer level pipeline
+// Batched calls with host arrays run in chunks of levels: chunk c is copied in
+// on one copy stream, transformed on the handle's stream and copied out on a
+// second copy stream, through two device staging slots, so that copies in
+// both directions overlap each other and the kernels.
+struct PipeArray {
+  const void* host;   // level 0 of the host array
+  size_t lds;         // bytes between levels
+  size_t last;        // bytes of one level
+  bool out;
+  size_t slot_off;    // offset in a staging slot
+};
+
+static int pipelined_levels(magic_sht_handle* h, int n, int chunk, std::vector<PipeArray>& arrs,
+                            const std::function<int(int, int, const std::vector<char*>&)>& compute) {
+  size_t slot = 0;
+  for (auto& a : arrs) {
+    a.slot_off = slot;
+    slot += align256((size_t)(chunk - 1) * a.lds + a.last);
+  }
+  if (2 * slot > h->stage_bytes) {
+    CK(cudaDeviceSynchronize());
+    if (h->stage) CK(cudaFree(h->stage));
+    h->stage = nullptr;
+    h->stage_bytes = 0;
+    CK(cudaMalloc((void**)&h->stage, 2 * slot));
+    h->stage_bytes = 2 * slot;
+  }
+  if (!h->cpy_in) {
+    CK(cudaStreamCreateWithFlags(&h->cpy_in, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&h->cpy_out, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+      CK(cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&h->ev_comp[i], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&h->ev_out[i], cudaEventDisableTiming));
+    }
+  }
+  // start after everything already queued on the handle's stream
+  CK(cudaEventRecord(h->ev_comp[1], h->stream));
+  CK(cudaStreamWaitEvent(h->cpy_in, h->ev_comp[1], 0));
+  CK(cudaStreamWaitEvent(h->cpy_out, h->ev_comp[1], 0));
+  const int nchunks = (n + chunk - 1) / chunk;
+  for (int c = 0; c < nchunks; ++c) {
+    const int sl = c & 1, r0 = c * chunk, nr = std::min(chunk, n - r0);
+    char* base = h->stage + (size_t)sl * slot;
+    if (c >= 2) CK(cudaStreamWaitEvent(h->cpy_in, h->ev_out[sl], 0));  // slot drained
+    std::vector<char*> dev(arrs.size());
+    for (size_t i = 0; i < arrs.size(); ++i) {
+      const PipeArray& a = arrs[i];
+      dev[i] = base + a.slot_off;
+      if (!a.out)
+        CK(cudaMemcpyAsync(dev[i], (const char*)a.host + (size_t)r0 * a.lds, (size_t)(nr - 1) * a.lds + a.last,
+                           cudaMemcpyHostToDevice, h->cpy_in));
+    }
+    CK(cudaEventRecord(h->ev_in[sl], h->cpy_in));
+    CK(cudaStreamWaitEvent(h->stream, h->ev_in[sl], 0));
+    if (c >= 2) CK(cudaStreamWaitEvent(h->stream, h->ev_out[sl], 0));  // outputs of c-2 copied
+    TRY(compute(r0, nr, dev));
+    CK(cudaEventRecord(h->ev_comp[sl], h->stream));
+    CK(cudaStreamWaitEvent(h->cpy_out, h->ev_comp[sl], 0));
+    for (size_t i = 0; i < arrs.size(); ++i) {
+      const PipeArray& a = arrs[i];
+      if (a.out)
+        CK(cudaMemcpyAsync((char*)a.host + (size_t)r0 * a.lds, dev[i], (size_t)(nr - 1) * a.lds + a.last,
+                           cudaMemcpyDeviceToHost, h->cpy_out));
+    }
+    CK(cudaEventRecord(h->ev_out[sl], h->cpy_out));
+  }
+  CK(cudaStreamSynchronize(h->cpy_out));
+  CK(cudaStreamSynchronize(h->stream));
+  return MAGIC_SHT_OK;
+}
+
+static bool any_host(std::initializer_list<const void*> ptrs) {
+  for (const void* p : ptrs)
+    if (p && !is_device_ptr(p)) return true;
+  return false;
+}
+
+static const int kPipeChunk = 8;  // radial levels per pipeline chunk
+
 // ------------------------------------------------------ radial-loop sets
 static int level_ctl(magic_sht_handle* h, CallCtx& cx, int n, const int* lcut, const double* or2,
                      LevelCtl& lv, std::vector<int>& lcut_copy) {
@@ -983,6 +1144,43 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
   if (a->spec_ld < g.lm_max || a->grid_ld < (long long)g.n_phi * g.ld)
     return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
   DeviceGuard dg(h->device);
+  if (n > kPipeChunk && !h->capturing &&
+      any_host({a->s, a->p, a->xi, a->w, a->dw, a->ddw, a->z, a->dz, a->b, a->db, a->ddb, a->aj, a->dj,
+                a->sc, a->pc, a->xic, a->vrc, a->vtc, a->vpc, a->cvrc, a->cvtc, a->cvpc, a->brc, a->btc,
+                a->bpc, a->cbrc, a->cbtc, a->cbpc})) {
+    if (lcut)
+      for (int i = 0; i < n; ++i)
+        if (!is_device_ptr(lcut) && (lcut[i] < 0 || lcut[i] > g.l_max))
+          return set_err(MAGIC_SHT_ERR_LCUT, "lcut[%d]=%d outside [0, %d]", i, lcut[i], g.l_max);
+    const double* const ins[13] = {a->s, a->p, a->xi, a->w, a->dw, a->ddw, a->z, a->dz,
+                                   a->b, a->db, a->ddb, a->aj, a->dj};
+    double* const outs[15] = {a->sc, a->pc, a->xic, a->vrc, a->vtc, a->vpc, a->cvrc, a->cvtc,
+                              a->cvpc, a->brc, a->btc, a->bpc, a->cbrc, a->cbtc, a->cbpc};
+    std::vector<PipeArray> arrs;
+    std::vector<int> idx_in(13, -1), idx_out(15, -1);
+    const size_t sb = (size_t)a->spec_ld * 16, gb = (size_t)a->grid_ld * 8;
+    for (int i = 0; i < 13; ++i)
+      if (ins[i]) { idx_in[i] = (int)arrs.size(); arrs.push_back({ins[i], sb, (size_t)g.lm_max * 16, false, 0}); }
+    for (int i = 0; i < 15; ++i)
+      if (outs[i]) { idx_out[i] = (int)arrs.size(); arrs.push_back({outs[i], gb, (size_t)g.n_phi * g.ld * 8, true, 0}); }
+    if (or2) arrs.push_back({or2, 8, 8, false, 0});
+    if (lcut) arrs.push_back({lcut, 4, 4, false, 0});
+    const int i_or2 = or2 ? (int)arrs.size() - (lcut ? 2 : 1) : -1;
+    const int i_lc = lcut ? (int)arrs.size() - 1 : -1;
+    return pipelined_levels(h, n, kPipeChunk, arrs, [&](int r0, int nr, const std::vector<char*>& d) {
+      magic_sht_grid_space_args b = *a;
+      double** pin[13] = {(double**)&b.s, (double**)&b.p, (double**)&b.xi, (double**)&b.w, (double**)&b.dw,
+                          (double**)&b.ddw, (double**)&b.z, (double**)&b.dz, (double**)&b.b, (double**)&b.db,
+                          (double**)&b.ddb, (double**)&b.aj, (double**)&b.dj};
+      double** pout[15] = {&b.sc, &b.pc, &b.xic, &b.vrc, &b.vtc, &b.vpc, &b.cvrc, &b.cvtc,
+                           &b.cvpc, &b.brc, &b.btc, &b.bpc, &b.cbrc, &b.cbtc, &b.cbpc};
+      for (int i = 0; i < 13; ++i) *pin[i] = idx_in[i] >= 0 ? (double*)d[idx_in[i]] : nullptr;
+      for (int i = 0; i < 15; ++i) *pout[i] = idx_out[i] >= 0 ? (double*)d[idx_out[i]] : nullptr;
+      (void)r0;
+      return magic_sht_transform_to_grid_space(h, nr, i_or2 >= 0 ? (const double*)d[i_or2] : nullptr,
+                                               i_lc >= 0 ? (const int*)d[i_lc] : nullptr, &b);
+    });
+  }
   CallCtx cx(h);
   LevelCtl lv;
   std::vector<int> lc;
@@ -1044,6 +1242,39 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
   if (a->spec_ld < g.lm_max || a->grid_ld < (long long)g.n_phi * g.ld)
     return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
   DeviceGuard dg(h->device);
+  if (n > kPipeChunk && !h->capturing &&
+      any_host({a->Advr, a->Advt, a->Advp, a->VSr, a->VSt, a->VSp, a->VxBr, a->VxBt, a->VxBp, a->heatTerms,
+                a->AdvrLM, a->AdvtLM, a->AdvpLM, a->VSrLM, a->VStLM, a->VSpLM, a->VxBrLM, a->VxBtLM,
+                a->VxBpLM, a->heatTermsLM})) {
+    if (lcut)
+      for (int i = 0; i < n; ++i)
+        if (!is_device_ptr(lcut) && (lcut[i] < 0 || lcut[i] > g.l_max))
+          return set_err(MAGIC_SHT_ERR_LCUT, "lcut[%d]=%d outside [0, %d]", i, lcut[i], g.l_max);
+    const double* const ins[10] = {a->Advr, a->Advt, a->Advp, a->VSr, a->VSt, a->VSp,
+                                   a->VxBr, a->VxBt, a->VxBp, a->heatTerms};
+    double* const outs[10] = {a->AdvrLM, a->AdvtLM, a->AdvpLM, a->VSrLM, a->VStLM,
+                              a->VSpLM, a->VxBrLM, a->VxBtLM, a->VxBpLM, a->heatTermsLM};
+    std::vector<PipeArray> arrs;
+    std::vector<int> idx_in(10, -1), idx_out(10, -1);
+    const size_t sb = (size_t)a->spec_ld * 16, gb = (size_t)a->grid_ld * 8;
+    for (int i = 0; i < 10; ++i)
+      if (ins[i]) { idx_in[i] = (int)arrs.size(); arrs.push_back({ins[i], gb, (size_t)g.n_phi * g.ld * 8, false, 0}); }
+    for (int i = 0; i < 10; ++i)
+      if (outs[i]) { idx_out[i] = (int)arrs.size(); arrs.push_back({outs[i], sb, (size_t)g.lm_max * 16, true, 0}); }
+    if (lcut) arrs.push_back({lcut, 4, 4, false, 0});
+    const int i_lc = lcut ? (int)arrs.size() - 1 : -1;
+    return pipelined_levels(h, n, kPipeChunk, arrs, [&](int r0, int nr, const std::vector<char*>& d) {
+      magic_sht_lm_space_args b = *a;
+      const double** pin[10] = {&b.Advr, &b.Advt, &b.Advp, &b.VSr, &b.VSt, &b.VSp, &b.VxBr, &b.VxBt,
+                                &b.VxBp, &b.heatTerms};
+      double** pout[10] = {&b.AdvrLM, &b.AdvtLM, &b.AdvpLM, &b.VSrLM, &b.VStLM, &b.VSpLM, &b.VxBrLM,
+                           &b.VxBtLM, &b.VxBpLM, &b.heatTermsLM};
+      for (int i = 0; i < 10; ++i) *pin[i] = idx_in[i] >= 0 ? (const double*)d[idx_in[i]] : nullptr;
+      for (int i = 0; i < 10; ++i) *pout[i] = idx_out[i] >= 0 ? (double*)d[idx_out[i]] : nullptr;
+      (void)r0;
+      return magic_sht_transform_to_lm_space(h, nr, i_lc >= 0 ? (const int*)d[i_lc] : nullptr, &b);
+    });
+  }
   CallCtx cx(h);
   LevelCtl lv;
   std::vector<int> lc;
@@ -1314,6 +1545,7 @@ extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double*
   s.f[0].out0 = scratch;
   s.f[0].out1 = nullptr;
   s.f[0].out_ld = hs_ld;
+  // the one-tile-per-CTA tensor-core kernel needs no data-image buffer
   if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, false, h->tct, h->stream));
   else CK(launch_inv_legendre_simt(g, s, false, fp64_pipes(h), h->stream));
   FftSet fs{};

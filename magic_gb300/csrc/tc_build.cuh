@@ -1,0 +1,144 @@
+// Builds of the data operand of the tensor-core Legendre sums, shared by
+// the one-tile-per-CTA and the persistent kernels.
+#pragma once
+#include "common.cuh"
+#include "cplx.cuh"
+
+// ---------------------------------------------------------------------------
+// Warp-cooperative builds of a whole data tile (B operand, K = 64 per chunk,
+// rows 2ql / 2ql+1 = real / imaginary part of complex column ql).  A warp
+// takes columns ql0, ql0 + qstride, ... in batches of CB: all global loads of
+// a batch are issued first (lane = k and k + 32; 16-byte loads, consecutive
+// lanes on consecutive entries), then the values are split to 3xBF16 and
+// written with 2-byte stores into the 128-byte-swizzled K-major tiles.
+#include <cuda_bf16.h>
+#include "tc_ptx.cuh"
+
+__device__ __forceinline__ void store_split1(unsigned char* tile0, uint32_t off, float v, uint32_t tile_bytes) {
+  __nv_bfloat16 h, md, lo;
+  tc::split3(v, h, md, lo);
+  *(__nv_bfloat16*)(tile0 + off) = h;
+  *(__nv_bfloat16*)(tile0 + tile_bytes + off) = md;
+  *(__nv_bfloat16*)(tile0 + 2 * tile_bytes + off) = lo;
+}
+
+template <bool VEC, int NC, int CB>
+__device__ __forceinline__ void inv_build_tile(const ShtGeom& g, const InvSet& s, unsigned char* B, int ct,
+                                               int ncplx, int m, int lm0, int p, int c, int ql0, int qstride,
+                                               int lane) {
+  constexpr uint32_t BT = NC * 128;
+  const int lb = p + 128 * c;  // l - m of k = 0
+  const int lmx = g.l_max - m;
+  for (int qb = ql0; qb < NC / 2; qb += CB * qstride) {
+    double2 a[CB][2], b[CB][2];
+    int opk[CB], lc[CB];
+    float o2[CB];
+#pragma unroll
+    for (int i = 0; i < CB; ++i) {
+      const int ql = qb + i * qstride;
+      const int q = ct * (NC / 2) + ql;
+      opk[i] = OP_ZERO;
+      lc[i] = -1;
+      o2[i] = 0.f;
+      if (ql < NC / 2 && q < ncplx) {
+        const int pair = VEC ? (q >> 1) : q;
+        const int r = pair / s.nf, f = pair - r * s.nf;
+        const SpecOperand& op = (VEC && (q & 1)) ? s.f[f].x1 : s.f[f].x0;
+        if (op.op != OP_ZERO && op.A != nullptr) {
+          opk[i] = op.op;
+          const double2* A = op.A + (long long)r * op.ld + lm0;  // indexed by l - m
+#pragma unroll
+          for (int h = 0; h < 2; ++h) a[i][h] = __ldg(A + min(lb + 2 * (lane + 32 * h), lmx));
+          if (op.op == OP_CURLT && op.B != nullptr) {
+            const double2* Bp = op.B + (long long)r * op.ld + lm0;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) b[i][h] = __ldg(Bp + min(lb + 2 * (lane + 32 * h), lmx));
+            o2[i] = d2f_int(s.or2 ? s.or2[r] : s.or2_0);
+          } else if (op.op == OP_CURLT) {
+            opk[i] = OP_ZERO;
+          }
+          lc[i] = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+        }
+      }
+    }
+    const float dm = (float)m;
+#pragma unroll
+    for (int i = 0; i < CB; ++i) {
+      const int ql = qb + i * qstride;
+      if (ql >= NC / 2) break;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = lane + 32 * h;
+        const int l = m + lb + 2 * k;
+        float ar = 0.f, ai = 0.f;
+        if (opk[i] != OP_ZERO) {
+          ar = d2f_int(a[i][h].x);
+          ai = d2f_int(a[i][h].y);
+          const float ll = (float)(l * (l + 1));
+          if (opk[i] == OP_DLH) {
+            ar *= ll;
+            ai *= ll;
+          } else if (opk[i] == OP_CURLT) {
+            const float d = o2[i] * ll;
+            ar = fmaf(d, ar, -d2f_int(b[i][h].x));
+            ai = fmaf(d, ai, -d2f_int(b[i][h].y));
+          } else if (opk[i] == OP_IM) {
+            const float t0 = ar;
+            ar = -dm * ai;
+            ai = dm * t0;
+          }
+          if (l > lc[i]) { ar = 0.f; ai = 0.f; }
+        }
+        store_split1(B, tc::sw128_offset(2 * ql, k), ar, BT);
+        store_split1(B, tc::sw128_offset(2 * ql + 1, k), ai, BT);
+      }
+    }
+  }
+}
+
+// Analysis tile: "mine" at B, "other" at B + 3 tiles (written when BOTH).
+template <bool VEC, int NC, int CB, bool BOTH = VEC>
+__device__ __forceinline__ void fwd_build_tile(const ShtGeom& g, const FwdSet& s, unsigned char* B, int ct,
+                                               int ncplx, int mc, int mine, int c, int ql0, int qstride,
+                                               int lane) {
+  constexpr uint32_t BT = NC * 128;
+  for (int qb = ql0; qb < NC / 2; qb += CB * qstride) {
+    float4 v[CB][2];
+#pragma unroll
+    for (int i = 0; i < CB; ++i) {
+      const int ql = qb + i * qstride;
+      const int q = ct * (NC / 2) + ql;
+      v[i][0] = v[i][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (ql < NC / 2 && q < ncplx) {
+        const int pair = VEC ? (q >> 1) : q;
+        const int r = pair / s.nf, f = pair - r * s.nf;
+        const float4* src = (const float4*)((const float2*)((VEC && (q & 1)) ? s.f[f].in1 : s.f[f].in0) +
+                                            (long long)r * s.f[f].in_ld + (long long)mc * g.nh * 2);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int j = 64 * c + lane + 32 * h;
+          v[i][h] = __ldg(src + min(j, g.nh - 1));  // (ES, EA) at colatitude j
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < CB; ++i) {
+      const int ql = qb + i * qstride;
+      if (ql >= NC / 2) break;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = lane + 32 * h;
+        float4 x = v[i][h];
+        if (64 * c + k >= g.nh) x = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float mr = mine ? x.z : x.x, mi = mine ? x.w : x.y;
+        store_split1(B, tc::sw128_offset(2 * ql, k), mr, BT);
+        store_split1(B, tc::sw128_offset(2 * ql + 1, k), mi, BT);
+        if (BOTH) {
+          const float orr = mine ? x.x : x.z, oi = mine ? x.y : x.w;
+          store_split1(B + 3 * BT, tc::sw128_offset(2 * ql, k), orr, BT);
+          store_split1(B + 3 * BT, tc::sw128_offset(2 * ql + 1, k), oi, BT);
+        }
+      }
+    }
+  }
+}

@@ -310,3 +310,64 @@ def test_bf16x3_full_size_levels(built, torch):
         assert torch.isfinite(lbf[k]).all(), k
         e = float(torch.linalg.vector_norm(lbf[k] - l64[k]) / torch.linalg.vector_norm(l64[k]))
         assert e < (1e-3 if k == "VStLM" else 2e-6), (k, e)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16x3"])
+def test_pipelined_host_levels_match_device_call(built, torch, prec):
+    """Host arrays with more levels than one pipeline chunk go through the
+    chunked copy/compute pipeline; results equal the device-pointer call."""
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    L, minc, N, P, n = 63, 1, 96, 192, 19
+    s = make(L, minc, N, P, prec=prec)
+    spec_np = grid_space_inputs(L, minc, n, seed=8)
+    or2 = or2_levels(n)
+    lcut = np.full(n, L, dtype=np.int32)
+    lcut[3] = L - 11
+    pin = {k: torch.from_numpy(v).pin_memory() for k, v in spec_np.items()}
+    host = s.transform_to_grid_space(pin, or2=or2, lcut=lcut)
+    dev = s.transform_to_grid_space({k: v.cuda() for k, v in pin.items()}, or2=or2, lcut=lcut)
+    torch.cuda.synchronize()
+    for k in dev:
+        assert torch.equal(host[k], dev[k].cpu()), k
+    fin = {k: host[v] for k, v in FORWARD_FROM_INVERSE.items()}
+    lh = s.transform_to_lm_space(fin, lcut=lcut)
+    ld = s.transform_to_lm_space({k: v.cuda() for k, v in fin.items()}, lcut=lcut)
+    torch.cuda.synchronize()
+    for k in ld:
+        assert torch.equal(lh[k], ld[k].cpu()), k
+    # pageable numpy arrays take the same path
+    hn = s.transform_to_grid_space(spec_np, or2=or2, lcut=lcut)
+    for k in dev:
+        assert np.array_equal(hn[k], dev[k].cpu().numpy()), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("grid", [(63, 1, 96, 192), (64, 4, 96, 48), (255, 1, 384, 768)])
+def test_persistent_tensor_core_kernels_equal_tiled(built, torch, grid, monkeypatch):
+    """The persistent warp-specialized tensor-core kernels issue the same MMA
+    sequence per accumulator as the one-tile-per-CTA kernels: the radial-loop
+    set agrees bit for bit (ragged lcut and the odd-parity m = l_max tile
+    included)."""
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    L, minc, N, P = grid
+    n = 5 if L > 200 else 11
+    spec_np = grid_space_inputs(L, minc, n, seed=21)
+    or2 = or2_levels(n)
+    lcut = np.full(n, L, dtype=np.int32)
+    lcut[1] = L - 7
+    spec_d = {k: torch.from_numpy(v).cuda() for k, v in spec_np.items()}
+    out = {}
+    for kern in ("tiled", "persistent"):
+        monkeypatch.setenv("MAGIC_SHT_TC_KERNEL", kern)
+        s = make(L, minc, N, P, prec="bf16x3")
+        g = s.transform_to_grid_space(spec_d, or2=or2, lcut=lcut)
+        fin = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
+        lm = s.transform_to_lm_space(fin, lcut=lcut)
+        torch.cuda.synchronize()
+        s.device_status()
+        out[kern] = ({k: v.cpu() for k, v in g.items()}, {k: v.cpu() for k, v in lm.items()})
+    for a, b in zip(out["tiled"], out["persistent"]):
+        for k in a:
+            x, y = (torch.view_as_real(t) if t.is_complex() else t for t in (a[k], b[k]))
+            if not torch.equal(x, y):  # same MMA order: at most last-bit differences
+                assert rel_max(y.numpy(), x.numpy()) < 1e-6, k
