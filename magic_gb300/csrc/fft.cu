@@ -159,7 +159,7 @@ __device__ __forceinline__ int pin(int k) { return (k % S) * 32 + k / S; }
 // odd pitch KP = n+1 so that row-parallel and index-parallel accesses both
 // spread over the banks.
 template <typename T, int S, int RT>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1)) fft_inv_fast(const ShtGeom g, const FftSet s) {
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1)) fft_inv_fast(const ShtGeom g, const FftSet s) {
   typedef typename V2<T>::t T2;
   constexpr int n = 32 * S, KP = n + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -168,7 +168,10 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   const int r = col / s.nf, f = col - r * s.nf;
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
-  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  const T2* __restrict__ twg = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  T2* stw = sm + RT * KP;  // twiddle table e^{+2 pi i k / P}, k < P, copied to shared memory
+  for (int i = threadIdx.x; i < 2 * n; i += 256) stw[i] = twg[i];
+  const T2* tw = stw;
   const T2* __restrict__ in = (const T2*)fd.in + (long long)r * fd.in_ld;
   const int n_m = g.n_m;
   const bool in_parity = (fd.flags & (FFT_IN_E | FFT_IN_EF)) != 0;
@@ -228,26 +231,27 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   double* out = (double*)fd.out + (long long)r * fd.out_ld;
   const bool osin = (fd.flags & FFT_OSIN2) != 0;
   const bool vec = (g.ld % 2) == 0;  // 16-byte stores of two rows need an even pitch
-#pragma unroll (sizeof(T) == 4 ? 8 : 2)
-  for (int i = threadIdx.x; i < g.n_phi * RT2; i += 256) {
-    const int ph = i / RT2, rr = 2 * (i - ph * RT2);
+#pragma unroll (sizeof(T) == 4 ? 4 : 2)
+  for (int i = threadIdx.x; i < n * RT2; i += 256) {
+    const int kk = i / RT2, rr = 2 * (i - kk * RT2);
     const int rowg = row0 + rr;
     if (rowg >= g.n_theta) continue;
-    const T2 v0 = sm[rr * KP + (ph >> 1)];
-    const T2 v1 = sm[(rr + 1) * KP + (ph >> 1)];
-    T x0 = (ph & 1) ? v0.y : v0.x;
-    T x1 = (ph & 1) ? v1.y : v1.x;
+    T2 v0 = sm[rr * KP + kk];        // phi = 2kk (x) and 2kk+1 (y) of row rr
+    T2 v1 = sm[(rr + 1) * KP + kk];
     if (osin) {
       const T o = from_f64<T>(g.osin2[rowg >> 1]);  // rows 2j and 2j+1 share theta_j
-      x0 *= o;
-      x1 *= o;
+      v0 = cscale(v0, o);
+      v1 = cscale(v1, o);
     }
-    double* dst = out + (long long)ph * g.ld + rowg;
+    double* dst = out + (long long)(2 * kk) * g.ld + rowg;
     if (vec) {
-      *reinterpret_cast<double2*>(dst) = make_double2(to_f64<T>(x0), to_f64<T>(x1));
+      *reinterpret_cast<double2*>(dst) = make_double2(to_f64<T>(v0.x), to_f64<T>(v1.x));
+      *reinterpret_cast<double2*>(dst + g.ld) = make_double2(to_f64<T>(v0.y), to_f64<T>(v1.y));
     } else {
-      dst[0] = to_f64<T>(x0);
-      dst[1] = to_f64<T>(x1);
+      dst[0] = to_f64<T>(v0.x);
+      dst[1] = to_f64<T>(v1.x);
+      dst[g.ld] = to_f64<T>(v0.y);
+      dst[g.ld + 1] = to_f64<T>(v1.y);
     }
   }
 }
@@ -263,29 +267,34 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   const int r = col / s.nf, f = col - r * s.nf;
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
-  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  const T2* __restrict__ twg = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  T2* stw = sm + RT * KP;  // twiddle table e^{+2 pi i k / P}, k < P, copied to shared memory
+  for (int i = threadIdx.x; i < 2 * n; i += 256) stw[i] = twg[i];
+  const T2* tw = stw;
   const double* __restrict__ in = (const double*)fd.in + (long long)r * fd.in_ld;
   constexpr int RT2 = RT / 2;
   const bool vec = (g.ld % 2) == 0;
-#pragma unroll (sizeof(T) == 4 ? 8 : 2)
-  for (int i = threadIdx.x; i < g.n_phi * RT2; i += 256) {
-    const int ph = i / RT2, rr = 2 * (i - ph * RT2);
+#pragma unroll (sizeof(T) == 4 ? 4 : 2)
+  for (int i = threadIdx.x; i < n * RT2; i += 256) {
+    const int kk = i / RT2, rr = 2 * (i - kk * RT2);
     const int row = row0 + rr;
-    double x0 = 0.0, x1 = 0.0;
+    double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;  // (phi 2kk | 2kk+1) x (row rr | rr+1)
     if (row < g.n_theta) {
-      const double* src = in + (long long)ph * g.ld + row;
+      const double* src = in + (long long)(2 * kk) * g.ld + row;
       if (vec) {
-        const double2 v = *reinterpret_cast<const double2*>(src);
-        x0 = v.x;
-        x1 = v.y;
+        const double2 u = *reinterpret_cast<const double2*>(src);
+        const double2 w = *reinterpret_cast<const double2*>(src + g.ld);
+        a0 = u.x; a1 = u.y; b0 = w.x; b1 = w.y;
       } else {
-        x0 = src[0];
-        x1 = src[1];
+        a0 = src[0]; a1 = src[1]; b0 = src[g.ld]; b1 = src[g.ld + 1];
       }
     }
-    const int pj = pin<S>(ph >> 1);
-    smr[2 * (rr * KP + pj) + (ph & 1)] = (T)x0;
-    smr[2 * ((rr + 1) * KP + pj) + (ph & 1)] = (T)x1;
+    const int pj = pin<S>(kk);
+    T2 z0, z1;
+    z0.x = (T)a0; z0.y = (T)b0;
+    z1.x = (T)a1; z1.y = (T)b1;
+    sm[rr * KP + pj] = z0;
+    sm[(rr + 1) * KP + pj] = z1;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -552,7 +561,7 @@ cudaError_t launch_fast(const ShtGeom& g, const FftSet& s, bool inverse, cudaStr
   constexpr int n = 32 * S;
   // 16 rows per CTA; 8 rows where 16 would leave one CTA per SM
   constexpr int RT = (sizeof(T2) * 16 * (n + 1) > 100 * 1024) ? 8 : 16;
-  const size_t smem = (size_t)RT * (n + 1) * sizeof(T2);
+  const size_t smem = ((size_t)RT * (n + 1) + 2 * n) * sizeof(T2);
   dim3 grid((g.n_theta + RT - 1) / RT, s.nf * s.nlev);
   if (inverse) {
     auto k = fft_inv_fast<T, S, RT>;

@@ -7,8 +7,8 @@
 //     exact shared-memory image of the MMA's K-major, 128-byte-swizzled
 //     operand (synthesis: spectra with their operator applied, one image per
 //     (m, parity, 64-degree chunk, column tile); analysis: the ES and EA half
-//     spectra, one image pair per (m, 64-colatitude chunk, column tile)).
-//     It runs at full occupancy and writes each tile with one bulk copy.
+//     spectra, one image each per (m, 64-colatitude chunk, column tile)).
+//     One CTA builds one tile and writes it with one bulk copy.
 //  2. one persistent CTA per SM walks a static list of output tiles
 //        synthesis tile = (m, parity, 128 colatitudes, column tile)
 //        analysis tile  = (m, parity, 128 degrees of that parity, column tile)
@@ -55,19 +55,24 @@ __device__ __forceinline__ void drain_copies(uint64_t* full, uint32_t use) {
 }
 
 // Issue the MMAs of one table split `sp` against the three data splits.
+// Descriptors are built once per call; a K step of 16 bf16 (32 bytes) and a
+// table tile of 16 KB advance the 16-byte-unit start address field.
 template <int NT, int NC>
 __device__ __forceinline__ void issue_split(uint32_t acc, const unsigned char* A, const unsigned char* B,
                                             int sp, bool first_chunk, uint32_t bstride_tb) {
   constexpr int BT = NC * 128;
   constexpr uint32_t IDESC = tc::idesc_bf16(128, NC);
+  const uint64_t a0 = tc::sw128_desc(tc::smem_u32(A));
+  const uint64_t bd0 = tc::sw128_desc(tc::smem_u32(B));
+#pragma unroll
   for (int ks = 0; ks < 4; ++ks)
+#pragma unroll
     for (int tb = 0; tb < NT; ++tb) {
       const uint32_t hi = acc + (uint32_t)((tb * 2 + 0) * NC), cr = acc + (uint32_t)((tb * 2 + 1) * NC);
-      const uint64_t ad = tc::sw128_desc(tc::smem_u32(A + tb * 16384) + ks * 32);
-      const unsigned char* b = B + tb * bstride_tb;
-      const uint64_t b0 = tc::sw128_desc(tc::smem_u32(b) + ks * 32);
-      const uint64_t b1 = tc::sw128_desc(tc::smem_u32(b + BT) + ks * 32);
-      const uint64_t b2 = tc::sw128_desc(tc::smem_u32(b + 2 * BT) + ks * 32);
+      const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
+      const uint64_t b0 = bd0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
+      const uint64_t b1 = b0 + (uint64_t)(BT >> 4);
+      const uint64_t b2 = b0 + (uint64_t)((2 * BT) >> 4);
       const uint32_t first = (!first_chunk || ks) ? 1u : 0u;
       if (sp == 0) {
         tc::mma_bf16(hi, ad, b0, IDESC, first);
@@ -83,63 +88,54 @@ __device__ __forceinline__ void issue_split(uint32_t acc, const unsigned char* A
 }
 
 // ------------------------------------------------------------------ packing
+// One data tile per CTA (grid: column tile, m, tile of that m), built in
+// shared memory and written with one bulk copy.
 // Synthesis data images: [pc = bpc0[m] + p*nch + c][ct] tiles of 3 splits.
 template <bool VEC>
-__global__ void __launch_bounds__(kPackThreads) pack_inv_kernel(const ShtGeom g, const InvSet s, const TcTables t,
-                                                               unsigned char* __restrict__ bimg, int nct) {
+__global__ void __launch_bounds__(kPackThreads, 3) pack_inv_kernel(const ShtGeom g, const InvSet s,
+                                                                  const TcTables t,
+                                                                  unsigned char* __restrict__ bimg, int nct) {
   constexpr int NC = VEC ? 64 : 128;
   constexpr uint32_t BSZ = 3u * NC * 128u;
   extern __shared__ unsigned char smem_raw[];
-  unsigned char* buf = align1k(smem_raw);
-  const int ct = blockIdx.x, mc = blockIdx.y;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m = mc * g.minc, lm0 = g.lmoff[mc];
+  unsigned char* B = align1k(smem_raw);
+  const int ct = blockIdx.x, mc = blockIdx.y, i = blockIdx.z;
+  const int m = mc * g.minc;
   const int nch = tc_nch(g.l_max - m + 1);
+  if (i >= 2 * nch) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  const long long pc0 = t.bpc0[mc];
-  for (int i = 0; i < 2 * nch; ++i) {
-    unsigned char* B = buf + (i & 1) * BSZ;
-    if (i >= 2) {  // the copy that last read this buffer has finished reading it
-      if (threadIdx.x == 0) tc::bulk_wait_read<1>();
-      __syncthreads();
-    }
-    inv_build_tile<VEC, NC, 4>(g, s, B, ct, ncplx, m, lm0, i / nch, i % nch, warp, kPackThreads / 32, lane);
-    tc::fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      tc::bulk_s2g(bimg + ((pc0 + i) * nct + ct) * (long long)BSZ, B, BSZ);
-      tc::bulk_commit();
-    }
+  inv_build_tile<VEC, NC, 2>(g, s, B, ct, ncplx, m, g.lmoff[mc], i / nch, i % nch, warp, kPackThreads / 32, lane);
+  tc::fence_proxy_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc::bulk_s2g(bimg + ((t.bpc0[mc] + i) * nct + ct) * (long long)BSZ, B, BSZ);
+    tc::bulk_commit();
+    tc::bulk_wait<0>();
   }
-  if (threadIdx.x == 0) tc::bulk_wait<0>();
 }
 
-// Analysis data images: [m][c][ct] pairs (ES tile, EA tile) of 3 splits each.
+// Analysis data images: [m][c][ct] pairs (ES tile, EA tile) of 3 splits each;
+// grid z = 2c + (0: ES, 1: EA).
 template <bool VEC>
-__global__ void __launch_bounds__(kPackThreads) pack_fwd_kernel(const ShtGeom g, const FwdSet s, const TcTables t,
-                                                               unsigned char* __restrict__ bimg, int nct) {
+__global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_kernel(const ShtGeom g, const FwdSet s,
+                                                                  const TcTables t,
+                                                                  unsigned char* __restrict__ bimg, int nct) {
   constexpr int NC = VEC ? 64 : 128;
-  constexpr uint32_t PSZ = 2u * 3u * NC * 128u;
+  constexpr uint32_t TS = 3u * NC * 128u;
   extern __shared__ unsigned char smem_raw[];
-  unsigned char* buf = align1k(smem_raw);
-  const int ct = blockIdx.x, mc = blockIdx.y;
+  unsigned char* B = align1k(smem_raw);
+  const int ct = blockIdx.x, mc = blockIdx.y, c = blockIdx.z >> 1, par = blockIdx.z & 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  for (int c = 0; c < t.ncj; ++c) {
-    unsigned char* B = buf + (c & 1) * PSZ;
-    if (c >= 2) {
-      if (threadIdx.x == 0) tc::bulk_wait_read<1>();
-      __syncthreads();
-    }
-    fwd_build_tile<VEC, NC, 4, true>(g, s, B, ct, ncplx, mc, 0, c, warp, kPackThreads / 32, lane);
-    tc::fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      tc::bulk_s2g(bimg + (((long long)mc * t.ncj + c) * nct + ct) * (long long)PSZ, B, PSZ);
-      tc::bulk_commit();
-    }
+  fwd_build_tile<VEC, NC, 2, false>(g, s, B, ct, ncplx, mc, par, c, warp, kPackThreads / 32, lane);
+  tc::fence_proxy_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc::bulk_s2g(bimg + ((((long long)mc * t.ncj + c) * nct + ct) * 2 + par) * (long long)TS, B, TS);
+    tc::bulk_commit();
+    tc::bulk_wait<0>();
   }
-  if (threadIdx.x == 0) tc::bulk_wait<0>();
 }
 
 // ------------------------------------------------------------ synthesis
@@ -555,9 +551,9 @@ cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, u
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
-  const size_t psmem = 1024 + 2 * 3 * (size_t)NC * 128;
+  const size_t psmem = 1024 + 3 * (size_t)NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(pack_inv_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_inv_kernel<VEC><<<dim3(nct, g.n_m), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  pack_inv_kernel<VEC><<<dim3(nct, g.n_m, 2 * tc_nch(g.l_max + 1)), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + 2 * 3 * (size_t)NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -574,9 +570,9 @@ cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, u
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
-  const size_t psmem = 1024 + 2 * 2 * 3 * (size_t)NC * 128;
+  const size_t psmem = 1024 + 3 * (size_t)NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(pack_fwd_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_fwd_kernel<VEC><<<dim3(nct, g.n_m), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  pack_fwd_kernel<VEC><<<dim3(nct, g.n_m, 2 * t.ncj), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + 2 * (size_t)NT * 3 * NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
