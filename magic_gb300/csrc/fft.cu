@@ -257,12 +257,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
 }
 
 template <typename T, int S, int RT>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1)) fft_fwd_fast(const ShtGeom g, const FftSet s) {
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1)) fft_fwd_fast(const ShtGeom g, const FftSet s) {
   typedef typename V2<T>::t T2;
   constexpr int n = 32 * S, KP = n + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2* sm = (T2*)smem_raw;
-  T* smr = (T*)smem_raw;
   const int col = blockIdx.y;
   const int r = col / s.nf, f = col - r * s.nf;
   const FftField& fd = s.f[f];

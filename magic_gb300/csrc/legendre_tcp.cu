@@ -8,19 +8,29 @@
 //     operand (synthesis: spectra with their operator applied, one image per
 //     (m, parity, 64-degree chunk, column tile); analysis: the ES and EA half
 //     spectra, one image each per (m, 64-colatitude chunk, column tile)).
-//     One CTA builds one tile and writes it with one bulk copy.
+//     One CTA builds the two tiles that share its input (both parities of a
+//     128-degree chunk; the ES and EA tiles of 64 colatitudes) and writes them
+//     with bulk copies.
 //  2. one persistent CTA per SM walks a static list of output tiles
-//        synthesis tile = (m, parity, 128 colatitudes, column tile)
-//        analysis tile  = (m, parity, 128 degrees of that parity, column tile)
+//        synthesis tile = (m, parity, 128 colatitudes, 32 complex columns)
+//        analysis tile  = (m, parity, 128 degrees of that parity, 32 complex columns)
 //     with three roles:
 //        warp 0      bulk-copy loader of table tiles (A ring) and data tiles (B ring)
 //        warp 1      tcgen05.mma issuer (one thread)
 //        warps 2..9  epilogue: two warps per TMEM lane quadrant, each draining
-//                    half of the columns of one of two accumulator sets while
-//                    the next tile accumulates in the other
+//                    half of the columns; the accumulators are summed into
+//                    registers and released before the outputs are computed
+//
+// Split products: the three splits of a data tile lie one after the other
+// (hi, mid, lo: 64 rows each), so one MMA with N = 192 multiplies a table
+// split by all three.  Per table and K step:
+//     A_hi  x [B_hi | B_mid | B_lo]  ->  [C0 | C1 | C2]   (N = 192)
+//     A_mid x [B_hi | B_mid]         ->       [C1 | C2]   (N = 128)
+//     A_lo  x [B_hi]                 ->            [C2]   (N = 64)
+// C0 = hi*hi, C1 the 2^-8-order and C2 the 2^-16-order cross products, each
+// accumulated apart in fp32 and summed (C2 + C1) + C0 in the epilogue.
 // Hand-offs use full/empty mbarriers; every wait is bounded and a wait that
-// gives up sets the device error word.  The MMA sequence per accumulator is
-// that of legendre_tc.cu: hi*hi and the five cross products accumulate apart.
+// gives up sets the device error word.
 #include <cuda_bf16.h>
 #include "common.cuh"
 #include "cplx.cuh"
@@ -29,6 +39,8 @@
 #include "tc_build.cuh"
 
 namespace {
+
+constexpr int kNC = 64;  // real data columns per tile (32 complex)
 
 constexpr int kThreads = 320;     // 10 warps
 constexpr int kEpiThreads = 256;  // warps 2..9
@@ -54,85 +66,92 @@ __device__ __forceinline__ void drain_copies(uint64_t* full, uint32_t use) {
   for (uint32_t u = use > N ? use - N : 0; u < use; ++u) wait_full(&full[u % N], u, N);
 }
 
-// Issue the MMAs of one table split `sp` against the three data splits.
-// Descriptors are built once per call; a K step of 16 bf16 (32 bytes) and a
-// table tile of 16 KB advance the 16-byte-unit start address field.
-template <int NT, int NC>
+// Issue the MMAs of table split `sp` (NT tables) against the stacked data
+// splits; D holds NT accumulator groups of 3*kNC columns.
+template <int NT>
 __device__ __forceinline__ void issue_split(uint32_t acc, const unsigned char* A, const unsigned char* B,
                                             int sp, bool first_chunk, uint32_t bstride_tb) {
-  constexpr int BT = NC * 128;
-  constexpr uint32_t IDESC = tc::idesc_bf16(128, NC);
+  constexpr uint32_t ID3 = tc::idesc_bf16(128, 3 * kNC), ID2 = tc::idesc_bf16(128, 2 * kNC),
+                     ID1 = tc::idesc_bf16(128, kNC);
   const uint64_t a0 = tc::sw128_desc(tc::smem_u32(A));
   const uint64_t bd0 = tc::sw128_desc(tc::smem_u32(B));
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks)
 #pragma unroll
     for (int tb = 0; tb < NT; ++tb) {
-      const uint32_t hi = acc + (uint32_t)((tb * 2 + 0) * NC), cr = acc + (uint32_t)((tb * 2 + 1) * NC);
+      const uint32_t d = acc + (uint32_t)(tb * 3 * kNC);
       const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
-      const uint64_t b0 = bd0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
-      const uint64_t b1 = b0 + (uint64_t)(BT >> 4);
-      const uint64_t b2 = b0 + (uint64_t)((2 * BT) >> 4);
-      const uint32_t first = (!first_chunk || ks) ? 1u : 0u;
-      if (sp == 0) {
-        tc::mma_bf16(hi, ad, b0, IDESC, first);
-        tc::mma_bf16(cr, ad, b1, IDESC, first);
-        tc::mma_bf16(cr, ad, b2, IDESC, 1u);
-      } else if (sp == 1) {
-        tc::mma_bf16(cr, ad, b0, IDESC, 1u);
-        tc::mma_bf16(cr, ad, b1, IDESC, 1u);
-      } else {
-        tc::mma_bf16(cr, ad, b0, IDESC, 1u);
-      }
+      const uint64_t bd = bd0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
+      if (sp == 0) tc::mma_bf16(d, ad, bd, ID3, (!first_chunk || ks) ? 1u : 0u);
+      else if (sp == 1) tc::mma_bf16(d + kNC, ad, bd, ID2, 1u);
+      else tc::mma_bf16(d + 2 * kNC, ad, bd, ID1, 1u);
     }
+}
+
+// (C2 + C1) + C0 of one table for the 32 columns at TMEM address `col`
+// (this warp's lane quadrant).
+__device__ __forceinline__ void drain_sum(uint32_t col, float (&v)[32]) {
+  uint32_t a[32], b[32];
+  tc::tmem_ld32_nw(col + 2 * kNC, a);
+  tc::tmem_ld32_nw(col + kNC, b);
+  tc::tmem_wait_ld();
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(a[i]) + __uint_as_float(b[i]);
+  tc::tmem_ld32_nw(col, a);
+  tc::tmem_wait_ld();
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] += __uint_as_float(a[i]);
 }
 
 // ------------------------------------------------------------------ packing
 // One data tile per CTA (grid: column tile, m, tile of that m), built in
 // shared memory and written with one bulk copy.
 // Synthesis data images: [pc = bpc0[m] + p*nch + c][ct] tiles of 3 splits.
+// One CTA builds both parity tiles of chunk c from 128 consecutive degrees.
 template <bool VEC>
-__global__ void __launch_bounds__(kPackThreads, 3) pack_inv_kernel(const ShtGeom g, const InvSet s,
+__global__ void __launch_bounds__(kPackThreads, 2) pack_inv_kernel(const ShtGeom g, const InvSet s,
                                                                   const TcTables t,
                                                                   unsigned char* __restrict__ bimg, int nct) {
-  constexpr int NC = VEC ? 64 : 128;
+  constexpr int NC = kNC;
   constexpr uint32_t BSZ = 3u * NC * 128u;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* B = align1k(smem_raw);
-  const int ct = blockIdx.x, mc = blockIdx.y, i = blockIdx.z;
+  const int ct = blockIdx.x, mc = blockIdx.y, c = blockIdx.z;
   const int m = mc * g.minc;
   const int nch = tc_nch(g.l_max - m + 1);
-  if (i >= 2 * nch) return;
+  if (c >= nch) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  inv_build_tile<VEC, NC, 2>(g, s, B, ct, ncplx, m, g.lmoff[mc], i / nch, i % nch, warp, kPackThreads / 32, lane);
+  inv_build_pair<VEC, NC, 2>(g, s, B, ct, ncplx, m, g.lmoff[mc], c, warp, kPackThreads / 32, lane);
   tc::fence_proxy_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
-    tc::bulk_s2g(bimg + ((t.bpc0[mc] + i) * nct + ct) * (long long)BSZ, B, BSZ);
+    const long long pc = t.bpc0[mc] + c;  // parity 0; parity 1 is nch further
+    tc::bulk_s2g(bimg + (pc * nct + ct) * (long long)BSZ, B, BSZ);
+    tc::bulk_s2g(bimg + ((pc + nch) * nct + ct) * (long long)BSZ, B + BSZ, BSZ);
     tc::bulk_commit();
     tc::bulk_wait<0>();
   }
 }
 
-// Analysis data images: [m][c][ct] pairs (ES tile, EA tile) of 3 splits each;
-// grid z = 2c + (0: ES, 1: EA).
+// Analysis data images: [m][c][ct] pairs (ES tile, EA tile) of 3 splits each,
+// both built by one CTA from the (ES, EA) entries of 64 colatitudes.
 template <bool VEC>
 __global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_kernel(const ShtGeom g, const FwdSet s,
                                                                   const TcTables t,
                                                                   unsigned char* __restrict__ bimg, int nct) {
-  constexpr int NC = VEC ? 64 : 128;
-  constexpr uint32_t TS = 3u * NC * 128u;
+  constexpr int NC = kNC;
+  constexpr uint32_t PSZ = 2u * 3u * NC * 128u;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* B = align1k(smem_raw);
-  const int ct = blockIdx.x, mc = blockIdx.y, c = blockIdx.z >> 1, par = blockIdx.z & 1;
+  const int ct = blockIdx.x, mc = blockIdx.y, c = blockIdx.z;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  fwd_build_tile<VEC, NC, 2, false>(g, s, B, ct, ncplx, mc, par, c, warp, kPackThreads / 32, lane);
+  fwd_build_tile<VEC, NC, 2, true>(g, s, B, ct, ncplx, mc, 0, c, warp, kPackThreads / 32, lane);
   tc::fence_proxy_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
-    tc::bulk_s2g(bimg + ((((long long)mc * t.ncj + c) * nct + ct) * 2 + par) * (long long)TS, B, TS);
+    tc::bulk_s2g(bimg + (((long long)mc * t.ncj + c) * nct + ct) * (long long)PSZ, B, PSZ);
     tc::bulk_commit();
     tc::bulk_wait<0>();
   }
@@ -159,15 +178,15 @@ template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, const InvSet s, const TcTables t,
                                                            const unsigned char* __restrict__ bimg, int nct) {
   constexpr int NT = VEC ? 2 : 1;
-  constexpr int NC = VEC ? 64 : 128;
+  constexpr int NC = kNC;
   constexpr int NA = VEC ? 3 : 4;
-  constexpr int NB = 2;
-  constexpr int BT = NC * 128;
+  constexpr int NB = VEC ? 2 : 3;
+  constexpr int NACC = VEC ? 1 : 2;  // accumulator sets (3*NC columns per table)
+  constexpr int BSZ = 3 * NC * 128;
   constexpr int ASZ = NT * 16384;
-  constexpr int BSZ = 3 * BT;
-  constexpr uint32_t ACC = NT * 2 * NC;  // one accumulator set (256 columns)
+  constexpr uint32_t ACC = NT * 3 * NC;
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[2], acc_empty[2], fin;
+  __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[NACC], acc_empty[NACC], fin;
   __shared__ uint32_t tmem_base;
   __shared__ int s_fail;
   unsigned char* base = align1k(smem_raw);
@@ -181,7 +200,7 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
   if (tid == 0) {
     for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], 1); }
     for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
-    for (int i = 0; i < 2; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
+    for (int i = 0; i < NACC; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
     tc::mbar_init(&fin, 1);
     s_fail = 0;
     tc::fence_mbar_init();
@@ -231,8 +250,8 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
       for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
         T.decode(g, t, nct, ix);
         if (T.nlp == 0 || T.ct * (NC / 2) >= ncplx) continue;
-        const uint32_t abuf = acc_use & 1u;
-        if (!wait_empty(&acc_empty[abuf], acc_use, 2)) { ok = false; break; }
+        const uint32_t abuf = acc_use % NACC;
+        if (!wait_empty(&acc_empty[abuf], acc_use, NACC)) { ok = false; break; }
         tc::tc_fence_after();
         const uint32_t acc = tmem + abuf * ACC;
         for (int c = 0; c < T.nchp && ok; ++c, ++b_use) {
@@ -242,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_split<NT, NC>(acc, sA + slot * ASZ, sB + bslot * BSZ, sp, c == 0, 0);
+            issue_split<NT>(acc, sA + slot * ASZ, sB + bslot * BSZ, sp, c == 0, 0);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -256,6 +275,7 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
     }
   } else {  // ------------------------------------------------------ epilogue
     const int q4 = warp & 3, half = (warp - 2) >> 2;
+    const int cc0 = half * (NC / 2);  // this warp's 32 real columns
     const int jl = 32 * q4 + lane;
     const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
     const int NHP = t.ntt * 128;
@@ -271,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
       };
       if (T.nlp == 0) {  // odd parity of m = l_max: zeros
         if (jg < g.nh)
-          for (int q = half * (NC / 4); q < (half + 1) * (NC / 4); ++q) {
+          for (int q = cc0 / 2; q < cc0 / 2 + 16; ++q) {
             const int cq = T.ct * (NC / 2) + q;
             if (cq >= ncplx) break;
             if (!VEC) {
@@ -287,54 +307,49 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
           }
         continue;
       }
-      const uint32_t abuf = acc_use & 1u;
-      if (!wait_full(&acc_full[abuf], acc_use, 2)) { ok = false; break; }
+      const uint32_t abuf = acc_use % NACC;
+      if (!wait_full(&acc_full[abuf], acc_use, NACC)) { ok = false; break; }
       tc::tc_fence_after();
-      const uint32_t acc = tmem + abuf * ACC + lane_off;
+      const uint32_t acc = tmem + abuf * ACC + lane_off + cc0;
+      float P[32], D[32];
+      drain_sum(acc, P);
+      if (VEC) drain_sum(acc + 3 * NC, D);
+      tc::tc_fence_before();
+      tc::mbar_arrive(&acc_empty[abuf]);  // tensor memory free for the next tile
+      ++acc_use;
       const float sP = t.inv_scale[(size_t)T.mc * NHP + jg];
-      const float sdP = VEC ? t.inv_scale[((size_t)g.n_m + T.mc) * NHP + jg] : 0.f;
-      const float dm = (float)(T.mc * g.minc);
-      for (int cc0 = half * (NC / 2); cc0 < (half + 1) * (NC / 2); cc0 += 32) {
-        float P[32], X[32];
-        tc::tmem_ld32(acc + 0 * NC + cc0, P);
-        tc::tmem_ld32(acc + 1 * NC + cc0, X);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) P[i] = (P[i] + X[i]) * sP;
-        if (!VEC) {
+      for (int i = 0; i < 32; ++i) P[i] *= sP;
+      if (!VEC) {
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int cq = T.ct * (NC / 2) + cc0 / 2 + q;
-            if (cq >= ncplx || jg >= g.nh) continue;
-            const int r = cq / s.nf, f = cq - r * s.nf;
-            *optr(s.f[f].out0, r, f, 0) = make_float2(P[2 * q], P[2 * q + 1]);
-          }
-        } else {
-          float D[32];
-          tc::tmem_ld32(acc + 2 * NC + cc0, D);
-          tc::tmem_ld32(acc + 3 * NC + cc0, X);
+        for (int q = 0; q < 16; ++q) {
+          const int cq = T.ct * (NC / 2) + cc0 / 2 + q;
+          if (cq >= ncplx || jg >= g.nh) continue;
+          const int r = cq / s.nf, f = cq - r * s.nf;
+          *optr(s.f[f].out0, r, f, 0) = make_float2(P[2 * q], P[2 * q + 1]);
+        }
+      } else {
+        const float sdP = t.inv_scale[((size_t)g.n_m + T.mc) * NHP + jg];
+        const float dm = (float)(T.mc * g.minc);
 #pragma unroll
-          for (int i = 0; i < 32; ++i) D[i] = (D[i] + X[i]) * sdP;
+        for (int i = 0; i < 32; ++i) D[i] *= sdP;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int pr = T.ct * (NC / 4) + cc0 / 4 + q;
-            if (pr >= npair || jg >= g.nh) continue;
-            const int r = pr / s.nf, f = pr - r * s.nf;
-            // C = sum S P, B = sum T P; A = sum S dP, D = sum T dP
-            const float Cr = P[4 * q], Ci = P[4 * q + 1], Br = P[4 * q + 2], Bi = P[4 * q + 3];
-            const float Ar = D[4 * q], Ai = D[4 * q + 1], Dr = D[4 * q + 2], Di = D[4 * q + 3];
-            // v_theta: U = i m B, W = A;   v_phi: U = i m C, W = -D
-            const float2 Ut = make_float2(-dm * Bi, dm * Br), Wt = make_float2(Ar, Ai);
-            const float2 Up = make_float2(-dm * Ci, dm * Cr), Wp = make_float2(-Dr, -Di);
-            *optr(s.f[f].out0, r, f, 0) = make_float2(Ut.x + Wt.x, Ut.y + Wt.y);
-            *optr(s.f[f].out0, r, f, 1) = make_float2(Ut.x - Wt.x, Ut.y - Wt.y);
-            *optr(s.f[f].out1, r, f, 0) = make_float2(Up.x + Wp.x, Up.y + Wp.y);
-            *optr(s.f[f].out1, r, f, 1) = make_float2(Up.x - Wp.x, Up.y - Wp.y);
-          }
+        for (int q = 0; q < 8; ++q) {
+          const int pr = T.ct * (NC / 4) + cc0 / 4 + q;
+          if (pr >= npair || jg >= g.nh) continue;
+          const int r = pr / s.nf, f = pr - r * s.nf;
+          // C = sum S P, B = sum T P; A = sum S dP, D = sum T dP
+          const float Cr = P[4 * q], Ci = P[4 * q + 1], Br = P[4 * q + 2], Bi = P[4 * q + 3];
+          const float Ar = D[4 * q], Ai = D[4 * q + 1], Dr = D[4 * q + 2], Di = D[4 * q + 3];
+          // v_theta: U = i m B, W = A;   v_phi: U = i m C, W = -D
+          const float2 Ut = make_float2(-dm * Bi, dm * Br), Wt = make_float2(Ar, Ai);
+          const float2 Up = make_float2(-dm * Ci, dm * Cr), Wp = make_float2(-Dr, -Di);
+          *optr(s.f[f].out0, r, f, 0) = make_float2(Ut.x + Wt.x, Ut.y + Wt.y);
+          *optr(s.f[f].out0, r, f, 1) = make_float2(Ut.x - Wt.x, Ut.y - Wt.y);
+          *optr(s.f[f].out1, r, f, 0) = make_float2(Up.x + Wp.x, Up.y + Wp.y);
+          *optr(s.f[f].out1, r, f, 1) = make_float2(Up.x - Wp.x, Up.y - Wp.y);
         }
       }
-      tc::tc_fence_before();
-      tc::mbar_arrive(&acc_empty[abuf]);
-      ++acc_use;
     }
   }
   if (!ok) atomicExch(&s_fail, 1);
@@ -363,16 +378,16 @@ template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, const FwdSet s, const TcTables t,
                                                            const unsigned char* __restrict__ bimg, int nct) {
   constexpr int NT = VEC ? 2 : 1;
-  constexpr int NC = VEC ? 64 : 128;
+  constexpr int NC = kNC;
   constexpr int NA = VEC ? 3 : 4;
-  constexpr int NB = 2;
-  constexpr int BT = NC * 128;
-  constexpr int TS = 3 * BT;        // one data operand (3 splits)
+  constexpr int NB = VEC ? 2 : 3;
+  constexpr int NACC = VEC ? 1 : 2;
+  constexpr int TS = 3 * NC * 128;  // one data operand (3 splits)
   constexpr int ASZ = NT * 16384;
   constexpr int BSZ = NT * TS;      // mine (and other)
-  constexpr uint32_t ACC = NT * 2 * NC;
+  constexpr uint32_t ACC = NT * 3 * NC;
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[2], acc_empty[2], fin;
+  __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[NACC], acc_empty[NACC], fin;
   __shared__ uint32_t tmem_base;
   __shared__ int s_fail;
   unsigned char* base = align1k(smem_raw);
@@ -386,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
   if (tid == 0) {
     for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], 1); }
     for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
-    for (int i = 0; i < 2; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
+    for (int i = 0; i < NACC; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
     tc::mbar_init(&fin, 1);
     s_fail = 0;
     tc::fence_mbar_init();
@@ -413,7 +428,7 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
           if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
           tc::mbar_expect_tx(&b_full[bslot], BSZ);
           const unsigned char* img = bimg + (((long long)T.mc * t.ncj + c) * nct + T.ct) * (2LL * TS);
-          tc::bulk_g2s(sB + bslot * BSZ, img + T.p * TS, TS, &b_full[bslot]);              // mine
+          tc::bulk_g2s(sB + bslot * BSZ, img + T.p * TS, TS, &b_full[bslot]);                    // mine
           if (VEC) tc::bulk_g2s(sB + bslot * BSZ + TS, img + (1 - T.p) * TS, TS, &b_full[bslot]);  // other
           ++b_use;
           for (int sp = 0; sp < 3; ++sp, ++a_use) {
@@ -437,8 +452,8 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
       for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
         T.decode(g, t, nct, ix);
         if (T.lt * 128 >= T.nlp || T.ct * (NC / 2) >= ncplx) continue;
-        const uint32_t abuf = acc_use & 1u;
-        if (!wait_empty(&acc_empty[abuf], acc_use, 2)) { ok = false; break; }
+        const uint32_t abuf = acc_use % NACC;
+        if (!wait_empty(&acc_empty[abuf], acc_use, NACC)) { ok = false; break; }
         tc::tc_fence_after();
         const uint32_t acc = tmem + abuf * ACC;
         for (int c = 0; c < t.ncj && ok; ++c, ++b_use) {
@@ -448,7 +463,7 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_split<NT, NC>(acc, sA + slot * ASZ, sB + bslot * BSZ, sp, c == 0, TS);
+            issue_split<NT>(acc, sA + slot * ASZ, sB + bslot * BSZ, sp, c == 0, TS);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -461,69 +476,66 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
     }
   } else {
     const int q4 = warp & 3, half = (warp - 2) >> 2;
+    const int cc0 = half * (NC / 2);
     const int lr = 32 * q4 + lane;
     const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
     uint32_t acc_use = 0;
     for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
       T.decode(g, t, nct, ix);
       if (T.lt * 128 >= T.nlp || T.ct * (NC / 2) >= ncplx) continue;
-      const uint32_t abuf = acc_use & 1u;
-      if (!wait_full(&acc_full[abuf], acc_use, 2)) { ok = false; break; }
+      const uint32_t abuf = acc_use % NACC;
+      if (!wait_full(&acc_full[abuf], acc_use, NACC)) { ok = false; break; }
       tc::tc_fence_after();
-      const uint32_t acc = tmem + abuf * ACC + lane_off;
+      const uint32_t acc = tmem + abuf * ACC + lane_off + cc0;
+      float D0[32], D1[32];
+      drain_sum(acc, D0);
+      if (VEC) drain_sum(acc + 3 * NC, D1);
+      tc::tc_fence_before();
+      tc::mbar_arrive(&acc_empty[abuf]);
+      ++acc_use;
       const int m = T.mc * g.minc;
       const int lp = T.lt * 128 + lr;
       const int l = m + T.p + 2 * lp;
       const bool valid = lp < T.nlp;
+      if (!valid) continue;
       const int lm = g.lmoff[T.mc] + l - m;
-      const float sP = valid ? t.fwd_scale[lm] : 0.f;
-      const float sdP = (VEC && valid) ? t.fwd_scale[(size_t)g.lm_max + lm] : 0.f;
-      const float dm = (float)m;
-      const float inv_ll = l > 0 ? 1.0f / (float)(l * (l + 1)) : 1.0f;
-      for (int cc0 = half * (NC / 2); cc0 < (half + 1) * (NC / 2); cc0 += 32) {
-        float D0[32], X[32];
-        tc::tmem_ld32(acc + 0 * NC + cc0, D0);
-        tc::tmem_ld32(acc + 1 * NC + cc0, X);
+      const float sP = t.fwd_scale[lm];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) D0[i] = (D0[i] + X[i]) * sP;
-        if (!VEC) {
+      for (int i = 0; i < 32; ++i) D0[i] *= sP;
+      if (!VEC) {
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int cq = T.ct * (NC / 2) + cc0 / 2 + q;
-            if (cq >= ncplx || !valid) continue;
-            const int r = cq / s.nf, f = cq - r * s.nf;
-            const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
-            const double2 v = (l <= lc) ? make_double2(f2d_int(D0[2 * q]), f2d_int(D0[2 * q + 1]))
-                                        : make_double2(0.0, 0.0);
-            s.f[f].out0[(long long)r * s.f[f].out_ld + lm] = v;
-          }
-        } else {
-          float D1[32];
-          tc::tmem_ld32(acc + 2 * NC + cc0, D1);
-          tc::tmem_ld32(acc + 3 * NC + cc0, X);
+        for (int q = 0; q < 16; ++q) {
+          const int cq = T.ct * (NC / 2) + cc0 / 2 + q;
+          if (cq >= ncplx) continue;
+          const int r = cq / s.nf, f = cq - r * s.nf;
+          const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+          const double2 v = (l <= lc) ? make_double2(f2d_int(D0[2 * q]), f2d_int(D0[2 * q + 1]))
+                                      : make_double2(0.0, 0.0);
+          s.f[f].out0[(long long)r * s.f[f].out_ld + lm] = v;
+        }
+      } else {
+        const float sdP = t.fwd_scale[(size_t)g.lm_max + lm];
+        const float dm = (float)m;
+        const float inv_ll = l > 0 ? 1.0f / (float)(l * (l + 1)) : 1.0f;
 #pragma unroll
-          for (int i = 0; i < 32; ++i) D1[i] = (D1[i] + X[i]) * sdP;
+        for (int i = 0; i < 32; ++i) D1[i] *= sdP;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int pr = T.ct * (NC / 4) + cc0 / 4 + q;
-            if (pr >= npair || !valid) continue;
-            const int r = pr / s.nf, f = pr - r * s.nf;
-            const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
-            // A = sum F1_mine P, D = sum F2_mine P, C = sum F1_other dP, B = sum F2_other dP
-            const float Ar = D0[4 * q], Ai = D0[4 * q + 1], Dr = D0[4 * q + 2], Di = D0[4 * q + 3];
-            const float Cr = D1[4 * q], Ci = D1[4 * q + 1], Br = D1[4 * q + 2], Bi = D1[4 * q + 3];
-            double2 Sv = make_double2(f2d_int((dm * Ai + Br) * inv_ll), f2d_int((-dm * Ar + Bi) * inv_ll));
-            double2 Tv = make_double2(f2d_int((-Cr + dm * Di) * inv_ll), f2d_int((-Ci - dm * Dr) * inv_ll));
-            if (l > lc) { Sv = make_double2(0.0, 0.0); Tv = Sv; }
-            const long long o = (long long)r * s.f[f].out_ld + lm;
-            s.f[f].out0[o] = Sv;
-            s.f[f].out1[o] = Tv;
-          }
+        for (int q = 0; q < 8; ++q) {
+          const int pr = T.ct * (NC / 4) + cc0 / 4 + q;
+          if (pr >= npair) continue;
+          const int r = pr / s.nf, f = pr - r * s.nf;
+          const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+          // A = sum F1_mine P, D = sum F2_mine P, C = sum F1_other dP, B = sum F2_other dP
+          const float Ar = D0[4 * q], Ai = D0[4 * q + 1], Dr = D0[4 * q + 2], Di = D0[4 * q + 3];
+          const float Cr = D1[4 * q], Ci = D1[4 * q + 1], Br = D1[4 * q + 2], Bi = D1[4 * q + 3];
+          double2 Sv = make_double2(f2d_int((dm * Ai + Br) * inv_ll), f2d_int((-dm * Ar + Bi) * inv_ll));
+          double2 Tv = make_double2(f2d_int((-Cr + dm * Di) * inv_ll), f2d_int((-Ci - dm * Dr) * inv_ll));
+          if (l > lc) { Sv = make_double2(0.0, 0.0); Tv = Sv; }
+          const long long o = (long long)r * s.f[f].out_ld + lm;
+          s.f[f].out0[o] = Sv;
+          s.f[f].out1[o] = Tv;
         }
       }
-      tc::tc_fence_before();
-      tc::mbar_arrive(&acc_empty[abuf]);
-      ++acc_use;
     }
   }
   if (!ok) atomicExch(&s_fail, 1);
@@ -547,15 +559,15 @@ int num_sms() {
 template <bool VEC>
 cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, unsigned char* bimg,
                          cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NC = VEC ? 64 : 128, NA = VEC ? 3 : 4;
+  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = VEC ? 3 : 4, NB = VEC ? 2 : 3;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
-  const size_t psmem = 1024 + 3 * (size_t)NC * 128;
+  const size_t psmem = 1024 + 2 * 3 * (size_t)NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(pack_inv_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_inv_kernel<VEC><<<dim3(nct, g.n_m, 2 * tc_nch(g.l_max + 1)), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  pack_inv_kernel<VEC><<<dim3(nct, g.n_m, tc_nch(g.l_max + 1)), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
   CUDA_TRY(cudaGetLastError());
-  const size_t smem = 1024 + (size_t)NA * NT * 16384 + 2 * 3 * (size_t)NC * 128;
+  const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * 3 * NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
   const int grid = (int)std::min<long long>(ntiles, num_sms());
@@ -566,15 +578,15 @@ cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, u
 template <bool VEC>
 cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, unsigned char* bimg,
                          cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NC = VEC ? 64 : 128, NA = VEC ? 3 : 4;
+  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = VEC ? 3 : 4, NB = VEC ? 2 : 3;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
-  const size_t psmem = 1024 + 3 * (size_t)NC * 128;
+  const size_t psmem = 1024 + 2 * 3 * (size_t)NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(pack_fwd_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_fwd_kernel<VEC><<<dim3(nct, g.n_m, 2 * t.ncj), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  pack_fwd_kernel<VEC><<<dim3(nct, g.n_m, t.ncj), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
   CUDA_TRY(cudaGetLastError());
-  const size_t smem = 1024 + (size_t)NA * NT * 16384 + 2 * (size_t)NT * 3 * NC * 128;
+  const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * 3 * NC * 128;
   CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
   const int grid = (int)std::min<long long>(ntiles, num_sms());
@@ -585,7 +597,8 @@ cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, u
 }  // namespace
 
 size_t tcp_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool vec, bool inverse) {
-  const int NC = vec ? 64 : 128;
+  const int NC = kNC;
+  (void)vec;
   const long long nct = (ncplx + NC / 2 - 1) / (NC / 2);
   const long long tile = 3LL * NC * 128;
   if (inverse) return (size_t)(t.npc * nct * tile);

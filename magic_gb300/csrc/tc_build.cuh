@@ -142,3 +142,82 @@ __device__ __forceinline__ void fwd_build_tile(const ShtGeom& g, const FwdSet& s
     }
   }
 }
+
+// Both parity tiles of one 128-degree chunk c (degrees l = m + 128c + i,
+// i < 128): tile p (p = i & 1) at B + p * 3 * NC * 128, K index (i >> 1).
+// Lane holds i = lane + 32h (h < 4): each load instruction reads 32
+// consecutive spectral entries, and both parities of every fetched sector are
+// used.
+template <bool VEC, int NC, int CB>
+__device__ __forceinline__ void inv_build_pair(const ShtGeom& g, const InvSet& s, unsigned char* B, int ct,
+                                               int ncplx, int m, int lm0, int c, int ql0, int qstride,
+                                               int lane) {
+  constexpr uint32_t BT = NC * 128;
+  const int lmx = g.l_max - m;
+  for (int qb = ql0; qb < NC / 2; qb += CB * qstride) {
+    double2 a[CB][4], b[CB][4];
+    int opk[CB], lc[CB];
+    float o2[CB];
+#pragma unroll
+    for (int i = 0; i < CB; ++i) {
+      const int ql = qb + i * qstride;
+      const int q = ct * (NC / 2) + ql;
+      opk[i] = OP_ZERO;
+      lc[i] = -1;
+      o2[i] = 0.f;
+      if (ql < NC / 2 && q < ncplx) {
+        const int pair = VEC ? (q >> 1) : q;
+        const int r = pair / s.nf, f = pair - r * s.nf;
+        const SpecOperand& op = (VEC && (q & 1)) ? s.f[f].x1 : s.f[f].x0;
+        if (op.op != OP_ZERO && op.A != nullptr) {
+          opk[i] = op.op;
+          const double2* A = op.A + (long long)r * op.ld + lm0;  // indexed by l - m
+#pragma unroll
+          for (int h = 0; h < 4; ++h) a[i][h] = __ldg(A + min(128 * c + lane + 32 * h, lmx));
+          if (op.op == OP_CURLT && op.B != nullptr) {
+            const double2* Bp = op.B + (long long)r * op.ld + lm0;
+#pragma unroll
+            for (int h = 0; h < 4; ++h) b[i][h] = __ldg(Bp + min(128 * c + lane + 32 * h, lmx));
+            o2[i] = d2f_int(s.or2 ? s.or2[r] : s.or2_0);
+          } else if (op.op == OP_CURLT) {
+            opk[i] = OP_ZERO;
+          }
+          lc[i] = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+        }
+      }
+    }
+    const float dm = (float)m;
+    unsigned char* Bp = B + (lane & 1) * 3 * BT;  // this lane's parity tile
+#pragma unroll
+    for (int i = 0; i < CB; ++i) {
+      const int ql = qb + i * qstride;
+      if (ql >= NC / 2) break;
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const int k = (lane >> 1) + 16 * h;
+        const int l = m + 128 * c + lane + 32 * h;
+        float ar = 0.f, ai = 0.f;
+        if (opk[i] != OP_ZERO) {
+          ar = d2f_int(a[i][h].x);
+          ai = d2f_int(a[i][h].y);
+          const float ll = (float)(l * (l + 1));
+          if (opk[i] == OP_DLH) {
+            ar *= ll;
+            ai *= ll;
+          } else if (opk[i] == OP_CURLT) {
+            const float d = o2[i] * ll;
+            ar = fmaf(d, ar, -d2f_int(b[i][h].x));
+            ai = fmaf(d, ai, -d2f_int(b[i][h].y));
+          } else if (opk[i] == OP_IM) {
+            const float t0 = ar;
+            ar = -dm * ai;
+            ai = dm * t0;
+          }
+          if (l > lc[i]) { ar = 0.f; ai = 0.f; }
+        }
+        store_split1(Bp, tc::sw128_offset(2 * ql, k), ar, BT);
+        store_split1(Bp, tc::sw128_offset(2 * ql + 1, k), ai, BT);
+      }
+    }
+  }
+}

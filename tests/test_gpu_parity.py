@@ -343,11 +343,11 @@ def test_pipelined_host_levels_match_device_call(built, torch, prec):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("grid", [(63, 1, 96, 192), (64, 4, 96, 48), (255, 1, 384, 768)])
-def test_persistent_tensor_core_kernels_equal_tiled(built, torch, grid, monkeypatch):
-    """The persistent warp-specialized tensor-core kernels issue the same MMA
-    sequence per accumulator as the one-tile-per-CTA kernels: the radial-loop
-    set agrees bit for bit (ragged lcut and the odd-parity m = l_max tile
-    included)."""
+def test_persistent_tensor_core_kernels_match_tiled(built, torch, grid, monkeypatch):
+    """The persistent tensor-core kernels (stacked split products) and the
+    one-tile-per-CTA kernels both stay within the 3xBF16 tolerance of the FP64
+    form on the radial-loop set (ragged lcut and the odd-parity m = l_max
+    tile included), and agree with each other."""
     from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
     L, minc, N, P = grid
     n = 5 if L > 200 else 11
@@ -357,17 +357,23 @@ def test_persistent_tensor_core_kernels_equal_tiled(built, torch, grid, monkeypa
     lcut[1] = L - 7
     spec_d = {k: torch.from_numpy(v).cuda() for k, v in spec_np.items()}
     out = {}
-    for kern in ("tiled", "persistent"):
+    for kern, prec in (("tiled", "fp64"), ("tiled", "bf16x3"), ("persistent", "bf16x3")):
         monkeypatch.setenv("MAGIC_SHT_TC_KERNEL", kern)
-        s = make(L, minc, N, P, prec="bf16x3")
+        s = make(L, minc, N, P, prec=prec)
         g = s.transform_to_grid_space(spec_d, or2=or2, lcut=lcut)
-        fin = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
-        lm = s.transform_to_lm_space(fin, lcut=lcut)
+        if prec == "fp64":
+            fin = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
+        lm = s.transform_to_lm_space(fin, lcut=lcut)  # same grid inputs for every form
         torch.cuda.synchronize()
         s.device_status()
-        out[kern] = ({k: v.cpu() for k, v in g.items()}, {k: v.cpu() for k, v in lm.items()})
-    for a, b in zip(out["tiled"], out["persistent"]):
-        for k in a:
-            x, y = (torch.view_as_real(t) if t.is_complex() else t for t in (a[k], b[k]))
-            if not torch.equal(x, y):  # same MMA order: at most last-bit differences
-                assert rel_max(y.numpy(), x.numpy()) < 1e-6, k
+        out[(kern, prec)] = {**{k: v.cpu() for k, v in g.items()}, **{k: v.cpu() for k, v in lm.items()}}
+    ref = out[("tiled", "fp64")]
+    flat = lambda t: (torch.view_as_real(t) if t.is_complex() else t).numpy().ravel()
+    for k in ref:
+        tol = 1e-3 if k == "VStLM" else 2e-6  # VStLM: small output of a near-cancelling pair
+        a = flat(out[("tiled", "bf16x3")][k])
+        b = flat(out[("persistent", "bf16x3")][k])
+        r = flat(ref[k])
+        assert rel_l2(a, r) < tol, (k, rel_l2(a, r))
+        assert rel_l2(b, r) < tol, (k, rel_l2(b, r))
+        assert rel_l2(b, a) < 2 * tol, (k, rel_l2(b, a))
