@@ -130,6 +130,7 @@ struct TcTables {
   int* err;                   // device error word (bounded waits that gave up)
   const long long* bpc0;      // [n_m] first (parity, chunk) pair of each m in the synthesis data images
   long long npc;              // total (parity, chunk) pairs over all m
+  int* tile_ctr;              // tile counter of the persistent kernels (reset before each launch)
   int ntt;                    // theta tiles of 128 northern points
   int nlt;                    // l' tiles of 128 rows per parity
   int ncj;                    // theta chunks of 64 (analysis K)

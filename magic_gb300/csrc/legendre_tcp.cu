@@ -11,7 +11,7 @@
 //     One CTA builds the two tiles that share its input (both parities of a
 //     128-degree chunk; the ES and EA tiles of 64 colatitudes) and writes them
 //     with bulk copies.
-//  2. one persistent CTA per SM walks a static list of output tiles
+//  2. one persistent CTA per SM takes output tiles from a global counter
 //        synthesis tile = (m, parity, 128 colatitudes, 32 complex columns)
 //        analysis tile  = (m, parity, 128 degrees of that parity, 32 complex columns)
 //     with three roles:
@@ -66,6 +66,32 @@ __device__ __forceinline__ void drain_copies(uint64_t* full, uint32_t use) {
   for (uint32_t u = use > N ? use - N : 0; u < use; ++u) wait_full(&full[u % N], u, N);
 }
 
+// Dynamic tile schedule: the loader thread takes tile indices from a global
+// counter and publishes them, in order, through a small shared-memory ring
+// that the MMA thread and the epilogue threads consume (-1 ends the list).
+constexpr int kNTR = 4;
+struct TileRing {
+  int* idx;
+  uint64_t* full;   // count 1 (the loader)
+  uint64_t* empty;  // count 1 + kEpiThreads (MMA thread and epilogue threads)
+};
+__device__ __forceinline__ bool ring_push(const TileRing& R, uint32_t& use, int ix) {
+  const uint32_t slot = use % kNTR;
+  if (!wait_empty(&R.empty[slot], use, kNTR)) return false;
+  R.idx[slot] = ix;
+  tc::mbar_arrive(&R.full[slot]);
+  ++use;
+  return true;
+}
+__device__ __forceinline__ bool ring_pop(const TileRing& R, uint32_t& use, int& ix) {
+  const uint32_t slot = use % kNTR;
+  if (!wait_full(&R.full[slot], use, kNTR)) return false;
+  ix = R.idx[slot];
+  tc::mbar_arrive(&R.empty[slot]);
+  ++use;
+  return true;
+}
+
 // Issue the MMAs of table split `sp` (NT tables) against the stacked data
 // splits; D holds NT accumulator groups of 3*kNC columns.
 template <int NT>
@@ -109,7 +135,7 @@ __device__ __forceinline__ void drain_sum(uint32_t col, float (&v)[32]) {
 // Synthesis data images: [pc = bpc0[m] + p*nch + c][ct] tiles of 3 splits.
 // One CTA builds both parity tiles of chunk c from 128 consecutive degrees.
 template <bool VEC>
-__global__ void __launch_bounds__(kPackThreads, 2) pack_inv_kernel(const ShtGeom g, const InvSet s,
+__global__ void __launch_bounds__(kPackThreads, 4) pack_inv_kernel(const ShtGeom g, const InvSet s,
                                                                   const TcTables t,
                                                                   unsigned char* __restrict__ bimg, int nct) {
   constexpr int NC = kNC;
@@ -122,7 +148,7 @@ __global__ void __launch_bounds__(kPackThreads, 2) pack_inv_kernel(const ShtGeom
   if (c >= nch) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  inv_build_pair<VEC, NC, 2>(g, s, B, ct, ncplx, m, g.lmoff[mc], c, warp, kPackThreads / 32, lane);
+  inv_build_pair<VEC, NC, 1>(g, s, B, ct, ncplx, m, g.lmoff[mc], c, warp, kPackThreads / 32, lane);
   tc::fence_proxy_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -187,6 +213,8 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
   constexpr uint32_t ACC = NT * 3 * NC;
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[NACC], acc_empty[NACC], fin;
+  __shared__ uint64_t tr_full[kNTR], tr_empty[kNTR];
+  __shared__ int tr_idx[kNTR];
   __shared__ uint32_t tmem_base;
   __shared__ int s_fail;
   unsigned char* base = align1k(smem_raw);
@@ -202,6 +230,7 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
     for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
     for (int i = 0; i < NACC; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
     tc::mbar_init(&fin, 1);
+    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], 1 + kEpiThreads); }
     s_fail = 0;
     tc::fence_mbar_init();
   }
@@ -213,15 +242,21 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_base;
+  const TileRing R{tr_idx, tr_full, tr_empty};
   bool ok = true;
   InvTile T;
 
   if (warp == 0) {
     if (lane == 0) {  // ---------------------------------------- loader
-      uint32_t a_use = 0, b_use = 0;
-      for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+      uint32_t a_use = 0, b_use = 0, tr = 0;
+      int ix = blockIdx.x;
+      while (ok) {
+        if (!ring_push(R, tr, ix < ntiles ? ix : -1)) { ok = false; break; }
+        if (ix >= ntiles) break;
+        const int next = atomicAdd(t.tile_ctr, 1) + (int)gridDim.x;
         T.decode(g, t, nct, ix);
-        if (T.nlp == 0 || T.ct * (NC / 2) >= ncplx) continue;
+        ix = next;
+        if (T.nlp == 0) continue;
         for (int c = 0; c < T.nchp && ok; ++c) {
           const uint32_t bslot = b_use % NB;
           if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
@@ -246,10 +281,13 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
     }
   } else if (warp == 1) {
     if (lane == 0) {  // ---------------------------------------- MMA issuer
-      uint32_t a_use = 0, b_use = 0, acc_use = 0;
-      for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+      uint32_t a_use = 0, b_use = 0, acc_use = 0, tr = 0;
+      while (ok) {
+        int ix;
+        if (!ring_pop(R, tr, ix)) { ok = false; break; }
+        if (ix < 0) break;
         T.decode(g, t, nct, ix);
-        if (T.nlp == 0 || T.ct * (NC / 2) >= ncplx) continue;
+        if (T.nlp == 0) continue;
         const uint32_t abuf = acc_use % NACC;
         if (!wait_empty(&acc_empty[abuf], acc_use, NACC)) { ok = false; break; }
         tc::tc_fence_after();
@@ -279,10 +317,12 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
     const int jl = 32 * q4 + lane;
     const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
     const int NHP = t.ntt * 128;
-    uint32_t acc_use = 0;
-    for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+    uint32_t acc_use = 0, tr = 0;
+    while (ok) {
+      int ix;
+      if (!ring_pop(R, tr, ix)) { ok = false; break; }
+      if (ix < 0) break;
       T.decode(g, t, nct, ix);
-      if (T.ct * (NC / 2) >= ncplx) continue;
       const int jg = T.tt * 128 + jl;
       const long long per_p = VEC ? 2LL * g.nh : (long long)g.nh;
       auto optr = [&](void* bp, int r, int f, int ef) -> float2* {
@@ -388,6 +428,8 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
   constexpr uint32_t ACC = NT * 3 * NC;
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[NACC], acc_empty[NACC], fin;
+  __shared__ uint64_t tr_full[kNTR], tr_empty[kNTR];
+  __shared__ int tr_idx[kNTR];
   __shared__ uint32_t tmem_base;
   __shared__ int s_fail;
   unsigned char* base = align1k(smem_raw);
@@ -403,6 +445,7 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
     for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
     for (int i = 0; i < NACC; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
     tc::mbar_init(&fin, 1);
+    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], 1 + kEpiThreads); }
     s_fail = 0;
     tc::fence_mbar_init();
   }
@@ -414,15 +457,21 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_base;
+  const TileRing R{tr_idx, tr_full, tr_empty};
   bool ok = true;
   FwdTile T;
 
   if (warp == 0) {
     if (lane == 0) {
-      uint32_t a_use = 0, b_use = 0;
-      for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+      uint32_t a_use = 0, b_use = 0, tr = 0;
+      int ix = blockIdx.x;
+      while (ok) {
+        if (!ring_push(R, tr, ix < ntiles ? ix : -1)) { ok = false; break; }
+        if (ix >= ntiles) break;
+        const int next = atomicAdd(t.tile_ctr, 1) + (int)gridDim.x;
         T.decode(g, t, nct, ix);
-        if (T.lt * 128 >= T.nlp || T.ct * (NC / 2) >= ncplx) continue;
+        ix = next;
+        if (T.lt * 128 >= T.nlp) continue;
         for (int c = 0; c < t.ncj && ok; ++c) {
           const uint32_t bslot = b_use % NB;
           if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
@@ -448,10 +497,13 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      uint32_t a_use = 0, b_use = 0, acc_use = 0;
-      for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+      uint32_t a_use = 0, b_use = 0, acc_use = 0, tr = 0;
+      while (ok) {
+        int ix;
+        if (!ring_pop(R, tr, ix)) { ok = false; break; }
+        if (ix < 0) break;
         T.decode(g, t, nct, ix);
-        if (T.lt * 128 >= T.nlp || T.ct * (NC / 2) >= ncplx) continue;
+        if (T.lt * 128 >= T.nlp) continue;
         const uint32_t abuf = acc_use % NACC;
         if (!wait_empty(&acc_empty[abuf], acc_use, NACC)) { ok = false; break; }
         tc::tc_fence_after();
@@ -479,10 +531,13 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
     const int cc0 = half * (NC / 2);
     const int lr = 32 * q4 + lane;
     const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
-    uint32_t acc_use = 0;
-    for (int ix = blockIdx.x; ix < ntiles && ok; ix += gridDim.x) {
+    uint32_t acc_use = 0, tr = 0;
+    while (ok) {
+      int ix;
+      if (!ring_pop(R, tr, ix)) { ok = false; break; }
+      if (ix < 0) break;
       T.decode(g, t, nct, ix);
-      if (T.lt * 128 >= T.nlp || T.ct * (NC / 2) >= ncplx) continue;
+      if (T.lt * 128 >= T.nlp) continue;
       const uint32_t abuf = acc_use % NACC;
       if (!wait_full(&acc_full[abuf], acc_use, NACC)) { ok = false; break; }
       tc::tc_fence_after();
@@ -571,6 +626,7 @@ cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, u
   CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
   const int grid = (int)std::min<long long>(ntiles, num_sms());
+  CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
   inv_leg_tcp<VEC><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
   return cudaGetLastError();
 }
@@ -590,6 +646,7 @@ cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, u
   CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
   const int grid = (int)std::min<long long>(ntiles, num_sms());
+  CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
   fwd_leg_tcp<VEC><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
   return cudaGetLastError();
 }

@@ -69,6 +69,7 @@ struct magic_sht_handle {
   long long* d_inv_blk0 = nullptr;
   long long* d_fwd_blk0 = nullptr;
   long long* d_bpc0 = nullptr;
+  int* d_tile_ctr = nullptr;
   unsigned char* d_bimg = nullptr;  // data-operand images of the persistent tensor-core kernels
   size_t bimg_bytes = 0;
   float* d_inv_scale = nullptr;
@@ -82,6 +83,10 @@ struct magic_sht_handle {
   char* stage = nullptr;
   size_t stage_bytes = 0;
   cudaStream_t cpy_in = nullptr, cpy_out = nullptr;
+  // tensor-core form: FFTs of one field group on a second stream, overlapping
+  // the other group's Legendre kernels (joined back by events)
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
   // per-phase CUDA-event timing (magic_sht_set_profiling)
   bool profiling = false;
@@ -364,6 +369,12 @@ SpecOperand make_operand(const CallCtx& cx, const SpecRef& r, long long ld) {
   return o;
 }
 
+// Field groups overlap on two streams in the persistent tensor-core form
+// (not while per-phase profiling, whose event pairs assume one stream).
+bool overlap_groups(const magic_sht_handle* h) {
+  return tc_form(h) && h->tc_persistent && !h->profiling && h->aux;
+}
+
 // Synthesis: Legendre sums into half spectra, then inverse FFTs.  The
 // half-spectrum temporaries must have been registered in `cx` before
 // prepare(); `hs` holds their ctx indices (one per output grid, in order).
@@ -378,10 +389,11 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
   const double* d_or2 = (const double*)cx.dev(lv.or2_idx);
   FftSet fs{};
   fs.nlev = lv.nlev;
+  cudaStream_t fft_st = h->stream;
   auto flush_fft = [&]() -> int {
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_INV);
-      CK(launch_fft_inverse(g, fs, f64, h->stream));
+      CK(launch_fft_inverse(g, fs, f64, fft_st));
       fs.nf = 0;
     }
     return MAGIC_SHT_OK;
@@ -406,6 +418,16 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     if (h->precision == MAGIC_SHT_BF16X3) TRY(inv_tc(h, g, s, false));
     else CK(launch_inv_legendre_simt(g, s, false, f64, h->stream));
   }
+  const bool ovl = overlap_groups(h) && !sc.empty() && !vc.empty();
+  if (ovl) {  // scalar FFTs on the second stream while the vector Legendre sums run
+    CK(cudaEventRecord(h->ev_fork, h->stream));
+    CK(cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
+    fft_st = h->aux;
+    for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
+    TRY(flush_fft());
+    CK(cudaEventRecord(h->ev_join, h->aux));
+    fft_st = h->stream;
+  }
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
     InvSet s{};
     s.nlev = lv.nlev; s.lcut = d_lcut; s.or2 = d_or2; s.lcut0 = lv.lcut0; s.or2_0 = lv.or2_0;
@@ -419,57 +441,23 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     if (h->precision == MAGIC_SHT_BF16X3) TRY(inv_tc(h, g, s, true));
     else CK(launch_inv_legendre_simt(g, s, true, f64, h->stream));
   }
-  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
+  if (!ovl)
+    for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
   for (size_t i = 0; i < vc.size(); ++i) {
     TRY(add_fft(cx.dev(hs_vc[2 * i]), vc[i].out_t, vc[i].flags | flag_v, hs_ld_v));
     TRY(add_fft(cx.dev(hs_vc[2 * i + 1]), vc[i].out_p, vc[i].flags | flag_v, hs_ld_v));
   }
-  return flush_fft();
+  TRY(flush_fft());
+  if (ovl) CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+  return MAGIC_SHT_OK;
 }
 
-// Analysis: forward FFTs into ES/EA half spectra, then Legendre sums.
-int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
-                const std::vector<ScalarFwd>& sc, const std::vector<VectorFwd>& vc,
-                const std::vector<int>& hs_sc, const std::vector<int>& hs_vc) {
+// Vector Legendre analysis of the radial set (after the vector FFTs).
+int run_forward_vectors(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv, const std::vector<VectorFwd>& vc,
+                        const std::vector<int>& hs_vc, const int* d_lcut) {
   const ShtGeom& g = h->g;
   const long long hs_ld = (long long)g.n_m * g.n_theta;
   const bool f64 = fp64_pipes(h);
-  const int* d_lcut = (const int*)cx.dev(lv.lcut_idx);
-  FftSet fs{};
-  fs.nlev = lv.nlev;
-  auto flush_fft = [&]() -> int {
-    if (fs.nf) {
-      PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_FWD);
-      CK(launch_fft_forward(g, fs, f64, h->stream));
-      fs.nf = 0;
-    }
-    return MAGIC_SHT_OK;
-  };
-  auto add_fft = [&](int in_idx, void* out, int flags) -> int {
-    if (fs.nf == MAGIC_MAX_FIELDS) TRY(flush_fft());
-    FftField& f = fs.f[fs.nf++];
-    f.in = cx.dev(in_idx); f.out = out; f.in_ld = lv.grid_ld; f.out_ld = hs_ld;
-    f.flags = flags; f.pad_ = 0;
-    return MAGIC_SHT_OK;
-  };
-  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(sc[i].in, cx.dev(hs_sc[i]), FFT_WEIGHT));
-  for (size_t i = 0; i < vc.size(); ++i) {
-    TRY(add_fft(vc[i].in_t, cx.dev(hs_vc[2 * i]), FFT_WEIGHT | FFT_OSIN2));
-    TRY(add_fft(vc[i].in_p, cx.dev(hs_vc[2 * i + 1]), FFT_WEIGHT | FFT_OSIN2));
-  }
-  TRY(flush_fft());
-  for (size_t i0 = 0; i0 < sc.size(); i0 += MAGIC_MAX_FIELDS) {
-    FwdSet s{};
-    s.nlev = lv.nlev; s.lcut = d_lcut; s.lcut0 = lv.lcut0;
-    for (size_t i = i0; i < sc.size() && i < i0 + MAGIC_MAX_FIELDS; ++i) {
-      FwdField& f = s.f[s.nf++];
-      f.in0 = cx.dev(hs_sc[i]); f.in1 = nullptr; f.in_ld = hs_ld;
-      f.out0 = (double2*)cx.dev(sc[i].out); f.out1 = nullptr; f.out_ld = lv.spec_ld;
-    }
-    PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_SCALAR);
-    if (h->precision == MAGIC_SHT_BF16X3) TRY(fwd_tc(h, g, s, false));
-    else CK(launch_fwd_legendre_simt(g, s, false, f64, h->stream));
-  }
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
     FwdSet s{};
     s.nlev = lv.nlev; s.lcut = d_lcut; s.lcut0 = lv.lcut0;
@@ -484,6 +472,69 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     if (h->precision == MAGIC_SHT_BF16X3) TRY(fwd_tc(h, g, s, true));
     else CK(launch_fwd_legendre_simt(g, s, true, f64, h->stream));
   }
+  return MAGIC_SHT_OK;
+}
+
+// Analysis: forward FFTs into ES/EA half spectra, then Legendre sums.
+int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
+                const std::vector<ScalarFwd>& sc, const std::vector<VectorFwd>& vc,
+                const std::vector<int>& hs_sc, const std::vector<int>& hs_vc) {
+  const ShtGeom& g = h->g;
+  const long long hs_ld = (long long)g.n_m * g.n_theta;
+  const bool f64 = fp64_pipes(h);
+  const int* d_lcut = (const int*)cx.dev(lv.lcut_idx);
+  FftSet fs{};
+  fs.nlev = lv.nlev;
+  cudaStream_t fft_st = h->stream;
+  auto flush_fft = [&]() -> int {
+    if (fs.nf) {
+      PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_FWD);
+      CK(launch_fft_forward(g, fs, f64, fft_st));
+      fs.nf = 0;
+    }
+    return MAGIC_SHT_OK;
+  };
+  auto add_fft = [&](int in_idx, void* out, int flags) -> int {
+    if (fs.nf == MAGIC_MAX_FIELDS) TRY(flush_fft());
+    FftField& f = fs.f[fs.nf++];
+    f.in = cx.dev(in_idx); f.out = out; f.in_ld = lv.grid_ld; f.out_ld = hs_ld;
+    f.flags = flags; f.pad_ = 0;
+    return MAGIC_SHT_OK;
+  };
+  // with two streams: scalar FFTs on the second stream while the vector FFTs
+  // and vector Legendre sums run; the scalar Legendre sums follow the join
+  const bool ovl = overlap_groups(h) && !sc.empty() && !vc.empty();
+  if (ovl) {
+    CK(cudaEventRecord(h->ev_fork, h->stream));
+    CK(cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
+    fft_st = h->aux;
+  }
+  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(sc[i].in, cx.dev(hs_sc[i]), FFT_WEIGHT));
+  if (ovl) {
+    TRY(flush_fft());
+    CK(cudaEventRecord(h->ev_join, h->aux));
+    fft_st = h->stream;
+  }
+  for (size_t i = 0; i < vc.size(); ++i) {
+    TRY(add_fft(vc[i].in_t, cx.dev(hs_vc[2 * i]), FFT_WEIGHT | FFT_OSIN2));
+    TRY(add_fft(vc[i].in_p, cx.dev(hs_vc[2 * i + 1]), FFT_WEIGHT | FFT_OSIN2));
+  }
+  TRY(flush_fft());
+  if (ovl) TRY(run_forward_vectors(h, cx, lv, vc, hs_vc, d_lcut));
+  if (ovl) CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+  for (size_t i0 = 0; i0 < sc.size(); i0 += MAGIC_MAX_FIELDS) {
+    FwdSet s{};
+    s.nlev = lv.nlev; s.lcut = d_lcut; s.lcut0 = lv.lcut0;
+    for (size_t i = i0; i < sc.size() && i < i0 + MAGIC_MAX_FIELDS; ++i) {
+      FwdField& f = s.f[s.nf++];
+      f.in0 = cx.dev(hs_sc[i]); f.in1 = nullptr; f.in_ld = hs_ld;
+      f.out0 = (double2*)cx.dev(sc[i].out); f.out1 = nullptr; f.out_ld = lv.spec_ld;
+    }
+    PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_SCALAR);
+    if (h->precision == MAGIC_SHT_BF16X3) TRY(fwd_tc(h, g, s, false));
+    else CK(launch_fwd_legendre_simt(g, s, false, f64, h->stream));
+  }
+  if (!ovl) TRY(run_forward_vectors(h, cx, lv, vc, hs_vc, d_lcut));
   return MAGIC_SHT_OK;
 }
 
@@ -662,6 +713,9 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     }                                                                                  \
   } while (0)
   INIT_CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  INIT_CK(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+  INIT_CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+  INIT_CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   h->own_stream = true;
   const size_t tab = (size_t)K * g.nh;
   INIT_CK(cudaMalloc((void**)&h->d_lmoff, sizeof(int) * n_m));
@@ -724,6 +778,8 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
       t.npc += 2LL * tc_nch(L - mc * minc + 1);
     }
     INIT_CK(cudaMalloc((void**)&h->d_bpc0, sizeof(long long) * n_m));
+    INIT_CK(cudaMalloc((void**)&h->d_tile_ctr, 256));
+    t.tile_ctr = h->d_tile_ctr;
     INIT_CK(cudaMemcpy(h->d_bpc0, pc.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
     t.bpc0 = h->d_bpc0;
     INIT_CK(cudaMemset(h->d_fwd_scale, 0, sizeof(float) * 2 * (size_t)K));
@@ -746,7 +802,7 @@ int magic_sht_finalize(magic_sht_handle* h) {
   void* ptrs[] = {h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP, h->d_wgt, h->d_osin2,
                   h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws, h->d_inv_img, h->d_fwd_img,
                   h->d_inv_blk0, h->d_fwd_blk0, h->d_inv_scale, h->d_fwd_scale, h->d_err,
-                  h->d_bpc0, h->d_bimg};
+                  h->d_bpc0, h->d_bimg, h->d_tile_ctr};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->stage) cudaFree(h->stage);
@@ -756,6 +812,9 @@ int magic_sht_finalize(magic_sht_handle* h) {
     if (h->ev_out[i]) cudaEventDestroy(h->ev_out[i]);
   }
   if (h->cpy_in) cudaStreamDestroy(h->cpy_in);
+  if (h->aux) cudaStreamDestroy(h->aux);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->cpy_out) cudaStreamDestroy(h->cpy_out);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
