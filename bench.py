@@ -149,7 +149,7 @@ def reference_arm(args):
         return
     import numpy as np
     from oracle import oracle
-    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    from magic_gb300.workload import grid_space_inputs, or2_levels
     oracle.build_oracle()
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
@@ -159,6 +159,9 @@ def reference_arm(args):
     or2 = or2_levels(N_LEVELS)
 
     def one_level(r):
+        """Both transform sets of level r; returns the seconds spent in them
+        (the nonlinear products between the sets are not timed, as on the GPU)."""
+        t0 = time.perf_counter()
         g = {}
         g["sc"] = o.scal_to_spat(spec["s"][r])
         g["pc"] = o.scal_to_spat(spec["p"][r])
@@ -169,19 +172,19 @@ def reference_arm(args):
         g["brc"], g["btc"], g["bpc"] = o.torpol_to_spat(spec["b"][r], spec["db"][r], spec["aj"][r])
         g["cbrc"], g["cbtc"], g["cbpc"] = o.torpol_to_curl_spat(or2[r], spec["b"][r], spec["ddb"][r],
                                                                 spec["aj"][r], spec["dj"][r])
-        f = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
+        t1 = time.perf_counter()
+        f = {k: v[0] for k, v in oracle.get_nl({k: v[None] for k, v in g.items()}, or2[r:r + 1], N_THETA).items()}
+        t2 = time.perf_counter()
         for pre in ("Adv", "VS", "VxB"):
             o.spat_to_qst(f[pre + "r"], f[pre + "t"], f[pre + "p"])
         o.scal_to_SH(f["heatTerms"])
+        return (t1 - t0) + (time.perf_counter() - t2)
 
     for w in range(args.warmup):
         one_level(w % N_LEVELS)
     times = []
     for k in range(args.steps):
-        t0 = time.perf_counter()
-        for i in range(n):
-            one_level((k * n + i) % N_LEVELS)
-        times.append(time.perf_counter() - t0)
+        times.append(sum(one_level((k * n + i) % N_LEVELS) for i in range(n)))
     total = sum(times)
     v = n * args.steps / total
     line = {
@@ -237,7 +240,7 @@ def our_arm(args):
     from magic_gb300 import build as b
     b.build()
     from magic_gb300 import SHT, measure_gflops, _lib
-    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    from magic_gb300.workload import grid_space_inputs, or2_levels
 
     dev = torch.device("cuda", local)
     hbm, bf16, peak_kind = peaks()
@@ -252,12 +255,13 @@ def our_arm(args):
 
     spec_np = grid_space_inputs(L_MAX, MINC, N_LEVELS, seed=1234 + 7919 * rank)
     spec = {k: torch.from_numpy(v).to(dev) for k, v in spec_np.items()}
-    or2 = torch.from_numpy(or2_levels(N_LEVELS)).to(dev)
+    or2_np = or2_levels(N_LEVELS)
+    or2 = torch.from_numpy(or2_np).to(dev)
+    fin = {}  # analysis inputs: nonlinear products of the FP64 synthesis grids (set below)
 
     def run_set(s, out_g, out_s):
         g = s.transform_to_grid_space(spec, or2=or2, out=out_g)
-        f = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
-        return g, s.transform_to_lm_space(f, out=out_s)
+        return g, s.transform_to_lm_space(fin, out=out_s)
 
     def barrier():
         if world > 1:
@@ -282,8 +286,11 @@ def our_arm(args):
             ms = float(t.item())
         return ms, launches
 
-    # ---- FP64 form
+    # ---- FP64 form; its synthesis grids give the analysis inputs of both forms
+    # (the grid-space nonlinear products of get_nl, outside the timed steps)
     s64 = SHT(L_MAX, MINC, N_THETA, N_PHI, precision="fp64", device=local)
+    fin.update(s64.get_nl(s64.transform_to_grid_space(spec, or2=or2), or2=or2_np))
+    torch.cuda.synchronize()
     k64 = max(1, min(args.steps, 3))
     if not args.only_reduced:
         g64, l64 = run_set(s64, None, None)
@@ -324,6 +331,21 @@ def our_arm(args):
         errs[k] = float(torch.linalg.vector_norm(lmx[k] - l64[k]) / torch.linalg.vector_norm(l64[k]))
     max_err = max(errs.values())
     maxabs = max(float((gm[k] - g64[k]).abs().max() / g64[k].abs().max()) for k in g64)
+    # normwise over the outputs of one call (a vector field's three grids, or the
+    # q, s, t of one spat_to_qst): insensitive to one output being much smaller
+    # than its partners
+    groups = {"v": ("vrc", "vtc", "vpc"), "curl v": ("cvrc", "cvtc", "cvpc"), "b": ("brc", "btc", "bpc"),
+              "curl b": ("cbrc", "cbtc", "cbpc"), "Adv": ("AdvrLM", "AdvtLM", "AdvpLM"),
+              "VS": ("VSrLM", "VStLM", "VSpLM"), "VxB": ("VxBrLM", "VxBtLM", "VxBpLM")}
+    allm = {**{k: (gm[k], g64[k]) for k in g64}, **{k: (lmx[k], l64[k]) for k in l64}}
+    normwise = {}
+    for name, ks in groups.items():
+        num = sum(float(torch.linalg.vector_norm(allm[k][0] - allm[k][1])) ** 2 for k in ks)
+        den = sum(float(torch.linalg.vector_norm(allm[k][1])) ** 2 for k in ks)
+        normwise[name] = (num / den) ** 0.5
+    for k in ("sc", "pc", "xic", "heatTermsLM"):
+        normwise[k] = errs[k]
+    max_normwise = max(normwise.values())
 
     # ---- per-phase kernel timing (CUDA events on the launching stream)
     sm.set_profiling(True)
@@ -386,10 +408,11 @@ def our_arm(args):
         hg = {k: torch.empty(tuple(v.shape), dtype=torch.float64, pin_memory=True) for k, v in gm.items()}
         hl = {k: torch.empty(tuple(v.shape), dtype=torch.complex128, pin_memory=True) for k, v in lmx.items()}
 
+        hfin = {k: v.cpu().pin_memory() for k, v in fin.items()}
+
         def host_set():
-            g = sm.transform_to_grid_space(hspec, or2=hor2, out=hg)
-            f = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
-            sm.transform_to_lm_space(f, out=hl)
+            sm.transform_to_grid_space(hspec, or2=hor2, out=hg)
+            sm.transform_to_lm_space(hfin, out=hl)
 
         host_set()
         barrier()
@@ -404,7 +427,7 @@ def our_arm(args):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             dt = float(t.item())
         h2d = sum(v.numel() * v.element_size() for v in hspec.values()) + \
-            sum(hg[v].numel() * 8 for v in FORWARD_FROM_INVERSE.values())
+            sum(v.numel() * 8 for v in hfin.values())
         d2h = sum(v.numel() * 8 for v in hg.values()) + sum(v.numel() * 16 for v in hl.values())
         e2e = {"value": world * N_LEVELS * ke / dt, "unit": "levels/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": ke}
@@ -428,7 +451,8 @@ def our_arm(args):
                          "steps": k64, "legendre_frac_of_fp64_peak": fp64_leg_frac,
                          "phases": phases64},
             "speedup_vs_fp64_gpu": value / lev64,
-            "rel_l2_vs_fp64": {"max": max_err, "max_abs_over_max": maxabs, "per_field": errs},
+            "rel_l2_vs_fp64": {"max": max_err, "max_abs_over_max": maxabs, "per_field": errs,
+                               "max_normwise_per_call": max_normwise, "normwise_per_call": normwise},
             "roofline": roof,
             "phases": phases,
             "peaks": {"fp64_gflops": fp64_peak, "fp32_gflops": fp32_peak, "hbm_gbs": hbm,

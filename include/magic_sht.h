@@ -179,6 +179,19 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n_levels, const d
 int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n_levels, const int* lcut,
                                     const magic_sht_lm_space_args* a);
 
+/* ---- grid-space nonlinear products between the two transform sets
+ * (get_nl.f90:213-441 and the Lorentz-force addition of rIter.f90:650-655).
+ * Reads the grids transform_to_grid_space writes (vrc..vpc, cvrc..cvpc,
+ * brc..bpc, cbrc..cbpc, sc of `g`) and writes the grids
+ * transform_to_lm_space reads (Advr..heatTerms of `nl`; their const
+ * qualifiers are cast away: they are this call's outputs).  Boussinesq form,
+ * curl-form advection, magnetic field and heat equation on, unit physical
+ * constants; heatTerms receives the ohmic losses.  Device pointers only,
+ * 16-byte aligned, even grid_ld and nlat_padded; or2 = 1/r^2 per level (host
+ * or device array of n_levels; NULL = 1).  FP64 in every precision form. */
+int magic_sht_get_nl(magic_sht_handle* h, int n_levels, const double* or2, const magic_sht_grid_space_args* g,
+                     const magic_sht_lm_space_args* nl);
+
 /* ---- CUDA-graph capture of a device-pointer call sequence on the handle's
  * stream (e.g. the radial loop's transform set), replayed with one launch. */
 int magic_sht_graph_begin(magic_sht_handle* h);

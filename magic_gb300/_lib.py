@@ -31,6 +31,8 @@ class Desc(ctypes.Structure):
                 ("device", ctypes.c_int)]
 
 
+# grids read and written by magic_sht_get_nl (nl.cu)
+NL_IN = ["vrc", "vtc", "vpc", "cvrc", "cvtc", "cvpc", "brc", "btc", "bpc", "cbrc", "cbtc", "cbpc", "sc"]
 GRID_SPACE_IN = ["s", "p", "xi", "w", "dw", "ddw", "z", "dz", "b", "db", "ddb", "aj", "dj"]
 GRID_SPACE_OUT = ["sc", "pc", "xic", "vrc", "vtc", "vpc", "cvrc", "cvtc", "cvpc",
                   "brc", "btc", "bpc", "cbrc", "cbtc", "cbpc"]
@@ -81,6 +83,7 @@ SIGNATURES = {
     "magic_sht_transform_to_grid_space": [_V, ctypes.c_int, _V, _V,
                                           ctypes.POINTER(GridSpaceArgs)],
     "magic_sht_transform_to_lm_space": [_V, ctypes.c_int, _V, ctypes.POINTER(LmSpaceArgs)],
+    "magic_sht_get_nl": [_V, ctypes.c_int, _V, ctypes.POINTER(GridSpaceArgs), ctypes.POINTER(LmSpaceArgs)],
     "magic_sht_graph_begin": [_V],
     "magic_sht_graph_end": [_V, ctypes.POINTER(_V)],
     "magic_sht_graph_launch": [_V, _V],

@@ -136,6 +136,17 @@ struct TcTables {
   int ncj;                    // theta chunks of 64 (analysis K)
 };
 
+// grids of the nonlinear products (nl.cu): inputs from the synthesis set,
+// outputs for the analysis set; ld = doubles between levels
+enum NlIn : int { NL_VR, NL_VT, NL_VP, NL_CVR, NL_CVT, NL_CVP, NL_BR, NL_BT, NL_BP,
+                  NL_CBR, NL_CBT, NL_CBP, NL_S, NL_NIN };
+enum NlOut : int { NL_ADVR, NL_ADVT, NL_ADVP, NL_VSR, NL_VST, NL_VSP, NL_VXBR, NL_VXBT, NL_VXBP,
+                   NL_HEAT, NL_NOUT };
+struct NlGrids {
+  double* p[NL_NIN];
+  long long ld;
+};
+
 __host__ __device__ inline int tc_nch(int n_l) { return ((n_l + 1) / 2 + 63) / 64; }
 
 #define CUDA_TRY(x)                                                        \

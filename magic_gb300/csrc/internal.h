@@ -43,3 +43,7 @@ cudaError_t launch_inv_legendre_tcp(const ShtGeom& g, const InvSet& s, bool vec,
                                     unsigned char* bimg, cudaStream_t st);
 cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
                                     unsigned char* bimg, cudaStream_t st);
+
+// nl.cu
+cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& out, const double* or2,
+                          double or2_0, int nlev, cudaStream_t st);

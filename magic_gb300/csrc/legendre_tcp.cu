@@ -42,6 +42,13 @@ namespace {
 
 constexpr int kNC = 64;  // real data columns per tile (32 complex)
 
+// ring depths: A = table splits (NT x 16 KB per slot), B = data tiles
+template <bool VEC, bool INV>
+struct Rings {
+  static constexpr int NA = VEC ? 3 : 4;
+  static constexpr int NB = VEC ? 2 : 3;
+};
+
 constexpr int kThreads = 320;     // 10 warps
 constexpr int kEpiThreads = 256;  // warps 2..9
 constexpr int kPackThreads = 256;
@@ -205,8 +212,8 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
                                                            const unsigned char* __restrict__ bimg, int nct) {
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NC = kNC;
-  constexpr int NA = VEC ? 3 : 4;
-  constexpr int NB = VEC ? 2 : 3;
+  constexpr int NA = Rings<VEC, true>::NA;
+  constexpr int NB = Rings<VEC, true>::NB;
   constexpr int NACC = VEC ? 1 : 2;  // accumulator sets (3*NC columns per table)
   constexpr int BSZ = 3 * NC * 128;
   constexpr int ASZ = NT * 16384;
@@ -419,8 +426,8 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
                                                            const unsigned char* __restrict__ bimg, int nct) {
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NC = kNC;
-  constexpr int NA = VEC ? 3 : 4;
-  constexpr int NB = VEC ? 2 : 3;
+  constexpr int NA = Rings<VEC, false>::NA;
+  constexpr int NB = Rings<VEC, false>::NB;
   constexpr int NACC = VEC ? 1 : 2;
   constexpr int TS = 3 * NC * 128;  // one data operand (3 splits)
   constexpr int ASZ = NT * 16384;
@@ -614,7 +621,7 @@ int num_sms() {
 template <bool VEC>
 cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, unsigned char* bimg,
                          cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = VEC ? 3 : 4, NB = VEC ? 2 : 3;
+  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, true>::NA, NB = Rings<VEC, true>::NB;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
@@ -634,7 +641,7 @@ cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, u
 template <bool VEC>
 cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, unsigned char* bimg,
                          cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = VEC ? 3 : 4, NB = VEC ? 2 : 3;
+  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, false>::NA, NB = Rings<VEC, false>::NB;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (ncplx + NC / 2 - 1) / (NC / 2);

@@ -83,10 +83,6 @@ struct magic_sht_handle {
   char* stage = nullptr;
   size_t stage_bytes = 0;
   cudaStream_t cpy_in = nullptr, cpy_out = nullptr;
-  // tensor-core form: FFTs of one field group on a second stream, overlapping
-  // the other group's Legendre kernels (joined back by events)
-  cudaStream_t aux = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
   // per-phase CUDA-event timing (magic_sht_set_profiling)
   bool profiling = false;
@@ -369,12 +365,6 @@ SpecOperand make_operand(const CallCtx& cx, const SpecRef& r, long long ld) {
   return o;
 }
 
-// Field groups overlap on two streams in the persistent tensor-core form
-// (not while per-phase profiling, whose event pairs assume one stream).
-bool overlap_groups(const magic_sht_handle* h) {
-  return tc_form(h) && h->tc_persistent && !h->profiling && h->aux;
-}
-
 // Synthesis: Legendre sums into half spectra, then inverse FFTs.  The
 // half-spectrum temporaries must have been registered in `cx` before
 // prepare(); `hs` holds their ctx indices (one per output grid, in order).
@@ -389,11 +379,10 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
   const double* d_or2 = (const double*)cx.dev(lv.or2_idx);
   FftSet fs{};
   fs.nlev = lv.nlev;
-  cudaStream_t fft_st = h->stream;
   auto flush_fft = [&]() -> int {
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_INV);
-      CK(launch_fft_inverse(g, fs, f64, fft_st));
+      CK(launch_fft_inverse(g, fs, f64, h->stream));
       fs.nf = 0;
     }
     return MAGIC_SHT_OK;
@@ -418,16 +407,6 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     if (h->precision == MAGIC_SHT_BF16X3) TRY(inv_tc(h, g, s, false));
     else CK(launch_inv_legendre_simt(g, s, false, f64, h->stream));
   }
-  const bool ovl = overlap_groups(h) && !sc.empty() && !vc.empty();
-  if (ovl) {  // scalar FFTs on the second stream while the vector Legendre sums run
-    CK(cudaEventRecord(h->ev_fork, h->stream));
-    CK(cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
-    fft_st = h->aux;
-    for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
-    TRY(flush_fft());
-    CK(cudaEventRecord(h->ev_join, h->aux));
-    fft_st = h->stream;
-  }
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
     InvSet s{};
     s.nlev = lv.nlev; s.lcut = d_lcut; s.or2 = d_or2; s.lcut0 = lv.lcut0; s.or2_0 = lv.or2_0;
@@ -441,15 +420,12 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     if (h->precision == MAGIC_SHT_BF16X3) TRY(inv_tc(h, g, s, true));
     else CK(launch_inv_legendre_simt(g, s, true, f64, h->stream));
   }
-  if (!ovl)
-    for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
+  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
   for (size_t i = 0; i < vc.size(); ++i) {
     TRY(add_fft(cx.dev(hs_vc[2 * i]), vc[i].out_t, vc[i].flags | flag_v, hs_ld_v));
     TRY(add_fft(cx.dev(hs_vc[2 * i + 1]), vc[i].out_p, vc[i].flags | flag_v, hs_ld_v));
   }
-  TRY(flush_fft());
-  if (ovl) CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
-  return MAGIC_SHT_OK;
+  return flush_fft();
 }
 
 // Vector Legendre analysis of the radial set (after the vector FFTs).
@@ -485,11 +461,10 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
   const int* d_lcut = (const int*)cx.dev(lv.lcut_idx);
   FftSet fs{};
   fs.nlev = lv.nlev;
-  cudaStream_t fft_st = h->stream;
   auto flush_fft = [&]() -> int {
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_FWD);
-      CK(launch_fft_forward(g, fs, f64, fft_st));
+      CK(launch_fft_forward(g, fs, f64, h->stream));
       fs.nf = 0;
     }
     return MAGIC_SHT_OK;
@@ -501,27 +476,12 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     f.flags = flags; f.pad_ = 0;
     return MAGIC_SHT_OK;
   };
-  // with two streams: scalar FFTs on the second stream while the vector FFTs
-  // and vector Legendre sums run; the scalar Legendre sums follow the join
-  const bool ovl = overlap_groups(h) && !sc.empty() && !vc.empty();
-  if (ovl) {
-    CK(cudaEventRecord(h->ev_fork, h->stream));
-    CK(cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
-    fft_st = h->aux;
-  }
   for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(sc[i].in, cx.dev(hs_sc[i]), FFT_WEIGHT));
-  if (ovl) {
-    TRY(flush_fft());
-    CK(cudaEventRecord(h->ev_join, h->aux));
-    fft_st = h->stream;
-  }
   for (size_t i = 0; i < vc.size(); ++i) {
     TRY(add_fft(vc[i].in_t, cx.dev(hs_vc[2 * i]), FFT_WEIGHT | FFT_OSIN2));
     TRY(add_fft(vc[i].in_p, cx.dev(hs_vc[2 * i + 1]), FFT_WEIGHT | FFT_OSIN2));
   }
   TRY(flush_fft());
-  if (ovl) TRY(run_forward_vectors(h, cx, lv, vc, hs_vc, d_lcut));
-  if (ovl) CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
   for (size_t i0 = 0; i0 < sc.size(); i0 += MAGIC_MAX_FIELDS) {
     FwdSet s{};
     s.nlev = lv.nlev; s.lcut = d_lcut; s.lcut0 = lv.lcut0;
@@ -534,8 +494,7 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     if (h->precision == MAGIC_SHT_BF16X3) TRY(fwd_tc(h, g, s, false));
     else CK(launch_fwd_legendre_simt(g, s, false, f64, h->stream));
   }
-  if (!ovl) TRY(run_forward_vectors(h, cx, lv, vc, hs_vc, d_lcut));
-  return MAGIC_SHT_OK;
+  return run_forward_vectors(h, cx, lv, vc, hs_vc, d_lcut);
 }
 
 int check_handle(const magic_sht_handle* h) {
@@ -713,9 +672,6 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     }                                                                                  \
   } while (0)
   INIT_CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-  INIT_CK(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
-  INIT_CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
-  INIT_CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   h->own_stream = true;
   const size_t tab = (size_t)K * g.nh;
   INIT_CK(cudaMalloc((void**)&h->d_lmoff, sizeof(int) * n_m));
@@ -812,9 +768,6 @@ int magic_sht_finalize(magic_sht_handle* h) {
     if (h->ev_out[i]) cudaEventDestroy(h->ev_out[i]);
   }
   if (h->cpy_in) cudaStreamDestroy(h->cpy_in);
-  if (h->aux) cudaStreamDestroy(h->aux);
-  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
-  if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->cpy_out) cudaStreamDestroy(h->cpy_out);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1289,6 +1242,42 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
   for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_inv_bytes(h, n, true)));
   TRY(cx.prepare());
   TRY(run_inverse(h, cx, lv, sc, vc, hs_sc, hs_vc));
+  return cx.finish();
+}
+
+int magic_sht_get_nl(magic_sht_handle* h, int n, const double* or2, const magic_sht_grid_space_args* gin,
+                     const magic_sht_lm_space_args* nl) {
+  TRY(check_handle(h));
+  if (!gin || !nl || n < 0) return set_err(MAGIC_SHT_ERR_ARG, "null args or n_levels < 0");
+  if (n == 0) return MAGIC_SHT_OK;
+  const ShtGeom& g = h->g;
+  if (gin->grid_ld < (long long)g.n_phi * g.ld || nl->grid_ld < (long long)g.n_phi * g.ld)
+    return set_err(MAGIC_SHT_ERR_ARG, "grid_ld smaller than one level");
+  if ((gin->grid_ld | nl->grid_ld | (long long)g.ld) & 1)
+    return set_err(MAGIC_SHT_ERR_ARG, "get_nl needs even grid_ld and nlat_padded (16-byte pairs of rows)");
+  DeviceGuard dg(h->device);
+  NlGrids in{}, out{};
+  const double* const ins[NL_NIN] = {gin->vrc, gin->vtc, gin->vpc, gin->cvrc, gin->cvtc, gin->cvpc,
+                                     gin->brc, gin->btc, gin->bpc, gin->cbrc, gin->cbtc, gin->cbpc, gin->sc};
+  const double* const outs[NL_NOUT] = {nl->Advr, nl->Advt, nl->Advp, nl->VSr, nl->VSt, nl->VSp,
+                                       nl->VxBr, nl->VxBt, nl->VxBp, nl->heatTerms};
+  for (int i = 0; i < NL_NIN; ++i) {
+    if (!ins[i] || !is_device_ptr(ins[i]) || ((uintptr_t)ins[i] & 15))
+      return set_err(MAGIC_SHT_ERR_ARG, "get_nl input grid %d: null, host or not 16-byte aligned", i);
+    in.p[i] = const_cast<double*>(ins[i]);
+  }
+  for (int i = 0; i < NL_NOUT; ++i) {
+    if (!outs[i] || !is_device_ptr(outs[i]) || ((uintptr_t)outs[i] & 15))
+      return set_err(MAGIC_SHT_ERR_ARG, "get_nl output grid %d: null, host or not 16-byte aligned", i);
+    out.p[i] = const_cast<double*>(outs[i]);  // the analysis inputs are written here
+  }
+  in.ld = gin->grid_ld;
+  out.ld = nl->grid_ld;
+  CallCtx cx(h);
+  const int i_or2 = or2 ? cx.raw_in(or2, (size_t)n * 8) : -1;
+  TRY(cx.prepare());
+  h->launches++;
+  CK(launch_get_nl(g, in, out, (const double*)cx.dev(i_or2), 1.0, n, h->stream));
   return cx.finish();
 }
 

@@ -357,6 +357,40 @@ class SHT:
         check(self._lib.magic_sht_transform_to_lm_space(self._h, n, plc, ctypes.byref(a)))
         return outs
 
+    def get_nl(self, grids: dict, or2=None, out: Optional[dict] = None):
+        """Grid-space nonlinear products between the two transform sets
+        (get_nl.f90:213-441, rIter.f90:650-655): from the synthesis grids
+        (``vrc`` .. ``cbpc``, ``sc``; CUDA tensors [level][phi][theta]) the
+        analysis inputs ``Advr`` .. ``heatTerms`` (Boussinesq, curl-form
+        advection, unit constants, heatTerms = ohmic losses)."""
+        import torch
+        missing = [k for k in _lib.NL_IN if grids.get(k) is None]
+        if missing:
+            raise ValueError("get_nl needs the grids %s" % missing)
+        first = grids[_lib.NL_IN[0]]
+        if not (_is_torch(first) and first.is_cuda):
+            raise ValueError("get_nl takes CUDA tensors")
+        n = int(first.shape[0])
+        g = _lib.GridSpaceArgs()
+        keep = []
+        for k in _lib.NL_IN:
+            t = grids[k].contiguous()
+            keep.append(t)
+            setattr(g, k, t.data_ptr())
+        g.grid_ld = self.n_phi_max * self.nlat_padded
+        outs = {} if out is None else dict(out)
+        nl = _lib.LmSpaceArgs()
+        for k in _lib.LM_SPACE_IN:
+            if k not in outs:
+                outs[k] = torch.empty_like(keep[0])
+            setattr(nl, k, outs[k].data_ptr())
+        nl.grid_ld = self.n_phi_max * self.nlat_padded
+        or2_arr = None if or2 is None else np.ascontiguousarray(or2, dtype=np.float64)
+        por2 = None if or2_arr is None else or2_arr.ctypes.data
+        self._bind_torch_stream()
+        check(self._lib.magic_sht_get_nl(self._h, n, por2, ctypes.byref(g), ctypes.byref(nl)))
+        return outs
+
     # ---------------------------------------------------------- profiling
     def set_profiling(self, on: bool):
         check(self._lib.magic_sht_set_profiling(self._h, 1 if on else 0))

@@ -291,3 +291,37 @@ class OracleSHT:
         b = np.zeros(self.n_theta_max)
         lib().oracle_toraxi_to_spat(self._h, pf, _p(a), _p(b), self._lc(lcut))
         return a, b
+
+
+def get_nl(grids: dict, or2, n_theta: int) -> dict:
+    """Grid-space nonlinear products (get_nl.f90:213-441 with the Lorentz-force
+    addition of rIter.f90:650-655), Boussinesq form (orho1 = 1), curl-form
+    advection (get_nl.f90:262-272), unit physical constants, heatTerms = the
+    ohmic losses (get_nl.f90:424-429).  Grids are [level][phi][theta] with
+    scrambled north/south rows (rows 2j, 2j+1 at colatitudes theta_j and
+    pi - theta_j); numpy FP64."""
+    theta, _ = gauleg(n_theta)                                # colatitudes, north to south
+    sn2 = np.repeat(1.0 / np.sin(theta[: n_theta // 2]) ** 2, 2)  # O_sin_theta_E2 per scrambled row
+    o2 = np.asarray(or2, dtype=np.float64)[:, None, None]
+    o4 = o2 * o2
+    g = {k: np.asarray(v, dtype=np.float64)[..., :n_theta] for k, v in grids.items()}
+    vr, vt, vp = g["vrc"], g["vtc"], g["vpc"]
+    wr, wt, wp = g["cvrc"], g["cvtc"], g["cvpc"]
+    br, bt, bp = g["brc"], g["btc"], g["bpc"]
+    jr, jt, jp = g["cbrc"], g["cbtc"], g["cbpc"]
+    s = g["sc"]
+    LFr = sn2 * (jt * bp - jp * bt)
+    LFt = o4 * (jp * br - jr * bp)
+    LFp = o4 * (jr * bt - jt * br)
+    return {
+        "Advr": -sn2 * (wt * vp - wp * vt) + LFr,
+        "Advt": -o4 * (wp * vr - wr * vp) + LFt,
+        "Advp": -o4 * (wr * vt - wt * vr) + LFp,
+        "VSr": vr * s,
+        "VSt": o2 * vt * s,
+        "VSp": o2 * vp * s,
+        "VxBr": sn2 * (vt * bp - vp * bt),
+        "VxBt": o4 * (vp * br - vr * bp),
+        "VxBp": o4 * (vr * bt - vt * br),
+        "heatTerms": o2 * (o2 * jr * jr + sn2 * jt * jt + sn2 * jp * jp),
+    }
