@@ -130,21 +130,27 @@ __device__ __forceinline__ int brev5(int x) { return __brev(x) >> 27; }
 template <typename T2, int S>
 __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tw, int P, int s) {
   const int lane = threadIdx.x & 31;
+  typedef typename ScalarOf<T2>::t T;
 #pragma unroll
   for (int d = 16; d >= 1; d >>= 1) {
+    // lower lane: a + b;  upper lane: (b - a) * w  -> t = b + sg*a, a = t * w
     const bool up = (lane & d) != 0;
-    const T2 w = twid(tw, (lane & (d - 1)) * (P / (2 * d)), s);
+    const T sg = up ? (T)-1 : (T)1;
+    T2 w = twid(tw, (lane & (d - 1)) * (P / (2 * d)), s);
+    if (!up) { w.x = (T)1; w.y = (T)0; }
 #pragma unroll
     for (int q = 0; q < S; ++q) {
       const T2 b = shfl_xor2(a[q], d);
-      if (up) a[q] = cmul(csub(b, a[q]), w);
-      else a[q] = cadd(a[q], b);
+      T2 t;
+      t.x = fma(sg, a[q].x, b.x);
+      t.y = fma(sg, a[q].y, b.y);
+      a[q] = cmul(t, w);
     }
   }
   const int k1 = brev5(lane);
 #pragma unroll
   for (int q = 1; q < S; ++q) {
-    if (k1) a[q] = cmul(a[q], twid(tw, (2 * q * k1) % P, s));  // omega_n^{q k1}
+    if (k1) a[q] = cmul(a[q], twid(tw, 2 * q * k1, s));  // omega_n^{q k1}; 2 q k1 < P
   }
   reg_fft<T2, S>(a, tw, P, s);
 }
@@ -209,11 +215,13 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
     T2 a[S];
 #pragma unroll
     for (int q = 0; q < S; ++q) {
+      // k = S*lane + q sits at pin(k) = 32q + lane; n - k at 32(S-q) + 31 - lane
+      // (q > 0) or 32 - lane (q = 0; k = 0 has no partner)
       const int k = S * lane + q;
       T2 ck = zero2<T2>(), cn = zero2<T2>();
-      if (k < n_m) ck = row[pin<S>(k)];
+      if (k < n_m) ck = row[32 * q + lane];
       const int kn = n - k;
-      if (kn < n_m) cn = row[pin<S>(kn)];
+      if (kn < n_m) cn = row[q == 0 ? 32 - lane : 32 * (S - q) + 31 - lane];
       if (k == 0) { ck.y = 0; cn.y = 0; }
       const T2 E = cadd(ck, cconj(cn));
       const T2 O = cmul(csub(ck, cconj(cn)), tw[k]);
@@ -324,7 +332,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
     for (int h = 0; h < 2; ++h) {
       const T2* row = sm + (2 * jp + h) * KP;
       const T2 Zk = row[k];
-      const T2 Zn = cconj(row[(n - k) % n]);
+      const T2 Zn = cconj(row[k == 0 ? 0 : n - k]);
       const T2 D = csub(Zk, Zn);
       const T2 u = cmul(cconj(tw[k]), D);
       T2 X;

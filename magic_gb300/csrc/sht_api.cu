@@ -188,6 +188,7 @@ int inv_tc(magic_sht_handle* h, const ShtGeom& g, const InvSet& s, bool vec) {
     return MAGIC_SHT_OK;
   }
   TRY(ensure_bimg(h, tcp_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), vec, true)));
+  h->launches++;  // pack kernel + persistent kernel
   CK(launch_inv_legendre_tcp(g, s, vec, h->tct, h->d_bimg, h->stream));
   return MAGIC_SHT_OK;
 }
@@ -197,6 +198,7 @@ int fwd_tc(magic_sht_handle* h, const ShtGeom& g, const FwdSet& s, bool vec) {
     return MAGIC_SHT_OK;
   }
   TRY(ensure_bimg(h, tcp_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), vec, false)));
+  h->launches++;  // pack kernel + persistent kernel
   CK(launch_fwd_legendre_tcp(g, s, vec, h->tct, h->d_bimg, h->stream));
   return MAGIC_SHT_OK;
 }
@@ -800,6 +802,7 @@ int magic_sht_gauss_grid(magic_sht_handle* h, double* theta_ord, double* gauss) 
 
 int magic_sht_set_stream(magic_sht_handle* h, void* s) {
   TRY(check_handle(h));
+  if ((cudaStream_t)s == h->stream && !h->own_stream) return MAGIC_SHT_OK;
   if (h->capturing) return set_err(MAGIC_SHT_ERR_ARG, "cannot change the stream during capture");
   DeviceGuard dg(h->device);
   CK(cudaStreamSynchronize(h->stream));

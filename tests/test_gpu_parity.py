@@ -429,3 +429,78 @@ def test_radial_step_with_nonlinear_products(built, torch):
     for k in r:
         tol = 2e-3 if k == "AdvpLM" else 2e-6
         assert rel_l2(a[k], r[k]) < tol, (k, rel_l2(a[k], r[k]))
+
+
+@pytest.mark.gpu
+def test_large_config_l511(built, oracle_mod, torch):
+    """The large configuration (l_max=511, 768 x 1536 grid): the FP64 form
+    against the oracle on one level of the radial set, the 3xBF16 form
+    against the FP64 form on three levels (normwise per call <= 1e-6)."""
+    from magic_gb300.workload import grid_space_inputs, or2_levels
+    L, minc, N, P, n = 511, 1, 768, 1536, 3
+    spec_np = grid_space_inputs(L, minc, n, seed=29)
+    or2 = or2_levels(n)
+    spec = {k: torch.from_numpy(v).cuda() for k, v in spec_np.items()}
+    s64 = make(L, minc, N, P, prec="fp64")
+    g64 = s64.transform_to_grid_space(spec, or2=or2)
+    torch.cuda.synchronize()
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    vr, vt, vp = o.torpol_to_spat(spec_np["w"][1], spec_np["dw"][1], spec_np["z"][1])
+    assert rel_l2(g64["vtc"][1].cpu().numpy(), vt) < 1e-12
+    assert rel_l2(g64["vpc"][1].cpu().numpy(), vp) < 1e-12
+    sc = o.scal_to_spat(spec_np["s"][1])
+    assert rel_l2(g64["sc"][1].cpu().numpy(), sc) < 1e-12
+    s16 = make(L, minc, N, P, prec="bf16x3")
+    g16 = s16.transform_to_grid_space(spec, or2=or2)
+    nl = s64.get_nl(g64, or2=or2)
+    l64 = s64.transform_to_lm_space(nl)
+    l16 = s16.transform_to_lm_space(nl)
+    torch.cuda.synchronize()
+    for name, ks, a, b in (("v", ("vrc", "vtc", "vpc"), g16, g64), ("b", ("brc", "btc", "bpc"), g16, g64),
+                           ("VxB", ("VxBrLM", "VxBtLM", "VxBpLM"), l16, l64),
+                           ("VS", ("VSrLM", "VStLM", "VSpLM"), l16, l64)):
+        num = sum(float(torch.linalg.vector_norm(a[k] - b[k])) ** 2 for k in ks) ** 0.5
+        den = sum(float(torch.linalg.vector_norm(b[k])) ** 2 for k in ks) ** 0.5
+        assert num / den < 1e-6, (name, num / den)
+
+
+@pytest.mark.gpu
+def test_sixteen_instances_in_one_graph(built, torch):
+    """Sixteen independent transform instances of mixed sizes (l_max in
+    {63, 127, 255}, minc in {1, 4}, a fixed seeded list) captured together in
+    one CUDA graph on one stream and replayed: every instance's grids equal
+    its direct call."""
+    from magic_gb300.workload import grid_space_inputs, or2_levels
+    rng = np.random.default_rng(1234)
+    insts = []
+    for i in range(16):
+        L = int(rng.choice([63, 127, 255]))
+        minc = int(rng.choice([1, 4]))
+        N = 3 * (L + 1) // 2
+        P = 2 * N // minc
+        n = int(rng.choice([3, 5, 9]))
+        s = make(L, minc, N, P, prec="bf16x3")
+        spec = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(L, minc, n, seed=100 + i).items()}
+        or2 = torch.from_numpy(or2_levels(n)).cuda()
+        ref = s.transform_to_grid_space(spec, or2=or2)
+        insts.append((s, spec, or2, ref, {k: torch.zeros_like(v) for k, v in ref.items()}, n))
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        for s, _, _, _, _, n in insts:
+            s.reserve(n)
+            s.set_stream(side.cuda_stream)  # bind before the capture (binding synchronizes)
+        side.synchronize()
+        insts[0][0].graph_begin()  # every handle is bound to this stream: one capture
+        try:
+            for s, spec, or2, _, out, _ in insts:
+                s.transform_to_grid_space(spec, or2=or2, out=out)
+        finally:
+            gr = insts[0][0].graph_end()
+        insts[0][0].graph_launch(gr)
+        side.synchronize()
+    for s, _, _, ref, out, _ in insts:
+        s.device_status()
+        for k in ref:
+            assert torch.equal(out[k], ref[k]), k
+    insts[0][0].graph_destroy(gr)
