@@ -179,6 +179,15 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n_levels, const d
 int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n_levels, const int* lcut,
                                     const magic_sht_lm_space_args* a);
 
+/* ---- asynchronous host-buffer batches.  With on != 0, a batched call whose
+ * arrays are all in host memory and that spans more than 8 levels returns once
+ * its chunked copies and kernels are queued (instead of when the host outputs
+ * are written); its host arrays must stay valid and untouched until
+ * magic_sht_synchronize(h).  Consecutive such calls overlap one call's
+ * device-to-host copies with the next call's host-to-device copies.  Off by
+ * default (the reference's calls return with their results). */
+int magic_sht_set_host_async(magic_sht_handle* h, int on);
+
 /* ---- grid-space nonlinear products between the two transform sets
  * (get_nl.f90:213-441 and the Lorentz-force addition of rIter.f90:650-655).
  * Reads the grids transform_to_grid_space writes (vrc..vpc, cvrc..cvpc,

@@ -83,6 +83,7 @@ SIGNATURES = {
     "magic_sht_transform_to_grid_space": [_V, ctypes.c_int, _V, _V,
                                           ctypes.POINTER(GridSpaceArgs)],
     "magic_sht_transform_to_lm_space": [_V, ctypes.c_int, _V, ctypes.POINTER(LmSpaceArgs)],
+    "magic_sht_set_host_async": [_V, ctypes.c_int],
     "magic_sht_get_nl": [_V, ctypes.c_int, _V, ctypes.POINTER(GridSpaceArgs), ctypes.POINTER(LmSpaceArgs)],
     "magic_sht_graph_begin": [_V],
     "magic_sht_graph_end": [_V, ctypes.POINTER(_V)],

@@ -121,6 +121,15 @@ __device__ __forceinline__ void issue_split(uint32_t acc, const unsigned char* A
     }
 }
 
+// Pointer held by lane `src` (whole warp participates).
+template <typename P>
+__device__ __forceinline__ P* shfl_ptr(P* p, int src) {
+  const unsigned long long v = (unsigned long long)p;
+  const unsigned lo = __shfl_sync(0xffffffffu, (unsigned)v, src);
+  const unsigned hi = __shfl_sync(0xffffffffu, (unsigned)(v >> 32), src);
+  return (P*)(((unsigned long long)hi << 32) | lo);
+}
+
 // (C2 + C1) + C0 of one table for the 32 columns at TMEM address `col`
 // (this warp's lane quadrant).
 __device__ __forceinline__ void drain_sum(uint32_t col, float (&v)[32]) {
@@ -331,27 +340,36 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
       if (ix < 0) break;
       T.decode(g, t, nct, ix);
       const int jg = T.tt * 128 + jl;
-      const long long per_p = VEC ? 2LL * g.nh : (long long)g.nh;
-      auto optr = [&](void* bp, int r, int f, int ef) -> float2* {
-        return (float2*)bp + (long long)r * s.f[f].out_ld + ((long long)T.mc * 2 + T.p) * per_p +
-               (long long)ef * g.nh + jg;
-      };
-      if (T.nlp == 0) {  // odd parity of m = l_max: zeros
-        if (jg < g.nh)
-          for (int q = cc0 / 2; q < cc0 / 2 + 16; ++q) {
-            const int cq = T.ct * (NC / 2) + q;
-            if (cq >= ncplx) break;
-            if (!VEC) {
-              const int r = cq / s.nf, f = cq - r * s.nf;
-              *optr(s.f[f].out0, r, f, 0) = make_float2(0.f, 0.f);
-            } else if ((cq & 1) == 0) {
-              const int pr = cq >> 1, r = pr / s.nf, f = pr - r * s.nf;
-              for (int ef = 0; ef < 2; ++ef) {
-                *optr(s.f[f].out0, r, f, ef) = make_float2(0.f, 0.f);
-                *optr(s.f[f].out1, r, f, ef) = make_float2(0.f, 0.f);
-              }
-            }
+      const bool row_ok = jg < g.nh;
+      // output column bases, one per lane, broadcast by shuffles: scalar: lane q <
+      // 16 holds column q's array; vector: lane q < 8 the v_theta array of pair
+      // q, lane 8 + q its v_phi array (E at +0, F at +nh)
+      float2* cb = nullptr;
+      {
+        const long long per_p = VEC ? 2LL * g.nh : (long long)g.nh;
+        const long long moff = ((long long)T.mc * 2 + T.p) * per_p;
+        if (!VEC && lane < 16) {
+          const int cq = T.ct * (NC / 2) + cc0 / 2 + lane;
+          if (cq < ncplx) {
+            const int r = cq / s.nf, f = cq - r * s.nf;
+            cb = (float2*)s.f[f].out0 + (long long)r * s.f[f].out_ld + moff;
           }
+        } else if (VEC && lane < 16) {
+          const int pr = T.ct * (NC / 4) + cc0 / 4 + (lane & 7);
+          if (pr < npair) {
+            const int r = pr / s.nf, f = pr - r * s.nf;
+            cb = (float2*)(lane < 8 ? s.f[f].out0 : s.f[f].out1) + (long long)r * s.f[f].out_ld + moff;
+          }
+        }
+      }
+      if (T.nlp == 0) {  // odd parity of m = l_max: zeros
+        for (int q = 0; q < 16; ++q) {
+          float2* b = shfl_ptr(cb, q);
+          if (b && row_ok) {
+            b[jg] = make_float2(0.f, 0.f);
+            if (VEC) b[g.nh + jg] = make_float2(0.f, 0.f);
+          }
+        }
         continue;
       }
       const uint32_t abuf = acc_use % NACC;
@@ -364,37 +382,36 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
       tc::tc_fence_before();
       tc::mbar_arrive(&acc_empty[abuf]);  // tensor memory free for the next tile
       ++acc_use;
-      const float sP = t.inv_scale[(size_t)T.mc * NHP + jg];
+      const float sP = row_ok ? t.inv_scale[(size_t)T.mc * NHP + jg] : 0.f;
 #pragma unroll
       for (int i = 0; i < 32; ++i) P[i] *= sP;
       if (!VEC) {
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          const int cq = T.ct * (NC / 2) + cc0 / 2 + q;
-          if (cq >= ncplx || jg >= g.nh) continue;
-          const int r = cq / s.nf, f = cq - r * s.nf;
-          *optr(s.f[f].out0, r, f, 0) = make_float2(P[2 * q], P[2 * q + 1]);
+          float2* b = shfl_ptr(cb, q);
+          if (b && row_ok) b[jg] = make_float2(P[2 * q], P[2 * q + 1]);
         }
       } else {
-        const float sdP = t.inv_scale[((size_t)g.n_m + T.mc) * NHP + jg];
+        const float sdP = row_ok ? t.inv_scale[((size_t)g.n_m + T.mc) * NHP + jg] : 0.f;
         const float dm = (float)(T.mc * g.minc);
 #pragma unroll
         for (int i = 0; i < 32; ++i) D[i] *= sdP;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const int pr = T.ct * (NC / 4) + cc0 / 4 + q;
-          if (pr >= npair || jg >= g.nh) continue;
-          const int r = pr / s.nf, f = pr - r * s.nf;
+          float2* bt = shfl_ptr(cb, q);
+          float2* bp = shfl_ptr(cb, 8 + q);
           // C = sum S P, B = sum T P; A = sum S dP, D = sum T dP
           const float Cr = P[4 * q], Ci = P[4 * q + 1], Br = P[4 * q + 2], Bi = P[4 * q + 3];
           const float Ar = D[4 * q], Ai = D[4 * q + 1], Dr = D[4 * q + 2], Di = D[4 * q + 3];
           // v_theta: U = i m B, W = A;   v_phi: U = i m C, W = -D
           const float2 Ut = make_float2(-dm * Bi, dm * Br), Wt = make_float2(Ar, Ai);
           const float2 Up = make_float2(-dm * Ci, dm * Cr), Wp = make_float2(-Dr, -Di);
-          *optr(s.f[f].out0, r, f, 0) = make_float2(Ut.x + Wt.x, Ut.y + Wt.y);
-          *optr(s.f[f].out0, r, f, 1) = make_float2(Ut.x - Wt.x, Ut.y - Wt.y);
-          *optr(s.f[f].out1, r, f, 0) = make_float2(Up.x + Wp.x, Up.y + Wp.y);
-          *optr(s.f[f].out1, r, f, 1) = make_float2(Up.x - Wp.x, Up.y - Wp.y);
+          if (bt && row_ok) {
+            bt[jg] = make_float2(Ut.x + Wt.x, Ut.y + Wt.y);
+            bt[g.nh + jg] = make_float2(Ut.x - Wt.x, Ut.y - Wt.y);
+            bp[jg] = make_float2(Up.x + Wp.x, Up.y + Wp.y);
+            bp[g.nh + jg] = make_float2(Up.x - Wp.x, Up.y - Wp.y);
+          }
         }
       }
     }
@@ -559,43 +576,53 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
       const int lp = T.lt * 128 + lr;
       const int l = m + T.p + 2 * lp;
       const bool valid = lp < T.nlp;
-      if (!valid) continue;
       const int lm = g.lmoff[T.mc] + l - m;
-      const float sP = t.fwd_scale[lm];
+      // per-column output bases and cut-offs, one per lane, broadcast by shuffles:
+      // scalar: lane q < 16 holds column q; vector: lane q < 8 pair q's S array,
+      // lane 8 + q its T array
+      double2* cb = nullptr;
+      int clc = -1;
+      if (lane < 16) {
+        const int q = VEC ? (lane & 7) : lane;
+        const int cq = VEC ? T.ct * (NC / 4) + cc0 / 4 + q : T.ct * (NC / 2) + cc0 / 2 + q;
+        if (cq < (VEC ? npair : ncplx)) {
+          const int r = cq / s.nf, f = cq - r * s.nf;
+          cb = (VEC && lane >= 8 ? s.f[f].out1 : s.f[f].out0) + (long long)r * s.f[f].out_ld;
+          clc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+        }
+      }
+      const float sP = valid ? t.fwd_scale[lm] : 0.f;
 #pragma unroll
       for (int i = 0; i < 32; ++i) D0[i] *= sP;
       if (!VEC) {
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          const int cq = T.ct * (NC / 2) + cc0 / 2 + q;
-          if (cq >= ncplx) continue;
-          const int r = cq / s.nf, f = cq - r * s.nf;
-          const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
-          const double2 v = (l <= lc) ? make_double2(f2d_int(D0[2 * q]), f2d_int(D0[2 * q + 1]))
-                                      : make_double2(0.0, 0.0);
-          s.f[f].out0[(long long)r * s.f[f].out_ld + lm] = v;
+          double2* b = shfl_ptr(cb, q);
+          const int lc = __shfl_sync(0xffffffffu, clc, q);
+          if (b && valid)
+            b[lm] = (l <= lc) ? make_double2(f2d_int(D0[2 * q]), f2d_int(D0[2 * q + 1])) : make_double2(0.0, 0.0);
         }
       } else {
-        const float sdP = t.fwd_scale[(size_t)g.lm_max + lm];
+        const float sdP = valid ? t.fwd_scale[(size_t)g.lm_max + lm] : 0.f;
         const float dm = (float)m;
         const float inv_ll = l > 0 ? 1.0f / (float)(l * (l + 1)) : 1.0f;
 #pragma unroll
         for (int i = 0; i < 32; ++i) D1[i] *= sdP;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const int pr = T.ct * (NC / 4) + cc0 / 4 + q;
-          if (pr >= npair) continue;
-          const int r = pr / s.nf, f = pr - r * s.nf;
-          const int lc = min(s.lcut ? s.lcut[r] : s.lcut0, g.l_max);
+          double2* bs = shfl_ptr(cb, q);
+          double2* bt = shfl_ptr(cb, 8 + q);
+          const int lc = __shfl_sync(0xffffffffu, clc, q);
           // A = sum F1_mine P, D = sum F2_mine P, C = sum F1_other dP, B = sum F2_other dP
           const float Ar = D0[4 * q], Ai = D0[4 * q + 1], Dr = D0[4 * q + 2], Di = D0[4 * q + 3];
           const float Cr = D1[4 * q], Ci = D1[4 * q + 1], Br = D1[4 * q + 2], Bi = D1[4 * q + 3];
           double2 Sv = make_double2(f2d_int((dm * Ai + Br) * inv_ll), f2d_int((-dm * Ar + Bi) * inv_ll));
           double2 Tv = make_double2(f2d_int((-Cr + dm * Di) * inv_ll), f2d_int((-Ci - dm * Dr) * inv_ll));
           if (l > lc) { Sv = make_double2(0.0, 0.0); Tv = Sv; }
-          const long long o = (long long)r * s.f[f].out_ld + lm;
-          s.f[f].out0[o] = Sv;
-          s.f[f].out1[o] = Tv;
+          if (bs && valid) {
+            bs[lm] = Sv;
+            bt[lm] = Tv;
+          }
         }
       }
     }

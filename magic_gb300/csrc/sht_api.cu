@@ -80,10 +80,21 @@ struct magic_sht_handle {
   size_t ws_bytes = 0;
   std::vector<int> lmoff;
   // host-buffer pipeline of the batched calls: two staging slots, two copy streams
-  char* stage = nullptr;
-  size_t stage_bytes = 0;
+  // Staging for the host-buffer pipeline: two pools that consecutive calls
+  // alternate, so one call's host->device copies never wait for the previous
+  // call's device->host copies.  A pool holds 2 chunk slots (synchronous
+  // calls) or one slot per chunk (asynchronous calls: the uploads then run
+  // ahead of the previous call's downloads instead of waiting for slot reuse).
+  struct StagePool {
+    char* buf = nullptr;
+    size_t bytes = 0, stride = 0;
+    std::vector<cudaEvent_t> ev_in, ev_comp, ev_out;
+    std::vector<char> used;
+  } pools[2];
+  int pool = 0;
   cudaStream_t cpy_in = nullptr, cpy_out = nullptr;
-  cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
+  // magic_sht_set_host_async: pipelined host-buffer calls return once queued
+  bool host_async = false;
   // per-phase CUDA-event timing (magic_sht_set_profiling)
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -763,11 +774,10 @@ int magic_sht_finalize(magic_sht_handle* h) {
                   h->d_bpc0, h->d_bimg, h->d_tile_ctr};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
-  if (h->stage) cudaFree(h->stage);
-  for (int i = 0; i < 2; ++i) {
-    if (h->ev_in[i]) cudaEventDestroy(h->ev_in[i]);
-    if (h->ev_comp[i]) cudaEventDestroy(h->ev_comp[i]);
-    if (h->ev_out[i]) cudaEventDestroy(h->ev_out[i]);
+  for (auto& P : h->pools) {
+    if (P.buf) cudaFree(P.buf);
+    for (auto* v : {&P.ev_in, &P.ev_comp, &P.ev_out})
+      for (cudaEvent_t e : *v) cudaEventDestroy(e);
   }
   if (h->cpy_in) cudaStreamDestroy(h->cpy_in);
   if (h->cpy_out) cudaStreamDestroy(h->cpy_out);
@@ -818,6 +828,15 @@ int magic_sht_synchronize(magic_sht_handle* h) {
   TRY(check_handle(h));
   DeviceGuard dg(h->device);
   CK(cudaStreamSynchronize(h->stream));
+  if (h->cpy_in) CK(cudaStreamSynchronize(h->cpy_in));
+  if (h->cpy_out) CK(cudaStreamSynchronize(h->cpy_out));
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_set_host_async(magic_sht_handle* h, int on) {
+  TRY(check_handle(h));
+  if (!on && h->host_async) TRY(magic_sht_synchronize(h));
+  h->host_async = on != 0;
   return MAGIC_SHT_OK;
 }
 
@@ -1070,32 +1089,48 @@ static int pipelined_levels(magic_sht_handle* h, int n, int chunk, std::vector<P
     a.slot_off = slot;
     slot += align256((size_t)(chunk - 1) * a.lds + a.last);
   }
-  if (2 * slot > h->stage_bytes) {
-    CK(cudaDeviceSynchronize());
-    if (h->stage) CK(cudaFree(h->stage));
-    h->stage = nullptr;
-    h->stage_bytes = 0;
-    CK(cudaMalloc((void**)&h->stage, 2 * slot));
-    h->stage_bytes = 2 * slot;
-  }
+  const int nchunks = (n + chunk - 1) / chunk;
+  const int ns = h->host_async ? nchunks : 2;
+  auto& P = h->pools[h->pool];
+  h->pool ^= 1;
   if (!h->cpy_in) {
     CK(cudaStreamCreateWithFlags(&h->cpy_in, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&h->cpy_out, cudaStreamNonBlocking));
-    for (int i = 0; i < 2; ++i) {
-      CK(cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&h->ev_comp[i], cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&h->ev_out[i], cudaEventDisableTiming));
-    }
   }
-  // start after everything already queued on the handle's stream
-  CK(cudaEventRecord(h->ev_comp[1], h->stream));
-  CK(cudaStreamWaitEvent(h->cpy_in, h->ev_comp[1], 0));
-  CK(cudaStreamWaitEvent(h->cpy_out, h->ev_comp[1], 0));
-  const int nchunks = (n + chunk - 1) / chunk;
+  if ((size_t)ns * slot > P.bytes || slot != P.stride) {
+    // new layout of this pool: its previous slots must be drained first
+    if ((size_t)ns * slot > P.bytes) {
+      CK(cudaDeviceSynchronize());
+      if (P.buf) CK(cudaFree(P.buf));
+      P.buf = nullptr;
+      P.bytes = 0;
+      CK(cudaMalloc((void**)&P.buf, (size_t)ns * slot));
+      P.bytes = (size_t)ns * slot;
+    } else {
+      for (size_t k = 0; k < P.used.size(); ++k)
+        if (P.used[k]) {
+          CK(cudaStreamWaitEvent(h->cpy_in, P.ev_out[k], 0));
+          CK(cudaStreamWaitEvent(h->stream, P.ev_out[k], 0));
+        }
+    }
+    P.stride = slot;
+    std::fill(P.used.begin(), P.used.end(), 0);
+  }
+  while ((int)P.used.size() < ns) {
+    cudaEvent_t e[3];
+    for (auto& x : e) CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    P.ev_in.push_back(e[0]);
+    P.ev_comp.push_back(e[1]);
+    P.ev_out.push_back(e[2]);
+    P.used.push_back(0);
+  }
+  // A slot is reused once the copies out of its previous use (in this call or
+  // an earlier one) are done; the host arrays need no other ordering.
   for (int c = 0; c < nchunks; ++c) {
-    const int sl = c & 1, r0 = c * chunk, nr = std::min(chunk, n - r0);
-    char* base = h->stage + (size_t)sl * slot;
-    if (c >= 2) CK(cudaStreamWaitEvent(h->cpy_in, h->ev_out[sl], 0));  // slot drained
+    const int sl = c % ns, r0 = c * chunk, nr = std::min(chunk, n - r0);
+    char* base = P.buf + (size_t)sl * P.stride;
+    const bool reuse = P.used[sl] != 0;
+    if (reuse) CK(cudaStreamWaitEvent(h->cpy_in, P.ev_out[sl], 0));  // slot drained
     std::vector<char*> dev(arrs.size());
     for (size_t i = 0; i < arrs.size(); ++i) {
       const PipeArray& a = arrs[i];
@@ -1104,29 +1139,37 @@ static int pipelined_levels(magic_sht_handle* h, int n, int chunk, std::vector<P
         CK(cudaMemcpyAsync(dev[i], (const char*)a.host + (size_t)r0 * a.lds, (size_t)(nr - 1) * a.lds + a.last,
                            cudaMemcpyHostToDevice, h->cpy_in));
     }
-    CK(cudaEventRecord(h->ev_in[sl], h->cpy_in));
-    CK(cudaStreamWaitEvent(h->stream, h->ev_in[sl], 0));
-    if (c >= 2) CK(cudaStreamWaitEvent(h->stream, h->ev_out[sl], 0));  // outputs of c-2 copied
+    CK(cudaEventRecord(P.ev_in[sl], h->cpy_in));
+    CK(cudaStreamWaitEvent(h->stream, P.ev_in[sl], 0));
+    if (reuse) CK(cudaStreamWaitEvent(h->stream, P.ev_out[sl], 0));  // previous outputs copied
     TRY(compute(r0, nr, dev));
-    CK(cudaEventRecord(h->ev_comp[sl], h->stream));
-    CK(cudaStreamWaitEvent(h->cpy_out, h->ev_comp[sl], 0));
+    CK(cudaEventRecord(P.ev_comp[sl], h->stream));
+    CK(cudaStreamWaitEvent(h->cpy_out, P.ev_comp[sl], 0));
     for (size_t i = 0; i < arrs.size(); ++i) {
       const PipeArray& a = arrs[i];
       if (a.out)
         CK(cudaMemcpyAsync((char*)a.host + (size_t)r0 * a.lds, dev[i], (size_t)(nr - 1) * a.lds + a.last,
                            cudaMemcpyDeviceToHost, h->cpy_out));
     }
-    CK(cudaEventRecord(h->ev_out[sl], h->cpy_out));
+    CK(cudaEventRecord(P.ev_out[sl], h->cpy_out));
+    P.used[sl] = 1;
   }
-  CK(cudaStreamSynchronize(h->cpy_out));
-  CK(cudaStreamSynchronize(h->stream));
+  if (!h->host_async) {
+    CK(cudaStreamSynchronize(h->cpy_out));
+    CK(cudaStreamSynchronize(h->stream));
+  }
   return MAGIC_SHT_OK;
 }
 
-static bool any_host(std::initializer_list<const void*> ptrs) {
-  for (const void* p : ptrs)
-    if (p && !is_device_ptr(p)) return true;
-  return false;
+// the host-buffer pipeline runs when every given array is in host memory
+static bool all_host(std::initializer_list<const void*> ptrs) {
+  bool any = false;
+  for (const void* p : ptrs) {
+    if (!p) continue;
+    if (is_device_ptr(p)) return false;
+    any = true;
+  }
+  return any;
 }
 
 static const int kPipeChunk = 8;  // radial levels per pipeline chunk
@@ -1160,9 +1203,9 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
     return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
   DeviceGuard dg(h->device);
   if (n > kPipeChunk && !h->capturing &&
-      any_host({a->s, a->p, a->xi, a->w, a->dw, a->ddw, a->z, a->dz, a->b, a->db, a->ddb, a->aj, a->dj,
+      all_host({a->s, a->p, a->xi, a->w, a->dw, a->ddw, a->z, a->dz, a->b, a->db, a->ddb, a->aj, a->dj,
                 a->sc, a->pc, a->xic, a->vrc, a->vtc, a->vpc, a->cvrc, a->cvtc, a->cvpc, a->brc, a->btc,
-                a->bpc, a->cbrc, a->cbtc, a->cbpc})) {
+                a->bpc, a->cbrc, a->cbtc, a->cbpc, lcut, or2})) {
     if (lcut)
       for (int i = 0; i < n; ++i)
         if (!is_device_ptr(lcut) && (lcut[i] < 0 || lcut[i] > g.l_max))
@@ -1294,7 +1337,7 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
     return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
   DeviceGuard dg(h->device);
   if (n > kPipeChunk && !h->capturing &&
-      any_host({a->Advr, a->Advt, a->Advp, a->VSr, a->VSt, a->VSp, a->VxBr, a->VxBt, a->VxBp, a->heatTerms,
+      all_host({lcut, a->Advr, a->Advt, a->Advp, a->VSr, a->VSt, a->VSp, a->VxBr, a->VxBt, a->VxBp, a->heatTerms,
                 a->AdvrLM, a->AdvtLM, a->AdvpLM, a->VSrLM, a->VStLM, a->VSpLM, a->VxBrLM, a->VxBtLM,
                 a->VxBpLM, a->heatTermsLM})) {
     if (lcut)

@@ -357,6 +357,11 @@ class SHT:
         check(self._lib.magic_sht_transform_to_lm_space(self._h, n, plc, ctypes.byref(a)))
         return outs
 
+    def set_host_async(self, on: bool):
+        """Batched calls on host arrays return once queued; results are valid
+        after ``synchronize()`` (magic_sht_set_host_async)."""
+        check(self._lib.magic_sht_set_host_async(self._h, 1 if on else 0))
+
     def get_nl(self, grids: dict, or2=None, out: Optional[dict] = None):
         """Grid-space nonlinear products between the two transform sets
         (get_nl.f90:213-441, rIter.f90:650-655): from the synthesis grids

@@ -504,3 +504,29 @@ def test_sixteen_instances_in_one_graph(built, torch):
         for k in ref:
             assert torch.equal(out[k], ref[k]), k
     insts[0][0].graph_destroy(gr)
+
+
+@pytest.mark.gpu
+def test_async_host_batches_match_sync(built, torch):
+    """With asynchronous host batches two consecutive pipelined calls overlap
+    and, after synchronize(), give the same host results as synchronous calls."""
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    L, minc, N, P, n = 63, 1, 96, 192, 21
+    s = make(L, minc, N, P, prec="bf16x3")
+    spec = {k: torch.from_numpy(v).pin_memory() for k, v in grid_space_inputs(L, minc, n, seed=44).items()}
+    or2 = or2_levels(n)
+    ref_g = s.transform_to_grid_space(spec, or2=or2)
+    fin = {k: ref_g[v].clone().pin_memory() for k, v in FORWARD_FROM_INVERSE.items()}
+    ref_l = s.transform_to_lm_space(fin)
+    out_g = {k: torch.zeros_like(v).pin_memory() for k, v in ref_g.items()}
+    out_l = {k: torch.zeros_like(v).pin_memory() for k, v in ref_l.items()}
+    s.set_host_async(True)
+    for _ in range(2):
+        s.transform_to_grid_space(spec, or2=or2, out=out_g)
+        s.transform_to_lm_space(fin, out=out_l)
+    s.synchronize()
+    s.set_host_async(False)
+    for k in ref_g:
+        assert torch.equal(out_g[k], ref_g[k]), k
+    for k in ref_l:
+        assert torch.equal(out_l[k], ref_l[k]), k
