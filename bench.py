@@ -40,10 +40,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3"])
+    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x2"])
     ap.add_argument("--cpu-levels", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-variant", action="store_true", help="skip the TF32 variant of the tensor-core form")
     ap.add_argument("--levels", type=int, default=N_LEVELS, help="radial levels (profiling cases)")
     ap.add_argument("--only-reduced", action="store_true", help="skip the FP64 form (profiling)")
     ap.add_argument("--clock-seconds", type=float, default=1.5,
@@ -361,6 +362,33 @@ def our_arm(args):
         normwise[k] = errs[k]
     max_normwise = max(normwise.values())
 
+    # ---- the TF32 variant of the tensor-core form (2xTF32 split products):
+    # same step, timing and normwise accuracy, reported beside the headline
+    variant = None
+    if form == "bf16x3" and not args.no_variant:
+        sv = SHT(L_MAX, MINC, N_THETA, N_PHI, precision="tf32x2", device=local)
+        gv, lv = run_set(sv, None, None)
+        for _ in range(max(0, args.warmup - 1)):
+            run_set(sv, gv, lv)
+        msv, _, perv = time_steps(sv, gv, lv, args.steps)
+        run_set(sv, gv, lv)
+        torch.cuda.synchronize()
+        sv.device_status()
+        allv = {**{k: (gv[k], g64[k]) for k in g64}, **{k: (lv[k], l64[k]) for k in l64}}
+        nwv = {}
+        for name, ks in groups.items():
+            num = sum(float(torch.linalg.vector_norm(allv[k][0] - allv[k][1])) ** 2 for k in ks)
+            den = sum(float(torch.linalg.vector_norm(allv[k][1])) ** 2 for k in ks)
+            nwv[name] = (num / den) ** 0.5
+        for k in ("sc", "pc", "xic", "heatTermsLM"):
+            nwv[k] = float(torch.linalg.vector_norm(allv[k][0] - allv[k][1]) / torch.linalg.vector_norm(allv[k][1]))
+        variant = {"form": "tf32x2", "value": world * N_LEVELS * args.steps / (msv * 1e-3), "unit": "levels/s",
+                   "ms_per_step": msv / args.steps, "median_ms_per_step": statistics.median(perv),
+                   "speedup_vs_fp64_gpu": (world * N_LEVELS * args.steps / (msv * 1e-3)) / lev64,
+                   "max_normwise_per_call": max(nwv.values()), "normwise_per_call": nwv}
+        sv.close()
+        del gv, lv
+
     # ---- per-phase kernel timing (CUDA events on the launching stream)
     sm.set_profiling(True)
     sm.phase_times(reset=True)
@@ -465,7 +493,7 @@ def our_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "median_ms_per_step": statistics.median(per_step), "timing": "graph replay of one step, CUDA events per step",
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fp32": "f32", "bf16x3": "bf16x3+f32", "fp64": "f64"}[form],
+            "dtype": {"fp32": "f32", "bf16x3": "bf16x3+f32", "tf32x2": "tf32x2+f32", "fp64": "f64"}[form],
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": form, "l_max": L_MAX, "n_theta": N_THETA,
                        "n_phi": N_PHI, "minc": MINC, "n_levels": N_LEVELS,
@@ -475,6 +503,7 @@ def our_arm(args):
                          "steps": k64, "legendre_frac_of_fp64_peak": fp64_leg_frac,
                          "phases": phases64},
             "speedup_vs_fp64_gpu": value / lev64,
+            "variant": variant,
             "rel_l2_vs_fp64": {"max": max_err, "max_abs_over_max": maxabs, "per_field": errs,
                                "max_normwise_per_call": max_normwise, "normwise_per_call": normwise},
             "roofline": roof,

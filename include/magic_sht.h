@@ -39,6 +39,8 @@ extern "C" {
 #define MAGIC_SHT_FP64 0    /* FP64 everywhere: the parity form */
 #define MAGIC_SHT_FP32 1    /* FP32 tables, FFTs and accumulation */
 #define MAGIC_SHT_BF16X3 2  /* tensor cores: 3xBF16 split products, FP32 accumulate, FP32 FFT */
+#define MAGIC_SHT_TF32X2 3  /* tensor cores: 2xTF32 split products (hi*hi, hi*lo, lo*hi), FP32 accumulate,
+                               FP32 FFT; persistent kernels only (no scal_to_spat_noalloc) */
 
 typedef struct magic_sht_desc {
   int l_max;       /* truncation degree (truncation.f90 l_max) */
@@ -47,7 +49,7 @@ typedef struct magic_sht_desc {
   int n_theta_max; /* Gauss points, multiple of 4 (truncation.f90:150) */
   int n_phi_max;   /* longitudes per symmetry sector, multiple of 4, 2^i 3^j 5^k */
   int nlat_padded; /* leading dimension of grid arrays; 0 -> n_theta_max */
-  int precision;   /* MAGIC_SHT_FP64 | MAGIC_SHT_FP32 | MAGIC_SHT_BF16X3 */
+  int precision;   /* MAGIC_SHT_FP64 | MAGIC_SHT_FP32 | MAGIC_SHT_BF16X3 | MAGIC_SHT_TF32X2 */
   int device;      /* CUDA device ordinal; -1 -> current device */
 } magic_sht_desc;
 
@@ -236,6 +238,8 @@ int magic_sht_measure_gflops(int device, int precision, double* gflops);
  * N = n (32/64/128/256), K = 64*kchunks (1 or 2) on bf16-exact inputs,
  * checked on the host; returns the max error relative to max |D|. */
 int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err);
+/* the same with tf32 operands (kind::tf32), K = 32*kchunks */
+int magic_sht_tc_selftest_tf32(int device, int n, int kchunks, double* max_rel_err);
 
 #ifdef __cplusplus
 }

@@ -14,8 +14,8 @@ LIB_PATH = os.path.join(HERE, "libmagic_sht.so")
 
 OK = 0
 ERR_ARG, ERR_SIZE, ERR_LCUT, ERR_CUDA, ERR_UNSUPPORTED, ERR_NOMEM, ERR_TIMEOUT = range(1, 8)
-FP64, FP32, BF16X3 = 0, 1, 2
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16x3": BF16X3}
+FP64, FP32, BF16X3, TF32X2 = 0, 1, 2, 3
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16x3": BF16X3, "tf32x2": TF32X2}
 PHASES = ["inv_leg_scalar", "inv_leg_vector", "fft_inv", "fft_fwd", "fwd_leg_scalar",
           "fwd_leg_vector"]
 
@@ -95,6 +95,7 @@ SIGNATURES = {
     "magic_sht_launch_count": [_V, ctypes.POINTER(ctypes.c_longlong)],
     "magic_sht_device_status": [_V, ctypes.c_int],
     "magic_sht_tc_selftest": [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D],
+    "magic_sht_tc_selftest_tf32": [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D],
 }
 
 _lib = None

@@ -27,21 +27,22 @@ cudaError_t convert_tables_fp32(const double* P, const double* dP, float* P32, f
 cudaError_t launch_fma_peak(void* out, bool fp64, int blocks, int iters, cudaStream_t st);
 
 // legendre_tc.cu
-cudaError_t launch_tc_selftest(int n, int kchunks, const float* A, const float* B, float* D, int* err,
+cudaError_t launch_tc_selftest(int n, int kchunks, bool tf32, const float* A, const float* B, float* D, int* err,
                                cudaStream_t st);
-void tc_table_layout(const ShtGeom& g, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
+void tc_table_layout(const ShtGeom& g, bool tf32, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
                      std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks);
-cudaError_t build_tc_images(const ShtGeom& g, const TcTables& t, unsigned char* inv_img, float* inv_scale,
+cudaError_t build_tc_images(const ShtGeom& g, const TcTables& t, bool tf32, unsigned char* inv_img, float* inv_scale,
                             unsigned char* fwd_img, float* fwd_scale, cudaStream_t st);
 cudaError_t launch_inv_legendre_tc(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
                                    cudaStream_t st);
 cudaError_t launch_fwd_legendre_tc(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
                                    cudaStream_t st);
 // legendre_tcp.cu (pack kernels + persistent, warp-specialized tensor-core kernels)
-size_t tcp_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool vec, bool inverse);
-cudaError_t launch_inv_legendre_tcp(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
+// tf32: the 2 x TF32 split form (kind::tf32) instead of 3 x BF16
+size_t tcp_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool vec, bool inverse, bool tf32);
+cudaError_t launch_inv_legendre_tcp(const ShtGeom& g, const InvSet& s, bool vec, bool tf32, const TcTables& t,
                                     unsigned char* bimg, cudaStream_t st);
-cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
+cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec, bool tf32, const TcTables& t,
                                     unsigned char* bimg, cudaStream_t st);
 
 // nl.cu

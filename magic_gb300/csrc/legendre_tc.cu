@@ -15,7 +15,9 @@
 namespace {
 
 // D[128][N] = A[128][K] * B[N][K]^T, K = 64*kchunks, one CTA of 4 warps.
-template <int N>
+// TF32 = false: bf16 operands, K tiles of 64 (kind::f16, K = 16 per MMA);
+// true: tf32 operands, K tiles of 32 (kind::tf32, K = 8 per MMA).
+template <int N, bool TF32>
 __global__ void __launch_bounds__(128) tc_selftest_kernel(const float* __restrict__ A,
                                                           const float* __restrict__ B, float* __restrict__ D,
                                                           int kchunks, int* __restrict__ err) {
@@ -26,15 +28,18 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float* __restric
   unsigned char* sA = base;                       // kchunks x [128][64] bf16
   unsigned char* sB = sA + 16384 * kchunks;       // kchunks x [N][64] bf16
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int K = 64 * kchunks;
+  constexpr int KW = TF32 ? 32 : 64;  // K per 128-byte tile row
+  const int K = KW * kchunks;
   constexpr uint32_t NCOL = N < 32 ? 32 : N;
   for (int i = tid; i < 128 * K; i += 128) {
     const int r = i / K, k = i - r * K;
-    *(__nv_bfloat16*)(sA + (k >> 6) * 16384 + tc::sw128_offset(r, k & 63)) = __float2bfloat16_rn(A[i]);
+    if (TF32) *(float*)(sA + (k / KW) * 16384 + tc::sw128_offset32(r, k % KW)) = A[i];
+    else *(__nv_bfloat16*)(sA + (k / KW) * 16384 + tc::sw128_offset(r, k % KW)) = __float2bfloat16_rn(A[i]);
   }
   for (int i = tid; i < N * K; i += 128) {
     const int r = i / K, k = i - r * K;
-    *(__nv_bfloat16*)(sB + (k >> 6) * (N * 128) + tc::sw128_offset(r, k & 63)) = __float2bfloat16_rn(B[i]);
+    if (TF32) *(float*)(sB + (k / KW) * (N * 128) + tc::sw128_offset32(r, k % KW)) = B[i];
+    else *(__nv_bfloat16*)(sB + (k / KW) * (N * 128) + tc::sw128_offset(r, k % KW)) = __float2bfloat16_rn(B[i]);
   }
   if (tid == 0) {
     tc::mbar_init(&bar, 1);
@@ -50,12 +55,13 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float* __restric
   tc::tc_fence_after();
   const uint32_t tmem = tmem_base;
   if (tid == 0) {
-    constexpr uint32_t idesc = tc::idesc_bf16(128, N);
+    constexpr uint32_t idesc = TF32 ? tc::idesc_tf32(128, N) : tc::idesc_bf16(128, N);
     for (int c = 0; c < kchunks; ++c)
-      for (int ks = 0; ks < 4; ++ks) {
+      for (int ks = 0; ks < 4; ++ks) {  // 32 bytes of K per MMA in both formats
         const uint64_t ad = tc::sw128_desc(tc::smem_u32(sA + c * 16384) + ks * 32);
         const uint64_t bd = tc::sw128_desc(tc::smem_u32(sB + c * (N * 128)) + ks * 32);
-        tc::mma_bf16(tmem, ad, bd, idesc, (c | ks) ? 1u : 0u);
+        if (TF32) tc::mma_tf32(tmem, ad, bd, idesc, (c | ks) ? 1u : 0u);
+        else tc::mma_bf16(tmem, ad, bd, idesc, (c | ks) ? 1u : 0u);
       }
     tc::mma_commit(&bar);
   }
@@ -76,23 +82,29 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float* __restric
 }
 
 template <int N>
-cudaError_t launch_selftest(const float* A, const float* B, float* D, int kchunks, int* err, cudaStream_t st) {
+cudaError_t launch_selftest(const float* A, const float* B, float* D, int kchunks, bool tf32, int* err,
+                            cudaStream_t st) {
   const size_t smem = 1024 + (size_t)kchunks * (16384 + N * 128);
-  CUDA_TRY(cudaFuncSetAttribute(tc_selftest_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  tc_selftest_kernel<N><<<1, 128, smem, st>>>(A, B, D, kchunks, err);
+  if (tf32) {
+    CUDA_TRY(cudaFuncSetAttribute(tc_selftest_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    tc_selftest_kernel<N, true><<<1, 128, smem, st>>>(A, B, D, kchunks, err);
+  } else {
+    CUDA_TRY(cudaFuncSetAttribute(tc_selftest_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    tc_selftest_kernel<N, false><<<1, 128, smem, st>>>(A, B, D, kchunks, err);
+  }
   return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_tc_selftest(int n, int kchunks, const float* A, const float* B, float* D, int* err,
+cudaError_t launch_tc_selftest(int n, int kchunks, bool tf32, const float* A, const float* B, float* D, int* err,
                                cudaStream_t st) {
   if (kchunks < 1 || kchunks > 2) return cudaErrorInvalidValue;
   switch (n) {
-    case 32: return launch_selftest<32>(A, B, D, kchunks, err, st);
-    case 64: return launch_selftest<64>(A, B, D, kchunks, err, st);
-    case 128: return launch_selftest<128>(A, B, D, kchunks, err, st);
-    case 256: return launch_selftest<256>(A, B, D, kchunks, err, st);
+    case 32: return launch_selftest<32>(A, B, D, kchunks, tf32, err, st);
+    case 64: return launch_selftest<64>(A, B, D, kchunks, tf32, err, st);
+    case 128: return launch_selftest<128>(A, B, D, kchunks, tf32, err, st);
+    case 256: return launch_selftest<256>(A, B, D, kchunks, tf32, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -500,6 +512,23 @@ __global__ void __launch_bounds__(TC_THREADS, 2) fwd_leg_tc(const ShtGeom g, con
 }
 
 // ------------------------------------------------------- table images
+// TF32 = false: 3 bf16 splits per 64-wide K chunk (3 blocks); true: 2 TF32
+// splits x 2 K tiles of 32 (4 blocks, block = 2 * split + K tile).
+template <bool TF32>
+__device__ __forceinline__ void store_table_value(unsigned char* img, long long blk0, int row, int k, double v) {
+  if (!TF32) {
+    __nv_bfloat16 h[3];
+    tc::split3((float)v, h[0], h[1], h[2]);
+    for (int sp = 0; sp < 3; ++sp) *(__nv_bfloat16*)(img + (blk0 + sp) * 16384 + tc::sw128_offset(row, k)) = h[sp];
+  } else {
+    float h[2];
+    tc::split_tf32((float)v, h[0], h[1]);
+    for (int sp = 0; sp < 2; ++sp)
+      *(float*)(img + (blk0 + 2 * sp + (k >> 5)) * 16384 + tc::sw128_offset32(row, k & 31)) = h[sp];
+  }
+}
+
+template <bool TF32>
 __global__ void build_inv_img_kernel(const ShtGeom g, TcTables t, unsigned char* img, float* scale) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int NHP = t.ntt * 128;
@@ -522,19 +551,17 @@ __global__ void build_inv_img_kernel(const ShtGeom g, TcTables t, unsigned char*
   const double inv = live ? ldexp(1.0, -e) : 0.0;
   const int nch = tc_nch(n_l);
   const int tt = j / 128, row = j % 128;
+  constexpr int BPC = TF32 ? 4 : 3;  // 16 KB blocks per chunk
   for (int p = 0; p < 2; ++p)
     for (int lp = 0; lp < nch * 64; ++lp) {
       const int loff = p + 2 * lp;
       const double v = (valid && loff < n_l) ? tab[(size_t)(lm0 + loff) * g.nh + j] * inv : 0.0;
-      __nv_bfloat16 h[3];
-      tc::split3((float)v, h[0], h[1], h[2]);
-      for (int sp = 0; sp < 3; ++sp) {
-        const long long blk = t.inv_blk0[mc] + ((((long long)tt * 2 + tb) * 2 + p) * nch + lp / 64) * 3 + sp;
-        *(__nv_bfloat16*)(img + blk * 16384 + tc::sw128_offset(row, lp % 64)) = h[sp];
-      }
+      const long long blk0 = t.inv_blk0[mc] + ((((long long)tt * 2 + tb) * 2 + p) * nch + lp / 64) * BPC;
+      store_table_value<TF32>(img, blk0, row, lp % 64, v);
     }
 }
 
+template <bool TF32>
 __global__ void build_fwd_img_kernel(const ShtGeom g, TcTables t, unsigned char* img, float* scale) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int NLP = t.nlt * 128;
@@ -556,14 +583,11 @@ __global__ void build_fwd_img_kernel(const ShtGeom g, TcTables t, unsigned char*
   if (valid) scale[(size_t)tb * g.lm_max + lm0 + loff] = live ? ldexpf(1.0f, e) : 0.0f;
   const double inv = live ? ldexp(1.0, -e) : 0.0;
   const int lt = lpad / 128, row = lpad % 128;
+  constexpr int BPC = TF32 ? 4 : 3;
   for (int j = 0; j < t.ncj * 64; ++j) {
     const double v = (valid && j < g.nh) ? tab[(size_t)(lm0 + loff) * g.nh + j] * inv : 0.0;
-    __nv_bfloat16 h[3];
-    tc::split3((float)v, h[0], h[1], h[2]);
-    for (int sp = 0; sp < 3; ++sp) {
-      const long long blk = t.fwd_blk0[mc] + ((((long long)p * t.nlt + lt) * 2 + tb) * t.ncj + j / 64) * 3 + sp;
-      *(__nv_bfloat16*)(img + blk * 16384 + tc::sw128_offset(row, j % 64)) = h[sp];
-    }
+    const long long blk0 = t.fwd_blk0[mc] + ((((long long)p * t.nlt + lt) * 2 + tb) * t.ncj + j / 64) * BPC;
+    store_table_value<TF32>(img, blk0, row, j % 64, v);
   }
 }
 
@@ -592,8 +616,9 @@ cudaError_t launch_fwd_tc_t(const ShtGeom& g, const FwdSet& s, const TcTables& t
 
 }  // namespace
 
-void tc_table_layout(const ShtGeom& g, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
+void tc_table_layout(const ShtGeom& g, bool tf32, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
                      std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks) {
+  const int bpc = tf32 ? 4 : 3;
   *ntt = (g.nh + 127) / 128;
   *nlt = ((g.l_max + 2) / 2 + 127) / 128;
   *ncj = (g.nh + 63) / 64;
@@ -603,24 +628,28 @@ void tc_table_layout(const ShtGeom& g, int* ntt, int* nlt, int* ncj, std::vector
   for (int mc = 0; mc < g.n_m; ++mc) {
     const int n_l = g.l_max - mc * g.minc + 1;
     inv_blk0[mc] = bi;
-    bi += (long long)(*ntt) * 2 * 2 * tc_nch(n_l) * 3;
+    bi += (long long)(*ntt) * 2 * 2 * tc_nch(n_l) * bpc;
     fwd_blk0[mc] = bf;
-    bf += 2LL * (*nlt) * 2 * (*ncj) * 3;
+    bf += 2LL * (*nlt) * 2 * (*ncj) * bpc;
   }
   *inv_blocks = bi;
   *fwd_blocks = bf;
 }
 
-cudaError_t build_tc_images(const ShtGeom& g, const TcTables& t, unsigned char* inv_img, float* inv_scale,
-                            unsigned char* fwd_img, float* fwd_scale, cudaStream_t st) {
+cudaError_t build_tc_images(const ShtGeom& g, const TcTables& t, bool tf32, unsigned char* inv_img,
+                            float* inv_scale, unsigned char* fwd_img, float* fwd_scale, cudaStream_t st) {
   {
     const long long n = (long long)g.n_m * 2 * t.ntt * 128;
-    build_inv_img_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g, t, inv_img, inv_scale);
+    const unsigned nb = (unsigned)((n + 127) / 128);
+    if (tf32) build_inv_img_kernel<true><<<nb, 128, 0, st>>>(g, t, inv_img, inv_scale);
+    else build_inv_img_kernel<false><<<nb, 128, 0, st>>>(g, t, inv_img, inv_scale);
     CUDA_TRY(cudaGetLastError());
   }
   {
     const long long n = (long long)g.n_m * 4 * t.nlt * 128;
-    build_fwd_img_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g, t, fwd_img, fwd_scale);
+    const unsigned nb = (unsigned)((n + 127) / 128);
+    if (tf32) build_fwd_img_kernel<true><<<nb, 128, 0, st>>>(g, t, fwd_img, fwd_scale);
+    else build_fwd_img_kernel<false><<<nb, 128, 0, st>>>(g, t, fwd_img, fwd_scale);
     CUDA_TRY(cudaGetLastError());
   }
   return cudaSuccess;

@@ -42,11 +42,24 @@ namespace {
 
 constexpr int kNC = 64;  // real data columns per tile (32 complex)
 
-// ring depths: A = table splits (NT x 16 KB per slot), B = data tiles
+// ring depths: A = one table split of one K tile (NT x 16 KB per slot), B = data tiles
 template <bool VEC, bool INV>
 struct Rings {
   static constexpr int NA = VEC ? 3 : 4;
   static constexpr int NB = VEC ? 2 : 3;
+};
+
+// Split format of the tensor-core form.  TF32 = false: 3 bf16 splits, one K
+// tile of 64 per chunk, kind::f16.  TF32 = true: 2 tf32 splits (hi, lo), two K
+// tiles of 32 per chunk, kind::tf32, products hi*hi, hi*lo, lo*hi.
+template <bool TF32>
+struct Form {
+  static constexpr int SPA = TF32 ? 2 : 3;            // table splits
+  static constexpr int KT = TF32 ? 2 : 1;             // K tiles per 64-wide chunk
+  static constexpr int AUSES = SPA * KT;              // A-ring uses per chunk
+  static constexpr int BPC = TF32 ? 4 : 3;            // 16 KB table blocks per chunk
+  static constexpr int NACCS = TF32 ? 2 : 3;          // accumulators per table
+  static constexpr uint32_t OPSZ = DataTile<TF32, kNC>::bytes;  // data operand per chunk
 };
 
 constexpr int kThreads = 320;     // 10 warps
@@ -99,26 +112,46 @@ __device__ __forceinline__ bool ring_pop(const TileRing& R, uint32_t& use, int& 
   return true;
 }
 
-// Issue the MMAs of table split `sp` (NT tables) against the stacked data
-// splits; D holds NT accumulator groups of 3*kNC columns.
-template <int NT>
-__device__ __forceinline__ void issue_split(uint32_t acc, const unsigned char* A, const unsigned char* B,
-                                            int sp, bool first_chunk, uint32_t bstride_tb) {
-  constexpr uint32_t ID3 = tc::idesc_bf16(128, 3 * kNC), ID2 = tc::idesc_bf16(128, 2 * kNC),
-                     ID1 = tc::idesc_bf16(128, kNC);
+// Issue the MMAs of A-ring use `u` of a chunk (NT tables) against the stacked
+// data splits; D holds NT accumulator groups of NACCS*kNC columns.
+//  bf16 (u = split):  A_hi x [B_hi|B_mid|B_lo] -> [C0|C1|C2],  A_mid x [B_hi|B_mid]
+//                     -> [C1|C2],  A_lo x B_hi -> C2   (K = 16 per MMA, 4 per tile)
+//  tf32 (u = 2*K tile + split):  A_hi x [B_hi|B_lo] -> [C0|C1],  A_lo x B_hi -> C1
+//                     (K = 8 per MMA, 4 per 32-wide K tile)
+template <int NT, bool TF32>
+__device__ __forceinline__ void issue_use(uint32_t acc, const unsigned char* A, const unsigned char* B,
+                                          int u, bool first_chunk, uint32_t bstride_tb) {
+  constexpr int NACCS = Form<TF32>::NACCS;
   const uint64_t a0 = tc::sw128_desc(tc::smem_u32(A));
   const uint64_t bd0 = tc::sw128_desc(tc::smem_u32(B));
+  if constexpr (!TF32) {
+    constexpr uint32_t ID3 = tc::idesc_bf16(128, 3 * kNC), ID2 = tc::idesc_bf16(128, 2 * kNC),
+                       ID1 = tc::idesc_bf16(128, kNC);
 #pragma unroll
-  for (int ks = 0; ks < 4; ++ks)
+    for (int ks = 0; ks < 4; ++ks)
 #pragma unroll
-    for (int tb = 0; tb < NT; ++tb) {
-      const uint32_t d = acc + (uint32_t)(tb * 3 * kNC);
-      const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
-      const uint64_t bd = bd0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
-      if (sp == 0) tc::mma_bf16(d, ad, bd, ID3, (!first_chunk || ks) ? 1u : 0u);
-      else if (sp == 1) tc::mma_bf16(d + kNC, ad, bd, ID2, 1u);
-      else tc::mma_bf16(d + 2 * kNC, ad, bd, ID1, 1u);
-    }
+      for (int tb = 0; tb < NT; ++tb) {
+        const uint32_t d = acc + (uint32_t)(tb * NACCS * kNC);
+        const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
+        const uint64_t bd = bd0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
+        if (u == 0) tc::mma_bf16(d, ad, bd, ID3, (!first_chunk || ks) ? 1u : 0u);
+        else if (u == 1) tc::mma_bf16(d + kNC, ad, bd, ID2, 1u);
+        else tc::mma_bf16(d + 2 * kNC, ad, bd, ID1, 1u);
+      }
+  } else {
+    constexpr uint32_t ID2 = tc::idesc_tf32(128, 2 * kNC), ID1 = tc::idesc_tf32(128, kNC);
+    const int kt = u >> 1, sp = u & 1;
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks)
+#pragma unroll
+      for (int tb = 0; tb < NT; ++tb) {
+        const uint32_t d = acc + (uint32_t)(tb * NACCS * kNC);
+        const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
+        const uint64_t bd = bd0 + (uint64_t)((tb * bstride_tb + kt * 2 * kNC * 128 + ks * 32) >> 4);
+        if (sp == 0) tc::mma_tf32(d, ad, bd, ID2, (!first_chunk || kt || ks) ? 1u : 0u);
+        else tc::mma_tf32(d + kNC, ad, bd, ID1, 1u);
+      }
+  }
 }
 
 // Pointer held by lane `src` (whole warp participates).
@@ -130,19 +163,29 @@ __device__ __forceinline__ P* shfl_ptr(P* p, int src) {
   return (P*)(((unsigned long long)hi << 32) | lo);
 }
 
-// (C2 + C1) + C0 of one table for the 32 columns at TMEM address `col`
-// (this warp's lane quadrant).
+// Accumulators of one table summed smallest first, (C2 + C1) + C0 (bf16) or
+// C1 + C0 (tf32), for the 32 columns at TMEM address `col` (this warp's lane
+// quadrant).
+template <bool TF32>
 __device__ __forceinline__ void drain_sum(uint32_t col, float (&v)[32]) {
   uint32_t a[32], b[32];
-  tc::tmem_ld32_nw(col + 2 * kNC, a);
-  tc::tmem_ld32_nw(col + kNC, b);
-  tc::tmem_wait_ld();
+  if (!TF32) {
+    tc::tmem_ld32_nw(col + 2 * kNC, a);
+    tc::tmem_ld32_nw(col + kNC, b);
+    tc::tmem_wait_ld();
 #pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(a[i]) + __uint_as_float(b[i]);
-  tc::tmem_ld32_nw(col, a);
-  tc::tmem_wait_ld();
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(a[i]) + __uint_as_float(b[i]);
+    tc::tmem_ld32_nw(col, a);
+    tc::tmem_wait_ld();
 #pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] += __uint_as_float(a[i]);
+    for (int i = 0; i < 32; ++i) v[i] += __uint_as_float(a[i]);
+  } else {
+    tc::tmem_ld32_nw(col + kNC, b);
+    tc::tmem_ld32_nw(col, a);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(b[i]) + __uint_as_float(a[i]);
+  }
 }
 
 // ------------------------------------------------------------------ packing
@@ -150,12 +193,12 @@ __device__ __forceinline__ void drain_sum(uint32_t col, float (&v)[32]) {
 // shared memory and written with one bulk copy.
 // Synthesis data images: [pc = bpc0[m] + p*nch + c][ct] tiles of 3 splits.
 // One CTA builds both parity tiles of chunk c from 128 consecutive degrees.
-template <bool VEC>
+template <bool VEC, bool TF32>
 __global__ void __launch_bounds__(kPackThreads, 4) pack_inv_kernel(const ShtGeom g, const InvSet s,
                                                                   const TcTables t,
                                                                   unsigned char* __restrict__ bimg, int nct) {
   constexpr int NC = kNC;
-  constexpr uint32_t BSZ = 3u * NC * 128u;
+  constexpr uint32_t BSZ = Form<TF32>::OPSZ;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* B = align1k(smem_raw);
   const int ct = blockIdx.x, mc = blockIdx.y, c = blockIdx.z;
@@ -164,7 +207,7 @@ __global__ void __launch_bounds__(kPackThreads, 4) pack_inv_kernel(const ShtGeom
   if (c >= nch) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  inv_build_pair<VEC, NC, 1>(g, s, B, ct, ncplx, m, g.lmoff[mc], c, warp, kPackThreads / 32, lane);
+  inv_build_pair<VEC, NC, 1, TF32>(g, s, B, ct, ncplx, m, g.lmoff[mc], c, warp, kPackThreads / 32, lane);
   tc::fence_proxy_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -178,18 +221,18 @@ __global__ void __launch_bounds__(kPackThreads, 4) pack_inv_kernel(const ShtGeom
 
 // Analysis data images: [m][c][ct] pairs (ES tile, EA tile) of 3 splits each,
 // both built by one CTA from the (ES, EA) entries of 64 colatitudes.
-template <bool VEC>
+template <bool VEC, bool TF32>
 __global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_kernel(const ShtGeom g, const FwdSet s,
                                                                   const TcTables t,
                                                                   unsigned char* __restrict__ bimg, int nct) {
   constexpr int NC = kNC;
-  constexpr uint32_t PSZ = 2u * 3u * NC * 128u;
+  constexpr uint32_t PSZ = 2u * Form<TF32>::OPSZ;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* B = align1k(smem_raw);
   const int ct = blockIdx.x, mc = blockIdx.y, c = blockIdx.z;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  fwd_build_tile<VEC, NC, 2, true>(g, s, B, ct, ncplx, mc, 0, c, warp, kPackThreads / 32, lane);
+  fwd_build_tile<VEC, NC, 2, true, TF32>(g, s, B, ct, ncplx, mc, 0, c, warp, kPackThreads / 32, lane);
   tc::fence_proxy_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -216,17 +259,18 @@ struct InvTile {
   }
 };
 
-template <bool VEC>
+template <bool VEC, bool TF32>
 __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, const InvSet s, const TcTables t,
                                                            const unsigned char* __restrict__ bimg, int nct) {
+  typedef Form<TF32> F;
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NC = kNC;
   constexpr int NA = Rings<VEC, true>::NA;
   constexpr int NB = Rings<VEC, true>::NB;
-  constexpr int NACC = VEC ? 1 : 2;  // accumulator sets (3*NC columns per table)
-  constexpr int BSZ = 3 * NC * 128;
+  constexpr uint32_t ACC = NT * F::NACCS * NC;  // one accumulator set
+  constexpr int NACC = 2 * ACC <= 512 ? 2 : 1;  // sets in the 512 TMEM columns
+  constexpr int BSZ = F::OPSZ;
   constexpr int ASZ = NT * 16384;
-  constexpr uint32_t ACC = NT * 3 * NC;
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[NACC], acc_empty[NACC], fin;
   __shared__ uint64_t tr_full[kNTR], tr_empty[kNTR];
@@ -280,13 +324,14 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
           tc::bulk_g2s(sB + bslot * BSZ, bimg + ((t.bpc0[T.mc] + T.p * T.nch + c) * nct + T.ct) * (long long)BSZ,
                        BSZ, &b_full[bslot]);
           ++b_use;
-          for (int sp = 0; sp < 3; ++sp, ++a_use) {
+          for (int u = 0; u < F::AUSES; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_empty(&a_empty[slot], a_use, NA)) { ok = false; break; }
             tc::mbar_expect_tx(&a_full[slot], ASZ);
+            const int blk_u = TF32 ? 2 * (u & 1) + (u >> 1) : u;  // tf32 blocks: 2 * split + K tile
             for (int tb = 0; tb < NT; ++tb) {
               const long long blk =
-                  t.inv_blk0[T.mc] + ((((long long)T.tt * 2 + tb) * 2 + T.p) * T.nch + c) * 3 + sp;
+                  t.inv_blk0[T.mc] + ((((long long)T.tt * 2 + tb) * 2 + T.p) * T.nch + c) * F::BPC + blk_u;
               tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.inv_img + blk * 16384, 16384, &a_full[slot]);
             }
           }
@@ -311,11 +356,11 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
         for (int c = 0; c < T.nchp && ok; ++c, ++b_use) {
           const uint32_t bslot = b_use % NB;
           if (!wait_full(&b_full[bslot], b_use, NB)) { ok = false; break; }
-          for (int sp = 0; sp < 3; ++sp, ++a_use) {
+          for (int u = 0; u < F::AUSES; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_split<NT>(acc, sA + slot * ASZ, sB + bslot * BSZ, sp, c == 0, 0);
+            issue_use<NT, TF32>(acc, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, 0);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -377,8 +422,8 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
       tc::tc_fence_after();
       const uint32_t acc = tmem + abuf * ACC + lane_off + cc0;
       float P[32], D[32];
-      drain_sum(acc, P);
-      if (VEC) drain_sum(acc + 3 * NC, D);
+      drain_sum<TF32>(acc, P);
+      if (VEC) drain_sum<TF32>(acc + F::NACCS * NC, D);
       tc::tc_fence_before();
       tc::mbar_arrive(&acc_empty[abuf]);  // tensor memory free for the next tile
       ++acc_use;
@@ -438,18 +483,19 @@ struct FwdTile {
   }
 };
 
-template <bool VEC>
+template <bool VEC, bool TF32>
 __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, const FwdSet s, const TcTables t,
                                                            const unsigned char* __restrict__ bimg, int nct) {
+  typedef Form<TF32> F;
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NC = kNC;
   constexpr int NA = Rings<VEC, false>::NA;
   constexpr int NB = Rings<VEC, false>::NB;
-  constexpr int NACC = VEC ? 1 : 2;
-  constexpr int TS = 3 * NC * 128;  // one data operand (3 splits)
+  constexpr uint32_t ACC = NT * F::NACCS * NC;
+  constexpr int NACC = 2 * ACC <= 512 ? 2 : 1;
+  constexpr int TS = F::OPSZ;       // one data operand
   constexpr int ASZ = NT * 16384;
   constexpr int BSZ = NT * TS;      // mine (and other)
-  constexpr uint32_t ACC = NT * 3 * NC;
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t a_full[NA], a_empty[NA], b_full[NB], b_empty[NB], acc_full[NACC], acc_empty[NACC], fin;
   __shared__ uint64_t tr_full[kNTR], tr_empty[kNTR];
@@ -504,13 +550,14 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
           tc::bulk_g2s(sB + bslot * BSZ, img + T.p * TS, TS, &b_full[bslot]);                    // mine
           if (VEC) tc::bulk_g2s(sB + bslot * BSZ + TS, img + (1 - T.p) * TS, TS, &b_full[bslot]);  // other
           ++b_use;
-          for (int sp = 0; sp < 3; ++sp, ++a_use) {
+          for (int u = 0; u < F::AUSES; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_empty(&a_empty[slot], a_use, NA)) { ok = false; break; }
             tc::mbar_expect_tx(&a_full[slot], ASZ);
+            const int blk_u = TF32 ? 2 * (u & 1) + (u >> 1) : u;
             for (int tb = 0; tb < NT; ++tb) {
               const long long blk =
-                  t.fwd_blk0[T.mc] + ((((long long)T.p * t.nlt + T.lt) * 2 + tb) * t.ncj + c) * 3 + sp;
+                  t.fwd_blk0[T.mc] + ((((long long)T.p * t.nlt + T.lt) * 2 + tb) * t.ncj + c) * F::BPC + blk_u;
               tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.fwd_img + blk * 16384, 16384, &a_full[slot]);
             }
           }
@@ -535,11 +582,11 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
         for (int c = 0; c < t.ncj && ok; ++c, ++b_use) {
           const uint32_t bslot = b_use % NB;
           if (!wait_full(&b_full[bslot], b_use, NB)) { ok = false; break; }
-          for (int sp = 0; sp < 3; ++sp, ++a_use) {
+          for (int u = 0; u < F::AUSES; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_split<NT>(acc, sA + slot * ASZ, sB + bslot * BSZ, sp, c == 0, TS);
+            issue_use<NT, TF32>(acc, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, TS);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -567,8 +614,8 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
       tc::tc_fence_after();
       const uint32_t acc = tmem + abuf * ACC + lane_off + cc0;
       float D0[32], D1[32];
-      drain_sum(acc, D0);
-      if (VEC) drain_sum(acc + 3 * NC, D1);
+      drain_sum<TF32>(acc, D0);
+      if (VEC) drain_sum<TF32>(acc + F::NACCS * NC, D1);
       tc::tc_fence_before();
       tc::mbar_arrive(&acc_empty[abuf]);
       ++acc_use;
@@ -645,63 +692,67 @@ int num_sms() {
   return n;
 }
 
-template <bool VEC>
+template <bool VEC, bool TF32>
 cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, unsigned char* bimg,
                          cudaStream_t st) {
   constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, true>::NA, NB = Rings<VEC, true>::NB;
+  constexpr size_t OPSZ = Form<TF32>::OPSZ;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
-  const size_t psmem = 1024 + 2 * 3 * (size_t)NC * 128;
-  CUDA_TRY(cudaFuncSetAttribute(pack_inv_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_inv_kernel<VEC><<<dim3(nct, g.n_m, tc_nch(g.l_max + 1)), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  const size_t psmem = 1024 + 2 * OPSZ;
+  CUDA_TRY(cudaFuncSetAttribute(pack_inv_kernel<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  pack_inv_kernel<VEC, TF32><<<dim3(nct, g.n_m, tc_nch(g.l_max + 1)), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
   CUDA_TRY(cudaGetLastError());
-  const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * 3 * NC * 128;
-  CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * OPSZ;
+  CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
   const int grid = (int)std::min<long long>(ntiles, num_sms());
   CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  inv_leg_tcp<VEC><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
+  inv_leg_tcp<VEC, TF32><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
   return cudaGetLastError();
 }
 
-template <bool VEC>
+template <bool VEC, bool TF32>
 cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, unsigned char* bimg,
                          cudaStream_t st) {
   constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, false>::NA, NB = Rings<VEC, false>::NB;
+  constexpr size_t OPSZ = Form<TF32>::OPSZ;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
-  const size_t psmem = 1024 + 2 * 3 * (size_t)NC * 128;
-  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_fwd_kernel<VEC><<<dim3(nct, g.n_m, t.ncj), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  const size_t psmem = 1024 + 2 * OPSZ;
+  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_kernel<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  pack_fwd_kernel<VEC, TF32><<<dim3(nct, g.n_m, t.ncj), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
   CUDA_TRY(cudaGetLastError());
-  const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * 3 * NC * 128;
-  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * OPSZ;
+  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
   const int grid = (int)std::min<long long>(ntiles, num_sms());
   CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  fwd_leg_tcp<VEC><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
+  fwd_leg_tcp<VEC, TF32><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-size_t tcp_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool vec, bool inverse) {
+size_t tcp_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool vec, bool inverse, bool tf32) {
   const int NC = kNC;
   (void)vec;
   const long long nct = (ncplx + NC / 2 - 1) / (NC / 2);
-  const long long tile = 3LL * NC * 128;
+  const long long tile = tf32 ? (long long)Form<true>::OPSZ : (long long)Form<false>::OPSZ;
   if (inverse) return (size_t)(t.npc * nct * tile);
   return (size_t)((long long)g.n_m * t.ncj * nct * 2 * tile);
 }
 
-cudaError_t launch_inv_legendre_tcp(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
+cudaError_t launch_inv_legendre_tcp(const ShtGeom& g, const InvSet& s, bool vec, bool tf32, const TcTables& t,
                                     unsigned char* bimg, cudaStream_t st) {
-  return vec ? launch_inv_p<true>(g, s, t, bimg, st) : launch_inv_p<false>(g, s, t, bimg, st);
+  if (tf32) return vec ? launch_inv_p<true, true>(g, s, t, bimg, st) : launch_inv_p<false, true>(g, s, t, bimg, st);
+  return vec ? launch_inv_p<true, false>(g, s, t, bimg, st) : launch_inv_p<false, false>(g, s, t, bimg, st);
 }
 
-cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
+cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec, bool tf32, const TcTables& t,
                                     unsigned char* bimg, cudaStream_t st) {
-  return vec ? launch_fwd_p<true>(g, s, t, bimg, st) : launch_fwd_p<false>(g, s, t, bimg, st);
+  if (tf32) return vec ? launch_fwd_p<true, true>(g, s, t, bimg, st) : launch_fwd_p<false, true>(g, s, t, bimg, st);
+  return vec ? launch_fwd_p<true, false>(g, s, t, bimg, st) : launch_fwd_p<false, false>(g, s, t, bimg, st);
 }

@@ -173,7 +173,10 @@ size_t hs_bytes(const magic_sht_handle* h, int nlev) {
 
 // Synthesis half spectra of a vector component in the tensor-core form hold
 // E and F for both parities: twice the entries of the N/S layout.
-bool tc_form(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_BF16X3; }
+bool tc_form(const magic_sht_handle* h) {
+  return h->precision == MAGIC_SHT_BF16X3 || h->precision == MAGIC_SHT_TF32X2;
+}
+bool tf32_form(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_TF32X2; }
 // data-operand images of the persistent tensor-core kernels (grown like the workspace)
 int ensure_bimg(magic_sht_handle* h, size_t bytes) {
   if (bytes <= h->bimg_bytes) return MAGIC_SHT_OK;
@@ -198,9 +201,9 @@ int inv_tc(magic_sht_handle* h, const ShtGeom& g, const InvSet& s, bool vec) {
     CK(launch_inv_legendre_tc(g, s, vec, h->tct, h->stream));
     return MAGIC_SHT_OK;
   }
-  TRY(ensure_bimg(h, tcp_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), vec, true)));
+  TRY(ensure_bimg(h, tcp_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), vec, true, tf32_form(h))));
   h->launches++;  // pack kernel + persistent kernel
-  CK(launch_inv_legendre_tcp(g, s, vec, h->tct, h->d_bimg, h->stream));
+  CK(launch_inv_legendre_tcp(g, s, vec, tf32_form(h), h->tct, h->d_bimg, h->stream));
   return MAGIC_SHT_OK;
 }
 int fwd_tc(magic_sht_handle* h, const ShtGeom& g, const FwdSet& s, bool vec) {
@@ -208,9 +211,9 @@ int fwd_tc(magic_sht_handle* h, const ShtGeom& g, const FwdSet& s, bool vec) {
     CK(launch_fwd_legendre_tc(g, s, vec, h->tct, h->stream));
     return MAGIC_SHT_OK;
   }
-  TRY(ensure_bimg(h, tcp_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), vec, false)));
+  TRY(ensure_bimg(h, tcp_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), vec, false, tf32_form(h))));
   h->launches++;  // pack kernel + persistent kernel
-  CK(launch_fwd_legendre_tcp(g, s, vec, h->tct, h->d_bimg, h->stream));
+  CK(launch_fwd_legendre_tcp(g, s, vec, tf32_form(h), h->tct, h->d_bimg, h->stream));
   return MAGIC_SHT_OK;
 }
 size_t hs_inv_bytes(const magic_sht_handle* h, int nlev, bool vec) {
@@ -417,7 +420,7 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = cx.dev(hs_sc[i]); f.out1 = nullptr; f.out_ld = hs_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_SCALAR);
-    if (h->precision == MAGIC_SHT_BF16X3) TRY(inv_tc(h, g, s, false));
+    if (tc_form(h)) TRY(inv_tc(h, g, s, false));
     else CK(launch_inv_legendre_simt(g, s, false, f64, h->stream));
   }
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
@@ -430,7 +433,7 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = cx.dev(hs_vc[2 * i]); f.out1 = cx.dev(hs_vc[2 * i + 1]); f.out_ld = hs_ld_v;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_VECTOR);
-    if (h->precision == MAGIC_SHT_BF16X3) TRY(inv_tc(h, g, s, true));
+    if (tc_form(h)) TRY(inv_tc(h, g, s, true));
     else CK(launch_inv_legendre_simt(g, s, true, f64, h->stream));
   }
   for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(cx.dev(hs_sc[i]), sc[i].out, sc[i].flags | flag_s, hs_ld));
@@ -458,7 +461,7 @@ int run_forward_vectors(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv, co
       f.out_ld = lv.spec_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_VECTOR);
-    if (h->precision == MAGIC_SHT_BF16X3) TRY(fwd_tc(h, g, s, true));
+    if (tc_form(h)) TRY(fwd_tc(h, g, s, true));
     else CK(launch_fwd_legendre_simt(g, s, true, f64, h->stream));
   }
   return MAGIC_SHT_OK;
@@ -504,7 +507,7 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
       f.out0 = (double2*)cx.dev(sc[i].out); f.out1 = nullptr; f.out_ld = lv.spec_ld;
     }
     PhaseScope ps(h, MAGIC_SHT_PHASE_FWD_LEG_SCALAR);
-    if (h->precision == MAGIC_SHT_BF16X3) TRY(fwd_tc(h, g, s, false));
+    if (tc_form(h)) TRY(fwd_tc(h, g, s, false));
     else CK(launch_fwd_legendre_simt(g, s, false, f64, h->stream));
   }
   return run_forward_vectors(h, cx, lv, vc, hs_vc, d_lcut);
@@ -647,7 +650,8 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   if (n_m > P / 2) return set_err(MAGIC_SHT_ERR_SIZE, "m_max/minc+1=%d exceeds n_phi_max/2=%d (aliasing)", n_m, P / 2);
   const int ld = d->nlat_padded > 0 ? d->nlat_padded : N;
   if (ld < N) return set_err(MAGIC_SHT_ERR_SIZE, "nlat_padded=%d < n_theta_max=%d", ld, N);
-  if (d->precision != MAGIC_SHT_FP64 && d->precision != MAGIC_SHT_FP32 && d->precision != MAGIC_SHT_BF16X3)
+  if (d->precision != MAGIC_SHT_FP64 && d->precision != MAGIC_SHT_FP32 && d->precision != MAGIC_SHT_BF16X3 &&
+      d->precision != MAGIC_SHT_TF32X2)
     return set_err(MAGIC_SHT_ERR_ARG, "unknown precision %d", d->precision);
 
   int dev = d->device;
@@ -723,15 +727,16 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   g.lmoff = h->d_lmoff;
   g.P64 = h->d_P; g.dP64 = h->d_dP; g.P32 = h->d_P32; g.dP32 = h->d_dP32;
   g.wgt = h->d_wgt; g.osin2 = h->d_osin2; g.tw64 = h->d_tw64; g.tw32 = h->d_tw32;
-  if (h->precision == MAGIC_SHT_BF16X3) {
+  if (tc_form(h)) {
     if (prop.major != 10)
       return fail(set_err(MAGIC_SHT_ERR_UNSUPPORTED, "the tensor-core form needs tcgen05 (sm_10x)"));
     const char* kern = getenv("MAGIC_SHT_TC_KERNEL");
-    h->tc_persistent = !(kern && strcmp(kern, "tiled") == 0);
+    // the TF32 form exists only in the persistent kernels
+    h->tc_persistent = tf32_form(h) || !(kern && strcmp(kern, "tiled") == 0);
     TcTables& t = h->tct;
     std::vector<long long> ib, fb;
     long long ninv = 0, nfwd = 0;
-    tc_table_layout(g, &t.ntt, &t.nlt, &t.ncj, ib, fb, &ninv, &nfwd);
+    tc_table_layout(g, tf32_form(h), &t.ntt, &t.nlt, &t.ncj, ib, fb, &ninv, &nfwd);
     INIT_CK(cudaMalloc((void**)&h->d_inv_img, (size_t)ninv * 16384));
     INIT_CK(cudaMalloc((void**)&h->d_fwd_img, (size_t)nfwd * 16384));
     INIT_CK(cudaMalloc((void**)&h->d_inv_blk0, sizeof(long long) * n_m));
@@ -756,7 +761,8 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     t.inv_blk0 = h->d_inv_blk0; t.fwd_blk0 = h->d_fwd_blk0;
     t.inv_scale = h->d_inv_scale; t.fwd_scale = h->d_fwd_scale;
     t.err = h->d_err;
-    INIT_CK(build_tc_images(g, t, h->d_inv_img, h->d_inv_scale, h->d_fwd_img, h->d_fwd_scale, h->stream));
+    INIT_CK(build_tc_images(g, t, tf32_form(h), h->d_inv_img, h->d_inv_scale, h->d_fwd_img, h->d_fwd_scale,
+                            h->stream));
     INIT_CK(cudaStreamSynchronize(h->stream));
   }
 #undef INIT_CK
@@ -852,10 +858,11 @@ int magic_sht_reserve(magic_sht_handle* h, int n) {
     // data images of the radial set's largest tensor-core launch (7 scalar + 4 vector
     // syntheses, 1 scalar + 3 vector analyses per level)
     const ShtGeom& g = h->g;
-    size_t b = tcp_data_bytes(g, h->tct, 7 * n, false, true);
-    b = std::max(b, tcp_data_bytes(g, h->tct, 4 * n * 2, true, true));
-    b = std::max(b, tcp_data_bytes(g, h->tct, n, false, false));
-    b = std::max(b, tcp_data_bytes(g, h->tct, 3 * n * 2, true, false));
+    const bool f = tf32_form(h);
+    size_t b = tcp_data_bytes(g, h->tct, 7 * n, false, true, f);
+    b = std::max(b, tcp_data_bytes(g, h->tct, 4 * n * 2, true, true, f));
+    b = std::max(b, tcp_data_bytes(g, h->tct, n, false, false, f));
+    b = std::max(b, tcp_data_bytes(g, h->tct, 3 * n * 2, true, false, f));
     TRY(ensure_bimg(h, b));
   }
   return MAGIC_SHT_OK;
@@ -1491,16 +1498,16 @@ int magic_sht_launch_count(const magic_sht_handle* h, long long* n) {
 }
 
 // ------------------------------------------------------------ self-test
-int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err) {
+static int tc_selftest(int device, int n, int kchunks, bool tf32, double* max_rel_err) {
   if (!max_rel_err) return set_err(MAGIC_SHT_ERR_ARG, "null output");
   if (!(n == 32 || n == 64 || n == 128 || n == 256) || kchunks < 1 || kchunks > 2)
     return set_err(MAGIC_SHT_ERR_ARG, "n must be 32/64/128/256 and kchunks 1 or 2");
   if (device < 0) CK(cudaGetDevice(&device));
   DeviceGuard dg(device);
-  const int K = 64 * kchunks;
+  const int K = (tf32 ? 32 : 64) * kchunks;
   std::vector<float> A((size_t)128 * K), B((size_t)n * K), D((size_t)128 * n);
   unsigned s = 12345u;
-  auto rnd = [&]() {  // small integers times powers of two: exact in bf16
+  auto rnd = [&]() {  // small integers times powers of two: exact in bf16 and tf32
     s = s * 1664525u + 1013904223u;
     const int v = (int)((s >> 9) % 255) - 127;
     const int e = (int)((s >> 20) % 7) - 3;
@@ -1518,7 +1525,7 @@ int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err) {
   CK(cudaMemcpy(dB, B.data(), B.size() * 4, cudaMemcpyHostToDevice));
   CK(cudaMemset(dD, 0, D.size() * 4));
   CK(cudaMemset(derr, 0, 4));
-  CK(launch_tc_selftest(n, kchunks, dA, dB, dD, derr, 0));
+  CK(launch_tc_selftest(n, kchunks, tf32, dA, dB, dD, derr, 0));
   CK(cudaDeviceSynchronize());
   int herr = 0;
   CK(cudaMemcpy(D.data(), dD, D.size() * 4, cudaMemcpyDeviceToHost));
@@ -1535,6 +1542,14 @@ int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err) {
     }
   *max_rel_err = worst / (scale > 0 ? scale : 1.0);
   return MAGIC_SHT_OK;
+}
+
+int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err) {
+  return tc_selftest(device, n, kchunks, false, max_rel_err);
+}
+
+int magic_sht_tc_selftest_tf32(int device, int n, int kchunks, double* max_rel_err) {
+  return tc_selftest(device, n, kchunks, true, max_rel_err);
 }
 
 // ------------------------------------------------------------ measurement
@@ -1620,6 +1635,9 @@ extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double*
   if (!is_device_ptr(Slm) || !is_device_ptr(fieldc))
     return set_err(MAGIC_SHT_ERR_ARG,
                    "scal_to_spat_noalloc takes device pointers only (host arrays would need staging buffers)");
+  if (tf32_form(h))
+    return set_err(MAGIC_SHT_ERR_UNSUPPORTED,
+                   "scal_to_spat_noalloc: the TF32 form has no allocation-free kernel (its data images need a buffer)");
   const ShtGeom& g = h->g;
   const size_t need = (size_t)g.n_m * g.n_theta * t2_bytes(h);
   if (need > MAGIC_SHT_NOALLOC_SCRATCH_BYTES)

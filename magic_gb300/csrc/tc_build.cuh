@@ -22,6 +22,25 @@ __device__ __forceinline__ void store_split1(unsigned char* tile0, uint32_t off,
   *(__nv_bfloat16*)(tile0 + 2 * tile_bytes + off) = lo;
 }
 
+// Data operand of one tile: TF32 = false: 3 bf16 splits, NC rows each (split
+// s at s * NC * 128 bytes); true: 2 K tiles of 32, each [hi rows | lo rows]
+// (2 * NC rows, 16 KB for NC = 64).
+template <bool TF32, int NC>
+struct DataTile {
+  static constexpr uint32_t bytes = TF32 ? 2u * 2u * NC * 128u : 3u * NC * 128u;
+  static __device__ __forceinline__ void store(unsigned char* tile, int row, int k, float v) {
+    if (!TF32) {
+      store_split1(tile, tc::sw128_offset(row, k), v, NC * 128);
+    } else {
+      float hi, lo;
+      tc::split_tf32(v, hi, lo);
+      unsigned char* t = tile + (k >> 5) * (2 * NC * 128);
+      *(float*)(t + tc::sw128_offset32(row, k & 31)) = hi;
+      *(float*)(t + tc::sw128_offset32(NC + row, k & 31)) = lo;
+    }
+  }
+};
+
 template <bool VEC, int NC, int CB>
 __device__ __forceinline__ void inv_build_tile(const ShtGeom& g, const InvSet& s, unsigned char* B, int ct,
                                                int ncplx, int m, int lm0, int p, int c, int ql0, int qstride,
@@ -97,7 +116,7 @@ __device__ __forceinline__ void inv_build_tile(const ShtGeom& g, const InvSet& s
 }
 
 // Analysis tile: "mine" at B, "other" at B + 3 tiles (written when BOTH).
-template <bool VEC, int NC, int CB, bool BOTH = VEC>
+template <bool VEC, int NC, int CB, bool BOTH = VEC, bool TF32 = false>
 __device__ __forceinline__ void fwd_build_tile(const ShtGeom& g, const FwdSet& s, unsigned char* B, int ct,
                                                int ncplx, int mc, int mine, int c, int ql0, int qstride,
                                                int lane) {
@@ -131,12 +150,13 @@ __device__ __forceinline__ void fwd_build_tile(const ShtGeom& g, const FwdSet& s
         float4 x = v[i][h];
         if (64 * c + k >= g.nh) x = make_float4(0.f, 0.f, 0.f, 0.f);
         const float mr = mine ? x.z : x.x, mi = mine ? x.w : x.y;
-        store_split1(B, tc::sw128_offset(2 * ql, k), mr, BT);
-        store_split1(B, tc::sw128_offset(2 * ql + 1, k), mi, BT);
+        typedef DataTile<TF32, NC> DT;
+        DT::store(B, 2 * ql, k, mr);
+        DT::store(B, 2 * ql + 1, k, mi);
         if (BOTH) {
           const float orr = mine ? x.x : x.z, oi = mine ? x.y : x.w;
-          store_split1(B + 3 * BT, tc::sw128_offset(2 * ql, k), orr, BT);
-          store_split1(B + 3 * BT, tc::sw128_offset(2 * ql + 1, k), oi, BT);
+          DT::store(B + DT::bytes, 2 * ql, k, orr);
+          DT::store(B + DT::bytes, 2 * ql + 1, k, oi);
         }
       }
     }
@@ -149,7 +169,7 @@ __device__ __forceinline__ void fwd_build_tile(const ShtGeom& g, const FwdSet& s
 // consecutive spectral entries, and both parities of every fetched sector are
 // used.  The FP64 -> FP32 conversions use the hardware instruction here: at
 // the pack kernel's occupancy they measured faster than the integer form.
-template <bool VEC, int NC, int CB>
+template <bool VEC, int NC, int CB, bool TF32 = false>
 __device__ __forceinline__ void inv_build_pair(const ShtGeom& g, const InvSet& s, unsigned char* B, int ct,
                                                int ncplx, int m, int lm0, int c, int ql0, int qstride,
                                                int lane) {
@@ -188,7 +208,8 @@ __device__ __forceinline__ void inv_build_pair(const ShtGeom& g, const InvSet& s
       }
     }
     const float dm = (float)m;
-    unsigned char* Bp = B + (lane & 1) * 3 * BT;  // this lane's parity tile
+    typedef DataTile<TF32, NC> DT;
+    unsigned char* Bp = B + (lane & 1) * DT::bytes;  // this lane's parity tile
 #pragma unroll
     for (int i = 0; i < CB; ++i) {
       const int ql = qb + i * qstride;
@@ -216,8 +237,8 @@ __device__ __forceinline__ void inv_build_pair(const ShtGeom& g, const InvSet& s
           }
           if (l > lc[i]) { ar = 0.f; ai = 0.f; }
         }
-        store_split1(Bp, tc::sw128_offset(2 * ql, k), ar, BT);
-        store_split1(Bp, tc::sw128_offset(2 * ql + 1, k), ai, BT);
+        DT::store(Bp, 2 * ql, k, ar);
+        DT::store(Bp, 2 * ql + 1, k, ai);
       }
     }
   }

@@ -193,3 +193,31 @@ __device__ __forceinline__ void tmem_ld32_nw(uint32_t taddr, uint32_t (&r)[32]) 
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 }  // namespace tc
+
+namespace tc {
+// ---- TF32 (kind::tf32): 4-byte elements, 32 per 128-byte swizzled row, K = 8 per MMA
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  // D = F32 (bits 4-5), A = TF32 (bits 7-9 = 2), B = TF32 (bits 10-12 = 2), K-major A and B
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// byte offset of element (row, k), k < 32, in a [rows][32] 4-byte tile with the 128-byte swizzle
+__host__ __device__ __forceinline__ uint32_t sw128_offset32(uint32_t row, uint32_t k) {
+  return (row >> 3) * 1024u + (row & 7u) * 128u + ((((k >> 2) ^ (row & 7u)) & 7u) << 4) + ((k & 3u) << 2);
+}
+// x = hi + lo with hi rounded to TF32 (10 stored mantissa bits, nearest even);
+// lo = x - hi is exact in FP32 and carries the next 11+ bits
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t r = (u + 0x0FFFu + ((u >> 13) & 1u)) & 0xFFFFE000u;
+  hi = ((u & 0x7F800000u) == 0x7F800000u) ? x : __uint_as_float(r);
+  lo = x - hi;
+}
+}  // namespace tc

@@ -530,3 +530,49 @@ def test_async_host_batches_match_sync(built, torch):
         assert torch.equal(out_g[k], ref_g[k]), k
     for k in ref_l:
         assert torch.equal(out_l[k], ref_l[k]), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("grid", [(63, 1, 96, 192), (64, 4, 96, 48), (128, 1, 192, 384)])
+def test_tf32x2_form_matches_oracle(built, oracle_mod, torch, grid):
+    """TF32 variant (2xTF32 split products hi*hi, hi*lo, lo*hi; FP32
+    accumulation, FP32 FFT) against the FP64 oracle: relative L2 within 4e-6."""
+    L, minc, N, P = grid
+    s = make(L, minc, N, P, prec="tf32x2")
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    S = spec(o, 4, 17)
+    for a, b in zip(s.torpol_to_spat(S[0], S[1], S[2]), o.torpol_to_spat(S[0], S[1], S[2])):
+        assert rel_l2(a, b) < 4e-6
+    assert rel_l2(s.scal_to_spat(S[3], L - 3), o.scal_to_spat(S[3], L - 3)) < 4e-6
+    g = o.torpol_to_spat(S[0], S[1], S[2])
+    for a, b in zip(s.spat_to_qst(*g), o.spat_to_qst(*g)):
+        assert rel_l2(a, b) < 4e-6
+    assert rel_l2(s.scal_to_SH(g[0], L - 2), o.scal_to_SH(g[0], L - 2)) < 4e-6
+    s.device_status()
+
+
+@pytest.mark.gpu
+def test_tf32x2_full_size_radial_set(built, torch):
+    """TF32 variant at l_max=255 (384 x 768), 3 levels of the radial set with
+    get_nl analysis inputs: normwise per call within 1e-6 of the FP64 form."""
+    from magic_gb300.workload import grid_space_inputs, or2_levels
+    n = 3
+    s64 = make(255, 1, 384, 768)
+    s32 = make(255, 1, 384, 768, prec="tf32x2")
+    spec_in = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(255, 1, n, seed=5).items()}
+    or2 = or2_levels(n)
+    g64 = s64.transform_to_grid_space(spec_in, or2=or2)
+    g32 = s32.transform_to_grid_space(spec_in, or2=or2)
+    nl = s64.get_nl(g64, or2=or2)
+    l64 = s64.transform_to_lm_space(nl)
+    l32 = s32.transform_to_lm_space(nl)
+    torch.cuda.synchronize()
+    s32.device_status()
+    groups = [("vrc", "vtc", "vpc"), ("cvrc", "cvtc", "cvpc"), ("brc", "btc", "bpc"), ("cbrc", "cbtc", "cbpc"),
+              ("sc",), ("pc",), ("xic",), ("AdvrLM", "AdvtLM", "AdvpLM"), ("VSrLM", "VStLM", "VSpLM"),
+              ("VxBrLM", "VxBtLM", "VxBpLM"), ("heatTermsLM",)]
+    a, b = {**g32, **l32}, {**g64, **l64}
+    for ks in groups:
+        num = sum(float(torch.linalg.vector_norm(a[k] - b[k])) ** 2 for k in ks) ** 0.5
+        den = sum(float(torch.linalg.vector_norm(b[k])) ** 2 for k in ks) ** 0.5
+        assert num / den < 1e-6, (ks, num / den)

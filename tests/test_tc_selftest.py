@@ -26,3 +26,12 @@ def test_tc_gemm_exact(lib, n, kc):
     v = ctypes.c_double()
     check(lib.magic_sht_tc_selftest(0, n, kc, ctypes.byref(v)))
     assert v.value < 1e-6, v.value
+
+
+@pytest.mark.parametrize("n,kc", [(128, 1), (64, 1), (256, 2), (128, 2)])
+def test_tc_gemm_exact_tf32(lib, n, kc):
+    """The same GEMM with tf32 operands (kind::tf32, K = 8 per MMA)."""
+    from magic_gb300._lib import check
+    v = ctypes.c_double()
+    check(lib.magic_sht_tc_selftest_tf32(0, n, kc, ctypes.byref(v)))
+    assert v.value < 1e-6, v.value
