@@ -203,6 +203,23 @@ int magic_sht_set_host_async(magic_sht_handle* h, int on);
 int magic_sht_get_nl(magic_sht_handle* h, int n_levels, const double* or2, const magic_sht_grid_space_args* g,
                      const magic_sht_lm_space_args* nl);
 
+/* ---- spectral assembly of the explicit time derivatives at interior radial
+ * levels (get_td.f90: get_dwdt :133-208, get_dpdt :311-379, get_dzdt
+ * :381-457, get_dsdt :459-521, get_dbdt :558-619) from the analysis outputs
+ * and the radial-loop spectra: Boussinesq form, Coriolis force (cor_fac =
+ * CorFac), magnetic field and heat equation on, no double-curl form.  Device
+ * arrays [n_levels][spec_ld] complex; r (radius), lcut (l_R, NULL = l_max) and
+ * epsc (internal heating added to dsdt at l = 0, NULL = 0) are per-level host
+ * or device arrays.  dpdt at l = 0 is set to 0 (the reference leaves it). */
+typedef struct magic_sht_td_args {
+  const double *w, *dw, *z;                                           /* spectra */
+  const double *AdvrLM, *AdvtLM, *AdvpLM, *VStLM, *VxBrLM, *VxBtLM, *VxBpLM;  /* analysis out */
+  double *dwdt, *dzdt, *dpdt, *dsdt, *dbdt, *djdt, *dVxBhLM;           /* outputs */
+  long long spec_ld;
+} magic_sht_td_args;
+int magic_sht_get_td(magic_sht_handle* h, int n_levels, const double* r, const int* lcut, double cor_fac,
+                     const double* epsc, const magic_sht_td_args* a);
+
 /* ---- CUDA-graph capture of a device-pointer call sequence on the handle's
  * stream (e.g. the radial loop's transform set), replayed with one launch. */
 int magic_sht_graph_begin(magic_sht_handle* h);

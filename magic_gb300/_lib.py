@@ -46,6 +46,14 @@ class GridSpaceArgs(ctypes.Structure):
                 [(n, _V) for n in GRID_SPACE_OUT] + [("grid_ld", ctypes.c_longlong)])
 
 
+TD_IN = ["w", "dw", "z", "AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "VxBrLM", "VxBtLM", "VxBpLM"]
+TD_OUT = ["dwdt", "dzdt", "dpdt", "dsdt", "dbdt", "djdt", "dVxBhLM"]
+
+
+class TdArgs(ctypes.Structure):
+    _fields_ = [(n, _V) for n in TD_IN + TD_OUT] + [("spec_ld", ctypes.c_longlong)]
+
+
 class LmSpaceArgs(ctypes.Structure):
     _fields_ = ([(n, _V) for n in LM_SPACE_IN] + [("grid_ld", ctypes.c_longlong)] +
                 [(n, _V) for n in LM_SPACE_OUT] + [("spec_ld", ctypes.c_longlong)])
@@ -84,6 +92,7 @@ SIGNATURES = {
                                           ctypes.POINTER(GridSpaceArgs)],
     "magic_sht_transform_to_lm_space": [_V, ctypes.c_int, _V, ctypes.POINTER(LmSpaceArgs)],
     "magic_sht_set_host_async": [_V, ctypes.c_int],
+    "magic_sht_get_td": [_V, ctypes.c_int, _V, _V, ctypes.c_double, _V, ctypes.POINTER(TdArgs)],
     "magic_sht_get_nl": [_V, ctypes.c_int, _V, ctypes.POINTER(GridSpaceArgs), ctypes.POINTER(LmSpaceArgs)],
     "magic_sht_graph_begin": [_V],
     "magic_sht_graph_end": [_V, ctypes.POINTER(_V)],

@@ -147,6 +147,18 @@ struct NlGrids {
   long long ld;
 };
 
+// spectral assembly of the time derivatives (td.cu); arrays [level][ld] complex
+struct TdArgs {
+  const double2 *w, *dw, *z;                                   // radial-loop spectra
+  const double2 *Advr, *Advt, *Advp, *VSt, *VxBr, *VxBt, *VxBp;  // analysis outputs
+  double2 *dwdt, *dzdt, *dpdt, *dsdt, *dbdt, *djdt, *dVxBh;     // outputs
+  long long ld;
+  const double* r;      // [level] radius
+  const int* lcut;      // [level] l_R, or null (= l_max)
+  const double* epsc;   // [level] internal heating of dsdt(l=0), or null (= 0)
+  double cor_fac;       // CorFac (1/E)
+};
+
 __host__ __device__ inline int tc_nch(int n_l) { return ((n_l + 1) / 2 + 63) / 64; }
 
 #define CUDA_TRY(x)                                                        \

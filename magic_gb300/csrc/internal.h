@@ -48,3 +48,6 @@ cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec,
 // nl.cu
 cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& out, const double* or2,
                           double or2_0, int nlev, cudaStream_t st);
+
+// td.cu
+cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, cudaStream_t st);

@@ -1334,6 +1334,46 @@ int magic_sht_get_nl(magic_sht_handle* h, int n, const double* or2, const magic_
   return cx.finish();
 }
 
+int magic_sht_get_td(magic_sht_handle* h, int n, const double* r, const int* lcut, double cor_fac,
+                     const double* epsc, const magic_sht_td_args* a) {
+  TRY(check_handle(h));
+  if (!a || !r || n < 0) return set_err(MAGIC_SHT_ERR_ARG, "null args/r or n_levels < 0");
+  if (n == 0) return MAGIC_SHT_OK;
+  const ShtGeom& g = h->g;
+  if (a->spec_ld < g.lm_max) return set_err(MAGIC_SHT_ERR_ARG, "spec_ld smaller than lm_max");
+  DeviceGuard dg(h->device);
+  const void* const arrs[17] = {a->w, a->dw, a->z, a->AdvrLM, a->AdvtLM, a->AdvpLM, a->VStLM, a->VxBrLM,
+                                a->VxBtLM, a->VxBpLM, a->dwdt, a->dzdt, a->dpdt, a->dsdt, a->dbdt, a->djdt,
+                                a->dVxBhLM};
+  for (int i = 0; i < 17; ++i)
+    if (!arrs[i] || !is_device_ptr(arrs[i]) || ((uintptr_t)arrs[i] & 15))
+      return set_err(MAGIC_SHT_ERR_ARG, "get_td array %d: null, host or not 16-byte aligned", i);
+  if (lcut && !is_device_ptr(lcut))
+    for (int i = 0; i < n; ++i)
+      if (lcut[i] < 0 || lcut[i] > g.l_max)
+        return set_err(MAGIC_SHT_ERR_LCUT, "lcut[%d]=%d outside [0, %d]", i, lcut[i], g.l_max);
+  CallCtx cx(h);
+  const int i_r = cx.raw_in(r, (size_t)n * 8);
+  const int i_lc = lcut ? cx.raw_in(lcut, (size_t)n * 4) : -1;
+  const int i_ep = epsc ? cx.raw_in(epsc, (size_t)n * 8) : -1;
+  TRY(cx.prepare());
+  TdArgs t{};
+  t.w = (const double2*)a->w; t.dw = (const double2*)a->dw; t.z = (const double2*)a->z;
+  t.Advr = (const double2*)a->AdvrLM; t.Advt = (const double2*)a->AdvtLM; t.Advp = (const double2*)a->AdvpLM;
+  t.VSt = (const double2*)a->VStLM; t.VxBr = (const double2*)a->VxBrLM; t.VxBt = (const double2*)a->VxBtLM;
+  t.VxBp = (const double2*)a->VxBpLM;
+  t.dwdt = (double2*)a->dwdt; t.dzdt = (double2*)a->dzdt; t.dpdt = (double2*)a->dpdt; t.dsdt = (double2*)a->dsdt;
+  t.dbdt = (double2*)a->dbdt; t.djdt = (double2*)a->djdt; t.dVxBh = (double2*)a->dVxBhLM;
+  t.ld = a->spec_ld;
+  t.r = (const double*)cx.dev(i_r);
+  t.lcut = (const int*)cx.dev(i_lc);
+  t.epsc = (const double*)cx.dev(i_ep);
+  t.cor_fac = cor_fac;
+  h->launches++;
+  CK(launch_get_td(g, t, n, h->stream));
+  return cx.finish();
+}
+
 int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
                                     const magic_sht_lm_space_args* a) {
   TRY(check_handle(h));

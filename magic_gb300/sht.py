@@ -396,6 +396,39 @@ class SHT:
         check(self._lib.magic_sht_get_nl(self._h, n, por2, ctypes.byref(g), ctypes.byref(nl)))
         return outs
 
+    def get_td(self, spec: dict, r, cor_fac: float, lcut=None, epsc=None, out: Optional[dict] = None):
+        """Spectral assembly of the explicit time derivatives (get_td.f90):
+        from CUDA tensors ``w``, ``dw``, ``z`` and the analysis outputs
+        (``AdvrLM`` .. ``VxBpLM``) the outputs ``dwdt``, ``dzdt``, ``dpdt``,
+        ``dsdt``, ``dbdt``, ``djdt``, ``dVxBhLM`` ([level][lm] complex)."""
+        import torch
+        missing = [k for k in _lib.TD_IN if spec.get(k) is None]
+        if missing:
+            raise ValueError("get_td needs %s" % missing)
+        first = spec[_lib.TD_IN[0]]
+        if not (_is_torch(first) and first.is_cuda):
+            raise ValueError("get_td takes CUDA tensors")
+        n = int(first.shape[0])
+        a = _lib.TdArgs()
+        keep = []
+        for k in _lib.TD_IN:
+            t = spec[k].contiguous()
+            keep.append(t)
+            setattr(a, k, t.data_ptr())
+        outs = {} if out is None else dict(out)
+        for k in _lib.TD_OUT:
+            if k not in outs:
+                outs[k] = torch.empty_like(keep[0])
+            setattr(a, k, outs[k].data_ptr())
+        a.spec_ld = self.lm_max
+        r_arr = np.ascontiguousarray(r, dtype=np.float64)
+        lc = None if lcut is None else np.ascontiguousarray(lcut, dtype=np.int32)
+        ep = None if epsc is None else np.ascontiguousarray(epsc, dtype=np.float64)
+        self._bind_torch_stream()
+        check(self._lib.magic_sht_get_td(self._h, n, r_arr.ctypes.data, None if lc is None else lc.ctypes.data,
+                                         float(cor_fac), None if ep is None else ep.ctypes.data, ctypes.byref(a)))
+        return outs
+
     # ---------------------------------------------------------- profiling
     def set_profiling(self, on: bool):
         check(self._lib.magic_sht_set_profiling(self._h, 1 if on else 0))

@@ -325,3 +325,72 @@ def get_nl(grids: dict, or2, n_theta: int) -> dict:
         "VxBp": o4 * (vr * bt - vt * br),
         "heatTerms": o2 * (o2 * jr * jr + sn2 * jt * jt + sn2 * jp * jp),
     }
+
+
+def get_td(spec: dict, r, cor_fac: float, l_max: int, minc: int = 1, lcut=None, epsc=None) -> dict:
+    """Spectral assembly of the explicit time derivatives at interior levels
+    (get_td.f90: get_dwdt :133-208, get_dpdt :311-379, get_dzdt :381-457,
+    get_dsdt :459-521, get_dbdt :558-619), Boussinesq, Coriolis on, no
+    double-curl form; operator coefficients of horizontal.f90:204-229.  Arrays
+    [level][lm] complex in the m-major st_map order; numpy FP64."""
+    ls, ms = [], []
+    for m in range(0, l_max + 1, minc):
+        for l in range(m, l_max + 1):
+            ls.append(l)
+            ms.append(m)
+    l = np.array(ls, dtype=np.float64)
+    m = np.array(ms, dtype=np.float64)
+    li = np.array(ls)
+    n = len(np.asarray(r))
+    K = len(ls)
+
+    def clm(ll, mm):
+        return np.sqrt(np.maximum((ll + mm) * (ll - mm), 0.0) / ((2 * ll - 1) * (2 * ll + 1)))
+
+    hasS = li > np.array(ms)                        # lm2lmS valid (l > m)
+    cS = np.where(hasS, clm(l, m), 0.0)
+    cA = clm(l + 1, m)
+    dLh = l * (l + 1)
+    t2S, t2A = (l - 1) * cS, (l + 2) * cA
+    t3S, t3A = (l - 1) * (l + 1) * cS, l * (l + 2) * cA
+    t4S, t4A = (l + 1) * cS * (l - 1) * l, l * cA * (l + 1) * (l + 2)
+    idxS = np.where(hasS, np.arange(K) - 1, np.arange(K))
+    idxA = np.minimum(np.arange(K) + 1, K - 1)
+    out = {k: np.zeros((n, K), dtype=np.complex128) for k in
+           ("dwdt", "dzdt", "dpdt", "dsdt", "dbdt", "djdt", "dVxBhLM")}
+    for ir in range(n):
+        rr = float(np.asarray(r)[ir])
+        or1, or2 = 1.0 / rr, 1.0 / rr ** 2
+        or4 = or2 * or2
+        lR = l_max if lcut is None else min(int(np.asarray(lcut)[ir]), l_max)
+        w, dw, z = (np.asarray(spec[k])[ir] for k in ("w", "dw", "z"))
+        A = np.where(li < lR, 1.0, 0.0)                # l+1 terms (l < l_R)
+        inside = li <= lR
+        zA, zS = z[idxA] * A, z[idxS]
+        dwA, dwS = dw[idxA] * A, dw[idxS]
+        wA, wS = w[idxA] * A, w[idxS]
+        dphi = 1j * m
+        cor = 2.0 * cor_fac
+        # get_dwdt
+        c = dphi * dw + t2A * zA - t2S * zS
+        c[0] = t2A[0] * zA[0]                            # lm = 1 (l = 0)
+        out["dwdt"][ir] = or2 * np.asarray(spec["AdvrLM"])[ir] + np.where(inside, cor * or1 * c, 0)
+        # get_dzdt
+        c = dphi * z + t3A * dwA + or1 * t4A * wA + t3S * dwS - or1 * t4S * wS
+        dz = dLh * np.asarray(spec["AdvpLM"])[ir] + np.where(inside, cor * or2 * c, 0)
+        dz[0] = cor * or2 * (t3A[0] * dwA[0] + or1 * t4A[0] * wA[0])
+        out["dzdt"][ir] = dz
+        # get_dpdt
+        c = -dphi * (dw + or1 * dLh * w) + t3A * zA + t3S * zS
+        dp = -dLh * np.asarray(spec["AdvtLM"])[ir] + np.where(inside, cor * or2 * c, 0)
+        dp[0] = 0.0
+        out["dpdt"][ir] = dp
+        # get_dsdt (Boussinesq)
+        ds = dLh * np.asarray(spec["VStLM"])[ir]
+        ds[0] = 0.0 if epsc is None else float(np.asarray(epsc)[ir])
+        out["dsdt"][ir] = ds
+        # get_dbdt
+        out["dbdt"][ir] = dLh * np.asarray(spec["VxBpLM"])[ir]
+        out["dVxBhLM"][ir] = -dLh * np.asarray(spec["VxBtLM"])[ir] * rr * rr
+        out["djdt"][ir] = dLh * or4 * np.asarray(spec["VxBrLM"])[ir]
+    return out
