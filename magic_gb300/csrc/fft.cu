@@ -155,19 +155,25 @@ __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tw, 
   reg_fft<T2, S>(a, tw, P, s);
 }
 
-// shared-memory position of input index k (digit swap k = S*i1 + q -> q*32 + i1)
+// Shared-memory row layouts of the fast path (row pitch KP = 33 S + 1, odd):
+// input position of index k (digit swap k = S*i1 + q -> 33 q + i1: the lanes
+// of a half warp storing neighbouring k, or reading one q, hit distinct banks)
 template <int S>
-__device__ __forceinline__ int pin(int k) { return (k % S) * 32 + k / S; }
+__device__ __forceinline__ int pin(int k) { return (k % S) * 33 + k / S; }
+// output position of the natural index k = k1 + 32 k2 (k1 < 32): the
+// bit-reversed lanes of a half warp write the even or the odd k1 of one
+// block, which pos() spreads over distinct banks
+__device__ __forceinline__ int pos(int k) { return (k & 31) + ((k >> 4) & 1) + 33 * (k >> 5); }
 
 // ------------------------------------------------------------ fast path ----
 // One CTA = RT consecutive theta rows of one (level, field) column; 8 warps,
 // each owning RT/8 rows in turn.  Shared memory holds the RT rows with an
-// odd pitch KP = n+1 so that row-parallel and index-parallel accesses both
-// spread over the banks.
+// odd pitch KP = 33 S + 1 and the layouts pin() / pos(), so that row-parallel
+// and index-parallel accesses both spread over the banks.
 template <typename T, int S, int RT>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1)) fft_inv_fast(const ShtGeom g, const FftSet s) {
   typedef typename V2<T>::t T2;
-  constexpr int n = 32 * S, KP = n + 1;
+  constexpr int n = 32 * S, KP = 33 * S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2* sm = (T2*)smem_raw;
   const int col = blockIdx.y;
@@ -215,13 +221,13 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
     T2 a[S];
 #pragma unroll
     for (int q = 0; q < S; ++q) {
-      // k = S*lane + q sits at pin(k) = 32q + lane; n - k at 32(S-q) + 31 - lane
+      // k = S*lane + q sits at pin(k) = 33q + lane; n - k at 33(S-q) + 31 - lane
       // (q > 0) or 32 - lane (q = 0; k = 0 has no partner)
       const int k = S * lane + q;
       T2 ck = zero2<T2>(), cn = zero2<T2>();
-      if (k < n_m) ck = row[32 * q + lane];
+      if (k < n_m) ck = row[33 * q + lane];
       const int kn = n - k;
-      if (kn < n_m) cn = row[q == 0 ? 32 - lane : 32 * (S - q) + 31 - lane];
+      if (kn < n_m) cn = row[q == 0 ? 32 - lane : 33 * (S - q) + 31 - lane];
       if (k == 0) { ck.y = 0; cn.y = 0; }
       const T2 E = cadd(ck, cconj(cn));
       const T2 O = cmul(csub(ck, cconj(cn)), tw[k]);
@@ -232,7 +238,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
     warp_fft<T2, S>(a, tw, g.n_phi, +1);
     const int k1 = brev5(lane);
 #pragma unroll
-    for (int k2 = 0; k2 < S; ++k2) row[k1 + 32 * k2] = a[k2];  // z_j = x_{2j} + i x_{2j+1}
+    for (int k2 = 0; k2 < S; ++k2) row[pos(k1 + 32 * k2)] = a[k2];  // z_j = x_{2j} + i x_{2j+1}
     __syncwarp();
   }
   __syncthreads();
@@ -244,8 +250,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
     const int kk = i / RT2, rr = 2 * (i - kk * RT2);
     const int rowg = row0 + rr;
     if (rowg >= g.n_theta) continue;
-    T2 v0 = sm[rr * KP + kk];        // phi = 2kk (x) and 2kk+1 (y) of row rr
-    T2 v1 = sm[(rr + 1) * KP + kk];
+    T2 v0 = sm[rr * KP + pos(kk)];        // phi = 2kk (x) and 2kk+1 (y) of row rr
+    T2 v1 = sm[(rr + 1) * KP + pos(kk)];
     if (osin) {
       const T o = from_f64<T>(g.osin2[rowg >> 1]);  // rows 2j and 2j+1 share theta_j
       v0 = cscale(v0, o);
@@ -267,7 +273,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
 template <typename T, int S, int RT>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1)) fft_fwd_fast(const ShtGeom g, const FftSet s) {
   typedef typename V2<T>::t T2;
-  constexpr int n = 32 * S, KP = n + 1;
+  constexpr int n = 32 * S, KP = 33 * S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2* sm = (T2*)smem_raw;
   const int col = blockIdx.y;
@@ -309,12 +315,12 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
     T2* row = sm + rr * KP;
     T2 a[S];
 #pragma unroll
-    for (int q = 0; q < S; ++q) a[q] = row[q * 32 + lane];  // = z[S*lane + q]
+    for (int q = 0; q < S; ++q) a[q] = row[q * 33 + lane];  // = z[S*lane + q]
     __syncwarp();
     warp_fft<T2, S>(a, tw, g.n_phi, -1);
     const int k1 = brev5(lane);
 #pragma unroll
-    for (int k2 = 0; k2 < S; ++k2) row[k1 + 32 * k2] = a[k2];
+    for (int k2 = 0; k2 < S; ++k2) row[pos(k1 + 32 * k2)] = a[k2];
     __syncwarp();
   }
   __syncthreads();
@@ -331,8 +337,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const T2* row = sm + (2 * jp + h) * KP;
-      const T2 Zk = row[k];
-      const T2 Zn = cconj(row[k == 0 ? 0 : n - k]);
+      const T2 Zk = row[pos(k)];
+      const T2 Zn = cconj(row[pos(k == 0 ? 0 : n - k)]);
       const T2 D = csub(Zk, Zn);
       const T2 u = cmul(cconj(tw[k]), D);
       T2 X;
@@ -567,8 +573,9 @@ cudaError_t launch_fast(const ShtGeom& g, const FftSet& s, bool inverse, cudaStr
   typedef typename V2<T>::t T2;
   constexpr int n = 32 * S;
   // 16 rows per CTA; 8 rows where 16 would leave one CTA per SM
-  constexpr int RT = (sizeof(T2) * 16 * (n + 1) > 100 * 1024) ? 8 : 16;
-  const size_t smem = ((size_t)RT * (n + 1) + 2 * n) * sizeof(T2);
+  constexpr int KP = 33 * S + 1;
+  constexpr int RT = (sizeof(T2) * 16 * KP > 100 * 1024) ? 8 : 16;
+  const size_t smem = ((size_t)RT * KP + 2 * n) * sizeof(T2);
   dim3 grid((g.n_theta + RT - 1) / RT, s.nf * s.nlev);
   if (inverse) {
     auto k = fft_inv_fast<T, S, RT>;
