@@ -120,7 +120,6 @@ template <bool VEC, int NC, int CB, bool BOTH = VEC, bool TF32 = false>
 __device__ __forceinline__ void fwd_build_tile(const ShtGeom& g, const FwdSet& s, unsigned char* B, int ct,
                                                int ncplx, int mc, int mine, int c, int ql0, int qstride,
                                                int lane) {
-  constexpr uint32_t BT = NC * 128;
   for (int qb = ql0; qb < NC / 2; qb += CB * qstride) {
     float4 v[CB][2];
 #pragma unroll
@@ -173,7 +172,6 @@ template <bool VEC, int NC, int CB, bool TF32 = false>
 __device__ __forceinline__ void inv_build_pair(const ShtGeom& g, const InvSet& s, unsigned char* B, int ct,
                                                int ncplx, int m, int lm0, int c, int ql0, int qstride,
                                                int lane) {
-  constexpr uint32_t BT = NC * 128;
   const int lmx = g.l_max - m;
   for (int qb = ql0; qb < NC / 2; qb += CB * qstride) {
     double2 a[CB][4], b[CB][4];
