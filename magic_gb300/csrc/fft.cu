@@ -134,17 +134,21 @@ __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tw, 
 #pragma unroll
   for (int d = 16; d >= 1; d >>= 1) {
     // lower lane: a + b;  upper lane: (b - a) * w  -> t = b + sg*a, a = t * w
+    // (the last stage, d = 1, has w = 1 on every lane)
     const bool up = (lane & d) != 0;
     const T sg = up ? (T)-1 : (T)1;
-    T2 w = twid(tw, (lane & (d - 1)) * (P / (2 * d)), s);
-    if (!up) { w.x = (T)1; w.y = (T)0; }
+    T2 w;
+    if (d > 1) {
+      w = twid(tw, (lane & (d - 1)) * (P / (2 * d)), s);
+      if (!up) { w.x = (T)1; w.y = (T)0; }
+    }
 #pragma unroll
     for (int q = 0; q < S; ++q) {
       const T2 b = shfl_xor2(a[q], d);
       T2 t;
       t.x = fma(sg, a[q].x, b.x);
       t.y = fma(sg, a[q].y, b.y);
-      a[q] = cmul(t, w);
+      a[q] = d > 1 ? cmul(t, w) : t;
     }
   }
   const int k1 = brev5(lane);
@@ -166,6 +170,64 @@ __device__ __forceinline__ int pin(int k) { return (k % S) * 33 + k / S; }
 __device__ __forceinline__ int pos(int k) { return (k & 31) + ((k >> 4) & 1) + 33 * (k >> 5); }
 
 // ------------------------------------------------------------ fast path ----
+// Stage-in of the inverse fast path: the spectra of RT theta rows into the
+// pin() layout, and the twiddle table into shared memory.  All loads of a
+// batch of NB orders (E at both parities, and F for vector fields), and of
+// the twiddle table, are issued before the first shared-memory store, so that
+// a thread waits for one memory latency per batch.
+template <typename T2, int S, int RT, int NB>
+__device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict__ in, bool in_parity,
+                                          bool has_f, long long per_p, const T2* __restrict__ twg, T2* sm, T2* stw,
+                                          int rp, int kq, int rowg, bool row_ok) {
+  constexpr int n = 32 * S, KP = 33 * S + 1, KS = 256 / (RT / 2), NTW = (2 * n + 255) / 256;
+  const int n_m = g.n_m;
+  T2 twr[NTW];
+#pragma unroll
+  for (int i = 0; i < NTW; ++i)
+    if (threadIdx.x + 256 * i < 2 * n) twr[i] = twg[threadIdx.x + 256 * i];
+  for (int kb = 0; kb < n_m; kb += KS * NB) {
+    T2 x[NB][4];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int k = kb + kq + KS * b;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) x[b][j] = zero2<T2>();
+      if (row_ok && k < n_m) {
+        if (in_parity) {
+          const T2* b0 = in + (long long)k * 2 * per_p + (rowg >> 1);
+          x[b][0] = b0[0];
+          x[b][1] = b0[per_p];
+          if (has_f) {
+            x[b][2] = b0[g.nh];
+            x[b][3] = b0[per_p + g.nh];
+          }
+        } else {
+          const T2* p = in + (long long)k * g.n_theta + rowg;
+          x[b][0] = p[0];
+          x[b][1] = p[1];
+        }
+      }
+    }
+    if (kb == 0) {  // n_m >= 1: the first batch always runs
+#pragma unroll
+      for (int i = 0; i < NTW; ++i)
+        if (threadIdx.x + 256 * i < 2 * n) stw[threadIdx.x + 256 * i] = twr[i];
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int k = kb + kq + KS * b;
+      if (k >= n_m) continue;
+      T2 v0 = x[b][0], v1 = x[b][1];
+      if (in_parity) {  // rows 2j, 2j + 1: north = ES + EA, south = ES - EA
+        v0 = cadd(x[b][0], x[b][1]);
+        v1 = has_f ? csub(x[b][2], x[b][3]) : csub(x[b][0], x[b][1]);
+      }
+      sm[rp * KP + pin<S>(k)] = v0;
+      sm[(rp + 1) * KP + pin<S>(k)] = v1;
+    }
+  }
+}
+
 // One CTA = RT consecutive theta rows of one (level, field) column; 8 warps,
 // each owning RT/8 rows in turn.  Shared memory holds the RT rows with an
 // odd pitch KP = 33 S + 1 and the layouts pin() / pos(), so that row-parallel
@@ -182,38 +244,19 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   const int row0 = blockIdx.x * RT;
   const T2* __restrict__ twg = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
   T2* stw = sm + RT * KP;  // twiddle table e^{+2 pi i k / P}, k < P, copied to shared memory
-  for (int i = threadIdx.x; i < 2 * n; i += 256) stw[i] = twg[i];
   const T2* tw = stw;
   const T2* __restrict__ in = (const T2*)fd.in + (long long)r * fd.in_ld;
   const int n_m = g.n_m;
   const bool in_parity = (fd.flags & (FFT_IN_E | FFT_IN_EF)) != 0;
   const bool has_f = (fd.flags & FFT_IN_EF) != 0;
   const long long per_p = has_f ? 2LL * g.nh : (long long)g.nh;
-  // two consecutive rows per thread (16 B for FP32 half spectra); n_theta is even
-  constexpr int RT2 = RT / 2;
-#pragma unroll (sizeof(T) == 4 ? 8 : 2)
-  for (int i = threadIdx.x; i < n_m * RT2; i += 256) {
-    const int k = i / RT2, rr = 2 * (i - k * RT2);
-    const int row = row0 + rr;
-    T2 v0 = zero2<T2>(), v1 = zero2<T2>();
-    if (row < g.n_theta) {
-      if (in_parity) {
-        const int jg = row >> 1;
-        const T2* b0 = in + (long long)k * 2 * per_p;
-        const T2* b1 = b0 + per_p;
-        const T2 e0 = b0[jg], e1 = b1[jg];
-        const T2 f0 = has_f ? b0[g.nh + jg] : e0, f1 = has_f ? b1[g.nh + jg] : e1;
-        v0 = cadd(e0, e1);
-        v1 = csub(f0, f1);
-      } else {
-        const T2* p = in + (long long)k * g.n_theta + row;
-        v0 = p[0];
-        v1 = p[1];
-      }
-    }
-    sm[rr * KP + pin<S>(k)] = v0;
-    sm[(rr + 1) * KP + pin<S>(k)] = v1;
-  }
+  // Each thread owns the row pair (rp, rp + 1) (16 B for FP32 half spectra;
+  // n_theta is even) and the orders k = kq + KS j.
+  constexpr int RT2 = RT / 2, KS = 256 / RT2;
+  const int rp = 2 * (threadIdx.x % RT2), kq = threadIdx.x / RT2;
+  const int rowg = row0 + rp;
+  const bool row_ok = rowg < g.n_theta;
+  inv_stage<T2, S, RT, sizeof(T) == 4 ? 4 : 2>(g, in, in_parity, has_f, per_p, twg, sm, stw, rp, kq, rowg, row_ok);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int rr = warp; rr < RT; rr += 8) {
@@ -243,20 +286,14 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   }
   __syncthreads();
   double* out = (double*)fd.out + (long long)r * fd.out_ld;
-  const bool osin = (fd.flags & FFT_OSIN2) != 0;
   const bool vec = (g.ld % 2) == 0;  // 16-byte stores of two rows need an even pitch
+  if (!row_ok) return;
+  // the row pair (rp, rp + 1) of this thread shares theta_j, j = rowg / 2
+  const T o = (fd.flags & FFT_OSIN2) ? from_f64<T>(g.osin2[rowg >> 1]) : (T)1;
 #pragma unroll (sizeof(T) == 4 ? 4 : 2)
-  for (int i = threadIdx.x; i < n * RT2; i += 256) {
-    const int kk = i / RT2, rr = 2 * (i - kk * RT2);
-    const int rowg = row0 + rr;
-    if (rowg >= g.n_theta) continue;
-    T2 v0 = sm[rr * KP + pos(kk)];        // phi = 2kk (x) and 2kk+1 (y) of row rr
-    T2 v1 = sm[(rr + 1) * KP + pos(kk)];
-    if (osin) {
-      const T o = from_f64<T>(g.osin2[rowg >> 1]);  // rows 2j and 2j+1 share theta_j
-      v0 = cscale(v0, o);
-      v1 = cscale(v1, o);
-    }
+  for (int kk = kq; kk < n; kk += KS) {
+    const T2 v0 = cscale(sm[rp * KP + pos(kk)], o);  // phi = 2kk (x) and 2kk+1 (y) of row rp
+    const T2 v1 = cscale(sm[(rp + 1) * KP + pos(kk)], o);
     double* dst = out + (long long)(2 * kk) * g.ld + rowg;
     if (vec) {
       *reinterpret_cast<double2*>(dst) = make_double2(to_f64<T>(v0.x), to_f64<T>(v1.x));
@@ -282,32 +319,53 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   const int row0 = blockIdx.x * RT;
   const T2* __restrict__ twg = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
   T2* stw = sm + RT * KP;  // twiddle table e^{+2 pi i k / P}, k < P, copied to shared memory
-  for (int i = threadIdx.x; i < 2 * n; i += 256) stw[i] = twg[i];
   const T2* tw = stw;
   const double* __restrict__ in = (const double*)fd.in + (long long)r * fd.in_ld;
-  constexpr int RT2 = RT / 2;
+  // Each thread owns the row pair (rp, rp + 1) and the indices kk = kq + KS j
+  // (phi = 2kk, 2kk + 1); the loads of a batch of NB indices, and of the
+  // twiddle table, are all issued before the first shared-memory store.
+  constexpr int RT2 = RT / 2, KS = 256 / RT2, NB = 4, NTW = (2 * n + 255) / 256;
+  const int rp = 2 * (threadIdx.x % RT2), kq = threadIdx.x / RT2;
+  const int rowg = row0 + rp;
+  const bool row_ok = rowg < g.n_theta;
   const bool vec = (g.ld % 2) == 0;
-#pragma unroll (sizeof(T) == 4 ? 4 : 2)
-  for (int i = threadIdx.x; i < n * RT2; i += 256) {
-    const int kk = i / RT2, rr = 2 * (i - kk * RT2);
-    const int row = row0 + rr;
-    double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;  // (phi 2kk | 2kk+1) x (row rr | rr+1)
-    if (row < g.n_theta) {
-      const double* src = in + (long long)(2 * kk) * g.ld + row;
-      if (vec) {
-        const double2 u = *reinterpret_cast<const double2*>(src);
-        const double2 w = *reinterpret_cast<const double2*>(src + g.ld);
-        a0 = u.x; a1 = u.y; b0 = w.x; b1 = w.y;
-      } else {
-        a0 = src[0]; a1 = src[1]; b0 = src[g.ld]; b1 = src[g.ld + 1];
+  T2 twr[NTW];
+#pragma unroll
+  for (int i = 0; i < NTW; ++i)
+    if (threadIdx.x + 256 * i < 2 * n) twr[i] = twg[threadIdx.x + 256 * i];
+  for (int kb = 0; kb < n; kb += KS * NB) {
+    double2 u[NB], w[NB];  // (row rp | rp+1) at phi 2kk (u) and 2kk+1 (w)
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int kk = kb + kq + KS * b;
+      u[b] = w[b] = make_double2(0.0, 0.0);
+      if (row_ok && kk < n) {
+        const double* src = in + (long long)(2 * kk) * g.ld + rowg;
+        if (vec) {
+          u[b] = *reinterpret_cast<const double2*>(src);
+          w[b] = *reinterpret_cast<const double2*>(src + g.ld);
+        } else {
+          u[b] = make_double2(src[0], src[1]);
+          w[b] = make_double2(src[g.ld], src[g.ld + 1]);
+        }
       }
     }
-    const int pj = pin<S>(kk);
-    T2 z0, z1;
-    z0.x = (T)a0; z0.y = (T)b0;
-    z1.x = (T)a1; z1.y = (T)b1;
-    sm[rr * KP + pj] = z0;
-    sm[(rr + 1) * KP + pj] = z1;
+    if (kb == 0) {
+#pragma unroll
+      for (int i = 0; i < NTW; ++i)
+        if (threadIdx.x + 256 * i < 2 * n) stw[threadIdx.x + 256 * i] = twr[i];
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int kk = kb + kq + KS * b;
+      if (kk >= n) continue;
+      const int pj = pin<S>(kk);
+      T2 z0, z1;
+      z0.x = (T)u[b].x; z0.y = (T)w[b].x;
+      z1.x = (T)u[b].y; z1.y = (T)w[b].y;
+      sm[rp * KP + pj] = z0;
+      sm[(rp + 1) * KP + pj] = z1;
+    }
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -326,13 +384,14 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   __syncthreads();
   // X_k = (Z_k + conj Z_{n-k})/2 - i e^{-2 pi i k/P} (Z_k - conj Z_{n-k})/2, then ES/EA
   typedef T Tt;
-  const Tt scale = (Tt)(1.0 / (double)g.n_phi);
-  constexpr int npair = RT / 2;
   T2* out = (T2*)fd.out + (long long)r * fd.out_ld;
-  for (int i = threadIdx.x; i < g.n_m * npair; i += 256) {
-    const int k = i / npair, jp = i - k * npair;
-    const int jg = (row0 >> 1) + jp;
-    if (jg >= g.nh) continue;
+  // this thread's colatitude pair jp (rows 2jp, 2jp + 1) and orders k = kq + KS j
+  const int jp = threadIdx.x % RT2, jg = (row0 >> 1) + jp;
+  if (jg >= g.nh) return;
+  Tt fac = (Tt)(1.0 / (double)g.n_phi);
+  if (fd.flags & FFT_OSIN2) fac *= from_f64<Tt>(g.osin2[jg]);
+  if (fd.flags & FFT_WEIGHT) fac *= from_f64<Tt>(g.wgt[jg]);
+  for (int k = kq; k < g.n_m; k += KS) {
     T2 c[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -342,14 +401,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
       const T2 D = csub(Zk, Zn);
       const T2 u = cmul(cconj(tw[k]), D);
       T2 X;
-      X.x = (Tt)0.5 * (Zk.x + Zn.x + u.y) * scale;
-      X.y = (Tt)0.5 * (Zk.y + Zn.y - u.x) * scale;
+      X.x = (Tt)0.5 * (Zk.x + Zn.x + u.y);
+      X.y = (Tt)0.5 * (Zk.y + Zn.y - u.x);
       if (k == 0) X.y = 0;
       c[h] = X;
     }
-    Tt fac = 1;
-    if (fd.flags & FFT_OSIN2) fac *= from_f64<Tt>(g.osin2[jg]);
-    if (fd.flags & FFT_WEIGHT) fac *= from_f64<Tt>(g.wgt[jg]);
     c[0] = cscale(c[0], fac);
     c[1] = cscale(c[1], fac);
     const long long o = ((long long)k * g.nh + jg) * 2;
