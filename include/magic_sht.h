@@ -220,6 +220,61 @@ typedef struct magic_sht_td_args {
 int magic_sht_get_td(magic_sht_handle* h, int n_levels, const double* r, const int* lcut, double cor_fac,
                      const double* epsc, const magic_sht_td_args* a);
 
+/* ---- Courant condition of the radial loop (courant.f90:54-278, the branch
+ * the reference compiles): per level, the maxima over the grid of the radial
+ * and horizontal velocity terms (fluid + damped Alfven velocity with the
+ * Lorentz force), then dtrkc = min(dtrkc, sqrt(delxr2 / vr2max)) and
+ * dthkc = min(dthkc, sqrt(delxh2 / vh2max)); a level whose maximum is 0 keeps
+ * its values.  Grids: device pointers as transform_to_grid_space writes them
+ * (level stride grid_ld); br = bt = bp = NULL drops the Lorentz-force term
+ * (l_mag_LF off or l_mag_kin).  Radial functions: arrays of n_levels (host or
+ * device); dtrkc, dthkc: in/out arrays of n_levels (host or device; the
+ * radial loop starts them at 1e10).  FP64 in every precision form. */
+typedef struct magic_sht_courant_args {
+  const double *vr, *vt, *vp, *br, *bt, *bp;
+  long long grid_ld;
+  const double *orho1, *orho2, *or2, *or4, *delxr2, *delxh2;
+  double courfac, alffac, LFfac, opm;
+  int l_cour_alf_damp;
+} magic_sht_courant_args;
+int magic_sht_courant(magic_sht_handle* h, int n_levels, const magic_sht_courant_args* a, double* dtrkc,
+                      double* dthkc);
+
+/* ---- new time step from the Courant steps (dt_courant, courant.f90:280-346,
+ * without its log lines): host arrays of n_levels; *l_new_dt = 1 and *dt_new
+ * the new step when dt > dtMax, dt > min(dtrkc, dthkc), or 2 dt < that
+ * minimum (and dt < dtMax); otherwise 0 and dt.  Needs no GPU. */
+int magic_sht_dt_courant(int n_levels, const double* dtrkc, const double* dthkc, double dt, double dtMax,
+                         int* l_new_dt, double* dt_new);
+
+/* ---- boundary pieces of the radial loop (nonlinear_bcs.f90), one radial
+ * level each; grids f(nlat_padded, n_phi_max) like the facade routines, host
+ * or device pointers.
+ * v_rigid_boundary (:120-175): a rigid boundary rotating at omega, with
+ * r2_rho0 = r^2 rho0 at that boundary: vr = 0 (kept when keep_vr, l_vr_cmb /
+ * l_vr_icb), vt = 0, vp = r2_rho0 sin^2(theta) omega; when lDeriv, cvr =
+ * 2 r2_rho0 cos(theta) omega and dvrdt, dvrdp, dvtdp, dvpdp = 0.  NULL grids
+ * are skipped (vr, vt, vp are required). */
+typedef struct magic_sht_rigid_args {
+  double *vr, *vt, *vp;                    /* required */
+  double *cvr, *dvrdt, *dvrdp, *dvtdp, *dvpdp; /* written when non-NULL (lDeriv) */
+} magic_sht_rigid_args;
+int magic_sht_v_rigid_boundary(magic_sht_handle* h, double r2_rho0, double omega, int keep_vr,
+                               const magic_sht_rigid_args* a);
+/* v_center_sphere (:177-224): the l = 1 flow at the centre of a full sphere
+ * from the spectrum ddw (lm_max complex; uses l = 1, m = 0 and m = 1). */
+int magic_sht_v_center_sphere(magic_sht_handle* h, const double* ddw, double* vr, double* vt, double* vp);
+/* get_br_v_bcs (:24-69): spat_to_sphertor of br vt / (r^2 sin^2) and
+ * br (vp / (r^2 sin^2) - omega), i.e. of fac br vt and br (fac vp - omega
+ * sin^2(theta)) with fac = or2 orho1, into br_vt_lm, br_vp_lm (lm_max complex). */
+int magic_sht_get_br_v_bcs(magic_sht_handle* h, const double* br, const double* vt, const double* vp, double omega,
+                           double or2, double orho1, double* br_vt_lm, double* br_vp_lm);
+/* get_b_nl_bcs (:71-118): b_nl_bc = -fac br_vt_lm and aj_nl_bc = -fac br_vp_lm
+ * for l > 0, 0 at l = m = 0; fac = conductance_ma prmag at the CMB (both
+ * outputs), sigma_ratio prmag at the ICB (b_nl_bc = NULL: aj only). */
+int magic_sht_get_b_nl_bcs(magic_sht_handle* h, double fac, const double* br_vt_lm, const double* br_vp_lm,
+                           double* b_nl_bc, double* aj_nl_bc);
+
 /* ---- CUDA-graph capture of a device-pointer call sequence on the handle's
  * stream (e.g. the radial loop's transform set), replayed with one launch. */
 int magic_sht_graph_begin(magic_sht_handle* h);

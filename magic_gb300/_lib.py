@@ -54,6 +54,20 @@ class TdArgs(ctypes.Structure):
     _fields_ = [(n, _V) for n in TD_IN + TD_OUT] + [("spec_ld", ctypes.c_longlong)]
 
 
+class CourantArgs(ctypes.Structure):
+    _fields_ = ([(n, _V) for n in ["vr", "vt", "vp", "br", "bt", "bp"]] + [("grid_ld", ctypes.c_longlong)] +
+                [(n, _V) for n in ["orho1", "orho2", "or2", "or4", "delxr2", "delxh2"]] +
+                [(n, ctypes.c_double) for n in ["courfac", "alffac", "LFfac", "opm"]] +
+                [("l_cour_alf_damp", ctypes.c_int)])
+
+
+RIGID = ["vr", "vt", "vp", "cvr", "dvrdt", "dvrdp", "dvtdp", "dvpdp"]
+
+
+class RigidArgs(ctypes.Structure):
+    _fields_ = [(n, _V) for n in RIGID]
+
+
 class LmSpaceArgs(ctypes.Structure):
     _fields_ = ([(n, _V) for n in LM_SPACE_IN] + [("grid_ld", ctypes.c_longlong)] +
                 [(n, _V) for n in LM_SPACE_OUT] + [("spec_ld", ctypes.c_longlong)])
@@ -94,6 +108,12 @@ SIGNATURES = {
     "magic_sht_set_host_async": [_V, ctypes.c_int],
     "magic_sht_get_td": [_V, ctypes.c_int, _V, _V, ctypes.c_double, _V, ctypes.POINTER(TdArgs)],
     "magic_sht_get_nl": [_V, ctypes.c_int, _V, ctypes.POINTER(GridSpaceArgs), ctypes.POINTER(LmSpaceArgs)],
+    "magic_sht_courant": [_V, ctypes.c_int, ctypes.POINTER(CourantArgs), _V, _V],
+    "magic_sht_dt_courant": [ctypes.c_int, _V, _V, ctypes.c_double, ctypes.c_double, _I, _D],
+    "magic_sht_v_rigid_boundary": [_V, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(RigidArgs)],
+    "magic_sht_v_center_sphere": [_V, _V, _V, _V, _V],
+    "magic_sht_get_br_v_bcs": [_V, _V, _V, _V, ctypes.c_double, ctypes.c_double, ctypes.c_double, _V, _V],
+    "magic_sht_get_b_nl_bcs": [_V, ctypes.c_double, _V, _V, _V, _V],
     "magic_sht_graph_begin": [_V],
     "magic_sht_graph_end": [_V, ctypes.POINTER(_V)],
     "magic_sht_graph_launch": [_V, _V],

@@ -159,6 +159,21 @@ struct TdArgs {
   double cor_fac;       // CorFac (1/E)
 };
 
+// Courant condition (courant.cu); grids [level][ld], radial functions [level]
+struct CourantArgs {
+  const double *vr, *vt, *vp, *br, *bt, *bp;  // br = null: no Lorentz-force term
+  long long ld;
+  const double *orho1, *orho2, *or2, *or4, *delxr2, *delxh2;
+  double courfac, alffac, LFfac, opm;
+  int alf_damp;
+};
+
+// grids of one level written at a rigid boundary (bcs.cu): vr, vt, vp, cvr,
+// dvrdt, dvrdp, dvtdp, dvpdp; null entries are skipped
+struct BcGrids {
+  double* p[8];
+};
+
 __host__ __device__ inline int tc_nch(int n_l) { return ((n_l + 1) / 2 + 63) / 64; }
 
 #define CUDA_TRY(x)                                                        \

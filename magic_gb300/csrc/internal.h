@@ -51,3 +51,16 @@ cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& ou
 
 // td.cu
 cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, cudaStream_t st);
+// boundary pieces of the radial loop, one level (bcs.cu); theta = the n_theta
+// Gauss colatitudes north to south
+cudaError_t launch_v_rigid_boundary(const ShtGeom& g, const double* theta, const BcGrids& a, double r2rho0,
+                                    double omega, int keep_vr, cudaStream_t st);
+cudaError_t launch_v_center_sphere(const ShtGeom& g, const double* theta, const double2* ddw, int lm11, double* vr,
+                                   double* vt, double* vp, cudaStream_t st);
+cudaError_t launch_br_v_products(const ShtGeom& g, const double* theta, const double* br, const double* vt,
+                                 const double* vp, double fac, double omega, double* out_t, double* out_p,
+                                 cudaStream_t st);
+cudaError_t launch_b_nl_bcs(int K, double fac, const double2* y, double2* x, cudaStream_t st);
+// per-level maxima into mx[2 * nlev] (zeroed here), then dtrkc / dthkc updated in place
+cudaError_t launch_courant(const ShtGeom& g, const CourantArgs& a, int nlev, unsigned long long* mx, double* dtrkc,
+                           double* dthkc, cudaStream_t st);

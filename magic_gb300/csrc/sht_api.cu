@@ -261,7 +261,7 @@ struct PhaseScope {
 // in place, temporaries come from the handle's workspace.
 class CallCtx {
  public:
-  enum Kind { IN = 0, OUT = 1, TMP = 2 };
+  enum Kind { IN = 0, OUT = 1, TMP = 2, INOUT = 3 };
   CallCtx(magic_sht_handle* h) : h_(h) {}
 
   // grid arrays: nlev levels of n_phi rows of ld doubles, level stride `lds`
@@ -273,6 +273,13 @@ class CallCtx {
   int raw_in(const void* p, size_t bytes) {
     Ent e;
     e.host = p; e.kind = IN; e.bytes = bytes; e.raw = true;
+    ents_.push_back(e);
+    return (int)ents_.size() - 1;
+  }
+  // staged in before the kernels and back after them when `p` is host memory
+  int raw_inout(void* p, size_t bytes) {
+    Ent e;
+    e.host = p; e.kind = INOUT; e.bytes = bytes; e.raw = true;
     ents_.push_back(e);
     return (int)ents_.size() - 1;
   }
@@ -299,7 +306,8 @@ class CallCtx {
       }
       e.dev = h_->ws + off;
       off += align256(e.bytes);
-      if (e.kind == IN && e.bytes) CK(cudaMemcpyAsync(e.dev, e.host, e.bytes, cudaMemcpyHostToDevice, h_->stream));
+      if ((e.kind == IN || e.kind == INOUT) && e.bytes)
+        CK(cudaMemcpyAsync(e.dev, e.host, e.bytes, cudaMemcpyHostToDevice, h_->stream));
     }
     return MAGIC_SHT_OK;
   }
@@ -309,7 +317,7 @@ class CallCtx {
   int finish() {
     const ShtGeom& g = h_->g;
     for (auto& e : ents_) {
-      if (e.kind != OUT || e.is_dev || !e.host) continue;
+      if ((e.kind != OUT && e.kind != INOUT) || e.is_dev || !e.host) continue;
       if (e.grid && g.ld > g.n_theta) {
         for (int r = 0; r < e.nlev; ++r)
           CK(cudaMemcpy2DAsync((char*)e.host + (size_t)r * e.lds * 8, (size_t)g.ld * 8,
@@ -1372,6 +1380,151 @@ int magic_sht_get_td(magic_sht_handle* h, int n, const double* r, const int* lcu
   h->launches++;
   CK(launch_get_td(g, t, n, h->stream));
   return cx.finish();
+}
+
+int magic_sht_courant(magic_sht_handle* h, int n, const magic_sht_courant_args* a, double* dtrkc, double* dthkc) {
+  TRY(check_handle(h));
+  if (!a || !dtrkc || !dthkc || n < 0) return set_err(MAGIC_SHT_ERR_ARG, "null args/dtrkc/dthkc or n_levels < 0");
+  if (n == 0) return MAGIC_SHT_OK;
+  const ShtGeom& g = h->g;
+  if (a->grid_ld < (long long)g.n_phi * g.ld) return set_err(MAGIC_SHT_ERR_ARG, "grid_ld smaller than one level");
+  const bool mag = a->br || a->bt || a->bp;
+  const double* const grids[6] = {a->vr, a->vt, a->vp, a->br, a->bt, a->bp};
+  for (int i = 0; i < (mag ? 6 : 3); ++i)
+    if (!grids[i] || !is_device_ptr(grids[i]))
+      return set_err(MAGIC_SHT_ERR_ARG, "courant grid %d: null or host pointer (device grids only)", i);
+  const double* const rf[6] = {a->orho1, a->orho2, a->or2, a->or4, a->delxr2, a->delxh2};
+  for (int i = 0; i < 6; ++i)
+    if (!rf[i]) return set_err(MAGIC_SHT_ERR_ARG, "courant radial function %d is null", i);
+  DeviceGuard dg(h->device);
+  CallCtx cx(h);
+  int irf[6];
+  for (int i = 0; i < 6; ++i) irf[i] = cx.raw_in(rf[i], (size_t)n * 8);
+  const int i_r = cx.raw_inout(dtrkc, (size_t)n * 8), i_h = cx.raw_inout(dthkc, (size_t)n * 8);
+  const int i_mx = cx.tmp((size_t)n * 16);
+  TRY(cx.prepare());
+  CourantArgs c{};
+  c.vr = a->vr; c.vt = a->vt; c.vp = a->vp;
+  if (mag) { c.br = a->br; c.bt = a->bt; c.bp = a->bp; }
+  c.ld = a->grid_ld;
+  c.orho1 = (const double*)cx.dev(irf[0]); c.orho2 = (const double*)cx.dev(irf[1]);
+  c.or2 = (const double*)cx.dev(irf[2]); c.or4 = (const double*)cx.dev(irf[3]);
+  c.delxr2 = (const double*)cx.dev(irf[4]); c.delxh2 = (const double*)cx.dev(irf[5]);
+  c.courfac = a->courfac; c.alffac = a->alffac; c.LFfac = a->LFfac; c.opm = a->opm;
+  c.alf_damp = a->l_cour_alf_damp;
+  h->launches += 2;
+  CK(launch_courant(g, c, n, (unsigned long long*)cx.dev(i_mx), (double*)cx.dev(i_r), (double*)cx.dev(i_h),
+                    h->stream));
+  return cx.finish();
+}
+
+int magic_sht_v_rigid_boundary(magic_sht_handle* h, double r2_rho0, double omega, int keep_vr,
+                               const magic_sht_rigid_args* a) {
+  TRY(check_handle(h));
+  if (!a || !a->vr || !a->vt || !a->vp) return set_err(MAGIC_SHT_ERR_ARG, "null args or vr/vt/vp");
+  DeviceGuard dg(h->device);
+  const long long gl = (long long)h->g.n_phi * h->g.ld;
+  double* const ps[8] = {a->vr, a->vt, a->vp, a->cvr, a->dvrdt, a->dvrdp, a->dvtdp, a->dvpdp};
+  CallCtx cx(h);
+  int idx[8];
+  // vr is read back unchanged when it is kept, so it is staged both ways
+  for (int i = 0; i < 8; ++i) idx[i] = (i == 0 && keep_vr) ? cx.grid_in(ps[i], 1, gl) : cx.grid_out(ps[i], 1, gl);
+  TRY(cx.prepare());
+  BcGrids b{};
+  for (int i = 0; i < 8; ++i) b.p[i] = (i == 0 && keep_vr) ? nullptr : (double*)cx.dev(idx[i]);
+  h->launches++;
+  CK(launch_v_rigid_boundary(h->g, h->d_theta, b, r2_rho0, omega, keep_vr, h->stream));
+  return cx.finish();
+}
+
+int magic_sht_v_center_sphere(magic_sht_handle* h, const double* ddw, double* vr, double* vt, double* vp) {
+  TRY(check_handle(h));
+  if (!ddw || !vr || !vt || !vp) return set_err(MAGIC_SHT_ERR_ARG, "null argument");
+  if (h->g.l_max < 1) return set_err(MAGIC_SHT_ERR_SIZE, "v_center_sphere needs l_max >= 1");
+  DeviceGuard dg(h->device);
+  const long long gl = (long long)h->g.n_phi * h->g.ld;
+  CallCtx cx(h);
+  const int i_s = cx.spec_in(ddw, 1, h->g.lm_max);
+  const int i_r = cx.grid_out(vr, 1, gl), i_t = cx.grid_out(vt, 1, gl), i_p = cx.grid_out(vp, 1, gl);
+  TRY(cx.prepare());
+  const int lm11 = (h->g.minc == 1 && h->g.n_m > 1) ? h->lmoff[1] : -1;
+  h->launches++;
+  CK(launch_v_center_sphere(h->g, h->d_theta, (const double2*)cx.dev(i_s), lm11, (double*)cx.dev(i_r),
+                            (double*)cx.dev(i_t), (double*)cx.dev(i_p), h->stream));
+  return cx.finish();
+}
+
+int magic_sht_get_br_v_bcs(magic_sht_handle* h, const double* br, const double* vt, const double* vp, double omega,
+                           double or2, double orho1, double* br_vt_lm, double* br_vp_lm) {
+  TRY(check_handle(h));
+  if (!br || !vt || !vp || !br_vt_lm || !br_vp_lm) return set_err(MAGIC_SHT_ERR_ARG, "null argument");
+  DeviceGuard dg(h->device);
+  const ShtGeom& g = h->g;
+  const long long gl = (long long)g.n_phi * g.ld;
+  CallCtx cx(h);
+  const int i_b = cx.grid_in(br, 1, gl), i_t = cx.grid_in(vt, 1, gl), i_p = cx.grid_in(vp, 1, gl);
+  const int t_t = cx.tmp((size_t)gl * 8), t_p = cx.tmp((size_t)gl * 8);
+  const int o_t = cx.spec_out(br_vt_lm, 1, g.lm_max), o_p = cx.spec_out(br_vp_lm, 1, g.lm_max);
+  std::vector<int> hs_vc = {cx.tmp(hs_bytes(h, 1)), cx.tmp(hs_bytes(h, 1))};
+  TRY(cx.prepare());
+  h->launches++;
+  CK(launch_br_v_products(g, h->d_theta, (const double*)cx.dev(i_b), (const double*)cx.dev(i_t),
+                          (const double*)cx.dev(i_p), or2 * orho1, omega, (double*)cx.dev(t_t),
+                          (double*)cx.dev(t_p), h->stream));
+  LevelCtl lv;
+  lv.nlev = 1; lv.lcut0 = g.l_max;
+  lv.spec_ld = g.lm_max; lv.grid_ld = gl;
+  std::vector<ScalarFwd> sc;
+  std::vector<VectorFwd> vc = {{t_t, t_p, o_t, o_p}};
+  TRY(run_forward(h, cx, lv, sc, vc, {}, hs_vc));
+  return cx.finish();
+}
+
+int magic_sht_get_b_nl_bcs(magic_sht_handle* h, double fac, const double* br_vt_lm, const double* br_vp_lm,
+                           double* b_nl_bc, double* aj_nl_bc) {
+  TRY(check_handle(h));
+  if (!br_vp_lm || !aj_nl_bc || (b_nl_bc && !br_vt_lm)) return set_err(MAGIC_SHT_ERR_ARG, "null argument");
+  DeviceGuard dg(h->device);
+  const int K = h->g.lm_max;
+  CallCtx cx(h);
+  const int i_vt = b_nl_bc ? cx.spec_in(br_vt_lm, 1, K) : -1, i_vp = cx.spec_in(br_vp_lm, 1, K);
+  const int o_b = b_nl_bc ? cx.spec_out(b_nl_bc, 1, K) : -1, o_j = cx.spec_out(aj_nl_bc, 1, K);
+  TRY(cx.prepare());
+  if (b_nl_bc) {
+    h->launches++;
+    CK(launch_b_nl_bcs(K, fac, (const double2*)cx.dev(i_vt), (double2*)cx.dev(o_b), h->stream));
+  }
+  h->launches++;
+  CK(launch_b_nl_bcs(K, fac, (const double2*)cx.dev(i_vp), (double2*)cx.dev(o_j), h->stream));
+  return cx.finish();
+}
+
+int magic_sht_dt_courant(int n, const double* dtrkc, const double* dthkc, double dt, double dtMax,
+                         int* l_new_dt, double* dt_new) {
+  if (!dtrkc || !dthkc || !l_new_dt || !dt_new || n < 0)
+    return set_err(MAGIC_SHT_ERR_ARG, "null argument or n_levels < 0");
+  const double dt_fac = 2.0;
+  double dt_r = 1000.0 * dtMax, dt_h = 1000.0 * dtMax;
+  for (int i = 0; i < n; ++i) {
+    dt_r = std::min(dtrkc[i], dt_r);
+    dt_h = std::min(dthkc[i], dt_h);
+  }
+  const double dtMin = std::min(dt_r, dt_h);
+  const double dt_2 = std::min(0.5 * (1.0 / dt_fac + 1.0) * dtMin, dtMax);
+  if (dt > dtMax) {
+    *l_new_dt = 1;
+    *dt_new = dtMax;
+  } else if (dt > dtMin) {
+    *l_new_dt = 1;
+    *dt_new = dt_2;
+  } else if (dt_fac * dt < dtMin && dt < dtMax) {
+    *l_new_dt = 1;
+    *dt_new = dt_2;
+  } else {
+    *l_new_dt = 0;
+    *dt_new = dt;
+  }
+  return MAGIC_SHT_OK;
 }
 
 int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,

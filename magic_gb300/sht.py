@@ -429,6 +429,96 @@ class SHT:
                                          float(cor_fac), None if ep is None else ep.ctypes.data, ctypes.byref(a)))
         return outs
 
+    def courant(self, grids: dict, radial: dict, courfac: float, alffac: float, LFfac: float = 1.0,
+                opm: float = 1.0, alf_damp: bool = True, dtrkc=None, dthkc=None):
+        """Courant condition of the radial loop (courant.f90:54-278) on CUDA
+        grids ``vrc``, ``vtc``, ``vpc`` (and ``brc``, ``btc``, ``bpc`` for the
+        Lorentz-force term; leave them out when it is off), [level][phi][theta].
+        ``radial`` holds per-level arrays ``orho1``, ``orho2``, ``or2``,
+        ``or4``, ``delxr2``, ``delxh2``.  Returns (dtrkc, dthkc) as numpy
+        arrays, each the minimum of its start value (1e10 by default, as in
+        the radial loop) and the level's Courant step."""
+        v = grids["vrc"]
+        if not (_is_torch(v) and v.is_cuda):
+            raise ValueError("courant takes CUDA grids")
+        n = int(v.shape[0])
+        a = _lib.CourantArgs()
+        keep = []
+        for k, f in (("vrc", "vr"), ("vtc", "vt"), ("vpc", "vp"), ("brc", "br"), ("btc", "bt"), ("bpc", "bp")):
+            t = grids.get(k)
+            if t is None:
+                continue
+            t = t.contiguous()
+            keep.append(t)
+            setattr(a, f, t.data_ptr())
+        a.grid_ld = int(v[0].numel())
+        rf = {}
+        for k in ("orho1", "orho2", "or2", "or4", "delxr2", "delxh2"):
+            rf[k] = np.ascontiguousarray(radial[k], dtype=np.float64)
+            if rf[k].shape != (n,):
+                raise ValueError("radial[%r] needs %d levels" % (k, n))
+            setattr(a, k, rf[k].ctypes.data)
+        a.courfac, a.alffac, a.LFfac, a.opm = float(courfac), float(alffac), float(LFfac), float(opm)
+        a.l_cour_alf_damp = 1 if alf_damp else 0
+        dr = np.full(n, 1e10) if dtrkc is None else np.array(dtrkc, dtype=np.float64)
+        dh = np.full(n, 1e10) if dthkc is None else np.array(dthkc, dtype=np.float64)
+        self._bind_torch_stream()
+        check(self._lib.magic_sht_courant(self._h, n, ctypes.byref(a), dr.ctypes.data, dh.ctypes.data))
+        return dr, dh
+
+    # ------------------------------------------------ boundary pieces
+    def v_rigid_boundary(self, grids: dict, r2_rho0: float, omega: float, keep_vr: bool = False):
+        """v_rigid_boundary (nonlinear_bcs.f90:120-175) in place on one level's
+        grids: ``vr``, ``vt``, ``vp`` and, when given (lDeriv), ``cvr``,
+        ``dvrdt``, ``dvrdp``, ``dvtdp``, ``dvpdp`` (numpy or CUDA, each
+        (n_phi_max, nlat_padded))."""
+        a = _lib.RigidArgs()
+        keep = []
+        for k in _lib.RIGID:
+            x = grids.get(k)
+            if x is None:
+                continue
+            if _is_torch(x) and not x.is_contiguous():
+                raise ValueError("%s must be contiguous (written in place)" % k)
+            if not _is_torch(x) and not (isinstance(x, np.ndarray) and x.flags.c_contiguous
+                                         and x.dtype == np.float64):
+                raise ValueError("%s must be a contiguous float64 array (written in place)" % k)
+            keep.append(x)
+            setattr(a, k, x.data_ptr() if _is_torch(x) else x.ctypes.data)
+        self._bind_torch_stream()
+        check(self._lib.magic_sht_v_rigid_boundary(self._h, float(r2_rho0), float(omega), 1 if keep_vr else 0,
+                                                   ctypes.byref(a)))
+        return grids
+
+    def v_center_sphere(self, ddw):
+        """v_center_sphere (nonlinear_bcs.f90:177-224): (vr, vt, vp) of the l = 1
+        flow at the centre of a full sphere from the spectrum ``ddw``."""
+        x, px = self._spec_in(ddw)
+        outs = [self._grid(x) for _ in range(3)]
+        check(self._lib.magic_sht_v_center_sphere(self._h, px, *[p for _, p in outs]))
+        return tuple(o for o, _ in outs)
+
+    def get_br_v_bcs(self, br, vt, vp, omega: float, or2: float, orho1: float):
+        """get_br_v_bcs (nonlinear_bcs.f90:24-69): (br_vt_lm, br_vp_lm)."""
+        ins = [self._grid_in(x) for x in (br, vt, vp)]
+        outs = [self._spec(ins[0][0]) for _ in range(2)]
+        check(self._lib.magic_sht_get_br_v_bcs(self._h, *[p for _, p in ins], float(omega), float(or2),
+                                               float(orho1), *[p for _, p in outs]))
+        return tuple(o for o, _ in outs)
+
+    def get_b_nl_bcs(self, bc: str, fac: float, br_vt_lm, br_vp_lm):
+        """get_b_nl_bcs (nonlinear_bcs.f90:71-118): (b_nl_bc, aj_nl_bc) at the
+        'CMB' (fac = conductance_ma prmag), (None, aj_nl_bc) at the 'ICB'
+        (fac = sigma_ratio prmag)."""
+        if bc not in ("CMB", "ICB"):
+            raise ValueError("bc must be 'CMB' or 'ICB'")
+        vp_, pvp = self._spec_in(br_vp_lm)
+        vt_, pvt = self._spec_in(br_vt_lm) if bc == "CMB" else (None, None)
+        aj, paj = self._spec(vp_)
+        b, pb = self._spec(vp_) if bc == "CMB" else (None, None)
+        check(self._lib.magic_sht_get_b_nl_bcs(self._h, float(fac), pvt, pvp, pb, paj))
+        return b, aj
+
     # ---------------------------------------------------------- profiling
     def set_profiling(self, on: bool):
         check(self._lib.magic_sht_set_profiling(self._h, 1 if on else 0))
@@ -466,6 +556,21 @@ class SHT:
 
     def graph_destroy(self, g):
         check(self._lib.magic_sht_graph_destroy(g))
+
+
+def dt_courant(dtrkc, dthkc, dt: float, dtMax: float):
+    """New time step from the Courant steps of all levels (dt_courant,
+    courant.f90:280-346): returns (l_new_dt, dt_new).  Host only."""
+    lib = _lib.load()
+    r = np.ascontiguousarray(dtrkc, dtype=np.float64)
+    h = np.ascontiguousarray(dthkc, dtype=np.float64)
+    if r.shape != h.shape or r.ndim != 1:
+        raise ValueError("dtrkc and dthkc need the same 1-d shape")
+    flag = ctypes.c_int(0)
+    new = ctypes.c_double(0.0)
+    check(lib.magic_sht_dt_courant(int(r.shape[0]), r.ctypes.data, h.ctypes.data, float(dt), float(dtMax),
+                                   ctypes.byref(flag), ctypes.byref(new)))
+    return bool(flag.value), new.value
 
 
 def measure_gflops(precision: str = "fp64", device: int = 0) -> float:

@@ -327,6 +327,134 @@ def get_nl(grids: dict, or2, n_theta: int) -> dict:
     }
 
 
+def courant(grids: dict, radial: dict, n_theta: int, courfac: float, alffac: float, LFfac: float = 1.0,
+            opm: float = 1.0, alf_damp: bool = True, dtrkc=None, dthkc=None):
+    """Courant steps per level (courant.f90:54-278, the XSH_COURANT == 0
+    branch :193-276): maxima over the grid of the radial and horizontal
+    velocity terms, fluid plus damped Alfven velocity when ``brc``, ``btc``,
+    ``bpc`` are given (:226-252), fluid only otherwise (:256-268); each
+    product rounded in the reference's order; a 0/0 term is left out of the
+    maximum.  Grids [level][phi][theta] (scrambled rows); numpy FP64."""
+    theta, _ = gauleg(n_theta)
+    sn2 = np.repeat(1.0 / np.sin(theta[: n_theta // 2]) ** 2, 2)
+    g = {k: np.asarray(v, dtype=np.float64)[..., :n_theta] for k, v in grids.items() if v is not None}
+    n = g["vrc"].shape[0]
+    rf = {k: np.asarray(radial[k], dtype=np.float64) for k in ("orho1", "orho2", "or2", "or4", "delxr2", "delxh2")}
+    dtr = np.full(n, 1e10) if dtrkc is None else np.array(dtrkc, dtype=np.float64)
+    dth = np.full(n, 1e10) if dthkc is None else np.array(dthkc, dtype=np.float64)
+    cf2, af2 = courfac * courfac, alffac * alffac
+    mag = "brc" in g
+    with np.errstate(invalid="ignore", divide="ignore"):
+        for i in range(n):
+            vr, vt, vp = g["vrc"][i], g["vtc"][i], g["vpc"][i]
+            vflr2 = rf["orho2"][i] * vr * vr
+            vflh2 = (vt * vt + vp * vp) * sn2 * rf["orho2"][i]
+            if mag:
+                if alf_damp:
+                    h = 0.5 * (1.0 + opm)
+                    valri2, valhi2 = h * h / rf["delxr2"][i], h * h / rf["delxh2"][i]
+                else:
+                    valri2 = valhi2 = 0.0
+                br, bt, bp = g["brc"][i], g["btc"][i], g["bpc"][i]
+                valr = br * br * LFfac * rf["orho1"][i]
+                valr2 = valr * valr / (valr + valri2)
+                vr2 = rf["or4"][i] * (cf2 * vflr2 + af2 * valr2)
+                valh2 = (bt * bt + bp * bp) * LFfac * sn2 * rf["orho1"][i]
+                valh2m = valh2 * valh2 / (valh2 + valhi2)
+                vh2 = rf["or2"][i] * (cf2 * vflh2 + af2 * valh2m)
+            else:
+                vr2 = cf2 * rf["or4"][i] * vflr2
+                vh2 = cf2 * rf["or2"][i] * vflh2
+            vr2max = float(np.fmax.reduce(np.fmax(vr2, 0.0), axis=None))
+            vh2max = float(np.fmax.reduce(np.fmax(vh2, 0.0), axis=None))
+            if vr2max != 0.0:
+                dtr[i] = min(dtr[i], np.sqrt(rf["delxr2"][i] / vr2max))
+            if vh2max != 0.0:
+                dth[i] = min(dth[i], np.sqrt(rf["delxh2"][i] / vh2max))
+    return dtr, dth
+
+
+def _row_trig(n_theta: int):
+    """sin and cos of the colatitude of every scrambled row (horizontal.f90:145-159):
+    rows 2j, 2j+1 at theta_j and pi - theta_j."""
+    theta, _ = gauleg(n_theta)
+    s = np.repeat(np.sin(theta[: n_theta // 2]), 2)
+    c = np.repeat(np.cos(theta[: n_theta // 2]), 2)
+    c[1::2] *= -1.0
+    return s, c
+
+
+def v_rigid_boundary(n_theta: int, n_phi: int, r2_rho0: float, omega: float, keep_vr: bool, vr):
+    """v_rigid_boundary (nonlinear_bcs.f90:120-175) for one level: returns
+    vr, vt, vp, cvr, dvrdt, dvrdp, dvtdp, dvpdp as (n_phi, n_theta) arrays."""
+    s, c = _row_trig(n_theta)
+    z = np.zeros((n_phi, n_theta))
+    vr_out = np.array(vr, dtype=np.float64)[:, :n_theta] if keep_vr else z.copy()
+    vp = np.broadcast_to(r2_rho0 * (s * s) * omega, (n_phi, n_theta)).copy()
+    cvr = np.broadcast_to(r2_rho0 * 2.0 * c * omega, (n_phi, n_theta)).copy()
+    return {"vr": vr_out, "vt": z.copy(), "vp": vp, "cvr": cvr, "dvrdt": z.copy(), "dvrdp": z.copy(),
+            "dvtdp": z.copy(), "dvpdp": z.copy()}
+
+
+def v_center_sphere(ddw, minc: int, n_theta: int, n_phi: int):
+    """v_center_sphere (nonlinear_bcs.f90:177-224): vr, vt, vp (n_phi, n_theta)
+    from ddw(l=1, m=0) (st_map index 1) and ddw(l=1, m=1) (index l_max + 1,
+    minc = 1); y10_norm, y11_norm of preCalculations.f90:313-314."""
+    ddw = np.asarray(ddw)
+    s, c = _row_trig(n_theta)
+    y10, y11 = 0.5 * np.sqrt(3.0 / np.pi), 0.5 * np.sqrt(1.5 / np.pi)
+    d10 = ddw[1].real
+    phi = np.arange(n_phi) * (2.0 * np.pi / (n_phi * minc))
+    if minc == 1:
+        l_max = (np.sqrt(8 * len(ddw) + 1) - 3) / 2  # lm_max = (L+1)(L+2)/2
+        d11 = ddw[int(round(l_max)) + 1]
+        cp, sp = np.cos(phi)[:, None], np.sin(phi)[:, None]
+        cc = d11.real * cp - d11.imag * sp
+        vr = y10 * d10 * c + 2.0 * y11 * s * cc
+        vt = s * (-y10 * d10 * s + 2.0 * y11 * c * cc)
+        vp = -2.0 * y11 * s * (d11.real * sp + d11.imag * cp)
+    else:
+        vr = np.broadcast_to(y10 * d10 * c, (n_phi, n_theta)).copy()
+        vt = np.broadcast_to(-s * y10 * d10 * s, (n_phi, n_theta)).copy()
+        vp = np.zeros((n_phi, n_theta))
+    return vr, vt, vp
+
+
+def get_br_v_bcs(sht: "OracleSHT", br, vt, vp, omega: float, or2: float, orho1: float):
+    """get_br_v_bcs (nonlinear_bcs.f90:24-69) with the oracle's spat_to_sphertor."""
+    n_theta = sht.n_theta_max
+    s, _ = _row_trig(n_theta)
+    fac = or2 * orho1
+    b = np.asarray(br)[:, :n_theta]
+    br_vt = fac * b * np.asarray(vt)[:, :n_theta]
+    br_vp = b * (fac * np.asarray(vp)[:, :n_theta] - omega * (s * s))
+    return sht.spat_to_sphertor(br_vt, br_vp, sht.l_max)
+
+
+def get_b_nl_bcs(fac: float, y):
+    """get_b_nl_bcs (nonlinear_bcs.f90:71-118): -fac y, 0 at l = m = 0."""
+    x = -fac * np.asarray(y, dtype=np.complex128)
+    x[0] = 0.0
+    return x
+
+
+def dt_courant(dtrkc, dthkc, dt: float, dtMax: float):
+    """New time step from the Courant steps (courant.f90:280-346, without the
+    log lines): returns (l_new_dt, dt_new)."""
+    dt_fac = 2.0
+    dt_r = min([1000.0 * dtMax] + [float(x) for x in dtrkc])
+    dt_h = min([1000.0 * dtMax] + [float(x) for x in dthkc])
+    dtMin = min(dt_r, dt_h)
+    dt_2 = min(0.5 * (1.0 / dt_fac + 1.0) * dtMin, dtMax)
+    if dt > dtMax:
+        return True, dtMax
+    if dt > dtMin:
+        return True, dt_2
+    if dt_fac * dt < dtMin and dt < dtMax:
+        return True, dt_2
+    return False, dt
+
+
 def get_td(spec: dict, r, cor_fac: float, l_max: int, minc: int = 1, lcut=None, epsc=None) -> dict:
     """Spectral assembly of the explicit time derivatives at interior levels
     (get_td.f90: get_dwdt :133-208, get_dpdt :311-379, get_dzdt :381-457,
