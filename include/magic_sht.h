@@ -219,6 +219,11 @@ typedef struct magic_sht_td_args {
 } magic_sht_td_args;
 int magic_sht_get_td(magic_sht_handle* h, int n_levels, const double* r, const int* lcut, double cor_fac,
                      const double* epsc, const magic_sht_td_args* a);
+/* The same with a boundary flag per level (nbc, host or device int array of
+ * n_levels; nBc of rIter.f90:193-215): at a level with nbc != 0 only dVxBhLM
+ * is written (get_td.f90:598-612) and the other outputs are left untouched. */
+int magic_sht_get_td_nbc(magic_sht_handle* h, int n_levels, const double* r, const int* lcut, double cor_fac,
+                         const double* epsc, const int* nbc, const magic_sht_td_args* a);
 
 /* ---- Courant condition of the radial loop (courant.f90:54-278, the branch
  * the reference compiles): per level, the maxima over the grid of the radial

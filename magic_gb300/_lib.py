@@ -107,6 +107,7 @@ SIGNATURES = {
     "magic_sht_transform_to_lm_space": [_V, ctypes.c_int, _V, ctypes.POINTER(LmSpaceArgs)],
     "magic_sht_set_host_async": [_V, ctypes.c_int],
     "magic_sht_get_td": [_V, ctypes.c_int, _V, _V, ctypes.c_double, _V, ctypes.POINTER(TdArgs)],
+    "magic_sht_get_td_nbc": [_V, ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, ctypes.POINTER(TdArgs)],
     "magic_sht_get_nl": [_V, ctypes.c_int, _V, ctypes.POINTER(GridSpaceArgs), ctypes.POINTER(LmSpaceArgs)],
     "magic_sht_courant": [_V, ctypes.c_int, ctypes.POINTER(CourantArgs), _V, _V],
     "magic_sht_dt_courant": [ctypes.c_int, _V, _V, ctypes.c_double, ctypes.c_double, _I, _D],

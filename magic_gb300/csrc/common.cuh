@@ -156,6 +156,7 @@ struct TdArgs {
   const double* r;      // [level] radius
   const int* lcut;      // [level] l_R, or null (= l_max)
   const double* epsc;   // [level] internal heating of dsdt(l=0), or null (= 0)
+  const int* nbc;       // [level] boundary flag (nBc != 0), or null (all interior)
   double cor_fac;       // CorFac (1/E)
 };
 

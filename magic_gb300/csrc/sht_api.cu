@@ -1344,6 +1344,11 @@ int magic_sht_get_nl(magic_sht_handle* h, int n, const double* or2, const magic_
 
 int magic_sht_get_td(magic_sht_handle* h, int n, const double* r, const int* lcut, double cor_fac,
                      const double* epsc, const magic_sht_td_args* a) {
+  return magic_sht_get_td_nbc(h, n, r, lcut, cor_fac, epsc, nullptr, a);
+}
+
+int magic_sht_get_td_nbc(magic_sht_handle* h, int n, const double* r, const int* lcut, double cor_fac,
+                         const double* epsc, const int* nbc, const magic_sht_td_args* a) {
   TRY(check_handle(h));
   if (!a || !r || n < 0) return set_err(MAGIC_SHT_ERR_ARG, "null args/r or n_levels < 0");
   if (n == 0) return MAGIC_SHT_OK;
@@ -1364,6 +1369,7 @@ int magic_sht_get_td(magic_sht_handle* h, int n, const double* r, const int* lcu
   const int i_r = cx.raw_in(r, (size_t)n * 8);
   const int i_lc = lcut ? cx.raw_in(lcut, (size_t)n * 4) : -1;
   const int i_ep = epsc ? cx.raw_in(epsc, (size_t)n * 8) : -1;
+  const int i_bc = nbc ? cx.raw_in(nbc, (size_t)n * 4) : -1;
   TRY(cx.prepare());
   TdArgs t{};
   t.w = (const double2*)a->w; t.dw = (const double2*)a->dw; t.z = (const double2*)a->z;
@@ -1376,6 +1382,7 @@ int magic_sht_get_td(magic_sht_handle* h, int n, const double* r, const int* lcu
   t.r = (const double*)cx.dev(i_r);
   t.lcut = (const int*)cx.dev(i_lc);
   t.epsc = (const double*)cx.dev(i_ep);
+  t.nbc = (const int*)cx.dev(i_bc);
   t.cor_fac = cor_fac;
   h->launches++;
   CK(launch_get_td(g, t, n, h->stream));

@@ -1,9 +1,11 @@
-// Spectral assembly of the explicit time derivatives at the interior radial
-// levels (get_td.f90:133-208 get_dwdt, :311-379 get_dpdt, :381-457 get_dzdt,
+// Spectral assembly of the explicit time derivatives at the radial levels
+// (get_td.f90:133-208 get_dwdt, :311-379 get_dpdt, :381-457 get_dzdt,
 // :459-521 get_dsdt, :558-619 get_dbdt) from the analysis outputs of the
 // radial loop: Boussinesq form, Coriolis force on, magnetic field and heat
-// equation on, no double-curl form.  One thread per (level, lm); the l-1 and
-// l+1 neighbours of lm in the m-major order are lm-1 and lm+1.
+// equation on, no double-curl form.  At a boundary level (nbc != 0) only
+// dVxBhLM is written; the other outputs are left as they are, as the
+// reference leaves them.  One thread per (level, lm); the l-1 and l+1
+// neighbours of lm in the m-major order are lm-1 and lm+1.
 // Operator coefficients as in horizontal.f90:204-229:
 //   clm(l,m) = sqrt((l+m)(l-m) / ((2l-1)(2l+1))), dLh = l(l+1), dPhi = i m,
 //   dTheta2S = (l-1) clm(l,m),  dTheta2A = (l+2) clm(l+1,m),
@@ -38,6 +40,10 @@ __global__ void __launch_bounds__(256) get_td_kernel(const ShtGeom g, const TdAr
     const double rr = a.r[r], or1 = 1.0 / rr, or2 = or1 * or1, or4 = or2 * or2;
     const int lR = a.lcut ? min(a.lcut[r], g.l_max) : g.l_max;
     const double dLh = (double)l * (l + 1);
+    if (a.nbc && a.nbc[r] != 0) {  // boundary level: only get_dbdt's dVxBhLM (get_td.f90:598-612)
+      a.dVxBh[o] = cscale(a.VxBt[o], -dLh * rr * rr);
+      continue;
+    }
     const double two_cor = 2.0 * a.cor_fac;
     const bool hasS = l > m, hasA = l < lR;  // l-1 and l+1 terms (clm(m,m) = 0; l = l_R drops l+1)
     const double cS = hasS ? clm(l, m) : 0.0, cA = hasA ? clm(l + 1, m) : 0.0;

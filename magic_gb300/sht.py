@@ -396,11 +396,14 @@ class SHT:
         check(self._lib.magic_sht_get_nl(self._h, n, por2, ctypes.byref(g), ctypes.byref(nl)))
         return outs
 
-    def get_td(self, spec: dict, r, cor_fac: float, lcut=None, epsc=None, out: Optional[dict] = None):
+    def get_td(self, spec: dict, r, cor_fac: float, lcut=None, epsc=None, out: Optional[dict] = None,
+               nbc=None):
         """Spectral assembly of the explicit time derivatives (get_td.f90):
         from CUDA tensors ``w``, ``dw``, ``z`` and the analysis outputs
         (``AdvrLM`` .. ``VxBpLM``) the outputs ``dwdt``, ``dzdt``, ``dpdt``,
-        ``dsdt``, ``dbdt``, ``djdt``, ``dVxBhLM`` ([level][lm] complex)."""
+        ``dsdt``, ``dbdt``, ``djdt``, ``dVxBhLM`` ([level][lm] complex).
+        ``nbc`` (per level, nBc of the radial loop): at a level with nbc != 0
+        only ``dVxBhLM`` is written."""
         import torch
         missing = [k for k in _lib.TD_IN if spec.get(k) is None]
         if missing:
@@ -424,9 +427,11 @@ class SHT:
         r_arr = np.ascontiguousarray(r, dtype=np.float64)
         lc = None if lcut is None else np.ascontiguousarray(lcut, dtype=np.int32)
         ep = None if epsc is None else np.ascontiguousarray(epsc, dtype=np.float64)
+        bc = None if nbc is None else np.ascontiguousarray(nbc, dtype=np.int32)
         self._bind_torch_stream()
-        check(self._lib.magic_sht_get_td(self._h, n, r_arr.ctypes.data, None if lc is None else lc.ctypes.data,
-                                         float(cor_fac), None if ep is None else ep.ctypes.data, ctypes.byref(a)))
+        check(self._lib.magic_sht_get_td_nbc(self._h, n, r_arr.ctypes.data, None if lc is None else lc.ctypes.data,
+                                             float(cor_fac), None if ep is None else ep.ctypes.data,
+                                             None if bc is None else bc.ctypes.data, ctypes.byref(a)))
         return outs
 
     def courant(self, grids: dict, radial: dict, courfac: float, alffac: float, LFfac: float = 1.0,

@@ -455,7 +455,7 @@ def dt_courant(dtrkc, dthkc, dt: float, dtMax: float):
     return False, dt
 
 
-def get_td(spec: dict, r, cor_fac: float, l_max: int, minc: int = 1, lcut=None, epsc=None) -> dict:
+def get_td(spec: dict, r, cor_fac: float, l_max: int, minc: int = 1, lcut=None, epsc=None, nbc=None) -> dict:
     """Spectral assembly of the explicit time derivatives at interior levels
     (get_td.f90: get_dwdt :133-208, get_dpdt :311-379, get_dzdt :381-457,
     get_dsdt :459-521, get_dbdt :558-619), Boussinesq, Coriolis on, no
@@ -488,6 +488,13 @@ def get_td(spec: dict, r, cor_fac: float, l_max: int, minc: int = 1, lcut=None, 
            ("dwdt", "dzdt", "dpdt", "dsdt", "dbdt", "djdt", "dVxBhLM")}
     for ir in range(n):
         rr = float(np.asarray(r)[ir])
+        if nbc is not None and int(np.asarray(nbc)[ir]) != 0:
+            # boundary level: get_dbdt's dVxBhLM only (get_td.f90:598-612); the
+            # reference leaves the other outputs unset (NaN here)
+            out["dVxBhLM"][ir] = -dLh * np.asarray(spec["VxBtLM"])[ir] * rr * rr
+            for k in ("dwdt", "dzdt", "dpdt", "dsdt", "dbdt", "djdt"):
+                out[k][ir] = np.nan
+            continue
         or1, or2 = 1.0 / rr, 1.0 / rr ** 2
         or4 = or2 * or2
         lR = l_max if lcut is None else min(int(np.asarray(lcut)[ir]), l_max)

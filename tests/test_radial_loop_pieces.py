@@ -128,3 +128,96 @@ def test_br_v_bcs_and_b_nl_bcs_match_oracle(built, torch, grid):
     assert np.array_equal(aj, orc.get_b_nl_bcs(2.5, got[1]))
     b2, aj2 = s.get_b_nl_bcs("ICB", 0.7, got[0], got[1])
     assert b2 is None and np.array_equal(aj2, orc.get_b_nl_bcs(0.7, got[1]))
+
+
+@pytest.mark.gpu
+def test_get_td_boundary_levels(built, torch):
+    """get_td with boundary flags (nBc of rIter.f90): at flagged levels only
+    dVxBhLM is written (get_td.f90:598-612), the other outputs keep the
+    caller's values; interior levels match the oracle as before."""
+    from oracle import oracle as orc
+    from magic_gb300 import _lib
+    from conftest import rel_l2
+    L, minc, N, P = 63, 1, 96, 192
+    s = make(L, minc, N, P)
+    n = 4
+    rng = np.random.default_rng(10)
+    spec = {k: torch.from_numpy(rng.standard_normal((n, s.lm_max)) + 1j * rng.standard_normal((n, s.lm_max))).cuda()
+            for k in _lib.TD_IN}
+    r = np.array([1.5, 1.2, 0.9, 0.6])
+    nbc = np.array([1, 0, 0, 2], dtype=np.int32)
+    sentinel = 7.0 + 3.0j
+    out = {k: torch.full((n, s.lm_max), sentinel, dtype=torch.complex128, device="cuda") for k in _lib.TD_OUT}
+    s.get_td(spec, r, cor_fac=1.0e2, out=out, nbc=nbc)
+    torch.cuda.synchronize()
+    ref = orc.get_td({k: v.cpu().numpy() for k, v in spec.items()}, r, 1.0e2, L, minc, nbc=nbc)
+    for k in _lib.TD_OUT:
+        got = out[k].cpu().numpy()
+        for i in range(n):
+            if nbc[i] != 0 and k != "dVxBhLM":
+                assert np.all(got[i] == sentinel), (k, i)
+            else:
+                assert rel_l2(got[i], ref[k][i]) < 1e-13, (k, i)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg", [
+    dict(ktopv=2, kbotv=2, omega_ma=0.3, omega_ic=-0.2),                    # rigid, lMagNlBc off
+    dict(ktopv=1, kbotv=1, l_cond_ma=True, omega_ma=0.25),                  # stress-free, conducting mantle
+])
+def test_radial_loop_stage_matches_oracle(built, torch, oracle_mod, cfg):
+    """One explicit stage of the radial loop (rIter.f90:94-464) over five
+    levels with both boundaries, FP64 form, against the same stage composed
+    from the oracle's transforms and restatements."""
+    from test_gpu_parity import _radial_set_ref, close
+    from magic_gb300.radial_loop import RadialLoop
+    from magic_gb300.workload import grid_space_inputs
+    from conftest import rel_l2
+    orc = oracle_mod
+    L, minc, N, P, n = 63, 1, 96, 192, 5
+    s = make(L, minc, N, P)
+    o = orc.OracleSHT(L, minc, N, P)
+    r = np.linspace(1.538, 0.538, n)                         # outer boundary first
+    lcut = np.array([L, L, L - 5, L, L], dtype=np.int32)
+    epsc = np.array([0.0, 0.3, 0.1, -0.2, 0.0])
+    spec_np = grid_space_inputs(L, minc, n, seed=8)
+    loop = RadialLoop(s, r, cor_fac=50.0, courfac=2.5, alffac=1.0, lcut=lcut, epsc=epsc, **cfg)
+    got = loop.step({k: torch.from_numpy(v).cuda() for k, v in spec_np.items()})
+    torch.cuda.synchronize()
+    # ---- the same stage from the oracle
+    or2 = 1.0 / r ** 2
+    g = _radial_set_ref(o, spec_np, or2, lcut)
+    for i, kind, om, kv in ((0, cfg["ktopv"], cfg.get("omega_ma", 0.0), False),
+                            (n - 1, cfg["kbotv"], cfg.get("omega_ic", 0.0), False)):
+        if kind == 1:
+            g["vrc"][i] = 0.0
+        else:
+            b = orc.v_rigid_boundary(N, P, r[i] ** 2, om, kv, g["vrc"][i])
+            g["vrc"][i], g["vtc"][i], g["vpc"][i] = b["vr"], b["vt"], b["vp"]
+    lo, hi = (0, n) if loop.lMagNlBc else (1, n - 1)
+    nl = orc.get_nl({k: v[lo:hi] for k, v in g.items()}, or2[lo:hi], N)
+    lm = {k: np.zeros((n, s.lm_max), dtype=np.complex128) for k in
+          ("AdvrLM", "AdvtLM", "AdvpLM", "VSrLM", "VStLM", "VSpLM", "VxBrLM", "VxBtLM", "VxBpLM")}
+    for j, i in enumerate(range(lo, hi)):
+        for pre in ("Adv", "VS", "VxB"):
+            q, ss, t = o.spat_to_qst(nl[pre + "r"][j], nl[pre + "t"][j], nl[pre + "p"][j], int(lcut[i]))
+            lm[pre + "rLM"][i], lm[pre + "tLM"][i], lm[pre + "pLM"][i] = q, ss, t
+    lm["VSrLM"][0] = 0.0
+    lm["VSrLM"][n - 1] = 0.0
+    td_in = {k: spec_np[k] for k in ("w", "dw", "z")}
+    td_in.update({k: lm[k] for k in ("AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "VxBrLM", "VxBtLM", "VxBpLM")})
+    td = orc.get_td(td_in, r, 50.0, L, minc, lcut, epsc, nbc=loop.nbc)
+    for k in ("dwdt", "dzdt", "dpdt", "dsdt", "dbdt", "djdt", "dVxBhLM"):
+        gk = got[k].cpu().numpy()
+        for i in range(n):
+            if loop.nbc[i] != 0 and k != "dVxBhLM":
+                continue
+            assert rel_l2(gk[i], td[k][i]) < 1e-10, (k, i, rel_l2(gk[i], td[k][i]))
+    close(got["VSrLM"].cpu().numpy(), lm["VSrLM"], tol=1e-10)
+    dtr, dth = orc.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, loop.radial, N, 2.5, 1.0)
+    np.testing.assert_allclose(got["dtrkc"], dtr, rtol=1e-10)
+    np.testing.assert_allclose(got["dthkc"], dth, rtol=1e-10)
+    if loop.l_b_nl_cmb:
+        exp = orc.get_br_v_bcs(o, g["brc"][0], g["vtc"][0], g["vpc"][0], cfg["omega_ma"], or2[0], 1.0)
+        close(got["br_vt_lm_cmb"].cpu().numpy(), exp[0], tol=1e-10)
+        close(got["br_vp_lm_cmb"].cpu().numpy(), exp[1], tol=1e-10)
