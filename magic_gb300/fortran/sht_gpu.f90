@@ -150,6 +150,7 @@ module sht
       end function
    end interface
 
+   public :: sht_handle, sht_check
    public :: initialize_sht, scal_to_spat, scal_to_grad_spat, pol_to_grad_spat, &
    &         torpol_to_spat, pol_to_curlr_spat, torpol_to_curl_spat,            &
    &         torpol_to_dphspat, scal_to_SH, spat_to_sphertor,                   &
@@ -173,6 +174,16 @@ contains
          call abortRun('magic_sht: '//trim(text))
       end if
    end subroutine check
+
+   type(c_ptr) function sht_handle()
+      ! the library handle, for the radial-loop pieces (module sht_gpu_radial)
+      sht_handle = handle
+   end function sht_handle
+
+   subroutine sht_check(rc)
+      integer(c_int), intent(in) :: rc
+      call check(rc)
+   end subroutine sht_check
 
    subroutine initialize_sht(l_scrambled_theta)
       logical, intent(out) :: l_scrambled_theta
