@@ -57,14 +57,16 @@ __device__ __forceinline__ float d2f_int(double x) {
   return __uint_as_float(f);
 }
 // exact widening (normal numbers, zero, Inf and NaN; FP32 subnormals flush to zero)
+// on 32-bit halves: the magnitude shifted right by 3 puts the exponent and the
+// top 20 mantissa bits in place, + (1023 - 127) << 20 rebiases the exponent
 __device__ __forceinline__ double f2d_int(float x) {
   const unsigned int u = __float_as_uint(x);
-  const unsigned int e = (u >> 23) & 0xFFu;
-  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
-  if (e == 0) return __longlong_as_double((long long)sign);
-  const unsigned long long ed = e == 0xFFu ? 0x7FFull : (unsigned long long)(e - 127 + 1023);
-  const unsigned long long bits = sign | (ed << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)bits);
+  const unsigned int a = u & 0x7FFFFFFFu;
+  unsigned int hi = (a >> 3) + 0x38000000u;
+  unsigned int lo = u << 29;
+  if (a >= 0x7F800000u) hi |= 0x7FF00000u;  // Inf, NaN (payload kept)
+  if (a < 0x00800000u) hi = lo = 0u;        // zero, subnormals
+  return __hiloint2double((int)(hi | (u & 0x80000000u)), (int)lo);
 }
 
 // Conversions between a transform's working type T and the FP64 of the

@@ -42,10 +42,12 @@ namespace {
 
 constexpr int kNC = 64;  // real data columns per tile (32 complex)
 
-// ring depths: A = one table split of one K tile (NT x 16 KB per slot), B = data tiles
+// ring depths: A = one table split of one K tile (NT x 16 KB per slot), B = data tiles.
+// The A ring is as deep as shared memory allows with the TF32 data tiles
+// (32 KB): the MMA thread mostly waits for table tiles, which come from L2.
 template <bool VEC, bool INV>
 struct Rings {
-  static constexpr int NA = VEC ? 3 : 4;
+  static constexpr int NA = VEC ? (INV ? 4 : 3) : 6;
   static constexpr int NB = VEC ? 2 : 3;
 };
 
