@@ -101,9 +101,10 @@ __device__ __forceinline__ void reg_stage(T2 (&a)[S], const T2* __restrict__ tw,
   for (int i = 0; i < S; ++i) a[i] = b[i];
 }
 
+// root[e] = e^{+2 pi i e / S}
 template <typename T2, int S>
-__device__ __forceinline__ void reg_fft(T2 (&a)[S], const T2* __restrict__ tw, int P, int s) {
-  const int ps = P / S;
+__device__ __forceinline__ void reg_fft(T2 (&a)[S], const T2* __restrict__ tw, int s) {
+  constexpr int ps = 1;
   if constexpr (S == 2) { reg_stage<T2, S, 2, 1>(a, tw, ps, s); }
   else if constexpr (S == 3) { reg_stage<T2, S, 3, 1>(a, tw, ps, s); }
   else if constexpr (S == 4) { reg_stage<T2, S, 4, 1>(a, tw, ps, s); }
@@ -127,8 +128,39 @@ __device__ __forceinline__ void reg_fft(T2 (&a)[S], const T2* __restrict__ tw, i
 // warp, which keeps the shared-memory write-back free of bank conflicts.
 __device__ __forceinline__ int brev5(int x) { return __brev(x) >> 27; }
 
+// Twiddle tables of the fast path in shared memory, laid out so that every
+// warp-wide read is either 32 consecutive entries (one per lane) or one entry
+// for all lanes (P = 2n = 64 S):
+//   lanew[st][l] = e^{+2 pi i (l mod d) / (2d)}, d = 16 >> st  (cross-lane stages, st < 4)
+//   post[q][l]   = e^{+2 pi i q brev5(l) / n}                   (four-step twiddles, q < S)
+//   root[e]      = e^{+2 pi i e / S}                            (register DFT, e < S)
+//   lo[q]        = e^{+2 pi i q / P},  hi[j] = e^{+2 pi i j KS / P}  (real <-> half-length
+//   complex twiddle e^{2 pi i k / P} as a per-thread factor times one of these)
+template <int S>
+struct TwTab {
+  static constexpr int kLane = 0, kPost = 128, kRoot = 128 + 32 * S, kLo = kRoot + S, kHi = kLo + S;
+  static constexpr int size = kHi + S + 1;
+  // index into the table e^{+2 pi i k / P} (k < P) of entry i; KS = order stride of the forward epilogue
+  static __device__ __forceinline__ int src(int i, int KS) {
+    constexpr int P = 64 * S;
+    if (i < kPost) {
+      const int st = i >> 5, l = i & 31, d = 16 >> st;
+      return (l & (d - 1)) * (P / (2 * d));
+    }
+    if (i < kRoot) {
+      const int q = (i - kPost) >> 5, l = (i - kPost) & 31;
+      return (2 * q * brev5(l)) % P;  // e^{2 pi i q k1 / n} = e^{2 pi i 2 q k1 / P}
+    }
+    if (i < kLo) return (i - kRoot) * (P / S);
+    if (i < kHi) return i - kLo;
+    const int j = i - kHi;
+    return KS * j < P ? KS * j : 0;  // entries past P are never read
+  }
+};
+
 template <typename T2, int S>
-__device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tw, int P, int s) {
+__device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tab, int s) {
+  typedef TwTab<S> TT;
   const int lane = threadIdx.x & 31;
   typedef typename ScalarOf<T2>::t T;
 #pragma unroll
@@ -139,7 +171,8 @@ __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tw, 
     const T sg = up ? (T)-1 : (T)1;
     T2 w;
     if (d > 1) {
-      w = twid(tw, (lane & (d - 1)) * (P / (2 * d)), s);
+      const int st = d == 16 ? 0 : d == 8 ? 1 : d == 4 ? 2 : 3;
+      w = twid(tab + TT::kLane, st * 32 + lane, s);
       if (!up) { w.x = (T)1; w.y = (T)0; }
     }
 #pragma unroll
@@ -151,12 +184,9 @@ __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tw, 
       a[q] = d > 1 ? cmul(t, w) : t;
     }
   }
-  const int k1 = brev5(lane);
 #pragma unroll
-  for (int q = 1; q < S; ++q) {
-    if (k1) a[q] = cmul(a[q], twid(tw, 2 * q * k1, s));  // omega_n^{q k1}; 2 q k1 < P
-  }
-  reg_fft<T2, S>(a, tw, P, s);
+  for (int q = 1; q < S; ++q) a[q] = cmul(a[q], twid(tab + TT::kPost, q * 32 + lane, s));  // omega_n^{q k1}
+  reg_fft<T2, S>(a, tab + TT::kRoot, s);
 }
 
 // Shared-memory row layouts of the fast path (row pitch KP = 33 S + 1, odd):
@@ -179,12 +209,12 @@ template <typename T2, int S, int RT, int NB>
 __device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict__ in, bool in_parity,
                                           bool has_f, long long per_p, const T2* __restrict__ twg, T2* sm, T2* stw,
                                           int rp, int kq, int rowg, bool row_ok) {
-  constexpr int n = 32 * S, KP = 33 * S + 1, KS = 256 / (RT / 2), NTW = (2 * n + 255) / 256;
+  constexpr int KP = 33 * S + 1, KS = 256 / (RT / 2), NT = TwTab<S>::size, NTW = (NT + 255) / 256;
   const int n_m = g.n_m;
   T2 twr[NTW];
 #pragma unroll
   for (int i = 0; i < NTW; ++i)
-    if (threadIdx.x + 256 * i < 2 * n) twr[i] = twg[threadIdx.x + 256 * i];
+    if (threadIdx.x + 256 * i < NT) twr[i] = twg[TwTab<S>::src(threadIdx.x + 256 * i, KS)];
   for (int kb = 0; kb < n_m; kb += KS * NB) {
     T2 x[NB][4];
 #pragma unroll
@@ -211,7 +241,7 @@ __device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict
     if (kb == 0) {  // n_m >= 1: the first batch always runs
 #pragma unroll
       for (int i = 0; i < NTW; ++i)
-        if (threadIdx.x + 256 * i < 2 * n) stw[threadIdx.x + 256 * i] = twr[i];
+        if (threadIdx.x + 256 * i < NT) stw[threadIdx.x + 256 * i] = twr[i];
     }
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
@@ -243,8 +273,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
   const T2* __restrict__ twg = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
-  T2* stw = sm + RT * KP;  // twiddle table e^{+2 pi i k / P}, k < P, copied to shared memory
-  const T2* tw = stw;
+  T2* stw = sm + RT * KP;  // twiddle tables (TwTab)
   const T2* __restrict__ in = (const T2*)fd.in + (long long)r * fd.in_ld;
   const int n_m = g.n_m;
   const bool in_parity = (fd.flags & (FFT_IN_E | FFT_IN_EF)) != 0;
@@ -259,6 +288,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   inv_stage<T2, S, RT, sizeof(T) == 4 ? 4 : 2>(g, in, in_parity, has_f, per_p, twg, sm, stw, rp, kq, rowg, row_ok);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const T2 base = twg[S * lane];  // e^{2 pi i S lane / P}: times lo[q] gives e^{2 pi i k / P}, k = S lane + q
   for (int rr = warp; rr < RT; rr += 8) {
     T2* row = sm + rr * KP;
     T2 a[S];
@@ -273,12 +303,12 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
       if (kn < n_m) cn = row[q == 0 ? 32 - lane : 33 * (S - q) + 31 - lane];
       if (k == 0) { ck.y = 0; cn.y = 0; }
       const T2 E = cadd(ck, cconj(cn));
-      const T2 O = cmul(csub(ck, cconj(cn)), tw[k]);
+      const T2 O = cmul(csub(ck, cconj(cn)), q == 0 ? base : cmul(base, stw[TwTab<S>::kLo + q]));
       a[q].x = E.x - O.y;
       a[q].y = E.y + O.x;
     }
     __syncwarp();
-    warp_fft<T2, S>(a, tw, g.n_phi, +1);
+    warp_fft<T2, S>(a, stw, +1);
     const int k1 = brev5(lane);
 #pragma unroll
     for (int k2 = 0; k2 < S; ++k2) row[pos(k1 + 32 * k2)] = a[k2];  // z_j = x_{2j} + i x_{2j+1}
@@ -318,13 +348,12 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
   const T2* __restrict__ twg = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
-  T2* stw = sm + RT * KP;  // twiddle table e^{+2 pi i k / P}, k < P, copied to shared memory
-  const T2* tw = stw;
+  T2* stw = sm + RT * KP;  // twiddle tables (TwTab)
   const double* __restrict__ in = (const double*)fd.in + (long long)r * fd.in_ld;
   // Each thread owns the row pair (rp, rp + 1) and the indices kk = kq + KS j
   // (phi = 2kk, 2kk + 1); the loads of a batch of NB indices, and of the
-  // twiddle table, are all issued before the first shared-memory store.
-  constexpr int RT2 = RT / 2, KS = 256 / RT2, NB = 4, NTW = (2 * n + 255) / 256;
+  // twiddle tables, are all issued before the first shared-memory store.
+  constexpr int RT2 = RT / 2, KS = 256 / RT2, NB = 4, NT = TwTab<S>::size, NTW = (NT + 255) / 256;
   const int rp = 2 * (threadIdx.x % RT2), kq = threadIdx.x / RT2;
   const int rowg = row0 + rp;
   const bool row_ok = rowg < g.n_theta;
@@ -332,7 +361,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   T2 twr[NTW];
 #pragma unroll
   for (int i = 0; i < NTW; ++i)
-    if (threadIdx.x + 256 * i < 2 * n) twr[i] = twg[threadIdx.x + 256 * i];
+    if (threadIdx.x + 256 * i < NT) twr[i] = twg[TwTab<S>::src(threadIdx.x + 256 * i, KS)];
   for (int kb = 0; kb < n; kb += KS * NB) {
     double2 u[NB], w[NB];  // (row rp | rp+1) at phi 2kk (u) and 2kk+1 (w)
 #pragma unroll
@@ -353,7 +382,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
     if (kb == 0) {
 #pragma unroll
       for (int i = 0; i < NTW; ++i)
-        if (threadIdx.x + 256 * i < 2 * n) stw[threadIdx.x + 256 * i] = twr[i];
+        if (threadIdx.x + 256 * i < NT) stw[threadIdx.x + 256 * i] = twr[i];
     }
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
@@ -375,7 +404,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
 #pragma unroll
     for (int q = 0; q < S; ++q) a[q] = row[q * 33 + lane];  // = z[S*lane + q]
     __syncwarp();
-    warp_fft<T2, S>(a, tw, g.n_phi, -1);
+    warp_fft<T2, S>(a, stw, -1);
     const int k1 = brev5(lane);
 #pragma unroll
     for (int k2 = 0; k2 < S; ++k2) row[pos(k1 + 32 * k2)] = a[k2];
@@ -391,7 +420,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   Tt fac = (Tt)(1.0 / (double)g.n_phi);
   if (fd.flags & FFT_OSIN2) fac *= from_f64<Tt>(g.osin2[jg]);
   if (fd.flags & FFT_WEIGHT) fac *= from_f64<Tt>(g.wgt[jg]);
-  for (int k = kq; k < g.n_m; k += KS) {
+  const T2 base = twg[kq];  // e^{2 pi i kq / P}: times hi[j] gives e^{2 pi i k / P}, k = kq + KS j
+  for (int k = kq, j = 0; k < g.n_m; k += KS, ++j) {
+    const T2 tk = j == 0 ? base : cmul(base, stw[TwTab<S>::kHi + j]);
     T2 c[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -399,7 +430,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
       const T2 Zk = row[pos(k)];
       const T2 Zn = cconj(row[pos(k == 0 ? 0 : n - k)]);
       const T2 D = csub(Zk, Zn);
-      const T2 u = cmul(cconj(tw[k]), D);
+      const T2 u = cmul(cconj(tk), D);
       T2 X;
       X.x = (Tt)0.5 * (Zk.x + Zn.x + u.y);
       X.y = (Tt)0.5 * (Zk.y + Zn.y - u.x);
@@ -627,11 +658,10 @@ bool factorize(int n, Radices& rad) {
 template <typename T, int S>
 cudaError_t launch_fast(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
   typedef typename V2<T>::t T2;
-  constexpr int n = 32 * S;
   // 16 rows per CTA; 8 rows where 16 would leave one CTA per SM
   constexpr int KP = 33 * S + 1;
   constexpr int RT = (sizeof(T2) * 16 * KP > 100 * 1024) ? 8 : 16;
-  const size_t smem = ((size_t)RT * KP + 2 * n) * sizeof(T2);
+  const size_t smem = ((size_t)RT * KP + TwTab<S>::size) * sizeof(T2);
   dim3 grid((g.n_theta + RT - 1) / RT, s.nf * s.nlev);
   if (inverse) {
     auto k = fft_inv_fast<T, S, RT>;
