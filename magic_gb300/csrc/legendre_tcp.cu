@@ -42,13 +42,24 @@ namespace {
 
 constexpr int kNC = 64;  // real data columns per tile (32 complex)
 
-// ring depths: A = one table split of one K tile (NT x 16 KB per slot), B = data tiles.
-// The A ring is as deep as shared memory allows with the TF32 data tiles
-// (32 KB): the MMA thread mostly waits for table tiles, which come from L2.
-template <bool VEC, bool INV>
+// CTAs per SM: the scalar kernels (one table, 192 accumulator columns) run two
+// CTAs per SM with 256 TMEM columns each, so that one CTA's MMA thread issues
+// while the other's waits for its operands or commits; the vector kernels (two
+// tables, 384 accumulator columns) need all 512 columns and run one.
+template <bool VEC>
+struct Occ {
+  static constexpr int CPS = VEC ? 1 : 2;
+  static constexpr int TCOLS = 512 / CPS;
+};
+
+// ring depths: A = one table split of one K tile (NT x 16 KB per slot), B = data
+// tiles (24 KB, 32 KB with TF32).  Two scalar CTAs share an SM's shared memory,
+// so their rings are shallower; a vector CTA's A ring is as deep as shared
+// memory allows with the TF32 data tiles.
+template <bool VEC, bool INV, bool TF32>
 struct Rings {
-  static constexpr int NA = VEC ? (INV ? 4 : 3) : 6;
-  static constexpr int NB = VEC ? 2 : 3;
+  static constexpr int NA = VEC ? (INV ? 4 : 3) : (TF32 ? 2 : 3);
+  static constexpr int NB = 2;
 };
 
 // Split format of the tensor-core form.  TF32 = false: 3 bf16 splits, one K
@@ -262,15 +273,15 @@ struct InvTile {
 };
 
 template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, const InvSet s, const TcTables t,
+__global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_tcp(const ShtGeom g, const InvSet s, const TcTables t,
                                                            const unsigned char* __restrict__ bimg, int nct) {
   typedef Form<TF32> F;
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NC = kNC;
-  constexpr int NA = Rings<VEC, true>::NA;
-  constexpr int NB = Rings<VEC, true>::NB;
+  constexpr int NA = Rings<VEC, true, TF32>::NA;
+  constexpr int NB = Rings<VEC, true, TF32>::NB;
   constexpr uint32_t ACC = NT * F::NACCS * NC;  // one accumulator set
-  constexpr int NACC = 2 * ACC <= 512 ? 2 : 1;  // sets in the 512 TMEM columns
+  constexpr int NACC = 2 * ACC <= Occ<VEC>::TCOLS ? 2 : 1;  // sets in the CTA's TMEM columns
   constexpr int BSZ = F::OPSZ;
   constexpr int ASZ = NT * 16384;
   extern __shared__ unsigned char smem_raw[];
@@ -297,7 +308,7 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(&tmem_base, 512);
+    tc::tmem_alloc(&tmem_base, Occ<VEC>::TCOLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
@@ -467,7 +478,7 @@ __global__ void __launch_bounds__(kThreads, 1) inv_leg_tcp(const ShtGeom g, cons
   tc::tc_fence_before();
   __syncthreads();
   if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
-  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC>::TCOLS);
 }
 
 // ------------------------------------------------------------ analysis
@@ -486,15 +497,15 @@ struct FwdTile {
 };
 
 template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, const FwdSet s, const TcTables t,
+__global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_tcp(const ShtGeom g, const FwdSet s, const TcTables t,
                                                            const unsigned char* __restrict__ bimg, int nct) {
   typedef Form<TF32> F;
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NC = kNC;
-  constexpr int NA = Rings<VEC, false>::NA;
-  constexpr int NB = Rings<VEC, false>::NB;
+  constexpr int NA = Rings<VEC, false, TF32>::NA;
+  constexpr int NB = Rings<VEC, false, TF32>::NB;
   constexpr uint32_t ACC = NT * F::NACCS * NC;
-  constexpr int NACC = 2 * ACC <= 512 ? 2 : 1;
+  constexpr int NACC = 2 * ACC <= Occ<VEC>::TCOLS ? 2 : 1;
   constexpr int TS = F::OPSZ;       // one data operand
   constexpr int ASZ = NT * 16384;
   constexpr int BSZ = NT * TS;      // mine (and other)
@@ -522,7 +533,7 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(&tmem_base, 512);
+    tc::tmem_alloc(&tmem_base, Occ<VEC>::TCOLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
@@ -680,7 +691,7 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_leg_tcp(const ShtGeom g, cons
   tc::tc_fence_before();
   __syncthreads();
   if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
-  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC>::TCOLS);
 }
 
 int num_sms() {
@@ -697,7 +708,7 @@ int num_sms() {
 template <bool VEC, bool TF32>
 cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, unsigned char* bimg,
                          cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, true>::NA, NB = Rings<VEC, true>::NB;
+  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, true, TF32>::NA, NB = Rings<VEC, true, TF32>::NB;
   constexpr size_t OPSZ = Form<TF32>::OPSZ;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
@@ -709,7 +720,7 @@ cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, u
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * OPSZ;
   CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
-  const int grid = (int)std::min<long long>(ntiles, num_sms());
+  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms() * Occ<VEC>::CPS);
   CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
   inv_leg_tcp<VEC, TF32><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
   return cudaGetLastError();
@@ -718,7 +729,7 @@ cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, u
 template <bool VEC, bool TF32>
 cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, unsigned char* bimg,
                          cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, false>::NA, NB = Rings<VEC, false>::NB;
+  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, false, TF32>::NA, NB = Rings<VEC, false, TF32>::NB;
   constexpr size_t OPSZ = Form<TF32>::OPSZ;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   if (ncplx <= 0) return cudaSuccess;
@@ -730,7 +741,7 @@ cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, u
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * OPSZ;
   CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
-  const int grid = (int)std::min<long long>(ntiles, num_sms());
+  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms() * Occ<VEC>::CPS);
   CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
   fwd_leg_tcp<VEC, TF32><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
   return cudaGetLastError();
