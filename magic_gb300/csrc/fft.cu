@@ -259,11 +259,13 @@ __device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict
 }
 
 // One CTA = RT consecutive theta rows of one (level, field) column; 8 warps,
-// each owning RT/8 rows in turn.  Shared memory holds the RT rows with an
+// each owning RT/8 rows in turn.  FP32: three CTAs per SM (80 registers per
+// thread); four CTAs at 64 registers measured 14% slower (inverse) and 3%
+// (forward).  Shared memory holds the RT rows with an
 // odd pitch KP = 33 S + 1 and the layouts pin() / pos(), so that row-parallel
 // and index-parallel accesses both spread over the banks.
 template <typename T, int S, int RT>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1)) fft_inv_fast(const ShtGeom g, const FftSet s) {
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1)) fft_inv_fast(const ShtGeom g, const FftSet s) {
   typedef typename V2<T>::t T2;
   constexpr int n = 32 * S, KP = 33 * S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -343,7 +345,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
 }
 
 template <typename T, int S, int RT>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1)) fft_fwd_fast(const ShtGeom g, const FftSet s) {
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1)) fft_fwd_fast(const ShtGeom g, const FftSet s) {
   typedef typename V2<T>::t T2;
   constexpr int n = 32 * S, KP = 33 * S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -358,7 +360,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 4) : 1))
   // Each thread owns the row pair (rp, rp + 1) and the indices kk = kq + KS j
   // (phi = 2kk, 2kk + 1); the loads of a batch of NB indices, and of the
   // twiddle tables, are all issued before the first shared-memory store.
-  constexpr int RT2 = RT / 2, KS = 256 / RT2, NB = 4, NT = TwTab<S>::size, NTW = (NT + 255) / 256;
+  constexpr int RT2 = RT / 2, KS = 256 / RT2, NB = 6, NT = TwTab<S>::size, NTW = (NT + 255) / 256;
   const int rp = 2 * (threadIdx.x % RT2), kq = threadIdx.x / RT2;
   const int rowg = row0 + rp;
   const bool row_ok = rowg < g.n_theta;
