@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kPackThreads, 4) pack_inv_kernel(const ShtGeom
 // Analysis data images: [m][c][ct] pairs (ES tile, EA tile) of 3 splits each,
 // both built by one CTA from the (ES, EA) entries of 64 colatitudes.
 template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_kernel(const ShtGeom g, const FwdSet s,
+__global__ void __launch_bounds__(kPackThreads, 4) pack_fwd_kernel(const ShtGeom g, const FwdSet s,
                                                                   const TcTables t,
                                                                   unsigned char* __restrict__ bimg, int nct) {
   constexpr int NC = kNC;
