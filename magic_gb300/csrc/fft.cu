@@ -8,10 +8,11 @@
 // A real FFT of length P runs as a complex FFT of length n = P/2 plus the
 // usual even/odd pre/post-processing.  Fast path (n = 32*S, S in
 // {1,2,3,4,5,6,8,10,12,16,20,24}): each warp owns one theta row; lane l holds
-// z[32q+l]; a length-S FFT runs in registers, then a twiddle, then a 32-point
-// radix-2 DIF network across lanes with warp shuffles.  Rows are staged
-// through shared memory so that global loads/stores stay coalesced along
-// theta.  Other sizes use a per-warp shared-memory Stockham FFT.
+// z[S*l + q], q < S; a 32-point radix-2 DIF network runs across the lanes with
+// warp shuffles, then the four-step twiddle, then a length-S FFT in registers
+// (warp_fft).  Rows are staged through shared memory so that global loads and
+// stores stay coalesced along theta.  Other sizes use a per-warp
+// shared-memory Stockham FFT.
 //
 // Forward epilogue (fused): 1/sin^2 theta (spat_to_sph_tor,
 // src/shtransforms.f90:789-794), the Gauss weight 2 pi w_j, and the
