@@ -46,10 +46,17 @@ constexpr int kNC = 64;  // real data columns per tile (32 complex)
 // CTAs per SM with 256 TMEM columns each, so that one CTA's MMA thread issues
 // while the other's waits for its operands or commits; the vector kernels (two
 // tables, 384 accumulator columns) need all 512 columns and run one.
-template <bool VEC>
+// The TF32 vector kernels (twice the MMA instructions of 3xBF16 per chunk) have
+// two MMA threads (warp 1 and warp 10), one per table (P and dP): each waits for
+// the same operands and issues the MMAs of its own table, so one thread's
+// waits, fences and commits overlap the other's MMAs (7% faster there; the
+// 3xBF16 synthesis measured 4% slower with two, so it keeps one).
+template <bool VEC, bool TF32>
 struct Occ {
   static constexpr int CPS = VEC ? 1 : 2;
   static constexpr int TCOLS = 512 / CPS;
+  static constexpr int NISS = (VEC && TF32) ? 2 : 1;  // MMA threads
+  static constexpr int XTRA = NISS == 2 ? 32 : 0;      // threads beyond kThreads (the second MMA warp)
 };
 
 // ring depths: A = one table split of one K tile (NT x 16 KB per slot), B = data
@@ -125,15 +132,16 @@ __device__ __forceinline__ bool ring_pop(const TileRing& R, uint32_t& use, int& 
   return true;
 }
 
-// Issue the MMAs of A-ring use `u` of a chunk (NT tables) against the stacked
-// data splits; D holds NT accumulator groups of NACCS*kNC columns.
+// Issue the MMAs of A-ring use `u` of a chunk (tables tb0 <= tb < tb1 of NT)
+// against the stacked data splits; D holds NT accumulator groups of
+// NACCS*kNC columns.
 //  bf16 (u = split):  A_hi x [B_hi|B_mid|B_lo] -> [C0|C1|C2],  A_mid x [B_hi|B_mid]
 //                     -> [C1|C2],  A_lo x B_hi -> C2   (K = 16 per MMA, 4 per tile)
 //  tf32 (u = 2*K tile + split):  A_hi x [B_hi|B_lo] -> [C0|C1],  A_lo x B_hi -> C1
 //                     (K = 8 per MMA, 4 per 32-wide K tile)
 template <int NT, bool TF32>
 __device__ __forceinline__ void issue_use(uint32_t acc, const unsigned char* A, const unsigned char* B,
-                                          int u, bool first_chunk, uint32_t bstride_tb) {
+                                          int u, bool first_chunk, uint32_t bstride_tb, int tb0, int tb1) {
   constexpr int NACCS = Form<TF32>::NACCS;
   const uint64_t a0 = tc::sw128_desc(tc::smem_u32(A));
   const uint64_t bd0 = tc::sw128_desc(tc::smem_u32(B));
@@ -144,6 +152,7 @@ __device__ __forceinline__ void issue_use(uint32_t acc, const unsigned char* A, 
     for (int ks = 0; ks < 4; ++ks)
 #pragma unroll
       for (int tb = 0; tb < NT; ++tb) {
+        if (tb < tb0 || tb >= tb1) continue;  // tables of the other MMA thread
         const uint32_t d = acc + (uint32_t)(tb * NACCS * kNC);
         const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
         const uint64_t bd = bd0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
@@ -158,6 +167,7 @@ __device__ __forceinline__ void issue_use(uint32_t acc, const unsigned char* A, 
     for (int ks = 0; ks < 4; ++ks)
 #pragma unroll
       for (int tb = 0; tb < NT; ++tb) {
+        if (tb < tb0 || tb >= tb1) continue;  // tables of the other MMA thread
         const uint32_t d = acc + (uint32_t)(tb * NACCS * kNC);
         const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
         const uint64_t bd = bd0 + (uint64_t)((tb * bstride_tb + kt * 2 * kNC * 128 + ks * 32) >> 4);
@@ -273,7 +283,7 @@ struct InvTile {
 };
 
 template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_tcp(const ShtGeom g, const InvSet s, const TcTables t,
+__global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32>::CPS) inv_leg_tcp(const ShtGeom g, const InvSet s, const TcTables t,
                                                            const unsigned char* __restrict__ bimg, int nct) {
   typedef Form<TF32> F;
   constexpr int NT = VEC ? 2 : 1;
@@ -281,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_tcp(const Sht
   constexpr int NA = Rings<VEC, true, TF32>::NA;
   constexpr int NB = Rings<VEC, true, TF32>::NB;
   constexpr uint32_t ACC = NT * F::NACCS * NC;  // one accumulator set
-  constexpr int NACC = 2 * ACC <= Occ<VEC>::TCOLS ? 2 : 1;  // sets in the CTA's TMEM columns
+  constexpr int NACC = 2 * ACC <= Occ<VEC, TF32>::TCOLS ? 2 : 1;  // sets in the CTA's TMEM columns
   constexpr int BSZ = F::OPSZ;
   constexpr int ASZ = NT * 16384;
   extern __shared__ unsigned char smem_raw[];
@@ -299,16 +309,17 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_tcp(const Sht
   const int ntiles = nct * t.ntt * 2 * g.n_m;
 
   if (tid == 0) {
-    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], 1); }
-    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
-    for (int i = 0; i < NACC; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
-    tc::mbar_init(&fin, 1);
-    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], 1 + kEpiThreads); }
+    constexpr int NI = Occ<VEC, TF32>::NISS;
+    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], NI); }
+    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], NI); }
+    for (int i = 0; i < NACC; ++i) { tc::mbar_init(&acc_full[i], NI); tc::mbar_init(&acc_empty[i], kEpiThreads); }
+    tc::mbar_init(&fin, NI);
+    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], NI + kEpiThreads); }
     s_fail = 0;
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(&tmem_base, Occ<VEC>::TCOLS);
+    tc::tmem_alloc(&tmem_base, Occ<VEC, TF32>::TCOLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
@@ -353,8 +364,10 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_tcp(const Sht
       drain_copies<NA>(a_full, a_use);
       drain_copies<NB>(b_full, b_use);
     }
-  } else if (warp == 1) {
-    if (lane == 0) {  // ---------------------------------------- MMA issuer
+  } else if (warp == 1 || (Occ<VEC, TF32>::NISS == 2 && warp == 2 + kEpiThreads / 32)) {
+    if (lane == 0) {  // ---------------------------------------- MMA issuer(s)
+      constexpr bool DUAL = Occ<VEC, TF32>::NISS == 2;
+      const int tb0 = DUAL ? (warp == 1 ? 0 : 1) : 0, tb1 = DUAL ? tb0 + 1 : NT;
       uint32_t a_use = 0, b_use = 0, acc_use = 0, tr = 0;
       while (ok) {
         int ix;
@@ -373,7 +386,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_tcp(const Sht
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_use<NT, TF32>(acc, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, 0);
+            issue_use<NT, TF32>(acc, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, 0, tb0, tb1);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -385,7 +398,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_tcp(const Sht
       tc::mma_commit(&fin);
       if (!tc::mbar_wait(&fin, 0)) ok = false;
     }
-  } else {  // ------------------------------------------------------ epilogue
+  } else if (warp < 2 + kEpiThreads / 32) {  // ---------------------- epilogue
     const int q4 = warp & 3, half = (warp - 2) >> 2;
     const int cc0 = half * (NC / 2);  // this warp's 32 real columns
     const int jl = 32 * q4 + lane;
@@ -478,7 +491,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_tcp(const Sht
   tc::tc_fence_before();
   __syncthreads();
   if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
-  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC>::TCOLS);
+  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC, TF32>::TCOLS);
 }
 
 // ------------------------------------------------------------ analysis
@@ -497,7 +510,7 @@ struct FwdTile {
 };
 
 template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_tcp(const ShtGeom g, const FwdSet s, const TcTables t,
+__global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32>::CPS) fwd_leg_tcp(const ShtGeom g, const FwdSet s, const TcTables t,
                                                            const unsigned char* __restrict__ bimg, int nct) {
   typedef Form<TF32> F;
   constexpr int NT = VEC ? 2 : 1;
@@ -505,7 +518,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_tcp(const Sht
   constexpr int NA = Rings<VEC, false, TF32>::NA;
   constexpr int NB = Rings<VEC, false, TF32>::NB;
   constexpr uint32_t ACC = NT * F::NACCS * NC;
-  constexpr int NACC = 2 * ACC <= Occ<VEC>::TCOLS ? 2 : 1;
+  constexpr int NACC = 2 * ACC <= Occ<VEC, TF32>::TCOLS ? 2 : 1;
   constexpr int TS = F::OPSZ;       // one data operand
   constexpr int ASZ = NT * 16384;
   constexpr int BSZ = NT * TS;      // mine (and other)
@@ -524,16 +537,17 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_tcp(const Sht
   const int ntiles = nct * t.nlt * 2 * g.n_m;
 
   if (tid == 0) {
-    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], 1); }
-    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
-    for (int i = 0; i < NACC; ++i) { tc::mbar_init(&acc_full[i], 1); tc::mbar_init(&acc_empty[i], kEpiThreads); }
-    tc::mbar_init(&fin, 1);
-    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], 1 + kEpiThreads); }
+    constexpr int NI = Occ<VEC, TF32>::NISS;
+    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], NI); }
+    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], NI); }
+    for (int i = 0; i < NACC; ++i) { tc::mbar_init(&acc_full[i], NI); tc::mbar_init(&acc_empty[i], kEpiThreads); }
+    tc::mbar_init(&fin, NI);
+    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], NI + kEpiThreads); }
     s_fail = 0;
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(&tmem_base, Occ<VEC>::TCOLS);
+    tc::tmem_alloc(&tmem_base, Occ<VEC, TF32>::TCOLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
@@ -579,8 +593,10 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_tcp(const Sht
       drain_copies<NA>(a_full, a_use);
       drain_copies<NB>(b_full, b_use);
     }
-  } else if (warp == 1) {
-    if (lane == 0) {
+  } else if (warp == 1 || (Occ<VEC, TF32>::NISS == 2 && warp == 2 + kEpiThreads / 32)) {
+    if (lane == 0) {  // MMA issuer(s)
+      constexpr bool DUAL = Occ<VEC, TF32>::NISS == 2;
+      const int tb0 = DUAL ? (warp == 1 ? 0 : 1) : 0, tb1 = DUAL ? tb0 + 1 : NT;
       uint32_t a_use = 0, b_use = 0, acc_use = 0, tr = 0;
       while (ok) {
         int ix;
@@ -599,7 +615,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_tcp(const Sht
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_use<NT, TF32>(acc, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, TS);
+            issue_use<NT, TF32>(acc, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, TS, tb0, tb1);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -610,7 +626,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_tcp(const Sht
       tc::mma_commit(&fin);
       if (!tc::mbar_wait(&fin, 0)) ok = false;
     }
-  } else {
+  } else if (warp < 2 + kEpiThreads / 32) {  // epilogue
     const int q4 = warp & 3, half = (warp - 2) >> 2;
     const int cc0 = half * (NC / 2);
     const int lr = 32 * q4 + lane;
@@ -691,7 +707,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_tcp(const Sht
   tc::tc_fence_before();
   __syncthreads();
   if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
-  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC>::TCOLS);
+  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC, TF32>::TCOLS);
 }
 
 int num_sms() {
@@ -720,9 +736,9 @@ cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, u
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * OPSZ;
   CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
-  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms() * Occ<VEC>::CPS);
+  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms() * Occ<VEC, TF32>::CPS);
   CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  inv_leg_tcp<VEC, TF32><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
+  inv_leg_tcp<VEC, TF32><<<grid, kThreads + Occ<VEC, TF32>::XTRA, smem, st>>>(g, s, t, bimg, nct);
   return cudaGetLastError();
 }
 
@@ -741,9 +757,9 @@ cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, u
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * OPSZ;
   CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
-  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms() * Occ<VEC>::CPS);
+  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms() * Occ<VEC, TF32>::CPS);
   CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  fwd_leg_tcp<VEC, TF32><<<grid, kThreads, smem, st>>>(g, s, t, bimg, nct);
+  fwd_leg_tcp<VEC, TF32><<<grid, kThreads + Occ<VEC, TF32>::XTRA, smem, st>>>(g, s, t, bimg, nct);
   return cudaGetLastError();
 }
 
