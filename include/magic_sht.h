@@ -315,6 +315,12 @@ int magic_sht_measure_gflops(int device, int precision, double* gflops);
  * N = n (32/64/128/256), K = 64*kchunks (1 or 2) on bf16-exact inputs,
  * checked on the host; returns the max error relative to max |D|. */
 int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err);
+/* Failure-detection check of the kernels' bounded waits: a one-thread kernel
+ * waits on an mbarrier that is (arrive != 0) or is never (arrive == 0)
+ * completed, giving up after max_cycles SM cycles (1 .. 2^31).  Returns
+ * MAGIC_SHT_ERR_TIMEOUT when the wait gave up (the device stays usable),
+ * MAGIC_SHT_OK when it completed. */
+int magic_sht_wait_selftest(int device, long long max_cycles, int arrive);
 /* the same with tf32 operands (kind::tf32), K = 32*kchunks */
 int magic_sht_tc_selftest_tf32(int device, int n, int kchunks, double* max_rel_err);
 

@@ -126,6 +126,7 @@ SIGNATURES = {
     "magic_sht_device_status": [_V, ctypes.c_int],
     "magic_sht_tc_selftest": [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D],
     "magic_sht_tc_selftest_tf32": [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D],
+    "magic_sht_wait_selftest": [ctypes.c_int, ctypes.c_longlong, ctypes.c_int],
 }
 
 _lib = None

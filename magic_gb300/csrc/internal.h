@@ -27,6 +27,7 @@ cudaError_t convert_tables_fp32(const double* P, const double* dP, float* P32, f
 cudaError_t launch_fma_peak(void* out, bool fp64, int blocks, int iters, cudaStream_t st);
 
 // legendre_tc.cu
+cudaError_t launch_wait_selftest(long long max_cycles, int arrive, int* err, cudaStream_t st);
 cudaError_t launch_tc_selftest(int n, int kchunks, bool tf32, const float* A, const float* B, float* D, int* err,
                                cudaStream_t st);
 void tc_table_layout(const ShtGeom& g, bool tf32, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,

@@ -97,6 +97,22 @@ cudaError_t launch_selftest(const float* A, const float* B, float* D, int kchunk
 
 }  // namespace
 
+// Failure-detection check of the bounded waits: one thread waits on an
+// mbarrier that is (arrive != 0) or is not (arrive == 0) completed; a wait that
+// gives up after max_cycles sets *err and the kernel returns normally.
+__global__ void wait_selftest_kernel(long long max_cycles, int arrive, int* err) {
+  __shared__ uint64_t bar;
+  tc::mbar_init(&bar, 1);
+  tc::fence_mbar_init();
+  if (arrive) tc::mbar_arrive(&bar);
+  if (!tc::mbar_wait(&bar, 0, max_cycles)) *err = 1;
+}
+
+cudaError_t launch_wait_selftest(long long max_cycles, int arrive, int* err, cudaStream_t st) {
+  wait_selftest_kernel<<<1, 1, 0, st>>>(max_cycles, arrive, err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_tc_selftest(int n, int kchunks, bool tf32, const float* A, const float* B, float* D, int* err,
                                cudaStream_t st) {
   if (kchunks < 1 || kchunks > 2) return cudaErrorInvalidValue;

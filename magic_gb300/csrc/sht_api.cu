@@ -1744,6 +1744,24 @@ static int tc_selftest(int device, int n, int kchunks, bool tf32, double* max_re
   return MAGIC_SHT_OK;
 }
 
+int magic_sht_wait_selftest(int device, long long max_cycles, int arrive) {
+  if (max_cycles < 1 || max_cycles > (1LL << 31)) return set_err(MAGIC_SHT_ERR_ARG, "max_cycles outside [1, 2^31]");
+  int cur = 0;
+  CK(cudaGetDevice(&cur));
+  if (device >= 0) CK(cudaSetDevice(device));
+  int* derr = nullptr;
+  CK(cudaMalloc((void**)&derr, 4));
+  CK(cudaMemset(derr, 0, 4));
+  CK(launch_wait_selftest(max_cycles, arrive, derr, 0));
+  CK(cudaDeviceSynchronize());
+  int herr = 0;
+  CK(cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost));
+  cudaFree(derr);
+  if (device >= 0) CK(cudaSetDevice(cur));
+  if (herr) return set_err(MAGIC_SHT_ERR_TIMEOUT, "bounded device wait gave up after %lld cycles", max_cycles);
+  return MAGIC_SHT_OK;
+}
+
 int magic_sht_tc_selftest(int device, int n, int kchunks, double* max_rel_err) {
   return tc_selftest(device, n, kchunks, false, max_rel_err);
 }
