@@ -292,6 +292,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const T2 base = twg[S * lane];  // e^{2 pi i S lane / P}: times lo[q] gives e^{2 pi i k / P}, k = S lane + q
+  T2 wq[S];  // the same for both rows of the warp
+#pragma unroll
+  for (int q = 0; q < S; ++q) wq[q] = q == 0 ? base : cmul(base, stw[TwTab<S>::kLo + q]);
   for (int rr = warp; rr < RT; rr += 8) {
     T2* row = sm + rr * KP;
     T2 a[S];
@@ -306,7 +309,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
       if (kn < n_m) cn = row[q == 0 ? 32 - lane : 33 * (S - q) + 31 - lane];
       if (k == 0) { ck.y = 0; cn.y = 0; }
       const T2 E = cadd(ck, cconj(cn));
-      const T2 O = cmul(csub(ck, cconj(cn)), q == 0 ? base : cmul(base, stw[TwTab<S>::kLo + q]));
+      const T2 O = cmul(csub(ck, cconj(cn)), wq[q]);
       a[q].x = E.x - O.y;
       a[q].y = E.y + O.x;
     }
