@@ -436,6 +436,22 @@ def our_arm(args):
                 "frac": achieved_gbs / hbm, "traffic": traffic, "kernel": dom,
                 "peak_source": peak_kind}
     phases = {k: {"ms_per_step": v[0] / 2, "launches_per_step": v[1] // 2} for k, v in ph.items()}
+    # every phase against its own roofline: algorithmic bytes (tables once per
+    # launch for the Legendre phases, whose time includes their pack kernels)
+    # over HBM, and for the Legendre phases algorithmic flops (the 2KN / 8KN
+    # per transform counts, not the split-product count) over the bf16 dense peak
+    for k, v in phases.items():
+        if k not in alg or v["ms_per_step"] <= 0:
+            continue
+        sec = v["ms_per_step"] * 1e-3
+        nb = alg[k]["bytes"] * N_LEVELS + (table_bytes(L_MAX, N_THETA, MINC, tab_elem) if "leg" in k else 0)
+        v["algorithmic_gb"] = nb / 1e9
+        v["achieved_gbs"] = nb / sec / 1e9
+        v["hbm_frac"] = v["achieved_gbs"] / hbm
+        if "leg" in k:
+            fl = alg[k]["flops"] * N_LEVELS
+            v["achieved_tflops"] = fl / sec / 1e12
+            v["tensor_frac_of_bf16_peak"] = v["achieved_tflops"] / bf16 if bf16 else None
     phases64 = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in ph64.items()}
     # FP64 form's Legendre against the FP64 pipe
     leg64_ms = sum(v[0] for k, v in ph64.items() if "leg" in k)
