@@ -327,10 +327,12 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   // the row pair (rp, rp + 1) of this thread shares theta_j, j = rowg / 2
   const T o = (fd.flags & FFT_OSIN2) ? from_f64<T>(g.osin2[rowg >> 1]) : (T)1;
 #pragma unroll (sizeof(T) == 4 ? 4 : 2)
-  for (int kk = kq; kk < n; kk += KS) {
-    const T2 v0 = cscale(sm[rp * KP + pos(kk)], o);  // phi = 2kk (x) and 2kk+1 (y) of row rp
-    const T2 v1 = cscale(sm[(rp + 1) * KP + pos(kk)], o);
-    double* dst = out + (long long)(2 * kk) * g.ld + rowg;
+  const T2* s0 = sm + rp * KP + pos(kq);  // pos(kk + 32 j) = pos(kk) + 33 j
+  const long long dstep = 2LL * KS * g.ld;
+  double* dst = out + (long long)(2 * kq) * g.ld + rowg;
+  for (int kk = kq; kk < n; kk += KS, s0 += 33 * (KS / 32), dst += dstep) {
+    const T2 v0 = cscale(s0[0], o);  // phi = 2kk (x) and 2kk+1 (y) of row rp
+    const T2 v1 = cscale(s0[KP], o);
     // row rp widens on the FP64 pipe (idle in this kernel), row rp + 1 with
     // integer instructions: splitting the conversions between the two pipes
     // measured faster than either alone.  Both are exact; FP32 subnormals
