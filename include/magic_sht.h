@@ -182,7 +182,7 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n_levels, const int
                                     const magic_sht_lm_space_args* a);
 
 /* ---- asynchronous host-buffer batches.  With on != 0, a batched call whose
- * arrays are all in host memory and that spans more than 8 levels returns once
+ * arrays are all in host memory and that spans more than 16 levels returns once
  * its chunked copies and kernels are queued (instead of when the host outputs
  * are written); its host arrays must stay valid and untouched until
  * magic_sht_synchronize(h).  Consecutive such calls overlap one call's

@@ -1187,7 +1187,7 @@ static bool all_host(std::initializer_list<const void*> ptrs) {
   return any;
 }
 
-static const int kPipeChunk = 8;  // radial levels per pipeline chunk
+static const int kPipeChunk = 16;  // radial levels per pipeline chunk (8: 2% slower end to end, 4: 5%)
 
 // ------------------------------------------------------ radial-loop sets
 static int level_ctl(magic_sht_handle* h, CallCtx& cx, int n, const int* lcut, const double* or2,
