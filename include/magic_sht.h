@@ -190,6 +190,23 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n_levels, const int
  * default (the reference's calls return with their results). */
 int magic_sht_set_host_async(magic_sht_handle* h, int on);
 
+/* ---- runtime tuning of one handle (magic_gb300/autotune.py searches these
+ * per geometry and caches the choice).  Results do not depend on them except
+ * tc_kernel, which selects between two kernels of the same arithmetic form;
+ * graphs captured earlier keep the settings they were captured with.
+ *   tc_kernel:  tensor-core forms, 0 persistent kernels, 1 one tile per CTA
+ *               (3xBF16 only)
+ *   tc_order:   persistent kernels' tile order, 0 consecutive tiles share the
+ *               table blocks, 1 they share the data tiles
+ *   pipe_chunk: radial levels per chunk of the host-buffer pipeline (1..1024)
+ *   fft_rows:   theta rows per CTA of the FP32 azimuthal FFT, 8 or 16
+ *               (0 = by size) */
+typedef struct magic_sht_tuning {
+  int tc_kernel, tc_order, pipe_chunk, fft_rows;
+} magic_sht_tuning;
+int magic_sht_set_tuning(magic_sht_handle* h, const magic_sht_tuning* t);
+int magic_sht_get_tuning(const magic_sht_handle* h, magic_sht_tuning* t);
+
 /* ---- grid-space nonlinear products between the two transform sets
  * (get_nl.f90:213-441 and the Lorentz-force addition of rIter.f90:650-655).
  * Reads the grids transform_to_grid_space writes (vrc..vpc, cvrc..cvpc,

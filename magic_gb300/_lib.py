@@ -68,6 +68,10 @@ class RigidArgs(ctypes.Structure):
     _fields_ = [(n, _V) for n in RIGID]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("tc_kernel", "tc_order", "pipe_chunk", "fft_rows")]
+
+
 class LmSpaceArgs(ctypes.Structure):
     _fields_ = ([(n, _V) for n in LM_SPACE_IN] + [("grid_ld", ctypes.c_longlong)] +
                 [(n, _V) for n in LM_SPACE_OUT] + [("spec_ld", ctypes.c_longlong)])
@@ -106,6 +110,8 @@ SIGNATURES = {
                                           ctypes.POINTER(GridSpaceArgs)],
     "magic_sht_transform_to_lm_space": [_V, ctypes.c_int, _V, ctypes.POINTER(LmSpaceArgs)],
     "magic_sht_set_host_async": [_V, ctypes.c_int],
+    "magic_sht_set_tuning": [_V, ctypes.POINTER(Tuning)],
+    "magic_sht_get_tuning": [_V, ctypes.POINTER(Tuning)],
     "magic_sht_get_td": [_V, ctypes.c_int, _V, _V, ctypes.c_double, _V, ctypes.POINTER(TdArgs)],
     "magic_sht_get_td_nbc": [_V, ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, ctypes.POINTER(TdArgs)],
     "magic_sht_get_nl": [_V, ctypes.c_int, _V, ctypes.POINTER(GridSpaceArgs), ctypes.POINTER(LmSpaceArgs)],

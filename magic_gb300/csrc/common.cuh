@@ -134,6 +134,8 @@ struct TcTables {
   int ntt;                    // theta tiles of 128 northern points
   int nlt;                    // l' tiles of 128 rows per parity
   int ncj;                    // theta chunks of 64 (analysis K)
+  int order;                  // tile order of the persistent kernels: 0 = consecutive tiles
+                              // share the table block, 1 = they share the data block
 };
 
 // grids of the nonlinear products (nl.cu): inputs from the synthesis set,

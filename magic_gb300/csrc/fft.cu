@@ -668,24 +668,30 @@ bool factorize(int n, Radices& rad) {
   return n == 1;
 }
 
-template <typename T, int S>
-cudaError_t launch_fast(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
+template <typename T, int S, int RT>
+cudaError_t launch_rt(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
   typedef typename V2<T>::t T2;
-  // 16 rows per CTA; 8 rows where 16 would leave one CTA per SM
   constexpr int KP = 33 * S + 1;
-  constexpr int RT = (sizeof(T2) * 16 * KP > 100 * 1024) ? 8 : 16;
   const size_t smem = ((size_t)RT * KP + TwTab<S>::size) * sizeof(T2);
   dim3 grid((g.n_theta + RT - 1) / RT, s.nf * s.nlev);
-  if (inverse) {
-    auto k = fft_inv_fast<T, S, RT>;
-    CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<grid, 256, smem, st>>>(g, s);
-  } else {
-    auto k = fft_fwd_fast<T, S, RT>;
-    CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<grid, 256, smem, st>>>(g, s);
-  }
+  auto k = inverse ? fft_inv_fast<T, S, RT> : fft_fwd_fast<T, S, RT>;
+  CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k<<<grid, 256, smem, st>>>(g, s);
   return cudaGetLastError();
+}
+
+// rows: theta rows per CTA, 8 or 16 (FP32; the FP64 kernels keep the size
+// rule), 0 = 16, or 8 where 16 would leave one CTA per SM
+template <typename T, int S>
+cudaError_t launch_fast(const ShtGeom& g, const FftSet& s, bool inverse, int rows, cudaStream_t st) {
+  typedef typename V2<T>::t T2;
+  constexpr int KP = 33 * S + 1;
+  constexpr int RT = (sizeof(T2) * 16 * KP > 100 * 1024) ? 8 : 16;
+  if constexpr (sizeof(T) == 4) {
+    if (rows == 8) return launch_rt<T, S, 8>(g, s, inverse, st);
+    if (rows == 16) return launch_rt<T, S, 16>(g, s, inverse, st);
+  }
+  return launch_rt<T, S, RT>(g, s, inverse, st);
 }
 
 template <typename T>
@@ -708,23 +714,23 @@ cudaError_t launch_gen(const ShtGeom& g, const FftSet& s, bool inverse, cudaStre
 }
 
 template <typename T>
-cudaError_t launch_any(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
+cudaError_t launch_any(const ShtGeom& g, const FftSet& s, bool inverse, int rows, cudaStream_t st) {
   if (s.nf * s.nlev <= 0) return cudaSuccess;
   const int n = g.n_phi / 2;
   if (n % 32 == 0) {
     switch (n / 32) {
-      case 1: return launch_fast<T, 1>(g, s, inverse, st);
-      case 2: return launch_fast<T, 2>(g, s, inverse, st);
-      case 3: return launch_fast<T, 3>(g, s, inverse, st);
-      case 4: return launch_fast<T, 4>(g, s, inverse, st);
-      case 5: return launch_fast<T, 5>(g, s, inverse, st);
-      case 6: return launch_fast<T, 6>(g, s, inverse, st);
-      case 8: return launch_fast<T, 8>(g, s, inverse, st);
-      case 10: return launch_fast<T, 10>(g, s, inverse, st);
-      case 12: return launch_fast<T, 12>(g, s, inverse, st);
-      case 16: return launch_fast<T, 16>(g, s, inverse, st);
-      case 20: return launch_fast<T, 20>(g, s, inverse, st);
-      case 24: return launch_fast<T, 24>(g, s, inverse, st);
+      case 1: return launch_fast<T, 1>(g, s, inverse, rows, st);
+      case 2: return launch_fast<T, 2>(g, s, inverse, rows, st);
+      case 3: return launch_fast<T, 3>(g, s, inverse, rows, st);
+      case 4: return launch_fast<T, 4>(g, s, inverse, rows, st);
+      case 5: return launch_fast<T, 5>(g, s, inverse, rows, st);
+      case 6: return launch_fast<T, 6>(g, s, inverse, rows, st);
+      case 8: return launch_fast<T, 8>(g, s, inverse, rows, st);
+      case 10: return launch_fast<T, 10>(g, s, inverse, rows, st);
+      case 12: return launch_fast<T, 12>(g, s, inverse, rows, st);
+      case 16: return launch_fast<T, 16>(g, s, inverse, rows, st);
+      case 20: return launch_fast<T, 20>(g, s, inverse, rows, st);
+      case 24: return launch_fast<T, 24>(g, s, inverse, rows, st);
       default: break;
     }
   }
@@ -743,10 +749,10 @@ bool fft_fast_path(int n_phi) {
   }
 }
 
-cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, bool fp64, cudaStream_t st) {
-  return fp64 ? launch_any<double>(g, s, true, st) : launch_any<float>(g, s, true, st);
+cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, bool fp64, int rows, cudaStream_t st) {
+  return fp64 ? launch_any<double>(g, s, true, rows, st) : launch_any<float>(g, s, true, rows, st);
 }
 
-cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, bool fp64, cudaStream_t st) {
-  return fp64 ? launch_any<double>(g, s, false, st) : launch_any<float>(g, s, false, st);
+cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, bool fp64, int rows, cudaStream_t st) {
+  return fp64 ? launch_any<double>(g, s, false, rows, st) : launch_any<float>(g, s, false, rows, st);
 }

@@ -12,8 +12,9 @@ cudaError_t launch_fwd_legendre_simt(const ShtGeom& g, const FwdSet& s, bool vec
 // fft.cu
 // Inverse: half spectrum T2 [n_m][n_theta] -> double grid [n_phi][ld].
 // Forward: double grid -> ES/EA half spectrum T2 [n_m][nh][2] (scaled 1/n_phi).
-cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, bool fp64, cudaStream_t st);
-cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, bool fp64, cudaStream_t st);
+// rows: theta rows per CTA of the fast path (8 or 16; 0 = chosen by size)
+cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, bool fp64, int rows, cudaStream_t st);
+cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, bool fp64, int rows, cudaStream_t st);
 bool fft_fast_path(int n_phi);
 
 // tables.cu

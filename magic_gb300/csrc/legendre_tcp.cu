@@ -269,10 +269,18 @@ __global__ void __launch_bounds__(kPackThreads, 4) pack_fwd_kernel(const ShtGeom
 struct InvTile {
   int mc, p, tt, ct, nch, nchp, nlp;
   __device__ void decode(const ShtGeom& g, const TcTables& t, int nct, int ix) {
-    ct = ix % nct;
-    int rest = ix / nct;
-    tt = rest % t.ntt;
-    rest /= t.ntt;
+    int rest;
+    if (t.order == 0) {  // column tile fastest: consecutive tiles read the same table blocks
+      ct = ix % nct;
+      rest = ix / nct;
+      tt = rest % t.ntt;
+      rest /= t.ntt;
+    } else {             // theta tile fastest: consecutive tiles read the same data tiles
+      tt = ix % t.ntt;
+      rest = ix / t.ntt;
+      ct = rest % nct;
+      rest /= nct;
+    }
     p = rest & 1;
     mc = rest >> 1;
     const int n_l = g.l_max - mc * g.minc + 1;
@@ -498,10 +506,18 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
 struct FwdTile {
   int mc, p, lt, ct, nlp;
   __device__ void decode(const ShtGeom& g, const TcTables& t, int nct, int ix) {
-    ct = ix % nct;
-    int rest = ix / nct;
-    lt = rest % t.nlt;
-    rest /= t.nlt;
+    int rest;
+    if (t.order == 0) {  // column tile fastest: consecutive tiles read the same table blocks
+      ct = ix % nct;
+      rest = ix / nct;
+      lt = rest % t.nlt;
+      rest /= t.nlt;
+    } else {             // degree tile fastest: consecutive tiles read the same data tiles
+      lt = ix % t.nlt;
+      rest = ix / t.nlt;
+      ct = rest % nct;
+      rest /= nct;
+    }
     p = rest & 1;
     mc = rest >> 1;
     const int n_l = g.l_max - mc * g.minc + 1;

@@ -76,6 +76,12 @@ struct magic_sht_handle {
   float* d_fwd_scale = nullptr;
   int* d_err = nullptr;
   bool tc_persistent = true;  // MAGIC_SHT_TC_KERNEL=tiled selects the one-tile-per-CTA kernels
+  // runtime tuning (magic_sht_set_tuning): levels per host-pipeline chunk
+  // (default 16: at l_max = 255, 8 measured 2% slower end to end and 4 5%
+  // slower) and theta rows per CTA of the fast FFT (0 = by size); the
+  // persistent kernels' tile order lives in tct.order
+  int pipe_chunk = 16;
+  int fft_rows = 0;
   char* ws = nullptr;
   size_t ws_bytes = 0;
   std::vector<int> lmoff;
@@ -406,7 +412,7 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
   auto flush_fft = [&]() -> int {
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_INV);
-      CK(launch_fft_inverse(g, fs, f64, h->stream));
+      CK(launch_fft_inverse(g, fs, f64, h->fft_rows, h->stream));
       fs.nf = 0;
     }
     return MAGIC_SHT_OK;
@@ -488,7 +494,7 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
   auto flush_fft = [&]() -> int {
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_FWD);
-      CK(launch_fft_forward(g, fs, f64, h->stream));
+      CK(launch_fft_forward(g, fs, f64, h->fft_rows, h->stream));
       fs.nf = 0;
     }
     return MAGIC_SHT_OK;
@@ -854,6 +860,33 @@ int magic_sht_set_host_async(magic_sht_handle* h, int on) {
   return MAGIC_SHT_OK;
 }
 
+int magic_sht_set_tuning(magic_sht_handle* h, const magic_sht_tuning* t) {
+  TRY(check_handle(h));
+  if (!t) return set_err(MAGIC_SHT_ERR_ARG, "null tuning");
+  if (t->tc_kernel < 0 || t->tc_kernel > 1 || t->tc_order < 0 || t->tc_order > 1)
+    return set_err(MAGIC_SHT_ERR_ARG, "tc_kernel and tc_order are 0 or 1");
+  if (t->pipe_chunk < 1 || t->pipe_chunk > 1024) return set_err(MAGIC_SHT_ERR_ARG, "pipe_chunk outside [1, 1024]");
+  if (t->fft_rows != 0 && t->fft_rows != 8 && t->fft_rows != 16)
+    return set_err(MAGIC_SHT_ERR_ARG, "fft_rows is 0, 8 or 16");
+  if (t->tc_kernel == 1 && tf32_form(h))
+    return set_err(MAGIC_SHT_ERR_UNSUPPORTED, "the TF32 form has only the persistent kernels");
+  if (tc_form(h)) h->tc_persistent = t->tc_kernel == 0;
+  h->tct.order = t->tc_order;
+  h->pipe_chunk = t->pipe_chunk;
+  h->fft_rows = t->fft_rows;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_get_tuning(const magic_sht_handle* h, magic_sht_tuning* t) {
+  TRY(check_handle(h));
+  if (!t) return set_err(MAGIC_SHT_ERR_ARG, "null tuning");
+  t->tc_kernel = h->tc_persistent ? 0 : 1;
+  t->tc_order = h->tct.order;
+  t->pipe_chunk = h->pipe_chunk;
+  t->fft_rows = h->fft_rows;
+  return MAGIC_SHT_OK;
+}
+
 int magic_sht_reserve(magic_sht_handle* h, int n) {
   TRY(check_handle(h));
   if (n < 1) return set_err(MAGIC_SHT_ERR_ARG, "n_levels=%d", n);
@@ -1187,7 +1220,6 @@ static bool all_host(std::initializer_list<const void*> ptrs) {
   return any;
 }
 
-static const int kPipeChunk = 16;  // radial levels per pipeline chunk (8: 2% slower end to end, 4: 5%)
 
 // ------------------------------------------------------ radial-loop sets
 static int level_ctl(magic_sht_handle* h, CallCtx& cx, int n, const int* lcut, const double* or2,
@@ -1217,7 +1249,7 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
   if (a->spec_ld < g.lm_max || a->grid_ld < (long long)g.n_phi * g.ld)
     return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
   DeviceGuard dg(h->device);
-  if (n > kPipeChunk && !h->capturing &&
+  if (n > h->pipe_chunk && !h->capturing &&
       all_host({a->s, a->p, a->xi, a->w, a->dw, a->ddw, a->z, a->dz, a->b, a->db, a->ddb, a->aj, a->dj,
                 a->sc, a->pc, a->xic, a->vrc, a->vtc, a->vpc, a->cvrc, a->cvtc, a->cvpc, a->brc, a->btc,
                 a->bpc, a->cbrc, a->cbtc, a->cbpc, lcut, or2})) {
@@ -1240,7 +1272,7 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
     if (lcut) arrs.push_back({lcut, 4, 4, false, 0});
     const int i_or2 = or2 ? (int)arrs.size() - (lcut ? 2 : 1) : -1;
     const int i_lc = lcut ? (int)arrs.size() - 1 : -1;
-    return pipelined_levels(h, n, kPipeChunk, arrs, [&](int r0, int nr, const std::vector<char*>& d) {
+    return pipelined_levels(h, n, h->pipe_chunk, arrs, [&](int r0, int nr, const std::vector<char*>& d) {
       magic_sht_grid_space_args b = *a;
       double** pin[13] = {(double**)&b.s, (double**)&b.p, (double**)&b.xi, (double**)&b.w, (double**)&b.dw,
                           (double**)&b.ddw, (double**)&b.z, (double**)&b.dz, (double**)&b.b, (double**)&b.db,
@@ -1543,7 +1575,7 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
   if (a->spec_ld < g.lm_max || a->grid_ld < (long long)g.n_phi * g.ld)
     return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
   DeviceGuard dg(h->device);
-  if (n > kPipeChunk && !h->capturing &&
+  if (n > h->pipe_chunk && !h->capturing &&
       all_host({lcut, a->Advr, a->Advt, a->Advp, a->VSr, a->VSt, a->VSp, a->VxBr, a->VxBt, a->VxBp, a->heatTerms,
                 a->AdvrLM, a->AdvtLM, a->AdvpLM, a->VSrLM, a->VStLM, a->VSpLM, a->VxBrLM, a->VxBtLM,
                 a->VxBpLM, a->heatTermsLM})) {
@@ -1564,7 +1596,7 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
       if (outs[i]) { idx_out[i] = (int)arrs.size(); arrs.push_back({outs[i], sb, (size_t)g.lm_max * 16, true, 0}); }
     if (lcut) arrs.push_back({lcut, 4, 4, false, 0});
     const int i_lc = lcut ? (int)arrs.size() - 1 : -1;
-    return pipelined_levels(h, n, kPipeChunk, arrs, [&](int r0, int nr, const std::vector<char*>& d) {
+    return pipelined_levels(h, n, h->pipe_chunk, arrs, [&](int r0, int nr, const std::vector<char*>& d) {
       magic_sht_lm_space_args b = *a;
       const double** pin[10] = {&b.Advr, &b.Advt, &b.Advp, &b.VSr, &b.VSt, &b.VSp, &b.VxBr, &b.VxBt,
                                 &b.VxBp, &b.heatTerms};
@@ -1886,6 +1918,6 @@ extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double*
   fs.f[0].in_ld = hs_ld;
   fs.f[0].out_ld = (long long)g.n_phi * g.ld;
   fs.f[0].flags = tc_form(h) ? FFT_IN_E : 0;  // parity-separated synthesis output
-  CK(launch_fft_inverse(g, fs, fp64_pipes(h), h->stream));
+  CK(launch_fft_inverse(g, fs, fp64_pipes(h), h->fft_rows, h->stream));
   return MAGIC_SHT_OK;
 }

@@ -357,6 +357,25 @@ class SHT:
         check(self._lib.magic_sht_transform_to_lm_space(self._h, n, plc, ctypes.byref(a)))
         return outs
 
+    def tuning(self) -> Dict[str, int]:
+        """Runtime tuning of this handle (magic_sht_get_tuning): tc_kernel,
+        tc_order, pipe_chunk, fft_rows."""
+        t = _lib.Tuning()
+        check(self._lib.magic_sht_get_tuning(self._h, ctypes.byref(t)))
+        return {n: getattr(t, n) for n, _ in _lib.Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        """Change some of tc_kernel, tc_order, pipe_chunk, fft_rows
+        (magic_sht_set_tuning); returns the previous settings."""
+        old = self.tuning()
+        bad = set(kw) - set(old)
+        if bad:
+            raise ValueError("unknown tuning keys %s" % sorted(bad))
+        new = dict(old, **kw)
+        t = _lib.Tuning(*[int(new[n]) for n, _ in _lib.Tuning._fields_])
+        check(self._lib.magic_sht_set_tuning(self._h, ctypes.byref(t)))
+        return old
+
     def set_host_async(self, on: bool):
         """Batched calls on host arrays return once queued; results are valid
         after ``synchronize()`` (magic_sht_set_host_async)."""
