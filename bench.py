@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variant", action="store_true", help="skip the TF32 variant of the tensor-core form")
     ap.add_argument("--levels", type=int, default=N_LEVELS, help="radial levels (profiling cases)")
+    ap.add_argument("--instances", action="store_true",
+                    help="instead of the bench line: sixteen mixed-size instances in one graph (one JSON line)")
     ap.add_argument("--only-reduced", action="store_true", help="skip the FP64 form (profiling)")
     ap.add_argument("--clock-seconds", type=float, default=1.5,
                     help="back-to-back steps sampled for clocks before the timed steps")
@@ -537,10 +539,78 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
+def instances_arm(args):
+    """Sixteen independent instances of mixed size (l_max in {63, 127, 255},
+    minc in {1, 4}, {33, 65, 129} radial levels, n_theta = 3(l_max+1)/2,
+    n_phi = 2 n_theta / minc; a fixed seeded list), both transform sets of every
+    instance captured into one CUDA graph on one stream and replayed.  The
+    analysis inputs are the instance's synthesis grids."""
+    import numpy as np
+    import torch
+    from magic_gb300 import SHT
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    form = "bf16x3" if args.form == "auto" else args.form
+    rng = np.random.default_rng(1234)
+    insts, desc = [], []
+    for i in range(16):
+        L = int(rng.choice([63, 127, 255]))
+        minc = int(rng.choice([1, 4]))
+        R = int(rng.choice([33, 65, 129]))
+        N = 3 * (L + 1) // 2
+        P = 2 * N // minc
+        s = SHT(L, minc, N, P, precision=form, device=local)
+        spec = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(L, minc, R, seed=500 + i).items()}
+        or2 = torch.from_numpy(or2_levels(R)).cuda()
+        g = s.transform_to_grid_space(spec, or2=or2)
+        fin = {k: g[v] for k, v in FORWARD_FROM_INVERSE.items()}
+        lm = s.transform_to_lm_space(fin)
+        insts.append((s, spec, or2, g, fin, lm, R))
+        desc.append({"l_max": L, "minc": minc, "n_theta": N, "n_phi": P, "levels": R})
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        for s, *_ in insts:
+            s.set_stream(side.cuda_stream)
+        side.synchronize()
+        insts[0][0].graph_begin()
+        try:
+            for s, spec, or2, g, fin, lm, _ in insts:
+                s.transform_to_grid_space(spec, or2=or2, out=g)
+                s.transform_to_lm_space(fin, out=lm)
+        finally:
+            gr = insts[0][0].graph_end()
+        for _ in range(max(args.warmup, 3)):
+            insts[0][0].graph_launch(gr)
+        side.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(side)
+        for _ in range(args.steps):
+            insts[0][0].graph_launch(gr)
+        e1.record(side)
+        side.synchronize()
+    ms = e0.elapsed_time(e1)
+    for s, *_ in insts:
+        s.device_status()
+    insts[0][0].graph_destroy(gr)
+    levels = sum(d["levels"] for d in desc)
+    if rank == 0:
+        print(json.dumps({"metric": "SHT radial levels/s, sixteen mixed instances in one graph",
+                          "value": levels * args.steps / (ms * 1e-3), "unit": "levels/s", "n_gpus": 1,
+                          "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+                          "higher_is_better": True, "form": form, "levels_per_step": levels,
+                          "timing": "graph replay, CUDA events on the replay stream",
+                          "instances": desc}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.instances:
+        instances_arm(args)
         return
     our_arm(args)
 
