@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--cpu-levels", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-stage", action="store_true", help="skip the radial-loop stage measurement")
     ap.add_argument("--no-variant", action="store_true", help="skip the TF32 variant of the tensor-core form")
     ap.add_argument("--levels", type=int, default=N_LEVELS, help="radial levels (profiling cases)")
     ap.add_argument("--instances", action="store_true",
@@ -138,6 +139,70 @@ def algorithmic_per_level(L, N, P, minc, t2):
         "fwd_leg_scalar": dict(bytes=4 * hs + 4 * spec, flops=4 * 2 * K * N),
         "fwd_leg_vector": dict(bytes=6 * hs + 6 * spec, flops=3 * 8 * K * N),
     }, K
+
+
+def stage_measure(sm, s64, spec, n_levels, steps, hbm):
+    """One explicit stage of the radial loop (RadialLoop.step: the synthesis
+    set, rigid-boundary overrides, get_nl on the interior levels, the
+    analysis set, the Courant steps and get_td with the boundary flags) over
+    every level, eager, as a caller runs it: the Courant steps return to the
+    host once per stage.  Wall time and CUDA events per stage, and the
+    radial-loop kernels (get_nl, courant, get_td, boundary kernels) against
+    the HBM roofline with their algorithmic bytes."""
+    import numpy as np
+    import torch
+    from magic_gb300.radial_loop import RadialLoop
+    from magic_gb300.workload import radii
+    loop = RadialLoop(sm, radii(n_levels), cor_fac=1e3, ktopv=2, kbotv=2)
+    # accuracy of the stage against the same stage on the FP64 handle
+    ref = RadialLoop(s64, radii(n_levels), cor_fac=1e3, ktopv=2, kbotv=2).step(spec)
+    got = loop.step(spec)
+    acc = {}
+    for k in ("dwdt", "dzdt", "dpdt", "dsdt", "dbdt", "djdt", "dVxBhLM"):
+        acc[k] = float(torch.linalg.vector_norm(got[k] - ref[k]) / torch.linalg.vector_norm(ref[k]))
+    acc["dtrkc"] = float(np.max(np.abs(got["dtrkc"] / ref["dtrkc"] - 1.0)))
+    acc["dthkc"] = float(np.max(np.abs(got["dthkc"] / ref["dthkc"] - 1.0)))
+    del ref, got
+    for _ in range(2):
+        loop.step(spec)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    t0 = time.perf_counter()
+    ev[0].record(st)
+    for k in range(steps):
+        loop.step(spec)
+        ev[k + 1].record(st)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / steps * 1e3
+    per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    sm.set_profiling(True)
+    sm.phase_times(reset=True)
+    loop.step(spec)
+    ph = sm.phase_times(reset=True)
+    sm.set_profiling(False)
+    torch.cuda.synchronize()
+    sm.device_status()
+    N, P, K = sm.nlat_padded, sm.n_phi_max, sm.lm_max
+    grid = 8 * N * P
+    interior = n_levels - 2  # rigid boundaries: get_nl on the interior levels only
+    alg = {"nl": (13 + 10) * grid * interior,          # 13 synthesis grids in, 10 analysis grids out
+           "courant": 6 * grid * n_levels,             # v and B grids in, two numbers per level out
+           "td": (10 + 7) * 16 * K * n_levels}         # 10 spectra in, 7 out
+    kern = {}
+    for k, (ms, n) in ph.items():
+        if not n:
+            continue
+        kern[k] = {"ms": ms, "launches": n}
+        if k in alg and ms > 0:
+            gbs = alg[k] / (ms * 1e-3) / 1e9
+            kern[k].update({"algorithmic_gb": alg[k] / 1e9, "achieved_gbs": gbs, "hbm_frac": gbs / hbm})
+    return {"what": "RadialLoop.step: transform_to_grid_space, rigid boundaries, get_nl (interior), "
+                    "transform_to_lm_space, courant (host dt arrays), get_td with nBc",
+            "levels": n_levels, "steps": steps, "ms_per_stage_wall": wall,
+            "ms_per_stage_events": statistics.median(per), "levels_per_s": n_levels / (wall * 1e-3),
+            "kernels": kern,
+            "rel_l2_vs_fp64_stage": acc}
 
 
 def table_bytes(L, N, minc, elem):
@@ -437,7 +502,7 @@ def our_arm(args):
         roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                 "frac": achieved_gbs / hbm, "traffic": traffic, "kernel": dom,
                 "peak_source": peak_kind}
-    phases = {k: {"ms_per_step": v[0] / 2, "launches_per_step": v[1] // 2} for k, v in ph.items()}
+    phases = {k: {"ms_per_step": v[0] / 2, "launches_per_step": v[1] // 2} for k, v in ph.items() if v[1]}
     # every phase against its own roofline: algorithmic bytes (tables once per
     # launch for the Legendre phases, whose time includes their pack kernels)
     # over HBM, and for the Legendre phases algorithmic flops (the 2KN / 8KN
@@ -454,7 +519,7 @@ def our_arm(args):
             fl = alg[k]["flops"] * N_LEVELS
             v["achieved_tflops"] = fl / sec / 1e12
             v["tensor_frac_of_bf16_peak"] = v["achieved_tflops"] / bf16 if bf16 else None
-    phases64 = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in ph64.items()}
+    phases64 = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in ph64.items() if v[1]}
     # FP64 form's Legendre against the FP64 pipe
     leg64_ms = sum(v[0] for k, v in ph64.items() if "leg" in k)
     leg_flops = sum(alg[k]["flops"] for k in alg if "leg" in k) * N_LEVELS
@@ -501,6 +566,11 @@ def our_arm(args):
                "path": "transform_to_grid_space + transform_to_lm_space on pinned host arrays, "
                        "asynchronous host batches, synchronized every step"}
 
+    # ---- one explicit stage of the radial loop (headline form)
+    stage = None
+    if not args.no_stage:
+        stage = stage_measure(sm, s64, spec, N_LEVELS, max(3, min(args.steps, 10)), hbm)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(args.cpu_levels)
@@ -531,6 +601,7 @@ def our_arm(args):
             "gpu_launches": launches,
             "clocks": clocks,
             "e2e": e2e,
+            "stage": stage,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -313,7 +313,11 @@ int magic_sht_graph_destroy(magic_sht_graph* graph);
 #define MAGIC_SHT_PHASE_FFT_FWD 3
 #define MAGIC_SHT_PHASE_FWD_LEG_SCALAR 4
 #define MAGIC_SHT_PHASE_FWD_LEG_VECTOR 5
-#define MAGIC_SHT_N_PHASES 6
+#define MAGIC_SHT_PHASE_NL 6      /* magic_sht_get_nl */
+#define MAGIC_SHT_PHASE_COURANT 7 /* magic_sht_courant (two kernels) */
+#define MAGIC_SHT_PHASE_TD 8      /* magic_sht_get_td / magic_sht_get_td_nbc */
+#define MAGIC_SHT_PHASE_BCS 9     /* the boundary kernels of nonlinear_bcs.f90 */
+#define MAGIC_SHT_N_PHASES 10
 int magic_sht_set_profiling(magic_sht_handle* h, int on);
 /* accumulated ms and launch counts per phase (arrays of MAGIC_SHT_N_PHASES) */
 int magic_sht_phase_times(magic_sht_handle* h, double* ms, long long* launches, int reset);

@@ -160,6 +160,8 @@ struct TdArgs {
   const double* epsc;   // [level] internal heating of dsdt(l=0), or null (= 0)
   const int* nbc;       // [level] boundary flag (nBc != 0), or null (all interior)
   double cor_fac;       // CorFac (1/E)
+  const double2* coef;  // [lm][4] level-independent coefficients (build_td_coef)
+  const int* lq;        // [lm] l | m << 16
 };
 
 // Courant condition (courant.cu); grids [level][ld], radial functions [level]

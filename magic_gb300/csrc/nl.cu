@@ -4,9 +4,11 @@
 // transform_to_grid_space.  Boussinesq form (orho1 = 1), curl form of the
 // advection (l_adv_curl), magnetic field and heat equation on, unit physical
 // constants (LFfac = OhmLossFac = 1, otemp1 = lambda = 1); heatTerms holds the
-// ohmic-loss part (get_nl.f90:424-429).  Elementwise, FP64, HBM-bound.
+// ohmic-loss part (get_nl.f90:424-429).  Elementwise: FP64 arithmetic in the
+// FP64 form, FP32 arithmetic (FP64 grids in and out) in the reduced forms.
 #include <algorithm>
 #include "common.cuh"
+#include "cplx.cuh"
 #include "internal.h"
 
 namespace {
@@ -19,38 +21,41 @@ __device__ __forceinline__ void st2(double* p, long long o, double a, double b) 
 }
 
 // one thread per (level, phi, pair of theta rows 2j, 2j+1); rows of a pair
-// share theta_j in the scrambled north/south order
+// share theta_j in the scrambled north/south order.  T is the arithmetic:
+// double (the FP64 form), or float for the reduced forms, whose grids carry
+// errors far above FP32 rounding: the FP64 grids are narrowed and the
+// products widened with integer instructions (d2f_int / f2d_int), so the
+// float kernel runs on the FP32 and integer pipes and is bound by HBM, while
+// the FP64 one is bound by the FP64 pipe (about 40 FP64 operations a point).
+template <typename T>
 __global__ void __launch_bounds__(256) get_nl_kernel(const ShtGeom g, const NlGrids in, NlGrids out,
-                                                     const double* __restrict__ or2, double or2_0, int nlev) {
-  const int nh = g.n_theta / 2;
-  const long long per_level = (long long)g.n_phi * nh;
-  const long long total = per_level * nlev;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(i / per_level);
-    const long long rem = i - (long long)r * per_level;
-    const int ph = (int)(rem / nh), j = (int)(rem - (long long)ph * nh);
-    const long long o_in = (long long)r * in.ld + (long long)ph * g.ld + 2 * j;
-    const long long o_out = (long long)r * out.ld + (long long)ph * g.ld + 2 * j;
-    const double o2 = or2 ? or2[r] : or2_0, o4 = o2 * o2;
-    const double sn2 = g.osin2[j];  // 1 / sin^2 theta_j
-    const double2 vr = ld2(in.p[NL_VR], o_in), vt = ld2(in.p[NL_VT], o_in), vp = ld2(in.p[NL_VP], o_in);
-    const double2 cvr = ld2(in.p[NL_CVR], o_in), cvt = ld2(in.p[NL_CVT], o_in), cvp = ld2(in.p[NL_CVP], o_in);
-    const double2 br = ld2(in.p[NL_BR], o_in), bt = ld2(in.p[NL_BT], o_in), bp = ld2(in.p[NL_BP], o_in);
-    const double2 cbr = ld2(in.p[NL_CBR], o_in), cbt = ld2(in.p[NL_CBT], o_in), cbp = ld2(in.p[NL_CBP], o_in);
-    const double2 sc = ld2(in.p[NL_S], o_in);
-    double res[NL_NOUT][2];
+                                                     const double* __restrict__ or2, double or2_0, int r0) {
+  const int r = r0 + blockIdx.y;
+  const unsigned nh = (unsigned)(g.n_theta / 2), per_level = (unsigned)g.n_phi * nh;
+  const double o2d = or2 ? or2[r] : or2_0;
+  const T o2 = from_f64<T>(o2d), o4 = from_f64<T>(o2d * o2d);
+  const long long b_in = (long long)r * in.ld, b_out = (long long)r * out.ld;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < per_level; i += gridDim.x * blockDim.x) {
+    const unsigned ph = i / nh, j = i - ph * nh;
+    const long long o_in = b_in + (long long)ph * g.ld + 2 * j;
+    const long long o_out = b_out + (long long)ph * g.ld + 2 * j;
+    const T sn2 = from_f64<T>(g.osin2[j]);  // 1 / sin^2 theta_j
+    double2 x[NL_NIN];
+#pragma unroll
+    for (int k = 0; k < NL_NIN; ++k) x[k] = ld2(in.p[k], o_in);
+    T res[NL_NOUT][2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const double Vr = h ? vr.y : vr.x, Vt = h ? vt.y : vt.x, Vp = h ? vp.y : vp.x;
-      const double Wr = h ? cvr.y : cvr.x, Wt = h ? cvt.y : cvt.x, Wp = h ? cvp.y : cvp.x;
-      const double Br = h ? br.y : br.x, Bt = h ? bt.y : bt.x, Bp = h ? bp.y : bp.x;
-      const double Jr = h ? cbr.y : cbr.x, Jt = h ? cbt.y : cbt.x, Jp = h ? cbp.y : cbp.x;
-      const double S = h ? sc.y : sc.x;
+      auto v = [&](int k) { return from_f64<T>(h ? x[k].y : x[k].x); };
+      const T Vr = v(NL_VR), Vt = v(NL_VT), Vp = v(NL_VP);
+      const T Wr = v(NL_CVR), Wt = v(NL_CVT), Wp = v(NL_CVP);
+      const T Br = v(NL_BR), Bt = v(NL_BT), Bp = v(NL_BP);
+      const T Jr = v(NL_CBR), Jt = v(NL_CBT), Jp = v(NL_CBP);
+      const T S = v(NL_S);
       // Lorentz force (get_nl.f90:243-256)
-      const double LFr = sn2 * (Jt * Bp - Jp * Bt);
-      const double LFt = o4 * (Jp * Br - Jr * Bp);
-      const double LFp = o4 * (Jr * Bt - Jt * Br);
+      const T LFr = sn2 * (Jt * Bp - Jp * Bt);
+      const T LFt = o4 * (Jp * Br - Jr * Bp);
+      const T LFp = o4 * (Jr * Bt - Jt * Br);
       // advection, curl form (get_nl.f90:262-272), plus the Lorentz force
       res[NL_ADVR][h] = -sn2 * (Wt * Vp - Wp * Vt) + LFr;
       res[NL_ADVT][h] = -o4 * (Wp * Vr - Wr * Vp) + LFt;
@@ -67,20 +72,26 @@ __global__ void __launch_bounds__(256) get_nl_kernel(const ShtGeom g, const NlGr
       res[NL_HEAT][h] = o2 * (o2 * Jr * Jr + sn2 * Jt * Jt + sn2 * Jp * Jp);
     }
 #pragma unroll
-    for (int k = 0; k < NL_NOUT; ++k) st2(out.p[k], o_out, res[k][0], res[k][1]);
+    for (int k = 0; k < NL_NOUT; ++k) st2(out.p[k], o_out, to_f64<T>(res[k][0]), to_f64<T>(res[k][1]));
   }
 }
 
 }  // namespace
 
 cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& out, const double* or2,
-                          double or2_0, int nlev, cudaStream_t st) {
-  const long long total = (long long)nlev * g.n_phi * (g.n_theta / 2);
-  if (total <= 0) return cudaSuccess;
+                          double or2_0, int nlev, bool f32, cudaStream_t st) {
+  const long long per_level = (long long)g.n_phi * (g.n_theta / 2);
+  if (nlev <= 0 || per_level <= 0) return cudaSuccess;
   int dev = 0, nsm = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const long long blocks = std::min<long long>((total + 255) / 256, (long long)nsm * 8);
-  get_nl_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, in, out, or2, or2_0, nlev);
-  return cudaGetLastError();
+  const int need = (int)((per_level + 255) / 256);
+  for (int r0 = 0; r0 < nlev; r0 += 65535) {
+    const int nl = std::min(nlev - r0, 65535);
+    const int gx = std::max(1, std::min(need, (8 * nsm + nl - 1) / nl));  // about eight blocks per SM in all
+    if (f32) get_nl_kernel<float><<<dim3(gx, nl), 256, 0, st>>>(g, in, out, or2, or2_0, r0);
+    else get_nl_kernel<double><<<dim3(gx, nl), 256, 0, st>>>(g, in, out, or2, or2_0, r0);
+    CUDA_TRY(cudaGetLastError());
+  }
+  return cudaSuccess;
 }

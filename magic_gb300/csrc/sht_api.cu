@@ -57,6 +57,8 @@ struct magic_sht_handle {
   bool own_stream = false;
   bool capturing = false;
   int* d_lmoff = nullptr;
+  double2* d_tdcoef = nullptr;  // get_td coefficients [lm][4]
+  int* d_tdlq = nullptr;        // [lm] l | m << 16
   double *d_theta = nullptr, *d_gauss = nullptr, *d_P = nullptr, *d_dP = nullptr;
   double *d_wgt = nullptr, *d_osin2 = nullptr;
   float *d_P32 = nullptr, *d_dP32 = nullptr;
@@ -244,9 +246,10 @@ struct PhaseScope {
   magic_sht_handle* h;
   int ph;
   cudaEvent_t e1 = nullptr;
-  PhaseScope(magic_sht_handle* h_, int ph_) : h(h_), ph(ph_) {
-    h->launches++;
-    h->phase_launches[ph]++;
+  // `nk` kernels launched inside the scope (timed together)
+  PhaseScope(magic_sht_handle* h_, int ph_, int nk = 1) : h(h_), ph(ph_) {
+    h->launches += nk;
+    h->phase_launches[ph] += nk;
     if (h->profiling && !h->capturing) {
       cudaEvent_t e0 = next_event(h);
       e1 = next_event(h);
@@ -652,7 +655,7 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   if (!d || !out) return set_err(MAGIC_SHT_ERR_ARG, "null descriptor or output pointer");
   *out = nullptr;
   const int L = d->l_max, minc = d->minc, N = d->n_theta_max, P = d->n_phi_max;
-  if (L < 1) return set_err(MAGIC_SHT_ERR_SIZE, "l_max=%d must be >= 1", L);
+  if (L < 1 || L > 32767) return set_err(MAGIC_SHT_ERR_SIZE, "l_max=%d must be in [1, 32767]", L);
   if (minc < 1) return set_err(MAGIC_SHT_ERR_SIZE, "minc=%d must be > 0", minc);
   if (N <= 2 || N % 4) return set_err(MAGIC_SHT_ERR_SIZE, "n_theta_max=%d must be a multiple of 4 and > 2", N);
   if (P % 4 || P / 2 <= 2) return set_err(MAGIC_SHT_ERR_SIZE, "n_phi_max=%d must be a multiple of 4 and > 4", P);
@@ -718,6 +721,8 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     INIT_CK(cudaMalloc((void**)&h->d_P32, sizeof(float) * tab));
     INIT_CK(cudaMalloc((void**)&h->d_dP32, sizeof(float) * tab));
   }
+  INIT_CK(cudaMalloc((void**)&h->d_tdcoef, sizeof(double2) * 4 * (size_t)K));
+  INIT_CK(cudaMalloc((void**)&h->d_tdlq, sizeof(int) * (size_t)K));
   INIT_CK(cudaMalloc((void**)&h->d_err, sizeof(int)));
   INIT_CK(cudaMemset(h->d_err, 0, sizeof(int)));
   INIT_CK(cudaMemcpyAsync(h->d_lmoff, h->lmoff.data(), sizeof(int) * n_m, cudaMemcpyHostToDevice, h->stream));
@@ -737,8 +742,9 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
                             h->d_wgt, h->d_osin2, h->stream));
   if (h->precision == MAGIC_SHT_FP32)
     INIT_CK(convert_tables_fp32(h->d_P, h->d_dP, h->d_P32, h->d_dP32, tab, h->stream));
-  INIT_CK(cudaStreamSynchronize(h->stream));
   g.lmoff = h->d_lmoff;
+  INIT_CK(build_td_coef(g, h->d_tdcoef, h->d_tdlq, h->stream));
+  INIT_CK(cudaStreamSynchronize(h->stream));
   g.P64 = h->d_P; g.dP64 = h->d_dP; g.P32 = h->d_P32; g.dP32 = h->d_dP32;
   g.wgt = h->d_wgt; g.osin2 = h->d_osin2; g.tw64 = h->d_tw64; g.tw32 = h->d_tw32;
   if (tc_form(h)) {
@@ -791,7 +797,7 @@ int magic_sht_finalize(magic_sht_handle* h) {
   void* ptrs[] = {h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP, h->d_wgt, h->d_osin2,
                   h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws, h->d_inv_img, h->d_fwd_img,
                   h->d_inv_blk0, h->d_fwd_blk0, h->d_inv_scale, h->d_fwd_scale, h->d_err,
-                  h->d_bpc0, h->d_bimg, h->d_tile_ctr};
+                  h->d_bpc0, h->d_bimg, h->d_tile_ctr, h->d_tdcoef, h->d_tdlq};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   for (auto& P : h->pools) {
@@ -1369,8 +1375,11 @@ int magic_sht_get_nl(magic_sht_handle* h, int n, const double* or2, const magic_
   CallCtx cx(h);
   const int i_or2 = or2 ? cx.raw_in(or2, (size_t)n * 8) : -1;
   TRY(cx.prepare());
-  h->launches++;
-  CK(launch_get_nl(g, in, out, (const double*)cx.dev(i_or2), 1.0, n, h->stream));
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_NL);
+    CK(launch_get_nl(g, in, out, (const double*)cx.dev(i_or2), 1.0, n, h->precision != MAGIC_SHT_FP64,
+                     h->stream));
+  }
   return cx.finish();
 }
 
@@ -1416,8 +1425,12 @@ int magic_sht_get_td_nbc(magic_sht_handle* h, int n, const double* r, const int*
   t.epsc = (const double*)cx.dev(i_ep);
   t.nbc = (const int*)cx.dev(i_bc);
   t.cor_fac = cor_fac;
-  h->launches++;
-  CK(launch_get_td(g, t, n, h->stream));
+  t.coef = h->d_tdcoef;
+  t.lq = h->d_tdlq;
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_TD);
+    CK(launch_get_td(g, t, n, h->stream));
+  }
   return cx.finish();
 }
 
@@ -1451,9 +1464,11 @@ int magic_sht_courant(magic_sht_handle* h, int n, const magic_sht_courant_args* 
   c.delxr2 = (const double*)cx.dev(irf[4]); c.delxh2 = (const double*)cx.dev(irf[5]);
   c.courfac = a->courfac; c.alffac = a->alffac; c.LFfac = a->LFfac; c.opm = a->opm;
   c.alf_damp = a->l_cour_alf_damp;
-  h->launches += 2;
-  CK(launch_courant(g, c, n, (unsigned long long*)cx.dev(i_mx), (double*)cx.dev(i_r), (double*)cx.dev(i_h),
-                    h->stream));
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_COURANT, 2);
+    CK(launch_courant(g, c, n, (unsigned long long*)cx.dev(i_mx), (double*)cx.dev(i_r), (double*)cx.dev(i_h),
+                      h->stream));
+  }
   return cx.finish();
 }
 
@@ -1471,8 +1486,10 @@ int magic_sht_v_rigid_boundary(magic_sht_handle* h, double r2_rho0, double omega
   TRY(cx.prepare());
   BcGrids b{};
   for (int i = 0; i < 8; ++i) b.p[i] = (i == 0 && keep_vr) ? nullptr : (double*)cx.dev(idx[i]);
-  h->launches++;
-  CK(launch_v_rigid_boundary(h->g, h->d_theta, b, r2_rho0, omega, keep_vr, h->stream));
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_BCS);
+    CK(launch_v_rigid_boundary(h->g, h->d_theta, b, r2_rho0, omega, keep_vr, h->stream));
+  }
   return cx.finish();
 }
 
@@ -1487,9 +1504,11 @@ int magic_sht_v_center_sphere(magic_sht_handle* h, const double* ddw, double* vr
   const int i_r = cx.grid_out(vr, 1, gl), i_t = cx.grid_out(vt, 1, gl), i_p = cx.grid_out(vp, 1, gl);
   TRY(cx.prepare());
   const int lm11 = (h->g.minc == 1 && h->g.n_m > 1) ? h->lmoff[1] : -1;
-  h->launches++;
-  CK(launch_v_center_sphere(h->g, h->d_theta, (const double2*)cx.dev(i_s), lm11, (double*)cx.dev(i_r),
-                            (double*)cx.dev(i_t), (double*)cx.dev(i_p), h->stream));
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_BCS);
+    CK(launch_v_center_sphere(h->g, h->d_theta, (const double2*)cx.dev(i_s), lm11, (double*)cx.dev(i_r),
+                              (double*)cx.dev(i_t), (double*)cx.dev(i_p), h->stream));
+  }
   return cx.finish();
 }
 
@@ -1506,10 +1525,12 @@ int magic_sht_get_br_v_bcs(magic_sht_handle* h, const double* br, const double* 
   const int o_t = cx.spec_out(br_vt_lm, 1, g.lm_max), o_p = cx.spec_out(br_vp_lm, 1, g.lm_max);
   std::vector<int> hs_vc = {cx.tmp(hs_bytes(h, 1)), cx.tmp(hs_bytes(h, 1))};
   TRY(cx.prepare());
-  h->launches++;
-  CK(launch_br_v_products(g, h->d_theta, (const double*)cx.dev(i_b), (const double*)cx.dev(i_t),
-                          (const double*)cx.dev(i_p), or2 * orho1, omega, (double*)cx.dev(t_t),
-                          (double*)cx.dev(t_p), h->stream));
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_BCS);
+    CK(launch_br_v_products(g, h->d_theta, (const double*)cx.dev(i_b), (const double*)cx.dev(i_t),
+                            (const double*)cx.dev(i_p), or2 * orho1, omega, (double*)cx.dev(t_t),
+                            (double*)cx.dev(t_p), h->stream));
+  }
   LevelCtl lv;
   lv.nlev = 1; lv.lcut0 = g.l_max;
   lv.spec_ld = g.lm_max; lv.grid_ld = gl;
@@ -1529,12 +1550,11 @@ int magic_sht_get_b_nl_bcs(magic_sht_handle* h, double fac, const double* br_vt_
   const int i_vt = b_nl_bc ? cx.spec_in(br_vt_lm, 1, K) : -1, i_vp = cx.spec_in(br_vp_lm, 1, K);
   const int o_b = b_nl_bc ? cx.spec_out(b_nl_bc, 1, K) : -1, o_j = cx.spec_out(aj_nl_bc, 1, K);
   TRY(cx.prepare());
-  if (b_nl_bc) {
-    h->launches++;
-    CK(launch_b_nl_bcs(K, fac, (const double2*)cx.dev(i_vt), (double2*)cx.dev(o_b), h->stream));
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_BCS, b_nl_bc ? 2 : 1);
+    if (b_nl_bc) CK(launch_b_nl_bcs(K, fac, (const double2*)cx.dev(i_vt), (double2*)cx.dev(o_b), h->stream));
+    CK(launch_b_nl_bcs(K, fac, (const double2*)cx.dev(i_vp), (double2*)cx.dev(o_j), h->stream));
   }
-  h->launches++;
-  CK(launch_b_nl_bcs(K, fac, (const double2*)cx.dev(i_vp), (double2*)cx.dev(o_j), h->stream));
   return cx.finish();
 }
 

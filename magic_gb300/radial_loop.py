@@ -113,17 +113,21 @@ class RadialLoop:
         gs = {k: v[lo:hi] for k, v in g.items()}
         nl = s.get_nl(gs, or2=self.or2[lo:hi])
         lc = None if self.lcut is None else self.lcut[lo:hi]
-        lm = s.transform_to_lm_space(nl, lcut=lc)
-        res = dict(out or {})
-        # analysis outputs at all levels; boundary levels without lMagNlBc
-        # have zero VxBt / VxBp (rIter.f90:256-259) and zero dVSrLM (get_td.f90:501-507)
-        full = {}
-        for k in _lib.LM_SPACE_OUT:
-            t = torch.zeros((n, s.lm_max), dtype=torch.complex128, device=lm[k].device)
-            t[lo:hi] = lm[k]
-            full[k] = t
+        # analysis outputs at all levels, written in place into rows lo..hi-1;
+        # boundary levels without lMagNlBc have zero VxBt / VxBp
+        # (rIter.f90:256-259) and every level's dVSrLM is zero at the
+        # boundaries (get_td.f90:501-507)
+        dev = g["vrc"].device
+        full = {k: torch.empty((n, s.lm_max), dtype=torch.complex128, device=dev) for k in _lib.LM_SPACE_OUT}
+        s.transform_to_lm_space(nl, lcut=lc, out={k: v[lo:hi] for k, v in full.items()})
+        for k, v in full.items():
+            if lo > 0:
+                v[:lo].zero_()
+            if hi < n:
+                v[hi:].zero_()
         full["VSrLM"][0].zero_()
         full["VSrLM"][n - 1].zero_()
+        res = dict(out or {})
         dtrkc, dthkc = s.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, self.radial,
                                  self.courfac, self.alffac, self.LFfac, self.opm, self.l_cour_alf_damp)
         if self.l_b_nl_cmb:

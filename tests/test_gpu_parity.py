@@ -400,6 +400,29 @@ def test_get_nl_matches_oracle(built, oracle_mod, torch, grid):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("form", ["bf16x3", "tf32x2", "fp32"])
+def test_get_nl_reduced_forms_compute_in_fp32(built, oracle_mod, torch, form):
+    """On a reduced-precision handle get_nl computes in FP32 (FP64 grids in
+    and out): every product within 1e-6 relative L2 of the FP64 restatement,
+    and not bit-identical to it (the FP32 kernel ran)."""
+    from oracle import oracle as orc
+    from magic_gb300 import _lib
+    L, minc, N, P = 63, 1, 96, 192
+    n = 3
+    s = make(L, minc, N, P, prec=form)
+    rng = np.random.default_rng(5)
+    grids = {k: torch.from_numpy(rng.standard_normal((n, P, N))).cuda() for k in _lib.NL_IN}
+    or2 = np.array([1.0, 0.37, 2.5])
+    out = s.get_nl(grids, or2=or2)
+    torch.cuda.synchronize()
+    ref = orc.get_nl({k: v.cpu().numpy() for k, v in grids.items()}, or2, N)
+    for k in _lib.LM_SPACE_IN:
+        e = rel_l2(out[k].cpu().numpy(), ref[k])
+        assert 0.0 < e < 1e-6, (k, e)
+    s.close()
+
+
+@pytest.mark.gpu
 def test_radial_step_with_nonlinear_products(built, torch):
     """The radial-loop step of rIter.f90:94-464 on the GPU: synthesis set,
     get_nl on the FP64 grids, analysis set.  Each vector analysis

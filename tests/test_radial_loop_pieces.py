@@ -221,3 +221,68 @@ def test_radial_loop_stage_matches_oracle(built, torch, oracle_mod, cfg):
         exp = orc.get_br_v_bcs(o, g["brc"][0], g["vtc"][0], g["vpc"][0], cfg["omega_ma"], or2[0], 1.0)
         close(got["br_vt_lm_cmb"].cpu().numpy(), exp[0], tol=1e-10)
         close(got["br_vp_lm_cmb"].cpu().numpy(), exp[1], tol=1e-10)
+
+
+@pytest.mark.gpu
+def test_radial_loop_kernels_have_phase_timers(built, torch):
+    """The radial-loop kernels are timed like the transforms: with profiling
+    on, one stage records CUDA-event time and launches under get_nl,
+    courant, get_td and the boundary kernels."""
+    from magic_gb300.radial_loop import RadialLoop
+    from magic_gb300.workload import grid_space_inputs
+    L, n = 31, 4
+    s = make(L, 1, 48, 96)
+    loop = RadialLoop(s, np.linspace(1.538, 0.538, n), cor_fac=10.0, ktopv=2, kbotv=2)
+    spec = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(L, 1, n, seed=3).items()}
+    s.set_profiling(True)
+    s.phase_times(reset=True)
+    loop.step(spec)
+    ph = s.phase_times(reset=True)
+    s.set_profiling(False)
+    assert ph["nl"][1] == 1 and ph["td"][1] == 1 and ph["courant"][1] == 2 and ph["bcs"][1] == 2
+    for k in ("nl", "courant", "td", "bcs", "fft_inv", "fft_fwd"):
+        assert ph[k][0] > 0.0, k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["wide", "ties", "tiny", "huge", "zeros_no_damp"])
+@pytest.mark.parametrize("mag", [True, False])
+def test_courant_filter_keeps_exact_maxima(built, torch, kind, mag):
+    """The Courant kernel skips points whose FP32 estimate cannot hold the
+    maximum; the maxima must still be the FP64 ones.  Inputs that stress the
+    estimate: a dynamic range of 1e+-20 (lognormal), near-ties (every value
+    1 + 1e-12 noise), fields of 1e-30 (below the estimate's absolute floor),
+    values of 1e200 (beyond FP32), and exact zeros in B without damping (0/0
+    terms left out of the maximum)."""
+    from oracle import oracle as orc
+    L, minc, N, P = 63, 1, 96, 192
+    s = make(L, minc, N, P)
+    n = 4
+    rng = np.random.default_rng(77)
+    shape = (n, s.n_phi_max, s.nlat_padded)
+    keys = ("vrc", "vtc", "vpc", "brc", "btc", "bpc")
+    if kind == "wide":
+        h = {k: rng.standard_normal(shape) * np.exp(rng.standard_normal(shape) * 15.0) for k in keys}
+    elif kind == "ties":
+        h = {k: np.sign(rng.standard_normal(shape)) * (1.0 + 1e-12 * rng.standard_normal(shape)) for k in keys}
+    elif kind == "tiny":
+        h = {k: 1e-30 * rng.standard_normal(shape) for k in keys}
+    elif kind == "huge":
+        h = {k: rng.standard_normal(shape) for k in keys}
+        for k in keys:
+            h[k][:, 3, 5] = 1e200 * (1.0 + rng.random(n))
+    else:
+        h = {k: rng.standard_normal(shape) for k in keys}
+        for k in ("brc", "btc", "bpc"):
+            h[k][:, ::2, :] = 0.0
+    damp = kind != "zeros_no_damp"
+    g = {k: torch.from_numpy(v).cuda() for k, v in h.items()}
+    if not mag:
+        for k in ("brc", "btc", "bpc"):
+            g.pop(k)
+            h[k] = None
+    rad = _radial(n, rng)
+    got_r, got_h = s.courant(g, rad, courfac=2.5, alffac=1.0, LFfac=1.3, opm=0.7, alf_damp=damp)
+    exp_r, exp_h = orc.courant(h, rad, N, courfac=2.5, alffac=1.0, LFfac=1.3, opm=0.7, alf_damp=damp)
+    np.testing.assert_allclose(got_r, exp_r, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(got_h, exp_h, rtol=1e-13, atol=0)
