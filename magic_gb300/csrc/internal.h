@@ -52,7 +52,7 @@ cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& ou
                           double or2_0, int nlev, bool f32, cudaStream_t st);
 
 // td.cu
-cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, cudaStream_t st);
+cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, bool f32, cudaStream_t st);
 cudaError_t build_td_coef(const ShtGeom& g, double2* coef, int* lq, cudaStream_t st);
 // boundary pieces of the radial loop, one level (bcs.cu); theta = the n_theta
 // Gauss colatitudes north to south

@@ -103,6 +103,12 @@ struct magic_sht_handle {
   cudaStream_t cpy_in = nullptr, cpy_out = nullptr;
   // magic_sht_set_host_async: pipelined host-buffer calls return once queued
   bool host_async = false;
+  // pinned ring for small host inputs (per-level arrays such as or2, r,
+  // lcut): their copies are issued from pinned memory, asynchronously, so a
+  // call whose only host arrays are such inputs needs no synchronisation
+  char* pin = nullptr;
+  size_t pin_cap = 0, pin_off = 0;
+  cudaEvent_t pin_ev = nullptr;
   // per-phase CUDA-event timing (magic_sht_set_profiling)
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -266,8 +272,49 @@ struct PhaseScope {
   }
 };
 
+constexpr size_t kPinRing = 1 << 20, kPinMax = 64 << 10;
+
+// Copies a small host input into the pinned ring and returns its slot, or
+// null (too large, or no pinned memory: the caller copies from the pageable
+// array).  A slot is written again only after every copy of the previous lap
+// has completed (all of them were issued on the handle's stream, and binding
+// another stream synchronises the old one).
+const void* pin_stage(magic_sht_handle* h, const void* src, size_t bytes) {
+  const size_t need = (bytes + 255) & ~(size_t)255;
+  if (need > kPinMax) return nullptr;
+  if (!h->pin) {
+    if (cudaHostAlloc((void**)&h->pin, kPinRing, cudaHostAllocDefault) != cudaSuccess) {
+      h->pin = nullptr;
+      cudaGetLastError();
+      return nullptr;
+    }
+    if (cudaEventCreateWithFlags(&h->pin_ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaFreeHost(h->pin);
+      h->pin = nullptr;
+      h->pin_ev = nullptr;
+      cudaGetLastError();
+      return nullptr;
+    }
+    h->pin_cap = kPinRing;
+    h->pin_off = 0;
+  }
+  if (h->pin_off + need > h->pin_cap) {
+    if (cudaEventRecord(h->pin_ev, h->stream) != cudaSuccess || cudaEventSynchronize(h->pin_ev) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    h->pin_off = 0;
+  }
+  char* p = h->pin + h->pin_off;
+  memcpy(p, src, bytes);
+  h->pin_off += need;
+  return p;
+}
+
 // One call's device buffers: host arrays are staged, device arrays are used
-// in place, temporaries come from the handle's workspace.
+// in place, temporaries come from the handle's workspace.  Small host inputs
+// of raw_in go through the pinned ring; a call with any other host array
+// synchronises its stream before returning.
 class CallCtx {
  public:
   enum Kind { IN = 0, OUT = 1, TMP = 2, INOUT = 3 };
@@ -301,11 +348,14 @@ class CallCtx {
 
   int prepare() {
     size_t total = 0;
+    bool host = false;
     for (auto& e : ents_) {
       if (e.kind != TMP) e.is_dev = is_device_ptr(e.host);
       if (e.kind == TMP || !e.is_dev) total += align256(e.bytes);
-      if (e.kind != TMP && !e.is_dev) any_host_ = true;
+      if (e.kind != TMP && !e.is_dev && e.host) host = true;
     }
+    if (host && h_->capturing)
+      return set_err(MAGIC_SHT_ERR_ARG, "host arrays in a captured call: pass device arrays while capturing");
     TRY(ensure_ws(h_, total));
     size_t off = 0;
     for (auto& e : ents_) {
@@ -315,8 +365,11 @@ class CallCtx {
       }
       e.dev = h_->ws + off;
       off += align256(e.bytes);
+      if (e.kind == TMP) continue;
+      const void* src = (e.raw && e.kind == IN && e.bytes) ? pin_stage(h_, e.host, e.bytes) : nullptr;
+      if (!src) any_host_ = true;
       if ((e.kind == IN || e.kind == INOUT) && e.bytes)
-        CK(cudaMemcpyAsync(e.dev, e.host, e.bytes, cudaMemcpyHostToDevice, h_->stream));
+        CK(cudaMemcpyAsync(e.dev, src ? src : e.host, e.bytes, cudaMemcpyHostToDevice, h_->stream));
     }
     return MAGIC_SHT_OK;
   }
@@ -800,6 +853,8 @@ int magic_sht_finalize(magic_sht_handle* h) {
                   h->d_bpc0, h->d_bimg, h->d_tile_ctr, h->d_tdcoef, h->d_tdlq};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  if (h->pin) cudaFreeHost(h->pin);
+  if (h->pin_ev) cudaEventDestroy(h->pin_ev);
   for (auto& P : h->pools) {
     if (P.buf) cudaFree(P.buf);
     for (auto* v : {&P.ev_in, &P.ev_comp, &P.ev_out})
@@ -1429,7 +1484,7 @@ int magic_sht_get_td_nbc(magic_sht_handle* h, int n, const double* r, const int*
   t.lq = h->d_tdlq;
   {
     PhaseScope sc(h, MAGIC_SHT_PHASE_TD);
-    CK(launch_get_td(g, t, n, h->stream));
+    CK(launch_get_td(g, t, n, h->precision != MAGIC_SHT_FP64, h->stream));
   }
   return cx.finish();
 }

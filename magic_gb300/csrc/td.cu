@@ -48,76 +48,85 @@ __global__ void td_coef_kernel(const ShtGeom g, double2* coef, int* lq) {
 }
 
 // One block row (blockIdx.y) per radial level, threads over lm; the
-// coefficients come from the tables of td_coef_kernel (L2-resident).
+// coefficients come from the tables of td_coef_kernel (L2-resident).  T is
+// the arithmetic: double in the FP64 form (about 60 FP64 operations per lm,
+// which bound the kernel by the FP64 pipe), float in the reduced forms, whose
+// spectra carry errors far above FP32 rounding (FP64 spectra narrowed and the
+// results widened with integer instructions; bound by HBM).
+template <typename T>
 __global__ void __launch_bounds__(256) get_td_kernel(const ShtGeom g, const TdArgs a, int r0) {
+  typedef typename V2<T>::t T2;
   const int r = r0 + blockIdx.y;
-  const double rr = a.r[r], or1 = 1.0 / rr, or2 = or1 * or1, or4 = or2 * or2;
+  const double rrd = a.r[r], or1d = 1.0 / rrd, or2d = or1d * or1d;
+  const T rr = from_f64<T>(rrd), or1 = from_f64<T>(or1d), or2 = from_f64<T>(or2d), or4 = from_f64<T>(or2d * or2d);
   const int lR = a.lcut ? min(a.lcut[r], g.l_max) : g.l_max;
   const bool boundary = a.nbc && a.nbc[r] != 0;
-  const double two_cor = 2.0 * a.cor_fac;
-  const double2 zero = make_double2(0.0, 0.0);
+  const T two_cor = from_f64<T>(2.0 * a.cor_fac);
+  const T2 zero = zero2<T2>();
   const long long o0 = (long long)r * a.ld;
+  auto ld = [&](const double2* p, long long o) { return cvt2<T2>(p[o]); };
   for (int lm = blockIdx.x * blockDim.x + threadIdx.x; lm < g.lm_max; lm += gridDim.x * blockDim.x) {
     const long long o = o0 + lm;
     const double2 c3 = a.coef[4 * lm + 3];
-    const double dLh = c3.x, dm = c3.y;
+    const T dLh = from_f64<T>(c3.x), dm = from_f64<T>(c3.y);
     if (boundary) {  // boundary level: only get_dbdt's dVxBhLM (get_td.f90:598-612)
-      a.dVxBh[o] = cscale(a.VxBt[o], -dLh * rr * rr);
+      a.dVxBh[o] = to_d2(cscale(ld(a.VxBt, o), -dLh * rr * rr));
       continue;
     }
     const int q = a.lq[lm], l = q & 0xFFFF, m = q >> 16;
     const bool hasS = l > m, hasA = l < lR;  // l-1 and l+1 terms (clm(m,m) = 0; l = l_R drops l+1)
-    const double2 c0 = a.coef[4 * lm + 0], c1 = a.coef[4 * lm + 1], c2 = a.coef[4 * lm + 2];
-    const double2 w = a.w[o], dw = a.dw[o], z = a.z[o];
-    const double2 zS = hasS ? a.z[o - 1] : zero, zA = hasA ? a.z[o + 1] : zero;
-    const double2 dwS = hasS ? a.dw[o - 1] : zero, dwA = hasA ? a.dw[o + 1] : zero;
-    const double2 wS = hasS ? a.w[o - 1] : zero, wA = hasA ? a.w[o + 1] : zero;
+    const double2 c0 = a.coef[4 * lm + 0], c1 = a.coef[4 * lm + 1];
+    const T2 w = ld(a.w, o), dw = ld(a.dw, o), z = ld(a.z, o);
+    const T2 zS = hasS ? ld(a.z, o - 1) : zero, zA = hasA ? ld(a.z, o + 1) : zero;
+    const T2 dwS = hasS ? ld(a.dw, o - 1) : zero, dwA = hasA ? ld(a.dw, o + 1) : zero;
+    const T2 wS = hasS ? ld(a.w, o - 1) : zero, wA = hasA ? ld(a.w, o + 1) : zero;
     const bool inside = l <= lR;
     // dPhi * x = i m x
-    auto iphi = [&](double2 x) { return make_double2(-dm * x.y, dm * x.x); };
+    auto iphi = [&](T2 x) { return mk2(-dm * x.y, dm * x.x); };
     // ---- get_dwdt: or2 AdvrLM + 2 CorFac or1 (dPhi dw + dTheta2A z(l+1) - dTheta2S z(l-1))
-    double2 dwdt = cscale(a.Advr[o], or2);
+    T2 dwdt = cscale(ld(a.Advr, o), or2);
     if (inside) {
-      const double t2A = c0.x, t2S = c0.y;
-      const double2 p = iphi(dw);
-      const double2 c = make_double2(p.x + t2A * zA.x - t2S * zS.x, p.y + t2A * zA.y - t2S * zS.y);
+      const T t2A = from_f64<T>(c0.x), t2S = from_f64<T>(c0.y);
+      const T2 p = iphi(dw);
+      const T2 c = mk2(p.x + t2A * zA.x - t2S * zS.x, p.y + t2A * zA.y - t2S * zS.y);
       if (l > 0) dwdt = cadd(dwdt, cscale(c, two_cor * or1));
-      else dwdt = cadd(dwdt, cscale(make_double2(t2A * zA.x, t2A * zA.y), two_cor * or1));  // lm = 1
+      else dwdt = cadd(dwdt, cscale(mk2(t2A * zA.x, t2A * zA.y), two_cor * or1));  // lm = 1
     }
     // ---- get_dzdt: dLh AdvpLM + 2 CorFac or2 (dPhi z + dTheta3A dw(l+1) + or1 dTheta4A w(l+1)
     //                                           + dTheta3S dw(l-1) - or1 dTheta4S w(l-1))
-    double2 dzdt = l > 0 ? cscale(a.Advp[o], dLh) : zero;
-    const double t3A = c1.x, t3S = c1.y;
+    T2 dzdt = l > 0 ? cscale(ld(a.Advp, o), dLh) : zero;
+    const T t3A = from_f64<T>(c1.x), t3S = from_f64<T>(c1.y);
     if (inside) {
-      const double t4A = c2.x, t4S = c2.y;
-      double2 c = make_double2(t3A * dwA.x + or1 * t4A * wA.x + t3S * dwS.x - or1 * t4S * wS.x,
-                               t3A * dwA.y + or1 * t4A * wA.y + t3S * dwS.y - or1 * t4S * wS.y);
+      const double2 c2 = a.coef[4 * lm + 2];
+      const T t4A = from_f64<T>(c2.x), t4S = from_f64<T>(c2.y);
+      T2 c = mk2(t3A * dwA.x + or1 * t4A * wA.x + t3S * dwS.x - or1 * t4S * wS.x,
+                 t3A * dwA.y + or1 * t4A * wA.y + t3S * dwS.y - or1 * t4S * wS.y);
       if (l > 0) c = cadd(c, iphi(z));
       dzdt = cadd(dzdt, cscale(c, two_cor * or2));
     }
     // ---- get_dpdt: -dLh AdvtLM + 2 CorFac or2 (-dPhi (dw + or1 dLh w) + dTheta3A z(l+1) + dTheta3S z(l-1))
-    double2 dpdt = zero;
+    T2 dpdt = zero;
     if (l > 0) {
-      dpdt = cscale(a.Advt[o], -dLh);
+      dpdt = cscale(ld(a.Advt, o), -dLh);
       if (inside) {
-        const double2 qq = iphi(make_double2(dw.x + or1 * dLh * w.x, dw.y + or1 * dLh * w.y));
-        const double2 c = make_double2(-qq.x + t3A * zA.x + t3S * zS.x, -qq.y + t3A * zA.y + t3S * zS.y);
+        const T2 qq = iphi(mk2(dw.x + or1 * dLh * w.x, dw.y + or1 * dLh * w.y));
+        const T2 c = mk2(-qq.x + t3A * zA.x + t3S * zS.x, -qq.y + t3A * zA.y + t3S * zS.y);
         dpdt = cadd(dpdt, cscale(c, two_cor * or2));
       }
     }
     // ---- get_dsdt (Boussinesq): dLh VStLM; l = 0: the internal heating epsc
-    const double2 dsdt = l > 0 ? cscale(a.VSt[o], dLh) : make_double2(a.epsc ? a.epsc[r] : 0.0, 0.0);
+    const double2 dsdt = l > 0 ? to_d2(cscale(ld(a.VSt, o), dLh)) : make_double2(a.epsc ? a.epsc[r] : 0.0, 0.0);
     // ---- get_dbdt
-    const double2 dbdt = cscale(a.VxBp[o], dLh);
-    const double2 dVxBh = cscale(a.VxBt[o], -dLh * rr * rr);
-    const double2 djdt = cscale(a.VxBr[o], dLh * or4);
-    a.dwdt[o] = dwdt;
-    a.dzdt[o] = dzdt;
-    a.dpdt[o] = dpdt;
+    const T2 dbdt = cscale(ld(a.VxBp, o), dLh);
+    const T2 dVxBh = cscale(ld(a.VxBt, o), -dLh * rr * rr);
+    const T2 djdt = cscale(ld(a.VxBr, o), dLh * or4);
+    a.dwdt[o] = to_d2(dwdt);
+    a.dzdt[o] = to_d2(dzdt);
+    a.dpdt[o] = to_d2(dpdt);
     a.dsdt[o] = dsdt;
-    a.dbdt[o] = dbdt;
-    a.djdt[o] = djdt;
-    a.dVxBh[o] = dVxBh;
+    a.dbdt[o] = to_d2(dbdt);
+    a.djdt[o] = to_d2(djdt);
+    a.dVxBh[o] = to_d2(dVxBh);
   }
 }
 
@@ -129,7 +138,7 @@ cudaError_t build_td_coef(const ShtGeom& g, double2* coef, int* lq, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, cudaStream_t st) {
+cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, bool f32, cudaStream_t st) {
   if (nlev <= 0 || g.lm_max <= 0) return cudaSuccess;
   int dev = 0, nsm = 148;
   cudaGetDevice(&dev);
@@ -138,7 +147,8 @@ cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, cudaStrea
   for (int r0 = 0; r0 < nlev; r0 += 65535) {
     const int nl = std::min(nlev - r0, 65535);
     const int gx = std::max(1, std::min(need, (8 * nsm + nl - 1) / nl));  // about eight blocks per SM in all
-    get_td_kernel<<<dim3(gx, nl), 256, 0, st>>>(g, a, r0);
+    if (f32) get_td_kernel<float><<<dim3(gx, nl), 256, 0, st>>>(g, a, r0);
+    else get_td_kernel<double><<<dim3(gx, nl), 256, 0, st>>>(g, a, r0);
     CUDA_TRY(cudaGetLastError());
   }
   return cudaSuccess;

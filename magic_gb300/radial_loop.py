@@ -16,8 +16,11 @@ unit physical constants in get_nl.  Level 0 is the outer boundary (n_r_cmb,
 nBc = ktopv), level n-1 the inner boundary (n_r_icb, nBc = kbotv), as in
 MagIC's radial ordering.  Every array is a CUDA tensor ([level][lm] complex
 spectra, [level][phi][theta] grids) and the stage runs on the current torch
-stream; the Courant steps come back to the host (numpy), as dt_courant
-(courant.f90:280-346) needs them there, which synchronizes the stream once.
+stream; the per-level arrays (radii, or2, lcut, nBc, the Courant radial
+functions) live on the device, so no call of the stage waits for the
+stream, and the Courant steps come back to the host (numpy) at the end, as
+dt_courant (courant.f90:280-346) needs them there: the stage's one
+synchronisation.
 The two boundary levels run the bulk synthesis set and are then overwritten
 (vrc = 0 at a stress-free boundary, v_rigid_boundary at a rigid one); the
 grids the reference does not compute there are not read afterwards.
@@ -90,6 +93,21 @@ class RadialLoop:
         self.l_b_nl_icb = kbotv == 1 and l_cond_ic
         self.nbc = np.zeros(n, dtype=np.int32)
         self.nbc[0], self.nbc[n - 1] = ktopv, kbotv
+        self._dev = {}
+
+    def _on(self, device):
+        """The per-level arrays as CUDA tensors on `device` (made once): every
+        call of the stage then takes device pointers, so none of them waits
+        for the stream."""
+        if device not in self._dev:
+            import torch
+            f = lambda x: torch.as_tensor(np.ascontiguousarray(x), device=device)  # noqa: E731
+            d = {"or2": f(self.or2), "r": f(self.r), "nbc": f(self.nbc),
+                 "lcut": None if self.lcut is None else f(self.lcut),
+                 "epsc": None if self.epsc is None else f(np.asarray(self.epsc, dtype=np.float64)),
+                 "radial": {k: f(v) for k, v in self.radial.items()}}
+            self._dev[device] = d
+        return self._dev[device]
 
     def _boundary_grids(self, g: Dict, i: int, kind: int, omega: float, keep_vr: bool):
         if kind == 1:  # stress-free: vrc = 0 (rIter.f90:552-556)
@@ -106,13 +124,14 @@ class RadialLoop:
         boundaries ``br_vt_lm_cmb`` / ``br_vp_lm_cmb`` (or ``_icb``)."""
         import torch
         s, n = self.s, self.n
-        g = s.transform_to_grid_space(spec, or2=self.or2, lcut=self.lcut)
+        dv = self._on(spec["w"].device)
+        g = s.transform_to_grid_space(spec, or2=dv["or2"], lcut=dv["lcut"])
         self._boundary_grids(g, 0, self.ktopv, self.omega_ma, self.l_vr_cmb)
         self._boundary_grids(g, n - 1, self.kbotv, self.omega_ic, self.l_vr_icb)
         lo, hi = (0, n) if self.lMagNlBc else (1, n - 1)
         gs = {k: v[lo:hi] for k, v in g.items()}
-        nl = s.get_nl(gs, or2=self.or2[lo:hi])
-        lc = None if self.lcut is None else self.lcut[lo:hi]
+        nl = s.get_nl(gs, or2=dv["or2"][lo:hi])
+        lc = None if dv["lcut"] is None else dv["lcut"][lo:hi]
         # analysis outputs at all levels, written in place into rows lo..hi-1;
         # boundary levels without lMagNlBc have zero VxBt / VxBp
         # (rIter.f90:256-259) and every level's dVSrLM is zero at the
@@ -128,8 +147,10 @@ class RadialLoop:
         full["VSrLM"][0].zero_()
         full["VSrLM"][n - 1].zero_()
         res = dict(out or {})
-        dtrkc, dthkc = s.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, self.radial,
-                                 self.courfac, self.alffac, self.LFfac, self.opm, self.l_cour_alf_damp)
+        dtrkc, dthkc = s.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, dv["radial"],
+                                 self.courfac, self.alffac, self.LFfac, self.opm, self.l_cour_alf_damp,
+                                 dtrkc=torch.full((n,), 1e10, dtype=torch.float64, device=dev),
+                                 dthkc=torch.full((n,), 1e10, dtype=torch.float64, device=dev))
         if self.l_b_nl_cmb:
             res["br_vt_lm_cmb"], res["br_vp_lm_cmb"] = s.get_br_v_bcs(g["brc"][0], g["vtc"][0], g["vpc"][0],
                                                                       self.omega_ma, self.or2[0], 1.0)
@@ -139,10 +160,11 @@ class RadialLoop:
                                                                       self.or2[n - 1], 1.0)
         tdin = {k: spec[k] for k in ("w", "dw", "z")}
         tdin.update({k: full[k] for k in ("AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "VxBrLM", "VxBtLM", "VxBpLM")})
-        td = s.get_td(tdin, self.r, self.cor_fac, lcut=self.lcut, epsc=self.epsc, nbc=self.nbc,
+        td = s.get_td(tdin, dv["r"], self.cor_fac, lcut=dv["lcut"], epsc=dv["epsc"], nbc=dv["nbc"],
                       out={k: res[k] for k in _lib.TD_OUT if k in res} or None)
         res.update(td)
         res["VSrLM"] = full["VSrLM"]
-        res["dtrkc"], res["dthkc"] = dtrkc, dthkc
+        # the stage's one synchronisation: dt_courant wants the steps on the host
+        res["dtrkc"], res["dthkc"] = dtrkc.cpu().numpy(), dthkc.cpu().numpy()
         res["grids"] = g
         return res

@@ -62,6 +62,25 @@ def _is_torch(x) -> bool:
     return t is not None and isinstance(x, t.Tensor)
 
 
+def _per_level(x, np_dtype, n: int, name: str):
+    """(keep-alive object, pointer) of a per-level array (or2, r, lcut, ...):
+    a CUDA tensor is passed as it is (device pointer); anything else as a
+    contiguous numpy array (host pointer, which the library copies through
+    pinned memory without synchronising the stream)."""
+    if x is None:
+        return None, None
+    if _is_torch(x) and x.is_cuda:
+        torch = _torch()
+        t = x.to(dtype=torch.float64 if np_dtype == np.float64 else torch.int32).contiguous()
+        if t.numel() != n:
+            raise ValueError("%s needs %d levels, got %d" % (name, n, t.numel()))
+        return t, t.data_ptr()
+    a = np.ascontiguousarray(x, dtype=np_dtype)
+    if a.size != n:
+        raise ValueError("%s needs %d levels, got %d" % (name, n, a.size))
+    return a, a.ctypes.data
+
+
 class SHT:
     """One transform instance (grid + truncation), the drop-in for ``module sht``."""
 
@@ -282,16 +301,7 @@ class SHT:
 
     # ------------------------------------- the radial loop's transform set
     def _levels(self, arr, n, lcut):
-        lc = None
-        if lcut is not None:
-            if _is_torch(arr):
-                torch = _torch()
-                lc = torch.as_tensor(lcut, dtype=torch.int32, device=arr.device).contiguous()
-                return lc, lc.data_ptr()
-            lc = np.ascontiguousarray(lcut, dtype=np.int32)
-            assert lc.shape == (n,)
-            return lc, lc.ctypes.data
-        return None, None
+        return _per_level(lcut, np.int32, n, "lcut")
 
     def transform_to_grid_space(self, spec: dict, or2=None, lcut=None, out: Optional[dict] = None):
         """rIter.f90:466-622 for many radial levels; `spec` maps the names of
@@ -320,15 +330,7 @@ class SHT:
                 outs[k], _ = self._grid(first, n)
             setattr(a, k, outs[k].data_ptr() if _is_torch(outs[k]) else outs[k].ctypes.data)
         a.grid_ld = self.n_phi_max * self.nlat_padded
-        or2_arr, por2 = (None, None)
-        if or2 is not None:
-            if _is_torch(first):
-                torch = _torch()
-                or2_arr = torch.as_tensor(or2, dtype=torch.float64, device=first.device).contiguous()
-                por2 = or2_arr.data_ptr()
-            else:
-                or2_arr = np.ascontiguousarray(or2, dtype=np.float64)
-                por2 = or2_arr.ctypes.data
+        or2_arr, por2 = _per_level(or2, np.float64, n, "or2")
         lc_arr, plc = self._levels(first, n, lcut)
         check(self._lib.magic_sht_transform_to_grid_space(self._h, n, por2, plc, ctypes.byref(a)))
         return outs
@@ -409,8 +411,7 @@ class SHT:
                 outs[k] = torch.empty_like(keep[0])
             setattr(nl, k, outs[k].data_ptr())
         nl.grid_ld = self.n_phi_max * self.nlat_padded
-        or2_arr = None if or2 is None else np.ascontiguousarray(or2, dtype=np.float64)
-        por2 = None if or2_arr is None else or2_arr.ctypes.data
+        or2_arr, por2 = _per_level(or2, np.float64, n, "or2")
         self._bind_torch_stream()
         check(self._lib.magic_sht_get_nl(self._h, n, por2, ctypes.byref(g), ctypes.byref(nl)))
         return outs
@@ -443,14 +444,12 @@ class SHT:
                 outs[k] = torch.empty_like(keep[0])
             setattr(a, k, outs[k].data_ptr())
         a.spec_ld = self.lm_max
-        r_arr = np.ascontiguousarray(r, dtype=np.float64)
-        lc = None if lcut is None else np.ascontiguousarray(lcut, dtype=np.int32)
-        ep = None if epsc is None else np.ascontiguousarray(epsc, dtype=np.float64)
-        bc = None if nbc is None else np.ascontiguousarray(nbc, dtype=np.int32)
+        r_arr, pr = _per_level(r, np.float64, n, "r")
+        lc, plc = _per_level(lcut, np.int32, n, "lcut")
+        ep, pep = _per_level(epsc, np.float64, n, "epsc")
+        bc, pbc = _per_level(nbc, np.int32, n, "nbc")
         self._bind_torch_stream()
-        check(self._lib.magic_sht_get_td_nbc(self._h, n, r_arr.ctypes.data, None if lc is None else lc.ctypes.data,
-                                             float(cor_fac), None if ep is None else ep.ctypes.data,
-                                             None if bc is None else bc.ctypes.data, ctypes.byref(a)))
+        check(self._lib.magic_sht_get_td_nbc(self._h, n, pr, plc, float(cor_fac), pep, pbc, ctypes.byref(a)))
         return outs
 
     def courant(self, grids: dict, radial: dict, courfac: float, alffac: float, LFfac: float = 1.0,
@@ -459,9 +458,10 @@ class SHT:
         grids ``vrc``, ``vtc``, ``vpc`` (and ``brc``, ``btc``, ``bpc`` for the
         Lorentz-force term; leave them out when it is off), [level][phi][theta].
         ``radial`` holds per-level arrays ``orho1``, ``orho2``, ``or2``,
-        ``or4``, ``delxr2``, ``delxh2``.  Returns (dtrkc, dthkc) as numpy
-        arrays, each the minimum of its start value (1e10 by default, as in
-        the radial loop) and the level's Courant step."""
+        ``or4``, ``delxr2``, ``delxh2`` (numpy or CUDA tensors).  Returns
+        (dtrkc, dthkc), each the minimum of its start value (1e10 by default,
+        as in the radial loop) and the level's Courant step: numpy arrays, or
+        the given CUDA tensors updated in place (then nothing synchronises)."""
         v = grids["vrc"]
         if not (_is_torch(v) and v.is_cuda):
             raise ValueError("courant takes CUDA grids")
@@ -478,16 +478,22 @@ class SHT:
         a.grid_ld = int(v[0].numel())
         rf = {}
         for k in ("orho1", "orho2", "or2", "or4", "delxr2", "delxh2"):
-            rf[k] = np.ascontiguousarray(radial[k], dtype=np.float64)
-            if rf[k].shape != (n,):
-                raise ValueError("radial[%r] needs %d levels" % (k, n))
-            setattr(a, k, rf[k].ctypes.data)
+            rf[k], p = _per_level(radial[k], np.float64, n, "radial[%r]" % k)
+            setattr(a, k, p)
         a.courfac, a.alffac, a.LFfac, a.opm = float(courfac), float(alffac), float(LFfac), float(opm)
         a.l_cour_alf_damp = 1 if alf_damp else 0
-        dr = np.full(n, 1e10) if dtrkc is None else np.array(dtrkc, dtype=np.float64)
-        dh = np.full(n, 1e10) if dthkc is None else np.array(dthkc, dtype=np.float64)
+
+        def start(x):
+            if _is_torch(x) and x.is_cuda:
+                if x.dtype != _torch().float64 or not x.is_contiguous() or x.numel() != n:
+                    raise ValueError("dtrkc / dthkc tensors: contiguous float64, %d levels (updated in place)" % n)
+                return x, x.data_ptr()
+            arr = np.full(n, 1e10) if x is None else np.array(x, dtype=np.float64)
+            return arr, arr.ctypes.data
+        dr, pdr = start(dtrkc)
+        dh, pdh = start(dthkc)
         self._bind_torch_stream()
-        check(self._lib.magic_sht_courant(self._h, n, ctypes.byref(a), dr.ctypes.data, dh.ctypes.data))
+        check(self._lib.magic_sht_courant(self._h, n, ctypes.byref(a), pdr, pdh))
         return dr, dh
 
     # ------------------------------------------------ boundary pieces

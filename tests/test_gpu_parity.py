@@ -623,3 +623,36 @@ def test_get_td_matches_oracle(built, torch, grid):
     for k in _lib.TD_OUT:
         got = out[k].cpu().numpy()
         assert rel_l2(got, ref[k]) < 1e-13, (k, rel_l2(got, ref[k]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["bf16x3", "fp32"])
+def test_get_td_reduced_forms_compute_in_fp32(built, torch, form):
+    """On a reduced-precision handle get_td computes in FP32 (FP64 spectra in
+    and out): every output within 1e-6 relative L2 of the FP64 restatement,
+    not bit-identical to it; device per-level arrays (r, lcut, epsc, nbc)
+    give the same results as host ones."""
+    from oracle import oracle as orc
+    from magic_gb300 import _lib
+    L, minc, N, P = 63, 1, 96, 192
+    s = make(L, minc, N, P, prec=form)
+    n = 4
+    rng = np.random.default_rng(9)
+    spec = {k: torch.from_numpy(rng.standard_normal((n, s.lm_max)) + 1j * rng.standard_normal((n, s.lm_max))).cuda()
+            for k in _lib.TD_IN}
+    r = np.array([0.6, 0.9, 1.2, 1.5])
+    lcut = np.array([L, L - 3, L, 1], dtype=np.int32)
+    epsc = np.array([0.0, 0.5, -1.0, 2.0])
+    nbc = np.array([1, 0, 0, 2], dtype=np.int32)
+    out = s.get_td(spec, r, cor_fac=2.0e3, lcut=lcut, epsc=epsc, nbc=nbc)
+    dev = s.get_td(spec, torch.from_numpy(r).cuda(), cor_fac=2.0e3, lcut=torch.from_numpy(lcut).cuda(),
+                   epsc=torch.from_numpy(epsc).cuda(), nbc=torch.from_numpy(nbc).cuda())
+    torch.cuda.synchronize()
+    ref = orc.get_td({k: v.cpu().numpy() for k, v in spec.items()}, r, 2.0e3, L, minc, lcut, epsc, nbc=nbc)
+    for k in _lib.TD_OUT:
+        got = out[k].cpu().numpy()
+        rows = [i for i in range(n) if nbc[i] == 0 or k == "dVxBhLM"]
+        e = rel_l2(got[rows], ref[k][rows])
+        assert 0.0 < e < 1e-6, (k, e)
+        assert np.array_equal(got[rows], dev[k].cpu().numpy()[rows]), k
+    s.close()
