@@ -182,6 +182,16 @@ def stage_measure(sm, s64, spec, n_levels, steps, hbm):
     ph = sm.phase_times(reset=True)
     sm.set_profiling(False)
     torch.cuda.synchronize()
+    # the same stage captured once as a CUDA graph and replayed (one launch and
+    # the Courant steps' synchronisation per stage)
+    sg = loop.capture(spec)
+    sg.replay()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sg.replay()
+    graph_ms = (time.perf_counter() - t0) / steps * 1e3
+    sg.close()
+    torch.cuda.synchronize()
     sm.device_status()
     N, P, K = sm.nlat_padded, sm.n_phi_max, sm.lm_max
     grid = 8 * N * P
@@ -201,6 +211,9 @@ def stage_measure(sm, s64, spec, n_levels, steps, hbm):
                     "transform_to_lm_space, courant (host dt arrays), get_td with nBc",
             "levels": n_levels, "steps": steps, "ms_per_stage_wall": wall,
             "ms_per_stage_events": statistics.median(per), "levels_per_s": n_levels / (wall * 1e-3),
+            "graph": {"ms_per_stage": graph_ms, "levels_per_s": n_levels / (graph_ms * 1e-3),
+                      "what": "RadialLoop.capture: the stage as one CUDA graph, replayed; wall time per "
+                              "replay including the Courant steps' copy to the host"},
             "kernels": kern,
             "rel_l2_vs_fp64_stage": acc}
 

@@ -116,55 +116,136 @@ class RadialLoop:
             self.s.v_rigid_boundary({"vr": g["vrc"][i], "vt": g["vtc"][i], "vp": g["vpc"][i]},
                                     self.r[i] ** 2, omega, keep_vr)
 
-    def step(self, spec: Dict, out: Optional[Dict] = None) -> Dict:
-        """One stage from the spectra of transform_to_grid_space (``s``, ``p``,
-        ``xi``, ``w`` .. ``dj``; [level][lm] complex CUDA tensors).  Returns
-        the get_td outputs (``dwdt`` .. ``dVxBhLM``), ``VSrLM`` (dVSrLM, 0 at
-        the boundaries), numpy ``dtrkc`` / ``dthkc``, and at conducting
-        boundaries ``br_vt_lm_cmb`` / ``br_vp_lm_cmb`` (or ``_icb``)."""
+    def _lohi(self):
+        return (0, self.n) if self.lMagNlBc else (1, self.n - 1)
+
+    def _alloc(self, spec: Dict, out: Optional[Dict] = None) -> Dict:
+        """Every output of one stage: the synthesis grids, the analysis inputs
+        of the get_nl levels, the analysis outputs, the get_td outputs (from
+        ``out`` where given), the Courant steps and the conducting-boundary
+        spectra."""
         import torch
         s, n = self.s, self.n
-        dv = self._on(spec["w"].device)
-        g = s.transform_to_grid_space(spec, or2=dv["or2"], lcut=dv["lcut"])
+        dev = spec["w"].device
+        f64 = dict(dtype=torch.float64, device=dev)
+        c128 = dict(dtype=torch.complex128, device=dev)
+        src = {"sc": "s", "pc": "p", "xic": "xi", "vrc": "w", "vtc": "w", "vpc": "w", "cvrc": "ddw", "cvtc": "ddw",
+               "cvpc": "ddw", "brc": "b", "btc": "b", "bpc": "b", "cbrc": "ddb", "cbtc": "ddb", "cbpc": "ddb"}
+        grids = {k: torch.empty((n, s.n_phi_max, s.nlat_padded), **f64) for k in _lib.GRID_SPACE_OUT
+                 if spec.get(src[k]) is not None}
+        lo, hi = self._lohi()
+        out = out or {}
+        b = {"device": dev, "grids": grids,
+             "nl": {k: torch.empty((hi - lo, s.n_phi_max, s.nlat_padded), **f64) for k in _lib.LM_SPACE_IN},
+             "lm": {k: torch.empty((n, s.lm_max), **c128) for k in _lib.LM_SPACE_OUT},
+             "td": {k: out[k] if k in out else torch.empty((n, s.lm_max), **c128) for k in _lib.TD_OUT},
+             "dtrkc": torch.empty(n, **f64), "dthkc": torch.empty(n, **f64)}
+        for flag, key in ((self.l_b_nl_cmb, "cmb"), (self.l_b_nl_icb, "icb")):
+            if flag:
+                b[key] = (torch.empty(s.lm_max, **c128), torch.empty(s.lm_max, **c128))
+        return b
+
+    def _enqueue(self, spec: Dict, b: Dict):
+        """Launch one stage into the buffers ``b`` on the current stream: no
+        allocation and no synchronisation (so it can be captured)."""
+        s, n = self.s, self.n
+        dv = self._on(b["device"])
+        g = s.transform_to_grid_space(spec, or2=dv["or2"], lcut=dv["lcut"], out=b["grids"])
         self._boundary_grids(g, 0, self.ktopv, self.omega_ma, self.l_vr_cmb)
         self._boundary_grids(g, n - 1, self.kbotv, self.omega_ic, self.l_vr_icb)
-        lo, hi = (0, n) if self.lMagNlBc else (1, n - 1)
-        gs = {k: v[lo:hi] for k, v in g.items()}
-        nl = s.get_nl(gs, or2=dv["or2"][lo:hi])
+        lo, hi = self._lohi()
+        nl = s.get_nl({k: v[lo:hi] for k, v in g.items()}, or2=dv["or2"][lo:hi], out=b["nl"])
         lc = None if dv["lcut"] is None else dv["lcut"][lo:hi]
         # analysis outputs at all levels, written in place into rows lo..hi-1;
         # boundary levels without lMagNlBc have zero VxBt / VxBp
         # (rIter.f90:256-259) and every level's dVSrLM is zero at the
         # boundaries (get_td.f90:501-507)
-        dev = g["vrc"].device
-        full = {k: torch.empty((n, s.lm_max), dtype=torch.complex128, device=dev) for k in _lib.LM_SPACE_OUT}
+        full = b["lm"]
         s.transform_to_lm_space(nl, lcut=lc, out={k: v[lo:hi] for k, v in full.items()})
-        for k, v in full.items():
+        for v in full.values():
             if lo > 0:
                 v[:lo].zero_()
             if hi < n:
                 v[hi:].zero_()
         full["VSrLM"][0].zero_()
         full["VSrLM"][n - 1].zero_()
-        res = dict(out or {})
-        dtrkc, dthkc = s.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, dv["radial"],
-                                 self.courfac, self.alffac, self.LFfac, self.opm, self.l_cour_alf_damp,
-                                 dtrkc=torch.full((n,), 1e10, dtype=torch.float64, device=dev),
-                                 dthkc=torch.full((n,), 1e10, dtype=torch.float64, device=dev))
+        b["dtrkc"].fill_(1e10)
+        b["dthkc"].fill_(1e10)
+        s.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, dv["radial"],
+                  self.courfac, self.alffac, self.LFfac, self.opm, self.l_cour_alf_damp,
+                  dtrkc=b["dtrkc"], dthkc=b["dthkc"])
         if self.l_b_nl_cmb:
-            res["br_vt_lm_cmb"], res["br_vp_lm_cmb"] = s.get_br_v_bcs(g["brc"][0], g["vtc"][0], g["vpc"][0],
-                                                                      self.omega_ma, self.or2[0], 1.0)
+            s.get_br_v_bcs(g["brc"][0], g["vtc"][0], g["vpc"][0], self.omega_ma, self.or2[0], 1.0, out=b["cmb"])
         if self.l_b_nl_icb:
-            res["br_vt_lm_icb"], res["br_vp_lm_icb"] = s.get_br_v_bcs(g["brc"][n - 1], g["vtc"][n - 1],
-                                                                      g["vpc"][n - 1], self.omega_ic,
-                                                                      self.or2[n - 1], 1.0)
+            s.get_br_v_bcs(g["brc"][n - 1], g["vtc"][n - 1], g["vpc"][n - 1], self.omega_ic, self.or2[n - 1], 1.0,
+                           out=b["icb"])
         tdin = {k: spec[k] for k in ("w", "dw", "z")}
         tdin.update({k: full[k] for k in ("AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "VxBrLM", "VxBtLM", "VxBpLM")})
-        td = s.get_td(tdin, dv["r"], self.cor_fac, lcut=dv["lcut"], epsc=dv["epsc"], nbc=dv["nbc"],
-                      out={k: res[k] for k in _lib.TD_OUT if k in res} or None)
-        res.update(td)
-        res["VSrLM"] = full["VSrLM"]
+        s.get_td(tdin, dv["r"], self.cor_fac, lcut=dv["lcut"], epsc=dv["epsc"], nbc=dv["nbc"], out=b["td"])
+
+    @staticmethod
+    def _result(b: Dict) -> Dict:
+        res = dict(b["td"])
+        res["VSrLM"] = b["lm"]["VSrLM"]
         # the stage's one synchronisation: dt_courant wants the steps on the host
-        res["dtrkc"], res["dthkc"] = dtrkc.cpu().numpy(), dthkc.cpu().numpy()
-        res["grids"] = g
+        res["dtrkc"], res["dthkc"] = b["dtrkc"].cpu().numpy(), b["dthkc"].cpu().numpy()
+        for key in ("cmb", "icb"):
+            if key in b:
+                res["br_vt_lm_" + key], res["br_vp_lm_" + key] = b[key]
+        res["grids"] = b["grids"]
         return res
+
+    def step(self, spec: Dict, out: Optional[Dict] = None) -> Dict:
+        """One stage from the spectra of transform_to_grid_space (``s``, ``p``,
+        ``xi``, ``w`` .. ``dj``; [level][lm] complex CUDA tensors).  Returns
+        the get_td outputs (``dwdt`` .. ``dVxBhLM``, into ``out`` where
+        given), ``VSrLM`` (dVSrLM, 0 at the boundaries), numpy ``dtrkc`` /
+        ``dthkc``, the synthesis ``grids``, and at conducting boundaries
+        ``br_vt_lm_cmb`` / ``br_vp_lm_cmb`` (or ``_icb``)."""
+        b = self._alloc(spec, out)
+        self._enqueue(spec, b)
+        return self._result(b)
+
+    def capture(self, spec: Dict) -> "StageGraph":
+        """The stage on ``spec`` captured once as a CUDA graph (see StageGraph)."""
+        return StageGraph(self, spec)
+
+
+class StageGraph:
+    """One explicit stage captured as a CUDA graph over fixed buffers: every
+    replay reads the spectra ``spec`` given at capture (update them in place
+    between replays) and rewrites the same output tensors, so a stage costs
+    one graph launch and the one synchronisation that brings the Courant
+    steps to the host.  The loop's handle must not be captured elsewhere
+    meanwhile; replay() binds it to the graph's own stream and returns once
+    the stage is complete."""
+
+    def __init__(self, loop: RadialLoop, spec: Dict):
+        import torch
+        self.loop, self.spec = loop, spec
+        s = loop.s
+        self.b = loop._alloc(spec)
+        s.reserve(loop.n)
+        self.stream = torch.cuda.Stream(device=spec["w"].device)
+        self.stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(self.stream):
+            loop._enqueue(spec, self.b)   # sizes the workspace, binds the handle to this stream
+            self.stream.synchronize()
+            s.graph_begin()
+            try:
+                loop._enqueue(spec, self.b)
+            finally:
+                self.graph = s.graph_end()
+
+    def replay(self) -> Dict:
+        import torch
+        with torch.cuda.stream(self.stream):
+            # the handle may have been bound to another stream since the capture
+            self.loop.s._bind_torch_stream()
+            self.loop.s.graph_launch(self.graph)
+            return RadialLoop._result(self.b)
+
+    def close(self):
+        if self.graph is not None:
+            self.loop.s.graph_destroy(self.graph)
+            self.graph = None

@@ -528,10 +528,14 @@ class SHT:
         check(self._lib.magic_sht_v_center_sphere(self._h, px, *[p for _, p in outs]))
         return tuple(o for o, _ in outs)
 
-    def get_br_v_bcs(self, br, vt, vp, omega: float, or2: float, orho1: float):
-        """get_br_v_bcs (nonlinear_bcs.f90:24-69): (br_vt_lm, br_vp_lm)."""
+    def get_br_v_bcs(self, br, vt, vp, omega: float, or2: float, orho1: float, out=None):
+        """get_br_v_bcs (nonlinear_bcs.f90:24-69): (br_vt_lm, br_vp_lm), into
+        the two spectra of ``out`` when given."""
         ins = [self._grid_in(x) for x in (br, vt, vp)]
-        outs = [self._spec(ins[0][0]) for _ in range(2)]
+        if out is None:
+            outs = [self._spec(ins[0][0]) for _ in range(2)]
+        else:
+            outs = [(o, o.data_ptr() if _is_torch(o) else o.ctypes.data) for o in out]
         check(self._lib.magic_sht_get_br_v_bcs(self._h, *[p for _, p in ins], float(omega), float(or2),
                                                float(orho1), *[p for _, p in outs]))
         return tuple(o for o, _ in outs)
