@@ -41,6 +41,19 @@ def test_binding_table_matches_header():
     assert sorted(_lib.SIGNATURES) == declared()
 
 
+def test_phase_numbers_match_python_names():
+    """MAGIC_SHT_PHASE_* in the header index _lib.PHASES (the names
+    SHT.phase_times returns), and MAGIC_SHT_N_PHASES is their count."""
+    from magic_gb300 import _lib
+    src = open(HEADER).read()
+    ph = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"#define MAGIC_SHT_PHASE_(\w+)\s+(\d+)", src)}
+    n = int(re.search(r"#define MAGIC_SHT_N_PHASES\s+(\d+)", src).group(1))
+    assert n == len(_lib.PHASES) == len(ph)
+    assert sorted(ph.values()) == list(range(n))
+    for name, i in ph.items():
+        assert _lib.PHASES[i] == name, (name, i)
+
+
 def test_reference_names_all_present():
     # public names of src/sht_native.f90:16-20
     names = ["scal_to_spat", "scal_to_grad_spat", "pol_to_grad_spat", "torpol_to_spat",
@@ -72,6 +85,7 @@ def _init(lib, **kw):
     (dict(n_phi_max=28), 2),          # 7 is not a factor of the FFT (fft.f90:73)
     (dict(minc=0), 2),                # minc < 1 (truncation.f90:131)
     (dict(l_max=0), 2),
+    (dict(l_max=40000, n_theta_max=60000, n_phi_max=120000), 2),   # l | m << 16 packing of the lm tables
     (dict(n_phi_max=32), 2),          # m_max/minc+1 > n_phi/2: aliasing
     (dict(nlat_padded=40), 2),        # padding smaller than n_theta
     (dict(precision=9), 1),
