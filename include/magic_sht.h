@@ -216,7 +216,8 @@ int magic_sht_get_tuning(const magic_sht_handle* h, magic_sht_tuning* t);
  * curl-form advection, magnetic field and heat equation on, unit physical
  * constants; heatTerms receives the ohmic losses.  Device pointers only,
  * 16-byte aligned, even grid_ld and nlat_padded; or2 = 1/r^2 per level (host
- * or device array of n_levels; NULL = 1).  FP64 in every precision form. */
+ * or device array of n_levels; NULL = 1).  Arithmetic: FP64 on an FP64
+ * handle; FP32 (FP64 grids in and out) on the reduced-precision forms. */
 int magic_sht_get_nl(magic_sht_handle* h, int n_levels, const double* or2, const magic_sht_grid_space_args* g,
                      const magic_sht_lm_space_args* nl);
 
@@ -227,7 +228,9 @@ int magic_sht_get_nl(magic_sht_handle* h, int n_levels, const double* or2, const
  * CorFac), magnetic field and heat equation on, no double-curl form.  Device
  * arrays [n_levels][spec_ld] complex; r (radius), lcut (l_R, NULL = l_max) and
  * epsc (internal heating added to dsdt at l = 0, NULL = 0) are per-level host
- * or device arrays.  dpdt at l = 0 is set to 0 (the reference leaves it). */
+ * or device arrays.  dpdt at l = 0 is set to 0 (the reference leaves it).
+ * Arithmetic: FP64 on an FP64 handle; FP32 (FP64 spectra in and out) on the
+ * reduced-precision forms. */
 typedef struct magic_sht_td_args {
   const double *w, *dw, *z;                                           /* spectra */
   const double *AdvrLM, *AdvtLM, *AdvpLM, *VStLM, *VxBrLM, *VxBtLM, *VxBpLM;  /* analysis out */
@@ -251,7 +254,9 @@ int magic_sht_get_td_nbc(magic_sht_handle* h, int n_levels, const double* r, con
  * (level stride grid_ld); br = bt = bp = NULL drops the Lorentz-force term
  * (l_mag_LF off or l_mag_kin).  Radial functions: arrays of n_levels (host or
  * device); dtrkc, dthkc: in/out arrays of n_levels (host or device; the
- * radial loop starts them at 1e10).  FP64 in every precision form. */
+ * radial loop starts them at 1e10).  The maxima are the FP64 values of the
+ * reference's expressions in every precision form (an FP32 estimate only
+ * selects the points that can hold them). */
 typedef struct magic_sht_courant_args {
   const double *vr, *vt, *vp, *br, *bt, *bp;
   long long grid_ld;

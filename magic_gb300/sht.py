@@ -388,7 +388,9 @@ class SHT:
         (get_nl.f90:213-441, rIter.f90:650-655): from the synthesis grids
         (``vrc`` .. ``cbpc``, ``sc``; CUDA tensors [level][phi][theta]) the
         analysis inputs ``Advr`` .. ``heatTerms`` (Boussinesq, curl-form
-        advection, unit constants, heatTerms = ohmic losses)."""
+        advection, unit constants, heatTerms = ohmic losses).  ``or2``: per
+        level, numpy or CUDA.  FP64 arithmetic on an FP64 handle, FP32 on the
+        reduced forms."""
         import torch
         missing = [k for k in _lib.NL_IN if grids.get(k) is None]
         if missing:
@@ -423,7 +425,9 @@ class SHT:
         (``AdvrLM`` .. ``VxBpLM``) the outputs ``dwdt``, ``dzdt``, ``dpdt``,
         ``dsdt``, ``dbdt``, ``djdt``, ``dVxBhLM`` ([level][lm] complex).
         ``nbc`` (per level, nBc of the radial loop): at a level with nbc != 0
-        only ``dVxBhLM`` is written."""
+        only ``dVxBhLM`` is written.  Per-level arrays (``r``, ``lcut``,
+        ``epsc``, ``nbc``): numpy or CUDA.  FP64 arithmetic on an FP64 handle,
+        FP32 on the reduced forms."""
         import torch
         missing = [k for k in _lib.TD_IN if spec.get(k) is None]
         if missing:
