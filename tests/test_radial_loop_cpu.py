@@ -44,3 +44,46 @@ def test_rejects_bad_boundaries_and_too_few_levels():
         RadialLoop(_Handle(), np.linspace(1.5, 0.5, 5), cor_fac=1.0, ktopv=3)
     with pytest.raises(ValueError):
         RadialLoop(_Handle(), np.array([1.5, 0.5]), cor_fac=1.0)
+
+
+class _Sized(_Handle):  # sizes _alloc reads
+    n_phi_max, nlat_padded, lm_max = 8, 6, 10
+
+
+@pytest.mark.parametrize("ktopv,cond", [(2, False), (1, True)])
+def test_stage_buffers(ktopv, cond):
+    """Every output buffer of a stage, allocated once per stage (and once for
+    a captured stage): synthesis grids of the given spectra, analysis inputs
+    of the get_nl levels (interior only unless lMagNlBc), analysis and get_td
+    outputs at all levels, Courant steps, conducting-boundary spectra; get_td
+    outputs given by the caller are used as they are."""
+    import torch
+    from magic_gb300._lib import GRID_SPACE_IN, GRID_SPACE_OUT, LM_SPACE_IN, LM_SPACE_OUT, TD_OUT
+    n = 5
+    loop = RadialLoop(_Sized(), np.linspace(1.5, 0.5, n), cor_fac=1.0, ktopv=ktopv, l_cond_ma=cond)
+    spec = {k: torch.zeros((n, 10), dtype=torch.complex128) for k in GRID_SPACE_IN if k != "xi"}
+    mine = torch.zeros((n, 10), dtype=torch.complex128)
+    b = loop._alloc(spec, out={"dwdt": mine})
+    assert set(b["grids"]) == set(GRID_SPACE_OUT) - {"xic"}
+    assert all(v.shape == (n, 8, 6) and v.dtype == torch.float64 for v in b["grids"].values())
+    lo, hi = loop._lohi()
+    assert (lo, hi) == ((0, n) if loop.lMagNlBc else (1, n - 1))
+    assert set(b["nl"]) == set(LM_SPACE_IN) and all(v.shape == (hi - lo, 8, 6) for v in b["nl"].values())
+    assert set(b["lm"]) == set(LM_SPACE_OUT) and set(b["td"]) == set(TD_OUT)
+    assert b["td"]["dwdt"] is mine
+    assert b["dtrkc"].shape == (n,) and b["dthkc"].shape == (n,)
+    assert ("cmb" in b) == loop.l_b_nl_cmb and "icb" not in b
+
+
+def test_per_level_arrays():
+    """Per-level arguments: numpy (and CPU tensors) pass as host pointers of
+    the right type, a wrong length is refused."""
+    import torch
+    from magic_gb300.sht import _per_level
+    a, p = _per_level([1, 2, 3], np.int32, 3, "lcut")
+    assert a.dtype == np.int32 and a.flags.c_contiguous and p == a.ctypes.data
+    a, p = _per_level(torch.arange(4, dtype=torch.float32), np.float64, 4, "or2")
+    assert a.dtype == np.float64 and list(a) == [0.0, 1.0, 2.0, 3.0]
+    assert _per_level(None, np.float64, 3, "epsc") == (None, None)
+    with pytest.raises(ValueError):
+        _per_level(np.ones(4), np.float64, 3, "r")
