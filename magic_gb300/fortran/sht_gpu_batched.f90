@@ -1,0 +1,270 @@
+module sht_gpu_batched
+   !
+   ! The batched entry points of the GB300 library, for a radial loop that
+   ! keeps its levels on the GPU: the radial loop's transform set for all of a
+   ! rank's levels in one call each (transform_to_grid_space,
+   ! rIter.f90:466-622; transform_to_lm_space, rIter.f90:624-712), the
+   ! grid-space products (get_nl.f90:213-441), the spectral assembly with the
+   ! boundary flags (get_td.f90:133-619) and the new time step
+   ! (dt_courant, courant.f90:280-346).
+   !
+   ! Spectral arrays are the reference's R-distributed fields
+   ! f_Rloc(lm_max, nRstart:nRstop) (one column per level); grids are
+   ! (nlat_padded, n_phi_max, levels), i.e. the per-level grids of
+   ! grid_space_arrays stacked over the levels.  Host arrays are staged by the
+   ! library and the call returns with its results; device arrays (CUDA
+   ! Fortran `device` arrays, or OpenACC `host_data use_device`) are used in
+   ! place and the call is asynchronous on the library's stream.  A non-zero
+   ! status becomes abortRun through module sht.
+   !
+   use iso_c_binding
+   use precision_mod, only: cp
+   use sht, only: sht_handle, sht_check
+
+   implicit none
+
+   private
+
+   type, bind(C) :: magic_sht_grid_space_args
+      type(c_ptr) :: s, p, xi, w, dw, ddw, z, dz, b, db, ddb, aj, dj
+      integer(c_long_long) :: spec_ld
+      type(c_ptr) :: sc, pc, xic, vrc, vtc, vpc, cvrc, cvtc, cvpc, brc, btc, bpc, cbrc, cbtc, cbpc
+      integer(c_long_long) :: grid_ld
+   end type magic_sht_grid_space_args
+
+   type, bind(C) :: magic_sht_lm_space_args
+      type(c_ptr) :: Advr, Advt, Advp, VSr, VSt, VSp, VxBr, VxBt, VxBp, heatTerms
+      integer(c_long_long) :: grid_ld
+      type(c_ptr) :: AdvrLM, AdvtLM, AdvpLM, VSrLM, VStLM, VSpLM, VxBrLM, VxBtLM, VxBpLM, heatTermsLM
+      integer(c_long_long) :: spec_ld
+   end type magic_sht_lm_space_args
+
+   type, bind(C) :: magic_sht_td_args
+      type(c_ptr) :: w, dw, z, AdvrLM, AdvtLM, AdvpLM, VStLM, VxBrLM, VxBtLM, VxBpLM
+      type(c_ptr) :: dwdt, dzdt, dpdt, dsdt, dbdt, djdt, dVxBhLM
+      integer(c_long_long) :: spec_ld
+   end type magic_sht_td_args
+
+   interface
+      integer(c_int) function c_to_grid(h, n, or2, lcut, a) bind(C, name='magic_sht_transform_to_grid_space')
+         import :: c_int, c_ptr, magic_sht_grid_space_args
+         type(c_ptr), value :: h
+         integer(c_int), value :: n
+         type(c_ptr), value :: or2, lcut
+         type(magic_sht_grid_space_args), intent(in) :: a
+      end function
+      integer(c_int) function c_to_lm(h, n, lcut, a) bind(C, name='magic_sht_transform_to_lm_space')
+         import :: c_int, c_ptr, magic_sht_lm_space_args
+         type(c_ptr), value :: h
+         integer(c_int), value :: n
+         type(c_ptr), value :: lcut
+         type(magic_sht_lm_space_args), intent(in) :: a
+      end function
+      integer(c_int) function c_get_nl(h, n, or2, g, nl) bind(C, name='magic_sht_get_nl')
+         import :: c_int, c_ptr, magic_sht_grid_space_args, magic_sht_lm_space_args
+         type(c_ptr), value :: h
+         integer(c_int), value :: n
+         type(c_ptr), value :: or2
+         type(magic_sht_grid_space_args), intent(in) :: g
+         type(magic_sht_lm_space_args), intent(in) :: nl
+      end function
+      integer(c_int) function c_get_td_nbc(h, n, r, lcut, cor_fac, epsc, nbc, a) &
+            &        bind(C, name='magic_sht_get_td_nbc')
+         import :: c_int, c_ptr, c_double, magic_sht_td_args
+         type(c_ptr), value :: h
+         integer(c_int), value :: n
+         type(c_ptr), value :: r, lcut
+         real(c_double), value :: cor_fac
+         type(c_ptr), value :: epsc, nbc
+         type(magic_sht_td_args), intent(in) :: a
+      end function
+      integer(c_int) function c_dt_courant(n, dtrkc, dthkc, dt, dtMax, l_new_dt, dt_new) &
+            &        bind(C, name='magic_sht_dt_courant')
+         import :: c_int, c_double
+         integer(c_int), value :: n
+         real(c_double), intent(in) :: dtrkc(*), dthkc(*)
+         real(c_double), value :: dt, dtMax
+         integer(c_int), intent(out) :: l_new_dt
+         real(c_double), intent(out) :: dt_new
+      end function
+      integer(c_int) function c_reserve(h, n) bind(C, name='magic_sht_reserve')
+         import :: c_int, c_ptr
+         type(c_ptr), value :: h
+         integer(c_int), value :: n
+      end function
+   end interface
+
+   public :: transform_to_grid_space_gpu, transform_to_lm_space_gpu, get_nl_gpu, get_td_gpu, &
+        &    dt_courant_gpu, reserve_levels_gpu
+
+contains
+
+   subroutine transform_to_grid_space_gpu(or2, lcut, w, dw, ddw, z, dz, vrc, vtc, vpc, cvrc, cvtc, cvpc, &
+              &                           s, p, xi, b, db, ddb, aj, dj, sc, pc, xic, brc, btc, bpc,    &
+              &                           cbrc, cbtc, cbpc)
+      ! transform_to_grid_space of every level (column) of the spectra at
+      ! once: or2(nR) = 1/r^2, lcut(nR) = l_R.  The velocity set is always
+      ! transformed; s, p, xi (scalars) and b, db, ddb, aj, dj (magnetic
+      ! field) with their grids only when present.
+      real(cp),       target, contiguous, intent(in) :: or2(:)
+      integer(c_int), target, contiguous, intent(in) :: lcut(:)
+      complex(cp), target, contiguous, intent(in) :: w(:,:), dw(:,:), ddw(:,:), z(:,:), dz(:,:)
+      real(cp), target, contiguous, intent(out) :: vrc(:,:,:), vtc(:,:,:), vpc(:,:,:)
+      real(cp), target, contiguous, intent(out) :: cvrc(:,:,:), cvtc(:,:,:), cvpc(:,:,:)
+      complex(cp), target, contiguous, optional, intent(in) :: s(:,:), p(:,:), xi(:,:)
+      complex(cp), target, contiguous, optional, intent(in) :: b(:,:), db(:,:), ddb(:,:), aj(:,:), dj(:,:)
+      real(cp), target, contiguous, optional, intent(out) :: sc(:,:,:), pc(:,:,:), xic(:,:,:)
+      real(cp), target, contiguous, optional, intent(out) :: brc(:,:,:), btc(:,:,:), bpc(:,:,:)
+      real(cp), target, contiguous, optional, intent(out) :: cbrc(:,:,:), cbtc(:,:,:), cbpc(:,:,:)
+      type(magic_sht_grid_space_args) :: a
+
+      call null_grid_args(a)
+      a%w = c_loc(w); a%dw = c_loc(dw); a%ddw = c_loc(ddw); a%z = c_loc(z); a%dz = c_loc(dz)
+      a%vrc = c_loc(vrc); a%vtc = c_loc(vtc); a%vpc = c_loc(vpc)
+      a%cvrc = c_loc(cvrc); a%cvtc = c_loc(cvtc); a%cvpc = c_loc(cvpc)
+      if ( present(s) .and. present(sc) ) then
+         a%s = c_loc(s); a%sc = c_loc(sc)
+      end if
+      if ( present(p) .and. present(pc) ) then
+         a%p = c_loc(p); a%pc = c_loc(pc)
+      end if
+      if ( present(xi) .and. present(xic) ) then
+         a%xi = c_loc(xi); a%xic = c_loc(xic)
+      end if
+      ! B from b, db, aj (rIter.f90:606); curl B from b, ddb, aj, dj (:610)
+      if ( present(b) .and. present(db) .and. present(aj) .and. present(brc) .and. &
+           present(btc) .and. present(bpc) ) then
+         a%b = c_loc(b); a%db = c_loc(db); a%aj = c_loc(aj)
+         a%brc = c_loc(brc); a%btc = c_loc(btc); a%bpc = c_loc(bpc)
+      end if
+      if ( present(b) .and. present(ddb) .and. present(aj) .and. present(dj) .and. present(cbrc) .and. &
+           present(cbtc) .and. present(cbpc) ) then
+         a%b = c_loc(b); a%ddb = c_loc(ddb); a%aj = c_loc(aj); a%dj = c_loc(dj)
+         a%cbrc = c_loc(cbrc); a%cbtc = c_loc(cbtc); a%cbpc = c_loc(cbpc)
+      end if
+      a%spec_ld = size(w, 1, kind=c_long_long)
+      a%grid_ld = size(vrc, 1, kind=c_long_long) * size(vrc, 2, kind=c_long_long)
+      call sht_check(c_to_grid(sht_handle(), int(size(w, 2), c_int), c_loc(or2), c_loc(lcut), a))
+   end subroutine transform_to_grid_space_gpu
+
+   subroutine transform_to_lm_space_gpu(lcut, Advr, Advt, Advp, VSr, VSt, VSp, VxBr, VxBt, VxBp, heatTerms, &
+              &                         AdvrLM, AdvtLM, AdvpLM, VSrLM, VStLM, VSpLM, VxBrLM, VxBtLM,      &
+              &                         VxBpLM, heatTermsLM)
+      ! transform_to_lm_space of every level (third dimension of the grids)
+      ! at once; lcut(nR) = l_R.
+      integer(c_int), target, contiguous, intent(in) :: lcut(:)
+      real(cp), target, contiguous, intent(in) :: Advr(:,:,:), Advt(:,:,:), Advp(:,:,:)
+      real(cp), target, contiguous, intent(in) :: VSr(:,:,:), VSt(:,:,:), VSp(:,:,:)
+      real(cp), target, contiguous, intent(in) :: VxBr(:,:,:), VxBt(:,:,:), VxBp(:,:,:), heatTerms(:,:,:)
+      complex(cp), target, contiguous, intent(out) :: AdvrLM(:,:), AdvtLM(:,:), AdvpLM(:,:)
+      complex(cp), target, contiguous, intent(out) :: VSrLM(:,:), VStLM(:,:), VSpLM(:,:)
+      complex(cp), target, contiguous, intent(out) :: VxBrLM(:,:), VxBtLM(:,:), VxBpLM(:,:), heatTermsLM(:,:)
+      type(magic_sht_lm_space_args) :: a
+
+      a%Advr = c_loc(Advr); a%Advt = c_loc(Advt); a%Advp = c_loc(Advp)
+      a%VSr = c_loc(VSr); a%VSt = c_loc(VSt); a%VSp = c_loc(VSp)
+      a%VxBr = c_loc(VxBr); a%VxBt = c_loc(VxBt); a%VxBp = c_loc(VxBp); a%heatTerms = c_loc(heatTerms)
+      a%grid_ld = size(Advr, 1, kind=c_long_long) * size(Advr, 2, kind=c_long_long)
+      a%AdvrLM = c_loc(AdvrLM); a%AdvtLM = c_loc(AdvtLM); a%AdvpLM = c_loc(AdvpLM)
+      a%VSrLM = c_loc(VSrLM); a%VStLM = c_loc(VStLM); a%VSpLM = c_loc(VSpLM)
+      a%VxBrLM = c_loc(VxBrLM); a%VxBtLM = c_loc(VxBtLM); a%VxBpLM = c_loc(VxBpLM)
+      a%heatTermsLM = c_loc(heatTermsLM)
+      a%spec_ld = size(AdvrLM, 1, kind=c_long_long)
+      call sht_check(c_to_lm(sht_handle(), int(size(Advr, 3), c_int), c_loc(lcut), a))
+   end subroutine transform_to_lm_space_gpu
+
+   subroutine get_nl_gpu(or2, vrc, vtc, vpc, cvrc, cvtc, cvpc, brc, btc, bpc, cbrc, cbtc, cbpc, sc, &
+              &          Advr, Advt, Advp, VSr, VSt, VSp, VxBr, VxBt, VxBp, heatTerms)
+      ! get_nl of every level (third dimension) at once: Boussinesq, curl-form
+      ! advection, magnetic field and heat equation, unit physical constants;
+      ! heatTerms receives the ohmic losses.  Device arrays only (16-byte
+      ! aligned, even nlat_padded); or2(nR) = 1/r^2 (host or device).
+      real(cp), target, contiguous, intent(in) :: or2(:)
+      real(cp), target, contiguous, intent(in) :: vrc(:,:,:), vtc(:,:,:), vpc(:,:,:)
+      real(cp), target, contiguous, intent(in) :: cvrc(:,:,:), cvtc(:,:,:), cvpc(:,:,:)
+      real(cp), target, contiguous, intent(in) :: brc(:,:,:), btc(:,:,:), bpc(:,:,:)
+      real(cp), target, contiguous, intent(in) :: cbrc(:,:,:), cbtc(:,:,:), cbpc(:,:,:), sc(:,:,:)
+      real(cp), target, contiguous, intent(out) :: Advr(:,:,:), Advt(:,:,:), Advp(:,:,:)
+      real(cp), target, contiguous, intent(out) :: VSr(:,:,:), VSt(:,:,:), VSp(:,:,:)
+      real(cp), target, contiguous, intent(out) :: VxBr(:,:,:), VxBt(:,:,:), VxBp(:,:,:), heatTerms(:,:,:)
+      type(magic_sht_grid_space_args) :: g
+      type(magic_sht_lm_space_args) :: nl
+
+      call null_grid_args(g)
+      g%vrc = c_loc(vrc); g%vtc = c_loc(vtc); g%vpc = c_loc(vpc)
+      g%cvrc = c_loc(cvrc); g%cvtc = c_loc(cvtc); g%cvpc = c_loc(cvpc)
+      g%brc = c_loc(brc); g%btc = c_loc(btc); g%bpc = c_loc(bpc)
+      g%cbrc = c_loc(cbrc); g%cbtc = c_loc(cbtc); g%cbpc = c_loc(cbpc); g%sc = c_loc(sc)
+      g%grid_ld = size(vrc, 1, kind=c_long_long) * size(vrc, 2, kind=c_long_long)
+      ! the analysis inputs are this call's outputs
+      nl%Advr = c_loc(Advr); nl%Advt = c_loc(Advt); nl%Advp = c_loc(Advp)
+      nl%VSr = c_loc(VSr); nl%VSt = c_loc(VSt); nl%VSp = c_loc(VSp)
+      nl%VxBr = c_loc(VxBr); nl%VxBt = c_loc(VxBt); nl%VxBp = c_loc(VxBp); nl%heatTerms = c_loc(heatTerms)
+      nl%grid_ld = size(Advr, 1, kind=c_long_long) * size(Advr, 2, kind=c_long_long)
+      nl%AdvrLM = c_null_ptr; nl%AdvtLM = c_null_ptr; nl%AdvpLM = c_null_ptr
+      nl%VSrLM = c_null_ptr; nl%VStLM = c_null_ptr; nl%VSpLM = c_null_ptr
+      nl%VxBrLM = c_null_ptr; nl%VxBtLM = c_null_ptr; nl%VxBpLM = c_null_ptr; nl%heatTermsLM = c_null_ptr
+      nl%spec_ld = 0
+      call sht_check(c_get_nl(sht_handle(), int(size(vrc, 3), c_int), c_loc(or2), g, nl))
+   end subroutine get_nl_gpu
+
+   subroutine get_td_gpu(r, lcut, cor_fac, epsc, nbc, w, dw, z, AdvrLM, AdvtLM, AdvpLM, VStLM, VxBrLM, VxBtLM, &
+              &          VxBpLM, dwdt, dzdt, dpdt, dsdt, dbdt, djdt, dVxBhLM)
+      ! get_dwdt, get_dzdt, get_dpdt, get_dsdt and get_dbdt of every level
+      ! (column) at once: Boussinesq, Coriolis force (cor_fac = CorFac),
+      ! magnetic field and heat equation, no double-curl form.  nbc(nR) is the
+      ! radial loop's nBc: at a level with nbc /= 0 only dVxBhLM is written.
+      ! epsc(nR): internal heating added to dsdt at l = 0.  Device spectra.
+      real(cp),       target, contiguous, intent(in) :: r(:), epsc(:)
+      integer(c_int), target, contiguous, intent(in) :: lcut(:), nbc(:)
+      real(cp), intent(in) :: cor_fac
+      complex(cp), target, contiguous, intent(in) :: w(:,:), dw(:,:), z(:,:)
+      complex(cp), target, contiguous, intent(in) :: AdvrLM(:,:), AdvtLM(:,:), AdvpLM(:,:), VStLM(:,:)
+      complex(cp), target, contiguous, intent(in) :: VxBrLM(:,:), VxBtLM(:,:), VxBpLM(:,:)
+      complex(cp), target, contiguous, intent(inout) :: dwdt(:,:), dzdt(:,:), dpdt(:,:), dsdt(:,:)
+      complex(cp), target, contiguous, intent(inout) :: dbdt(:,:), djdt(:,:), dVxBhLM(:,:)
+      type(magic_sht_td_args) :: a
+
+      a%w = c_loc(w); a%dw = c_loc(dw); a%z = c_loc(z)
+      a%AdvrLM = c_loc(AdvrLM); a%AdvtLM = c_loc(AdvtLM); a%AdvpLM = c_loc(AdvpLM); a%VStLM = c_loc(VStLM)
+      a%VxBrLM = c_loc(VxBrLM); a%VxBtLM = c_loc(VxBtLM); a%VxBpLM = c_loc(VxBpLM)
+      a%dwdt = c_loc(dwdt); a%dzdt = c_loc(dzdt); a%dpdt = c_loc(dpdt); a%dsdt = c_loc(dsdt)
+      a%dbdt = c_loc(dbdt); a%djdt = c_loc(djdt); a%dVxBhLM = c_loc(dVxBhLM)
+      a%spec_ld = size(w, 1, kind=c_long_long)
+      call sht_check(c_get_td_nbc(sht_handle(), int(size(w, 2), c_int), c_loc(r), c_loc(lcut), &
+           &                      real(cor_fac, c_double), c_loc(epsc), c_loc(nbc), a))
+   end subroutine get_td_gpu
+
+   subroutine dt_courant_gpu(dtrkc, dthkc, dt, dtMax, l_new_dt, dt_new)
+      ! dt_courant without its log lines (host arrays of all levels)
+      real(cp), intent(in) :: dtrkc(:), dthkc(:), dt, dtMax
+      logical,  intent(out) :: l_new_dt
+      real(cp), intent(out) :: dt_new
+      integer(c_int) :: flag
+      real(c_double) :: dnew
+      call sht_check(c_dt_courant(int(size(dtrkc), c_int), dtrkc, dthkc, real(dt, c_double), &
+           &                      real(dtMax, c_double), flag, dnew))
+      l_new_dt = flag /= 0
+      dt_new = dnew
+   end subroutine dt_courant_gpu
+
+   subroutine reserve_levels_gpu(n_levels)
+      ! size the library's workspace and tensor-core data images for batches
+      ! of n_levels levels ahead of the first call (and of graph capture)
+      integer, intent(in) :: n_levels
+      call sht_check(c_reserve(sht_handle(), int(n_levels, c_int)))
+   end subroutine reserve_levels_gpu
+
+   subroutine null_grid_args(a)
+      type(magic_sht_grid_space_args), intent(out) :: a
+      a%s = c_null_ptr; a%p = c_null_ptr; a%xi = c_null_ptr; a%w = c_null_ptr; a%dw = c_null_ptr
+      a%ddw = c_null_ptr; a%z = c_null_ptr; a%dz = c_null_ptr; a%b = c_null_ptr; a%db = c_null_ptr
+      a%ddb = c_null_ptr; a%aj = c_null_ptr; a%dj = c_null_ptr
+      a%sc = c_null_ptr; a%pc = c_null_ptr; a%xic = c_null_ptr; a%vrc = c_null_ptr; a%vtc = c_null_ptr
+      a%vpc = c_null_ptr; a%cvrc = c_null_ptr; a%cvtc = c_null_ptr; a%cvpc = c_null_ptr
+      a%brc = c_null_ptr; a%btc = c_null_ptr; a%bpc = c_null_ptr; a%cbrc = c_null_ptr
+      a%cbtc = c_null_ptr; a%cbpc = c_null_ptr
+      a%spec_ld = 0; a%grid_ld = 0
+   end subroutine null_grid_args
+
+end module sht_gpu_batched
