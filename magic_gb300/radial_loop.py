@@ -222,8 +222,16 @@ class StageGraph:
 
     def __init__(self, loop: RadialLoop, spec: Dict):
         import torch
-        self.loop, self.spec = loop, spec
         s = loop.s
+        for k, v in spec.items():
+            if v is None:
+                continue
+            if not (isinstance(v, torch.Tensor) and v.is_cuda and v.is_contiguous() and v.dtype == torch.complex128
+                    and tuple(v.shape) == (loop.n, s.lm_max)):
+                raise ValueError("captured spectra must be contiguous complex128 CUDA tensors of shape "
+                                 "(%d, %d): %r" % (loop.n, s.lm_max, k))
+        self.graph = None
+        self.loop, self.spec = loop, spec
         self.b = loop._alloc(spec)
         s.reserve(loop.n)
         self.stream = torch.cuda.Stream(device=spec["w"].device)

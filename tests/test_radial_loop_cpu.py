@@ -87,3 +87,14 @@ def test_per_level_arrays():
     assert _per_level(None, np.float64, 3, "epsc") == (None, None)
     with pytest.raises(ValueError):
         _per_level(np.ones(4), np.float64, 3, "r")
+
+
+def test_capture_refuses_spectra_it_cannot_read_in_place():
+    """A captured stage reads the spectra by address at every replay: host,
+    non-contiguous or wrongly shaped spectra are refused before any launch."""
+    import torch
+    from magic_gb300.radial_loop import StageGraph
+    n = 5
+    loop = RadialLoop(_Sized(), np.linspace(1.5, 0.5, n), cor_fac=1.0)
+    with pytest.raises(ValueError):
+        StageGraph(loop, {"w": torch.zeros((n, 10), dtype=torch.complex128)})  # host tensor
