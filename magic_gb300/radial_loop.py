@@ -143,7 +143,18 @@ class RadialLoop:
         for flag, key in ((self.l_b_nl_cmb, "cmb"), (self.l_b_nl_icb, "icb")):
             if flag:
                 b[key] = (torch.empty(s.lm_max, **c128), torch.empty(s.lm_max, **c128))
+        if self._rigid_kept_vr():
+            b["zero_grid"] = torch.zeros((1, s.n_phi_max, s.nlat_padded), **f64)
         return b
+
+    def _rigid_kept_vr(self):
+        """Boundary levels whose products get_nl forms at all (lMagNlBc) and
+        whose grid keeps a radial velocity at a rigid boundary (l_vr_cmb /
+        l_vr_icb)."""
+        if not self.lMagNlBc:
+            return []
+        return [i for i, kind, keep in ((0, self.ktopv, self.l_vr_cmb), (self.n - 1, self.kbotv, self.l_vr_icb))
+                if kind == 2 and keep]
 
     def _enqueue(self, spec: Dict, b: Dict):
         """Launch one stage into the buffers ``b`` on the current stream: no
@@ -155,6 +166,14 @@ class RadialLoop:
         self._boundary_grids(g, n - 1, self.kbotv, self.omega_ic, self.l_vr_icb)
         lo, hi = self._lohi()
         nl = s.get_nl({k: v[lo:hi] for k, v in g.items()}, or2=dv["or2"][lo:hi], out=b["nl"])
+        # at a rigid boundary the reference forms V x B with vr = vt = 0 (nBc = 2
+        # branch of get_nl.f90:391-395: VxBt = or4 vp br, VxBp = 0); where the grid
+        # keeps its radial velocity, that level's products come from a zero vr grid
+        # (the other products of a boundary level are not used)
+        for i in self._rigid_kept_vr():
+            gi = {k: v[i:i + 1] for k, v in g.items()}
+            gi["vrc"] = b["zero_grid"]
+            s.get_nl(gi, or2=dv["or2"][i:i + 1], out={k: v[i - lo:i - lo + 1] for k, v in b["nl"].items()})
         lc = None if dv["lcut"] is None else dv["lcut"][lo:hi]
         # analysis outputs at all levels, written in place into rows lo..hi-1;
         # boundary levels without lMagNlBc have zero VxBt / VxBp

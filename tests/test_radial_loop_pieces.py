@@ -164,6 +164,7 @@ def test_get_td_boundary_levels(built, torch):
 @pytest.mark.parametrize("cfg", [
     dict(ktopv=2, kbotv=2, omega_ma=0.3, omega_ic=-0.2),                    # rigid, lMagNlBc off
     dict(ktopv=1, kbotv=1, l_cond_ma=True, omega_ma=0.25),                  # stress-free, conducting mantle
+    dict(ktopv=2, kbotv=1, l_rot_ma=True, l_vr_cmb=True, omega_ma=0.3),     # rigid with vr kept, lMagNlBc
 ])
 def test_radial_loop_stage_matches_oracle(built, torch, oracle_mod, cfg):
     """One explicit stage of the radial loop (rIter.f90:94-464) over five
@@ -187,8 +188,8 @@ def test_radial_loop_stage_matches_oracle(built, torch, oracle_mod, cfg):
     # ---- the same stage from the oracle
     or2 = 1.0 / r ** 2
     g = _radial_set_ref(o, spec_np, or2, lcut)
-    for i, kind, om, kv in ((0, cfg["ktopv"], cfg.get("omega_ma", 0.0), False),
-                            (n - 1, cfg["kbotv"], cfg.get("omega_ic", 0.0), False)):
+    for i, kind, om, kv in ((0, cfg["ktopv"], cfg.get("omega_ma", 0.0), cfg.get("l_vr_cmb", False)),
+                            (n - 1, cfg["kbotv"], cfg.get("omega_ic", 0.0), cfg.get("l_vr_icb", False))):
         if kind == 1:
             g["vrc"][i] = 0.0
         else:
@@ -196,6 +197,14 @@ def test_radial_loop_stage_matches_oracle(built, torch, oracle_mod, cfg):
             g["vrc"][i], g["vtc"][i], g["vpc"][i] = b["vr"], b["vt"], b["vp"]
     lo, hi = (0, n) if loop.lMagNlBc else (1, n - 1)
     nl = orc.get_nl({k: v[lo:hi] for k, v in g.items()}, or2[lo:hi], N)
+    # a rigid boundary's V x B has vr = vt = 0 in the reference (get_nl.f90:391-395)
+    for i, kind, kv in ((0, cfg["ktopv"], cfg.get("l_vr_cmb", False)), (n - 1, cfg["kbotv"], cfg.get("l_vr_icb", False))):
+        if loop.lMagNlBc and kind == 2 and kv:
+            gz = {k: np.array(v[i:i + 1]) for k, v in g.items()}
+            gz["vrc"][:] = 0.0
+            nz = orc.get_nl(gz, or2[i:i + 1], N)
+            for k in nz:
+                nl[k][i - lo] = nz[k][0]
     lm = {k: np.zeros((n, s.lm_max), dtype=np.complex128) for k in
           ("AdvrLM", "AdvtLM", "AdvpLM", "VSrLM", "VStLM", "VSpLM", "VxBrLM", "VxBtLM", "VxBpLM")}
     for j, i in enumerate(range(lo, hi)):
