@@ -296,6 +296,17 @@ int magic_sht_v_center_sphere(magic_sht_handle* h, const double* ddw, double* vr
  * sin^2(theta)) with fac = or2 orho1, into br_vt_lm, br_vp_lm (lm_max complex). */
 int magic_sht_get_br_v_bcs(magic_sht_handle* h, const double* br, const double* vt, const double* vp, double omega,
                            double or2, double orho1, double* br_vt_lm, double* br_vp_lm);
+/* ---- Lorentz torque on a rotating, conducting mantle or inner core
+ * (get_lorentz_torque, outRot.f90:423-483) from one boundary level's grids
+ * br (r^2 B_r) and bp (r sin(theta) B_phi) as transform_to_grid_space writes
+ * them: *torque = LFfac 2 pi / n_phi_max times the sum over the grid of
+ * gauss(theta) (br - b0 cos(theta)) bp, with b0 = 2 BIC r_icb^2 (times
+ * r_icb / r_cmb at the outer boundary) in the Grenoble setup and 0 otherwise.
+ * Grids and *torque host or device.  The radial loop uses the value at the
+ * inner boundary and minus the value at the outer one (rIter.f90:278-292,
+ * :462). */
+int magic_sht_lorentz_torque(magic_sht_handle* h, const double* br, const double* bp, double LFfac, double b0,
+                             double* torque);
 /* get_b_nl_bcs (:71-118): b_nl_bc = -fac br_vt_lm and aj_nl_bc = -fac br_vp_lm
  * for l > 0, 0 at l = m = 0; fac = conductance_ma prmag at the CMB (both
  * outputs), sigma_ratio prmag at the ICB (b_nl_bc = NULL: aj only). */

@@ -121,6 +121,7 @@ SIGNATURES = {
     "magic_sht_v_center_sphere": [_V, _V, _V, _V, _V],
     "magic_sht_get_br_v_bcs": [_V, _V, _V, _V, ctypes.c_double, ctypes.c_double, ctypes.c_double, _V, _V],
     "magic_sht_get_b_nl_bcs": [_V, ctypes.c_double, _V, _V, _V, _V],
+    "magic_sht_lorentz_torque": [_V, _V, _V, ctypes.c_double, ctypes.c_double, _V],
     "magic_sht_graph_begin": [_V],
     "magic_sht_graph_end": [_V, ctypes.POINTER(_V)],
     "magic_sht_graph_launch": [_V, _V],

@@ -99,7 +99,59 @@ int grid_blocks(const ShtGeom& g) {
   return (int)(b < 2048 ? b : 2048);
 }
 
+// Lorentz torque on a rotating, conducting boundary (get_lorentz_torque,
+// outRot.f90:423-483): LFfac 2 pi / n_phi times the sum over one level's grid
+// of gauss(theta) (br - b0 cos(theta)) bp.  Deterministic: block b sums the
+// phi rows [b n_phi / nblk, (b+1) n_phi / nblk) (threads over the colatitude
+// pairs j: rows 2j and 2j+1 at theta_j and pi - theta_j share the weight
+// 2 pi w_j), and one thread adds the block sums in order.
+__global__ void __launch_bounds__(256) torque_partial_kernel(const ShtGeom g, const double* __restrict__ theta,
+                                                             const double* __restrict__ br,
+                                                             const double* __restrict__ bp, double b0,
+                                                             double* __restrict__ partial) {
+  __shared__ double red[256 / 32];
+  const int p0 = (int)((long long)blockIdx.x * g.n_phi / gridDim.x);
+  const int p1 = (int)((long long)(blockIdx.x + 1) * g.n_phi / gridDim.x);
+  double acc = 0.0;
+  for (int j = threadIdx.x; j < g.nh; j += blockDim.x) {
+    const double c = b0 != 0.0 ? b0 * cos(theta[j]) : 0.0;  // b0r of row 2j; row 2j+1 has -c
+    double sj = 0.0;
+    for (int ph = p0; ph < p1; ++ph) {
+      const long long o = (long long)ph * g.ld + 2 * j;
+      sj += (br[o] - c) * bp[o] + (br[o + 1] + c) * bp[o + 1];
+    }
+    acc += g.wgt[j] * sj;
+  }
+  for (int d = 16; d >= 1; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void torque_finish_kernel(const double* __restrict__ partial, int n, double fac, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < n; ++i) t += partial[i];
+    out[0] = fac * t;
+  }
+}
+
 }  // namespace
+
+int lorentz_torque_blocks(const ShtGeom& g) { return g.n_phi < 128 ? g.n_phi : 128; }
+
+cudaError_t launch_lorentz_torque(const ShtGeom& g, const double* theta, const double* br, const double* bp,
+                                  double LFfac, double b0, double* partial, double* out, cudaStream_t st) {
+  const int nblk = lorentz_torque_blocks(g);
+  torque_partial_kernel<<<nblk, 256, 0, st>>>(g, theta, br, bp, b0, partial);
+  CUDA_TRY(cudaGetLastError());
+  torque_finish_kernel<<<1, 32, 0, st>>>(partial, nblk, LFfac / (double)g.n_phi, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_v_rigid_boundary(const ShtGeom& g, const double* theta, const BcGrids& a, double r2rho0,
                                     double omega, int keep_vr, cudaStream_t st) {

@@ -64,6 +64,9 @@ cudaError_t launch_br_v_products(const ShtGeom& g, const double* theta, const do
                                  const double* vp, double fac, double omega, double* out_t, double* out_p,
                                  cudaStream_t st);
 cudaError_t launch_b_nl_bcs(int K, double fac, const double2* y, double2* x, cudaStream_t st);
+int lorentz_torque_blocks(const ShtGeom& g);
+cudaError_t launch_lorentz_torque(const ShtGeom& g, const double* theta, const double* br, const double* bp,
+                                  double LFfac, double b0, double* partial, double* out, cudaStream_t st);
 // per-level maxima into mx[2 * nlev] (zeroed here), then dtrkc / dthkc updated in place
 cudaError_t launch_courant(const ShtGeom& g, const CourantArgs& a, int nlev, unsigned long long* mx, double* dtrkc,
                            double* dthkc, cudaStream_t st);

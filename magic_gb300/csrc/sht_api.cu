@@ -1595,6 +1595,26 @@ int magic_sht_get_br_v_bcs(magic_sht_handle* h, const double* br, const double* 
   return cx.finish();
 }
 
+int magic_sht_lorentz_torque(magic_sht_handle* h, const double* br, const double* bp, double LFfac, double b0,
+                             double* torque) {
+  TRY(check_handle(h));
+  if (!br || !bp || !torque) return set_err(MAGIC_SHT_ERR_ARG, "null argument");
+  DeviceGuard dg(h->device);
+  const ShtGeom& g = h->g;
+  const long long gl = (long long)g.n_phi * g.ld;
+  CallCtx cx(h);
+  const int i_r = cx.grid_in(br, 1, gl), i_p = cx.grid_in(bp, 1, gl);
+  const int i_part = cx.tmp(sizeof(double) * (size_t)lorentz_torque_blocks(g));
+  const int i_t = cx.raw_inout(torque, sizeof(double));
+  TRY(cx.prepare());
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_BCS, 2);
+    CK(launch_lorentz_torque(g, h->d_theta, (const double*)cx.dev(i_r), (const double*)cx.dev(i_p), LFfac, b0,
+                             (double*)cx.dev(i_part), (double*)cx.dev(i_t), h->stream));
+  }
+  return cx.finish();
+}
+
 int magic_sht_get_b_nl_bcs(magic_sht_handle* h, double fac, const double* br_vt_lm, const double* br_vp_lm,
                            double* b_nl_bc, double* aj_nl_bc) {
   TRY(check_handle(h));

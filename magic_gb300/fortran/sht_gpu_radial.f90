@@ -2,10 +2,11 @@ module sht_gpu_radial
    !
    ! The radial-loop pieces around the transforms on the GB300 library:
    ! Courant steps (courant.f90:54-278) and the boundary routines of
-   ! nonlinear_bcs.f90, with the reference's argument lists plus the radial
+   ! nonlinear_bcs.f90 and the Lorentz torques of outRot.f90, with the
+   ! reference's argument lists plus the radial
    ! quantities the reference takes from its modules.  rIter.f90 calls these
    ! in place of `courant`, `v_rigid_boundary`, `v_center_sphere`,
-   ! `get_br_v_bcs` and `get_b_nl_bcs`; a non-zero status becomes abortRun
+   ! `get_br_v_bcs`, `get_b_nl_bcs` and `get_lorentz_torque`; a non-zero status becomes abortRun
    ! through module sht.  Host arrays are staged by the library.
    !
    use iso_c_binding
@@ -56,6 +57,13 @@ module sht_gpu_radial
          real(c_double), value :: omega, or2, orho1
          complex(c_double_complex), intent(out) :: bvt(*), bvp(*)
       end function
+      integer(c_int) function c_torque(h, br, bp, LFfac, b0, torque) bind(C, name='magic_sht_lorentz_torque')
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(in) :: br(*), bp(*)
+         real(c_double), value :: LFfac, b0
+         real(c_double), intent(out) :: torque
+      end function
       integer(c_int) function c_b_nl(h, fac, bvt, bvp, b_nl, aj_nl) bind(C, name='magic_sht_get_b_nl_bcs')
          import :: c_int, c_ptr, c_double
          type(c_ptr), value :: h
@@ -64,7 +72,8 @@ module sht_gpu_radial
       end function
    end interface
 
-   public :: courant_gpu, v_rigid_boundary_gpu, v_center_sphere_gpu, get_br_v_bcs_gpu, get_b_nl_bcs_gpu
+   public :: courant_gpu, v_rigid_boundary_gpu, v_center_sphere_gpu, get_br_v_bcs_gpu, get_b_nl_bcs_gpu, &
+        &    get_lorentz_torque_gpu
 
 contains
 
@@ -123,6 +132,18 @@ contains
       complex(cp), intent(out) :: br_vt_lm(:), br_vp_lm(:)
       call sht_check(c_br_v(sht_handle(), br, vt, vp, omega, O_r_E_2, O_rho, br_vt_lm, br_vp_lm))
    end subroutine get_br_v_bcs_gpu
+
+   subroutine get_lorentz_torque_gpu(lorentz_torque, br, bp, LFfac, b0)
+      ! get_lorentz_torque of one boundary level; b0 = 2*BIC*r_icb**2 (times
+      ! r_icb/r_cmb at the CMB) with lGrenoble, else 0.  The radial loop
+      ! negates the mantle's value (rIter.f90:462).
+      real(cp), intent(out) :: lorentz_torque
+      real(cp), intent(in) :: br(:,:), bp(:,:)
+      real(cp), intent(in) :: LFfac, b0
+      real(c_double) :: t
+      call sht_check(c_torque(sht_handle(), br, bp, LFfac, b0, t))
+      lorentz_torque = t
+   end subroutine get_lorentz_torque_gpu
 
    subroutine get_b_nl_bcs_gpu(bc, fac, br_vt_lm, br_vp_lm, b_nl_bc, aj_nl_bc)
       ! get_b_nl_bcs with fac = conductance_ma*prmag ('CMB') or sigma_ratio*prmag ('ICB')

@@ -65,7 +65,7 @@ class RadialLoop:
                  LFfac: float = 1.0, opm: float = 1.0, l_cour_alf_damp: bool = True, lcut=None, epsc=None,
                  ktopv: int = 2, kbotv: int = 2, l_vr_cmb: bool = False, l_vr_icb: bool = False,
                  omega_ma: float = 0.0, omega_ic: float = 0.0, l_rot_ma: bool = False, l_rot_ic: bool = False,
-                 l_cond_ma: bool = False, l_cond_ic: bool = False):
+                 l_cond_ma: bool = False, l_cond_ic: bool = False, BIC: float = 0.0):
         if ktopv not in (1, 2) or kbotv not in (1, 2):
             raise ValueError("ktopv and kbotv are 1 (stress-free) or 2 (rigid)")
         self.s = sht
@@ -91,6 +91,14 @@ class RadialLoop:
                          or (kbotv == 1 or l_cond_ic or (kbotv == 2 and l_rot_ic)))
         self.l_b_nl_cmb = ktopv == 1 and l_cond_ma
         self.l_b_nl_icb = kbotv == 1 and l_cond_ic
+        # Lorentz torques on a rotating, conducting mantle / inner core
+        # (rIter.f90:278-292; the Lorentz force is on); b0 of the Grenoble
+        # setup's imposed dipole (outRot.f90:466-472), 0 without it
+        self.torque_ma = bool(l_rot_ma and l_cond_ma)
+        self.torque_ic = bool(l_rot_ic and l_cond_ic)
+        r_icb, r_cmb = float(self.r[-1]), float(self.r[0])
+        self.b0_ic = 2.0 * BIC * r_icb ** 2
+        self.b0_ma = 2.0 * BIC * r_icb ** 2 * (r_icb / r_cmb)
         self.nbc = np.zeros(n, dtype=np.int32)
         self.nbc[0], self.nbc[n - 1] = ktopv, kbotv
         self._dev = {}
@@ -145,6 +153,9 @@ class RadialLoop:
                 b[key] = (torch.empty(s.lm_max, **c128), torch.empty(s.lm_max, **c128))
         if self._rigid_kept_vr():
             b["zero_grid"] = torch.zeros((1, s.n_phi_max, s.nlat_padded), **f64)
+        for flag, key in ((self.torque_ma, "torque_ma"), (self.torque_ic, "torque_ic")):
+            if flag:
+                b[key] = torch.empty(1, **f64)
         return b
 
     def _rigid_kept_vr(self):
@@ -193,6 +204,10 @@ class RadialLoop:
         s.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, dv["radial"],
                   self.courfac, self.alffac, self.LFfac, self.opm, self.l_cour_alf_damp,
                   dtrkc=b["dtrkc"], dthkc=b["dthkc"])
+        if self.torque_ic:
+            s.lorentz_torque(g["brc"][n - 1], g["bpc"][n - 1], self.LFfac, self.b0_ic, out=b["torque_ic"])
+        if self.torque_ma:
+            s.lorentz_torque(g["brc"][0], g["bpc"][0], self.LFfac, self.b0_ma, out=b["torque_ma"])
         if self.l_b_nl_cmb:
             s.get_br_v_bcs(g["brc"][0], g["vtc"][0], g["vpc"][0], self.omega_ma, self.or2[0], 1.0, out=b["cmb"])
         if self.l_b_nl_icb:
@@ -211,6 +226,12 @@ class RadialLoop:
         for key in ("cmb", "icb"):
             if key in b:
                 res["br_vt_lm_" + key], res["br_vp_lm_" + key] = b[key]
+        # the mantle's torque is computed with the inward normal: the radial
+        # loop negates it (rIter.f90:462)
+        if "torque_ic" in b:
+            res["lorentz_torque_ic"] = float(b["torque_ic"].item())
+        if "torque_ma" in b:
+            res["lorentz_torque_ma"] = -float(b["torque_ma"].item())
         res["grids"] = b["grids"]
         return res
 
@@ -219,8 +240,10 @@ class RadialLoop:
         ``xi``, ``w`` .. ``dj``; [level][lm] complex CUDA tensors).  Returns
         the get_td outputs (``dwdt`` .. ``dVxBhLM``, into ``out`` where
         given), ``VSrLM`` (dVSrLM, 0 at the boundaries), numpy ``dtrkc`` /
-        ``dthkc``, the synthesis ``grids``, and at conducting boundaries
-        ``br_vt_lm_cmb`` / ``br_vp_lm_cmb`` (or ``_icb``)."""
+        ``dthkc``, the synthesis ``grids``, at conducting boundaries
+        ``br_vt_lm_cmb`` / ``br_vp_lm_cmb`` (or ``_icb``), and with a
+        rotating, conducting mantle / inner core ``lorentz_torque_ma`` /
+        ``lorentz_torque_ic``."""
         b = self._alloc(spec, out)
         self._enqueue(spec, b)
         return self._result(b)

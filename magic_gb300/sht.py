@@ -544,6 +544,23 @@ class SHT:
                                                float(orho1), *[p for _, p in outs]))
         return tuple(o for o, _ in outs)
 
+    def lorentz_torque(self, br, bp, LFfac: float = 1.0, b0: float = 0.0, out=None):
+        """get_lorentz_torque (outRot.f90:423-483) of one boundary level's
+        grids br, bp (numpy or CUDA): LFfac 2 pi / n_phi_max times the
+        Gauss-weighted sum of (br - b0 cos(theta)) bp.  Returns the torque as
+        a float, or writes it into the one-element float64 CUDA tensor
+        ``out`` (then nothing synchronises)."""
+        (a, pa), (b, pb) = self._grid_in(br), self._grid_in(bp)
+        if out is not None:
+            if not (_is_torch(out) and out.is_cuda and out.dtype == _torch().float64 and out.numel() == 1):
+                raise ValueError("out: a one-element float64 CUDA tensor")
+            pt, res = out.data_ptr(), None
+        else:
+            res = np.zeros(1)
+            pt = res.ctypes.data
+        check(self._lib.magic_sht_lorentz_torque(self._h, pa, pb, float(LFfac), float(b0), pt))
+        return out if res is None else float(res[0])
+
     def get_b_nl_bcs(self, bc: str, fac: float, br_vt_lm, br_vp_lm):
         """get_b_nl_bcs (nonlinear_bcs.f90:71-118): (b_nl_bc, aj_nl_bc) at the
         'CMB' (fac = conductance_ma prmag), (None, aj_nl_bc) at the 'ICB'

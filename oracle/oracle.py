@@ -431,6 +431,19 @@ def get_br_v_bcs(sht: "OracleSHT", br, vt, vp, omega: float, or2: float, orho1: 
     return sht.spat_to_sphertor(br_vt, br_vp, sht.l_max)
 
 
+def lorentz_torque(br, bp, n_theta: int, LFfac: float = 1.0, b0: float = 0.0) -> float:
+    """get_lorentz_torque (outRot.f90:423-483) of one level's grids
+    [phi][theta] (scrambled rows; gauss is stored scrambled too, horizontal.f90:
+    180-184): LFfac 2 pi / n_phi_max sum of gauss (br - b0 cos(theta)) bp."""
+    _, w = gauleg(n_theta)
+    gauss = np.repeat(w[: n_theta // 2], 2)
+    _, c = _row_trig(n_theta)
+    br = np.asarray(br, dtype=np.float64)[:, :n_theta]
+    bp = np.asarray(bp, dtype=np.float64)[:, :n_theta]
+    fac = LFfac * 2.0 * np.pi / br.shape[0]
+    return float(np.sum(fac * gauss[None, :] * (br - b0 * c[None, :]) * bp))
+
+
 def get_b_nl_bcs(fac: float, y):
     """get_b_nl_bcs (nonlinear_bcs.f90:71-118): -fac y, 0 at l = m = 0."""
     x = -fac * np.asarray(y, dtype=np.complex128)

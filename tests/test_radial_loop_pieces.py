@@ -164,7 +164,7 @@ def test_get_td_boundary_levels(built, torch):
 @pytest.mark.parametrize("cfg", [
     dict(ktopv=2, kbotv=2, omega_ma=0.3, omega_ic=-0.2),                    # rigid, lMagNlBc off
     dict(ktopv=1, kbotv=1, l_cond_ma=True, omega_ma=0.25),                  # stress-free, conducting mantle
-    dict(ktopv=2, kbotv=1, l_rot_ma=True, l_vr_cmb=True, omega_ma=0.3),     # rigid with vr kept, lMagNlBc
+    dict(ktopv=2, kbotv=1, l_rot_ma=True, l_cond_ma=True, l_vr_cmb=True, omega_ma=0.3),  # rigid, vr kept, torque
 ])
 def test_radial_loop_stage_matches_oracle(built, torch, oracle_mod, cfg):
     """One explicit stage of the radial loop (rIter.f90:94-464) over five
@@ -226,6 +226,10 @@ def test_radial_loop_stage_matches_oracle(built, torch, oracle_mod, cfg):
     dtr, dth = orc.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, loop.radial, N, 2.5, 1.0)
     np.testing.assert_allclose(got["dtrkc"], dtr, rtol=1e-10)
     np.testing.assert_allclose(got["dthkc"], dth, rtol=1e-10)
+    if loop.torque_ma:  # the mantle's torque, negated by the radial loop (rIter.f90:462)
+        exp_t = -orc.lorentz_torque(g["brc"][0], g["bpc"][0], N)
+        scale = orc.lorentz_torque(np.abs(g["brc"][0]), np.abs(g["bpc"][0]), N)
+        assert abs(got["lorentz_torque_ma"] - exp_t) <= 1e-12 * scale, (got["lorentz_torque_ma"], exp_t)
     if loop.l_b_nl_cmb:
         exp = orc.get_br_v_bcs(o, g["brc"][0], g["vtc"][0], g["vpc"][0], cfg["omega_ma"], or2[0], 1.0)
         close(got["br_vt_lm_cmb"].cpu().numpy(), exp[0], tol=1e-10)
@@ -334,4 +338,29 @@ def test_radial_loop_stage_graph_matches_eager(built, torch, form):
         assert same(got[k], ref[k], k), k
     assert np.array_equal(got["dtrkc"], ref["dtrkc"])
     sg.close()
+    s.device_status()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("grid", GRIDS + [(255, 1, 384, 768)])
+def test_lorentz_torque_matches_oracle(built, torch, grid):
+    """get_lorentz_torque (outRot.f90:423-483) of one boundary grid, host and
+    device arrays, with and without the Grenoble b0 term, against the numpy
+    restatement (summation order differs: tolerance relative to the sum of
+    the absolute terms)."""
+    from oracle import oracle as orc
+    L, minc, N, P = grid
+    s = make(L, minc, N, P)
+    rng = np.random.default_rng(31)
+    br = rng.standard_normal((s.n_phi_max, s.nlat_padded))
+    bp = rng.standard_normal((s.n_phi_max, s.nlat_padded))
+    scale = orc.lorentz_torque(np.abs(br), np.abs(bp) * 2.0, N, 1.7, 0.0)
+    for b0 in (0.0, 0.45):
+        exp = orc.lorentz_torque(br, bp, N, 1.7, b0)
+        got_h = s.lorentz_torque(br, bp, 1.7, b0)
+        out = torch.empty(1, dtype=torch.float64, device="cuda")
+        s.lorentz_torque(torch.from_numpy(br).cuda(), torch.from_numpy(bp).cuda(), 1.7, b0, out=out)
+        got_d = float(out.item())
+        assert abs(got_h - exp) <= 1e-12 * scale, (got_h, exp)
+        assert got_d == got_h
     s.device_status()
