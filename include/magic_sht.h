@@ -123,9 +123,11 @@ int magic_sht_toraxi_to_spat(magic_sht_handle* h, const double* fl_ax, double* f
  *   - Limit: n_m_max * n_theta_max * 16 bytes (FP64 form; 8 bytes for the
  *     other forms) must not exceed 4 MiB, else MAGIC_SHT_ERR_SIZE; e.g.
  *     l_max=255 with 384 Gauss points uses 1.5 MiB.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *   - magic_sht_init loads the library's module on its device and looks
+ *     up the array's device address there (cudaGetSymbolAddress, with that
+ *     device current), so the array is reserved when the first handle on a
+ *     device is created, not by this call; this call only reads the cached
+ *     address.
  *   - Every call shares the one array, which keeps the last call's contents
  *     (each call overwrites all of it before reading it); calls that overlap
  *     on the GPU (other streams, other handles on the same device) race. */

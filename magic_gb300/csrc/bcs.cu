@@ -149,6 +149,8 @@ cudaError_t launch_lorentz_torque(const ShtGeom& g, const double* theta, const d
   const int nblk = lorentz_torque_blocks(g);
   torque_partial_kernel<<<nblk, 256, 0, st>>>(g, theta, br, bp, b0, partial);
   CUDA_TRY(cudaGetLastError());
+  // the 2 pi of LFfac 2 pi / n_phi is already inside g.wgt (2 pi w_j, built
+  // by the table kernels), so the remaining factor is LFfac / n_phi
   torque_finish_kernel<<<1, 32, 0, st>>>(partial, nblk, LFfac / (double)g.n_phi, out);
   return cudaGetLastError();
 }

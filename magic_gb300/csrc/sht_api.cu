@@ -125,6 +125,11 @@ struct magic_sht_graph {
 };
 
 namespace {
+// device address of the allocation-free entry point's static scratch (defined at the end of this file)
+int noalloc_scratch(int dev, void** out);
+}  // namespace
+
+namespace {
 
 struct DeviceGuard {
   int prev = -1;
@@ -839,6 +844,15 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     INIT_CK(cudaStreamSynchronize(h->stream));
   }
 #undef INIT_CK
+  {
+    // Load this file's module on the device now and resolve the static
+    // scratch of magic_sht_scal_to_spat_noalloc: with lazy module loading the
+    // first use of the module reserves its 4 MiB array, and that reservation
+    // belongs here, not inside the allocation-free call.
+    void* scratch = nullptr;
+    rc = noalloc_scratch(dev, &scratch);
+    if (rc != MAGIC_SHT_OK) return fail(rc);
+  }
   *out = h;
   return MAGIC_SHT_OK;
 }
@@ -2003,8 +2017,11 @@ extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double*
   s.f[0].out1 = nullptr;
   s.f[0].out_ld = hs_ld;
   // the one-tile-per-CTA tensor-core kernel needs no data-image buffer
-  if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, false, h->tct, h->stream));
-  else CK(launch_inv_legendre_simt(g, s, false, fp64_pipes(h), h->stream));
+  {
+    PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_SCALAR);
+    if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, false, h->tct, h->stream));
+    else CK(launch_inv_legendre_simt(g, s, false, fp64_pipes(h), h->stream));
+  }
   FftSet fs{};
   fs.nf = 1;
   fs.nlev = 1;
@@ -2013,6 +2030,9 @@ extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double*
   fs.f[0].in_ld = hs_ld;
   fs.f[0].out_ld = (long long)g.n_phi * g.ld;
   fs.f[0].flags = tc_form(h) ? FFT_IN_E : 0;  // parity-separated synthesis output
-  CK(launch_fft_inverse(g, fs, fp64_pipes(h), h->fft_rows, h->stream));
+  {
+    PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_INV);
+    CK(launch_fft_inverse(g, fs, fp64_pipes(h), h->fft_rows, h->stream));
+  }
   return MAGIC_SHT_OK;
 }

@@ -33,16 +33,25 @@ def test_noalloc_matches_ordinary_entry_point(torch, prec, tol):
     lib = _lib.load()
     s = SHT(255, 1, 384, 768, precision=prec, device=0)
     S = [torch.from_numpy(x).cuda() for x in spectra(255, 1, 2, seed=31)]
-    for call in range(2):  # two calls in a row share the static scratch
-        Sk = S[call]
-        ref = s.scal_to_spat(Sk, 250)  # ordinary entry point, same stream
+    # Calls in a row share the static scratch.  The first one (lcut = l_max)
+    # leaves non-zero half-spectrum entries at every order, including the
+    # orders above 250 that the later calls (lcut = 250) must overwrite with
+    # zeros; stale entries would show up as a mismatch there.
+    for call, (Sk, lc) in enumerate(((S[0], 255), (S[1], 250), (S[0], 250))):
+        ref = s.scal_to_spat(Sk, lc)  # ordinary entry point, same stream
         out = torch.full((s.n_phi_max, s.nlat_padded), float("nan"), dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
         s.set_stream(None)
-        _lib.check(lib.magic_sht_scal_to_spat_noalloc(s._h, Sk.data_ptr(), out.data_ptr(), 250))
+        n0, n1 = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        _lib.check(lib.magic_sht_launch_count(s._h, ctypes.byref(n0)))
+        _lib.check(lib.magic_sht_scal_to_spat_noalloc(s._h, Sk.data_ptr(), out.data_ptr(), lc))
+        _lib.check(lib.magic_sht_launch_count(s._h, ctypes.byref(n1)))
         s.synchronize()
         err = float(torch.linalg.vector_norm(out - ref) / torch.linalg.vector_norm(ref))
         assert err <= tol, (call, err)
+        # the call counts its two kernels (Legendre sums, inverse FFT) in the
+        # handle's launch counters like the ordinary entry points do
+        assert n1.value - n0.value == 2, (call, n0.value, n1.value)
     s.close()
 
 
