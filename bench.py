@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x2"])
+    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x2", "fp64tc"])
     ap.add_argument("--cpu-levels", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -411,8 +411,14 @@ def our_arm(args):
     value = world * N_LEVELS * args.steps / (ms * 1e-3)
 
     if args.only_reduced:
-        print(json.dumps({"form": form, "value": value, "ms_per_step": ms / args.steps,
-                          "levels": N_LEVELS}), flush=True)
+        sm.set_profiling(True)
+        sm.phase_times(reset=True)
+        run_set(sm, gm, lmx)
+        ph = sm.phase_times(reset=True)
+        sm.set_profiling(False)
+        sm.device_status()
+        print(json.dumps({"form": form, "value": value, "ms_per_step": ms / args.steps, "levels": N_LEVELS,
+                          "phases_ms": {k: v[0] for k, v in ph.items() if v[1]}}), flush=True)
         return
     # ---- accuracy of the reduced form against the FP64 form (same inputs)
     run_set(sm, gm, lmx)

@@ -41,6 +41,9 @@ extern "C" {
 #define MAGIC_SHT_BF16X3 2  /* tensor cores: 3xBF16 split products, FP32 accumulate, FP32 FFT */
 #define MAGIC_SHT_TF32X2 3  /* tensor cores: 2xTF32 split products (hi*hi, hi*lo, lo*hi), FP32 accumulate,
                                FP32 FFT; persistent kernels only (no scal_to_spat_noalloc) */
+#define MAGIC_SHT_FP64TC 4  /* FP64-accurate on tensor cores: seven fixed-point BF16 digits per operand, 28 digit
+                               products accumulated exactly in FP32, double-float (FP32-pair) FFTs and
+                               half spectra, FP64 radial-loop kernels; values within the FP32 exponent range */
 
 typedef struct magic_sht_desc {
   int l_max;       /* truncation degree (truncation.f90 l_max) */
@@ -49,7 +52,7 @@ typedef struct magic_sht_desc {
   int n_theta_max; /* Gauss points, multiple of 4 (truncation.f90:150) */
   int n_phi_max;   /* longitudes per symmetry sector, multiple of 4, 2^i 3^j 5^k */
   int nlat_padded; /* leading dimension of grid arrays; 0 -> n_theta_max */
-  int precision;   /* MAGIC_SHT_FP64 | MAGIC_SHT_FP32 | MAGIC_SHT_BF16X3 | MAGIC_SHT_TF32X2 */
+  int precision;   /* MAGIC_SHT_FP64 | _FP32 | _BF16X3 | _TF32X2 | _FP64TC */
   int device;      /* CUDA device ordinal; -1 -> current device */
 } magic_sht_desc;
 
@@ -197,7 +200,8 @@ int magic_sht_set_host_async(magic_sht_handle* h, int on);
  * tc_kernel, which selects between two kernels of the same arithmetic form;
  * graphs captured earlier keep the settings they were captured with.
  *   tc_kernel:  tensor-core forms, 0 persistent kernels, 1 one tile per CTA
- *               (3xBF16 only)
+ *               (3xBF16) or the FP64 SIMT Legendre sums (FP64TC, with its
+ *               double-float FFTs)
  *   tc_order:   persistent kernels' tile order, 0 consecutive tiles share the
  *               table blocks, 1 they share the data tiles
  *   pipe_chunk: radial levels per chunk of the host-buffer pipeline (1..1024)

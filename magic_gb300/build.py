@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmagic_sht.so")
-SOURCES = ["sht_api.cu", "legendre_simt.cu", "legendre_tc.cu", "legendre_tcp.cu", "fft.cu", "tables.cu", "peak.cu", "nl.cu", "td.cu",
+SOURCES = ["sht_api.cu", "legendre_simt.cu", "legendre_tc.cu", "legendre_tcp.cu", "legendre_oz.cu", "fft.cu", "tables.cu", "peak.cu", "nl.cu", "td.cu",
            "courant.cu", "bcs.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -77,7 +77,13 @@ enum FftFlags : int {
   // N = E_0 + E_1, S = F_0 - F_1 (F = E with FFT_IN_E)
   FFT_IN_E = 4,
   FFT_IN_EF = 8,
+  // double-float transforms: the half spectra (inverse input, forward output)
+  // are FP64 instead of double-float pairs
+  FFT_HS_F64 = 16,
 };
+
+// arithmetic of the azimuthal FFTs
+enum FftArith : int { FFT_ARITH_F32 = 0, FFT_ARITH_F64 = 1, FFT_ARITH_DF = 2 };
 
 struct FftField {
   const void* in;
@@ -110,6 +116,7 @@ struct ShtGeom {
   const double* osin2;           // device [nh]  1/sin^2 theta_j
   const double2* tw64;           // device [n_phi]  e^{+2 pi i k/n_phi}
   const float2* tw32;
+  const void* twdf;              // device [n_phi]  the same as double-float pairs (hi, lo) x (re, im)
 };
 
 // Pre-split (3xBF16) and pre-tiled Legendre tables of the tensor-core form.
@@ -127,6 +134,8 @@ struct TcTables {
   const unsigned char* fwd_img;
   const long long* fwd_blk0;  // [n_m]
   const float* fwd_scale;     // [2][lm_max]
+  const short* inv_exp;       // FP64-accurate form: row exponents [2][n_m][ntt*128] (the scales are 2^exp)
+  const short* fwd_exp;       // [2][lm_max]
   int* err;                   // device error word (bounded waits that gave up)
   const long long* bpc0;      // [n_m] first (parity, chunk) pair of each m in the synthesis data images
   long long npc;              // total (parity, chunk) pairs over all m

@@ -1,14 +1,17 @@
 // Small complex helpers for double2 / float2 (device only).
 #pragma once
 #include <cuda_runtime.h>
+#include "dfloat.cuh"
 
 template <typename T> struct V2;
 template <> struct V2<double> { typedef double2 t; };
 template <> struct V2<float> { typedef float2 t; };
+template <> struct V2<dfl> { typedef dfl2 t; };
 
 template <typename T2> struct ScalarOf;
 template <> struct ScalarOf<double2> { typedef double t; };
 template <> struct ScalarOf<float2> { typedef float t; };
+template <> struct ScalarOf<dfl2> { typedef dfl t; };
 
 __device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
 __device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
@@ -20,6 +23,9 @@ template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { T2 r; r.
 template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { T2 r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
 template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
   T2 r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <> __device__ __forceinline__ dfl2 cmul<dfl2>(dfl2 a, dfl2 b) {
+  dfl2 r; r.x = df_dot2_sub(a.x, b.x, a.y, b.y); r.y = df_dot2_add(a.x, b.y, a.y, b.x); return r;
 }
 template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { a.y = -a.y; return a; }
 // multiply by +i (s>0) or -i (s<0)
@@ -33,6 +39,17 @@ template <typename T2, typename S> __device__ __forceinline__ T2 cscale(T2 a, S 
 
 template <typename T2> __device__ __forceinline__ T2 shfl_xor2(T2 v, int d) {
   T2 r; r.x = __shfl_xor_sync(0xffffffffu, v.x, d); r.y = __shfl_xor_sync(0xffffffffu, v.y, d); return r;
+}
+template <> __device__ __forceinline__ dfl2 shfl_xor2<dfl2>(dfl2 v, int d) {
+  dfl2 r;
+  r.x.h = __shfl_xor_sync(0xffffffffu, v.x.h, d); r.x.l = __shfl_xor_sync(0xffffffffu, v.x.l, d);
+  r.y.h = __shfl_xor_sync(0xffffffffu, v.y.h, d); r.y.l = __shfl_xor_sync(0xffffffffu, v.y.l, d);
+  return r;
+}
+// b + sg a for sg = +-1 (the cross-lane butterflies of the FFT)
+template <typename T> __device__ __forceinline__ T add_signed(T sg, T a, T b) { return fma(sg, a, b); }
+template <> __device__ __forceinline__ dfl add_signed<dfl>(dfl sg, dfl a, dfl b) {
+  return b + (sg.h < 0.f ? -a : a);
 }
 
 // FP64 <-> FP32 conversions with integer instructions only (the FP64 pipe of
@@ -74,12 +91,21 @@ __device__ __forceinline__ double f2d_int(float x) {
 template <typename T> __device__ __forceinline__ double to_f64(T x);
 template <> __device__ __forceinline__ double to_f64<double>(double x) { return x; }
 template <> __device__ __forceinline__ double to_f64<float>(float x) { return f2d_int(x); }
+template <> __device__ __forceinline__ double to_f64<dfl>(dfl x) { return df_to_double(x); }
 template <typename T> __device__ __forceinline__ T from_f64(double x);
 template <> __device__ __forceinline__ double from_f64<double>(double x) { return x; }
 template <> __device__ __forceinline__ float from_f64<float>(double x) { return d2f_int(x); }
+template <> __device__ __forceinline__ dfl from_f64<dfl>(double x) { return df_from_double(x); }
 
 template <typename T2> __device__ __forceinline__ T2 cvt2(double2 a);
 template <> __device__ __forceinline__ double2 cvt2<double2>(double2 a) { return a; }
 template <> __device__ __forceinline__ float2 cvt2<float2>(double2 a) { return make_float2(d2f_int(a.x), d2f_int(a.y)); }
+template <> __device__ __forceinline__ dfl2 cvt2<dfl2>(double2 a) { dfl2 r; r.x = df_from_double(a.x); r.y = df_from_double(a.y); return r; }
 __device__ __forceinline__ double2 to_d2(double2 a) { return a; }
 __device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(f2d_int(a.x), f2d_int(a.y)); }
+__device__ __forceinline__ double2 to_d2(dfl2 a) { return make_double2(df_to_double(a.x), df_to_double(a.y)); }
+
+// A grid value read in FP64 into a transform's working type: plain
+// conversion for float and double, the double-float split for dfl.
+template <typename T> __device__ __forceinline__ T cvt_in(double x) { return (T)x; }
+template <> __device__ __forceinline__ dfl cvt_in<dfl>(double x) { return df_from_double(x); }

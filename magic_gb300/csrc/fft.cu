@@ -17,12 +17,41 @@
 // Forward epilogue (fused): 1/sin^2 theta (spat_to_sph_tor,
 // src/shtransforms.f90:789-794), the Gauss weight 2 pi w_j, and the
 // north/south -> ES/EA combination (src/shtransforms.f90:704-709, :811-818).
+#include <type_traits>
 #include <vector>
 #include "common.cuh"
 #include "cplx.cuh"
 #include "internal.h"
 
 namespace {
+
+// Twiddle table e^{+2 pi i k / P} in the working type of a transform.
+template <typename T> struct Tw;
+template <> struct Tw<float> { static __device__ __forceinline__ const float2* get(const ShtGeom& g) { return g.tw32; } };
+template <> struct Tw<double> { static __device__ __forceinline__ const double2* get(const ShtGeom& g) { return g.tw64; } };
+template <> struct Tw<dfl> {
+  static __device__ __forceinline__ const dfl2* get(const ShtGeom& g) { return (const dfl2*)g.twdf; }
+};
+
+// CTAs per SM of the fast path: FP32 three (two for the longest rows), FP64
+// one, double-float two (its rows are twice the FP32 size, its arithmetic
+// needs the latency hiding of a second CTA)
+template <typename T, int S> struct FftOcc { static constexpr int v = S >= 20 ? 2 : 3; };
+template <int S> struct FftOcc<double, S> { static constexpr int v = 1; };
+template <int S> struct FftOcc<dfl, S> { static constexpr int v = 2; };
+
+// Half-spectrum entries of the double-float transforms may be held in FP64
+// (FFT_HS_F64: the FP64 SIMT Legendre sums on either side); the other forms
+// read and write their own type.
+template <typename T2> __device__ __forceinline__ T2 ld_hs(const T2* p, bool) { return *p; }
+template <> __device__ __forceinline__ dfl2 ld_hs<dfl2>(const dfl2* p, bool f64) {
+  return f64 ? cvt2<dfl2>(*(const double2*)p) : *p;
+}
+template <typename T2> __device__ __forceinline__ void st_hs(T2* p, T2 v, bool) { *p = v; }
+template <> __device__ __forceinline__ void st_hs<dfl2>(dfl2* p, dfl2 v, bool f64) {
+  if (f64) *(double2*)p = to_d2(v);
+  else *p = v;
+}
 
 template <typename T2, int R> struct Bfly;
 template <typename T2> struct Bfly<T2, 2> {
@@ -180,8 +209,8 @@ __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tab,
     for (int q = 0; q < S; ++q) {
       const T2 b = shfl_xor2(a[q], d);
       T2 t;
-      t.x = fma(sg, a[q].x, b.x);
-      t.y = fma(sg, a[q].y, b.y);
+      t.x = add_signed(sg, a[q].x, b.x);
+      t.y = add_signed(sg, a[q].y, b.y);
       a[q] = d > 1 ? cmul(t, w) : t;
     }
   }
@@ -208,8 +237,8 @@ __device__ __forceinline__ int pos(int k) { return (k & 31) + ((k >> 4) & 1) + 3
 // a thread waits for one memory latency per batch.
 template <typename T2, int S, int RT, int NB>
 __device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict__ in, bool in_parity,
-                                          bool has_f, long long per_p, const T2* __restrict__ twg, T2* sm, T2* stw,
-                                          int rp, int kq, int rowg, bool row_ok) {
+                                          bool has_f, bool hs64, long long per_p, const T2* __restrict__ twg, T2* sm,
+                                          T2* stw, int rp, int kq, int rowg, bool row_ok) {
   constexpr int KP = 33 * S + 1, KS = 256 / (RT / 2), NT = TwTab<S>::size, NTW = (NT + 255) / 256;
   const int n_m = g.n_m;
   T2 twr[NTW];
@@ -226,16 +255,16 @@ __device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict
       if (row_ok && k < n_m) {
         if (in_parity) {
           const T2* b0 = in + (long long)k * 2 * per_p + (rowg >> 1);
-          x[b][0] = b0[0];
-          x[b][1] = b0[per_p];
+          x[b][0] = ld_hs(b0, hs64);
+          x[b][1] = ld_hs(b0 + per_p, hs64);
           if (has_f) {
-            x[b][2] = b0[g.nh];
-            x[b][3] = b0[per_p + g.nh];
+            x[b][2] = ld_hs(b0 + g.nh, hs64);
+            x[b][3] = ld_hs(b0 + per_p + g.nh, hs64);
           }
         } else {
           const T2* p = in + (long long)k * g.n_theta + rowg;
-          x[b][0] = p[0];
-          x[b][1] = p[1];
+          x[b][0] = ld_hs(p, hs64);
+          x[b][1] = ld_hs(p + 1, hs64);
         }
       }
     }
@@ -266,7 +295,7 @@ __device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict
 // odd pitch KP = 33 S + 1 and the layouts pin() / pos(), so that row-parallel
 // and index-parallel accesses both spread over the banks.
 template <typename T, int S, int RT>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1)) fft_inv_fast(const ShtGeom g, const FftSet s) {
+__global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_inv_fast(const ShtGeom g, const FftSet s) {
   typedef typename V2<T>::t T2;
   constexpr int n = 32 * S, KP = 33 * S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -275,7 +304,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   const int r = col / s.nf, f = col - r * s.nf;
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
-  const T2* __restrict__ twg = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  const T2* __restrict__ twg = Tw<T>::get(g);
   T2* stw = sm + RT * KP;  // twiddle tables (TwTab)
   const T2* __restrict__ in = (const T2*)fd.in + (long long)r * fd.in_ld;
   const int n_m = g.n_m;
@@ -288,7 +317,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   const int rp = 2 * (threadIdx.x % RT2), kq = threadIdx.x / RT2;
   const int rowg = row0 + rp;
   const bool row_ok = rowg < g.n_theta;
-  inv_stage<T2, S, RT, sizeof(T) == 4 ? 4 : 2>(g, in, in_parity, has_f, per_p, twg, sm, stw, rp, kq, rowg, row_ok);
+  const bool hs64 = (fd.flags & FFT_HS_F64) != 0;
+  inv_stage<T2, S, RT, sizeof(T) == 4 ? 4 : 2>(g, in, in_parity, has_f, hs64, per_p, twg, sm, stw, rp, kq, rowg,
+                                               row_ok);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const T2 base = twg[S * lane];  // e^{2 pi i S lane / P}: times lo[q] gives e^{2 pi i k / P}, k = S lane + q
@@ -337,7 +368,14 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
     // integer instructions: splitting the conversions between the two pipes
     // measured faster than either alone.  Both are exact; FP32 subnormals
     // (below 1.2e-38) are kept by the first and flushed to zero by the second.
-    const double x0 = (double)v0.x, y0 = (double)v0.y;
+    double x0, y0;
+    if constexpr (std::is_same<T, dfl>::value) {
+      x0 = to_f64<T>(v0.x);
+      y0 = to_f64<T>(v0.y);
+    } else {
+      x0 = (double)v0.x;
+      y0 = (double)v0.y;
+    }
     if (vec) {
       *reinterpret_cast<double2*>(dst) = make_double2(x0, to_f64<T>(v1.x));
       *reinterpret_cast<double2*>(dst + g.ld) = make_double2(y0, to_f64<T>(v1.y));
@@ -351,7 +389,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
 }
 
 template <typename T, int S, int RT>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1)) fft_fwd_fast(const ShtGeom g, const FftSet s) {
+__global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_fwd_fast(const ShtGeom g, const FftSet s) {
   typedef typename V2<T>::t T2;
   constexpr int n = 32 * S, KP = 33 * S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -360,7 +398,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   const int r = col / s.nf, f = col - r * s.nf;
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
-  const T2* __restrict__ twg = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  const T2* __restrict__ twg = Tw<T>::get(g);
   T2* stw = sm + RT * KP;  // twiddle tables (TwTab)
   const double* __restrict__ in = (const double*)fd.in + (long long)r * fd.in_ld;
   // Each thread owns the row pair (rp, rp + 1) and the indices kk = kq + KS j
@@ -403,8 +441,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
       if (kk >= n) continue;
       const int pj = pin<S>(kk);
       T2 z0, z1;
-      z0.x = (T)u[b].x; z0.y = (T)w[b].x;
-      z1.x = (T)u[b].y; z1.y = (T)w[b].y;
+      z0.x = cvt_in<T>(u[b].x); z0.y = cvt_in<T>(w[b].x);
+      z1.x = cvt_in<T>(u[b].y); z1.y = cvt_in<T>(w[b].y);
       sm[rp * KP + pj] = z0;
       sm[(rp + 1) * KP + pj] = z1;
     }
@@ -427,6 +465,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
   // X_k = (Z_k + conj Z_{n-k})/2 - i e^{-2 pi i k/P} (Z_k - conj Z_{n-k})/2, then ES/EA
   typedef T Tt;
   T2* out = (T2*)fd.out + (long long)r * fd.out_ld;
+  const bool hs64 = (fd.flags & FFT_HS_F64) != 0;
   // this thread's colatitude pair jp (rows 2jp, 2jp + 1) and orders k = kq + KS j
   const int jp = threadIdx.x % RT2, jg = (row0 >> 1) + jp;
   if (jg >= g.nh) return;
@@ -453,8 +492,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (S >= 20 ? 2 : 3) : 1))
     c[0] = cscale(c[0], fac);
     c[1] = cscale(c[1], fac);
     const long long o = ((long long)k * g.nh + jg) * 2;
-    out[o] = cadd(c[0], c[1]);
-    out[o + 1] = csub(c[0], c[1]);
+    st_hs(out + o, cadd(c[0], c[1]), hs64);
+    st_hs(out + o + 1, csub(c[0], c[1]), hs64);
   }
 }
 
@@ -464,6 +503,7 @@ __device__ __forceinline__ void stage_spectrum(const ShtGeom& g, const T2* __res
                                                int row0, int RT, int RP, T2* sm, int flags) {
   const bool in_parity = (flags & (FFT_IN_E | FFT_IN_EF)) != 0;
   const bool has_f = (flags & FFT_IN_EF) != 0;
+  const bool hs64 = (flags & FFT_HS_F64) != 0;
   const long long per_p = has_f ? 2LL * g.nh : (long long)g.nh;
   for (int i = threadIdx.x; i < g.n_m * RT; i += blockDim.x) {
     const int k = i / RT, rr = i - k * RT;
@@ -474,10 +514,11 @@ __device__ __forceinline__ void stage_spectrum(const ShtGeom& g, const T2* __res
         const int jg = row >> 1;
         const T2* b0 = in + (long long)k * 2 * per_p;
         const T2* b1 = b0 + per_p;
-        if ((row & 1) == 0) v = cadd(b0[jg], b1[jg]);
-        else v = has_f ? csub(b0[g.nh + jg], b1[g.nh + jg]) : csub(b0[jg], b1[jg]);
+        if ((row & 1) == 0) v = cadd(ld_hs(b0 + jg, hs64), ld_hs(b1 + jg, hs64));
+        else v = has_f ? csub(ld_hs(b0 + g.nh + jg, hs64), ld_hs(b1 + g.nh + jg, hs64))
+                       : csub(ld_hs(b0 + jg, hs64), ld_hs(b1 + jg, hs64));
       } else {
-        v = in[(long long)k * g.n_theta + row];
+        v = ld_hs(in + (long long)k * g.n_theta + row, hs64);
       }
     }
     sm[k * RP + rr] = v;
@@ -524,7 +565,7 @@ __device__ __forceinline__ void stage_grid(const ShtGeom& g, const double* __res
     const int row = row0 + rr;
     double x = 0.0;
     if (row < g.n_theta) x = in[(long long)ph * g.ld + row];
-    smr[((ph >> 1) * RP + rr) * 2 + (ph & 1)] = (T)x;
+    smr[((ph >> 1) * RP + rr) * 2 + (ph & 1)] = cvt_in<T>(x);
   }
 }
 
@@ -560,8 +601,9 @@ __device__ __forceinline__ void fwd_post(const ShtGeom& g, const FftField& fd, T
     if (fd.flags & FFT_WEIGHT) fac *= from_f64<T>(g.wgt[jg]);
     c[0] = cscale(c[0], fac); c[1] = cscale(c[1], fac);
     const long long o = ((long long)k * g.nh + jg) * 2;
-    out[o] = cadd(c[0], c[1]);
-    out[o + 1] = csub(c[0], c[1]);
+    const bool hs64 = (fd.flags & FFT_HS_F64) != 0;
+    st_hs(out + o, cadd(c[0], c[1]), hs64);
+    st_hs(out + o + 1, csub(c[0], c[1]), hs64);
   }
 }
 
@@ -620,7 +662,7 @@ __global__ void __launch_bounds__(256) fft_inv_gen(const ShtGeom g, const FftSet
   const int r = col / s.nf, f = col - r * s.nf;
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
-  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  const T2* __restrict__ tw = Tw<T>::get(g);
   stage_spectrum<T2>(g, (const T2*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm, fd.flags);
   __syncthreads();
   for (int k = lane; k < n; k += 32) wa[k] = inv_pre<T2>(g, sm, RP, warp, k, n, tw);
@@ -647,7 +689,7 @@ __global__ void __launch_bounds__(256) fft_fwd_gen(const ShtGeom g, const FftSet
   const int r = col / s.nf, f = col - r * s.nf;
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
-  const T2* __restrict__ tw = (const T2*)(sizeof(T) == 8 ? (const void*)g.tw64 : (const void*)g.tw32);
+  const T2* __restrict__ tw = Tw<T>::get(g);
   stage_grid<T2>(g, (const double*)fd.in + (long long)r * fd.in_ld, row0, RT, RP, sm);
   __syncthreads();
   for (int k = lane; k < n; k += 32) wa[k] = sm[k * RP + warp];
@@ -749,10 +791,12 @@ bool fft_fast_path(int n_phi) {
   }
 }
 
-cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, bool fp64, int rows, cudaStream_t st) {
-  return fp64 ? launch_any<double>(g, s, true, rows, st) : launch_any<float>(g, s, true, rows, st);
+cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, int arith, int rows, cudaStream_t st) {
+  if (arith == FFT_ARITH_DF) return launch_any<dfl>(g, s, true, rows, st);
+  return arith == FFT_ARITH_F64 ? launch_any<double>(g, s, true, rows, st) : launch_any<float>(g, s, true, rows, st);
 }
 
-cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, bool fp64, int rows, cudaStream_t st) {
-  return fp64 ? launch_any<double>(g, s, false, rows, st) : launch_any<float>(g, s, false, rows, st);
+cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, int arith, int rows, cudaStream_t st) {
+  if (arith == FFT_ARITH_DF) return launch_any<dfl>(g, s, false, rows, st);
+  return arith == FFT_ARITH_F64 ? launch_any<double>(g, s, false, rows, st) : launch_any<float>(g, s, false, rows, st);
 }

@@ -13,8 +13,9 @@ cudaError_t launch_fwd_legendre_simt(const ShtGeom& g, const FwdSet& s, bool vec
 // Inverse: half spectrum T2 [n_m][n_theta] -> double grid [n_phi][ld].
 // Forward: double grid -> ES/EA half spectrum T2 [n_m][nh][2] (scaled 1/n_phi).
 // rows: theta rows per CTA of the fast path (8 or 16; 0 = chosen by size)
-cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, bool fp64, int rows, cudaStream_t st);
-cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, bool fp64, int rows, cudaStream_t st);
+// arith: FFT_ARITH_F32 / _F64 / _DF (double-float, working type dfl)
+cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, int arith, int rows, cudaStream_t st);
+cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, int arith, int rows, cudaStream_t st);
 bool fft_fast_path(int n_phi);
 
 // tables.cu
@@ -33,6 +34,9 @@ cudaError_t launch_tc_selftest(int n, int kchunks, bool tf32, const float* A, co
                                cudaStream_t st);
 void tc_table_layout(const ShtGeom& g, bool tf32, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
                      std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks);
+// the same with `bpc` 16 KB blocks per K chunk
+void tc_table_layout_bpc(const ShtGeom& g, int bpc, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
+                         std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks);
 cudaError_t build_tc_images(const ShtGeom& g, const TcTables& t, bool tf32, unsigned char* inv_img, float* inv_scale,
                             unsigned char* fwd_img, float* fwd_scale, cudaStream_t st);
 cudaError_t launch_inv_legendre_tc(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
@@ -70,3 +74,18 @@ cudaError_t launch_lorentz_torque(const ShtGeom& g, const double* theta, const d
 // per-level maxima into mx[2 * nlev] (zeroed here), then dtrkc / dthkc updated in place
 cudaError_t launch_courant(const ShtGeom& g, const CourantArgs& a, int nlev, unsigned long long* mx, double* dtrkc,
                            double* dthkc, cudaStream_t st);
+
+// legendre_oz.cu: the FP64-accurate tensor-core form (six fixed-point BF16
+// digits per operand, exact FP32 accumulation); TcTables with inv_exp / fwd_exp
+void oz_table_layout(const ShtGeom& g, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
+                     std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks);
+cudaError_t build_oz_images(const ShtGeom& g, const TcTables& t, unsigned char* inv_img, short* inv_exp,
+                            unsigned char* fwd_img, short* fwd_exp, cudaStream_t st);
+// data images (digits + column exponents) of one call of ncplx complex columns
+size_t oz_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool inverse);
+// synthesis: double-float half spectra in the parity-separated layout of the
+// tensor-core forms; analysis: double-float (ES, EA) half spectra in
+cudaError_t launch_inv_legendre_oz(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
+                                   unsigned char* bimg, cudaStream_t st);
+cudaError_t launch_fwd_legendre_oz(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
+                                   unsigned char* bimg, cudaStream_t st);

@@ -634,7 +634,11 @@ cudaError_t launch_fwd_tc_t(const ShtGeom& g, const FwdSet& s, const TcTables& t
 
 void tc_table_layout(const ShtGeom& g, bool tf32, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
                      std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks) {
-  const int bpc = tf32 ? 4 : 3;
+  tc_table_layout_bpc(g, tf32 ? 4 : 3, ntt, nlt, ncj, inv_blk0, fwd_blk0, inv_blocks, fwd_blocks);
+}
+
+void tc_table_layout_bpc(const ShtGeom& g, int bpc, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
+                         std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks) {
   *ntt = (g.nh + 127) / 128;
   *nlt = ((g.l_max + 2) / 2 + 127) / 128;
   *ncj = (g.nh + 63) / 64;

@@ -64,6 +64,9 @@ struct magic_sht_handle {
   float *d_P32 = nullptr, *d_dP32 = nullptr;
   double2* d_tw64 = nullptr;
   float2* d_tw32 = nullptr;
+  float4* d_twdf = nullptr;  // e^{+2 pi i k/P} as double-float (hi re, lo re, hi im, lo im)
+  short* d_inv_exp = nullptr;  // FP64-accurate tensor-core form: table row exponents
+  short* d_fwd_exp = nullptr;
   // tensor-core form: pre-split table images
   TcTables tct{};
   unsigned char* d_inv_img = nullptr;
@@ -184,7 +187,15 @@ bool is_device_ptr(const void* p) {
 }
 
 bool fp64_pipes(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_FP64; }
-size_t t2_bytes(const magic_sht_handle* h) { return fp64_pipes(h) ? 16 : 8; }
+// the FP64-accurate tensor-core form: Legendre sums of fixed-point BF16 digits
+// (or, with tc_kernel = 1, the FP64 SIMT sums) and double-float FFTs
+bool oz_form(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_FP64TC; }
+// FP64 arithmetic in the SIMT Legendre sums and the radial-loop kernels
+bool f64_sums(const magic_sht_handle* h) { return fp64_pipes(h) || oz_form(h); }
+size_t t2_bytes(const magic_sht_handle* h) { return f64_sums(h) ? 16 : 8; }
+int fft_arith(const magic_sht_handle* h) {
+  return fp64_pipes(h) ? FFT_ARITH_F64 : oz_form(h) ? FFT_ARITH_DF : FFT_ARITH_F32;
+}
 
 size_t hs_bytes(const magic_sht_handle* h, int nlev) {
   return (size_t)nlev * h->g.n_m * h->g.n_theta * t2_bytes(h);
@@ -192,9 +203,14 @@ size_t hs_bytes(const magic_sht_handle* h, int nlev) {
 
 // Synthesis half spectra of a vector component in the tensor-core form hold
 // E and F for both parities: twice the entries of the N/S layout.
-bool tc_form(const magic_sht_handle* h) {
+// The split-product forms (3xBF16, 2xTF32) always; the FP64-accurate form when
+// its tensor-core kernels run (tc_kernel = 0).
+bool split_form(const magic_sht_handle* h) {
   return h->precision == MAGIC_SHT_BF16X3 || h->precision == MAGIC_SHT_TF32X2;
 }
+bool tc_form(const magic_sht_handle* h) { return split_form(h) || (oz_form(h) && h->tc_persistent); }
+// FP64 half spectra between the FP64 SIMT Legendre sums and the double-float FFTs
+int fft_hs_flag(const magic_sht_handle* h) { return (oz_form(h) && !h->tc_persistent) ? FFT_HS_F64 : 0; }
 bool tf32_form(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_TF32X2; }
 // data-operand images of the persistent tensor-core kernels (grown like the workspace)
 int ensure_bimg(magic_sht_handle* h, size_t bytes) {
@@ -216,6 +232,12 @@ int ensure_bimg(magic_sht_handle* h, size_t bytes) {
   return MAGIC_SHT_OK;
 }
 int inv_tc(magic_sht_handle* h, const ShtGeom& g, const InvSet& s, bool vec) {
+  if (oz_form(h)) {
+    TRY(ensure_bimg(h, oz_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), true)));
+    h->launches++;  // pack kernel + persistent kernel
+    CK(launch_inv_legendre_oz(g, s, vec, h->tct, h->d_bimg, h->stream));
+    return MAGIC_SHT_OK;
+  }
   if (!h->tc_persistent) {
     CK(launch_inv_legendre_tc(g, s, vec, h->tct, h->stream));
     return MAGIC_SHT_OK;
@@ -226,6 +248,12 @@ int inv_tc(magic_sht_handle* h, const ShtGeom& g, const InvSet& s, bool vec) {
   return MAGIC_SHT_OK;
 }
 int fwd_tc(magic_sht_handle* h, const ShtGeom& g, const FwdSet& s, bool vec) {
+  if (oz_form(h)) {
+    TRY(ensure_bimg(h, oz_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), false)));
+    h->launches++;  // pack kernel + persistent kernel
+    CK(launch_fwd_legendre_oz(g, s, vec, h->tct, h->d_bimg, h->stream));
+    return MAGIC_SHT_OK;
+  }
   if (!h->tc_persistent) {
     CK(launch_fwd_legendre_tc(g, s, vec, h->tct, h->stream));
     return MAGIC_SHT_OK;
@@ -464,8 +492,9 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
                 const std::vector<int>& hs_sc, const std::vector<int>& hs_vc) {
   const ShtGeom& g = h->g;
   const long long hs_ld = hs_inv_ld(h, false), hs_ld_v = hs_inv_ld(h, true);
-  const int flag_s = tc_form(h) ? FFT_IN_E : 0, flag_v = tc_form(h) ? FFT_IN_EF : 0;
-  const bool f64 = fp64_pipes(h);
+  const int hsf = fft_hs_flag(h);
+  const int flag_s = (tc_form(h) ? FFT_IN_E : 0) | hsf, flag_v = (tc_form(h) ? FFT_IN_EF : 0) | hsf;
+  const bool f64 = f64_sums(h);
   const int* d_lcut = (const int*)cx.dev(lv.lcut_idx);
   const double* d_or2 = (const double*)cx.dev(lv.or2_idx);
   FftSet fs{};
@@ -473,7 +502,7 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
   auto flush_fft = [&]() -> int {
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_INV);
-      CK(launch_fft_inverse(g, fs, f64, h->fft_rows, h->stream));
+      CK(launch_fft_inverse(g, fs, fft_arith(h), h->fft_rows, h->stream));
       fs.nf = 0;
     }
     return MAGIC_SHT_OK;
@@ -524,7 +553,7 @@ int run_forward_vectors(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv, co
                         const std::vector<int>& hs_vc, const int* d_lcut) {
   const ShtGeom& g = h->g;
   const long long hs_ld = (long long)g.n_m * g.n_theta;
-  const bool f64 = fp64_pipes(h);
+  const bool f64 = f64_sums(h);
   for (size_t i0 = 0; i0 < vc.size(); i0 += MAGIC_MAX_FIELDS) {
     FwdSet s{};
     s.nlev = lv.nlev; s.lcut = d_lcut; s.lcut0 = lv.lcut0;
@@ -548,14 +577,15 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
                 const std::vector<int>& hs_sc, const std::vector<int>& hs_vc) {
   const ShtGeom& g = h->g;
   const long long hs_ld = (long long)g.n_m * g.n_theta;
-  const bool f64 = fp64_pipes(h);
+  const bool f64 = f64_sums(h);
+  const int hsf = fft_hs_flag(h);
   const int* d_lcut = (const int*)cx.dev(lv.lcut_idx);
   FftSet fs{};
   fs.nlev = lv.nlev;
   auto flush_fft = [&]() -> int {
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_FWD);
-      CK(launch_fft_forward(g, fs, f64, h->fft_rows, h->stream));
+      CK(launch_fft_forward(g, fs, fft_arith(h), h->fft_rows, h->stream));
       fs.nf = 0;
     }
     return MAGIC_SHT_OK;
@@ -567,10 +597,10 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
     f.flags = flags; f.pad_ = 0;
     return MAGIC_SHT_OK;
   };
-  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(sc[i].in, cx.dev(hs_sc[i]), FFT_WEIGHT));
+  for (size_t i = 0; i < sc.size(); ++i) TRY(add_fft(sc[i].in, cx.dev(hs_sc[i]), FFT_WEIGHT | hsf));
   for (size_t i = 0; i < vc.size(); ++i) {
-    TRY(add_fft(vc[i].in_t, cx.dev(hs_vc[2 * i]), FFT_WEIGHT | FFT_OSIN2));
-    TRY(add_fft(vc[i].in_p, cx.dev(hs_vc[2 * i + 1]), FFT_WEIGHT | FFT_OSIN2));
+    TRY(add_fft(vc[i].in_t, cx.dev(hs_vc[2 * i]), FFT_WEIGHT | FFT_OSIN2 | hsf));
+    TRY(add_fft(vc[i].in_p, cx.dev(hs_vc[2 * i + 1]), FFT_WEIGHT | FFT_OSIN2 | hsf));
   }
   TRY(flush_fft());
   for (size_t i0 = 0; i0 < sc.size(); i0 += MAGIC_MAX_FIELDS) {
@@ -726,7 +756,7 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   const int ld = d->nlat_padded > 0 ? d->nlat_padded : N;
   if (ld < N) return set_err(MAGIC_SHT_ERR_SIZE, "nlat_padded=%d < n_theta_max=%d", ld, N);
   if (d->precision != MAGIC_SHT_FP64 && d->precision != MAGIC_SHT_FP32 && d->precision != MAGIC_SHT_BF16X3 &&
-      d->precision != MAGIC_SHT_TF32X2)
+      d->precision != MAGIC_SHT_TF32X2 && d->precision != MAGIC_SHT_FP64TC)
     return set_err(MAGIC_SHT_ERR_ARG, "unknown precision %d", d->precision);
 
   int dev = d->device;
@@ -775,6 +805,7 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   INIT_CK(cudaMalloc((void**)&h->d_dP, sizeof(double) * tab));
   INIT_CK(cudaMalloc((void**)&h->d_tw64, sizeof(double2) * P));
   INIT_CK(cudaMalloc((void**)&h->d_tw32, sizeof(float2) * P));
+  INIT_CK(cudaMalloc((void**)&h->d_twdf, sizeof(float4) * P));
   if (h->precision == MAGIC_SHT_FP32) {
     INIT_CK(cudaMalloc((void**)&h->d_P32, sizeof(float) * tab));
     INIT_CK(cudaMalloc((void**)&h->d_dP32, sizeof(float) * tab));
@@ -787,13 +818,17 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   {
     std::vector<double2> tw(P);
     std::vector<float2> tw32(P);
+    std::vector<float4> twdf(P);
     for (int k = 0; k < P; ++k) {
       const long double a = 2.0L * 3.14159265358979323846264338327950288L * (long double)k / (long double)P;
       tw[k] = make_double2((double)cosl(a), (double)sinl(a));
       tw32[k] = make_float2((float)tw[k].x, (float)tw[k].y);
+      const float ch = (float)cosl(a), sh = (float)sinl(a);
+      twdf[k] = make_float4(ch, (float)(cosl(a) - (long double)ch), sh, (float)(sinl(a) - (long double)sh));
     }
     INIT_CK(cudaMemcpyAsync(h->d_tw64, tw.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, h->stream));
     INIT_CK(cudaMemcpyAsync(h->d_tw32, tw32.data(), sizeof(float2) * P, cudaMemcpyHostToDevice, h->stream));
+    INIT_CK(cudaMemcpyAsync(h->d_twdf, twdf.data(), sizeof(float4) * P, cudaMemcpyHostToDevice, h->stream));
     INIT_CK(cudaStreamSynchronize(h->stream));
   }
   INIT_CK(build_tables_fp64(L, m_max, minc, N, h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP,
@@ -804,8 +839,43 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   INIT_CK(build_td_coef(g, h->d_tdcoef, h->d_tdlq, h->stream));
   INIT_CK(cudaStreamSynchronize(h->stream));
   g.P64 = h->d_P; g.dP64 = h->d_dP; g.P32 = h->d_P32; g.dP32 = h->d_dP32;
-  g.wgt = h->d_wgt; g.osin2 = h->d_osin2; g.tw64 = h->d_tw64; g.tw32 = h->d_tw32;
-  if (tc_form(h)) {
+  g.wgt = h->d_wgt; g.osin2 = h->d_osin2; g.tw64 = h->d_tw64; g.tw32 = h->d_tw32; g.twdf = h->d_twdf;
+  if (oz_form(h)) {
+    if (prop.major != 10)
+      return fail(set_err(MAGIC_SHT_ERR_UNSUPPORTED, "the tensor-core form needs tcgen05 (sm_10x)"));
+    h->tc_persistent = true;
+    TcTables& t = h->tct;
+    std::vector<long long> ib, fb;
+    long long ninv = 0, nfwd = 0;
+    oz_table_layout(g, &t.ntt, &t.nlt, &t.ncj, ib, fb, &ninv, &nfwd);
+    INIT_CK(cudaMalloc((void**)&h->d_inv_img, (size_t)ninv * 16384));
+    INIT_CK(cudaMalloc((void**)&h->d_fwd_img, (size_t)nfwd * 16384));
+    INIT_CK(cudaMalloc((void**)&h->d_inv_blk0, sizeof(long long) * n_m));
+    INIT_CK(cudaMalloc((void**)&h->d_fwd_blk0, sizeof(long long) * n_m));
+    INIT_CK(cudaMalloc((void**)&h->d_inv_exp, sizeof(short) * 2 * n_m * t.ntt * 128));
+    INIT_CK(cudaMalloc((void**)&h->d_fwd_exp, sizeof(short) * 2 * (size_t)K));
+    INIT_CK(cudaMemcpy(h->d_inv_blk0, ib.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
+    INIT_CK(cudaMemcpy(h->d_fwd_blk0, fb.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
+    std::vector<long long> pc(n_m);
+    t.npc = 0;
+    for (int mc = 0; mc < n_m; ++mc) {
+      pc[mc] = t.npc;
+      t.npc += 2LL * tc_nch(L - mc * minc + 1);
+    }
+    INIT_CK(cudaMalloc((void**)&h->d_bpc0, sizeof(long long) * n_m));
+    INIT_CK(cudaMalloc((void**)&h->d_tile_ctr, 256));
+    t.tile_ctr = h->d_tile_ctr;
+    INIT_CK(cudaMemcpy(h->d_bpc0, pc.data(), sizeof(long long) * n_m, cudaMemcpyHostToDevice));
+    t.bpc0 = h->d_bpc0;
+    INIT_CK(cudaMemset(h->d_fwd_exp, 0, sizeof(short) * 2 * (size_t)K));
+    t.inv_img = h->d_inv_img; t.fwd_img = h->d_fwd_img;
+    t.inv_blk0 = h->d_inv_blk0; t.fwd_blk0 = h->d_fwd_blk0;
+    t.inv_exp = h->d_inv_exp; t.fwd_exp = h->d_fwd_exp;
+    t.err = h->d_err;
+    INIT_CK(build_oz_images(g, t, h->d_inv_img, h->d_inv_exp, h->d_fwd_img, h->d_fwd_exp, h->stream));
+    INIT_CK(cudaStreamSynchronize(h->stream));
+  }
+  if (split_form(h)) {
     if (prop.major != 10)
       return fail(set_err(MAGIC_SHT_ERR_UNSUPPORTED, "the tensor-core form needs tcgen05 (sm_10x)"));
     const char* kern = getenv("MAGIC_SHT_TC_KERNEL");
@@ -864,7 +934,8 @@ int magic_sht_finalize(magic_sht_handle* h) {
   void* ptrs[] = {h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP, h->d_wgt, h->d_osin2,
                   h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws, h->d_inv_img, h->d_fwd_img,
                   h->d_inv_blk0, h->d_fwd_blk0, h->d_inv_scale, h->d_fwd_scale, h->d_err,
-                  h->d_bpc0, h->d_bimg, h->d_tile_ctr, h->d_tdcoef, h->d_tdlq};
+                  h->d_bpc0, h->d_bimg, h->d_tile_ctr, h->d_tdcoef, h->d_tdlq, h->d_twdf,
+                  h->d_inv_exp, h->d_fwd_exp};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->pin) cudaFreeHost(h->pin);
@@ -945,7 +1016,7 @@ int magic_sht_set_tuning(magic_sht_handle* h, const magic_sht_tuning* t) {
     return set_err(MAGIC_SHT_ERR_ARG, "fft_rows is 0, 8 or 16");
   if (t->tc_kernel == 1 && tf32_form(h))
     return set_err(MAGIC_SHT_ERR_UNSUPPORTED, "the TF32 form has only the persistent kernels");
-  if (tc_form(h)) h->tc_persistent = t->tc_kernel == 0;
+  if (split_form(h) || oz_form(h)) h->tc_persistent = t->tc_kernel == 0;
   h->tct.order = t->tc_order;
   h->pipe_chunk = t->pipe_chunk;
   h->fft_rows = t->fft_rows;
@@ -970,7 +1041,14 @@ int magic_sht_reserve(magic_sht_handle* h, int n) {
   // plus per-level lcut/or2 staging
   const size_t need = (tc_form(h) ? 23 : 15) * align256(hs_bytes(h, n)) + 4 * align256((size_t)n * 8) + 4096;
   TRY(ensure_ws(h, need));
-  if (tc_form(h) && h->tc_persistent) {
+  if (oz_form(h) && h->tc_persistent) {
+    const ShtGeom& g = h->g;
+    size_t b = oz_data_bytes(g, h->tct, 7 * n, true);
+    b = std::max(b, oz_data_bytes(g, h->tct, 4 * n * 2, true));
+    b = std::max(b, oz_data_bytes(g, h->tct, n, false));
+    b = std::max(b, oz_data_bytes(g, h->tct, 3 * n * 2, false));
+    TRY(ensure_bimg(h, b));
+  } else if (tc_form(h) && h->tc_persistent) {
     // data images of the radial set's largest tensor-core launch (7 scalar + 4 vector
     // syntheses, 1 scalar + 3 vector analyses per level)
     const ShtGeom& g = h->g;
@@ -1446,8 +1524,7 @@ int magic_sht_get_nl(magic_sht_handle* h, int n, const double* or2, const magic_
   TRY(cx.prepare());
   {
     PhaseScope sc(h, MAGIC_SHT_PHASE_NL);
-    CK(launch_get_nl(g, in, out, (const double*)cx.dev(i_or2), 1.0, n, h->precision != MAGIC_SHT_FP64,
-                     h->stream));
+    CK(launch_get_nl(g, in, out, (const double*)cx.dev(i_or2), 1.0, n, !f64_sums(h), h->stream));
   }
   return cx.finish();
 }
@@ -1498,7 +1575,7 @@ int magic_sht_get_td_nbc(magic_sht_handle* h, int n, const double* r, const int*
   t.lq = h->d_tdlq;
   {
     PhaseScope sc(h, MAGIC_SHT_PHASE_TD);
-    CK(launch_get_td(g, t, n, h->precision != MAGIC_SHT_FP64, h->stream));
+    CK(launch_get_td(g, t, n, !f64_sums(h), h->stream));
   }
   return cx.finish();
 }
@@ -2020,7 +2097,7 @@ extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double*
   {
     PhaseScope ps(h, MAGIC_SHT_PHASE_INV_LEG_SCALAR);
     if (h->precision == MAGIC_SHT_BF16X3) CK(launch_inv_legendre_tc(g, s, false, h->tct, h->stream));
-    else CK(launch_inv_legendre_simt(g, s, false, fp64_pipes(h), h->stream));
+    else CK(launch_inv_legendre_simt(g, s, false, f64_sums(h), h->stream));
   }
   FftSet fs{};
   fs.nf = 1;
@@ -2029,10 +2106,12 @@ extern "C" int magic_sht_scal_to_spat_noalloc(magic_sht_handle* h, const double*
   fs.f[0].out = fieldc;
   fs.f[0].in_ld = hs_ld;
   fs.f[0].out_ld = (long long)g.n_phi * g.ld;
-  fs.f[0].flags = tc_form(h) ? FFT_IN_E : 0;  // parity-separated synthesis output
+  // parity-separated synthesis output of the 3xBF16 one-tile kernel; FP64 half
+  // spectra into the double-float FFT of the FP64-accurate form
+  fs.f[0].flags = (h->precision == MAGIC_SHT_BF16X3 ? FFT_IN_E : 0) | (oz_form(h) ? FFT_HS_F64 : 0);
   {
     PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_INV);
-    CK(launch_fft_inverse(g, fs, fp64_pipes(h), h->fft_rows, h->stream));
+    CK(launch_fft_inverse(g, fs, fft_arith(h), h->fft_rows, h->stream));
   }
   return MAGIC_SHT_OK;
 }

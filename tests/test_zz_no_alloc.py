@@ -5,8 +5,8 @@ It serves callers that must not allocate device memory while they run (GPU
 memory owned by a pool allocator, time-critical loops that cannot absorb the
 device synchronisation of cudaMalloc/cudaFree): its only scratch is a static
 device array shared by all calls.  Two calls in a row must both reproduce the
-ordinary entry point (FP64 form: 1e-12 relative, the tolerance of the parity
-tests; the 3xBF16 form: its own 2e-6), and oversized grids and host pointers
+ordinary entry point (FP64 form and FP64-accurate tensor-core form: 1e-12
+relative, the tolerance of the parity tests; the 3xBF16 form: its own 2e-6), and oversized grids and host pointers
 are rejected with an error code.  This file is collected last on purpose."""
 import ctypes
 
@@ -26,7 +26,7 @@ def torch():
     return torch
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("bf16x3", 2e-6)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("bf16x3", 2e-6), ("fp64tc", 1e-12)])
 def test_noalloc_matches_ordinary_entry_point(torch, prec, tol):
     from magic_gb300 import SHT, _lib
     from magic_gb300.workload import spectra
