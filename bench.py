@@ -45,11 +45,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stage", action="store_true", help="skip the radial-loop stage measurement")
-    ap.add_argument("--no-variant", action="store_true", help="skip the TF32 variant of the tensor-core form")
+    ap.add_argument("--no-variant", action="store_true", help="skip the other precision forms (3xBF16, 2xTF32)")
     ap.add_argument("--levels", type=int, default=N_LEVELS, help="radial levels (profiling cases)")
     ap.add_argument("--instances", action="store_true",
                     help="instead of the bench line: sixteen mixed-size instances in one graph (one JSON line)")
     ap.add_argument("--only-reduced", action="store_true", help="skip the FP64 form (profiling)")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other configurations (C0, C1, C3, C4)")
     ap.add_argument("--clock-seconds", type=float, default=1.5,
                     help="back-to-back steps sampled for clocks before the timed steps")
     return ap.parse_args()
@@ -308,6 +309,207 @@ def cpu_baseline(levels: int):
             "sample": "%d levels of the full 15+10 transform set at l_max=255 (oracle, OpenMP)" % levels}
 
 
+def tc_available(local) -> bool:
+    from magic_gb300 import SHT
+    try:
+        SHT(15, 1, 24, 48, precision="fp64tc", device=local).close()
+        return True
+    except Exception:
+        return False
+
+
+def field_errors(a_g, a_l, b_g, b_l):
+    """Relative L2 of every output field of a against b, the normwise error
+    of every call (a vector field's three grids, the q, s, t of one
+    spat_to_qst) and the fields above 1e-6."""
+    import torch
+    errs = {}
+    for a, b in ((a_g, b_g), (a_l, b_l)):
+        for k in b:
+            errs[k] = float(torch.linalg.vector_norm(a[k] - b[k]) / torch.linalg.vector_norm(b[k]))
+    groups = {"v": ("vrc", "vtc", "vpc"), "curl v": ("cvrc", "cvtc", "cvpc"), "b": ("brc", "btc", "bpc"),
+              "curl b": ("cbrc", "cbtc", "cbpc"), "Adv": ("AdvrLM", "AdvtLM", "AdvpLM"),
+              "VS": ("VSrLM", "VStLM", "VSpLM"), "VxB": ("VxBrLM", "VxBtLM", "VxBpLM")}
+    allm = dict({k: (a_g[k], b_g[k]) for k in b_g}, **{k: (a_l[k], b_l[k]) for k in b_l})
+    normwise = {}
+    for name, ks in groups.items():
+        if not all(k in allm for k in ks):
+            continue
+        num = sum(float(torch.linalg.vector_norm(allm[k][0] - allm[k][1])) ** 2 for k in ks)
+        den = sum(float(torch.linalg.vector_norm(allm[k][1])) ** 2 for k in ks)
+        normwise[name] = (num / den) ** 0.5
+    for k in ("sc", "pc", "xic", "heatTermsLM"):
+        if k in errs:
+            normwise[k] = errs[k]
+    over = sorted(k for k, v in errs.items() if not v <= 1e-6)
+    return {"max": max(errs.values()), "per_field": errs, "max_normwise_per_call": max(normwise.values()),
+            "normwise_per_call": normwise, "over_1e-6": over, "every_output_within_1e-6": not over}
+
+
+def checkpoint_accuracy(form, local):
+    """The report of field_errors on the reference's own sample spectra
+    (samples/boussBenchSat/checkpoint_end.start: l_max = 64, minc = 4, five
+    radial levels of w, z, s, b, j, committed as tests/golden/
+    checkpoint_spectra.npz): the radial-loop synthesis set with every spectral
+    slot filled from the checkpoint field of its kind (radial derivatives are
+    not in the checkpoint), the nonlinear products of the FP64 grids, then
+    the analysis set; `form` against the FP64 form."""
+    import numpy as np
+    import torch
+    from magic_gb300 import SHT
+    d = np.load(os.path.join(ROOT, "tests", "golden", "checkpoint_spectra.npz"))
+    L, minc, N = int(d["l_max"]), int(d["minc"]), int(d["n_theta_max"])
+    P = int(d["n_phi_tot"]) // minc
+    w, z, s, b, j = (d[k] for k in ("wpol", "ztor", "entropy", "bpol", "btor"))
+    spec = {"s": s, "p": s, "xi": s, "w": w, "dw": w, "ddw": w, "z": z, "dz": z,
+            "b": b, "db": b, "ddb": b, "aj": j, "dj": j}
+    spec = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in spec.items()}
+    or2 = 1.0 / np.asarray(d["radius"], dtype=np.float64) ** 2
+    s64 = SHT(L, minc, N, P, precision="fp64", device=local)
+    sm = SHT(L, minc, N, P, precision=form, device=local)
+    g64 = s64.transform_to_grid_space(spec, or2=or2)
+    nl = s64.get_nl(g64, or2=or2)
+    l64 = s64.transform_to_lm_space(nl)
+    gm = sm.transform_to_grid_space(spec, or2=or2)
+    lm = sm.transform_to_lm_space(nl)
+    torch.cuda.synchronize()
+    sm.device_status()
+    out = field_errors(gm, lm, g64, l64)
+    out["what"] = ("reference sample spectra (boussBenchSat checkpoint, l_max=%d, minc=%d, %d levels); "
+                   "analysis inputs = get_nl of the FP64 grids" % (L, minc, w.shape[0]))
+    s64.close()
+    sm.close()
+    return out
+
+
+def batched_set_ms(s, spec, fin, or2, batch, steps, warmup):
+    """Both transform sets over every level in batches of `batch` levels (the
+    large configuration does not keep all levels' grids resident); `fin`
+    holds the analysis inputs of one batch, reused by every batch.  Returns
+    the ms of one pass (CUDA events, mean of `steps`)."""
+    import torch
+    n = next(iter(spec.values())).shape[0]
+    st = torch.cuda.current_stream()
+    out_g, out_l = {}, {}
+
+    def one():
+        for r0 in range(0, n, batch):
+            r1 = min(n, r0 + batch)
+            full = r1 - r0 == batch
+            g = s.transform_to_grid_space({k: v[r0:r1] for k, v in spec.items()}, or2=or2[r0:r1],
+                                          out=out_g if (full and out_g) else None)
+            lm = s.transform_to_lm_space({k: v[:r1 - r0] for k, v in fin.items()},
+                                         out=out_l if (full and out_l) else None)
+            if full and not out_g:
+                out_g.update(g)
+                out_l.update(lm)
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(steps):
+        one()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def config_measure(name, L, minc, N, P, R, forms, local, hbm, full_set=True, batch=None, steps=3,
+                   cpu_levels=0, what=""):
+    """One configuration: every form's levels/s over R levels of the radial
+    set (or of the scalar + QST round trip when full_set is False), its
+    per-output error against the FP64 form, the dominant kernel's HBM
+    fraction, and the oracle's CPU rate on a bounded sample."""
+    import torch
+    from magic_gb300 import SHT
+    from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
+    fields = None if full_set else ("s", "w", "dw", "z")
+    spec_np = grid_space_inputs(L, minc, R, seed=4321 + L)
+    if fields:
+        spec_np = {k: v for k, v in spec_np.items() if k in fields}
+    spec = {k: torch.from_numpy(v).cuda() for k, v in spec_np.items()}
+    or2 = torch.from_numpy(or2_levels(R)).cuda()
+    fwd_map = FORWARD_FROM_INVERSE if full_set else {"Advr": "vrc", "Advt": "vtc", "Advp": "vpc",
+                                                      "heatTerms": "sc"}
+    batch = batch or R
+    res = {"workload": what, "l_max": L, "minc": minc, "n_theta": N, "n_phi": P, "levels": R, "forms": {}}
+    ref = None
+    t2_of = {"fp64": 16, "fp64tc": 16}
+    for form in forms:
+        s = SHT(L, minc, N, P, precision=form, device=local)
+        s.reserve(batch)
+        g = s.transform_to_grid_space({k: v[:batch] for k, v in spec.items()}, or2=or2[:batch])
+        fin_b = {k: g[v] for k, v in fwd_map.items()}
+        lm = s.transform_to_lm_space(fin_b)
+        if form == "fp64":
+            ref = (g, fin_b, lm)
+        # analysis inputs of every form and batch: the FP64 form's synthesis grids of the first batch
+        fin = ref[1] if ref else fin_b
+        ms = batched_set_ms(s, spec, fin, or2, batch, 1 if form == "fp64" else steps, 1)
+        entry = {"value": R / (ms * 1e-3), "unit": "levels/s", "ms_per_step": ms}
+        if ref is not None and form != "fp64":
+            gm = s.transform_to_grid_space({k: v[:batch] for k, v in spec.items()}, or2=or2[:batch])
+            lmm = s.transform_to_lm_space(ref[1])
+            torch.cuda.synchronize()
+            acc = field_errors(gm, lmm, ref[0], ref[2])
+            entry["rel_l2_vs_fp64_max"] = acc["max"]
+            entry["max_normwise_per_call"] = acc["max_normwise_per_call"]
+            entry["over_1e-6"] = acc["over_1e-6"]
+            del gm, lmm
+        s.set_profiling(True)
+        s.phase_times(reset=True)
+        s.transform_to_grid_space({k: v[:batch] for k, v in spec.items()}, or2=or2[:batch])
+        s.transform_to_lm_space(fin)
+        ph = s.phase_times(reset=True)
+        s.set_profiling(False)
+        s.device_status()
+        alg, _ = algorithmic_per_level(L, N, P, minc, t2_of.get(form, 8))
+        dom = max(ph, key=lambda k: ph[k][0])
+        if dom in alg and ph[dom][0] > 0:
+            gbs = alg[dom]["bytes"] * batch / (ph[dom][0] * 1e-3) / 1e9
+            entry["dominant_kernel"] = {"phase": dom, "ms_per_batch": ph[dom][0], "achieved_gbs": gbs,
+                                        "hbm_frac": gbs / hbm}
+        entry["phases_ms_per_batch"] = {k: v[0] for k, v in ph.items() if v[1]}
+        res["forms"][form] = entry
+        s.close()
+        del g, lm, fin_b, fin
+        torch.cuda.synchronize()
+    if "fp64" in res["forms"]:
+        for f, e in res["forms"].items():
+            e["speedup_vs_fp64_gpu"] = e["value"] / res["forms"]["fp64"]["value"]
+    del ref
+    torch.cuda.synchronize()
+    if cpu_levels > 0:
+        from oracle import oracle
+        oracle.build_oracle()
+        threads = os.cpu_count() or 1
+        oracle.set_threads(threads)
+        o = oracle.OracleSHT(L, minc, N, P)
+        t0 = time.perf_counter()
+        for r in range(cpu_levels):
+            if full_set:
+                sc = o.scal_to_spat(spec_np["s"][r])
+                o.scal_to_spat(spec_np["p"][r])
+                o.scal_to_spat(spec_np["xi"][r])
+                v = o.torpol_to_spat(spec_np["w"][r], spec_np["dw"][r], spec_np["z"][r])
+                o.torpol_to_curl_spat(0.7, spec_np["w"][r], spec_np["ddw"][r], spec_np["z"][r], spec_np["dz"][r])
+                o.torpol_to_spat(spec_np["b"][r], spec_np["db"][r], spec_np["aj"][r])
+                o.torpol_to_curl_spat(0.7, spec_np["b"][r], spec_np["ddb"][r], spec_np["aj"][r], spec_np["dj"][r])
+                for _ in range(3):
+                    o.spat_to_qst(*v)
+                o.scal_to_SH(sc)
+            else:
+                f = o.scal_to_spat(spec_np["s"][r])
+                v = o.torpol_to_spat(spec_np["w"][r], spec_np["dw"][r], spec_np["z"][r])
+                o.spat_to_qst(*v)
+                o.scal_to_SH(f)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": cpu_levels / dt, "unit": "levels/s", "cores": threads, "kind": "port",
+                               "sample": "%d of %d levels (oracle, OpenMP)" % (cpu_levels, R)}
+    return res
+
+
 def our_arm(args):
     global N_LEVELS
     N_LEVELS = args.levels
@@ -327,12 +529,7 @@ def our_arm(args):
     hbm, bf16, peak_kind = peaks()
     form = args.form
     if form == "auto":
-        form = "fp32"
-        try:
-            SHT(15, 1, 24, 48, precision="bf16x3", device=local).close()
-            form = "bf16x3"
-        except Exception:
-            form = "fp32"
+        form = "fp64tc" if tc_available(local) else "fp32"
 
     spec_np = grid_space_inputs(L_MAX, MINC, N_LEVELS, seed=1234 + 7919 * rank)
     spec = {k: torch.from_numpy(v).to(dev) for k, v in spec_np.items()}
@@ -381,7 +578,7 @@ def our_arm(args):
             ms = float(t.item())
         return ms, per_step_launches * steps, per
 
-    # ---- FP64 form; its synthesis grids give the analysis inputs of both forms
+    # ---- FP64 form; its synthesis grids give the analysis inputs of every form
     # (the grid-space nonlinear products of get_nl, outside the timed steps)
     s64 = SHT(L_MAX, MINC, N_THETA, N_PHI, precision="fp64", device=local)
     fin.update(s64.get_nl(s64.transform_to_grid_space(spec, or2=or2), or2=or2_np))
@@ -394,7 +591,7 @@ def our_arm(args):
         ms64, _, _ = time_steps(s64, g64, l64, k64)
         lev64 = world * N_LEVELS * k64 / (ms64 * 1e-3)
 
-    # ---- reduced-precision form (headline)
+    # ---- headline form
     sm = SHT(L_MAX, MINC, N_THETA, N_PHI, precision=form, device=local)
     gm, lmx = run_set(sm, None, None)
     for _ in range(max(0, args.warmup - 1)):
@@ -420,60 +617,48 @@ def our_arm(args):
         print(json.dumps({"form": form, "value": value, "ms_per_step": ms / args.steps, "levels": N_LEVELS,
                           "phases_ms": {k: v[0] for k, v in ph.items() if v[1]}}), flush=True)
         return
-    # ---- accuracy of the reduced form against the FP64 form (same inputs)
+    # ---- accuracy of the headline form against the FP64 form (same inputs): every output
     run_set(sm, gm, lmx)
     run_set(s64, g64, l64)
     torch.cuda.synchronize()
     sm.device_status()
-    errs = {}
-    for k in g64:
-        errs[k] = float(torch.linalg.vector_norm(gm[k] - g64[k]) / torch.linalg.vector_norm(g64[k]))
-    for k in l64:
-        errs[k] = float(torch.linalg.vector_norm(lmx[k] - l64[k]) / torch.linalg.vector_norm(l64[k]))
-    max_err = max(errs.values())
-    maxabs = max(float((gm[k] - g64[k]).abs().max() / g64[k].abs().max()) for k in g64)
-    # normwise over the outputs of one call (a vector field's three grids, or the
-    # q, s, t of one spat_to_qst): insensitive to one output being much smaller
-    # than its partners
-    groups = {"v": ("vrc", "vtc", "vpc"), "curl v": ("cvrc", "cvtc", "cvpc"), "b": ("brc", "btc", "bpc"),
-              "curl b": ("cbrc", "cbtc", "cbpc"), "Adv": ("AdvrLM", "AdvtLM", "AdvpLM"),
-              "VS": ("VSrLM", "VStLM", "VSpLM"), "VxB": ("VxBrLM", "VxBtLM", "VxBpLM")}
-    allm = {**{k: (gm[k], g64[k]) for k in g64}, **{k: (lmx[k], l64[k]) for k in l64}}
-    normwise = {}
-    for name, ks in groups.items():
-        num = sum(float(torch.linalg.vector_norm(allm[k][0] - allm[k][1])) ** 2 for k in ks)
-        den = sum(float(torch.linalg.vector_norm(allm[k][1])) ** 2 for k in ks)
-        normwise[name] = (num / den) ** 0.5
-    for k in ("sc", "pc", "xic", "heatTermsLM"):
-        normwise[k] = errs[k]
-    max_normwise = max(normwise.values())
+    acc = field_errors(gm, lmx, g64, l64)
+    acc["max_abs_over_max"] = max(float((gm[k] - g64[k]).abs().max() / g64[k].abs().max()) for k in g64)
+    # the whole chain in the headline form: its synthesis grids -> get_nl on its
+    # handle -> its analysis, against the same chain on the FP64 handle
+    gA = sm.transform_to_grid_space(spec, or2=or2)
+    lA = sm.transform_to_lm_space(sm.get_nl(gA, or2=or2_np))
+    torch.cuda.synchronize()
+    chain = field_errors(gA, lA, g64, l64)
+    chain["what"] = ("synthesis -> get_nl -> analysis, all on the %s handle, against the same chain "
+                     "on the FP64 handle" % form)
+    del gA, lA
+    checkpoint = checkpoint_accuracy(form, local)
 
-    # ---- the TF32 variant of the tensor-core form (2xTF32 split products):
-    # same step, timing and normwise accuracy, reported beside the headline
-    variant = None
-    if form == "bf16x3" and not args.no_variant:
-        sv = SHT(L_MAX, MINC, N_THETA, N_PHI, precision="tf32x2", device=local)
-        gv, lv = run_set(sv, None, None)
-        for _ in range(max(0, args.warmup - 1)):
+    # ---- the other precision forms: same step, timing and accuracy, beside the headline
+    others = {}
+    if not args.no_variant:
+        for f in ("bf16x3", "tf32x2"):
+            if f == form:
+                continue
+            sv = SHT(L_MAX, MINC, N_THETA, N_PHI, precision=f, device=local)
+            gv, lv = run_set(sv, None, None)
+            for _ in range(max(0, args.warmup - 1)):
+                run_set(sv, gv, lv)
+            msv, _, perv = time_steps(sv, gv, lv, args.steps)
             run_set(sv, gv, lv)
-        msv, _, perv = time_steps(sv, gv, lv, args.steps)
-        run_set(sv, gv, lv)
-        torch.cuda.synchronize()
-        sv.device_status()
-        allv = {**{k: (gv[k], g64[k]) for k in g64}, **{k: (lv[k], l64[k]) for k in l64}}
-        nwv = {}
-        for name, ks in groups.items():
-            num = sum(float(torch.linalg.vector_norm(allv[k][0] - allv[k][1])) ** 2 for k in ks)
-            den = sum(float(torch.linalg.vector_norm(allv[k][1])) ** 2 for k in ks)
-            nwv[name] = (num / den) ** 0.5
-        for k in ("sc", "pc", "xic", "heatTermsLM"):
-            nwv[k] = float(torch.linalg.vector_norm(allv[k][0] - allv[k][1]) / torch.linalg.vector_norm(allv[k][1]))
-        variant = {"form": "tf32x2", "value": world * N_LEVELS * args.steps / (msv * 1e-3), "unit": "levels/s",
-                   "ms_per_step": msv / args.steps, "median_ms_per_step": statistics.median(perv),
-                   "speedup_vs_fp64_gpu": (world * N_LEVELS * args.steps / (msv * 1e-3)) / lev64,
-                   "max_normwise_per_call": max(nwv.values()), "normwise_per_call": nwv}
-        sv.close()
-        del gv, lv
+            torch.cuda.synchronize()
+            sv.device_status()
+            av = field_errors(gv, lv, g64, l64)
+            vv = world * N_LEVELS * args.steps / (msv * 1e-3)
+            others[f] = {"value": vv, "unit": "levels/s", "ms_per_step": msv / args.steps,
+                         "median_ms_per_step": statistics.median(perv), "speedup_vs_fp64_gpu": vv / lev64,
+                         "rel_l2_vs_fp64_max": av["max"], "over_1e-6": av["over_1e-6"],
+                         "max_normwise_per_call": av["max_normwise_per_call"],
+                         "rel_l2_vs_fp64": av}
+            sv.close()
+            del gv, lv
+            torch.cuda.synchronize()
 
     # ---- per-phase kernel timing (CUDA events on the launching stream)
     sm.set_profiling(True)
@@ -488,9 +673,11 @@ def our_arm(args):
     ph64 = s64.phase_times(reset=True)
     s64.set_profiling(False)
 
-    t2 = 16 if form == "fp64" else 8
+    t2 = 16 if form in ("fp64", "fp64tc") else 8
     alg, K = algorithmic_per_level(L_MAX, N_THETA, N_PHI, MINC, t2)
-    tab_elem = 4
+    # table bytes per Legendre launch: the split images (7 bf16 digits for
+    # fp64tc, 3 bf16 for bf16x3, 2 tf32 for tf32x2) of P and dP
+    tab_elem = {"fp64tc": 14, "bf16x3": 6, "tf32x2": 8, "fp32": 4, "fp64": 8}[form]
     dom = max(ph, key=lambda k: ph[k][0])
     dom_ms, dom_n = ph[dom]
     per_launch_ms = dom_ms / max(dom_n, 1)
@@ -521,6 +708,11 @@ def our_arm(args):
         roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                 "frac": achieved_gbs / hbm, "traffic": traffic, "kernel": dom,
                 "peak_source": peak_kind}
+        if form == "fp64tc" and "fft" in dom:
+            # the double-float FFTs execute ~10 FP32 operations per FP32-FFT operation:
+            # their binding pipe is FP32 issue; the FP32 probe beside the HBM figure
+            roof["note"] = ("double-float FFT: FP32-pipe bound (HBM fraction reported as the contract's "
+                            "roofline; FP32 FMA probe %.1f TFLOP/s in this run)" % (fp32_peak / 1e3))
     phases = {k: {"ms_per_step": v[0] / 2, "launches_per_step": v[1] // 2} for k, v in ph.items() if v[1]}
     # every phase against its own roofline: algorithmic bytes (tables once per
     # launch for the Legendre phases, whose time includes their pack kernels)
@@ -538,6 +730,10 @@ def our_arm(args):
             fl = alg[k]["flops"] * N_LEVELS
             v["achieved_tflops"] = fl / sec / 1e12
             v["tensor_frac_of_bf16_peak"] = v["achieved_tflops"] / bf16 if bf16 else None
+            if form == "fp64tc":
+                # 28 digit products per algorithmic multiply-add
+                v["digit_product_tflops"] = 28 * v["achieved_tflops"]
+                v["digit_product_frac_of_bf16_peak"] = 28 * v["achieved_tflops"] / bf16 if bf16 else None
     phases64 = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in ph64.items() if v[1]}
     # FP64 form's Legendre against the FP64 pipe
     leg64_ms = sum(v[0] for k, v in ph64.items() if "leg" in k)
@@ -584,11 +780,33 @@ def our_arm(args):
                "d2h_bytes_per_step": d2h, "steps": ke,
                "path": "transform_to_grid_space + transform_to_lm_space on pinned host arrays, "
                        "asynchronous host batches, synchronized every step"}
+        del hspec, hg, hl, hfin
 
     # ---- one explicit stage of the radial loop (headline form)
     stage = None
     if not args.no_stage:
         stage = stage_measure(sm, s64, spec, N_LEVELS, max(3, min(args.steps, 10)), hbm)
+
+    # ---- the other configurations of the benchmark set (each with every form's
+    # levels/s, accuracy against the FP64 form and dominant kernel)
+    configs = None
+    if not args.no_configs and world == 1:
+        sm.close()
+        s64.close()
+        del gm, lmx, g64, l64
+        torch.cuda.synchronize()
+        configs = {
+            "C0": config_measure("C0", 64, 1, 96, 192, 33, ("fp64", form), local, hbm, full_set=False,
+                                 steps=5, cpu_levels=33,
+                                 what="scalar + toroidal/poloidal round trip, l_max=64, 96x192, 33 levels"),
+            "C1": config_measure("C1", 128, 1, 192, 384, 65, ("fp64", form), local, hbm, steps=5, cpu_levels=2,
+                                 what="full 15+10 set, l_max=128, 192x384, 65 levels"),
+            "C4": config_measure("C4", 511, 1, 768, 1536, 193, ("fp64", form, "bf16x3"), local, hbm,
+                                 batch=65, steps=1, cpu_levels=1,
+                                 what="full 15+10 set, l_max=511, 768x1536, 193 levels in batches of 65 "
+                                      "(the grids of one batch resident)"),
+        }
+        configs["C3"] = instances_measure(form, local, max(3, args.warmup), 5)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -600,7 +818,8 @@ def our_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "median_ms_per_step": statistics.median(per_step), "timing": "graph replay of one step, CUDA events per step",
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fp32": "f32", "bf16x3": "bf16x3+f32", "tf32x2": "tf32x2+f32", "fp64": "f64"}[form],
+            "dtype": {"fp32": "f32", "bf16x3": "bf16x3+f32", "tf32x2": "tf32x2+f32", "fp64": "f64",
+                      "fp64tc": "bf16 digits x7 + exact f32 accumulate; f32x2 FFT"}[form],
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": form, "l_max": L_MAX, "n_theta": N_THETA,
                        "n_phi": N_PHI, "minc": MINC, "n_levels": N_LEVELS,
@@ -609,10 +828,13 @@ def our_arm(args):
             "fp64_gpu": {"value": lev64, "unit": "levels/s", "ms_per_step": ms64 / k64,
                          "steps": k64, "legendre_frac_of_fp64_peak": fp64_leg_frac,
                          "phases": phases64},
+            "rel_l2_vs_fp64_max": acc["max"],
+            "every_output_within_1e-6": acc["every_output_within_1e-6"],
             "speedup_vs_fp64_gpu": value / lev64,
-            "variant": variant,
-            "rel_l2_vs_fp64": {"max": max_err, "max_abs_over_max": maxabs, "per_field": errs,
-                               "max_normwise_per_call": max_normwise, "normwise_per_call": normwise},
+            "rel_l2_vs_fp64": acc,
+            "accuracy_chain": chain,
+            "accuracy_checkpoint_spectra": checkpoint,
+            "other_forms": others,
             "roofline": roof,
             "phases": phases,
             "peaks": {"fp64_gflops": fp64_peak, "fp32_gflops": fp32_peak, "hbm_gbs": hbm,
@@ -621,6 +843,7 @@ def our_arm(args):
             "clocks": clocks,
             "e2e": e2e,
             "stage": stage,
+            "configs": configs,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
@@ -629,7 +852,20 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
-def instances_arm(args):
+def instances_measure(form, local, warmup, steps):
+    """The sixteen-instance batching case (see instances_arm) in `form` and in
+    3xBF16, as a nested entry of the headline line."""
+    out = {}
+    r = None
+    for f in (form, "bf16x3"):
+        r = instances_run(f, local, warmup, steps)
+        out[f] = {k: r[k] for k in ("value", "unit", "ms_per_step", "levels_per_step")}
+    out["instances"] = r["instances"]
+    out["what"] = "sixteen mixed-size instances, both transform sets, captured in one CUDA graph"
+    return out
+
+
+def instances_run(form, local, warmup, steps):
     """Sixteen independent instances of mixed size (l_max in {63, 127, 255},
     minc in {1, 4}, {33, 65, 129} radial levels, n_theta = 3(l_max+1)/2,
     n_phi = 2 n_theta / minc; a fixed seeded list), both transform sets of every
@@ -639,9 +875,6 @@ def instances_arm(args):
     import torch
     from magic_gb300 import SHT
     from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
-    world, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    form = "bf16x3" if args.form == "auto" else args.form
     rng = np.random.default_rng(1234)
     insts, desc = [], []
     for i in range(16):
@@ -671,12 +904,12 @@ def instances_arm(args):
                 s.transform_to_lm_space(fin, out=lm)
         finally:
             gr = insts[0][0].graph_end()
-        for _ in range(max(args.warmup, 3)):
+        for _ in range(max(warmup, 3)):
             insts[0][0].graph_launch(gr)
         side.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(side)
-        for _ in range(args.steps):
+        for _ in range(steps):
             insts[0][0].graph_launch(gr)
         e1.record(side)
         side.synchronize()
@@ -685,13 +918,30 @@ def instances_arm(args):
         s.device_status()
     insts[0][0].graph_destroy(gr)
     levels = sum(d["levels"] for d in desc)
+    for s, *_ in insts:
+        s.close()
+    del insts
+    torch.cuda.synchronize()
+    return {"metric": "SHT radial levels/s, sixteen mixed instances in one graph",
+            "value": levels * steps / (ms * 1e-3), "unit": "levels/s", "n_gpus": 1,
+            "steps": steps, "warmup": max(warmup, 3), "ms_per_step": ms / steps,
+            "higher_is_better": True, "form": form, "levels_per_step": levels,
+            "timing": "graph replay, CUDA events on the replay stream", "instances": desc}
+
+
+def instances_arm(args):
+    """Sixteen independent instances of mixed size (l_max in {63, 127, 255},
+    minc in {1, 4}, {33, 65, 129} radial levels, n_theta = 3(l_max+1)/2,
+    n_phi = 2 n_theta / minc; a fixed seeded list), both transform sets of every
+    instance captured into one CUDA graph on one stream and replayed.  The
+    analysis inputs are the instance's synthesis grids."""
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    form = "bf16x3" if args.form == "auto" else args.form
+    r = instances_run(form, local, args.warmup, args.steps)
     if rank == 0:
-        print(json.dumps({"metric": "SHT radial levels/s, sixteen mixed instances in one graph",
-                          "value": levels * args.steps / (ms * 1e-3), "unit": "levels/s", "n_gpus": 1,
-                          "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
-                          "higher_is_better": True, "form": form, "levels_per_step": levels,
-                          "timing": "graph replay, CUDA events on the replay stream",
-                          "instances": desc}), flush=True)
+        print(json.dumps(r), flush=True)
 
 
 def main():
