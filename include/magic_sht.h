@@ -179,6 +179,10 @@ typedef struct magic_sht_lm_space_args {
   double *VxBrLM, *VxBtLM, *VxBpLM;
   double *heatTermsLM;
   long long spec_ld;
+  /* composition (l_chemical_conv): spat_to_qst of V Xi (rIter.f90:699-702);
+   * grid inputs at grid_ld, spectral outputs at spec_ld; NULL skips them */
+  const double *VXir, *VXit, *VXip;
+  double *VXirLM, *VXitLM, *VXipLM;
 } magic_sht_lm_space_args;
 
 int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n_levels, const double* or2,
@@ -227,6 +231,50 @@ int magic_sht_get_tuning(const magic_sht_handle* h, magic_sht_tuning* t);
 int magic_sht_get_nl(magic_sht_handle* h, int n_levels, const double* or2, const magic_sht_grid_space_args* g,
                      const magic_sht_lm_space_args* nl);
 
+/* ---- the grid-space nonlinear products with the reference's switches and
+ * physical parameters (get_nl.f90:213-441) and the Lorentz-force combination
+ * of transform_to_lm_space (rIter.f90:645-662).  Per level:
+ *   Adv (where nBc = 0 and l_conv_nl or l_mag_LF): the advection, curl form
+ *     (l_adv_curl, :260-272) or u.grad u (:274-302), when l_conv_nl, plus
+ *     LFfac times the Lorentz force (:243-256) when l_mag_LF and the level is
+ *     outside the low-conductivity region;
+ *   VS, VXi (where nBc = 0 and l_heat_nl / l_chemical_conv, :316-327);
+ *   VxB (l_mag_nl, :376-395): the full product where nBc = 0 outside the
+ *     region; VxBt, VxBp of the stress-free form where nBc = 1 or inside the
+ *     region; of the rigid form (VxBp = 0) where nBc = 2; VxBr is written
+ *     with the full product only;
+ *   heatTerms (where nBc = 0 and l_anel, :398-432): viscous heating plus, with
+ *     l_mag_nl outside the region, ohmic losses.
+ * Outputs a level does not produce are left untouched (the reference leaves
+ * them as they were).  Grids: device pointers, 16-byte aligned, even grid_ld
+ * and nlat_padded; the inputs each enabled term needs must be non-NULL
+ * (velocity and vorticity; the derivative grids for u.grad u and l_anel;
+ * B and curl B for the Lorentz force, the induction and the ohmic losses; s,
+ * xi).  Per-level arrays: host or device, n_levels entries; r is required,
+ * NULL orho1 / beta / otemp1 / visc / lambda / nbc / lcr mean 1 / 0 / 1 /
+ * 1 / 1 / 0 / 0.  Arithmetic: FP64 on the FP64 and FP64-accurate tensor-core
+ * handles, FP32 (FP64 grids in and out) on the reduced forms. */
+typedef struct magic_sht_nl_opts {
+  int l_conv_nl, l_adv_curl, l_mag_LF, l_heat_nl, l_chemical_conv, l_mag_nl, l_anel, pad_;
+  double LFfac, ViscHeatFac, OhmLossFac;
+  const double *r, *orho1, *beta, *otemp1, *visc, *lambda;
+  const int *nbc;   /* nBc per level */
+  const int *lcr;   /* nonzero: nR <= n_r_LCR (inside the low-conductivity region) */
+} magic_sht_nl_opts;
+typedef struct magic_sht_nl_grids {
+  const double *vrc, *vtc, *vpc, *cvrc, *cvtc, *cvpc;
+  const double *dvrdrc, *dvtdrc, *dvpdrc, *dvrdtc, *dvrdpc, *dvtdpc, *dvpdpc;
+  const double *brc, *btc, *bpc, *cbrc, *cbtc, *cbpc;
+  const double *sc, *xic;
+  long long grid_ld;
+} magic_sht_nl_grids;
+typedef struct magic_sht_nl_out {
+  double *Advr, *Advt, *Advp, *VSr, *VSt, *VSp, *VXir, *VXit, *VXip, *VxBr, *VxBt, *VxBp, *heatTerms;
+  long long grid_ld;
+} magic_sht_nl_out;
+int magic_sht_get_nl_opts(magic_sht_handle* h, int n_levels, const magic_sht_nl_opts* opts,
+                          const magic_sht_nl_grids* in, const magic_sht_nl_out* out);
+
 /* ---- spectral assembly of the explicit time derivatives at interior radial
  * levels (get_td.f90: get_dwdt :133-208, get_dpdt :311-379, get_dzdt
  * :381-457, get_dsdt :459-521, get_dbdt :558-619) from the analysis outputs
@@ -250,6 +298,37 @@ int magic_sht_get_td(magic_sht_handle* h, int n_levels, const double* r, const i
  * is written (get_td.f90:598-612) and the other outputs are left untouched. */
 int magic_sht_get_td_nbc(magic_sht_handle* h, int n_levels, const double* r, const int* lcut, double cor_fac,
                          const double* epsc, const int* nbc, const magic_sht_td_args* a);
+
+/* ---- the spectral assembly with the reference's switches, as the radial
+ * loop calls it (rIter.f90:410-428): get_dzdt (get_td.f90:381-457),
+ * get_dwdt (:133-208) or, with l_double_curl, get_dwdt_double_curl
+ * (:210-309, also dVxVhLM), get_dpdt (:311-379), get_dsdt (:459-521: the
+ * anelastic heatTermsLM, times temp0 in the anelastic-liquid form), get_dxidt
+ * (:523-556), get_dbdt (:558-619; zeros without l_mag_nl).  An output is
+ * computed where its pointer is non-NULL (its equation is on) and left
+ * untouched otherwise; at a level with nbc != 0 only dVxBhLM, dVxVhLM (double
+ * curl; zero), dVSrLM (with dsdt; zero) and dVXirLM (with dxidt; zero) are
+ * written; dpdt and dVxVhLM at l = 0 are never written (the reference leaves
+ * them).  Spectra: device arrays [n_levels][spec_ld] complex; per-level
+ * arrays host or device (r required; NULL orho1 / beta / temp0 / epsc / lcut
+ * / nbc mean 1 / 0 / 1 / 0 / l_max / 0).  Arithmetic as magic_sht_get_td. */
+typedef struct magic_sht_td_opts {
+  int l_conv_nl, l_corr, l_double_curl, l_single_matrix, l_anel, l_anelastic_liquid, l_mag_nl, pad_;
+  double cor_fac, epscXi;
+  const double *r, *orho1, *beta, *temp0, *epsc;
+  const int *lcut, *nbc;
+} magic_sht_td_opts;
+typedef struct magic_sht_td_in {
+  const double *w, *dw, *ddw, *z, *dz;
+  const double *AdvrLM, *AdvtLM, *AdvpLM, *VStLM, *heatTermsLM, *VXitLM, *VxBrLM, *VxBtLM, *VxBpLM;
+  long long spec_ld;
+} magic_sht_td_in;
+typedef struct magic_sht_td_out {
+  double *dwdt, *dzdt, *dpdt, *dsdt, *dxidt, *dbdt, *djdt, *dVxBhLM, *dVxVhLM, *dVSrLM, *dVXirLM;
+  long long spec_ld;
+} magic_sht_td_out;
+int magic_sht_get_td_opts(magic_sht_handle* h, int n_levels, const magic_sht_td_opts* opts,
+                          const magic_sht_td_in* in, const magic_sht_td_out* out);
 
 /* ---- Courant condition of the radial loop (courant.f90:54-278, the branch
  * the reference compiles): per level, the maxima over the grid of the radial

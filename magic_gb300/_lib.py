@@ -72,9 +72,62 @@ class Tuning(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("tc_kernel", "tc_order", "pipe_chunk", "fft_rows")]
 
 
+# the composition flux of l_chemical_conv, at the end of magic_sht_lm_space_args
+LM_SPACE_IN_XI = ["VXir", "VXit", "VXip"]
+LM_SPACE_OUT_XI = ["VXirLM", "VXitLM", "VXipLM"]
+
+
 class LmSpaceArgs(ctypes.Structure):
     _fields_ = ([(n, _V) for n in LM_SPACE_IN] + [("grid_ld", ctypes.c_longlong)] +
-                [(n, _V) for n in LM_SPACE_OUT] + [("spec_ld", ctypes.c_longlong)])
+                [(n, _V) for n in LM_SPACE_OUT] + [("spec_ld", ctypes.c_longlong)] +
+                [(n, _V) for n in LM_SPACE_IN_XI + LM_SPACE_OUT_XI])
+
+
+# the general get_nl (magic_sht_get_nl_opts): switches, constants, per-level arrays
+NL_SWITCHES = ["l_conv_nl", "l_adv_curl", "l_mag_LF", "l_heat_nl", "l_chemical_conv", "l_mag_nl", "l_anel"]
+NL_PROFILES = ["r", "orho1", "beta", "otemp1", "visc", "lambda"]
+
+
+class NlOpts(ctypes.Structure):
+    _fields_ = ([(n, ctypes.c_int) for n in NL_SWITCHES + ["pad_"]] +
+                [(n, ctypes.c_double) for n in ("LFfac", "ViscHeatFac", "OhmLossFac")] +
+                [(n, _V) for n in NL_PROFILES + ["nbc", "lcr"]])
+
+
+NLF_IN = ["vrc", "vtc", "vpc", "cvrc", "cvtc", "cvpc", "dvrdrc", "dvtdrc", "dvpdrc", "dvrdtc", "dvrdpc",
+          "dvtdpc", "dvpdpc", "brc", "btc", "bpc", "cbrc", "cbtc", "cbpc", "sc", "xic"]
+NLF_OUT = ["Advr", "Advt", "Advp", "VSr", "VSt", "VSp", "VXir", "VXit", "VXip", "VxBr", "VxBt", "VxBp",
+           "heatTerms"]
+
+
+class NlGrids(ctypes.Structure):
+    _fields_ = [(n, _V) for n in NLF_IN] + [("grid_ld", ctypes.c_longlong)]
+
+
+class NlOut(ctypes.Structure):
+    _fields_ = [(n, _V) for n in NLF_OUT] + [("grid_ld", ctypes.c_longlong)]
+
+
+# the general get_td (magic_sht_get_td_opts)
+TD_SWITCHES = ["l_conv_nl", "l_corr", "l_double_curl", "l_single_matrix", "l_anel", "l_anelastic_liquid",
+               "l_mag_nl"]
+TDF_IN = ["w", "dw", "ddw", "z", "dz", "AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "heatTermsLM", "VXitLM",
+          "VxBrLM", "VxBtLM", "VxBpLM"]
+TDF_OUT = ["dwdt", "dzdt", "dpdt", "dsdt", "dxidt", "dbdt", "djdt", "dVxBhLM", "dVxVhLM", "dVSrLM", "dVXirLM"]
+
+
+class TdOpts(ctypes.Structure):
+    _fields_ = ([(n, ctypes.c_int) for n in TD_SWITCHES + ["pad_"]] +
+                [(n, ctypes.c_double) for n in ("cor_fac", "epscXi")] +
+                [(n, _V) for n in ("r", "orho1", "beta", "temp0", "epsc", "lcut", "nbc")])
+
+
+class TdIn(ctypes.Structure):
+    _fields_ = [(n, _V) for n in TDF_IN] + [("spec_ld", ctypes.c_longlong)]
+
+
+class TdOut(ctypes.Structure):
+    _fields_ = [(n, _V) for n in TDF_OUT] + [("spec_ld", ctypes.c_longlong)]
 
 
 # every entry point of include/magic_sht.h with its argument types
@@ -115,6 +168,10 @@ SIGNATURES = {
     "magic_sht_get_td": [_V, ctypes.c_int, _V, _V, ctypes.c_double, _V, ctypes.POINTER(TdArgs)],
     "magic_sht_get_td_nbc": [_V, ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, ctypes.POINTER(TdArgs)],
     "magic_sht_get_nl": [_V, ctypes.c_int, _V, ctypes.POINTER(GridSpaceArgs), ctypes.POINTER(LmSpaceArgs)],
+    "magic_sht_get_td_opts": [_V, ctypes.c_int, ctypes.POINTER(TdOpts), ctypes.POINTER(TdIn),
+                              ctypes.POINTER(TdOut)],
+    "magic_sht_get_nl_opts": [_V, ctypes.c_int, ctypes.POINTER(NlOpts), ctypes.POINTER(NlGrids),
+                              ctypes.POINTER(NlOut)],
     "magic_sht_courant": [_V, ctypes.c_int, ctypes.POINTER(CourantArgs), _V, _V],
     "magic_sht_dt_courant": [ctypes.c_int, _V, _V, ctypes.c_double, ctypes.c_double, _I, _D],
     "magic_sht_v_rigid_boundary": [_V, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(RigidArgs)],

@@ -158,6 +158,26 @@ struct NlGrids {
   long long ld;
 };
 
+// the general get_nl (nl.cu): the reference's switches and radial functions
+// (device arrays of the levels; null: the Boussinesq default, r required)
+struct NlOpts {
+  int conv, curl, lf, heat, chem, mag, anel, pad_;
+  double LFfac, ViscHeatFac, OhmLossFac;
+  const double *r, *orho1, *beta, *otemp1, *visc, *lambda;
+  const int *nbc, *lcr;
+};
+enum NlfIn : int { NLF_VR, NLF_VT, NLF_VP, NLF_CVR, NLF_CVT, NLF_CVP, NLF_DVRDR, NLF_DVTDR, NLF_DVPDR,
+                   NLF_DVRDT, NLF_DVRDP, NLF_DVTDP, NLF_DVPDP, NLF_BR, NLF_BT, NLF_BP, NLF_CBR, NLF_CBT,
+                   NLF_CBP, NLF_S, NLF_XI, NLF_NIN };
+enum NlfOut : int { NLF_ADVR, NLF_ADVT, NLF_ADVP, NLF_VSR, NLF_VST, NLF_VSP, NLF_VXIR, NLF_VXIT, NLF_VXIP,
+                    NLF_VXBR, NLF_VXBT, NLF_VXBP, NLF_HEAT, NLF_NOUT };
+struct NlFull {
+  NlOpts o;
+  const double* in[NLF_NIN];  // null: not needed by the switches
+  double* out[NLF_NOUT];
+  long long ld_in, ld_out;    // doubles between levels
+};
+
 // spectral assembly of the time derivatives (td.cu); arrays [level][ld] complex
 struct TdArgs {
   const double2 *w, *dw, *z;                                   // radial-loop spectra
@@ -171,6 +191,23 @@ struct TdArgs {
   double cor_fac;       // CorFac (1/E)
   const double2* coef;  // [lm][4] level-independent coefficients (build_td_coef)
   const int* lq;        // [lm] l | m << 16
+};
+
+// the general get_td (td.cu): the reference's switches; null outputs are skipped
+struct TdOpts {
+  int conv, corr, dcurl, single_matrix, anel, liquid, mag_nl, pad_;
+  double cor_fac, epscXi;
+  const double *r, *orho1, *beta, *temp0, *epsc;  // [level]; r required
+  const int *lcut, *nbc;                          // [level] or null
+};
+struct TdFull {
+  TdOpts o;
+  const double2 *w, *dw, *ddw, *z, *dz;
+  const double2 *Advr, *Advt, *Advp, *VSt, *heat, *VXit, *VxBr, *VxBt, *VxBp;
+  double2 *dwdt, *dzdt, *dpdt, *dsdt, *dxidt, *dbdt, *djdt, *dVxBh, *dVxVh, *dVSr, *dVXir;
+  long long ld;
+  const double2* coef;
+  const int* lq;
 };
 
 // Courant condition (courant.cu); grids [level][ld], radial functions [level]

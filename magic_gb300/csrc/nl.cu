@@ -95,3 +95,157 @@ cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& ou
   }
   return cudaSuccess;
 }
+
+// ------------------------------------------------- the general get_nl
+// get_nl.f90:213-441 with the reference's switches and radial functions and
+// the Lorentz-force combination of transform_to_lm_space
+// (rIter.f90:645-662).  Per level: the Lorentz force where l_mag_LF, nBc = 0
+// and outside the low-conductivity region; the advection in the curl form
+// (:260-272) or as u.grad u (:274-302) where l_conv_nl and nBc = 0; V S, V Xi
+// where nBc = 0; V x B in its bulk, stress-free (nBc = 1 or inside the
+// region) or rigid (nBc = 2) form; heatTerms (viscous heating and ohmic
+// losses, :398-432) where l_anel and nBc = 0.  Outputs a level does not
+// produce are left untouched, as the reference leaves them.
+namespace {
+
+template <typename T>
+__global__ void __launch_bounds__(256) get_nl_full_kernel(const ShtGeom g, const NlFull a, const double* __restrict__ cosn2,
+                                                          int r0) {
+  const int r = r0 + blockIdx.y;
+  const unsigned nh = (unsigned)(g.n_theta / 2), per_level = (unsigned)g.n_phi * nh;
+  const NlOpts& o = a.o;
+  const int nbc = o.nbc ? o.nbc[r] : 0;
+  const bool bulk = nbc == 0, lcr = o.lcr && o.lcr[r] != 0;
+  const double rd = o.r[r], o1d = 1.0 / rd, o2d = o1d * o1d;
+  const T rr = from_f64<T>(rd), o1 = from_f64<T>(o1d), o2 = from_f64<T>(o2d), o4 = from_f64<T>(o2d * o2d);
+  const T oh = from_f64<T>(o.orho1 ? o.orho1[r] : 1.0), bt = from_f64<T>(o.beta ? o.beta[r] : 0.0);
+  const T ot = from_f64<T>(o.otemp1 ? o.otemp1[r] : 1.0), vi = from_f64<T>(o.visc ? o.visc[r] : 1.0);
+  const T la = from_f64<T>(o.lambda ? o.lambda[r] : 1.0);
+  const T LFfac = from_f64<T>(o.LFfac), VHF = from_f64<T>(o.ViscHeatFac), OLF = from_f64<T>(o.OhmLossFac);
+  const bool do_lf = o.lf && bulk && !lcr;
+  const bool do_adv = bulk && (o.conv || o.lf);
+  const bool do_vs = o.heat && bulk, do_vxi = o.chem && bulk, do_heat = o.anel && bulk;
+  const int vxb = !o.mag ? 0 : (bulk && !lcr) ? 1 : (nbc == 1 || lcr) ? 2 : (nbc == 2) ? 3 : 0;
+  const T two = (T)2, third = (T)(1.0 / 3.0);
+  const long long b_in = (long long)r * a.ld_in, b_out = (long long)r * a.ld_out;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < per_level; i += gridDim.x * blockDim.x) {
+    const unsigned ph = i / nh, j = i - ph * nh;
+    const long long oi = b_in + (long long)ph * g.ld + 2 * j;
+    const long long oo = b_out + (long long)ph * g.ld + 2 * j;
+    const T sn2 = from_f64<T>(g.osin2[j]);
+    const T cn2n = from_f64<T>(cosn2[j]);  // cos/sin^2 of the northern row; the southern row has -cos
+    auto ld = [&](int k) { return __ldg(reinterpret_cast<const double2*>(a.in[k] + oi)); };
+    double2 x[NLF_NIN];
+#pragma unroll
+    for (int k = 0; k < NLF_NIN; ++k) x[k] = a.in[k] ? ld(k) : make_double2(0.0, 0.0);
+    T res[NLF_NOUT][2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      auto v = [&](int k) { return from_f64<T>(h ? x[k].y : x[k].x); };
+      const T cn2 = h ? -cn2n : cn2n;
+      const T vr = v(NLF_VR), vt = v(NLF_VT), vp = v(NLF_VP);
+      const T br = v(NLF_BR), btt = v(NLF_BT), bp = v(NLF_BP);
+      const T jr = v(NLF_CBR), jt = v(NLF_CBT), jp = v(NLF_CBP);
+      T ar = 0, at = 0, ap = 0;
+      if (o.conv) {
+        if (o.curl) {
+          const T wr = v(NLF_CVR), wt = v(NLF_CVT), wp = v(NLF_CVP);
+          ar = -sn2 * (wt * vp - wp * vt);
+          at = -o4 * (wp * vr - wr * vp);
+          ap = -o4 * (wr * vt - wt * vr);
+        } else {
+          const T drr = v(NLF_DVRDR), dtr = v(NLF_DVTDR), dpr = v(NLF_DVPDR);
+          const T drt = v(NLF_DVRDT), drp = v(NLF_DVRDP), dtp = v(NLF_DVTDP), dpp = v(NLF_DVPDP);
+          const T wr = v(NLF_CVR);
+          ar = -o2 * oh * (vr * (drr - (two * o1 + bt) * vr) + sn2 * (vt * (drt - rr * vt) + vp * (drp - rr * vp)));
+          at = o4 * oh * (-vr * (dtr - bt * vt) + vt * (cn2 * vt + dpp + drr) + vp * (cn2 * vp - dtp));
+          ap = o4 * oh * (-vr * (dpr - bt * vp) - vt * (dtp + wr) - vp * dpp);
+        }
+      }
+      if (do_lf) {
+        ar += LFfac * sn2 * (jt * bp - jp * btt);
+        at += LFfac * o4 * (jp * br - jr * bp);
+        ap += LFfac * o4 * (jr * btt - jt * br);
+      }
+      res[NLF_ADVR][h] = ar;
+      res[NLF_ADVT][h] = at;
+      res[NLF_ADVP][h] = ap;
+      const T s = v(NLF_S), xi = v(NLF_XI);
+      res[NLF_VSR][h] = vr * s;
+      res[NLF_VST][h] = o2 * vt * s;
+      res[NLF_VSP][h] = o2 * vp * s;
+      res[NLF_VXIR][h] = vr * xi;
+      res[NLF_VXIT][h] = o2 * vt * xi;
+      res[NLF_VXIP][h] = o2 * vp * xi;
+      if (vxb == 1) {
+        res[NLF_VXBR][h] = oh * sn2 * (vt * bp - vp * btt);
+        res[NLF_VXBT][h] = oh * o4 * (vp * br - vr * bp);
+        res[NLF_VXBP][h] = oh * o4 * (vr * btt - vt * br);
+      } else {
+        res[NLF_VXBR][h] = 0;
+        res[NLF_VXBT][h] = o4 * oh * vp * br;
+        res[NLF_VXBP][h] = vxb == 2 ? -o4 * oh * vt * br : (T)0;
+      }
+      T heat = 0;
+      if (do_heat) {
+        const T drr = v(NLF_DVRDR), dtr = v(NLF_DVTDR), dpr = v(NLF_DVPDR);
+        const T drt = v(NLF_DVRDT), drp = v(NLF_DVRDP), dtp = v(NLF_DVTDP), dpp = v(NLF_DVPDP);
+        const T wr = v(NLF_CVR);
+        const T e1 = drr - (two * o1 + bt) * vr;
+        const T e2 = cn2 * vt + dpp + drr - o1 * vr;
+        const T e3 = dpp + cn2 * vt + o1 * vr;
+        const T e6 = two * dtp + wr - two * cn2 * vp;
+        const T e4 = rr * dtr - (two + bt * rr) * vt + o1 * drt;
+        const T e5 = rr * dpr - (two + bt * rr) * vp + o1 * drp;
+        heat = VHF * o4 * oh * ot * vi *
+               (two * e1 * e1 + two * e2 * e2 + two * e3 * e3 + e6 * e6 + sn2 * (e4 * e4 + e5 * e5) -
+                two * third * (bt * vr) * (bt * vr));
+        if (o.mag && !lcr) heat += OLF * o2 * ot * la * (o2 * jr * jr + sn2 * jt * jt + sn2 * jp * jp);
+      }
+      res[NLF_HEAT][h] = heat;
+    }
+    auto st = [&](int k) {
+      *reinterpret_cast<double2*>(a.out[k] + oo) = make_double2(to_f64<T>(res[k][0]), to_f64<T>(res[k][1]));
+    };
+    if (do_adv && a.out[NLF_ADVR]) { st(NLF_ADVR); st(NLF_ADVT); st(NLF_ADVP); }
+    if (do_vs && a.out[NLF_VSR]) { st(NLF_VSR); st(NLF_VST); st(NLF_VSP); }
+    if (do_vxi && a.out[NLF_VXIR]) { st(NLF_VXIR); st(NLF_VXIT); st(NLF_VXIP); }
+    if (vxb == 1 && a.out[NLF_VXBR]) st(NLF_VXBR);
+    if (vxb && a.out[NLF_VXBT]) { st(NLF_VXBT); st(NLF_VXBP); }
+    if (do_heat && a.out[NLF_HEAT]) st(NLF_HEAT);
+  }
+}
+
+__global__ void cosn2_kernel(int nh, const double* __restrict__ theta, double* __restrict__ cosn2) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nh) {
+    const double s = sin(theta[j]);
+    cosn2[j] = cos(theta[j]) / s / s;  // horizontal.f90:156
+  }
+}
+
+}  // namespace
+
+cudaError_t build_cosn2(const ShtGeom& g, const double* theta, double* cosn2, cudaStream_t st) {
+  const int nh = g.n_theta / 2;
+  cosn2_kernel<<<(nh + 127) / 128, 128, 0, st>>>(nh, theta, cosn2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_get_nl_full(const ShtGeom& g, const NlFull& a, const double* cosn2, int nlev, bool f32,
+                               cudaStream_t st) {
+  const long long per_level = (long long)g.n_phi * (g.n_theta / 2);
+  if (nlev <= 0 || per_level <= 0) return cudaSuccess;
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int need = (int)((per_level + 255) / 256);
+  for (int r0 = 0; r0 < nlev; r0 += 65535) {
+    const int nl = std::min(nlev - r0, 65535);
+    const int gx = std::max(1, std::min(need, (8 * nsm + nl - 1) / nl));
+    if (f32) get_nl_full_kernel<float><<<dim3(gx, nl), 256, 0, st>>>(g, a, cosn2, r0);
+    else get_nl_full_kernel<double><<<dim3(gx, nl), 256, 0, st>>>(g, a, cosn2, r0);
+    CUDA_TRY(cudaGetLastError());
+  }
+  return cudaSuccess;
+}

@@ -67,6 +67,7 @@ struct magic_sht_handle {
   float4* d_twdf = nullptr;  // e^{+2 pi i k/P} as double-float (hi re, lo re, hi im, lo im)
   short* d_inv_exp = nullptr;  // FP64-accurate tensor-core form: table row exponents
   short* d_fwd_exp = nullptr;
+  double* d_cosn2 = nullptr;  // cos / sin^2 of the northern colatitudes (general get_nl)
   // tensor-core form: pre-split table images
   TcTables tct{};
   unsigned char* d_inv_img = nullptr;
@@ -837,6 +838,8 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     INIT_CK(convert_tables_fp32(h->d_P, h->d_dP, h->d_P32, h->d_dP32, tab, h->stream));
   g.lmoff = h->d_lmoff;
   INIT_CK(build_td_coef(g, h->d_tdcoef, h->d_tdlq, h->stream));
+  INIT_CK(cudaMalloc((void**)&h->d_cosn2, sizeof(double) * g.nh));
+  INIT_CK(build_cosn2(g, h->d_theta, h->d_cosn2, h->stream));
   INIT_CK(cudaStreamSynchronize(h->stream));
   g.P64 = h->d_P; g.dP64 = h->d_dP; g.P32 = h->d_P32; g.dP32 = h->d_dP32;
   g.wgt = h->d_wgt; g.osin2 = h->d_osin2; g.tw64 = h->d_tw64; g.tw32 = h->d_tw32; g.twdf = h->d_twdf;
@@ -935,7 +938,7 @@ int magic_sht_finalize(magic_sht_handle* h) {
                   h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws, h->d_inv_img, h->d_fwd_img,
                   h->d_inv_blk0, h->d_fwd_blk0, h->d_inv_scale, h->d_fwd_scale, h->d_err,
                   h->d_bpc0, h->d_bimg, h->d_tile_ctr, h->d_tdcoef, h->d_tdlq, h->d_twdf,
-                  h->d_inv_exp, h->d_fwd_exp};
+                  h->d_inv_exp, h->d_fwd_exp, h->d_cosn2};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->pin) cudaFreeHost(h->pin);
@@ -1529,6 +1532,148 @@ int magic_sht_get_nl(magic_sht_handle* h, int n, const double* or2, const magic_
   return cx.finish();
 }
 
+int magic_sht_get_nl_opts(magic_sht_handle* h, int n, const magic_sht_nl_opts* o, const magic_sht_nl_grids* gin,
+                          const magic_sht_nl_out* gout) {
+  TRY(check_handle(h));
+  if (!o || !gin || !gout || n < 0) return set_err(MAGIC_SHT_ERR_ARG, "null args or n_levels < 0");
+  if (n == 0) return MAGIC_SHT_OK;
+  if (!o->r) return set_err(MAGIC_SHT_ERR_ARG, "get_nl_opts needs the radius of every level (opts->r)");
+  const ShtGeom& g = h->g;
+  if (gin->grid_ld < (long long)g.n_phi * g.ld || gout->grid_ld < (long long)g.n_phi * g.ld)
+    return set_err(MAGIC_SHT_ERR_ARG, "grid_ld smaller than one level");
+  if ((gin->grid_ld | gout->grid_ld | (long long)g.ld) & 1)
+    return set_err(MAGIC_SHT_ERR_ARG, "get_nl needs even grid_ld and nlat_padded (16-byte pairs of rows)");
+  DeviceGuard dg(h->device);
+  NlFull a{};
+  const double* const ins[NLF_NIN] = {gin->vrc,   gin->vtc,    gin->vpc,    gin->cvrc,   gin->cvtc,   gin->cvpc,
+                                      gin->dvrdrc, gin->dvtdrc, gin->dvpdrc, gin->dvrdtc, gin->dvrdpc, gin->dvtdpc,
+                                      gin->dvpdpc, gin->brc,    gin->btc,    gin->bpc,    gin->cbrc,   gin->cbtc,
+                                      gin->cbpc,   gin->sc,     gin->xic};
+  double* const outs[NLF_NOUT] = {gout->Advr, gout->Advt, gout->Advp, gout->VSr,  gout->VSt,
+                                  gout->VSp,  gout->VXir, gout->VXit, gout->VXip, gout->VxBr,
+                                  gout->VxBt, gout->VxBp, gout->heatTerms};
+  // inputs each enabled term reads (get_nl.f90:241-432)
+  bool need[NLF_NIN] = {};
+  const bool conv = o->l_conv_nl, anel = o->l_anel, mag = o->l_mag_nl, lf = o->l_mag_LF;
+  if (conv || o->l_heat_nl || o->l_chemical_conv || mag || anel) need[NLF_VR] = need[NLF_VT] = need[NLF_VP] = true;
+  if (conv && o->l_adv_curl) need[NLF_CVR] = need[NLF_CVT] = need[NLF_CVP] = true;
+  if ((conv && !o->l_adv_curl) || anel) {
+    for (int k : {NLF_DVRDR, NLF_DVTDR, NLF_DVPDR, NLF_DVRDT, NLF_DVRDP, NLF_DVTDP, NLF_DVPDP, NLF_CVR}) need[k] = true;
+  }
+  if (lf || mag) need[NLF_BR] = need[NLF_BT] = need[NLF_BP] = true;
+  if (lf || (anel && mag)) need[NLF_CBR] = need[NLF_CBT] = need[NLF_CBP] = true;
+  if (o->l_heat_nl) need[NLF_S] = true;
+  if (o->l_chemical_conv) need[NLF_XI] = true;
+  for (int i = 0; i < NLF_NIN; ++i) {
+    if (!ins[i]) {
+      if (need[i]) return set_err(MAGIC_SHT_ERR_ARG, "get_nl_opts: input grid %d is needed by the switches", i);
+      continue;
+    }
+    if (!is_device_ptr(ins[i]) || ((uintptr_t)ins[i] & 15))
+      return set_err(MAGIC_SHT_ERR_ARG, "get_nl_opts input grid %d: host or not 16-byte aligned", i);
+    if (need[i]) a.in[i] = ins[i];
+  }
+  for (int i = 0; i < NLF_NOUT; ++i) {
+    if (!outs[i]) continue;
+    if (!is_device_ptr(outs[i]) || ((uintptr_t)outs[i] & 15))
+      return set_err(MAGIC_SHT_ERR_ARG, "get_nl_opts output grid %d: host or not 16-byte aligned", i);
+    a.out[i] = outs[i];
+  }
+  a.ld_in = gin->grid_ld;
+  a.ld_out = gout->grid_ld;
+  a.o.conv = conv; a.o.curl = o->l_adv_curl; a.o.lf = lf; a.o.heat = o->l_heat_nl;
+  a.o.chem = o->l_chemical_conv; a.o.mag = mag; a.o.anel = anel;
+  a.o.LFfac = o->LFfac; a.o.ViscHeatFac = o->ViscHeatFac; a.o.OhmLossFac = o->OhmLossFac;
+  CallCtx cx(h);
+  const size_t nb = (size_t)n * 8, ni = (size_t)n * 4;
+  const int i_r = cx.raw_in(o->r, nb);
+  const int i_rho = o->orho1 ? cx.raw_in(o->orho1, nb) : -1, i_beta = o->beta ? cx.raw_in(o->beta, nb) : -1;
+  const int i_ot = o->otemp1 ? cx.raw_in(o->otemp1, nb) : -1, i_vi = o->visc ? cx.raw_in(o->visc, nb) : -1;
+  const int i_la = o->lambda ? cx.raw_in(o->lambda, nb) : -1;
+  const int i_nbc = o->nbc ? cx.raw_in(o->nbc, ni) : -1, i_lcr = o->lcr ? cx.raw_in(o->lcr, ni) : -1;
+  TRY(cx.prepare());
+  a.o.r = (const double*)cx.dev(i_r);
+  a.o.orho1 = (const double*)cx.dev(i_rho);
+  a.o.beta = (const double*)cx.dev(i_beta);
+  a.o.otemp1 = (const double*)cx.dev(i_ot);
+  a.o.visc = (const double*)cx.dev(i_vi);
+  a.o.lambda = (const double*)cx.dev(i_la);
+  a.o.nbc = (const int*)cx.dev(i_nbc);
+  a.o.lcr = (const int*)cx.dev(i_lcr);
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_NL);
+    CK(launch_get_nl_full(g, a, h->d_cosn2, n, !f64_sums(h), h->stream));
+  }
+  return cx.finish();
+}
+
+int magic_sht_get_td_opts(magic_sht_handle* h, int n, const magic_sht_td_opts* o, const magic_sht_td_in* in,
+                          const magic_sht_td_out* out) {
+  TRY(check_handle(h));
+  if (!o || !in || !out || n < 0) return set_err(MAGIC_SHT_ERR_ARG, "null args or n_levels < 0");
+  if (n == 0) return MAGIC_SHT_OK;
+  if (!o->r) return set_err(MAGIC_SHT_ERR_ARG, "get_td_opts needs the radius of every level (opts->r)");
+  const ShtGeom& g = h->g;
+  if (in->spec_ld < g.lm_max || out->spec_ld < g.lm_max || in->spec_ld != out->spec_ld)
+    return set_err(MAGIC_SHT_ERR_ARG, "spec_ld must be >= lm_max and equal for inputs and outputs");
+  DeviceGuard dg(h->device);
+  TdFull t{};
+  t.o.conv = o->l_conv_nl; t.o.corr = o->l_corr; t.o.dcurl = o->l_double_curl;
+  t.o.single_matrix = o->l_single_matrix; t.o.anel = o->l_anel; t.o.liquid = o->l_anelastic_liquid;
+  t.o.mag_nl = o->l_mag_nl; t.o.cor_fac = o->cor_fac; t.o.epscXi = o->epscXi;
+  double2** const outs[] = {&t.dwdt, &t.dzdt, &t.dpdt, &t.dsdt, &t.dxidt, &t.dbdt, &t.djdt, &t.dVxBh,
+                            &t.dVxVh, &t.dVSr, &t.dVXir};
+  double* const outp[] = {out->dwdt, out->dzdt, out->dpdt, out->dsdt, out->dxidt, out->dbdt, out->djdt,
+                          out->dVxBhLM, out->dVxVhLM, out->dVSrLM, out->dVXirLM};
+  for (int i = 0; i < 11; ++i) {
+    if (outp[i] && !is_device_ptr(outp[i])) return set_err(MAGIC_SHT_ERR_ARG, "get_td_opts output %d: host pointer", i);
+    *outs[i] = (double2*)outp[i];
+  }
+  // inputs each computed output reads
+  const bool vel = o->l_corr && (out->dwdt || out->dzdt || out->dpdt);
+  struct In { const double* p; const double2** dst; bool need; const char* name; } ins[] = {
+      {in->w, &t.w, vel, "w"}, {in->dw, &t.dw, vel, "dw"}, {in->z, &t.z, vel, "z"},
+      {in->ddw, &t.ddw, vel && o->l_double_curl && out->dwdt, "ddw"},
+      {in->dz, &t.dz, vel && o->l_double_curl && out->dwdt, "dz"},
+      {in->AdvrLM, &t.Advr, o->l_conv_nl && out->dwdt, "AdvrLM"},
+      {in->AdvtLM, &t.Advt, o->l_conv_nl && (out->dpdt || (o->l_double_curl && out->dVxVhLM)), "AdvtLM"},
+      {in->AdvpLM, &t.Advp, o->l_conv_nl && out->dzdt, "AdvpLM"},
+      {in->VStLM, &t.VSt, out->dsdt != nullptr, "VStLM"},
+      {in->heatTermsLM, &t.heat, o->l_anel && out->dsdt, "heatTermsLM"},
+      {in->VXitLM, &t.VXit, out->dxidt != nullptr, "VXitLM"},
+      {in->VxBrLM, &t.VxBr, o->l_mag_nl && out->djdt, "VxBrLM"},
+      {in->VxBtLM, &t.VxBt, o->l_mag_nl && out->dVxBhLM, "VxBtLM"},
+      {in->VxBpLM, &t.VxBp, o->l_mag_nl && out->dbdt, "VxBpLM"}};
+  for (auto& x : ins) {
+    if (!x.need) continue;
+    if (!x.p || !is_device_ptr(x.p))
+      return set_err(MAGIC_SHT_ERR_ARG, "get_td_opts: input %s is needed (a device array)", x.name);
+    *x.dst = (const double2*)x.p;
+  }
+  t.ld = in->spec_ld;
+  t.coef = h->d_tdcoef;
+  t.lq = h->d_tdlq;
+  CallCtx cx(h);
+  const size_t nb = (size_t)n * 8, ni = (size_t)n * 4;
+  const int i_r = cx.raw_in(o->r, nb);
+  const int i_rho = o->orho1 ? cx.raw_in(o->orho1, nb) : -1, i_beta = o->beta ? cx.raw_in(o->beta, nb) : -1;
+  const int i_t0 = o->temp0 ? cx.raw_in(o->temp0, nb) : -1, i_ep = o->epsc ? cx.raw_in(o->epsc, nb) : -1;
+  const int i_lc = o->lcut ? cx.raw_in(o->lcut, ni) : -1, i_nbc = o->nbc ? cx.raw_in(o->nbc, ni) : -1;
+  TRY(cx.prepare());
+  t.o.r = (const double*)cx.dev(i_r);
+  t.o.orho1 = (const double*)cx.dev(i_rho);
+  t.o.beta = (const double*)cx.dev(i_beta);
+  t.o.temp0 = (const double*)cx.dev(i_t0);
+  t.o.epsc = (const double*)cx.dev(i_ep);
+  t.o.lcut = (const int*)cx.dev(i_lc);
+  t.o.nbc = (const int*)cx.dev(i_nbc);
+  {
+    PhaseScope sc(h, MAGIC_SHT_PHASE_TD);
+    CK(launch_get_td_full(g, t, n, !f64_sums(h), h->stream));
+  }
+  return cx.finish();
+}
+
 int magic_sht_get_td(magic_sht_handle* h, int n, const double* r, const int* lcut, double cor_fac,
                      const double* epsc, const magic_sht_td_args* a) {
   return magic_sht_get_td_nbc(h, n, r, lcut, cor_fac, epsc, nullptr, a);
@@ -1764,32 +1909,33 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
   if (n > h->pipe_chunk && !h->capturing &&
       all_host({lcut, a->Advr, a->Advt, a->Advp, a->VSr, a->VSt, a->VSp, a->VxBr, a->VxBt, a->VxBp, a->heatTerms,
                 a->AdvrLM, a->AdvtLM, a->AdvpLM, a->VSrLM, a->VStLM, a->VSpLM, a->VxBrLM, a->VxBtLM,
-                a->VxBpLM, a->heatTermsLM})) {
+                a->VxBpLM, a->heatTermsLM, a->VXir, a->VXit, a->VXip, a->VXirLM, a->VXitLM, a->VXipLM})) {
     if (lcut)
       for (int i = 0; i < n; ++i)
         if (!is_device_ptr(lcut) && (lcut[i] < 0 || lcut[i] > g.l_max))
           return set_err(MAGIC_SHT_ERR_LCUT, "lcut[%d]=%d outside [0, %d]", i, lcut[i], g.l_max);
-    const double* const ins[10] = {a->Advr, a->Advt, a->Advp, a->VSr, a->VSt, a->VSp,
-                                   a->VxBr, a->VxBt, a->VxBp, a->heatTerms};
-    double* const outs[10] = {a->AdvrLM, a->AdvtLM, a->AdvpLM, a->VSrLM, a->VStLM,
-                              a->VSpLM, a->VxBrLM, a->VxBtLM, a->VxBpLM, a->heatTermsLM};
+    constexpr int NF = 13;
+    const double* const ins[NF] = {a->Advr, a->Advt, a->Advp, a->VSr, a->VSt, a->VSp, a->VxBr,
+                                   a->VxBt, a->VxBp, a->heatTerms, a->VXir, a->VXit, a->VXip};
+    double* const outs[NF] = {a->AdvrLM, a->AdvtLM, a->AdvpLM, a->VSrLM, a->VStLM, a->VSpLM, a->VxBrLM,
+                              a->VxBtLM, a->VxBpLM, a->heatTermsLM, a->VXirLM, a->VXitLM, a->VXipLM};
     std::vector<PipeArray> arrs;
-    std::vector<int> idx_in(10, -1), idx_out(10, -1);
+    std::vector<int> idx_in(NF, -1), idx_out(NF, -1);
     const size_t sb = (size_t)a->spec_ld * 16, gb = (size_t)a->grid_ld * 8;
-    for (int i = 0; i < 10; ++i)
+    for (int i = 0; i < NF; ++i)
       if (ins[i]) { idx_in[i] = (int)arrs.size(); arrs.push_back({ins[i], gb, (size_t)g.n_phi * g.ld * 8, false, 0}); }
-    for (int i = 0; i < 10; ++i)
+    for (int i = 0; i < NF; ++i)
       if (outs[i]) { idx_out[i] = (int)arrs.size(); arrs.push_back({outs[i], sb, (size_t)g.lm_max * 16, true, 0}); }
     if (lcut) arrs.push_back({lcut, 4, 4, false, 0});
     const int i_lc = lcut ? (int)arrs.size() - 1 : -1;
     return pipelined_levels(h, n, h->pipe_chunk, arrs, [&](int r0, int nr, const std::vector<char*>& d) {
       magic_sht_lm_space_args b = *a;
-      const double** pin[10] = {&b.Advr, &b.Advt, &b.Advp, &b.VSr, &b.VSt, &b.VSp, &b.VxBr, &b.VxBt,
-                                &b.VxBp, &b.heatTerms};
-      double** pout[10] = {&b.AdvrLM, &b.AdvtLM, &b.AdvpLM, &b.VSrLM, &b.VStLM, &b.VSpLM, &b.VxBrLM,
-                           &b.VxBtLM, &b.VxBpLM, &b.heatTermsLM};
-      for (int i = 0; i < 10; ++i) *pin[i] = idx_in[i] >= 0 ? (const double*)d[idx_in[i]] : nullptr;
-      for (int i = 0; i < 10; ++i) *pout[i] = idx_out[i] >= 0 ? (double*)d[idx_out[i]] : nullptr;
+      const double** pin[NF] = {&b.Advr, &b.Advt, &b.Advp, &b.VSr, &b.VSt, &b.VSp, &b.VxBr, &b.VxBt,
+                                &b.VxBp, &b.heatTerms, &b.VXir, &b.VXit, &b.VXip};
+      double** pout[NF] = {&b.AdvrLM, &b.AdvtLM, &b.AdvpLM, &b.VSrLM, &b.VStLM, &b.VSpLM, &b.VxBrLM,
+                           &b.VxBtLM, &b.VxBpLM, &b.heatTermsLM, &b.VXirLM, &b.VXitLM, &b.VXipLM};
+      for (int i = 0; i < NF; ++i) *pin[i] = idx_in[i] >= 0 ? (const double*)d[idx_in[i]] : nullptr;
+      for (int i = 0; i < NF; ++i) *pout[i] = idx_out[i] >= 0 ? (double*)d[idx_out[i]] : nullptr;
       (void)r0;
       return magic_sht_transform_to_lm_space(h, nr, i_lc >= 0 ? (const int*)d[i_lc] : nullptr, &b);
     });
@@ -1805,9 +1951,10 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
   std::vector<ScalarFwd> sc;
   std::vector<VectorFwd> vc;
   struct Q { const double *f, *g, *h; double *q, *s, *t; };
-  const Q qs[3] = {{a->Advr, a->Advt, a->Advp, a->AdvrLM, a->AdvtLM, a->AdvpLM},
+  const Q qs[4] = {{a->Advr, a->Advt, a->Advp, a->AdvrLM, a->AdvtLM, a->AdvpLM},
                    {a->VSr, a->VSt, a->VSp, a->VSrLM, a->VStLM, a->VSpLM},
-                   {a->VxBr, a->VxBt, a->VxBp, a->VxBrLM, a->VxBtLM, a->VxBpLM}};
+                   {a->VxBr, a->VxBt, a->VxBp, a->VxBrLM, a->VxBtLM, a->VxBpLM},
+                   {a->VXir, a->VXit, a->VXip, a->VXirLM, a->VXitLM, a->VXipLM}};
   for (const Q& q : qs) {
     if (q.f && q.q) sc.push_back({gi(q.f), so(q.q)});
     if (q.g && q.h && q.s && q.t) vc.push_back({gi(q.g), gi(q.h), so(q.s), so(q.t)});

@@ -37,6 +37,8 @@ module sht_gpu_batched
       integer(c_long_long) :: grid_ld
       type(c_ptr) :: AdvrLM, AdvtLM, AdvpLM, VSrLM, VStLM, VSpLM, VxBrLM, VxBtLM, VxBpLM, heatTermsLM
       integer(c_long_long) :: spec_ld
+      type(c_ptr) :: VXir, VXit, VXip
+      type(c_ptr) :: VXirLM, VXitLM, VXipLM
    end type magic_sht_lm_space_args
 
    type, bind(C) :: magic_sht_td_args
@@ -170,6 +172,8 @@ contains
       a%VxBrLM = c_loc(VxBrLM); a%VxBtLM = c_loc(VxBtLM); a%VxBpLM = c_loc(VxBpLM)
       a%heatTermsLM = c_loc(heatTermsLM)
       a%spec_ld = size(AdvrLM, 1, kind=c_long_long)
+      a%VXir = c_null_ptr; a%VXit = c_null_ptr; a%VXip = c_null_ptr
+      a%VXirLM = c_null_ptr; a%VXitLM = c_null_ptr; a%VXipLM = c_null_ptr
       call sht_check(c_to_lm(sht_handle(), int(size(Advr, 3), c_int), c_loc(lcut), a))
    end subroutine transform_to_lm_space_gpu
 
@@ -205,6 +209,8 @@ contains
       nl%VSrLM = c_null_ptr; nl%VStLM = c_null_ptr; nl%VSpLM = c_null_ptr
       nl%VxBrLM = c_null_ptr; nl%VxBtLM = c_null_ptr; nl%VxBpLM = c_null_ptr; nl%heatTermsLM = c_null_ptr
       nl%spec_ld = 0
+      nl%VXir = c_null_ptr; nl%VXit = c_null_ptr; nl%VXip = c_null_ptr
+      nl%VXirLM = c_null_ptr; nl%VXitLM = c_null_ptr; nl%VXipLM = c_null_ptr
       call sht_check(c_get_nl(sht_handle(), int(size(vrc, 3), c_int), c_loc(or2), g, nl))
    end subroutine get_nl_gpu
 

@@ -336,8 +336,11 @@ class SHT:
         return outs
 
     def transform_to_lm_space(self, grids: dict, lcut=None, out: Optional[dict] = None):
-        """rIter.f90:624-712 for many radial levels."""
-        keys = [k for k in _lib.LM_SPACE_IN if grids.get(k) is not None]
+        """rIter.f90:624-712 for many radial levels (also V Xi -> VXirLM,
+        VXitLM, VXipLM when ``VXir`` .. ``VXip`` are given)."""
+        names_in = _lib.LM_SPACE_IN + _lib.LM_SPACE_IN_XI
+        names_out = _lib.LM_SPACE_OUT + _lib.LM_SPACE_OUT_XI
+        keys = [k for k in names_in if grids.get(k) is not None]
         first = grids[keys[0]]
         n = int(first.shape[0])
         a = _lib.LmSpaceArgs()
@@ -348,7 +351,7 @@ class SHT:
             setattr(a, k, p)
         a.grid_ld = self.n_phi_max * self.nlat_padded
         outs = {} if out is None else dict(out)
-        for kin, kout in zip(_lib.LM_SPACE_IN, _lib.LM_SPACE_OUT):
+        for kin, kout in zip(names_in, names_out):
             if grids.get(kin) is None:
                 continue
             if kout not in outs:
@@ -416,6 +419,112 @@ class SHT:
         or2_arr, por2 = _per_level(or2, np.float64, n, "or2")
         self._bind_torch_stream()
         check(self._lib.magic_sht_get_nl(self._h, n, por2, ctypes.byref(g), ctypes.byref(nl)))
+        return outs
+
+    def get_nl_opts(self, grids: dict, r, out: Optional[dict] = None, LFfac: float = 1.0,
+                    ViscHeatFac: float = 1.0, OhmLossFac: float = 1.0, orho1=None, beta=None, otemp1=None,
+                    visc=None, lam=None, nbc=None, lcr=None, l_conv_nl=True, l_adv_curl=True, l_mag_LF=True,
+                    l_heat_nl=True, l_chemical_conv=False, l_mag_nl=True, l_anel=False):
+        """The grid-space nonlinear products with the reference's switches and
+        radial functions (get_nl.f90:213-441, rIter.f90:645-662;
+        magic_sht_get_nl_opts).  ``grids``: CUDA tensors [level][phi][theta]
+        named as in the reference (``vrc`` .. ``cvpc``, ``dvrdrc`` ..
+        ``dvpdpc``, ``brc`` .. ``cbpc``, ``sc``, ``xic``; the ones the switches
+        need).  ``r`` and the profiles: per level, numpy or CUDA.  Returns the
+        outputs ``Advr`` .. ``heatTerms`` (new zero-filled tensors unless given
+        in ``out``; entries a level does not produce keep their values)."""
+        import torch
+        first = next(v for v in grids.values() if v is not None)
+        if not (_is_torch(first) and first.is_cuda):
+            raise ValueError("get_nl_opts takes CUDA tensors")
+        n = int(first.shape[0])
+        g = _lib.NlGrids()
+        keep = []
+        for k in _lib.NLF_IN:
+            t = grids.get(k)
+            if t is not None:
+                t = t.contiguous()
+                keep.append(t)
+                setattr(g, k, t.data_ptr())
+        g.grid_ld = self.n_phi_max * self.nlat_padded
+        outs = {} if out is None else dict(out)
+        o = _lib.NlOut()
+        for k in _lib.NLF_OUT:
+            if k not in outs:
+                outs[k] = torch.zeros_like(first)
+            setattr(o, k, outs[k].data_ptr())
+        o.grid_ld = self.n_phi_max * self.nlat_padded
+        opt = _lib.NlOpts()
+        for k, v in (("l_conv_nl", l_conv_nl), ("l_adv_curl", l_adv_curl), ("l_mag_LF", l_mag_LF),
+                     ("l_heat_nl", l_heat_nl), ("l_chemical_conv", l_chemical_conv), ("l_mag_nl", l_mag_nl),
+                     ("l_anel", l_anel)):
+            setattr(opt, k, 1 if v else 0)
+        opt.LFfac, opt.ViscHeatFac, opt.OhmLossFac = LFfac, ViscHeatFac, OhmLossFac
+        held = []
+        for k, v in (("r", r), ("orho1", orho1), ("beta", beta), ("otemp1", otemp1), ("visc", visc),
+                     ("lambda", lam)):
+            arr, ptr = _per_level(v, np.float64, n, k)
+            held.append(arr)
+            setattr(opt, k, ptr)
+        for k, v in (("nbc", nbc), ("lcr", lcr)):
+            arr, ptr = _per_level(v, np.int32, n, k)
+            held.append(arr)
+            setattr(opt, k, ptr)
+        self._bind_torch_stream()
+        check(self._lib.magic_sht_get_nl_opts(self._h, n, ctypes.byref(opt), ctypes.byref(g), ctypes.byref(o)))
+        return outs
+
+    def get_td_opts(self, spec: dict, r, cor_fac: float, outputs=None, out: Optional[dict] = None,
+                    lcut=None, nbc=None, orho1=None, beta=None, temp0=None, epsc=None, epscXi: float = 0.0,
+                    l_conv_nl=True, l_corr=True, l_double_curl=False, l_single_matrix=False, l_anel=False,
+                    l_anelastic_liquid=False, l_mag_nl=True):
+        """The spectral assembly with the reference's switches
+        (magic_sht_get_td_opts, get_td.f90 as rIter.f90:410-428 calls it).
+        ``spec``: CUDA tensors [level][lm] named as in the reference (``w``,
+        ``dw``, ``ddw``, ``z``, ``dz``, ``AdvrLM`` .. ``VxBpLM``, ``VXitLM``,
+        ``heatTermsLM``; the ones the outputs need).  ``outputs``: the names
+        to compute (default: all of dwdt, dzdt, dpdt, dsdt, dxidt, dbdt, djdt,
+        dVxBhLM, dVxVhLM, dVSrLM, dVXirLM); tensors not given in ``out`` are
+        new and zero-filled, and entries not produced keep their values."""
+        import torch
+        first = next(v for v in spec.values() if v is not None)
+        if not (_is_torch(first) and first.is_cuda):
+            raise ValueError("get_td_opts takes CUDA tensors")
+        n = int(first.shape[0])
+        names = list(_lib.TDF_OUT) if outputs is None else list(outputs)
+        a = _lib.TdIn()
+        keep = []
+        for k in _lib.TDF_IN:
+            t = spec.get(k)
+            if t is not None:
+                t = t.contiguous()
+                keep.append(t)
+                setattr(a, k, t.data_ptr())
+        a.spec_ld = self.lm_max
+        outs = {} if out is None else dict(out)
+        b = _lib.TdOut()
+        for k in names:
+            if k not in outs:
+                outs[k] = torch.zeros((n, self.lm_max), dtype=torch.complex128, device=first.device)
+            setattr(b, k, outs[k].data_ptr())
+        b.spec_ld = self.lm_max
+        o = _lib.TdOpts()
+        for k, v in (("l_conv_nl", l_conv_nl), ("l_corr", l_corr), ("l_double_curl", l_double_curl),
+                     ("l_single_matrix", l_single_matrix), ("l_anel", l_anel),
+                     ("l_anelastic_liquid", l_anelastic_liquid), ("l_mag_nl", l_mag_nl)):
+            setattr(o, k, 1 if v else 0)
+        o.cor_fac, o.epscXi = cor_fac, epscXi
+        held = []
+        for k, v in (("r", r), ("orho1", orho1), ("beta", beta), ("temp0", temp0), ("epsc", epsc)):
+            arr, ptr = _per_level(v, np.float64, n, k)
+            held.append(arr)
+            setattr(o, k, ptr)
+        for k, v in (("lcut", lcut), ("nbc", nbc)):
+            arr, ptr = _per_level(v, np.int32, n, k)
+            held.append(arr)
+            setattr(o, k, ptr)
+        self._bind_torch_stream()
+        check(self._lib.magic_sht_get_td_opts(self._h, n, ctypes.byref(o), ctypes.byref(a), ctypes.byref(b)))
         return outs
 
     def get_td(self, spec: dict, r, cor_fac: float, lcut=None, epsc=None, out: Optional[dict] = None,

@@ -542,3 +542,275 @@ def get_td(spec: dict, r, cor_fac: float, l_max: int, minc: int = 1, lcut=None, 
         out["dVxBhLM"][ir] = -dLh * np.asarray(spec["VxBtLM"])[ir] * rr * rr
         out["djdt"][ir] = dLh * or4 * np.asarray(spec["VxBrLM"])[ir]
     return out
+
+
+def _row_factors(n_theta: int):
+    """O_sin_theta_E2 and cosn_theta_E2 on the scrambled rows (2j: colatitude
+    theta_j, 2j+1: pi - theta_j), horizontal.f90:145-157."""
+    theta, _ = gauleg(n_theta)
+    colat = theta[: n_theta // 2]
+    sn2 = np.repeat(1.0 / (np.sin(colat) * np.sin(colat)), 2)
+    c = np.cos(colat) / np.sin(colat) / np.sin(colat)
+    cn2 = np.empty(n_theta)
+    cn2[0::2] = c
+    cn2[1::2] = -c
+    return sn2, cn2
+
+
+def get_nl_full(grids: dict, n_theta: int, r, l_conv_nl=True, l_adv_curl=True, l_mag_LF=True,
+                l_heat_nl=True, l_chemical_conv=False, l_mag_nl=True, l_anel=False, LFfac=1.0,
+                ViscHeatFac=1.0, OhmLossFac=1.0, orho1=None, beta=None, otemp1=None, visc=None,
+                lam=None, nbc=None, lcr=None) -> dict:
+    """Grid-space nonlinear products with the reference's switches and radial
+    functions (get_nl.f90:213-441) and the Lorentz-force combination of
+    transform_to_lm_space (rIter.f90:645-662), per level:
+      Lorentz force LF (:243-256) where l_mag_LF, nBc = 0 and the level is
+      outside the low-conductivity region (lcr = 0, nR > n_r_LCR);
+      advection, curl form (:260-272) or u.grad u (:274-302), where l_conv_nl
+      and nBc = 0; Adv += LF (rIter.f90:648-652) or Adv = LF / 0 without
+      l_conv_nl (:653-661);
+      V S (:316-320), V Xi (:323-327) where nBc = 0;
+      V x B (:376-395): the full product where nBc = 0 outside the region,
+      the stress-free form where nBc = 1 or inside it, the rigid form where
+      nBc = 2;
+      heatTerms (:398-432): viscous heating plus ohmic losses (outside the
+      region, with l_mag_nl) where l_anel and nBc = 0.
+    Entries a level does not write are NaN (the reference leaves them as they
+    were).  Grids [level][phi][theta] in the scrambled row order; numpy FP64."""
+    sn2, cn2 = _row_factors(n_theta)
+    nl = len(np.asarray(r))
+    one = np.ones(nl)
+    rr = np.asarray(r, dtype=np.float64)
+    prof = {k: (one if v is None else np.asarray(v, dtype=np.float64))
+            for k, v in (("orho1", orho1), ("otemp1", otemp1), ("visc", visc), ("lam", lam))}
+    bet = np.zeros(nl) if beta is None else np.asarray(beta, dtype=np.float64)
+    nb = np.zeros(nl, dtype=int) if nbc is None else np.asarray(nbc)
+    lc = np.zeros(nl, dtype=int) if lcr is None else np.asarray(lcr)
+    g = {k: np.asarray(v, dtype=np.float64)[..., :n_theta] for k, v in grids.items() if v is not None}
+    shape = next(iter(g.values())).shape
+    names = ("Advr", "Advt", "Advp", "VSr", "VSt", "VSp", "VXir", "VXit", "VXip", "VxBr", "VxBt", "VxBp",
+             "heatTerms")
+    out = {k: np.full(shape, np.nan) for k in names}
+    two, third = 2.0, 1.0 / 3.0
+    for i in range(nl):
+        o1 = 1.0 / rr[i]
+        o2 = o1 * o1
+        o4 = o2 * o2
+        oh, bt_, ot, vi, la = prof["orho1"][i], bet[i], prof["otemp1"][i], prof["visc"][i], prof["lam"][i]
+        bulk = nb[i] == 0
+        x = {k: v[i] for k, v in g.items()}
+        LF = None
+        if l_mag_LF and bulk and lc[i] == 0:
+            LF = (LFfac * sn2 * (x["cbtc"] * x["bpc"] - x["cbpc"] * x["btc"]),
+                  LFfac * o4 * (x["cbpc"] * x["brc"] - x["cbrc"] * x["bpc"]),
+                  LFfac * o4 * (x["cbrc"] * x["btc"] - x["cbtc"] * x["brc"]))
+        adv = None
+        if l_conv_nl and bulk:
+            vr, vt, vp = x["vrc"], x["vtc"], x["vpc"]
+            if l_adv_curl:
+                adv = [-sn2 * (x["cvtc"] * vp - x["cvpc"] * vt),
+                       -o4 * (x["cvpc"] * vr - x["cvrc"] * vp),
+                       -o4 * (x["cvrc"] * vt - x["cvtc"] * vr)]
+            else:
+                adv = [-o2 * oh * (vr * (x["dvrdrc"] - (two * o1 + bt_) * vr) +
+                                   sn2 * (vt * (x["dvrdtc"] - rr[i] * vt) + vp * (x["dvrdpc"] - rr[i] * vp))),
+                       o4 * oh * (-vr * (x["dvtdrc"] - bt_ * vt) +
+                                  vt * (cn2 * vt + x["dvpdpc"] + x["dvrdrc"]) +
+                                  vp * (cn2 * vp - x["dvtdpc"])),
+                       o4 * oh * (-vr * (x["dvpdrc"] - bt_ * vp) - vt * (x["dvtdpc"] + x["cvrc"]) -
+                                  vp * x["dvpdpc"])]
+        # transform_to_lm_space (rIter.f90:645-662)
+        if bulk and (l_conv_nl or l_mag_LF):
+            if l_conv_nl and l_mag_LF:
+                if lc[i] == 0:
+                    adv = [a + b for a, b in zip(adv, LF)]
+            elif l_mag_LF:
+                adv = list(LF) if lc[i] == 0 else [np.zeros(shape[1:])] * 3
+            for k, v in zip(("Advr", "Advt", "Advp"), adv):
+                out[k][i] = v
+        if l_heat_nl and bulk:
+            out["VSr"][i] = x["vrc"] * x["sc"]
+            out["VSt"][i] = o2 * x["vtc"] * x["sc"]
+            out["VSp"][i] = o2 * x["vpc"] * x["sc"]
+        if l_chemical_conv and bulk:
+            out["VXir"][i] = x["vrc"] * x["xic"]
+            out["VXit"][i] = o2 * x["vtc"] * x["xic"]
+            out["VXip"][i] = o2 * x["vpc"] * x["xic"]
+        if l_mag_nl:
+            if bulk and lc[i] == 0:
+                out["VxBr"][i] = oh * sn2 * (x["vtc"] * x["bpc"] - x["vpc"] * x["btc"])
+                out["VxBt"][i] = oh * o4 * (x["vpc"] * x["brc"] - x["vrc"] * x["bpc"])
+                out["VxBp"][i] = oh * o4 * (x["vrc"] * x["btc"] - x["vtc"] * x["brc"])
+            elif nb[i] == 1 or lc[i] != 0:
+                out["VxBt"][i] = o4 * oh * x["vpc"] * x["brc"]
+                out["VxBp"][i] = -o4 * oh * x["vtc"] * x["brc"]
+            elif nb[i] == 2:
+                out["VxBt"][i] = o4 * oh * x["vpc"] * x["brc"]
+                out["VxBp"][i] = 0.0
+        if l_anel and bulk:
+            vr, vt, vp = x["vrc"], x["vtc"], x["vpc"]
+            h = ViscHeatFac * o4 * oh * ot * vi * (
+                two * (x["dvrdrc"] - (two * o1 + bt_) * vr) ** 2 +
+                two * (cn2 * vt + x["dvpdpc"] + x["dvrdrc"] - o1 * vr) ** 2 +
+                two * (x["dvpdpc"] + cn2 * vt + o1 * vr) ** 2 +
+                (two * x["dvtdpc"] + x["cvrc"] - two * cn2 * vp) ** 2 +
+                sn2 * ((rr[i] * x["dvtdrc"] - (two + bt_ * rr[i]) * vt + o1 * x["dvrdtc"]) ** 2 +
+                       (rr[i] * x["dvpdrc"] - (two + bt_ * rr[i]) * vp + o1 * x["dvrdpc"]) ** 2) -
+                two * third * (bt_ * vr) ** 2)
+            if l_mag_nl and lc[i] == 0:
+                h = h + OhmLossFac * o2 * ot * la * (o2 * x["cbrc"] ** 2 + sn2 * x["cbtc"] ** 2 +
+                                                     sn2 * x["cbpc"] ** 2)
+            out["heatTerms"][i] = h
+    return out
+
+
+def get_td_full(spec: dict, r, cor_fac: float, l_max: int, minc: int = 1, lcut=None, nbc=None,
+                l_conv_nl=True, l_corr=True, l_double_curl=False, l_single_matrix=False, l_anel=False,
+                l_anelastic_liquid=False, l_mag_nl=True, orho1=None, beta=None, temp0=None, epsc=None,
+                epscXi=0.0, outputs=("dwdt", "dzdt", "dpdt", "dsdt", "dxidt", "dbdt", "djdt", "dVxBhLM",
+                                     "dVxVhLM", "dVSrLM", "dVXirLM")) -> dict:
+    """The spectral assembly of get_td.f90 with the reference's switches, per
+    level (the calls of rIter.f90:410-428; an output is computed when it is
+    in ``outputs``, standing for the equation being on):
+      get_dwdt (:133-208) or get_dwdt_double_curl (:210-309, with dVxVhLM),
+      get_dpdt (:311-379), get_dzdt (:381-457), get_dsdt (:459-521, with the
+      anelastic heatTermsLM and temp0), get_dxidt (:523-556), get_dbdt
+      (:558-619; l_mag_nl False: zeros).
+    Entries the reference does not set at a level are NaN.  Arrays
+    [level][lm] complex in the m-major st_map order; numpy FP64."""
+    ls, ms = [], []
+    for m in range(0, l_max + 1, minc):
+        for l in range(m, l_max + 1):
+            ls.append(l)
+            ms.append(m)
+    l = np.array(ls, dtype=np.float64)
+    m = np.array(ms, dtype=np.float64)
+    li = np.array(ls)
+    rr_all = np.asarray(r, dtype=np.float64)
+    n = rr_all.size
+    K = len(ls)
+
+    def clm(ll, mm):
+        return np.sqrt(np.maximum((ll + mm) * (ll - mm), 0.0) / ((2 * ll - 1) * (2 * ll + 1)))
+
+    hasS = li > np.array(ms)
+    cS = np.where(hasS, clm(l, m), 0.0)
+    cA = clm(l + 1, m)
+    dLh = l * (l + 1)
+    t2S, t2A = (l - 1) * cS, (l + 2) * cA
+    t3S, t3A = (l - 1) * (l + 1) * cS, l * (l + 2) * cA
+    t4S, t4A = (l + 1) * cS * (l - 1) * l, l * cA * (l + 1) * (l + 2)
+    idxS = np.where(hasS, np.arange(K) - 1, np.arange(K))
+    idxA = np.minimum(np.arange(K) + 1, K - 1)
+    one = np.ones(n)
+    oh_all = one if orho1 is None else np.asarray(orho1, dtype=np.float64)
+    be_all = np.zeros(n) if beta is None else np.asarray(beta, dtype=np.float64)
+    t0_all = one if temp0 is None else np.asarray(temp0, dtype=np.float64)
+    ep_all = np.zeros(n) if epsc is None else np.asarray(epsc, dtype=np.float64)
+    nb_all = np.zeros(n, dtype=int) if nbc is None else np.asarray(nbc)
+    out = {k: np.full((n, K), np.nan + 0j, dtype=np.complex128) for k in outputs}
+    S = {k: (None if spec.get(k) is None else np.asarray(spec[k])) for k in
+         ("w", "dw", "ddw", "z", "dz", "AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "heatTermsLM", "VXitLM",
+          "VxBrLM", "VxBtLM", "VxBpLM")}
+    cor = 2.0 * cor_fac
+    dphi = 1j * m
+    for ir in range(n):
+        rr = rr_all[ir]
+        or1, or2 = 1.0 / rr, 1.0 / rr ** 2
+        or4 = or2 * or2
+        oh, be = oh_all[ir], be_all[ir]
+        bulk = int(nb_all[ir]) == 0
+        lR = l_max if lcut is None else min(int(np.asarray(lcut)[ir]), l_max)
+        A = np.where(li < lR, 1.0, 0.0)
+        inside = li <= lR
+        lv = {k: (None if v is None else v[ir]) for k, v in S.items()}
+
+        def nb(x):
+            return x[idxA] * A, x[idxS]
+        if bulk:
+            w, dw, z = lv["w"], lv["dw"], lv["z"]
+            zA, zS = nb(z)
+            dwA, dwS = nb(dw)
+            wA, wS = nb(w)
+            if "dzdt" in out:
+                dz_ = (dLh * lv["AdvpLM"]) if l_conv_nl else np.zeros(K, complex)
+                if l_corr:
+                    c = dphi * z + t3A * dwA + or1 * t4A * wA + t3S * dwS - or1 * t4S * wS
+                    dz_ = dz_ + np.where(inside, cor * or2 * c, 0)
+                # lm = 1 (get_td.f90:401-409)
+                dz_[0] = cor * or2 * (t3A[0] * dw[idxA[0]] + or1 * t4A[0] * w[idxA[0]]) if l_corr else 0.0
+                out["dzdt"][ir] = dz_
+            if "dwdt" in out:
+                d0 = or2 * lv["AdvrLM"][0] if l_conv_nl else 0.0
+                if l_corr and not l_single_matrix:
+                    d0 = d0 + cor * or1 * t2A[0] * z[idxA[0]]
+                if not l_double_curl:
+                    dw_ = (or2 * lv["AdvrLM"]) if l_conv_nl else np.zeros(K, complex)
+                    if l_corr:
+                        c = dphi * dw + t2A * zA - t2S * zS
+                        dw_ = dw_ + np.where(inside, cor * or1 * c, 0)
+                else:
+                    ddw, dzz = lv["ddw"], lv["dz"]
+                    dzA, dzS = nb(dzz)
+                    if l_conv_nl:
+                        dw_ = dLh * or4 * oh * lv["AdvrLM"]
+                        vh = -oh * rr * rr * dLh * lv["AdvtLM"]
+                    else:
+                        dw_ = np.zeros(K, complex)
+                        vh = np.zeros(K, complex)
+                    if l_corr:
+                        c = (dphi * (-ddw + be * dw + (be * or1 + or2) * dLh * w) +
+                             t3A * (dzA - be * zA) + t3S * (dzS - be * zS) + or1 * (t4A * zA - t4S * zS))
+                        dw_ = dw_ + np.where(inside, cor * or2 * oh * c, 0)
+                    if "dVxVhLM" in out:
+                        vh = vh.copy()
+                        vh[0] = out["dVxVhLM"][ir][0]  # lm = 1 left as it was
+                        out["dVxVhLM"][ir] = vh
+                dw_ = dw_.copy()
+                dw_[0] = d0
+                out["dwdt"][ir] = dw_
+            if "dpdt" in out:
+                dp = (-dLh * lv["AdvtLM"]) if l_conv_nl else np.zeros(K, complex)
+                if l_corr:
+                    c = -dphi * (dw + or1 * dLh * w) + t3A * zA + t3S * zS
+                    dp = dp + np.where(inside, cor * or2 * c, 0)
+                dp = dp.copy()
+                dp[0] = np.nan  # get_dpdt leaves lm = 1
+                out["dpdt"][ir] = dp
+            if "dsdt" in out:
+                ds = dLh * lv["VStLM"]
+                if l_anel:
+                    ds = ds + (t0_all[ir] if l_anelastic_liquid else 1.0) * lv["heatTermsLM"]
+                ds = ds.copy()
+                ds[0] = ep_all[ir] + ((t0_all[ir] if l_anelastic_liquid else 1.0) * lv["heatTermsLM"][0]
+                                      if l_anel else 0.0)
+                out["dsdt"][ir] = ds
+            if "dxidt" in out:
+                dx = dLh * lv["VXitLM"]
+                dx = dx.copy()
+                dx[0] = epscXi
+                out["dxidt"][ir] = dx
+            if l_mag_nl:
+                for k, v in (("dbdt", dLh * lv["VxBpLM"]), ("dVxBhLM", -dLh * lv["VxBtLM"] * rr * rr),
+                             ("djdt", dLh * or4 * lv["VxBrLM"])):
+                    if k in out:
+                        out[k][ir] = v
+            else:
+                for k in ("dbdt", "djdt", "dVxBhLM"):
+                    if k in out:
+                        out[k][ir] = 0.0
+        else:
+            if l_double_curl and "dVxVhLM" in out:
+                out["dVxVhLM"][ir] = 0.0
+            if "dsdt" in out and "dVSrLM" in out:
+                out["dVSrLM"][ir] = 0.0
+            if "dxidt" in out and "dVXirLM" in out:
+                out["dVXirLM"][ir] = 0.0
+            if "dVxBhLM" in out:
+                if l_mag_nl:
+                    v = -dLh * lv["VxBtLM"] * rr * rr
+                    v[0] = 0.0
+                    out["dVxBhLM"][ir] = v
+                else:
+                    out["dVxBhLM"][ir] = 0.0
+    return out

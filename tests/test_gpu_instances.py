@@ -3,10 +3,12 @@
 minc in {1, 4}) against the oracle on one radial level of the radial-loop
 transform set (rIter.f90:466-712: 15 grids from 13 spectra, then 10 spectra
 from the grids):
-  - FP64 form: every output <= 1e-12 relative L2 (the parity tolerance);
-  - FP64-accurate tensor-core form: every output <= 1e-11 relative L2 (its
-    double-float FFTs round at 2^-48; outputs much smaller than the other
-    outputs of their call carry that error times the ratio);
+  - FP64 form and FP64-accurate tensor-core form: every call normwise
+    <= 1e-12 and every output <= 1e-11 relative L2.  An output much smaller
+    than the other outputs of its call carries the call's rounding error
+    times the ratio: the spheroidal part of the curl's spat_to_qst at
+    l_max = 255 is ~600x smaller than its partners, and the FP64 form itself
+    differs from the oracle there by 2.8e-12;
   - 3xBF16 form: every call normwise <= 1e-6 (a vector field's three grids,
     or the q, s, t of one spat_to_qst).
 minc = 4 with l_max = 63 or 127 runs the general-size FFT (n_phi/2 = 24 or
@@ -71,7 +73,7 @@ def test_instance_size_matches_oracle(built, oracle_mod, torch, L, minc):
     groups = [("vrc", "vtc", "vpc"), ("cvrc", "cvtc", "cvpc"), ("brc", "btc", "bpc"), ("cbrc", "cbtc", "cbpc"),
               ("AdvrLM", "AdvtLM", "AdvpLM"), ("VSrLM", "VStLM", "VSpLM"), ("VxBrLM", "VxBtLM", "VxBpLM"),
               ("sc",), ("pc",), ("xic",), ("heatTermsLM",)]
-    for prec, tol in (("fp64", 1e-12), ("fp64tc", 1e-11), ("bf16x3", 1e-6)):
+    for prec, tol in (("fp64", 1e-12), ("fp64tc", 1e-12), ("bf16x3", 1e-6)):
         s = SHT(L, minc, N, P, precision=prec, device=0)
         g = s.transform_to_grid_space(d, or2=torch.from_numpy(or2).cuda())
         lm = s.transform_to_lm_space(dfwd)
@@ -83,10 +85,9 @@ def test_instance_size_matches_oracle(built, oracle_mod, torch, L, minc):
         if prec != "bf16x3":
             for k in ref:
                 e = rel_l2(got[k], ref[k])
-                assert e <= tol, (prec, k, e)
-        else:
-            for ks in groups:
-                num = sum(float(np.linalg.norm(got[k] - ref[k])) ** 2 for k in ks) ** 0.5
-                den = sum(float(np.linalg.norm(ref[k])) ** 2 for k in ks) ** 0.5
-                assert num / den <= tol, (prec, ks, num / den)
+                assert e <= 10 * tol, (prec, k, e)
+        for ks in groups:
+            num = sum(float(np.linalg.norm(got[k] - ref[k])) ** 2 for k in ks) ** 0.5
+            den = sum(float(np.linalg.norm(ref[k])) ** 2 for k in ks) ** 0.5
+            assert num / den <= tol, (prec, ks, num / den)
         s.close()
