@@ -49,8 +49,14 @@ template <> __device__ __forceinline__ dfl2 ld_hs<dfl2>(const dfl2* p, bool f64)
 }
 template <typename T2> __device__ __forceinline__ void st_hs(T2* p, T2 v, bool) { *p = v; }
 template <> __device__ __forceinline__ void st_hs<dfl2>(dfl2* p, dfl2 v, bool f64) {
-  if (f64) *(double2*)p = to_d2(v);
-  else *p = v;
+  if (f64) {
+    *(double2*)p = to_d2(v);
+  } else {
+    // normalized pairs: the tensor-core analysis scales its digits by max |hi|
+    v.x = df_norm(v.x);
+    v.y = df_norm(v.y);
+    *p = v;
+  }
 }
 
 template <typename T2, int R> struct Bfly;
@@ -188,10 +194,44 @@ struct TwTab {
   }
 };
 
+// One cross-lane radix-2 DIF stage of distance d (d = 16, 8, 4, 2, 1).
+template <typename T2, int S>
+__device__ __forceinline__ void lane_stage(T2 (&a)[S], const T2* __restrict__ tab, int s, int d, int lane) {
+  typedef TwTab<S> TT;
+  typedef typename ScalarOf<T2>::t T;
+  const bool up = (lane & d) != 0;
+  const T sg = up ? (T)-1 : (T)1;
+  T2 w;
+  if (d > 1) {
+    const int st = d == 16 ? 0 : d == 8 ? 1 : d == 4 ? 2 : 3;
+    w = twid(tab + TT::kLane, st * 32 + lane, s);
+    if (!up) { w.x = (T)1; w.y = (T)0; }
+  }
+#pragma unroll
+  for (int q = 0; q < S; ++q) {
+    const T2 b = shfl_xor2(a[q], d);
+    T2 t;
+    t.x = add_signed(sg, a[q].x, b.x);
+    t.y = add_signed(sg, a[q].y, b.y);
+    a[q] = d > 1 ? cmul(t, w) : t;
+  }
+}
+
 template <typename T2, int S>
 __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tab, int s) {
   typedef TwTab<S> TT;
   const int lane = threadIdx.x & 31;
+  if constexpr (std::is_same<T2, dfl2>::value) {
+    // double-float: the five cross-lane stages as a loop (the unrolled code
+    // stalled on instruction fetch), then the same four-step twiddles and
+    // register FFT
+#pragma unroll 1
+    for (int d = 16; d >= 1; d >>= 1) lane_stage<T2, S>(a, tab, s, d, lane);
+#pragma unroll
+    for (int q = 1; q < S; ++q) a[q] = cmul(a[q], twid(tab + TT::kPost, q * 32 + lane, s));
+    reg_fft<T2, S>(a, tab + TT::kRoot, s);
+    return;
+  }
   typedef typename ScalarOf<T2>::t T;
 #pragma unroll
   for (int d = 16; d >= 1; d >>= 1) {
@@ -362,8 +402,17 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_inv_fast(const ShtGe
   const long long dstep = 2LL * KS * g.ld;
   double* dst = out + (long long)(2 * kq) * g.ld + rowg;
   for (int kk = kq; kk < n; kk += KS, s0 += 33 * (KS / 32), dst += dstep) {
-    const T2 v0 = cscale(s0[0], o);  // phi = 2kk (x) and 2kk+1 (y) of row rp
-    const T2 v1 = cscale(s0[KP], o);
+    T2 v0 = s0[0], v1 = s0[KP];  // phi = 2kk (x) and 2kk+1 (y) of rows rp, rp + 1
+    if constexpr (std::is_same<T, dfl>::value) {
+      // a double-float product costs ~10 FP32 operations: only the 1/sin^2 fields pay it
+      if (fd.flags & FFT_OSIN2) {
+        v0 = cscale(v0, o);
+        v1 = cscale(v1, o);
+      }
+    } else {
+      v0 = cscale(v0, o);
+      v1 = cscale(v1, o);
+    }
     // row rp widens on the FP64 pipe (idle in this kernel), row rp + 1 with
     // integer instructions: splitting the conversions between the two pipes
     // measured faster than either alone.  Both are exact; FP32 subnormals

@@ -449,7 +449,9 @@ __global__ void __launch_bounds__(kPackThreads) pack_fwd_oz(const ShtGeom g, con
                                                             unsigned char* __restrict__ bimg, short* __restrict__ cexp,
                                                             int nct) {
   extern __shared__ unsigned char smem_raw[];
-  unsigned char* buf = align1k(smem_raw);  // two (ES, EA) tile pairs
+  // one (ES, EA) tile pair (56 KB): four CTAs per SM; the next chunk waits for
+  // the bulk store of the previous one (two pairs measured 1 CTA per SM, 1.8 ms)
+  unsigned char* buf = align1k(smem_raw);
   __shared__ int sE[2][kNC];
   const int ct = blockIdx.x, mc = blockIdx.y;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
@@ -499,9 +501,9 @@ __global__ void __launch_bounds__(kPackThreads) pack_fwd_oz(const ShtGeom g, con
 #pragma unroll
   for (int i = 0; i < 4; ++i) srcs[i] = src_of(ct * (kNC / 2) + qg + 4 * i);
   for (int c = 0; c < t.ncj; ++c) {
-    unsigned char* B = buf + (c & 1) * 2 * kTS;
-    if (c >= 2) {
-      if (tid == 0) tc::bulk_wait_read<1>();
+    unsigned char* B = buf;
+    if (c >= 1) {
+      if (tid == 0) tc::bulk_wait_read<0>();
       __syncthreads();
     }
     const int j = 64 * c + k;
@@ -1050,7 +1052,7 @@ cudaError_t launch_fwd_oz(const ShtGeom& g, const FwdSet& s, const TcTables& t, 
   if (ncplx <= 0) return cudaSuccess;
   const int nct = (int)oz_nct(ncplx);
   short* cexp = (short*)(bimg + oz_tiles_bytes_fwd(g, t, nct));
-  const size_t psmem = 1024 + 4 * (size_t)kTS;
+  const size_t psmem = 1024 + 2 * (size_t)kTS;
   CUDA_TRY(cudaFuncSetAttribute(pack_fwd_oz<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
   pack_fwd_oz<VEC><<<dim3(nct, g.n_m), kPackThreads, psmem, st>>>(g, s, t, bimg, cexp, nct);
   CUDA_TRY(cudaGetLastError());
