@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x2", "fp64tc"])
+    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x2", "fp64tc", "fp64"])
     ap.add_argument("--cpu-levels", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -51,6 +51,8 @@ def parse():
                     help="instead of the bench line: sixteen mixed-size instances in one graph (one JSON line)")
     ap.add_argument("--only-reduced", action="store_true", help="skip the FP64 form (profiling)")
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations (C0, C1, C3, C4)")
+    ap.add_argument("--stage-only", action="store_true",
+                    help="profiling case: two radial-loop stages of --form over --levels levels, then exit")
     ap.add_argument("--clock-seconds", type=float, default=1.5,
                     help="back-to-back steps sampled for clocks before the timed steps")
     return ap.parse_args()
@@ -533,6 +535,17 @@ def our_arm(args):
 
     spec_np = grid_space_inputs(L_MAX, MINC, N_LEVELS, seed=1234 + 7919 * rank)
     spec = {k: torch.from_numpy(v).to(dev) for k, v in spec_np.items()}
+    if args.stage_only:
+        from magic_gb300.radial_loop import RadialLoop
+        from magic_gb300.workload import radii
+        sp = SHT(L_MAX, MINC, N_THETA, N_PHI, precision=form, device=local)
+        loop = RadialLoop(sp, radii(N_LEVELS), cor_fac=1e3, ktopv=2, kbotv=2)
+        for _ in range(2):
+            loop.step(spec)
+        torch.cuda.synchronize()
+        sp.device_status()
+        print(json.dumps({"form": form, "levels": N_LEVELS, "stage_only": True}), flush=True)
+        return
     or2_np = or2_levels(N_LEVELS)
     or2 = torch.from_numpy(or2_np).to(dev)
     fin = {}  # analysis inputs: nonlinear products of the FP64 synthesis grids (set below)
