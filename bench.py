@@ -9,8 +9,11 @@ seeded spectra with std (l+1)^-2 and a radial envelope; the forward inputs
 are the grids produced by the inverse transforms.
 
 One step = both transform sets over all 129 levels.  The headline `value` is
-radial levels/s of the reduced-precision form; the FP64 form is timed in the
-same run, and the reduced form's relative L2 error against it is reported.
+radial levels/s of the FP64-accurate tensor-core form (fp64tc: every output
+within 1e-6 relative L2 of the FP64 form, reported per output); the FP64 form
+is timed in the same run, and the 3xBF16 / 2xTF32 forms, the other
+configurations (l_max 63 and 511, the sixteen-instance case), one explicit
+stage of the radial loop and the CPU oracle are reported beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
