@@ -159,9 +159,11 @@ __device__ __forceinline__ void reg_fft(T2 (&a)[S], const T2* __restrict__ tw, i
 
 // Complex FFT of length n = 32*S held by one warp, four-step with the
 // 32-point radix-2 DIF across lanes first and the length-S DFT in registers
-// last:  input a[q] = z[S*lane + q],  output a[k2] = Z[brev5(lane) + 32*k2].
-// Outputs of one register are therefore 32 consecutive indices across the
-// warp, which keeps the shared-memory write-back free of bank conflicts.
+// last:  input a[q] = z[S*lane + q],  output a[k2] = Z[brev5(lane) + 32*k2]
+// (brev5(hx_pos(lane)) in the half-exchange form of the double-float
+// transforms).  Outputs of one register are therefore 32 consecutive indices
+// across the warp, which keeps the shared-memory write-back free of bank
+// conflicts.
 __device__ __forceinline__ int brev5(int x) { return __brev(x) >> 27; }
 
 // Twiddle tables of the fast path in shared memory, laid out so that every
@@ -217,11 +219,90 @@ __device__ __forceinline__ void lane_stage(T2 (&a)[S], const T2* __restrict__ ta
   }
 }
 
+// Double-float cross-lane stages as half exchanges (S even, H = S/2).  In the
+// stage of lane bit d the lane with that bit clear combines the pairs held in
+// its registers 0..H-1, its partner the pairs in H..S-1: each lane sends and
+// receives H values instead of S and twiddles H differences instead of S
+// values (half of which the full exchange multiplies by 1).  Sums go to
+// register j, differences to j + H, so a stage swaps lane bit d with the
+// register half: after the five stages lane bits 4..0 hold (q / H, l4, l3,
+// l2, l1) of the DIF position l and of the register index q, the register
+// half holds l0.  One more exchange across lane bit 16 gives every lane all S
+// values of the position hx_pos(lane).  The upper lane of a pair forms
+// own - received = -(lower - upper): its sign is folded into the twiddle.
+// The d = 2 twiddles are 1 and s i, applied as a swap and signs.
+__device__ __forceinline__ int hx_pos(int lane) { return ((lane & 15) << 1) | (lane >> 4); }
+__device__ __forceinline__ dfl df_sgn(dfl a, float g) { return mkdf(a.h * g, a.l * g); }  // g = +-1: exact
+
+template <int S>
+__device__ __forceinline__ void warp_fft_hx(dfl2 (&a)[S], const dfl2* __restrict__ tab, int s, int lane) {
+  typedef TwTab<S> TT;
+  constexpr int H = S / 2;
+#pragma unroll 1
+  for (int d = 16; d >= 1; d >>= 1) {
+    const bool up = (lane & d) != 0;
+    const float g = up ? -1.f : 1.f;
+    if (d >= 4) {
+      const int st = d == 16 ? 0 : d == 8 ? 1 : 2;
+      dfl2 w = twid(tab + TT::kLane, st * 32 + lane, s);
+      w.x = df_sgn(w.x, g);
+      w.y = df_sgn(w.y, g);
+#pragma unroll
+      for (int j = 0; j < H; ++j) {
+        const dfl2 snd = up ? a[j] : a[j + H];
+        const dfl2 own = up ? a[j + H] : a[j];
+        const dfl2 rcv = shfl_xor2(snd, d);
+        a[j] = cadd(own, rcv);
+        a[j + H] = cmul(csub(own, rcv), w);
+      }
+    } else {
+      // d = 2: t (g s i) on odd lanes = g s (-t.y, t.x), t g on even lanes; d = 1: t g
+      const bool sw = d == 2 && (lane & 1);
+      const float fx = sw ? -g * (float)s : g, fy = sw ? g * (float)s : g;
+#pragma unroll
+      for (int j = 0; j < H; ++j) {
+        const dfl2 snd = up ? a[j] : a[j + H];
+        const dfl2 own = up ? a[j + H] : a[j];
+        const dfl2 rcv = shfl_xor2(snd, d);
+        a[j] = cadd(own, rcv);
+        const dfl2 t = csub(own, rcv);
+        dfl2 r;
+        r.x = df_sgn(sw ? t.y : t.x, fx);
+        r.y = df_sgn(sw ? t.x : t.y, fy);
+        a[j + H] = r;
+      }
+    }
+  }
+  // lane bit 16 <-> register half: the lower lane keeps l0 = 0, the upper l0 = 1
+  const bool up4 = (lane & 16) != 0;
+#pragma unroll
+  for (int j = 0; j < H; ++j) {
+    const dfl2 snd = up4 ? a[j] : a[j + H];
+    const dfl2 rcv = shfl_xor2(snd, 16);
+    a[j] = up4 ? rcv : a[j];
+    a[j + H] = up4 ? a[j + H] : rcv;
+  }
+  const int pl = hx_pos(lane);
+#pragma unroll
+  for (int q = 1; q < S; ++q) a[q] = cmul(a[q], twid(tab + TT::kPost, q * 32 + pl, s));
+  reg_fft<dfl2, S>(a, tab + TT::kRoot, s);
+}
+
+// DIF position held by a lane after warp_fft: output a[k2] = Z[brev5(pos) + 32 k2]
+template <typename T2, int S>
+__device__ __forceinline__ int fft_pos(int lane) {
+  if constexpr (std::is_same<T2, dfl2>::value && S % 2 == 0) return hx_pos(lane);
+  else return lane;
+}
+
 template <typename T2, int S>
 __device__ __forceinline__ void warp_fft(T2 (&a)[S], const T2* __restrict__ tab, int s) {
   typedef TwTab<S> TT;
   const int lane = threadIdx.x & 31;
-  if constexpr (std::is_same<T2, dfl2>::value) {
+  if constexpr (std::is_same<T2, dfl2>::value && S % 2 == 0) {
+    warp_fft_hx<S>(a, tab, s, lane);
+    return;
+  } else if constexpr (std::is_same<T2, dfl2>::value) {
     // double-float: the five cross-lane stages as a loop (the unrolled code
     // stalled on instruction fetch), then the same four-step twiddles and
     // register FFT
@@ -386,7 +467,7 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_inv_fast(const ShtGe
     }
     __syncwarp();
     warp_fft<T2, S>(a, stw, +1);
-    const int k1 = brev5(lane);
+    const int k1 = brev5(fft_pos<T2, S>(lane));
 #pragma unroll
     for (int k2 = 0; k2 < S; ++k2) row[pos(k1 + 32 * k2)] = a[k2];  // z_j = x_{2j} + i x_{2j+1}
     __syncwarp();
@@ -505,7 +586,7 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_fwd_fast(const ShtGe
     for (int q = 0; q < S; ++q) a[q] = row[q * 33 + lane];  // = z[S*lane + q]
     __syncwarp();
     warp_fft<T2, S>(a, stw, -1);
-    const int k1 = brev5(lane);
+    const int k1 = brev5(fft_pos<T2, S>(lane));
 #pragma unroll
     for (int k2 = 0; k2 < S; ++k2) row[pos(k1 + 32 * k2)] = a[k2];
     __syncwarp();

@@ -87,22 +87,32 @@ __device__ __forceinline__ long long fixed_from_float(float x, int sh) {
   else F = (long long)((m + (1ull << (-s - 1))) >> (-s));
   return (b >> 31) ? -F : F;
 }
-// The seven balanced base-256 digits of F (|F| <= 2^55) as BF16 bit patterns:
-// F = sum_i d_i 2^(8(6-i)), |d_i| <= 128.
-__device__ __forceinline__ uint16_t bf16_of_int(int d) {
-  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;  // exact for |d| < 2^22
-  return (uint16_t)(__float_as_uint(f) >> 16);                    // exact: |d| <= 128
+// The seven balanced base-256 digits of F as FP32 values (exact small
+// integers; d_0 the most significant), with one byte permute and one FP32
+// subtraction per digit: every byte of U = F + 0x80808080808080 (a bias of
+// 128 in each of the seven bytes) is u = d + 128 with d in [-128, 127], and
+// the top digit is (U >> 48) - 128 in [-128, 128] (|F| <= 2^55 keeps U in
+// [0, 2^56 + 2^48]).  A byte u placed in the mantissa of 0x4B400000 is the
+// float 1.5 2^23 + u.
+__device__ __forceinline__ void digits7f(long long F, float (&f)[kS]) {
+  const unsigned long long U = (unsigned long long)F + 0x80808080808080ull;
+  const uint32_t lo = (uint32_t)U, hi = (uint32_t)(U >> 32);
+  constexpr uint32_t kMag = 0x4B400000u;
+  constexpr float kOff = 12583040.0f;  // 1.5 2^23 + 128
+  f[6] = __uint_as_float(__byte_perm(lo, kMag, 0x7640)) - kOff;
+  f[5] = __uint_as_float(__byte_perm(lo, kMag, 0x7641)) - kOff;
+  f[4] = __uint_as_float(__byte_perm(lo, kMag, 0x7642)) - kOff;
+  f[3] = __uint_as_float(__byte_perm(lo, kMag, 0x7643)) - kOff;
+  f[2] = __uint_as_float(__byte_perm(hi, kMag, 0x7640)) - kOff;
+  f[1] = __uint_as_float(__byte_perm(hi, kMag, 0x7641)) - kOff;
+  f[0] = __uint_as_float(__byte_perm(hi, kMag, 0x7632)) - kOff;  // bytes 6 and 7 of U
 }
-__device__ __forceinline__ void digits7(long long F, uint16_t (&d)[kS]) {
-#pragma unroll
-  for (int i = kS - 1; i >= 1; --i) {
-    int v = (int)(F & 255);
-    v -= (v >= 128) ? 256 : 0;
-    d[i] = bf16_of_int(v);
-    F = (F - v) >> 8;
-  }
-  d[0] = bf16_of_int((int)F);
+// two FP32 values (small integers, exact) as one bf16x2 word, lo at the lower address
+__device__ __forceinline__ uint32_t bf16x2_of(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x = lo in the low half
+  return *reinterpret_cast<const uint32_t*>(&v);
 }
+__device__ __forceinline__ uint16_t bf16_bits(float x) { return (uint16_t)(bf16x2_of(x, 0.f) & 0xFFFFu); }
 // Synthesis degree weights: the table is stored times w_l and the spectra
 // divided by w_l, w_l = 2^-k(l), k(l) = floor(log2(l+1)) (exact, cancels in
 // the sum).  dP grows about like l along a table row while the spectra fall
@@ -125,14 +135,18 @@ __device__ __forceinline__ int scale_exp(double mx) {
 }
 // fixed-point position of the digits: F = round(x 2^(kFix - E)), |x| < 2^E
 constexpr int kFix = 8 * kS - 1;
-// digits of x scaled by 2^-E (|x| < 2^E)
+// digits of x scaled by 2^-E (|x| < 2^E), as BF16 bit patterns
 __device__ __forceinline__ void digits_of(double x, int E, uint16_t (&d)[kS]) {
-  digits7(fixed_from_double(x, kFix - E), d);
-}
-__device__ __forceinline__ void store_digits(unsigned char* tile, int row, int k, const uint16_t (&d)[kS]) {
-  // digit block i holds rows i*kNC .. i*kNC + kNC - 1 of the stacked B operand
+  float f[kS];
+  digits7f(fixed_from_double(x, kFix - E), f);
 #pragma unroll
-  for (int i = 0; i < kS; ++i) *(uint16_t*)(tile + tc::sw128_offset(i * kNC + row, k)) = d[i];
+  for (int i = 0; i < kS; ++i) d[i] = bf16_bits(f[i]);
+}
+// the digits of one row at the even index k (f[0]) and k + 1 (f[1]): one
+// 32-bit store per digit block
+__device__ __forceinline__ void store_digit_pairs(unsigned char* tile, int row, int k, const float (&f)[2][kS]) {
+#pragma unroll
+  for (int i = 0; i < kS; ++i) *(uint32_t*)(tile + tc::sw128_offset(i * kNC + row, k)) = bf16x2_of(f[0][i], f[1][i]);
 }
 
 // ------------------------------------------------------------ accumulators
@@ -363,7 +377,7 @@ __device__ __forceinline__ PackCol pack_col(const ShtGeom& g, const InvSet& s, i
 }
 
 template <bool VEC>
-__global__ void __launch_bounds__(kPackThreads) pack_inv_oz(const ShtGeom g, const InvSet s, const TcTables t,
+__global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const ShtGeom g, const InvSet s, const TcTables t,
                                                             unsigned char* __restrict__ bimg, short* __restrict__ cexp,
                                                             int nct) {
   extern __shared__ unsigned char smem_raw[];
@@ -380,13 +394,24 @@ __global__ void __launch_bounds__(kPackThreads) pack_inv_oz(const ShtGeom g, con
     const PackCol c = pack_col<VEC>(g, s, ct * (kNC / 2) + ql, ncplx);
     // largest exponent of x 2^k(l) (the spectra divided by the degree weights)
     int er = -4096, ei = -4096;
-    if (c.op.op != OP_ZERO)
-      for (int loff = li; loff < n_l && m + loff <= c.lc; loff += 16) {
-        const double2 v = oz_operand(c.op, c.r, lm0, loff, m + loff, m, c.or2);
-        const int k = deg_shift(m + loff);
-        er = max(er, exp_bound(v.x) + k);
-        ei = max(ei, exp_bound(v.y) + k);
+    if (c.op.op != OP_ZERO) {
+      const int nl = min(n_l, c.lc - m + 1);
+      // eight independent loads per thread in flight before their exponents are taken
+      for (int l0 = li; l0 < nl; l0 += 16 * 8) {
+        double2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int loff = l0 + 16 * u;
+          v[u] = loff < nl ? oz_operand(c.op, c.r, lm0, loff, m + loff, m, c.or2) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = deg_shift(m + l0 + 16 * u);
+          er = max(er, exp_bound(v[u].x) + k);
+          ei = max(ei, exp_bound(v[u].y) + k);
+        }
       }
+    }
 #pragma unroll
     for (int d = 8; d >= 1; d >>= 1) {
       er = max(er, __shfl_xor_sync(0xffffffffu, er, d));
@@ -402,11 +427,11 @@ __global__ void __launch_bounds__(kPackThreads) pack_inv_oz(const ShtGeom g, con
     }
   }
   __syncthreads();
-  // pass 2: thread = (degree index k of the chunk, column group qg)
-  const int k = tid & 63, qg = tid >> 6;
-  PackCol cols[4];
+  // pass 2: thread = (degree indices 2 kp, 2 kp + 1 of the chunk, column group qg)
+  const int kp = tid & 31, qg = tid >> 5;
+  PackCol cols[2];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) cols[i] = pack_col<VEC>(g, s, ct * (kNC / 2) + qg + 4 * i, ncplx);
+  for (int i = 0; i < 2; ++i) cols[i] = pack_col<VEC>(g, s, ct * (kNC / 2) + qg + 8 * i, ncplx);
   int nb = 0;
   for (int p = 0; p < 2; ++p)
     for (int c = 0; c < nch; ++c, ++nb) {
@@ -415,20 +440,27 @@ __global__ void __launch_bounds__(kPackThreads) pack_inv_oz(const ShtGeom g, con
         if (tid == 0) tc::bulk_wait_read<1>();
         __syncthreads();
       }
-      const int loff = p + 2 * (64 * c + k);
-      const int l = m + loff;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int ql = qg + 4 * i;
-        double2 v = make_double2(0.0, 0.0);
-        if (cols[i].op.op != OP_ZERO && loff < n_l && l <= cols[i].lc)
-          v = oz_operand(cols[i].op, cols[i].r, lm0, loff, l, m, cols[i].or2);
-        const int kw = deg_shift(l);  // x 2^k(l): the spectra divided by the degree weight
-        uint16_t d[kS];
-        digits7(fixed_from_double(v.x, kFix - sE[2 * ql] + kw), d);
-        store_digits(B, 2 * ql, k, d);
-        digits7(fixed_from_double(v.y, kFix - sE[2 * ql + 1] + kw), d);
-        store_digits(B, 2 * ql + 1, k, d);
+      for (int i = 0; i < 2; ++i) {
+        const int ql = qg + 8 * i;
+        double2 v[2];
+        int kw[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int loff = p + 2 * (64 * c + 2 * kp + h);
+          const int l = m + loff;
+          v[h] = make_double2(0.0, 0.0);
+          if (cols[i].op.op != OP_ZERO && loff < n_l && l <= cols[i].lc)
+            v[h] = oz_operand(cols[i].op, cols[i].r, lm0, loff, l, m, cols[i].or2);
+          kw[h] = deg_shift(l);  // x 2^k(l): the spectra divided by the degree weight
+        }
+        float d[2][kS];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) digits7f(fixed_from_double(v[h].x, kFix - sE[2 * ql] + kw[h]), d[h]);
+        store_digit_pairs(B, 2 * ql, 2 * kp, d);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) digits7f(fixed_from_double(v[h].y, kFix - sE[2 * ql + 1] + kw[h]), d[h]);
+        store_digit_pairs(B, 2 * ql + 1, 2 * kp, d);
       }
       tc::fence_proxy_async_smem();
       __syncthreads();
@@ -445,11 +477,11 @@ __global__ void __launch_bounds__(kPackThreads) pack_inv_oz(const ShtGeom g, con
 // half spectra of 16 complex columns over the nh colatitudes.  Exponents per
 // (ES | EA, real column): cexp[mc][2][nct * kNC]; tiles [mc][chunk][ct][ES|EA].
 template <bool VEC>
-__global__ void __launch_bounds__(kPackThreads) pack_fwd_oz(const ShtGeom g, const FwdSet s, const TcTables t,
+__global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_oz(const ShtGeom g, const FwdSet s, const TcTables t,
                                                             unsigned char* __restrict__ bimg, short* __restrict__ cexp,
                                                             int nct) {
   extern __shared__ unsigned char smem_raw[];
-  // one (ES, EA) tile pair (56 KB): four CTAs per SM; the next chunk waits for
+  // one (ES, EA) tile pair (56 KB): three CTAs per SM; the next chunk waits for
   // the bulk store of the previous one (two pairs measured 1 CTA per SM, 1.8 ms)
   unsigned char* buf = align1k(smem_raw);
   __shared__ int sE[2][kNC];
@@ -468,12 +500,25 @@ __global__ void __launch_bounds__(kPackThreads) pack_fwd_oz(const ShtGeom g, con
     const dfl2* src = src_of(ct * (kNC / 2) + ql);
     float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
     if (src)
-      for (int j = li; j < g.nh; j += 16) {
-        const dfl2 es = src[2 * j], ea = src[2 * j + 1];
-        m0 = fmaxf(m0, fabsf(es.x.h));
-        m1 = fmaxf(m1, fabsf(es.y.h));
-        m2 = fmaxf(m2, fabsf(ea.x.h));
-        m3 = fmaxf(m3, fabsf(ea.y.h));
+      for (int j0 = li; j0 < g.nh; j0 += 16 * 4) {
+        dfl2 es[4], ea[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = j0 + 16 * u;
+          es[u] = {dfl(0), dfl(0)};
+          ea[u] = es[u];
+          if (j < g.nh) {
+            es[u] = src[2 * j];
+            ea[u] = src[2 * j + 1];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          m0 = fmaxf(m0, fabsf(es[u].x.h));
+          m1 = fmaxf(m1, fabsf(es[u].y.h));
+          m2 = fmaxf(m2, fabsf(ea[u].x.h));
+          m3 = fmaxf(m3, fabsf(ea[u].y.h));
+        }
       }
 #pragma unroll
     for (int d = 8; d >= 1; d >>= 1) {
@@ -496,33 +541,42 @@ __global__ void __launch_bounds__(kPackThreads) pack_fwd_oz(const ShtGeom g, con
     }
   }
   __syncthreads();
-  const int k = tid & 63, qg = tid >> 6;
-  const dfl2* srcs[4];
+  // pass 2: thread = (colatitudes 2 kp, 2 kp + 1 of the chunk, column group qg)
+  const int kp = tid & 31, qg = tid >> 5;
+  const dfl2* srcs[2];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) srcs[i] = src_of(ct * (kNC / 2) + qg + 4 * i);
+  for (int i = 0; i < 2; ++i) srcs[i] = src_of(ct * (kNC / 2) + qg + 8 * i);
   for (int c = 0; c < t.ncj; ++c) {
     unsigned char* B = buf;
     if (c >= 1) {
       if (tid == 0) tc::bulk_wait_read<0>();
       __syncthreads();
     }
-    const int j = 64 * c + k;
+    const int j0 = 64 * c + 2 * kp;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int ql = qg + 4 * i;
-      dfl2 es = {dfl(0), dfl(0)}, ea = es;
-      if (srcs[i] && j < g.nh) {
-        es = srcs[i][2 * j];
-        ea = srcs[i][2 * j + 1];
+    for (int i = 0; i < 2; ++i) {
+      const int ql = qg + 8 * i;
+      dfl2 es[2], ea[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        es[h] = {dfl(0), dfl(0)};
+        ea[h] = es[h];
+        if (srcs[i] && j0 + h < g.nh) {
+          es[h] = srcs[i][2 * (j0 + h)];
+          ea[h] = srcs[i][2 * (j0 + h) + 1];
+        }
       }
-      const dfl v[4] = {es.x, es.y, ea.x, ea.y};
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const int which = w >> 1, row = 2 * ql + (w & 1);
         const int sh = kFix - sE[which][row];
-        uint16_t d[kS];
-        digits7(fixed_from_float(v[w].h, sh) + fixed_from_float(v[w].l, sh), d);
-        store_digits(B + which * kTS, row, k, d);
+        float d[2][kS];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const dfl v = w == 0 ? es[h].x : w == 1 ? es[h].y : w == 2 ? ea[h].x : ea[h].y;
+          digits7f(fixed_from_float(v.h, sh) + fixed_from_float(v.l, sh), d[h]);
+        }
+        store_digit_pairs(B + which * kTS, row, 2 * kp, d);
       }
     }
     tc::fence_proxy_async_smem();
