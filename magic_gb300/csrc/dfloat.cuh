@@ -74,35 +74,40 @@ __device__ __forceinline__ dfl& operator*=(dfl& a, dfl b) { return a = a * b; }
 // exact scaling by a power of two
 __device__ __forceinline__ dfl df_ldexp(dfl a, int e) { return mkdf(ldexpf(a.h, e), ldexpf(a.l, e)); }
 
-// FP64 <-> double-float with integer instructions and one FP64 add (the
-// FP64 pipe of GB300 is narrow): hi = x rounded to FP32, lo = (x - hi)
-// rounded to FP32; back: hi + lo rounded to FP64.
-__device__ __forceinline__ float d2f_rn_int(double x);
+// FP64 <-> double-float with integer instructions (the FP64 pipe of GB300
+// is narrow).  From FP64: the 53-bit mantissa is T 2^29 + R with T its top
+// 24 bits; hi = T rounded to nearest even (T + 1 and R - 2^29 when rounding
+// up), lo = R 2^(e-1075) rounded to FP32 by one integer -> float conversion
+// and moved to its exponent by an integer add (lo = RN(x - hi), |R| <= 2^28).
+// Below 2^-126 hi (and lo) are signed zeros, a lo below 2^-126 is zero; above
+// the FP32 range hi is Inf (NaN for NaN) and lo zero.  Back: hi + lo rounded
+// to FP64 (one FP64 add).
 __device__ __forceinline__ double f2d_exact_int(float x);
 __device__ __forceinline__ dfl df_from_double(double x) {
-  const float h = d2f_rn_int(x);
-  return mkdf(h, d2f_rn_int(x - f2d_exact_int(h)));
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int whi = (unsigned int)(b >> 32), wlo = (unsigned int)b;
+  const unsigned int sign = whi & 0x80000000u;
+  const int e = (int)((whi >> 20) & 0x7FF);
+  if (e < 1023 - 126) return mkdf(__uint_as_float(sign), __uint_as_float(sign));
+  if (e > 1023 + 127) {
+    const bool nan = e == 0x7FF && ((whi & 0xFFFFFu) | wlo) != 0u;
+    return mkdf(__uint_as_float(sign | 0x7F800000u | (nan ? 0x400000u : 0u)), 0.f);
+  }
+  unsigned int T = 0x800000u | ((whi & 0xFFFFFu) << 3) | (wlo >> 29);
+  int R = (int)(wlo & 0x1FFFFFFFu);
+  const bool up = R > 0x10000000 || (R == 0x10000000 && (T & 1u));
+  T += up ? 1u : 0u;
+  R -= up ? 0x20000000 : 0;
+  // T = 2^24 after rounding carries into the exponent field (Inf past the range)
+  const unsigned int hb = sign | (((unsigned int)(e - 1023 + 127) << 23) + (T - 0x800000u));
+  const float rf = __int2float_rn(sign ? -R : R);
+  unsigned int lb = __float_as_uint(rf);
+  const int sh = e - 1075;
+  lb = (rf != 0.f && (int)((lb >> 23) & 0xFFu) + sh > 0) ? lb + ((unsigned int)sh << 23) : (lb & 0x80000000u);
+  return mkdf(__uint_as_float(hb), __uint_as_float(lb));
 }
 __device__ __forceinline__ double df_to_double(dfl a) { return f2d_exact_int(a.h) + f2d_exact_int(a.l); }
 
-// round to nearest even; below 2^-126 -> signed zero; overflow -> Inf
-__device__ __forceinline__ float d2f_rn_int(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned int hi = (unsigned int)(b >> 32), lo = (unsigned int)b;
-  const int e = (int)((hi >> 20) & 0x7FF);
-  const unsigned int sign = hi & 0x80000000u;
-  if (e < 1023 - 126) return __uint_as_float(sign);
-  const unsigned int mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-  if (e > 1023 + 127) {
-    const bool nan = e == 0x7FF && ((hi & 0xFFFFFu) | lo) != 0u;
-    return __uint_as_float(sign | 0x7F800000u | (nan ? 0x400000u : 0u));
-  }
-  unsigned int f = sign | ((unsigned int)(e - 1023 + 127) << 23) | mant;
-  const unsigned int rbit = (lo >> 28) & 1u;
-  const unsigned int sticky = (lo & 0x0FFFFFFFu) != 0u;
-  if (rbit && (sticky || (mant & 1u))) f += 1u;
-  return __uint_as_float(f);
-}
 // exact for normal numbers, zero, Inf and NaN (FP32 subnormals flush to zero)
 __device__ __forceinline__ double f2d_exact_int(float x) {
   const unsigned int u = __float_as_uint(x);
