@@ -222,11 +222,13 @@ __device__ __forceinline__ bool ring_pop(const TileRing& R, uint32_t& use, int& 
   return true;
 }
 
-// MMAs of table digit u against the stacked data digits: K = 16 per MMA, 4 per
-// 64-wide chunk; table tb's accumulators at acc + tb * kS * kNC.
+// MMAs of table digit u against the stacked data digits: K = 16 per MMA, the
+// first nks (<= 4) of a 64-wide chunk (the K rows past a synthesis order's
+// degrees are zero in both operands and are skipped); table tb's
+// accumulators at acc + tb * kS * kNC.
 template <int NT>
 __device__ __forceinline__ void issue_digit(uint32_t acc, const unsigned char* A, const unsigned char* B, int u,
-                                            bool first_chunk, uint32_t bstride_tb) {
+                                            bool first_chunk, uint32_t bstride_tb, int nks = 4) {
   const uint64_t a0 = tc::sw128_desc(tc::smem_u32(A));
   const uint64_t b0 = tc::sw128_desc(tc::smem_u32(B));
   const uint32_t idesc = tc::idesc_bf16(128, (kS - u) * kNC);
@@ -234,12 +236,20 @@ __device__ __forceinline__ void issue_digit(uint32_t acc, const unsigned char* A
   for (int ks = 0; ks < 4; ++ks)
 #pragma unroll
     for (int tb = 0; tb < NT; ++tb) {
+      if (ks >= nks) continue;
       const uint32_t d = acc + (uint32_t)((tb * kS + u) * kNC);
       const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
       const uint64_t bd = b0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
       tc::mma_bf16(d, ad, bd, idesc, (u != 0 || !first_chunk || ks) ? 1u : 0u);
     }
 }
+
+// Bytes of a 128-row table block that hold its first `rows` rows (8-row
+// groups of 1 KB in the 128-byte-swizzled layout).  The rows past a block's
+// colatitudes (synthesis) or degrees (analysis) are zero and are not loaded:
+// the MMA reads whatever the ring slot held there into accumulator rows that
+// the epilogue does not store.
+__device__ __forceinline__ uint32_t table_rows_bytes(int rows) { return (uint32_t)((min(rows, 128) + 7) >> 3) << 10; }
 
 template <typename P>
 __device__ __forceinline__ P* shfl_ptr(P* p, int src) {
@@ -684,14 +694,15 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_oz(const ShtG
           tc::bulk_g2s(sB + bslot * kTS, bimg + ((t.bpc0[T.mc] + T.p * T.nch + c) * nct + T.ct) * (long long)kTS,
                        kTS, &b_full[bslot]);
           ++b_use;
+          const uint32_t abytes = table_rows_bytes(g.nh - T.tt * 128);
           for (int u = 0; u < kS; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_empty(&a_empty[slot], a_use, NA)) { ok = false; break; }
-            tc::mbar_expect_tx(&a_full[slot], ASZ);
+            tc::mbar_expect_tx(&a_full[slot], NT * abytes);
             for (int tb = 0; tb < NT; ++tb) {
               const long long blk =
                   t.inv_blk0[T.mc] + ((((long long)T.tt * 2 + tb) * 2 + T.p) * T.nch + c) * kS + u;
-              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.inv_img + blk * 16384, 16384, &a_full[slot]);
+              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.inv_img + blk * 16384, abytes, &a_full[slot]);
             }
           }
         }
@@ -713,11 +724,12 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_oz(const ShtG
         for (int c = 0; c < T.nchp && ok; ++c, ++b_use) {
           const uint32_t bslot = b_use % NB;
           if (!wait_full(&b_full[bslot], b_use, NB)) { ok = false; break; }
+          const int nks = min(4, (T.nlp - 64 * c + 15) >> 4);  // K steps holding degrees of the order
           for (int u = 0; u < kS; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_digit<NT>(tmem, sA + slot * ASZ, sB + bslot * kTS, u, c == 0, 0);
+            issue_digit<NT>(tmem, sA + slot * ASZ, sB + bslot * kTS, u, c == 0, 0, nks);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -923,14 +935,15 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_oz(const ShtG
           tc::bulk_g2s(sB + bslot * BSZ, img + T.p * kTS, kTS, &b_full[bslot]);                     // mine
           if (VEC) tc::bulk_g2s(sB + bslot * BSZ + kTS, img + (1 - T.p) * kTS, kTS, &b_full[bslot]);  // other
           ++b_use;
+          const uint32_t abytes = table_rows_bytes(T.nlp - T.lt * 128);
           for (int u = 0; u < kS; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_empty(&a_empty[slot], a_use, NA)) { ok = false; break; }
-            tc::mbar_expect_tx(&a_full[slot], ASZ);
+            tc::mbar_expect_tx(&a_full[slot], NT * abytes);
             for (int tb = 0; tb < NT; ++tb) {
               const long long blk =
                   t.fwd_blk0[T.mc] + ((((long long)T.p * t.nlt + T.lt) * 2 + tb) * t.ncj + c) * kS + u;
-              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.fwd_img + blk * 16384, 16384, &a_full[slot]);
+              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.fwd_img + blk * 16384, abytes, &a_full[slot]);
             }
           }
         }

@@ -139,9 +139,12 @@ __device__ __forceinline__ bool ring_pop(const TileRing& R, uint32_t& use, int& 
 //                     -> [C1|C2],  A_lo x B_hi -> C2   (K = 16 per MMA, 4 per tile)
 //  tf32 (u = 2*K tile + split):  A_hi x [B_hi|B_lo] -> [C0|C1],  A_lo x B_hi -> C1
 //                     (K = 8 per MMA, 4 per 32-wide K tile)
+// nk: K rows of the chunk that hold degrees of the order (synthesis; 64 in
+// the analysis): K steps past them multiply zero rows and are skipped.
 template <int NT, bool TF32>
 __device__ __forceinline__ void issue_use(uint32_t acc, const unsigned char* A, const unsigned char* B,
-                                          int u, bool first_chunk, uint32_t bstride_tb, int tb0, int tb1) {
+                                          int u, bool first_chunk, uint32_t bstride_tb, int tb0, int tb1,
+                                          int nk = 64) {
   constexpr int NACCS = Form<TF32>::NACCS;
   const uint64_t a0 = tc::sw128_desc(tc::smem_u32(A));
   const uint64_t bd0 = tc::sw128_desc(tc::smem_u32(B));
@@ -153,6 +156,7 @@ __device__ __forceinline__ void issue_use(uint32_t acc, const unsigned char* A, 
 #pragma unroll
       for (int tb = 0; tb < NT; ++tb) {
         if (tb < tb0 || tb >= tb1) continue;  // tables of the other MMA thread
+        if (16 * ks >= nk) continue;
         const uint32_t d = acc + (uint32_t)(tb * NACCS * kNC);
         const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
         const uint64_t bd = bd0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
@@ -168,6 +172,7 @@ __device__ __forceinline__ void issue_use(uint32_t acc, const unsigned char* A, 
 #pragma unroll
       for (int tb = 0; tb < NT; ++tb) {
         if (tb < tb0 || tb >= tb1) continue;  // tables of the other MMA thread
+        if (32 * kt + 8 * ks >= nk) continue;
         const uint32_t d = acc + (uint32_t)(tb * NACCS * kNC);
         const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
         const uint64_t bd = bd0 + (uint64_t)((tb * bstride_tb + kt * 2 * kNC * 128 + ks * 32) >> 4);
@@ -178,6 +183,13 @@ __device__ __forceinline__ void issue_use(uint32_t acc, const unsigned char* A, 
 }
 
 // Pointer held by lane `src` (whole warp participates).
+// Bytes of a 128-row table block that hold its first `rows` rows (8-row
+// groups of 1 KB in the 128-byte-swizzled layout).  The rows past a block's
+// colatitudes (synthesis) or degrees (analysis) are zero and are not loaded:
+// the MMA reads whatever the ring slot held there into accumulator rows that
+// the epilogue does not store.
+__device__ __forceinline__ uint32_t table_rows_bytes(int rows) { return (uint32_t)((min(rows, 128) + 7) >> 3) << 10; }
+
 template <typename P>
 __device__ __forceinline__ P* shfl_ptr(P* p, int src) {
   const unsigned long long v = (unsigned long long)p;
@@ -359,12 +371,13 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
           for (int u = 0; u < F::AUSES; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_empty(&a_empty[slot], a_use, NA)) { ok = false; break; }
-            tc::mbar_expect_tx(&a_full[slot], ASZ);
+            const uint32_t abytes = table_rows_bytes(g.nh - T.tt * 128);
+            tc::mbar_expect_tx(&a_full[slot], NT * abytes);
             const int blk_u = TF32 ? 2 * (u & 1) + (u >> 1) : u;  // tf32 blocks: 2 * split + K tile
             for (int tb = 0; tb < NT; ++tb) {
               const long long blk =
                   t.inv_blk0[T.mc] + ((((long long)T.tt * 2 + tb) * 2 + T.p) * T.nch + c) * F::BPC + blk_u;
-              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.inv_img + blk * 16384, 16384, &a_full[slot]);
+              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.inv_img + blk * 16384, abytes, &a_full[slot]);
             }
           }
         }
@@ -390,11 +403,12 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
         for (int c = 0; c < T.nchp && ok; ++c, ++b_use) {
           const uint32_t bslot = b_use % NB;
           if (!wait_full(&b_full[bslot], b_use, NB)) { ok = false; break; }
+          const int nk = min(64, T.nlp - 64 * c);  // K rows holding degrees of the order
           for (int u = 0; u < F::AUSES; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_use<NT, TF32>(acc, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, 0, tb0, tb1);
+            issue_use<NT, TF32>(acc, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, 0, tb0, tb1, nk);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -596,12 +610,13 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
           for (int u = 0; u < F::AUSES; ++u, ++a_use) {
             const uint32_t slot = a_use % NA;
             if (!wait_empty(&a_empty[slot], a_use, NA)) { ok = false; break; }
-            tc::mbar_expect_tx(&a_full[slot], ASZ);
+            const uint32_t abytes = table_rows_bytes(T.nlp - T.lt * 128);
+            tc::mbar_expect_tx(&a_full[slot], NT * abytes);
             const int blk_u = TF32 ? 2 * (u & 1) + (u >> 1) : u;
             for (int tb = 0; tb < NT; ++tb) {
               const long long blk =
                   t.fwd_blk0[T.mc] + ((((long long)T.p * t.nlt + T.lt) * 2 + tb) * t.ncj + c) * F::BPC + blk_u;
-              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.fwd_img + blk * 16384, 16384, &a_full[slot]);
+              tc::bulk_g2s(sA + slot * ASZ + tb * 16384, t.fwd_img + blk * 16384, abytes, &a_full[slot]);
             }
           }
         }
