@@ -228,7 +228,7 @@ __device__ __forceinline__ bool ring_pop(const TileRing& R, uint32_t& use, int& 
 // accumulators at acc + tb * kS * kNC.
 template <int NT>
 __device__ __forceinline__ void issue_digit(uint32_t acc, const unsigned char* A, const unsigned char* B, int u,
-                                            bool first_chunk, uint32_t bstride_tb, int nks = 4) {
+                                            bool first_chunk, uint32_t bstride_tb, int nks, int tb0, int tb1) {
   const uint64_t a0 = tc::sw128_desc(tc::smem_u32(A));
   const uint64_t b0 = tc::sw128_desc(tc::smem_u32(B));
   const uint32_t idesc = tc::idesc_bf16(128, (kS - u) * kNC);
@@ -236,7 +236,7 @@ __device__ __forceinline__ void issue_digit(uint32_t acc, const unsigned char* A
   for (int ks = 0; ks < 4; ++ks)
 #pragma unroll
     for (int tb = 0; tb < NT; ++tb) {
-      if (ks >= nks) continue;
+      if (ks >= nks || tb < tb0 || tb >= tb1) continue;  // tb0..tb1-1: this MMA thread's tables
       const uint32_t d = acc + (uint32_t)((tb * kS + u) * kNC);
       const uint64_t ad = a0 + (uint64_t)((tb * 16384 + ks * 32) >> 4);
       const uint64_t bd = b0 + (uint64_t)((tb * bstride_tb + ks * 32) >> 4);
@@ -260,13 +260,19 @@ __device__ __forceinline__ P* shfl_ptr(P* p, int src) {
 }
 
 // CTAs per SM and TMEM columns: one table (224 accumulator columns) two
-// CTAs per SM with 256 columns each; two tables (448) one CTA with 512.
-template <bool VEC>
+// CTAs per SM with 256 columns each; two tables (448) one CTA with 512.  MMA
+// threads: one per CTA, but one per table in the two-table analysis (warps 1
+// and 10; 4% faster there, 13% slower in the synthesis, whose two tables
+// share the data tiles).
+template <bool VEC, bool INV>
 struct Occ {
   static constexpr int CPS = VEC ? 1 : 2;
   static constexpr int TCOLS = VEC ? 512 : 256;
+  static constexpr int NISS = (VEC && !INV) ? 2 : 1;
+  static constexpr int THREADS = kThreads + 32 * (NISS - 1);
 };
-// ring depths: A = one table digit of one K chunk (NT x 16 KB), B = data tiles
+// ring depths: A = one table digit of one K chunk (NT x 16 KB), B = data
+// tiles (a fifth table slot for the two-table kernels measured no faster)
 template <bool VEC, bool INV>
 struct Rings {
   static constexpr int NA = VEC ? (INV ? 4 : 3) : 3;
@@ -634,7 +640,7 @@ __device__ __forceinline__ float pow2f(int e) {
 }
 
 template <bool VEC>
-__global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_oz(const ShtGeom g, const InvSet s,
+__global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS) inv_leg_oz(const ShtGeom g, const InvSet s,
                                                                       const TcTables t,
                                                                       const unsigned char* __restrict__ bimg,
                                                                       const short* __restrict__ cexp, int nct) {
@@ -655,17 +661,18 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_oz(const ShtG
   const int ntiles = nct * t.ntt * 2 * g.n_m;
 
   if (tid == 0) {
-    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], 1); }
-    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
-    tc::mbar_init(&acc_full, 1);
+    constexpr int NI = Occ<VEC, true>::NISS;  // every MMA thread commits to the empty / full barriers
+    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], NI); }
+    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], NI); }
+    tc::mbar_init(&acc_full, NI);
     tc::mbar_init(&acc_empty, kEpiThreads);
-    tc::mbar_init(&fin, 1);
-    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], 1 + kEpiThreads); }
+    tc::mbar_init(&fin, NI);
+    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], NI + kEpiThreads); }
     s_fail = 0;
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(&tmem_base, Occ<VEC>::TCOLS);
+    tc::tmem_alloc(&tmem_base, Occ<VEC, true>::TCOLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
@@ -710,8 +717,9 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_oz(const ShtG
       drain_copies<NA>(a_full, a_use);
       drain_copies<NB>(b_full, b_use);
     }
-  } else if (warp == 1) {
-    if (lane == 0) {  // ---------------------------------------- MMA issuer
+  } else if (warp == 1 || (Occ<VEC, true>::NISS == 2 && warp == 2 + kEpiThreads / 32)) {
+    if (lane == 0) {  // ---------------------------------------- MMA issuer(s)
+      const int tb0 = warp == 1 ? 0 : 1, tb1 = Occ<VEC, true>::NISS == 2 ? tb0 + 1 : NT;
       uint32_t a_use = 0, b_use = 0, acc_use = 0, tr = 0;
       while (ok) {
         int ix;
@@ -729,7 +737,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_oz(const ShtG
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_digit<NT>(tmem, sA + slot * ASZ, sB + bslot * kTS, u, c == 0, 0, nks);
+            issue_digit<NT>(tmem, sA + slot * ASZ, sB + bslot * kTS, u, c == 0, 0, nks, tb0, tb1);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -740,7 +748,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_oz(const ShtG
       tc::mma_commit(&fin);
       if (!tc::mbar_wait(&fin, 0)) ok = false;
     }
-  } else {  // ---------------------------------------------------- epilogue
+  } else if (warp < 2 + kEpiThreads / 32) {  // ------------------ epilogue
     const int q4 = warp & 3, half = (warp - 2) >> 2;
     const int cc0 = half * (kNC / 2);  // this warp's 16 real columns
     const int jl = 32 * q4 + lane;
@@ -846,7 +854,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) inv_leg_oz(const ShtG
   tc::tc_fence_before();
   __syncthreads();
   if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
-  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC>::TCOLS);
+  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC, true>::TCOLS);
 }
 
 // ------------------------------------------------------------ analysis
@@ -873,7 +881,7 @@ struct FwdTile {
 };
 
 template <bool VEC>
-__global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_oz(const ShtGeom g, const FwdSet s,
+__global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS) fwd_leg_oz(const ShtGeom g, const FwdSet s,
                                                                       const TcTables t,
                                                                       const unsigned char* __restrict__ bimg,
                                                                       const short* __restrict__ cexp, int nct) {
@@ -895,17 +903,18 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_oz(const ShtG
   const int ntiles = nct * t.nlt * 2 * g.n_m;
 
   if (tid == 0) {
-    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], 1); }
-    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], 1); }
-    tc::mbar_init(&acc_full, 1);
+    constexpr int NI = Occ<VEC, false>::NISS;  // every MMA thread commits to the empty / full barriers
+    for (int i = 0; i < NA; ++i) { tc::mbar_init(&a_full[i], 1); tc::mbar_init(&a_empty[i], NI); }
+    for (int i = 0; i < NB; ++i) { tc::mbar_init(&b_full[i], 1); tc::mbar_init(&b_empty[i], NI); }
+    tc::mbar_init(&acc_full, NI);
     tc::mbar_init(&acc_empty, kEpiThreads);
-    tc::mbar_init(&fin, 1);
-    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], 1 + kEpiThreads); }
+    tc::mbar_init(&fin, NI);
+    for (int i = 0; i < kNTR; ++i) { tc::mbar_init(&tr_full[i], 1); tc::mbar_init(&tr_empty[i], NI + kEpiThreads); }
     s_fail = 0;
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(&tmem_base, Occ<VEC>::TCOLS);
+    tc::tmem_alloc(&tmem_base, Occ<VEC, false>::TCOLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
@@ -951,8 +960,9 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_oz(const ShtG
       drain_copies<NA>(a_full, a_use);
       drain_copies<NB>(b_full, b_use);
     }
-  } else if (warp == 1) {
-    if (lane == 0) {
+  } else if (warp == 1 || (Occ<VEC, false>::NISS == 2 && warp == 2 + kEpiThreads / 32)) {
+    if (lane == 0) {  // MMA issuer(s)
+      const int tb0 = warp == 1 ? 0 : 1, tb1 = Occ<VEC, false>::NISS == 2 ? tb0 + 1 : NT;
       uint32_t a_use = 0, b_use = 0, acc_use = 0, tr = 0;
       while (ok) {
         int ix;
@@ -969,7 +979,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_oz(const ShtG
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_digit<NT>(tmem, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, kTS);
+            issue_digit<NT>(tmem, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, kTS, 4, tb0, tb1);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -980,7 +990,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_oz(const ShtG
       tc::mma_commit(&fin);
       if (!tc::mbar_wait(&fin, 0)) ok = false;
     }
-  } else {  // epilogue
+  } else if (warp < 2 + kEpiThreads / 32) {  // epilogue
     const int q4 = warp & 3, half = (warp - 2) >> 2;
     const int cc0 = half * (kNC / 2);
     const int lr = 32 * q4 + lane;
@@ -1068,7 +1078,7 @@ __global__ void __launch_bounds__(kThreads, Occ<VEC>::CPS) fwd_leg_oz(const ShtG
   tc::tc_fence_before();
   __syncthreads();
   if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
-  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC>::TCOLS);
+  if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC, false>::TCOLS);
 }
 
 size_t align256_oz(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -1105,9 +1115,9 @@ cudaError_t launch_inv_oz(const ShtGeom& g, const InvSet& s, const TcTables& t, 
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * kTS;
   CUDA_TRY(cudaFuncSetAttribute(inv_leg_oz<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
-  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC>::CPS);
+  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC, true>::CPS);
   CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  inv_leg_oz<VEC><<<grid, kThreads, smem, st>>>(g, s, t, bimg, cexp, nct);
+  inv_leg_oz<VEC><<<grid, Occ<VEC, true>::THREADS, smem, st>>>(g, s, t, bimg, cexp, nct);
   return cudaGetLastError();
 }
 
@@ -1126,9 +1136,9 @@ cudaError_t launch_fwd_oz(const ShtGeom& g, const FwdSet& s, const TcTables& t, 
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * kTS;
   CUDA_TRY(cudaFuncSetAttribute(fwd_leg_oz<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
-  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC>::CPS);
+  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC, false>::CPS);
   CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  fwd_leg_oz<VEC><<<grid, kThreads, smem, st>>>(g, s, t, bimg, cexp, nct);
+  fwd_leg_oz<VEC><<<grid, Occ<VEC, false>::THREADS, smem, st>>>(g, s, t, bimg, cexp, nct);
   return cudaGetLastError();
 }
 
