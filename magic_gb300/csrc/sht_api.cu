@@ -187,6 +187,18 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// page-locked host memory (cudaHostAlloc / cudaHostRegister): asynchronous copies from it do not block the host
+bool is_pinned_host(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 bool fp64_pipes(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_FP64; }
 // the FP64-accurate tensor-core form: Legendre sums of fixed-point BF16 digits
 // (or, with tc_kernel = 1, the FP64 SIMT sums) and double-float FFTs
@@ -1288,6 +1300,16 @@ struct PipeArray {
 
 static int pipelined_levels(magic_sht_handle* h, int n, int chunk, std::vector<PipeArray>& arrs,
                             const std::function<int(int, int, const std::vector<char*>&)>& compute) {
+  // A copy from pageable memory returns only once the copy stream has reached
+  // it, which would hold the host at every chunk: small pageable inputs (the
+  // per-level radii, or2, lcut) are staged once in the pinned ring and copied
+  // from there.
+  for (auto& a : arrs) {
+    if (a.out) continue;
+    const size_t all = (size_t)(n - 1) * a.lds + a.last;
+    if (!is_pinned_host(a.host))
+      if (const void* pinned = pin_stage(h, a.host, all)) a.host = pinned;
+  }
   size_t slot = 0;
   for (auto& a : arrs) {
     a.slot_off = slot;
