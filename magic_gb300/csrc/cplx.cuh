@@ -15,6 +15,7 @@ template <> struct ScalarOf<dfl2> { typedef dfl t; };
 
 __device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
 __device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ dfl2 mk2(dfl a, dfl b) { dfl2 r; r.x = a; r.y = b; return r; }
 
 template <typename T2> __device__ __forceinline__ T2 zero2() {
   T2 z; z.x = 0; z.y = 0; return z;

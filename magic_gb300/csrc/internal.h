@@ -53,17 +53,17 @@ cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec,
 
 // nl.cu
 cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& out, const double* or2,
-                          double or2_0, int nlev, bool f32, cudaStream_t st);
+                          double or2_0, int nlev, int arith, cudaStream_t st);
 
 // the general get_nl with the reference's switches; cosn2[nh] = cos/sin^2 of the northern colatitudes
 cudaError_t build_cosn2(const ShtGeom& g, const double* theta, double* cosn2, cudaStream_t st);
-cudaError_t launch_get_nl_full(const ShtGeom& g, const NlFull& a, const double* cosn2, int nlev, bool f32,
+cudaError_t launch_get_nl_full(const ShtGeom& g, const NlFull& a, const double* cosn2, int nlev, int arith,
                                cudaStream_t st);
 
 // td.cu
-cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, bool f32, cudaStream_t st);
+cudaError_t launch_get_td(const ShtGeom& g, const TdArgs& a, int nlev, int arith, cudaStream_t st);
 cudaError_t build_td_coef(const ShtGeom& g, double2* coef, int* lq, cudaStream_t st);
-cudaError_t launch_get_td_full(const ShtGeom& g, const TdFull& a, int nlev, bool f32, cudaStream_t st);
+cudaError_t launch_get_td_full(const ShtGeom& g, const TdFull& a, int nlev, int arith, cudaStream_t st);
 // boundary pieces of the radial loop, one level (bcs.cu); theta = the n_theta
 // Gauss colatitudes north to south
 cudaError_t launch_v_rigid_boundary(const ShtGeom& g, const double* theta, const BcGrids& a, double r2rho0,

@@ -5,7 +5,9 @@
 // advection (l_adv_curl), magnetic field and heat equation on, unit physical
 // constants (LFfac = OhmLossFac = 1, otemp1 = lambda = 1); heatTerms holds the
 // ohmic-loss part (get_nl.f90:424-429).  Elementwise: FP64 arithmetic in the
-// FP64 form, FP32 arithmetic (FP64 grids in and out) in the reduced forms.
+// FP64 form, double-float arithmetic on the FP32 pipe in the FP64-accurate
+// form (about 2^-48 per operation), FP32 arithmetic in the reduced forms (FP64
+// grids in and out in all of them).
 #include <algorithm>
 #include "common.cuh"
 #include "cplx.cuh"
@@ -79,7 +81,7 @@ __global__ void __launch_bounds__(256) get_nl_kernel(const ShtGeom g, const NlGr
 }  // namespace
 
 cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& out, const double* or2,
-                          double or2_0, int nlev, bool f32, cudaStream_t st) {
+                          double or2_0, int nlev, int arith, cudaStream_t st) {
   const long long per_level = (long long)g.n_phi * (g.n_theta / 2);
   if (nlev <= 0 || per_level <= 0) return cudaSuccess;
   int dev = 0, nsm = 148;
@@ -89,7 +91,8 @@ cudaError_t launch_get_nl(const ShtGeom& g, const NlGrids& in, const NlGrids& ou
   for (int r0 = 0; r0 < nlev; r0 += 65535) {
     const int nl = std::min(nlev - r0, 65535);
     const int gx = std::max(1, std::min(need, (8 * nsm + nl - 1) / nl));  // about eight blocks per SM in all
-    if (f32) get_nl_kernel<float><<<dim3(gx, nl), 256, 0, st>>>(g, in, out, or2, or2_0, r0);
+    if (arith == FFT_ARITH_F32) get_nl_kernel<float><<<dim3(gx, nl), 256, 0, st>>>(g, in, out, or2, or2_0, r0);
+    else if (arith == FFT_ARITH_DF) get_nl_kernel<dfl><<<dim3(gx, nl), 256, 0, st>>>(g, in, out, or2, or2_0, r0);
     else get_nl_kernel<double><<<dim3(gx, nl), 256, 0, st>>>(g, in, out, or2, or2_0, r0);
     CUDA_TRY(cudaGetLastError());
   }
@@ -232,7 +235,7 @@ cudaError_t build_cosn2(const ShtGeom& g, const double* theta, double* cosn2, cu
   return cudaGetLastError();
 }
 
-cudaError_t launch_get_nl_full(const ShtGeom& g, const NlFull& a, const double* cosn2, int nlev, bool f32,
+cudaError_t launch_get_nl_full(const ShtGeom& g, const NlFull& a, const double* cosn2, int nlev, int arith,
                                cudaStream_t st) {
   const long long per_level = (long long)g.n_phi * (g.n_theta / 2);
   if (nlev <= 0 || per_level <= 0) return cudaSuccess;
@@ -243,7 +246,8 @@ cudaError_t launch_get_nl_full(const ShtGeom& g, const NlFull& a, const double* 
   for (int r0 = 0; r0 < nlev; r0 += 65535) {
     const int nl = std::min(nlev - r0, 65535);
     const int gx = std::max(1, std::min(need, (8 * nsm + nl - 1) / nl));
-    if (f32) get_nl_full_kernel<float><<<dim3(gx, nl), 256, 0, st>>>(g, a, cosn2, r0);
+    if (arith == FFT_ARITH_F32) get_nl_full_kernel<float><<<dim3(gx, nl), 256, 0, st>>>(g, a, cosn2, r0);
+    else if (arith == FFT_ARITH_DF) get_nl_full_kernel<dfl><<<dim3(gx, nl), 256, 0, st>>>(g, a, cosn2, r0);
     else get_nl_full_kernel<double><<<dim3(gx, nl), 256, 0, st>>>(g, a, cosn2, r0);
     CUDA_TRY(cudaGetLastError());
   }

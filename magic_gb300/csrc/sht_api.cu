@@ -1549,7 +1549,7 @@ int magic_sht_get_nl(magic_sht_handle* h, int n, const double* or2, const magic_
   TRY(cx.prepare());
   {
     PhaseScope sc(h, MAGIC_SHT_PHASE_NL);
-    CK(launch_get_nl(g, in, out, (const double*)cx.dev(i_or2), 1.0, n, !f64_sums(h), h->stream));
+    CK(launch_get_nl(g, in, out, (const double*)cx.dev(i_or2), 1.0, n, fft_arith(h), h->stream));
   }
   return cx.finish();
 }
@@ -1624,7 +1624,7 @@ int magic_sht_get_nl_opts(magic_sht_handle* h, int n, const magic_sht_nl_opts* o
   a.o.lcr = (const int*)cx.dev(i_lcr);
   {
     PhaseScope sc(h, MAGIC_SHT_PHASE_NL);
-    CK(launch_get_nl_full(g, a, h->d_cosn2, n, !f64_sums(h), h->stream));
+    CK(launch_get_nl_full(g, a, h->d_cosn2, n, fft_arith(h), h->stream));
   }
   return cx.finish();
 }
@@ -1691,7 +1691,7 @@ int magic_sht_get_td_opts(magic_sht_handle* h, int n, const magic_sht_td_opts* o
   t.o.nbc = (const int*)cx.dev(i_nbc);
   {
     PhaseScope sc(h, MAGIC_SHT_PHASE_TD);
-    CK(launch_get_td_full(g, t, n, !f64_sums(h), h->stream));
+    CK(launch_get_td_full(g, t, n, fft_arith(h), h->stream));
   }
   return cx.finish();
 }
@@ -1742,7 +1742,7 @@ int magic_sht_get_td_nbc(magic_sht_handle* h, int n, const double* r, const int*
   t.lq = h->d_tdlq;
   {
     PhaseScope sc(h, MAGIC_SHT_PHASE_TD);
-    CK(launch_get_td(g, t, n, !f64_sums(h), h->stream));
+    CK(launch_get_td(g, t, n, fft_arith(h), h->stream));
   }
   return cx.finish();
 }

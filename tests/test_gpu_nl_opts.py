@@ -6,7 +6,9 @@ u.grad u advection, the Lorentz force with and without the advection,
 entropy and composition advection, the induction in its bulk, stress-free
 (nBc = 1, low-conductivity region) and rigid (nBc = 2) forms, anelastic
 profiles, viscous heating and ohmic losses.  FP64 handle: <= 1e-13 relative
-L2 per output and level; the 3xBF16 handle computes in FP32: <= 1e-6.
+L2 per output and level; the FP64-accurate handle computes in double-float
+arithmetic (2^-48 per operation): <= 1e-12; the 3xBF16 handle computes in
+FP32: <= 1e-6.
 Outputs a level does not produce must keep the values they had."""
 import numpy as np
 import pytest
@@ -51,7 +53,7 @@ def _inputs():
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("bf16x3", 1e-6)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("fp64tc", 1e-12), ("bf16x3", 1e-6)])
 def test_get_nl_opts_matches_oracle(built, oracle_mod, torch, case, prec, tol):
     from magic_gb300 import SHT, _lib
     grids, r, prof = _inputs()

@@ -423,6 +423,28 @@ def test_get_nl_reduced_forms_compute_in_fp32(built, oracle_mod, torch, form):
 
 
 @pytest.mark.gpu
+def test_get_nl_fp64_accurate_form_computes_in_double_float(built, oracle_mod, torch):
+    """On an FP64-accurate handle get_nl computes in double-float arithmetic
+    on the FP32 pipe (FP64 grids in and out, about 2^-48 per operation):
+    every product within 1e-12 relative L2 of the FP64 restatement."""
+    from oracle import oracle as orc
+    from magic_gb300 import _lib
+    L, minc, N, P = 63, 1, 96, 192
+    n = 3
+    s = make(L, minc, N, P, prec="fp64tc")
+    rng = np.random.default_rng(5)
+    grids = {k: torch.from_numpy(rng.standard_normal((n, P, N))).cuda() for k in _lib.NL_IN}
+    or2 = np.array([1.0, 0.37, 2.5])
+    out = s.get_nl(grids, or2=or2)
+    torch.cuda.synchronize()
+    ref = orc.get_nl({k: v.cpu().numpy() for k, v in grids.items()}, or2, N)
+    for k in _lib.LM_SPACE_IN:
+        e = rel_l2(out[k].cpu().numpy(), ref[k])
+        assert e < 1e-12, (k, e)
+    s.close()
+
+
+@pytest.mark.gpu
 def test_radial_step_with_nonlinear_products(built, torch):
     """The radial-loop step of rIter.f90:94-464 on the GPU: synthesis set,
     get_nl on the FP64 grids, analysis set.  Each vector analysis

@@ -5,8 +5,8 @@ of dwdt (with dVxVhLM), the anelastic profiles, heatTermsLM and temp0 in
 dsdt, dxidt with epscXi, the switches off (advection, Coriolis force,
 induction), l_single_matrix, a cut-off degree l_R, and boundary levels where
 only dVxBhLM, dVxVhLM, dVSrLM and dVXirLM are written.  FP64 handle:
-<= 1e-13 relative L2 per output and level; 3xBF16 handle (FP32 arithmetic):
-<= 1e-6.  Entries the reference leaves as they were must keep their values."""
+<= 1e-13 relative L2 per output and level; FP64-accurate handle (FP64
+arithmetic as well): <= 1e-12; 3xBF16 handle (FP32 arithmetic): <= 1e-6.  Entries the reference leaves as they were must keep their values."""
 import numpy as np
 import pytest
 
@@ -40,7 +40,7 @@ def built():
 
 @pytest.mark.parametrize("L,minc,N,P", [(31, 1, 48, 96), (32, 2, 64, 64)])
 @pytest.mark.parametrize("case", sorted(CASES))
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("bf16x3", 1e-6)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("fp64tc", 1e-12), ("bf16x3", 1e-6)])
 def test_get_td_opts_matches_oracle(built, oracle_mod, torch, L, minc, N, P, case, prec, tol):
     from magic_gb300 import SHT, _lib
     from magic_gb300.workload import spectra
