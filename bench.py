@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--levels", type=int, default=N_LEVELS, help="radial levels (profiling cases)")
     ap.add_argument("--instances", action="store_true",
                     help="instead of the bench line: sixteen mixed-size instances in one graph (one JSON line)")
+    ap.add_argument("--group", action="store_true",
+                    help="with --instances: the sixteen instances as one group (magic_sht_group_*)")
     ap.add_argument("--only-reduced", action="store_true", help="skip the FP64 form (profiling)")
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations (C0, C1, C3, C4)")
     ap.add_argument("--stage-only", action="store_true",
@@ -871,26 +873,33 @@ def our_arm(args):
 
 def instances_measure(form, local, warmup, steps):
     """The sixteen-instance batching case (see instances_arm) in `form` and in
-    3xBF16, as a nested entry of the headline line."""
+    3xBF16, as a nested entry of the headline line: each as one group (one
+    pack + one persistent launch per direction and field kind over all sixteen
+    instances) and as the instances' own launches."""
     out = {}
     r = None
-    for f in (form, "bf16x3"):
-        r = instances_run(f, local, warmup, steps)
-        out[f] = {k: r[k] for k in ("value", "unit", "ms_per_step", "levels_per_step")}
+    runs = [(form, True), (form, False), ("bf16x3", True), ("bf16x3", False)]
+    for f, grp in runs:
+        r = instances_run(f, local, warmup, steps, group=grp)
+        out[f + ("_group" if grp else "")] = {k: r[k] for k in ("value", "unit", "ms_per_step", "levels_per_step",
+                                                                  "gpu_launches_per_step")}
     out["instances"] = r["instances"]
-    out["what"] = "sixteen mixed-size instances, both transform sets, captured in one CUDA graph"
+    out["what"] = ("sixteen mixed-size instances, both transform sets, captured in one CUDA graph: "
+                   "<form>_group = one pack + one persistent tensor-core launch per direction and field kind "
+                   "over every instance (magic_sht_group_*), <form> = each instance's own launches")
     return out
 
 
-def instances_run(form, local, warmup, steps):
+def instances_run(form, local, warmup, steps, group=False):
     """Sixteen independent instances of mixed size (l_max in {63, 127, 255},
     minc in {1, 4}, {33, 65, 129} radial levels, n_theta = 3(l_max+1)/2,
     n_phi = 2 n_theta / minc; a fixed seeded list), both transform sets of every
     instance captured into one CUDA graph on one stream and replayed.  The
-    analysis inputs are the instance's synthesis grids."""
+    analysis inputs are the instance's synthesis grids.  group: the instances'
+    Legendre sums as one launch per direction and field kind (SHTGroup)."""
     import numpy as np
     import torch
-    from magic_gb300 import SHT
+    from magic_gb300 import SHT, SHTGroup
     from magic_gb300.workload import grid_space_inputs, or2_levels, FORWARD_FROM_INVERSE
     rng = np.random.default_rng(1234)
     insts, desc = [], []
@@ -910,17 +919,32 @@ def instances_run(form, local, warmup, steps):
         desc.append({"l_max": L, "minc": minc, "n_theta": N, "n_phi": P, "levels": R})
     torch.cuda.synchronize()
     side = torch.cuda.Stream()
+    grp = None
     with torch.cuda.stream(side):
         for s, *_ in insts:
             s.set_stream(side.cuda_stream)
+        if group:
+            grp = SHTGroup([i[0] for i in insts])
+            args = ([i[1] for i in insts], [i[2] for i in insts], [i[3] for i in insts],
+                    [i[4] for i in insts], [i[5] for i in insts])
+
+            def step():
+                grp.transform_to_grid_space(args[0], or2s=args[1], outs=args[2])
+                grp.transform_to_lm_space(args[3], outs=args[4])
+        else:
+            def step():
+                for s, spec, or2, g, fin, lm, _ in insts:
+                    s.transform_to_grid_space(spec, or2=or2, out=g)
+                    s.transform_to_lm_space(fin, out=lm)
+        step()  # sizes the workspaces (and uploads the group's instance tables)
         side.synchronize()
+        n0 = sum(i[0].launch_count() for i in insts)
         insts[0][0].graph_begin()
         try:
-            for s, spec, or2, g, fin, lm, _ in insts:
-                s.transform_to_grid_space(spec, or2=or2, out=g)
-                s.transform_to_lm_space(fin, out=lm)
+            step()
         finally:
             gr = insts[0][0].graph_end()
+        launches = sum(i[0].launch_count() for i in insts) - n0
         for _ in range(max(warmup, 3)):
             insts[0][0].graph_launch(gr)
         side.synchronize()
@@ -935,6 +959,8 @@ def instances_run(form, local, warmup, steps):
         s.device_status()
     insts[0][0].graph_destroy(gr)
     levels = sum(d["levels"] for d in desc)
+    if grp is not None:
+        grp.close()
     for s, *_ in insts:
         s.close()
     del insts
@@ -942,7 +968,8 @@ def instances_run(form, local, warmup, steps):
     return {"metric": "SHT radial levels/s, sixteen mixed instances in one graph",
             "value": levels * steps / (ms * 1e-3), "unit": "levels/s", "n_gpus": 1,
             "steps": steps, "warmup": max(warmup, 3), "ms_per_step": ms / steps,
-            "higher_is_better": True, "form": form, "levels_per_step": levels,
+            "higher_is_better": True, "form": form, "group": group, "levels_per_step": levels,
+            "gpu_launches_per_step": launches,
             "timing": "graph replay, CUDA events on the replay stream", "instances": desc}
 
 
@@ -956,7 +983,7 @@ def instances_arm(args):
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
     form = "bf16x3" if args.form == "auto" else args.form
-    r = instances_run(form, local, args.warmup, args.steps)
+    r = instances_run(form, local, args.warmup, args.steps, group=args.group)
     if rank == 0:
         print(json.dumps(r), flush=True)
 

@@ -405,6 +405,36 @@ int magic_sht_graph_end(magic_sht_handle* h, magic_sht_graph** graph);
 int magic_sht_graph_launch(magic_sht_handle* h, const magic_sht_graph* graph);
 int magic_sht_graph_destroy(magic_sht_graph* graph);
 
+/* ---- several independent instances in one launch per kind.  A group holds
+ * handles of different l_max / minc / grids (each its own initialize_transforms,
+ * all MAGIC_SHT_FP64TC or all MAGIC_SHT_BF16X3, with the persistent
+ * tensor-core kernels, one device).
+ * A group call runs the batched call of every instance (argument i for handle
+ * i, the same meaning as magic_sht_transform_to_grid_space /
+ * magic_sht_transform_to_lm_space), but the Legendre sums of all instances go
+ * into one pack and one persistent tensor-core launch per direction and field
+ * kind (scalar, vector), the instances with the largest l_max first, with the
+ * FFTs of every instance after them (synthesis) or before them (analysis).
+ * The results equal those of the separate calls bit for bit.  The reference
+ * runs one instance per process and loops its radial levels (rIter.f90:190);
+ * this is the batching form of the same per-level set.
+ * Device arrays only for spectra and grids (or2 / lcut may be host arrays);
+ * every handle must be bound to one stream (magic_sht_set_stream), on which
+ * the call is asynchronous and may be captured with magic_sht_graph_begin on
+ * the first handle: make the same calls once before capturing (they size the
+ * workspaces and upload the per-instance tables the launches read, which the
+ * group keeps until magic_sht_group_destroy).  A handle belongs to at most
+ * one group call at a time; n_levels, or2, lcut and args are arrays of
+ * n_handles entries (or2 / lcut may be NULL for all). */
+typedef struct magic_sht_group magic_sht_group;
+int magic_sht_group_create(magic_sht_handle* const* handles, int n_handles, magic_sht_group** group);
+int magic_sht_group_destroy(magic_sht_group* group);
+int magic_sht_group_transform_to_grid_space(magic_sht_group* group, const int* n_levels,
+                                            const double* const* or2, const int* const* lcut,
+                                            const magic_sht_grid_space_args* args);
+int magic_sht_group_transform_to_lm_space(magic_sht_group* group, const int* n_levels, const int* const* lcut,
+                                          const magic_sht_lm_space_args* args);
+
 /* ---- per-phase timing: CUDA events recorded on the handle's stream around
  * every kernel launch while profiling is on (timer counterpart of the
  * reference's lm2phy/phy2lm counters, timing.f90:17-163). */

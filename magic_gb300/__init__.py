@@ -4,4 +4,4 @@
 (src/sht_native.f90:16-20) over the C ABI of ``libmagic_sht.so``
 (include/magic_sht.h).
 """
-from .sht import SHT, truncation, prime_decomposition, measure_gflops, dt_courant  # noqa: F401
+from .sht import SHT, SHTGroup, truncation, prime_decomposition, measure_gflops, dt_courant  # noqa: F401

@@ -183,6 +183,10 @@ SIGNATURES = {
     "magic_sht_graph_end": [_V, ctypes.POINTER(_V)],
     "magic_sht_graph_launch": [_V, _V],
     "magic_sht_graph_destroy": [_V],
+    "magic_sht_group_create": [_V, ctypes.c_int, ctypes.POINTER(_V)],
+    "magic_sht_group_destroy": [_V],
+    "magic_sht_group_transform_to_grid_space": [_V, _V, _V, _V, ctypes.POINTER(GridSpaceArgs)],
+    "magic_sht_group_transform_to_lm_space": [_V, _V, _V, ctypes.POINTER(LmSpaceArgs)],
     "magic_sht_measure_gflops": [ctypes.c_int, ctypes.c_int, _D],
     "magic_sht_set_profiling": [_V, ctypes.c_int],
     "magic_sht_phase_times": [_V, _V, _V, ctypes.c_int],

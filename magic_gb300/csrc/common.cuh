@@ -44,6 +44,7 @@ struct InvSet {
   const int* lcut;    // device [nlev] or null (then lcut0 for every level)
   const double* or2;  // device [nlev] or null (then or2_0; only OP_CURLT uses it)
   int lcut0;
+  int pad_;  // no padding bytes: group calls compare descriptors bytewise
   double or2_0;
 };
 
@@ -65,6 +66,7 @@ struct FwdSet {
   int nlev;
   const int* lcut;    // device [nlev] or null (then lcut0)
   int lcut0;
+  int pad_;
 };
 
 // Azimuthal FFT field.
@@ -107,6 +109,7 @@ struct ShtGeom {
   int n_phi;                     // n_phi_max = n_phi_tot/minc
   int lm_max;
   int ld;                        // leading dimension (nlat_padded) of grid arrays
+  int pad_;
   const int* lmoff;              // device [n_m] start of each m block (st_map)
   const double* P64;             // device [lm_max][nh]
   const double* dP64;
@@ -224,6 +227,100 @@ struct CourantArgs {
 struct BcGrids {
   double* p[8];
 };
+
+// One transform instance of a persistent tensor-core launch: its geometry,
+// its field set (InvSet or FwdSet), its table images and its data-operand
+// images (`bimg`, column exponents `cexp` after the tiles), with `nct` column
+// tiles.  A launch over several instances (magic_sht_group_*) takes an array
+// of them: tile0 / blk0 are the instance's first tile of the persistent
+// kernel and first block of the pack kernel, and the instances' tiles follow
+// each other in the array's order.
+// (The structs above hold no padding bytes, so that equal descriptors compare
+// equal bytewise.)
+template <class Set>
+struct LegInst {
+  ShtGeom g;
+  Set s;
+  TcTables t;
+  unsigned char* bimg;
+  short* cexp;
+  int nct;
+  int tile0;
+  int blk0;
+  int pad_;
+};
+
+// First tile / pack block of each instance of a launch over several
+// instances, passed as a kernel parameter (constant bank: the per-tile lookup
+// reads no global memory).
+constexpr int kMaxGroupInst = 64;
+struct InstIndex {
+  int n;
+  int tile0[kMaxGroupInst];
+  int blk0[kMaxGroupInst];
+};
+
+template <class Set>
+inline InstIndex inst_index(const LegInst<Set>* inst, int n) {
+  InstIndex X{};
+  X.n = n;
+  for (int i = 0; i < n && i < kMaxGroupInst; ++i) {
+    X.tile0[i] = inst[i].tile0;
+    X.blk0[i] = inst[i].blk0;
+  }
+  return X;
+}
+
+#ifdef __CUDACC__
+// the last instance whose first index (tile or block) is <= x
+__device__ __forceinline__ int inst_search(const int* first, int n, int x) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (first[mid] <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+// A persistent launch covers one instance (the kernel parameter `one`) or,
+// with MULTI, the X.n instances of `many` (device memory), whose tiles and
+// pack blocks follow each other; `one` then holds the first instance (the
+// tile counter and the error word of the launch).
+// The instance of persistent-kernel tile `ix`; ix becomes the tile within it.
+template <bool MULTI, class I>
+__device__ __forceinline__ const I& tile_inst(const I& one, const I* many, const InstIndex& X, int& ix) {
+  if constexpr (!MULTI) {
+    return one;
+  } else {
+    const int k = inst_search(X.tile0, X.n, ix);
+    ix -= X.tile0[k];
+    return many[k];
+  }
+}
+// The instance, column tile ct, order mc and chunk c of this pack-kernel
+// block: a 3-D grid (ct, mc, c) for one instance; with MULTI a 1-D grid whose
+// blocks of one instance run column tile fastest, then order, then chunk.
+template <bool MULTI, class I>
+__device__ __forceinline__ const I& block_inst(const I& one, const I* many, const InstIndex& X, int& ct, int& mc,
+                                               int& c) {
+  if constexpr (!MULTI) {
+    ct = blockIdx.x;
+    mc = blockIdx.y;
+    c = blockIdx.z;
+    return one;
+  } else {
+    const int b = blockIdx.x;
+    const int k = inst_search(X.blk0, X.n, b);
+    const I& in = many[k];
+    int r = b - X.blk0[k];
+    ct = r % in.nct;
+    r /= in.nct;
+    mc = r % in.g.n_m;
+    c = r / in.g.n_m;
+    return in;
+  }
+}
+#endif
 
 __host__ __device__ inline int tc_nch(int n_l) { return ((n_l + 1) / 2 + 63) / 64; }
 

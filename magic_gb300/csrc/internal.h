@@ -95,3 +95,21 @@ cudaError_t launch_inv_legendre_oz(const ShtGeom& g, const InvSet& s, bool vec, 
                                    unsigned char* bimg, cudaStream_t st);
 cudaError_t launch_fwd_legendre_oz(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
                                    unsigned char* bimg, cudaStream_t st);
+// several instances in one pack + one persistent launch (magic_sht_group_*):
+// oz_layout_insts fills nct, cexp, tile0 and blk0 of every instance (g, s, t
+// and bimg set by the caller) and returns the launch's pack blocks and tiles;
+// inst[0..n) on the host, d_inst the same array in device memory, n at most
+// kMaxGroupInst
+template <class Set>
+void oz_layout_insts(LegInst<Set>* inst, int n, bool vec, long long* nblocks, long long* ntiles);
+cudaError_t launch_inv_legendre_oz_multi(const LegInst<InvSet>* inst, const LegInst<InvSet>* d_inst, int n,
+                                         bool vec, long long nblocks, long long ntiles, cudaStream_t st);
+cudaError_t launch_fwd_legendre_oz_multi(const LegInst<FwdSet>* inst, const LegInst<FwdSet>* d_inst, int n,
+                                         bool vec, long long nblocks, long long ntiles, cudaStream_t st);
+// the same for the 3xBF16 persistent kernels (legendre_tcp.cu); cexp unused
+template <class Set>
+void tcp_layout_insts(LegInst<Set>* inst, int n, bool vec, long long* nblocks, long long* ntiles);
+cudaError_t launch_inv_legendre_tcp_multi(const LegInst<InvSet>* inst, const LegInst<InvSet>* d_inst, int n,
+                                          bool vec, long long nblocks, long long ntiles, cudaStream_t st);
+cudaError_t launch_fwd_legendre_tcp_multi(const LegInst<FwdSet>* inst, const LegInst<FwdSet>* d_inst, int n,
+                                          bool vec, long long nblocks, long long ntiles, cudaStream_t st);

@@ -38,6 +38,8 @@
 //     A_i x [B_0 | ... | B_{6-i}]  ->  [C_i | ... | C_6]     (N = 32 (7 - i))
 // because the data digits of a tile lie one after the other along N.
 #include <algorithm>
+#include <type_traits>
+#include <vector>
 #include <cuda_bf16.h>
 #include "common.cuh"
 #include "cplx.cuh"
@@ -251,6 +253,11 @@ __device__ __forceinline__ void issue_digit(uint32_t acc, const unsigned char* A
 // the epilogue does not store.
 __device__ __forceinline__ uint32_t table_rows_bytes(int rows) { return (uint32_t)((min(rows, 128) + 7) >> 3) << 10; }
 
+// ------------------------------------------------------------ instances
+// (tile_inst / block_inst of common.cuh: one instance, or several with MULTI)
+using OzInv = LegInst<InvSet>;
+using OzFwd = LegInst<FwdSet>;
+
 template <typename P>
 __device__ __forceinline__ P* shfl_ptr(P* p, int src) {
   const unsigned long long v = (unsigned long long)p;
@@ -392,14 +399,21 @@ __device__ __forceinline__ PackCol pack_col(const ShtGeom& g, const InvSet& s, i
   return c;
 }
 
-template <bool VEC>
-__global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const ShtGeom g, const InvSet s, const TcTables t,
-                                                            unsigned char* __restrict__ bimg, short* __restrict__ cexp,
-                                                            int nct) {
+template <bool VEC, bool MULTI>
+__global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const __grid_constant__ OzInv one,
+                                                            const OzInv* __restrict__ many,
+                                                            const __grid_constant__ InstIndex X) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* buf = align1k(smem_raw);  // two tiles of kTS bytes
   __shared__ int sE[kNC];
-  const int ct = blockIdx.x, mc = blockIdx.y;
+  int ct, mc, c_unused;
+  const OzInv& I = block_inst<MULTI>(one, many, X, ct, mc, c_unused);
+  const ShtGeom& g = I.g;
+  const InvSet& s = I.s;
+  const TcTables& t = I.t;
+  unsigned char* __restrict__ bimg = I.bimg;
+  short* __restrict__ cexp = I.cexp;
+  const int nct = I.nct;
   const int m = mc * g.minc, n_l = g.l_max - m + 1, lm0 = g.lmoff[mc];
   const int nch = tc_nch(n_l);
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
@@ -492,16 +506,23 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const ShtGeom g, 
 // Analysis data of one (column tile ct, order mc): the double-float (ES, EA)
 // half spectra of 16 complex columns over the nh colatitudes.  Exponents per
 // (ES | EA, real column): cexp[mc][2][nct * kNC]; tiles [mc][chunk][ct][ES|EA].
-template <bool VEC>
-__global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_oz(const ShtGeom g, const FwdSet s, const TcTables t,
-                                                            unsigned char* __restrict__ bimg, short* __restrict__ cexp,
-                                                            int nct) {
+template <bool VEC, bool MULTI>
+__global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_oz(const __grid_constant__ OzFwd one,
+                                                            const OzFwd* __restrict__ many,
+                                                            const __grid_constant__ InstIndex X) {
   extern __shared__ unsigned char smem_raw[];
   // one (ES, EA) tile pair (56 KB): three CTAs per SM; the next chunk waits for
   // the bulk store of the previous one (two pairs measured 1 CTA per SM, 1.8 ms)
   unsigned char* buf = align1k(smem_raw);
   __shared__ int sE[2][kNC];
-  const int ct = blockIdx.x, mc = blockIdx.y;
+  int ct, mc, c_unused;
+  const OzFwd& I = block_inst<MULTI>(one, many, X, ct, mc, c_unused);
+  const ShtGeom& g = I.g;
+  const FwdSet& s = I.s;
+  const TcTables& t = I.t;
+  unsigned char* __restrict__ bimg = I.bimg;
+  short* __restrict__ cexp = I.cexp;
+  const int nct = I.nct;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   const int tid = threadIdx.x;
   auto src_of = [&](int q) -> const dfl2* {
@@ -639,11 +660,10 @@ __device__ __forceinline__ float pow2f(int e) {
   return __int_as_float((e + 127) << 23);
 }
 
-template <bool VEC>
-__global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS) inv_leg_oz(const ShtGeom g, const InvSet s,
-                                                                      const TcTables t,
-                                                                      const unsigned char* __restrict__ bimg,
-                                                                      const short* __restrict__ cexp, int nct) {
+template <bool VEC, bool MULTI>
+__global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS)
+    inv_leg_oz(const __grid_constant__ OzInv one, const OzInv* __restrict__ many,
+               const __grid_constant__ InstIndex X, int ntiles) {
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NA = Rings<VEC, true>::NA, NB = Rings<VEC, true>::NB;
   constexpr uint32_t ASZ = NT * 16384;
@@ -656,9 +676,6 @@ __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS) 
   unsigned char* sA = align1k(smem_raw);
   unsigned char* sB = sA + NA * ASZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int npair = s.nf * s.nlev;
-  const int ncplx = npair * (VEC ? 2 : 1);
-  const int ntiles = nct * t.ntt * 2 * g.n_m;
 
   if (tid == 0) {
     constexpr int NI = Occ<VEC, true>::NISS;  // every MMA thread commits to the empty / full barriers
@@ -690,15 +707,20 @@ __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS) 
       while (ok) {
         if (!ring_push(R, tr, ix < ntiles ? ix : -1)) { ok = false; break; }
         if (ix >= ntiles) break;
-        const int next = atomicAdd(t.tile_ctr, 1) + (int)gridDim.x;
-        T.decode(g, t, nct, ix);
+        const int next = atomicAdd(one.t.tile_ctr, 1) + (int)gridDim.x;
+        int lix = ix;
+        const OzInv& I = tile_inst<MULTI>(one, many, X, lix);
+        const ShtGeom& g = I.g;
+        const TcTables& t = I.t;
+        const int nct = I.nct;
+        T.decode(g, t, nct, lix);
         ix = next;
         if (T.nlp == 0) continue;
         for (int c = 0; c < T.nchp && ok; ++c) {
           const uint32_t bslot = b_use % NB;
           if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
           tc::mbar_expect_tx(&b_full[bslot], kTS);
-          tc::bulk_g2s(sB + bslot * kTS, bimg + ((t.bpc0[T.mc] + T.p * T.nch + c) * nct + T.ct) * (long long)kTS,
+          tc::bulk_g2s(sB + bslot * kTS, I.bimg + ((t.bpc0[T.mc] + T.p * T.nch + c) * nct + T.ct) * (long long)kTS,
                        kTS, &b_full[bslot]);
           ++b_use;
           const uint32_t abytes = table_rows_bytes(g.nh - T.tt * 128);
@@ -725,7 +747,8 @@ __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS) 
         int ix;
         if (!ring_pop(R, tr, ix)) { ok = false; break; }
         if (ix < 0) break;
-        T.decode(g, t, nct, ix);
+        const OzInv& I = tile_inst<MULTI>(one, many, X, ix);
+        T.decode(I.g, I.t, I.nct, ix);
         if (T.nlp == 0) continue;
         if (!wait_empty(&acc_empty, acc_use, 1)) { ok = false; break; }
         tc::tc_fence_after();
@@ -753,12 +776,19 @@ __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS) 
     const int cc0 = half * (kNC / 2);  // this warp's 16 real columns
     const int jl = 32 * q4 + lane;
     const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
-    const int NHP = t.ntt * 128;
     uint32_t acc_use = 0, tr = 0;
     while (ok) {
       int ix;
       if (!ring_pop(R, tr, ix)) { ok = false; break; }
       if (ix < 0) break;
+      const OzInv& I = tile_inst<MULTI>(one, many, X, ix);
+      const ShtGeom& g = I.g;
+      const InvSet& s = I.s;
+      const TcTables& t = I.t;
+      const int nct = I.nct;
+      const int npair = s.nf * s.nlev;
+      const int ncplx = npair * (VEC ? 2 : 1);
+      const int NHP = t.ntt * 128;
       T.decode(g, t, nct, ix);
       const int jg = T.tt * 128 + jl;
       const bool row_ok = jg < g.nh;
@@ -797,7 +827,7 @@ __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS) 
       // exponents: this thread's row (both tables) and the warp's 16 columns
       const int erow0 = row_ok ? t.inv_exp[(size_t)T.mc * NHP + jg] : 0;
       const int erow1 = (VEC && row_ok) ? t.inv_exp[((size_t)g.n_m + T.mc) * NHP + jg] : 0;
-      const short* ce = cexp + (long long)T.mc * nct * kNC + T.ct * kNC + cc0;
+      const short* ce = I.cexp + (long long)T.mc * nct * kNC + T.ct * kNC + cc0;
       if (!wait_full(&acc_full, acc_use, 1)) { ok = false; break; }
       tc::tc_fence_after();
       const uint32_t acc = tmem + lane_off + cc0;
@@ -853,7 +883,7 @@ __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS) 
   if (!ok) atomicExch(&s_fail, 1);
   tc::tc_fence_before();
   __syncthreads();
-  if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
+  if (tid == 0 && s_fail && one.t.err) atomicExch(one.t.err, 1);
   if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC, true>::TCOLS);
 }
 
@@ -880,11 +910,10 @@ struct FwdTile {
   }
 };
 
-template <bool VEC>
-__global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS) fwd_leg_oz(const ShtGeom g, const FwdSet s,
-                                                                      const TcTables t,
-                                                                      const unsigned char* __restrict__ bimg,
-                                                                      const short* __restrict__ cexp, int nct) {
+template <bool VEC, bool MULTI>
+__global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS)
+    fwd_leg_oz(const __grid_constant__ OzFwd one, const OzFwd* __restrict__ many,
+               const __grid_constant__ InstIndex X, int ntiles) {
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NA = Rings<VEC, false>::NA, NB = Rings<VEC, false>::NB;
   constexpr uint32_t ASZ = NT * 16384;
@@ -898,9 +927,6 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
   unsigned char* sA = align1k(smem_raw);
   unsigned char* sB = sA + NA * ASZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int npair = s.nf * s.nlev;
-  const int ncplx = npair * (VEC ? 2 : 1);
-  const int ntiles = nct * t.nlt * 2 * g.n_m;
 
   if (tid == 0) {
     constexpr int NI = Occ<VEC, false>::NISS;  // every MMA thread commits to the empty / full barriers
@@ -932,15 +958,19 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
       while (ok) {
         if (!ring_push(R, tr, ix < ntiles ? ix : -1)) { ok = false; break; }
         if (ix >= ntiles) break;
-        const int next = atomicAdd(t.tile_ctr, 1) + (int)gridDim.x;
-        T.decode(g, t, nct, ix);
+        const int next = atomicAdd(one.t.tile_ctr, 1) + (int)gridDim.x;
+        int lix = ix;
+        const OzFwd& I = tile_inst<MULTI>(one, many, X, lix);
+        const TcTables& t = I.t;
+        const int nct = I.nct;
+        T.decode(I.g, t, nct, lix);
         ix = next;
         if (T.lt * 128 >= T.nlp) continue;
         for (int c = 0; c < t.ncj && ok; ++c) {
           const uint32_t bslot = b_use % NB;
           if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
           tc::mbar_expect_tx(&b_full[bslot], BSZ);
-          const unsigned char* img = bimg + (((long long)T.mc * t.ncj + c) * nct + T.ct) * (2LL * kTS);
+          const unsigned char* img = I.bimg + (((long long)T.mc * t.ncj + c) * nct + T.ct) * (2LL * kTS);
           tc::bulk_g2s(sB + bslot * BSZ, img + T.p * kTS, kTS, &b_full[bslot]);                     // mine
           if (VEC) tc::bulk_g2s(sB + bslot * BSZ + kTS, img + (1 - T.p) * kTS, kTS, &b_full[bslot]);  // other
           ++b_use;
@@ -968,11 +998,12 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
         int ix;
         if (!ring_pop(R, tr, ix)) { ok = false; break; }
         if (ix < 0) break;
-        T.decode(g, t, nct, ix);
+        const OzFwd& I = tile_inst<MULTI>(one, many, X, ix);
+        T.decode(I.g, I.t, I.nct, ix);
         if (T.lt * 128 >= T.nlp) continue;
         if (!wait_empty(&acc_empty, acc_use, 1)) { ok = false; break; }
         tc::tc_fence_after();
-        for (int c = 0; c < t.ncj && ok; ++c, ++b_use) {
+        for (int c = 0; c < I.t.ncj && ok; ++c, ++b_use) {
           const uint32_t bslot = b_use % NB;
           if (!wait_full(&b_full[bslot], b_use, NB)) { ok = false; break; }
           for (int u = 0; u < kS; ++u, ++a_use) {
@@ -1000,6 +1031,13 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
       int ix;
       if (!ring_pop(R, tr, ix)) { ok = false; break; }
       if (ix < 0) break;
+      const OzFwd& I = tile_inst<MULTI>(one, many, X, ix);
+      const ShtGeom& g = I.g;
+      const FwdSet& s = I.s;
+      const TcTables& t = I.t;
+      const int nct = I.nct;
+      const int npair = s.nf * s.nlev;
+      const int ncplx = npair * (VEC ? 2 : 1);
       T.decode(g, t, nct, ix);
       if (T.lt * 128 >= T.nlp) continue;
       const int m = T.mc * g.minc;
@@ -1022,7 +1060,7 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
       }
       const int erow0 = valid ? t.fwd_exp[lm] : 0;
       const int erow1 = (VEC && valid) ? t.fwd_exp[(size_t)g.lm_max + lm] : 0;
-      const short* ce = cexp + (long long)T.mc * 2 * nct * kNC + T.ct * kNC + cc0;
+      const short* ce = I.cexp + (long long)T.mc * 2 * nct * kNC + T.ct * kNC + cc0;
       const short* ce_mine = ce + (long long)T.p * nct * kNC;
       const short* ce_other = ce + (long long)(1 - T.p) * nct * kNC;
       if (!wait_full(&acc_full, acc_use, 1)) { ok = false; break; }
@@ -1077,7 +1115,7 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
   if (!ok) atomicExch(&s_fail, 1);
   tc::tc_fence_before();
   __syncthreads();
-  if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
+  if (tid == 0 && s_fail && one.t.err) atomicExch(one.t.err, 1);
   if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC, false>::TCOLS);
 }
 
@@ -1100,45 +1138,43 @@ int num_sms_oz() {
 
 long long oz_nct(int ncplx) { return (ncplx + kNC / 2 - 1) / (kNC / 2); }
 
-template <bool VEC>
-cudaError_t launch_inv_oz(const ShtGeom& g, const InvSet& s, const TcTables& t, unsigned char* bimg,
+// tiles of the persistent kernels and blocks of the pack kernels of one instance
+long long oz_inv_tiles(const ShtGeom& g, const TcTables& t, int nct) { return (long long)nct * t.ntt * 2 * g.n_m; }
+long long oz_fwd_tiles(const ShtGeom& g, const TcTables& t, int nct) { return (long long)nct * t.nlt * 2 * g.n_m; }
+
+template <bool VEC, bool MULTI>
+cudaError_t launch_inv_oz(const OzInv& one, const OzInv* many, const InstIndex& X, long long nblocks, long long ntiles,
                           cudaStream_t st) {
   constexpr int NT = VEC ? 2 : 1, NA = Rings<VEC, true>::NA, NB = Rings<VEC, true>::NB;
-  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  if (ncplx <= 0) return cudaSuccess;
-  const int nct = (int)oz_nct(ncplx);
-  short* cexp = (short*)(bimg + oz_tiles_bytes_inv(t, nct));
+  if (ntiles <= 0) return cudaSuccess;
   const size_t psmem = 1024 + 2 * (size_t)kTS;
-  CUDA_TRY(cudaFuncSetAttribute(pack_inv_oz<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_inv_oz<VEC><<<dim3(nct, g.n_m), kPackThreads, psmem, st>>>(g, s, t, bimg, cexp, nct);
+  CUDA_TRY(cudaFuncSetAttribute(pack_inv_oz<VEC, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  const dim3 pgrid = MULTI ? dim3((unsigned)nblocks) : dim3(one.nct, one.g.n_m);
+  pack_inv_oz<VEC, MULTI><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * kTS;
-  CUDA_TRY(cudaFuncSetAttribute(inv_leg_oz<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
+  CUDA_TRY(cudaFuncSetAttribute(inv_leg_oz<VEC, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC, true>::CPS);
-  CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  inv_leg_oz<VEC><<<grid, Occ<VEC, true>::THREADS, smem, st>>>(g, s, t, bimg, cexp, nct);
+  CUDA_TRY(cudaMemsetAsync(one.t.tile_ctr, 0, sizeof(int), st));
+  inv_leg_oz<VEC, MULTI><<<grid, Occ<VEC, true>::THREADS, smem, st>>>(one, many, X, (int)ntiles);
   return cudaGetLastError();
 }
 
-template <bool VEC>
-cudaError_t launch_fwd_oz(const ShtGeom& g, const FwdSet& s, const TcTables& t, unsigned char* bimg,
+template <bool VEC, bool MULTI>
+cudaError_t launch_fwd_oz(const OzFwd& one, const OzFwd* many, const InstIndex& X, long long nblocks, long long ntiles,
                           cudaStream_t st) {
   constexpr int NT = VEC ? 2 : 1, NA = Rings<VEC, false>::NA, NB = Rings<VEC, false>::NB;
-  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  if (ncplx <= 0) return cudaSuccess;
-  const int nct = (int)oz_nct(ncplx);
-  short* cexp = (short*)(bimg + oz_tiles_bytes_fwd(g, t, nct));
+  if (ntiles <= 0) return cudaSuccess;
   const size_t psmem = 1024 + 2 * (size_t)kTS;
-  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_oz<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_fwd_oz<VEC><<<dim3(nct, g.n_m), kPackThreads, psmem, st>>>(g, s, t, bimg, cexp, nct);
+  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_oz<VEC, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  const dim3 pgrid = MULTI ? dim3((unsigned)nblocks) : dim3(one.nct, one.g.n_m);
+  pack_fwd_oz<VEC, MULTI><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * kTS;
-  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_oz<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
+  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_oz<VEC, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC, false>::CPS);
-  CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  fwd_leg_oz<VEC><<<grid, Occ<VEC, false>::THREADS, smem, st>>>(g, s, t, bimg, cexp, nct);
+  CUDA_TRY(cudaMemsetAsync(one.t.tile_ctr, 0, sizeof(int), st));
+  fwd_leg_oz<VEC, MULTI><<<grid, Occ<VEC, false>::THREADS, smem, st>>>(one, many, X, (int)ntiles);
   return cudaGetLastError();
 }
 
@@ -1174,10 +1210,65 @@ cudaError_t build_oz_images(const ShtGeom& g, const TcTables& t, unsigned char* 
 
 cudaError_t launch_inv_legendre_oz(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,
                                    unsigned char* bimg, cudaStream_t st) {
-  return vec ? launch_inv_oz<true>(g, s, t, bimg, st) : launch_inv_oz<false>(g, s, t, bimg, st);
+  std::vector<OzInv> one(1);
+  one[0].g = g;
+  one[0].s = s;
+  one[0].t = t;
+  one[0].bimg = bimg;
+  long long nblocks = 0, ntiles = 0;
+  oz_layout_insts(one.data(), 1, vec, &nblocks, &ntiles);
+  InstIndex X{};
+  return vec ? launch_inv_oz<true, false>(one[0], nullptr, X, nblocks, ntiles, st)
+             : launch_inv_oz<false, false>(one[0], nullptr, X, nblocks, ntiles, st);
 }
 
 cudaError_t launch_fwd_legendre_oz(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
                                    unsigned char* bimg, cudaStream_t st) {
-  return vec ? launch_fwd_oz<true>(g, s, t, bimg, st) : launch_fwd_oz<false>(g, s, t, bimg, st);
+  std::vector<OzFwd> one(1);
+  one[0].g = g;
+  one[0].s = s;
+  one[0].t = t;
+  one[0].bimg = bimg;
+  long long nblocks = 0, ntiles = 0;
+  oz_layout_insts(one.data(), 1, vec, &nblocks, &ntiles);
+  InstIndex X{};
+  return vec ? launch_fwd_oz<true, false>(one[0], nullptr, X, nblocks, ntiles, st)
+             : launch_fwd_oz<false, false>(one[0], nullptr, X, nblocks, ntiles, st);
+}
+
+template <class Set>
+void oz_layout_insts(LegInst<Set>* inst, int n, bool vec, long long* nblocks, long long* ntiles) {
+  constexpr bool INV = std::is_same<Set, InvSet>::value;
+  long long nb = 0, nt = 0;
+  for (int i = 0; i < n; ++i) {
+    LegInst<Set>& I = inst[i];
+    const int ncplx = I.s.nf * I.s.nlev * (vec ? 2 : 1);
+    I.nct = (int)oz_nct(ncplx > 0 ? ncplx : 0);
+    I.cexp = (short*)(I.bimg + (INV ? oz_tiles_bytes_inv(I.t, I.nct) : oz_tiles_bytes_fwd(I.g, I.t, I.nct)));
+    I.blk0 = (int)nb;
+    I.tile0 = (int)nt;
+    I.pad_ = 0;
+    nb += (long long)I.nct * I.g.n_m;
+    nt += INV ? oz_inv_tiles(I.g, I.t, I.nct) : oz_fwd_tiles(I.g, I.t, I.nct);
+  }
+  *nblocks = nb;
+  *ntiles = nt;
+}
+template void oz_layout_insts<InvSet>(LegInst<InvSet>*, int, bool, long long*, long long*);
+template void oz_layout_insts<FwdSet>(LegInst<FwdSet>*, int, bool, long long*, long long*);
+
+cudaError_t launch_inv_legendre_oz_multi(const LegInst<InvSet>* inst, const LegInst<InvSet>* d_inst, int n,
+                                         bool vec, long long nblocks, long long ntiles, cudaStream_t st) {
+  if (n < 1 || n > kMaxGroupInst) return cudaErrorInvalidValue;
+  const InstIndex X = inst_index(inst, n);
+  return vec ? launch_inv_oz<true, true>(inst[0], d_inst, X, nblocks, ntiles, st)
+             : launch_inv_oz<false, true>(inst[0], d_inst, X, nblocks, ntiles, st);
+}
+
+cudaError_t launch_fwd_legendre_oz_multi(const LegInst<FwdSet>* inst, const LegInst<FwdSet>* d_inst, int n,
+                                         bool vec, long long nblocks, long long ntiles, cudaStream_t st) {
+  if (n < 1 || n > kMaxGroupInst) return cudaErrorInvalidValue;
+  const InstIndex X = inst_index(inst, n);
+  return vec ? launch_fwd_oz<true, true>(inst[0], d_inst, X, nblocks, ntiles, st)
+             : launch_fwd_oz<false, true>(inst[0], d_inst, X, nblocks, ntiles, st);
 }

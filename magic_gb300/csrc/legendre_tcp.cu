@@ -31,6 +31,9 @@
 // accumulated apart in fp32 and summed (C2 + C1) + C0 in the epilogue.
 // Hand-offs use full/empty mbarriers; every wait is bounded and a wait that
 // gives up sets the device error word.
+#include <algorithm>
+#include <type_traits>
+#include <vector>
 #include <cuda_bf16.h>
 #include "common.cuh"
 #include "cplx.cuh"
@@ -228,15 +231,24 @@ __device__ __forceinline__ void drain_sum(uint32_t col, float (&v)[32]) {
 // shared memory and written with one bulk copy.
 // Synthesis data images: [pc = bpc0[m] + p*nch + c][ct] tiles of 3 splits.
 // One CTA builds both parity tiles of chunk c from 128 consecutive degrees.
-template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kPackThreads, 4) pack_inv_kernel(const ShtGeom g, const InvSet s,
-                                                                  const TcTables t,
-                                                                  unsigned char* __restrict__ bimg, int nct) {
+using TcInv = LegInst<InvSet>;
+using TcFwd = LegInst<FwdSet>;
+
+template <bool VEC, bool TF32, bool MULTI>
+__global__ void __launch_bounds__(kPackThreads, 4) pack_inv_kernel(const __grid_constant__ TcInv one,
+                                                                  const TcInv* __restrict__ many,
+                                                                  const __grid_constant__ InstIndex X) {
   constexpr int NC = kNC;
   constexpr uint32_t BSZ = Form<TF32>::OPSZ;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* B = align1k(smem_raw);
-  const int ct = blockIdx.x, mc = blockIdx.y, c = blockIdx.z;
+  int ct, mc, c;
+  const TcInv& I = block_inst<MULTI>(one, many, X, ct, mc, c);
+  const ShtGeom& g = I.g;
+  const InvSet& s = I.s;
+  const TcTables& t = I.t;
+  unsigned char* __restrict__ bimg = I.bimg;
+  const int nct = I.nct;
   const int m = mc * g.minc;
   const int nch = tc_nch(g.l_max - m + 1);
   if (c >= nch) return;
@@ -256,15 +268,21 @@ __global__ void __launch_bounds__(kPackThreads, 4) pack_inv_kernel(const ShtGeom
 
 // Analysis data images: [m][c][ct] pairs (ES tile, EA tile) of 3 splits each,
 // both built by one CTA from the (ES, EA) entries of 64 colatitudes.
-template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kPackThreads, 4) pack_fwd_kernel(const ShtGeom g, const FwdSet s,
-                                                                  const TcTables t,
-                                                                  unsigned char* __restrict__ bimg, int nct) {
+template <bool VEC, bool TF32, bool MULTI>
+__global__ void __launch_bounds__(kPackThreads, 4) pack_fwd_kernel(const __grid_constant__ TcFwd one,
+                                                                  const TcFwd* __restrict__ many,
+                                                                  const __grid_constant__ InstIndex X) {
   constexpr int NC = kNC;
   constexpr uint32_t PSZ = 2u * Form<TF32>::OPSZ;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* B = align1k(smem_raw);
-  const int ct = blockIdx.x, mc = blockIdx.y, c = blockIdx.z;
+  int ct, mc, c;
+  const TcFwd& I = block_inst<MULTI>(one, many, X, ct, mc, c);
+  const ShtGeom& g = I.g;
+  const FwdSet& s = I.s;
+  const TcTables& t = I.t;
+  unsigned char* __restrict__ bimg = I.bimg;
+  const int nct = I.nct;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
   fwd_build_tile<VEC, NC, 2, true, TF32>(g, s, B, ct, ncplx, mc, 0, c, warp, kPackThreads / 32, lane);
@@ -302,9 +320,10 @@ struct InvTile {
   }
 };
 
-template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32>::CPS) inv_leg_tcp(const ShtGeom g, const InvSet s, const TcTables t,
-                                                           const unsigned char* __restrict__ bimg, int nct) {
+template <bool VEC, bool TF32, bool MULTI>
+__global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32>::CPS)
+    inv_leg_tcp(const __grid_constant__ TcInv one, const TcInv* __restrict__ many, const __grid_constant__ InstIndex X,
+                int ntiles) {
   typedef Form<TF32> F;
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NC = kNC;
@@ -324,9 +343,6 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
   unsigned char* sA = base;
   unsigned char* sB = sA + NA * ASZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int npair = s.nf * s.nlev;
-  const int ncplx = npair * (VEC ? 2 : 1);
-  const int ntiles = nct * t.ntt * 2 * g.n_m;
 
   if (tid == 0) {
     constexpr int NI = Occ<VEC, TF32>::NISS;
@@ -357,15 +373,20 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
       while (ok) {
         if (!ring_push(R, tr, ix < ntiles ? ix : -1)) { ok = false; break; }
         if (ix >= ntiles) break;
-        const int next = atomicAdd(t.tile_ctr, 1) + (int)gridDim.x;
-        T.decode(g, t, nct, ix);
+        const int next = atomicAdd(one.t.tile_ctr, 1) + (int)gridDim.x;
+        int lix = ix;
+        const TcInv& I = tile_inst<MULTI>(one, many, X, lix);
+        const ShtGeom& g = I.g;
+        const TcTables& t = I.t;
+        const int nct = I.nct;
+        T.decode(g, t, nct, lix);
         ix = next;
         if (T.nlp == 0) continue;
         for (int c = 0; c < T.nchp && ok; ++c) {
           const uint32_t bslot = b_use % NB;
           if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
           tc::mbar_expect_tx(&b_full[bslot], BSZ);
-          tc::bulk_g2s(sB + bslot * BSZ, bimg + ((t.bpc0[T.mc] + T.p * T.nch + c) * nct + T.ct) * (long long)BSZ,
+          tc::bulk_g2s(sB + bslot * BSZ, I.bimg + ((t.bpc0[T.mc] + T.p * T.nch + c) * nct + T.ct) * (long long)BSZ,
                        BSZ, &b_full[bslot]);
           ++b_use;
           for (int u = 0; u < F::AUSES; ++u, ++a_use) {
@@ -394,7 +415,8 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
         int ix;
         if (!ring_pop(R, tr, ix)) { ok = false; break; }
         if (ix < 0) break;
-        T.decode(g, t, nct, ix);
+        const TcInv& I = tile_inst<MULTI>(one, many, X, ix);
+        T.decode(I.g, I.t, I.nct, ix);
         if (T.nlp == 0) continue;
         const uint32_t abuf = acc_use % NACC;
         if (!wait_empty(&acc_empty[abuf], acc_use, NACC)) { ok = false; break; }
@@ -425,13 +447,19 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
     const int cc0 = half * (NC / 2);  // this warp's 32 real columns
     const int jl = 32 * q4 + lane;
     const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
-    const int NHP = t.ntt * 128;
     uint32_t acc_use = 0, tr = 0;
     while (ok) {
       int ix;
       if (!ring_pop(R, tr, ix)) { ok = false; break; }
       if (ix < 0) break;
-      T.decode(g, t, nct, ix);
+      const TcInv& I = tile_inst<MULTI>(one, many, X, ix);
+      const ShtGeom& g = I.g;
+      const InvSet& s = I.s;
+      const TcTables& t = I.t;
+      const int npair = s.nf * s.nlev;
+      const int ncplx = npair * (VEC ? 2 : 1);
+      const int NHP = t.ntt * 128;
+      T.decode(g, t, I.nct, ix);
       const int jg = T.tt * 128 + jl;
       const bool row_ok = jg < g.nh;
       // output column bases, one per lane, broadcast by shuffles: scalar: lane q <
@@ -512,7 +540,7 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
   if (!ok) atomicExch(&s_fail, 1);
   tc::tc_fence_before();
   __syncthreads();
-  if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
+  if (tid == 0 && s_fail && one.t.err) atomicExch(one.t.err, 1);
   if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC, TF32>::TCOLS);
 }
 
@@ -539,9 +567,10 @@ struct FwdTile {
   }
 };
 
-template <bool VEC, bool TF32>
-__global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32>::CPS) fwd_leg_tcp(const ShtGeom g, const FwdSet s, const TcTables t,
-                                                           const unsigned char* __restrict__ bimg, int nct) {
+template <bool VEC, bool TF32, bool MULTI>
+__global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32>::CPS)
+    fwd_leg_tcp(const __grid_constant__ TcFwd one, const TcFwd* __restrict__ many, const __grid_constant__ InstIndex X,
+                int ntiles) {
   typedef Form<TF32> F;
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NC = kNC;
@@ -562,9 +591,6 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
   unsigned char* sA = base;
   unsigned char* sB = sA + NA * ASZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int npair = s.nf * s.nlev;
-  const int ncplx = npair * (VEC ? 2 : 1);
-  const int ntiles = nct * t.nlt * 2 * g.n_m;
 
   if (tid == 0) {
     constexpr int NI = Occ<VEC, TF32>::NISS;
@@ -595,15 +621,19 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
       while (ok) {
         if (!ring_push(R, tr, ix < ntiles ? ix : -1)) { ok = false; break; }
         if (ix >= ntiles) break;
-        const int next = atomicAdd(t.tile_ctr, 1) + (int)gridDim.x;
-        T.decode(g, t, nct, ix);
+        const int next = atomicAdd(one.t.tile_ctr, 1) + (int)gridDim.x;
+        int lix = ix;
+        const TcFwd& I = tile_inst<MULTI>(one, many, X, lix);
+        const TcTables& t = I.t;
+        const int nct = I.nct;
+        T.decode(I.g, t, nct, lix);
         ix = next;
         if (T.lt * 128 >= T.nlp) continue;
         for (int c = 0; c < t.ncj && ok; ++c) {
           const uint32_t bslot = b_use % NB;
           if (!wait_empty(&b_empty[bslot], b_use, NB)) { ok = false; break; }
           tc::mbar_expect_tx(&b_full[bslot], BSZ);
-          const unsigned char* img = bimg + (((long long)T.mc * t.ncj + c) * nct + T.ct) * (2LL * TS);
+          const unsigned char* img = I.bimg + (((long long)T.mc * t.ncj + c) * nct + T.ct) * (2LL * TS);
           tc::bulk_g2s(sB + bslot * BSZ, img + T.p * TS, TS, &b_full[bslot]);                    // mine
           if (VEC) tc::bulk_g2s(sB + bslot * BSZ + TS, img + (1 - T.p) * TS, TS, &b_full[bslot]);  // other
           ++b_use;
@@ -633,13 +663,14 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
         int ix;
         if (!ring_pop(R, tr, ix)) { ok = false; break; }
         if (ix < 0) break;
-        T.decode(g, t, nct, ix);
+        const TcFwd& I = tile_inst<MULTI>(one, many, X, ix);
+        T.decode(I.g, I.t, I.nct, ix);
         if (T.lt * 128 >= T.nlp) continue;
         const uint32_t abuf = acc_use % NACC;
         if (!wait_empty(&acc_empty[abuf], acc_use, NACC)) { ok = false; break; }
         tc::tc_fence_after();
         const uint32_t acc = tmem + abuf * ACC;
-        for (int c = 0; c < t.ncj && ok; ++c, ++b_use) {
+        for (int c = 0; c < I.t.ncj && ok; ++c, ++b_use) {
           const uint32_t bslot = b_use % NB;
           if (!wait_full(&b_full[bslot], b_use, NB)) { ok = false; break; }
           for (int u = 0; u < F::AUSES; ++u, ++a_use) {
@@ -667,7 +698,13 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
       int ix;
       if (!ring_pop(R, tr, ix)) { ok = false; break; }
       if (ix < 0) break;
-      T.decode(g, t, nct, ix);
+      const TcFwd& I = tile_inst<MULTI>(one, many, X, ix);
+      const ShtGeom& g = I.g;
+      const FwdSet& s = I.s;
+      const TcTables& t = I.t;
+      const int npair = s.nf * s.nlev;
+      const int ncplx = npair * (VEC ? 2 : 1);
+      T.decode(g, t, I.nct, ix);
       if (T.lt * 128 >= T.nlp) continue;
       const uint32_t abuf = acc_use % NACC;
       if (!wait_full(&acc_full[abuf], acc_use, NACC)) { ok = false; break; }
@@ -737,7 +774,7 @@ __global__ void __launch_bounds__(kThreads + Occ<VEC, TF32>::XTRA, Occ<VEC, TF32
   if (!ok) atomicExch(&s_fail, 1);
   tc::tc_fence_before();
   __syncthreads();
-  if (tid == 0 && s_fail && t.err) atomicExch(t.err, 1);
+  if (tid == 0 && s_fail && one.t.err) atomicExch(one.t.err, 1);
   if (warp == 0) tc::tmem_dealloc(tmem, Occ<VEC, TF32>::TCOLS);
 }
 
@@ -752,45 +789,45 @@ int num_sms() {
   return n;
 }
 
-template <bool VEC, bool TF32>
-cudaError_t launch_inv_p(const ShtGeom& g, const InvSet& s, const TcTables& t, unsigned char* bimg,
+int tcp_nct(int ncplx) { return (ncplx + kNC / 2 - 1) / (kNC / 2); }
+
+template <bool VEC, bool TF32, bool MULTI>
+cudaError_t launch_inv_p(const TcInv& one, const TcInv* many, const InstIndex& X, long long nblocks, long long ntiles,
                          cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, true, TF32>::NA, NB = Rings<VEC, true, TF32>::NB;
+  constexpr int NT = VEC ? 2 : 1, NA = Rings<VEC, true, TF32>::NA, NB = Rings<VEC, true, TF32>::NB;
   constexpr size_t OPSZ = Form<TF32>::OPSZ;
-  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  if (ncplx <= 0) return cudaSuccess;
-  const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
+  if (ntiles <= 0) return cudaSuccess;
   const size_t psmem = 1024 + 2 * OPSZ;
-  CUDA_TRY(cudaFuncSetAttribute(pack_inv_kernel<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_inv_kernel<VEC, TF32><<<dim3(nct, g.n_m, tc_nch(g.l_max + 1)), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  CUDA_TRY(cudaFuncSetAttribute(pack_inv_kernel<VEC, TF32, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)psmem));
+  const dim3 pgrid = MULTI ? dim3((unsigned)nblocks) : dim3(one.nct, one.g.n_m, tc_nch(one.g.l_max + 1));
+  pack_inv_kernel<VEC, TF32, MULTI><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * OPSZ;
-  CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const long long ntiles = (long long)nct * t.ntt * 2 * g.n_m;
+  CUDA_TRY(cudaFuncSetAttribute(inv_leg_tcp<VEC, TF32, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = (int)std::min<long long>(ntiles, (long long)num_sms() * Occ<VEC, TF32>::CPS);
-  CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  inv_leg_tcp<VEC, TF32><<<grid, kThreads + Occ<VEC, TF32>::XTRA, smem, st>>>(g, s, t, bimg, nct);
+  CUDA_TRY(cudaMemsetAsync(one.t.tile_ctr, 0, sizeof(int), st));
+  inv_leg_tcp<VEC, TF32, MULTI><<<grid, kThreads + Occ<VEC, TF32>::XTRA, smem, st>>>(one, many, X, (int)ntiles);
   return cudaGetLastError();
 }
 
-template <bool VEC, bool TF32>
-cudaError_t launch_fwd_p(const ShtGeom& g, const FwdSet& s, const TcTables& t, unsigned char* bimg,
+template <bool VEC, bool TF32, bool MULTI>
+cudaError_t launch_fwd_p(const TcFwd& one, const TcFwd* many, const InstIndex& X, long long nblocks, long long ntiles,
                          cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NC = kNC, NA = Rings<VEC, false, TF32>::NA, NB = Rings<VEC, false, TF32>::NB;
+  constexpr int NT = VEC ? 2 : 1, NA = Rings<VEC, false, TF32>::NA, NB = Rings<VEC, false, TF32>::NB;
   constexpr size_t OPSZ = Form<TF32>::OPSZ;
-  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  if (ncplx <= 0) return cudaSuccess;
-  const int nct = (ncplx + NC / 2 - 1) / (NC / 2);
+  if (ntiles <= 0) return cudaSuccess;
   const size_t psmem = 1024 + 2 * OPSZ;
-  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_kernel<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  pack_fwd_kernel<VEC, TF32><<<dim3(nct, g.n_m, t.ncj), kPackThreads, psmem, st>>>(g, s, t, bimg, nct);
+  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_kernel<VEC, TF32, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)psmem));
+  const dim3 pgrid = MULTI ? dim3((unsigned)nblocks) : dim3(one.nct, one.g.n_m, one.t.ncj);
+  pack_fwd_kernel<VEC, TF32, MULTI><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * OPSZ;
-  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC, TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const long long ntiles = (long long)nct * t.nlt * 2 * g.n_m;
+  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_tcp<VEC, TF32, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = (int)std::min<long long>(ntiles, (long long)num_sms() * Occ<VEC, TF32>::CPS);
-  CUDA_TRY(cudaMemsetAsync(t.tile_ctr, 0, sizeof(int), st));
-  fwd_leg_tcp<VEC, TF32><<<grid, kThreads + Occ<VEC, TF32>::XTRA, smem, st>>>(g, s, t, bimg, nct);
+  CUDA_TRY(cudaMemsetAsync(one.t.tile_ctr, 0, sizeof(int), st));
+  fwd_leg_tcp<VEC, TF32, MULTI><<<grid, kThreads + Occ<VEC, TF32>::XTRA, smem, st>>>(one, many, X, (int)ntiles);
   return cudaGetLastError();
 }
 
@@ -805,14 +842,78 @@ size_t tcp_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool vec, 
   return (size_t)((long long)g.n_m * t.ncj * nct * 2 * tile);
 }
 
+// tiles of the persistent kernels and blocks of the pack kernels of every
+// instance (nct, tile0, blk0; g, s, t and bimg set by the caller)
+template <class Set>
+void tcp_layout_insts(LegInst<Set>* inst, int n, bool vec, long long* nblocks, long long* ntiles) {
+  constexpr bool INV = std::is_same<Set, InvSet>::value;
+  long long nb = 0, nt = 0;
+  for (int i = 0; i < n; ++i) {
+    LegInst<Set>& I = inst[i];
+    const int ncplx = I.s.nf * I.s.nlev * (vec ? 2 : 1);
+    I.nct = tcp_nct(ncplx > 0 ? ncplx : 0);
+    I.cexp = nullptr;
+    I.blk0 = (int)nb;
+    I.tile0 = (int)nt;
+    I.pad_ = 0;
+    nb += (long long)I.nct * I.g.n_m * (INV ? tc_nch(I.g.l_max + 1) : I.t.ncj);
+    nt += (long long)I.nct * (INV ? I.t.ntt : I.t.nlt) * 2 * I.g.n_m;
+  }
+  *nblocks = nb;
+  *ntiles = nt;
+}
+template void tcp_layout_insts<InvSet>(LegInst<InvSet>*, int, bool, long long*, long long*);
+template void tcp_layout_insts<FwdSet>(LegInst<FwdSet>*, int, bool, long long*, long long*);
+
 cudaError_t launch_inv_legendre_tcp(const ShtGeom& g, const InvSet& s, bool vec, bool tf32, const TcTables& t,
                                     unsigned char* bimg, cudaStream_t st) {
-  if (tf32) return vec ? launch_inv_p<true, true>(g, s, t, bimg, st) : launch_inv_p<false, true>(g, s, t, bimg, st);
-  return vec ? launch_inv_p<true, false>(g, s, t, bimg, st) : launch_inv_p<false, false>(g, s, t, bimg, st);
+  std::vector<TcInv> one(1);
+  one[0].g = g;
+  one[0].s = s;
+  one[0].t = t;
+  one[0].bimg = bimg;
+  long long nb = 0, nt = 0;
+  tcp_layout_insts(one.data(), 1, vec, &nb, &nt);
+  const InstIndex X{};
+  const TcInv& o = one[0];
+  if (tf32)
+    return vec ? launch_inv_p<true, true, false>(o, nullptr, X, nb, nt, st)
+               : launch_inv_p<false, true, false>(o, nullptr, X, nb, nt, st);
+  return vec ? launch_inv_p<true, false, false>(o, nullptr, X, nb, nt, st)
+             : launch_inv_p<false, false, false>(o, nullptr, X, nb, nt, st);
 }
 
 cudaError_t launch_fwd_legendre_tcp(const ShtGeom& g, const FwdSet& s, bool vec, bool tf32, const TcTables& t,
                                     unsigned char* bimg, cudaStream_t st) {
-  if (tf32) return vec ? launch_fwd_p<true, true>(g, s, t, bimg, st) : launch_fwd_p<false, true>(g, s, t, bimg, st);
-  return vec ? launch_fwd_p<true, false>(g, s, t, bimg, st) : launch_fwd_p<false, false>(g, s, t, bimg, st);
+  std::vector<TcFwd> one(1);
+  one[0].g = g;
+  one[0].s = s;
+  one[0].t = t;
+  one[0].bimg = bimg;
+  long long nb = 0, nt = 0;
+  tcp_layout_insts(one.data(), 1, vec, &nb, &nt);
+  const InstIndex X{};
+  const TcFwd& o = one[0];
+  if (tf32)
+    return vec ? launch_fwd_p<true, true, false>(o, nullptr, X, nb, nt, st)
+               : launch_fwd_p<false, true, false>(o, nullptr, X, nb, nt, st);
+  return vec ? launch_fwd_p<true, false, false>(o, nullptr, X, nb, nt, st)
+             : launch_fwd_p<false, false, false>(o, nullptr, X, nb, nt, st);
+}
+
+// several instances of the 3xBF16 form in one pack + one persistent launch
+cudaError_t launch_inv_legendre_tcp_multi(const LegInst<InvSet>* inst, const LegInst<InvSet>* d_inst, int n,
+                                          bool vec, long long nblocks, long long ntiles, cudaStream_t st) {
+  if (n < 1 || n > kMaxGroupInst) return cudaErrorInvalidValue;
+  const InstIndex X = inst_index(inst, n);
+  return vec ? launch_inv_p<true, false, true>(inst[0], d_inst, X, nblocks, ntiles, st)
+             : launch_inv_p<false, false, true>(inst[0], d_inst, X, nblocks, ntiles, st);
+}
+
+cudaError_t launch_fwd_legendre_tcp_multi(const LegInst<FwdSet>* inst, const LegInst<FwdSet>* d_inst, int n,
+                                          bool vec, long long nblocks, long long ntiles, cudaStream_t st) {
+  if (n < 1 || n > kMaxGroupInst) return cudaErrorInvalidValue;
+  const InstIndex X = inst_index(inst, n);
+  return vec ? launch_fwd_p<true, false, true>(inst[0], d_inst, X, nblocks, ntiles, st)
+             : launch_fwd_p<false, false, true>(inst[0], d_inst, X, nblocks, ntiles, st);
 }

@@ -11,6 +11,7 @@
 #include <functional>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/magic_sht.h"
@@ -121,6 +122,30 @@ struct magic_sht_handle {
   double phase_ms[MAGIC_SHT_N_PHASES] = {0};
   long long phase_launches[MAGIC_SHT_N_PHASES] = {0};
   long long launches = 0;
+  // a group call (magic_sht_group_*) collects this handle's tensor-core
+  // Legendre and FFT launches here instead of issuing them; defer_bimg counts
+  // the data-image bytes its collected Legendre launches need
+  struct Deferred* defer = nullptr;
+  size_t defer_bimg = 0;
+};
+
+// Launches of the handles of one group call, held back so that the Legendre
+// launches of every instance run as one pack + one persistent kernel per kind.
+struct Deferred {
+  struct Leg {
+    magic_sht_handle* h;
+    bool inverse, vec;
+    InvSet inv;
+    FwdSet fwd;
+    size_t bimg_off;  // in h->d_bimg
+  };
+  struct Fft {
+    magic_sht_handle* h;
+    bool inverse;
+    FftSet fs;
+  };
+  std::vector<Leg> leg;
+  std::vector<Fft> fft;
 };
 
 struct magic_sht_graph {
@@ -244,7 +269,23 @@ int ensure_bimg(magic_sht_handle* h, size_t bytes) {
   h->bimg_bytes = nb;
   return MAGIC_SHT_OK;
 }
+// a Legendre launch of a group call: recorded with its data-image offset
+int defer_leg(magic_sht_handle* h, const InvSet* inv, const FwdSet* fwd, bool vec) {
+  Deferred::Leg j{};
+  j.h = h;
+  j.inverse = inv != nullptr;
+  j.vec = vec;
+  if (inv) j.inv = *inv;
+  if (fwd) j.fwd = *fwd;
+  const int ncplx = inv ? inv->nf * inv->nlev * (vec ? 2 : 1) : fwd->nf * fwd->nlev * (vec ? 2 : 1);
+  j.bimg_off = h->defer_bimg;
+  h->defer_bimg += align256(oz_form(h) ? oz_data_bytes(h->g, h->tct, ncplx, inv != nullptr)
+                                       : tcp_data_bytes(h->g, h->tct, ncplx, vec, inv != nullptr, tf32_form(h)));
+  h->defer->leg.push_back(j);
+  return MAGIC_SHT_OK;
+}
 int inv_tc(magic_sht_handle* h, const ShtGeom& g, const InvSet& s, bool vec) {
+  if (h->defer) return defer_leg(h, &s, nullptr, vec);
   if (oz_form(h)) {
     TRY(ensure_bimg(h, oz_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), true)));
     h->launches++;  // pack kernel + persistent kernel
@@ -261,6 +302,7 @@ int inv_tc(magic_sht_handle* h, const ShtGeom& g, const InvSet& s, bool vec) {
   return MAGIC_SHT_OK;
 }
 int fwd_tc(magic_sht_handle* h, const ShtGeom& g, const FwdSet& s, bool vec) {
+  if (h->defer) return defer_leg(h, nullptr, &s, vec);
   if (oz_form(h)) {
     TRY(ensure_bimg(h, oz_data_bytes(g, h->tct, s.nf * s.nlev * (vec ? 2 : 1), false)));
     h->launches++;  // pack kernel + persistent kernel
@@ -300,6 +342,7 @@ struct PhaseScope {
   cudaEvent_t e1 = nullptr;
   // `nk` kernels launched inside the scope (timed together)
   PhaseScope(magic_sht_handle* h_, int ph_, int nk = 1) : h(h_), ph(ph_) {
+    if (h->defer) return;  // collected for a group launch: counted there
     h->launches += nk;
     h->phase_launches[ph] += nk;
     if (h->profiling && !h->capturing) {
@@ -513,6 +556,10 @@ int run_inverse(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
   FftSet fs{};
   fs.nlev = lv.nlev;
   auto flush_fft = [&]() -> int {
+    if (fs.nf && h->defer) {
+      h->defer->fft.push_back({h, true, fs});
+      fs.nf = 0;
+    }
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_INV);
       CK(launch_fft_inverse(g, fs, fft_arith(h), h->fft_rows, h->stream));
@@ -596,6 +643,10 @@ int run_forward(magic_sht_handle* h, CallCtx& cx, const LevelCtl& lv,
   FftSet fs{};
   fs.nlev = lv.nlev;
   auto flush_fft = [&]() -> int {
+    if (fs.nf && h->defer) {
+      h->defer->fft.push_back({h, false, fs});
+      fs.nf = 0;
+    }
     if (fs.nf) {
       PhaseScope ps(h, MAGIC_SHT_PHASE_FFT_FWD);
       CK(launch_fft_forward(g, fs, fft_arith(h), h->fft_rows, h->stream));
@@ -2038,6 +2089,268 @@ int magic_sht_graph_destroy(magic_sht_graph* gr) {
   if (gr->graph) cudaGraphDestroy(gr->graph);
   delete gr;
   return MAGIC_SHT_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ groups
+// Several instances (handles of different l_max, minc and grids, all in the
+// FP64-accurate or all in the 3xBF16 tensor-core form) transformed together: each handle builds
+// its call as usual, but its Legendre and FFT launches are collected
+// (magic_sht_handle::defer); then one pack + one persistent tensor-core launch
+// per direction and field kind covers the tiles of every instance, heaviest
+// instances first, and the FFTs follow (synthesis) or precede (analysis).
+struct magic_sht_group {
+  std::vector<magic_sht_handle*> h;
+  int device = 0;
+  // Device copies of the launches' instance arrays, append-only while the
+  // group lives (a graph captured from a group call reads the copies it was
+  // captured with); an identical array is uploaded once.
+  struct Chunk {
+    char* host = nullptr;  // pinned: the source of the asynchronous copies
+    char* dev = nullptr;
+    size_t cap = 0, used = 0;
+  };
+  std::vector<Chunk> chunks;
+  struct Slot {
+    const char* host;
+    const char* dev;
+    size_t bytes;
+  };
+  std::vector<Slot> slots;
+};
+
+namespace {
+
+static_assert(sizeof(ShtGeom) == 10 * 4 + 10 * 8, "ShtGeom holds padding bytes");
+static_assert(sizeof(InvSet) == MAGIC_MAX_FIELDS * sizeof(InvField) + 40, "InvSet holds padding bytes");
+static_assert(sizeof(FwdSet) == MAGIC_MAX_FIELDS * sizeof(FwdField) + 24, "FwdSet holds padding bytes");
+static_assert(sizeof(TcTables) == 12 * 8 + 4 * 4, "TcTables holds padding bytes");
+static_assert(sizeof(LegInst<InvSet>) == sizeof(ShtGeom) + sizeof(InvSet) + sizeof(TcTables) + 32,
+              "LegInst holds padding bytes");
+
+constexpr size_t kGroupChunk = 1 << 20;
+
+int group_upload(magic_sht_group* G, const void* p, size_t bytes, bool capturing, cudaStream_t st,
+                 const void** out) {
+  for (const auto& sl : G->slots)
+    if (sl.bytes == bytes && !memcmp(sl.host, p, bytes)) {
+      *out = sl.dev;
+      return MAGIC_SHT_OK;
+    }
+  const size_t need = align256(bytes);
+  if (G->chunks.empty() || G->chunks.back().used + need > G->chunks.back().cap) {
+    if (capturing)
+      return set_err(MAGIC_SHT_ERR_NOMEM,
+                     "group instance tables full during graph capture: make the same calls once before capturing");
+    magic_sht_group::Chunk c;
+    c.cap = std::max(kGroupChunk, need);
+    CK(cudaHostAlloc((void**)&c.host, c.cap, cudaHostAllocDefault));
+    if (cudaMalloc((void**)&c.dev, c.cap) != cudaSuccess) {
+      cudaFreeHost(c.host);
+      cudaGetLastError();
+      return set_err(MAGIC_SHT_ERR_NOMEM, "group instance tables: cudaMalloc of %zu bytes failed", c.cap);
+    }
+    G->chunks.push_back(c);
+  }
+  magic_sht_group::Chunk& c = G->chunks.back();
+  char* hp = c.host + c.used;
+  char* dp = c.dev + c.used;
+  c.used += need;
+  memcpy(hp, p, bytes);
+  CK(cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, st));
+  G->slots.push_back({hp, dp, bytes});
+  *out = dp;
+  return MAGIC_SHT_OK;
+}
+
+// one pack + one persistent launch over the collected Legendre launches of
+// one direction and field kind
+template <class Set>
+int group_legendre(magic_sht_group* G, const Deferred& D, bool inverse, bool vec, bool capturing, cudaStream_t st) {
+  std::vector<LegInst<Set>> v;
+  for (const auto& j : D.leg) {
+    if (j.inverse != inverse || j.vec != vec) continue;
+    LegInst<Set> I;
+    memset(&I, 0, sizeof(I));
+    I.g = j.h->g;
+    if constexpr (std::is_same<Set, InvSet>::value) I.s = j.inv;
+    else I.s = j.fwd;
+    I.t = j.h->tct;
+    I.bimg = j.h->d_bimg + j.bimg_off;
+    if (I.s.nf * I.s.nlev > 0) v.push_back(I);
+  }
+  if (v.empty()) return MAGIC_SHT_OK;
+  if (v.size() > (size_t)kMaxGroupInst)
+    return set_err(MAGIC_SHT_ERR_SIZE, "group call of %zu instance sets of one kind (at most %d)", v.size(),
+                   kMaxGroupInst);
+  // the heaviest tiles (the largest l_max) are handed out first
+  std::stable_sort(v.begin(), v.end(),
+                   [](const LegInst<Set>& a, const LegInst<Set>& b) { return a.g.l_max > b.g.l_max; });
+  magic_sht_handle* h0 = G->h[0];
+  const bool oz = oz_form(h0);
+  long long nblocks = 0, ntiles = 0;
+  if (oz) oz_layout_insts(v.data(), (int)v.size(), vec, &nblocks, &ntiles);
+  else tcp_layout_insts(v.data(), (int)v.size(), vec, &nblocks, &ntiles);
+  if (ntiles >= (1LL << 31) || nblocks >= (1LL << 31))
+    return set_err(MAGIC_SHT_ERR_SIZE, "group call of %lld tiles: split it", ntiles);
+  const void* dv = nullptr;
+  TRY(group_upload(G, v.data(), v.size() * sizeof(LegInst<Set>), capturing, st, &dv));
+  const int ph = inverse ? (vec ? MAGIC_SHT_PHASE_INV_LEG_VECTOR : MAGIC_SHT_PHASE_INV_LEG_SCALAR)
+                         : (vec ? MAGIC_SHT_PHASE_FWD_LEG_VECTOR : MAGIC_SHT_PHASE_FWD_LEG_SCALAR);
+  PhaseScope ps(h0, ph, 2);
+  const int n = (int)v.size();
+  if constexpr (std::is_same<Set, InvSet>::value) {
+    const LegInst<InvSet>* d = (const LegInst<InvSet>*)dv;
+    CK(oz ? launch_inv_legendre_oz_multi(v.data(), d, n, vec, nblocks, ntiles, st)
+          : launch_inv_legendre_tcp_multi(v.data(), d, n, vec, nblocks, ntiles, st));
+  } else {
+    const LegInst<FwdSet>* d = (const LegInst<FwdSet>*)dv;
+    CK(oz ? launch_fwd_legendre_oz_multi(v.data(), d, n, vec, nblocks, ntiles, st)
+          : launch_fwd_legendre_tcp_multi(v.data(), d, n, vec, nblocks, ntiles, st));
+  }
+  return MAGIC_SHT_OK;
+}
+
+int group_ffts(const Deferred& D, bool inverse, cudaStream_t st) {
+  for (const auto& f : D.fft) {
+    if (f.inverse != inverse) continue;
+    magic_sht_handle* h = f.h;
+    PhaseScope ps(h, inverse ? MAGIC_SHT_PHASE_FFT_INV : MAGIC_SHT_PHASE_FFT_FWD);
+    if (inverse) CK(launch_fft_inverse(h->g, f.fs, fft_arith(h), h->fft_rows, st));
+    else CK(launch_fft_forward(h->g, f.fs, fft_arith(h), h->fft_rows, st));
+  }
+  return MAGIC_SHT_OK;
+}
+
+// a group call: the checks, then every instance's call with its launches
+// collected, then the group launches
+int group_call(magic_sht_group* G, bool inverse, const std::vector<const void*>& arrays,
+               const std::function<int(int)>& call) {
+  if (!G) return set_err(MAGIC_SHT_ERR_ARG, "null group");
+  magic_sht_handle* h0 = G->h[0];
+  const cudaStream_t st = h0->stream;
+  for (magic_sht_handle* h : G->h) {
+    if (h->stream != st)
+      return set_err(MAGIC_SHT_ERR_ARG, "the handles of a group share one stream (magic_sht_set_stream)");
+    if (!h->tc_persistent)
+      return set_err(MAGIC_SHT_ERR_UNSUPPORTED, "group calls need the persistent tensor-core kernels (tc_kernel 0)");
+  }
+  for (const void* p : arrays)
+    if (p && !is_device_ptr(p))
+      return set_err(MAGIC_SHT_ERR_ARG, "group calls take device arrays for the spectra and grids");
+  DeviceGuard dg(G->device);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(st, &cs));
+  const bool capturing = cs == cudaStreamCaptureStatusActive;
+  Deferred D;
+  std::vector<char> was(G->h.size());
+  int rc = MAGIC_SHT_OK;
+  for (size_t i = 0; i < G->h.size() && rc == MAGIC_SHT_OK; ++i) {
+    magic_sht_handle* h = G->h[i];
+    was[i] = h->capturing;
+    h->capturing = h->capturing || capturing;
+    h->defer = &D;
+    h->defer_bimg = 0;
+    rc = call((int)i);
+    h->defer = nullptr;
+  }
+  for (size_t i = 0; i < G->h.size() && rc == MAGIC_SHT_OK; ++i)
+    if (G->h[i]->defer_bimg) rc = ensure_bimg(G->h[i], G->h[i]->defer_bimg);
+  if (rc == MAGIC_SHT_OK) {
+    if (inverse) {
+      rc = group_legendre<InvSet>(G, D, true, false, capturing, st);
+      if (!rc) rc = group_legendre<InvSet>(G, D, true, true, capturing, st);
+      if (!rc) rc = group_ffts(D, true, st);
+    } else {
+      rc = group_ffts(D, false, st);
+      if (!rc) rc = group_legendre<FwdSet>(G, D, false, false, capturing, st);
+      if (!rc) rc = group_legendre<FwdSet>(G, D, false, true, capturing, st);
+    }
+  }
+  for (size_t i = 0; i < G->h.size(); ++i) G->h[i]->capturing = was[i];
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int magic_sht_group_create(magic_sht_handle* const* handles, int n, magic_sht_group** out) {
+  if (!handles || !out || n <= 0) return set_err(MAGIC_SHT_ERR_ARG, "null handles/output or n <= 0");
+  if (n > kMaxGroupInst) return set_err(MAGIC_SHT_ERR_SIZE, "a group holds at most %d handles", kMaxGroupInst);
+  for (int i = 0; i < n; ++i) {
+    if (!handles[i]) return set_err(MAGIC_SHT_ERR_ARG, "null handle %d", i);
+    if (handles[i]->device != handles[0]->device)
+      return set_err(MAGIC_SHT_ERR_ARG, "the handles of a group are on one device");
+    const int pr = handles[i]->precision;
+    if (pr != MAGIC_SHT_FP64TC && pr != MAGIC_SHT_BF16X3)
+      return set_err(MAGIC_SHT_ERR_UNSUPPORTED,
+                     "group calls need the FP64-accurate or the 3xBF16 tensor-core form (handle %d)", i);
+    if (pr != handles[0]->precision)
+      return set_err(MAGIC_SHT_ERR_ARG, "the handles of a group share one arithmetic form (handle %d)", i);
+    for (int k = 0; k < i; ++k)
+      if (handles[k] == handles[i]) return set_err(MAGIC_SHT_ERR_ARG, "handle %d appears twice in the group", i);
+  }
+  magic_sht_group* G = new magic_sht_group();
+  G->h.assign(handles, handles + n);
+  G->device = handles[0]->device;
+  *out = G;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_group_destroy(magic_sht_group* G) {
+  if (!G) return MAGIC_SHT_OK;
+  DeviceGuard dg(G->device);
+  cudaDeviceSynchronize();
+  for (auto& c : G->chunks) {
+    if (c.dev) cudaFree(c.dev);
+    if (c.host) cudaFreeHost(c.host);
+  }
+  delete G;
+  return MAGIC_SHT_OK;
+}
+
+int magic_sht_group_transform_to_grid_space(magic_sht_group* G, const int* n_levels, const double* const* or2,
+                                            const int* const* lcut, const magic_sht_grid_space_args* a) {
+  if (!G || !n_levels || !a) return set_err(MAGIC_SHT_ERR_ARG, "null group, n_levels or args");
+  std::vector<const void*> arr;
+  for (size_t i = 0; i < G->h.size(); ++i) {
+    const magic_sht_grid_space_args& b = a[i];
+    for (const void* p : {(const void*)b.s, (const void*)b.p, (const void*)b.xi, (const void*)b.w,
+                          (const void*)b.dw, (const void*)b.ddw, (const void*)b.z, (const void*)b.dz,
+                          (const void*)b.b, (const void*)b.db, (const void*)b.ddb, (const void*)b.aj,
+                          (const void*)b.dj, (const void*)b.sc, (const void*)b.pc, (const void*)b.xic,
+                          (const void*)b.vrc, (const void*)b.vtc, (const void*)b.vpc, (const void*)b.cvrc,
+                          (const void*)b.cvtc, (const void*)b.cvpc, (const void*)b.brc, (const void*)b.btc,
+                          (const void*)b.bpc, (const void*)b.cbrc, (const void*)b.cbtc, (const void*)b.cbpc})
+      arr.push_back(p);
+  }
+  return group_call(G, true, arr, [&](int i) {
+    return magic_sht_transform_to_grid_space(G->h[i], n_levels[i], or2 ? or2[i] : nullptr,
+                                             lcut ? lcut[i] : nullptr, &a[i]);
+  });
+}
+
+int magic_sht_group_transform_to_lm_space(magic_sht_group* G, const int* n_levels, const int* const* lcut,
+                                          const magic_sht_lm_space_args* a) {
+  if (!G || !n_levels || !a) return set_err(MAGIC_SHT_ERR_ARG, "null group, n_levels or args");
+  std::vector<const void*> arr;
+  for (size_t i = 0; i < G->h.size(); ++i) {
+    const magic_sht_lm_space_args& b = a[i];
+    for (const void* p :
+         {(const void*)b.Advr, (const void*)b.Advt, (const void*)b.Advp, (const void*)b.VSr, (const void*)b.VSt,
+          (const void*)b.VSp, (const void*)b.VxBr, (const void*)b.VxBt, (const void*)b.VxBp,
+          (const void*)b.heatTerms, (const void*)b.AdvrLM, (const void*)b.AdvtLM, (const void*)b.AdvpLM,
+          (const void*)b.VSrLM, (const void*)b.VStLM, (const void*)b.VSpLM, (const void*)b.VxBrLM,
+          (const void*)b.VxBtLM, (const void*)b.VxBpLM, (const void*)b.heatTermsLM, (const void*)b.VXir,
+          (const void*)b.VXit, (const void*)b.VXip, (const void*)b.VXirLM, (const void*)b.VXitLM,
+          (const void*)b.VXipLM})
+      arr.push_back(p);
+  }
+  return group_call(G, false, arr, [&](int i) {
+    return magic_sht_transform_to_lm_space(G->h[i], n_levels[i], lcut ? lcut[i] : nullptr, &a[i]);
+  });
 }
 
 // ------------------------------------------------------------ profiling

@@ -303,9 +303,9 @@ class SHT:
     def _levels(self, arr, n, lcut):
         return _per_level(lcut, np.int32, n, "lcut")
 
-    def transform_to_grid_space(self, spec: dict, or2=None, lcut=None, out: Optional[dict] = None):
-        """rIter.f90:466-622 for many radial levels; `spec` maps the names of
-        _lib.GRID_SPACE_IN to (n_levels, lm_max) arrays; returns the grid dict."""
+    def _grid_space_call(self, spec: dict, or2, lcut, out):
+        """The argument block of one transform_to_grid_space call: (n, args,
+        outputs, or2 pointer, lcut pointer, arrays to keep alive)."""
         keys = [k for k in _lib.GRID_SPACE_IN if spec.get(k) is not None]
         first = spec[keys[0]]
         n = int(first.shape[0])
@@ -332,12 +332,19 @@ class SHT:
         a.grid_ld = self.n_phi_max * self.nlat_padded
         or2_arr, por2 = _per_level(or2, np.float64, n, "or2")
         lc_arr, plc = self._levels(first, n, lcut)
+        keep += [or2_arr, lc_arr]
+        return n, a, outs, por2, plc, keep
+
+    def transform_to_grid_space(self, spec: dict, or2=None, lcut=None, out: Optional[dict] = None):
+        """rIter.f90:466-622 for many radial levels; `spec` maps the names of
+        _lib.GRID_SPACE_IN to (n_levels, lm_max) arrays; returns the grid dict."""
+        n, a, outs, por2, plc, keep = self._grid_space_call(spec, or2, lcut, out)
         check(self._lib.magic_sht_transform_to_grid_space(self._h, n, por2, plc, ctypes.byref(a)))
         return outs
 
-    def transform_to_lm_space(self, grids: dict, lcut=None, out: Optional[dict] = None):
-        """rIter.f90:624-712 for many radial levels (also V Xi -> VXirLM,
-        VXitLM, VXipLM when ``VXir`` .. ``VXip`` are given)."""
+    def _lm_space_call(self, grids: dict, lcut, out):
+        """The argument block of one transform_to_lm_space call: (n, args,
+        outputs, lcut pointer, arrays to keep alive)."""
         names_in = _lib.LM_SPACE_IN + _lib.LM_SPACE_IN_XI
         names_out = _lib.LM_SPACE_OUT + _lib.LM_SPACE_OUT_XI
         keys = [k for k in names_in if grids.get(k) is not None]
@@ -359,6 +366,13 @@ class SHT:
             setattr(a, kout, outs[kout].data_ptr() if _is_torch(outs[kout]) else outs[kout].ctypes.data)
         a.spec_ld = self.lm_max
         lc_arr, plc = self._levels(first, n, lcut)
+        keep.append(lc_arr)
+        return n, a, outs, plc, keep
+
+    def transform_to_lm_space(self, grids: dict, lcut=None, out: Optional[dict] = None):
+        """rIter.f90:624-712 for many radial levels (also V Xi -> VXirLM,
+        VXitLM, VXipLM when ``VXir`` .. ``VXip`` are given)."""
+        n, a, outs, plc, keep = self._lm_space_call(grids, lcut, out)
         check(self._lib.magic_sht_transform_to_lm_space(self._h, n, plc, ctypes.byref(a)))
         return outs
 
@@ -720,6 +734,69 @@ class SHT:
 
     def graph_destroy(self, g):
         check(self._lib.magic_sht_graph_destroy(g))
+
+
+class SHTGroup:
+    """Several independent instances (SHT handles of different l_max, minc and
+    grids, all precision="fp64tc" or all "bf16x3") transformed together
+    (magic_sht_group_*): the Legendre sums of every instance run as one pack
+    and one persistent tensor-core launch per direction and field kind, with
+    results equal to the instances' own calls bit for bit.  Spectra and grids
+    are CUDA tensors; every call runs on torch's current stream, to which all
+    instances are bound."""
+
+    def __init__(self, shts):
+        self.shts = list(shts)
+        self._lib = _lib.load()
+        arr = (ctypes.c_void_p * len(self.shts))(*[s._h.value for s in self.shts])
+        g = ctypes.c_void_p()
+        check(self._lib.magic_sht_group_create(arr, len(self.shts), ctypes.byref(g)))
+        self._g = g
+
+    def close(self):
+        if getattr(self, "_g", None):
+            self._lib.magic_sht_group_destroy(self._g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _bind(self):
+        for s in self.shts:
+            s._bind_torch_stream()
+
+    def transform_to_grid_space(self, specs, or2s=None, lcuts=None, outs=None):
+        """specs[i] (and or2s[i], lcuts[i], outs[i]) as
+        SHT.transform_to_grid_space of instance i; returns the list of grid dicts."""
+        k = len(self.shts)
+        or2s = or2s or [None] * k
+        lcuts = lcuts or [None] * k
+        outs = outs or [None] * k
+        calls = [s._grid_space_call(specs[i], or2s[i], lcuts[i], outs[i]) for i, s in enumerate(self.shts)]
+        self._bind()
+        n = (ctypes.c_int * k)(*[c[0] for c in calls])
+        args = (_lib.GridSpaceArgs * k)(*[c[1] for c in calls])
+        por2 = (ctypes.c_void_p * k)(*[c[3] for c in calls])
+        plc = (ctypes.c_void_p * k)(*[c[4] for c in calls])
+        check(self._lib.magic_sht_group_transform_to_grid_space(self._g, n, por2, plc, args))
+        return [c[2] for c in calls]
+
+    def transform_to_lm_space(self, grids, lcuts=None, outs=None):
+        """grids[i] (and lcuts[i], outs[i]) as SHT.transform_to_lm_space of
+        instance i; returns the list of spectral dicts."""
+        k = len(self.shts)
+        lcuts = lcuts or [None] * k
+        outs = outs or [None] * k
+        calls = [s._lm_space_call(grids[i], lcuts[i], outs[i]) for i, s in enumerate(self.shts)]
+        self._bind()
+        n = (ctypes.c_int * k)(*[c[0] for c in calls])
+        args = (_lib.LmSpaceArgs * k)(*[c[1] for c in calls])
+        plc = (ctypes.c_void_p * k)(*[c[3] for c in calls])
+        check(self._lib.magic_sht_group_transform_to_lm_space(self._g, n, plc, args))
+        return [c[2] for c in calls]
 
 
 def dt_courant(dtrkc, dthkc, dt: float, dtMax: float):
