@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x2", "fp64tc", "fp64"])
+    ap.add_argument("--form", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x2", "fp64tc", "bf16x5", "fp64"])
     ap.add_argument("--cpu-levels", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -442,7 +442,7 @@ def config_measure(name, L, minc, N, P, R, forms, local, hbm, full_set=True, bat
     batch = batch or R
     res = {"workload": what, "l_max": L, "minc": minc, "n_theta": N, "n_phi": P, "levels": R, "forms": {}}
     ref = None
-    t2_of = {"fp64": 16, "fp64tc": 16}
+    t2_of = {"fp64": 16, "fp64tc": 16, "bf16x5": 16}
     for form in forms:
         s = SHT(L, minc, N, P, precision=form, device=local)
         s.reserve(batch)
@@ -656,7 +656,7 @@ def our_arm(args):
     # ---- the other precision forms: same step, timing and accuracy, beside the headline
     others = {}
     if not args.no_variant:
-        for f in ("bf16x3", "tf32x2"):
+        for f in ("fp64tc", "bf16x5", "bf16x3", "tf32x2"):
             if f == form:
                 continue
             sv = SHT(L_MAX, MINC, N_THETA, N_PHI, precision=f, device=local)
@@ -691,11 +691,11 @@ def our_arm(args):
     ph64 = s64.phase_times(reset=True)
     s64.set_profiling(False)
 
-    t2 = 16 if form in ("fp64", "fp64tc") else 8
+    t2 = 16 if form in ("fp64", "fp64tc", "bf16x5") else 8
     alg, K = algorithmic_per_level(L_MAX, N_THETA, N_PHI, MINC, t2)
     # table bytes per Legendre launch: the split images (7 bf16 digits for
-    # fp64tc, 3 bf16 for bf16x3, 2 tf32 for tf32x2) of P and dP
-    tab_elem = {"fp64tc": 14, "bf16x3": 6, "tf32x2": 8, "fp32": 4, "fp64": 8}[form]
+    # fp64tc, 5 for bf16x5, 3 bf16 for bf16x3, 2 tf32 for tf32x2) of P and dP
+    tab_elem = {"fp64tc": 14, "bf16x5": 10, "bf16x3": 6, "tf32x2": 8, "fp32": 4, "fp64": 8}[form]
     dom = max(ph, key=lambda k: ph[k][0])
     dom_ms, dom_n = ph[dom]
     per_launch_ms = dom_ms / max(dom_n, 1)
@@ -726,7 +726,7 @@ def our_arm(args):
         roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                 "frac": achieved_gbs / hbm, "traffic": traffic, "kernel": dom,
                 "peak_source": peak_kind}
-        if form == "fp64tc" and "fft" in dom:
+        if form in ("fp64tc", "bf16x5") and "fft" in dom:
             # the double-float FFTs execute ~10 FP32 operations per FP32-FFT operation:
             # their binding pipe is FP32 issue; the FP32 probe beside the HBM figure
             roof["note"] = ("double-float FFT: FP32-pipe bound (HBM fraction reported as the contract's "
@@ -748,10 +748,11 @@ def our_arm(args):
             fl = alg[k]["flops"] * N_LEVELS
             v["achieved_tflops"] = fl / sec / 1e12
             v["tensor_frac_of_bf16_peak"] = v["achieved_tflops"] / bf16 if bf16 else None
-            if form == "fp64tc":
-                # 28 digit products per algorithmic multiply-add
-                v["digit_product_tflops"] = 28 * v["achieved_tflops"]
-                v["digit_product_frac_of_bf16_peak"] = 28 * v["achieved_tflops"] / bf16 if bf16 else None
+            if form in ("fp64tc", "bf16x5"):
+                # 28 (seven digits) or 15 (five digits) digit products per algorithmic multiply-add
+                nprod = 28 if form == "fp64tc" else 15
+                v["digit_product_tflops"] = nprod * v["achieved_tflops"]
+                v["digit_product_frac_of_bf16_peak"] = nprod * v["achieved_tflops"] / bf16 if bf16 else None
     phases64 = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in ph64.items() if v[1]}
     # FP64 form's Legendre against the FP64 pipe
     leg64_ms = sum(v[0] for k, v in ph64.items() if "leg" in k)
@@ -838,7 +839,8 @@ def our_arm(args):
             "median_ms_per_step": statistics.median(per_step), "timing": "graph replay of one step, CUDA events per step",
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp32": "f32", "bf16x3": "bf16x3+f32", "tf32x2": "tf32x2+f32", "fp64": "f64",
-                      "fp64tc": "bf16 digits x7 + exact f32 accumulate; f32x2 FFT"}[form],
+                      "fp64tc": "bf16 digits x7 + exact f32 accumulate; f32x2 FFT",
+                      "bf16x5": "bf16 digits x5 + exact f32 accumulate; f32x2 FFT"}[form],
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": form, "l_max": L_MAX, "n_theta": N_THETA,
                        "n_phi": N_PHI, "minc": MINC, "n_levels": N_LEVELS,

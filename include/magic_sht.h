@@ -44,6 +44,9 @@ extern "C" {
 #define MAGIC_SHT_FP64TC 4  /* FP64-accurate on tensor cores: seven fixed-point BF16 digits per operand, 28 digit
                                products accumulated exactly in FP32, double-float (FP32-pair) FFTs and
                                half spectra, FP64 radial-loop kernels; values within the FP32 exponent range */
+#define MAGIC_SHT_BF16X5 5  /* the same tensor-core form with five fixed-point BF16 digits per operand (15 digit
+                               products, the dropped digits below 2^-39 of the row and column scales): double-float
+                               FFTs and half spectra, FP64 radial-loop kernels, the FP32 exponent range */
 
 typedef struct magic_sht_desc {
   int l_max;       /* truncation degree (truncation.f90 l_max) */
@@ -52,7 +55,7 @@ typedef struct magic_sht_desc {
   int n_theta_max; /* Gauss points, multiple of 4 (truncation.f90:150) */
   int n_phi_max;   /* longitudes per symmetry sector, multiple of 4, 2^i 3^j 5^k */
   int nlat_padded; /* leading dimension of grid arrays; 0 -> n_theta_max */
-  int precision;   /* MAGIC_SHT_FP64 | _FP32 | _BF16X3 | _TF32X2 | _FP64TC */
+  int precision;   /* MAGIC_SHT_FP64 | _FP32 | _BF16X3 | _TF32X2 | _FP64TC | _BF16X5 */
   int device;      /* CUDA device ordinal; -1 -> current device */
 } magic_sht_desc;
 
@@ -407,8 +410,8 @@ int magic_sht_graph_destroy(magic_sht_graph* graph);
 
 /* ---- several independent instances in one launch per kind.  A group holds
  * handles of different l_max / minc / grids (each its own initialize_transforms,
- * all MAGIC_SHT_FP64TC or all MAGIC_SHT_BF16X3, with the persistent
- * tensor-core kernels, one device).
+ * all MAGIC_SHT_FP64TC, all MAGIC_SHT_BF16X5 or all MAGIC_SHT_BF16X3, with the
+ * persistent tensor-core kernels, one device).
  * A group call runs the batched call of every instance (argument i for handle
  * i, the same meaning as magic_sht_transform_to_grid_space /
  * magic_sht_transform_to_lm_space), but the Legendre sums of all instances go

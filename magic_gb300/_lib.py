@@ -14,8 +14,8 @@ LIB_PATH = os.path.join(HERE, "libmagic_sht.so")
 
 OK = 0
 ERR_ARG, ERR_SIZE, ERR_LCUT, ERR_CUDA, ERR_UNSUPPORTED, ERR_NOMEM, ERR_TIMEOUT = range(1, 8)
-FP64, FP32, BF16X3, TF32X2, FP64TC = 0, 1, 2, 3, 4
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16x3": BF16X3, "tf32x2": TF32X2, "fp64tc": FP64TC}
+FP64, FP32, BF16X3, TF32X2, FP64TC, BF16X5 = 0, 1, 2, 3, 4, 5
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16x3": BF16X3, "tf32x2": TF32X2, "fp64tc": FP64TC, "bf16x5": BF16X5}
 PHASES = ["inv_leg_scalar", "inv_leg_vector", "fft_inv", "fft_fwd", "fwd_leg_scalar",
           "fwd_leg_vector", "nl", "courant", "td", "bcs"]
 

@@ -148,6 +148,8 @@ struct TcTables {
   int ncj;                    // theta chunks of 64 (analysis K)
   int order;                  // tile order of the persistent kernels: 0 = consecutive tiles
                               // share the table block, 1 = they share the data block
+  int ndig;                   // fixed-point digits per operand of the FP64TC / BF16X5 forms (7 / 5)
+  int pad_;
 };
 
 // grids of the nonlinear products (nl.cu): inputs from the synthesis set,

@@ -81,9 +81,10 @@ cudaError_t launch_lorentz_torque(const ShtGeom& g, const double* theta, const d
 cudaError_t launch_courant(const ShtGeom& g, const CourantArgs& a, int nlev, unsigned long long* mx, double* dtrkc,
                            double* dthkc, cudaStream_t st);
 
-// legendre_oz.cu: the FP64-accurate tensor-core form (six fixed-point BF16
-// digits per operand, exact FP32 accumulation); TcTables with inv_exp / fwd_exp
-void oz_table_layout(const ShtGeom& g, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
+// legendre_oz.cu: the fixed-point tensor-core forms (seven (FP64TC) or five
+// (BF16X5) BF16 digits per operand, TcTables::ndig, exact FP32 accumulation);
+// TcTables with inv_exp / fwd_exp
+void oz_table_layout(const ShtGeom& g, int digits, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
                      std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks);
 cudaError_t build_oz_images(const ShtGeom& g, const TcTables& t, unsigned char* inv_img, short* inv_exp,
                             unsigned char* fwd_img, short* fwd_exp, cudaStream_t st);

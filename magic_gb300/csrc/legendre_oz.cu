@@ -48,9 +48,18 @@
 
 namespace {
 
-constexpr int kS = 7;                    // digits per operand
+// Digits per operand S: 7 (MAGIC_SHT_FP64TC) or 5 (MAGIC_SHT_BF16X5); every
+// kernel below is a template on S, with kS = S, kTS its data-tile bytes and
+// kFix its fixed-point position.
 constexpr int kNC = 32;                  // real data columns per tile (16 complex)
-constexpr uint32_t kTS = kS * kNC * 128; // data tile: 7 digit blocks of 32 rows x 64 K bf16 (28 KB)
+// data tile: S digit blocks of 32 rows x 64 K bf16 (4 KB each)
+__host__ __device__ constexpr uint32_t tile_bytes(int S) { return (uint32_t)S * kNC * 128; }
+#define OZ_DIGITS(S)                          \
+  constexpr int kS = (S);                     \
+  constexpr uint32_t kTS = tile_bytes(S);     \
+  constexpr int kFix = 8 * (S) - 1;           \
+  (void)kTS;                                  \
+  (void)kFix
 constexpr int kThreads = 320;            // 10 warps
 constexpr int kEpiThreads = 256;         // warps 2..9
 constexpr int kPackThreads = 256;
@@ -89,25 +98,27 @@ __device__ __forceinline__ long long fixed_from_float(float x, int sh) {
   else F = (long long)((m + (1ull << (-s - 1))) >> (-s));
   return (b >> 31) ? -F : F;
 }
-// The seven balanced base-256 digits of F as FP32 values (exact small
-// integers; d_0 the most significant), with one byte permute and one FP32
-// subtraction per digit: every byte of U = F + 0x80808080808080 (a bias of
-// 128 in each of the seven bytes) is u = d + 128 with d in [-128, 127], and
-// the top digit is (U >> 48) - 128 in [-128, 128] (|F| <= 2^55 keeps U in
-// [0, 2^56 + 2^48]).  A byte u placed in the mantissa of 0x4B400000 is the
-// float 1.5 2^23 + u.
-__device__ __forceinline__ void digits7f(long long F, float (&f)[kS]) {
-  const unsigned long long U = (unsigned long long)F + 0x80808080808080ull;
+// The S balanced base-256 digits of F as FP32 values (exact small integers;
+// d_0 the most significant), with one byte permute and one FP32 subtraction
+// per digit: every byte of U = F + 0x80...80 (a bias of 128 in each of the S
+// bytes) is u = d + 128 with d in [-128, 127], and the top digit is
+// (U >> 8(S-1)) - 128 in [-128, 128] (|F| <= 2^(8S-1) keeps U in
+// [0, 2^(8S) + 2^(8S-8)]).  A byte u placed in the mantissa of 0x4B400000 is
+// the float 1.5 2^23 + u.
+template <int S>
+__device__ __forceinline__ void digitsf(long long F, float (&f)[S]) {
+  static_assert(S >= 5 && S <= 7, "five to seven digits");
+  constexpr unsigned long long kBias = 0x8080808080808080ull >> (8 * (8 - S));
+  const unsigned long long U = (unsigned long long)F + kBias;
   const uint32_t lo = (uint32_t)U, hi = (uint32_t)(U >> 32);
   constexpr uint32_t kMag = 0x4B400000u;
   constexpr float kOff = 12583040.0f;  // 1.5 2^23 + 128
-  f[6] = __uint_as_float(__byte_perm(lo, kMag, 0x7640)) - kOff;
-  f[5] = __uint_as_float(__byte_perm(lo, kMag, 0x7641)) - kOff;
-  f[4] = __uint_as_float(__byte_perm(lo, kMag, 0x7642)) - kOff;
-  f[3] = __uint_as_float(__byte_perm(lo, kMag, 0x7643)) - kOff;
-  f[2] = __uint_as_float(__byte_perm(hi, kMag, 0x7640)) - kOff;
-  f[1] = __uint_as_float(__byte_perm(hi, kMag, 0x7641)) - kOff;
-  f[0] = __uint_as_float(__byte_perm(hi, kMag, 0x7632)) - kOff;  // bytes 6 and 7 of U
+#pragma unroll
+  for (int b = 0; b < S - 1; ++b)  // byte b of U: digit S-1-b
+    f[S - 1 - b] = __uint_as_float(__byte_perm(b < 4 ? lo : hi, kMag, 0x7640u | (uint32_t)(b & 3))) - kOff;
+  // bytes S-1 and S of U (in hi: S >= 5)
+  constexpr uint32_t kTop = 0x7600u | ((uint32_t)(S - 4) << 4) | (uint32_t)(S - 5);
+  f[0] = __uint_as_float(__byte_perm(hi, kMag, kTop)) - kOff;
 }
 // two FP32 values (small integers, exact) as one bf16x2 word, lo at the lower address
 __device__ __forceinline__ uint32_t bf16x2_of(float lo, float hi) {
@@ -135,44 +146,65 @@ __device__ __forceinline__ int scale_exp(double mx) {
   if (mx > 0.0 && mx <= 1.79e308) frexp(mx, &e);
   return e;
 }
-// fixed-point position of the digits: F = round(x 2^(kFix - E)), |x| < 2^E
-constexpr int kFix = 8 * kS - 1;
-// digits of x scaled by 2^-E (|x| < 2^E), as BF16 bit patterns
-__device__ __forceinline__ void digits_of(double x, int E, uint16_t (&d)[kS]) {
+// digits of x scaled by 2^-E (|x| < 2^E), as BF16 bit patterns; fixed-point
+// position F = round(x 2^(kFix - E))
+template <int S>
+__device__ __forceinline__ void digits_of(double x, int E, uint16_t (&d)[S]) {
+  OZ_DIGITS(S);
   float f[kS];
-  digits7f(fixed_from_double(x, kFix - E), f);
+  digitsf<S>(fixed_from_double(x, kFix - E), f);
 #pragma unroll
   for (int i = 0; i < kS; ++i) d[i] = bf16_bits(f[i]);
 }
 // the digits of one row at the even index k (f[0]) and k + 1 (f[1]): one
 // 32-bit store per digit block
-__device__ __forceinline__ void store_digit_pairs(unsigned char* tile, int row, int k, const float (&f)[2][kS]) {
+template <int S>
+__device__ __forceinline__ void store_digit_pairs(unsigned char* tile, int row, int k, const float (&f)[2][S]) {
+  constexpr int kS = S;
 #pragma unroll
   for (int i = 0; i < kS; ++i) *(uint32_t*)(tile + tc::sw128_offset(i * kNC + row, k)) = bf16x2_of(f[0][i], f[1][i]);
 }
 
 // ------------------------------------------------------------ accumulators
-// C_0..C_6 of 16 columns (this thread's TMEM lane) at `col` (digit block d at
-// col + d * kNC), summed into double-float.  The balanced digits do not
+// C_0..C_{S-1} of 16 columns (this thread's TMEM lane) at `col` (digit block
+// d at col + d * kNC), summed into double-float.  The balanced digits do not
 // shrink with their position, so every C_d is about as large as C_0: only
 // C_4..C_6 (weights 2^-32 and below) may be added in FP32, whose rounding at
 // 2^-24 of C_4 is 2^-56 of C_0; C_3, C_2, C_1 and C_0 enter with error-free
 // additions (an FP32 sum from C_3 on measured 2e-14 instead of 1e-15).
+template <int S>
 __device__ __forceinline__ void drain16(uint32_t col, dfl (&v)[16]) {
-  static_assert(kS == 7, "drain16 sums seven accumulators");
+  static_assert(S >= 5 && S <= 7, "five to seven accumulators");
   uint32_t a[16], b[16];
   float t[16];
-  tc::tmem_ld16_nw(col + 6 * kNC, a);
-  tc::tmem_ld16_nw(col + 5 * kNC, b);
-  tc::tmem_wait_ld();
+  if constexpr (S == 7) {
+    tc::tmem_ld16_nw(col + 6 * kNC, a);
+    tc::tmem_ld16_nw(col + 5 * kNC, b);
+    tc::tmem_wait_ld();
 #pragma unroll
-  for (int i = 0; i < 16; ++i) t[i] = __fmaf_rn(__uint_as_float(a[i]), 0.00390625f, __uint_as_float(b[i]));
-  tc::tmem_ld16_nw(col + 4 * kNC, a);
-  tc::tmem_ld16_nw(col + 3 * kNC, b);
-  tc::tmem_wait_ld();
+    for (int i = 0; i < 16; ++i) t[i] = __fmaf_rn(__uint_as_float(a[i]), 0.00390625f, __uint_as_float(b[i]));
+    tc::tmem_ld16_nw(col + 4 * kNC, a);
+    tc::tmem_ld16_nw(col + 3 * kNC, b);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) t[i] = __fmaf_rn(t[i], 0.00390625f, __uint_as_float(a[i]));  // C4 + 2^-8 C5 + 2^-16 C6
+  } else if constexpr (S == 6) {
+    tc::tmem_ld16_nw(col + 5 * kNC, a);
+    tc::tmem_ld16_nw(col + 4 * kNC, b);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) t[i] = __fmaf_rn(__uint_as_float(a[i]), 0.00390625f, __uint_as_float(b[i]));
+    tc::tmem_ld16_nw(col + 3 * kNC, b);
+    tc::tmem_wait_ld();
+  } else {
+    tc::tmem_ld16_nw(col + 4 * kNC, a);
+    tc::tmem_ld16_nw(col + 3 * kNC, b);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) t[i] = __uint_as_float(a[i]);  // C4
+  }
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
-    t[i] = __fmaf_rn(t[i], 0.00390625f, __uint_as_float(a[i]));  // C4 + 2^-8 C5 + 2^-16 C6
     float s, e;
     two_sum(__uint_as_float(b[i]), __fmul_rn(t[i], 0.00390625f), s, e);  // C3 + 2^-8 (...), exact
     v[i] = mkdf(s, e);
@@ -228,9 +260,10 @@ __device__ __forceinline__ bool ring_pop(const TileRing& R, uint32_t& use, int& 
 // first nks (<= 4) of a 64-wide chunk (the K rows past a synthesis order's
 // degrees are zero in both operands and are skipped); table tb's
 // accumulators at acc + tb * kS * kNC.
-template <int NT>
+template <int NT, int S>
 __device__ __forceinline__ void issue_digit(uint32_t acc, const unsigned char* A, const unsigned char* B, int u,
                                             bool first_chunk, uint32_t bstride_tb, int nks, int tb0, int tb1) {
+  constexpr int kS = S;
   const uint64_t a0 = tc::sw128_desc(tc::smem_u32(A));
   const uint64_t b0 = tc::sw128_desc(tc::smem_u32(B));
   const uint32_t idesc = tc::idesc_bf16(128, (kS - u) * kNC);
@@ -292,7 +325,9 @@ struct Rings {
 // (m, parity, l' tile, table, theta chunk, digit), 128 rows = degrees, 64
 // columns = colatitudes.  Row exponents in inv_exp [2][n_m][ntt*128] and
 // fwd_exp [2][lm_max].
+template <int S>
 __global__ void build_inv_oz_kernel(const ShtGeom g, TcTables t, unsigned char* img, short* rexp) {
+  OZ_DIGITS(S);
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int NHP = t.ntt * 128;
   if (idx >= (long long)g.n_m * 2 * NHP) return;
@@ -321,7 +356,9 @@ __global__ void build_inv_oz_kernel(const ShtGeom g, TcTables t, unsigned char* 
     }
 }
 
+template <int S>
 __global__ void build_fwd_oz_kernel(const ShtGeom g, TcTables t, unsigned char* img, short* rexp) {
+  OZ_DIGITS(S);
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int NLP = t.nlt * 128;
   if (idx >= (long long)g.n_m * 2 * 2 * NLP) return;
@@ -399,11 +436,12 @@ __device__ __forceinline__ PackCol pack_col(const ShtGeom& g, const InvSet& s, i
   return c;
 }
 
-template <bool VEC, bool MULTI>
+template <bool VEC, bool MULTI, int S>
 __global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const __grid_constant__ OzInv one,
                                                             const OzInv* __restrict__ many,
                                                             const __grid_constant__ InstIndex X) {
   extern __shared__ unsigned char smem_raw[];
+  OZ_DIGITS(S);
   unsigned char* buf = align1k(smem_raw);  // two tiles of kTS bytes
   __shared__ int sE[kNC];
   int ct, mc, c_unused;
@@ -486,10 +524,10 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const __grid_cons
         }
         float d[2][kS];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) digits7f(fixed_from_double(v[h].x, kFix - sE[2 * ql] + kw[h]), d[h]);
+        for (int h = 0; h < 2; ++h) digitsf<S>(fixed_from_double(v[h].x, kFix - sE[2 * ql] + kw[h]), d[h]);
         store_digit_pairs(B, 2 * ql, 2 * kp, d);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) digits7f(fixed_from_double(v[h].y, kFix - sE[2 * ql + 1] + kw[h]), d[h]);
+        for (int h = 0; h < 2; ++h) digitsf<S>(fixed_from_double(v[h].y, kFix - sE[2 * ql + 1] + kw[h]), d[h]);
         store_digit_pairs(B, 2 * ql + 1, 2 * kp, d);
       }
       tc::fence_proxy_async_smem();
@@ -506,13 +544,14 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const __grid_cons
 // Analysis data of one (column tile ct, order mc): the double-float (ES, EA)
 // half spectra of 16 complex columns over the nh colatitudes.  Exponents per
 // (ES | EA, real column): cexp[mc][2][nct * kNC]; tiles [mc][chunk][ct][ES|EA].
-template <bool VEC, bool MULTI>
+template <bool VEC, bool MULTI, int S>
 __global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_oz(const __grid_constant__ OzFwd one,
                                                             const OzFwd* __restrict__ many,
                                                             const __grid_constant__ InstIndex X) {
   extern __shared__ unsigned char smem_raw[];
   // one (ES, EA) tile pair (56 KB): three CTAs per SM; the next chunk waits for
   // the bulk store of the previous one (two pairs measured 1 CTA per SM, 1.8 ms)
+  OZ_DIGITS(S);
   unsigned char* buf = align1k(smem_raw);
   __shared__ int sE[2][kNC];
   int ct, mc, c_unused;
@@ -611,7 +650,7 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_oz(const __grid_cons
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const dfl v = w == 0 ? es[h].x : w == 1 ? es[h].y : w == 2 ? ea[h].x : ea[h].y;
-          digits7f(fixed_from_float(v.h, sh) + fixed_from_float(v.l, sh), d[h]);
+          digitsf<S>(fixed_from_float(v.h, sh) + fixed_from_float(v.l, sh), d[h]);
         }
         store_digit_pairs(B + which * kTS, row, 2 * kp, d);
       }
@@ -660,10 +699,11 @@ __device__ __forceinline__ float pow2f(int e) {
   return __int_as_float((e + 127) << 23);
 }
 
-template <bool VEC, bool MULTI>
+template <bool VEC, bool MULTI, int S>
 __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS)
     inv_leg_oz(const __grid_constant__ OzInv one, const OzInv* __restrict__ many,
                const __grid_constant__ InstIndex X, int ntiles) {
+  OZ_DIGITS(S);
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NA = Rings<VEC, true>::NA, NB = Rings<VEC, true>::NB;
   constexpr uint32_t ASZ = NT * 16384;
@@ -760,7 +800,7 @@ __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS)
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_digit<NT>(tmem, sA + slot * ASZ, sB + bslot * kTS, u, c == 0, 0, nks, tb0, tb1);
+            issue_digit<NT, S>(tmem, sA + slot * ASZ, sB + bslot * kTS, u, c == 0, 0, nks, tb0, tb1);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -832,8 +872,8 @@ __global__ void __launch_bounds__(Occ<VEC, true>::THREADS, Occ<VEC, true>::CPS)
       tc::tc_fence_after();
       const uint32_t acc = tmem + lane_off + cc0;
       dfl P[16], D[16];
-      drain16(acc, P);
-      if (VEC) drain16(acc + kS * kNC, D);
+      drain16<S>(acc, P);
+      if (VEC) drain16<S>(acc + kS * kNC, D);
       tc::tc_fence_before();
       tc::mbar_arrive(&acc_empty);  // tensor memory free for the next tile
       ++acc_use;
@@ -910,10 +950,11 @@ struct FwdTile {
   }
 };
 
-template <bool VEC, bool MULTI>
+template <bool VEC, bool MULTI, int S>
 __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS)
     fwd_leg_oz(const __grid_constant__ OzFwd one, const OzFwd* __restrict__ many,
                const __grid_constant__ InstIndex X, int ntiles) {
+  OZ_DIGITS(S);
   constexpr int NT = VEC ? 2 : 1;
   constexpr int NA = Rings<VEC, false>::NA, NB = Rings<VEC, false>::NB;
   constexpr uint32_t ASZ = NT * 16384;
@@ -1010,7 +1051,7 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
             const uint32_t slot = a_use % NA;
             if (!wait_full(&a_full[slot], a_use, NA)) { ok = false; break; }
             tc::tc_fence_after();
-            issue_digit<NT>(tmem, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, kTS, 4, tb0, tb1);
+            issue_digit<NT, S>(tmem, sA + slot * ASZ, sB + bslot * BSZ, u, c == 0, kTS, 4, tb0, tb1);
             tc::mma_commit(&a_empty[slot]);
           }
           tc::mma_commit(&b_empty[bslot]);
@@ -1067,8 +1108,8 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
       tc::tc_fence_after();
       const uint32_t acc = tmem + lane_off + cc0;
       dfl D0[16], D1[16];
-      drain16(acc, D0);
-      if (VEC) drain16(acc + kS * kNC, D1);
+      drain16<S>(acc, D0);
+      if (VEC) drain16<S>(acc + kS * kNC, D1);
       tc::tc_fence_before();
       tc::mbar_arrive(&acc_empty);
       ++acc_use;
@@ -1120,9 +1161,9 @@ __global__ void __launch_bounds__(Occ<VEC, false>::THREADS, Occ<VEC, false>::CPS
 }
 
 size_t align256_oz(size_t x) { return (x + 255) & ~(size_t)255; }
-size_t oz_tiles_bytes_inv(const TcTables& t, int nct) { return align256_oz((size_t)t.npc * nct * kTS); }
+size_t oz_tiles_bytes_inv(const TcTables& t, int nct) { return align256_oz((size_t)t.npc * nct * tile_bytes(t.ndig)); }
 size_t oz_tiles_bytes_fwd(const ShtGeom& g, const TcTables& t, int nct) {
-  return align256_oz((size_t)g.n_m * t.ncj * nct * 2 * kTS);
+  return align256_oz((size_t)g.n_m * t.ncj * nct * 2 * tile_bytes(t.ndig));
 }
 
 int num_sms_oz() {
@@ -1142,40 +1183,58 @@ long long oz_nct(int ncplx) { return (ncplx + kNC / 2 - 1) / (kNC / 2); }
 long long oz_inv_tiles(const ShtGeom& g, const TcTables& t, int nct) { return (long long)nct * t.ntt * 2 * g.n_m; }
 long long oz_fwd_tiles(const ShtGeom& g, const TcTables& t, int nct) { return (long long)nct * t.nlt * 2 * g.n_m; }
 
-template <bool VEC, bool MULTI>
-cudaError_t launch_inv_oz(const OzInv& one, const OzInv* many, const InstIndex& X, long long nblocks, long long ntiles,
-                          cudaStream_t st) {
+template <bool VEC, bool MULTI, int S>
+cudaError_t launch_inv_oz_s(const OzInv& one, const OzInv* many, const InstIndex& X, long long nblocks,
+                            long long ntiles, cudaStream_t st) {
   constexpr int NT = VEC ? 2 : 1, NA = Rings<VEC, true>::NA, NB = Rings<VEC, true>::NB;
+  constexpr uint32_t kTS = tile_bytes(S);
   if (ntiles <= 0) return cudaSuccess;
   const size_t psmem = 1024 + 2 * (size_t)kTS;
-  CUDA_TRY(cudaFuncSetAttribute(pack_inv_oz<VEC, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  CUDA_TRY(cudaFuncSetAttribute(pack_inv_oz<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
   const dim3 pgrid = MULTI ? dim3((unsigned)nblocks) : dim3(one.nct, one.g.n_m);
-  pack_inv_oz<VEC, MULTI><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
+  pack_inv_oz<VEC, MULTI, S><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * kTS;
-  CUDA_TRY(cudaFuncSetAttribute(inv_leg_oz<VEC, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CUDA_TRY(cudaFuncSetAttribute(inv_leg_oz<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC, true>::CPS);
   CUDA_TRY(cudaMemsetAsync(one.t.tile_ctr, 0, sizeof(int), st));
-  inv_leg_oz<VEC, MULTI><<<grid, Occ<VEC, true>::THREADS, smem, st>>>(one, many, X, (int)ntiles);
+  inv_leg_oz<VEC, MULTI, S><<<grid, Occ<VEC, true>::THREADS, smem, st>>>(one, many, X, (int)ntiles);
   return cudaGetLastError();
 }
 
+template <bool VEC, bool MULTI, int S>
+cudaError_t launch_fwd_oz_s(const OzFwd& one, const OzFwd* many, const InstIndex& X, long long nblocks,
+                            long long ntiles, cudaStream_t st) {
+  constexpr int NT = VEC ? 2 : 1, NA = Rings<VEC, false>::NA, NB = Rings<VEC, false>::NB;
+  constexpr uint32_t kTS = tile_bytes(S);
+  if (ntiles <= 0) return cudaSuccess;
+  const size_t psmem = 1024 + 2 * (size_t)kTS;
+  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_oz<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  const dim3 pgrid = MULTI ? dim3((unsigned)nblocks) : dim3(one.nct, one.g.n_m);
+  pack_fwd_oz<VEC, MULTI, S><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
+  CUDA_TRY(cudaGetLastError());
+  const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * kTS;
+  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_oz<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC, false>::CPS);
+  CUDA_TRY(cudaMemsetAsync(one.t.tile_ctr, 0, sizeof(int), st));
+  fwd_leg_oz<VEC, MULTI, S><<<grid, Occ<VEC, false>::THREADS, smem, st>>>(one, many, X, (int)ntiles);
+  return cudaGetLastError();
+}
+
+// the digit count of the tables (t.ndig: 7 or 5) selects the instantiation
+template <bool VEC, bool MULTI>
+cudaError_t launch_inv_oz(const OzInv& one, const OzInv* many, const InstIndex& X, long long nblocks, long long ntiles,
+                          cudaStream_t st) {
+  if (one.t.ndig == 7) return launch_inv_oz_s<VEC, MULTI, 7>(one, many, X, nblocks, ntiles, st);
+  if (one.t.ndig == 5) return launch_inv_oz_s<VEC, MULTI, 5>(one, many, X, nblocks, ntiles, st);
+  return cudaErrorInvalidValue;
+}
 template <bool VEC, bool MULTI>
 cudaError_t launch_fwd_oz(const OzFwd& one, const OzFwd* many, const InstIndex& X, long long nblocks, long long ntiles,
                           cudaStream_t st) {
-  constexpr int NT = VEC ? 2 : 1, NA = Rings<VEC, false>::NA, NB = Rings<VEC, false>::NB;
-  if (ntiles <= 0) return cudaSuccess;
-  const size_t psmem = 1024 + 2 * (size_t)kTS;
-  CUDA_TRY(cudaFuncSetAttribute(pack_fwd_oz<VEC, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-  const dim3 pgrid = MULTI ? dim3((unsigned)nblocks) : dim3(one.nct, one.g.n_m);
-  pack_fwd_oz<VEC, MULTI><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
-  CUDA_TRY(cudaGetLastError());
-  const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * NT * kTS;
-  CUDA_TRY(cudaFuncSetAttribute(fwd_leg_oz<VEC, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms_oz() * Occ<VEC, false>::CPS);
-  CUDA_TRY(cudaMemsetAsync(one.t.tile_ctr, 0, sizeof(int), st));
-  fwd_leg_oz<VEC, MULTI><<<grid, Occ<VEC, false>::THREADS, smem, st>>>(one, many, X, (int)ntiles);
-  return cudaGetLastError();
+  if (one.t.ndig == 7) return launch_fwd_oz_s<VEC, MULTI, 7>(one, many, X, nblocks, ntiles, st);
+  if (one.t.ndig == 5) return launch_fwd_oz_s<VEC, MULTI, 5>(one, many, X, nblocks, ntiles, st);
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -1188,24 +1247,32 @@ size_t oz_data_bytes(const ShtGeom& g, const TcTables& t, int ncplx, bool invers
   return tiles + ex;
 }
 
-void oz_table_layout(const ShtGeom& g, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
+void oz_table_layout(const ShtGeom& g, int digits, int* ntt, int* nlt, int* ncj, std::vector<long long>& inv_blk0,
                      std::vector<long long>& fwd_blk0, long long* inv_blocks, long long* fwd_blocks) {
-  tc_table_layout_bpc(g, kS, ntt, nlt, ncj, inv_blk0, fwd_blk0, inv_blocks, fwd_blocks);
+  tc_table_layout_bpc(g, digits, ntt, nlt, ncj, inv_blk0, fwd_blk0, inv_blocks, fwd_blocks);
 }
 
-cudaError_t build_oz_images(const ShtGeom& g, const TcTables& t, unsigned char* inv_img, short* inv_exp,
-                            unsigned char* fwd_img, short* fwd_exp, cudaStream_t st) {
+template <int S>
+cudaError_t build_oz_images_s(const ShtGeom& g, const TcTables& t, unsigned char* inv_img, short* inv_exp,
+                              unsigned char* fwd_img, short* fwd_exp, cudaStream_t st) {
   {
     const long long n = (long long)g.n_m * 2 * t.ntt * 128;
-    build_inv_oz_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g, t, inv_img, inv_exp);
+    build_inv_oz_kernel<S><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g, t, inv_img, inv_exp);
     CUDA_TRY(cudaGetLastError());
   }
   {
     const long long n = (long long)g.n_m * 4 * t.nlt * 128;
-    build_fwd_oz_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g, t, fwd_img, fwd_exp);
+    build_fwd_oz_kernel<S><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g, t, fwd_img, fwd_exp);
     CUDA_TRY(cudaGetLastError());
   }
   return cudaSuccess;
+}
+
+cudaError_t build_oz_images(const ShtGeom& g, const TcTables& t, unsigned char* inv_img, short* inv_exp,
+                            unsigned char* fwd_img, short* fwd_exp, cudaStream_t st) {
+  if (t.ndig == 7) return build_oz_images_s<7>(g, t, inv_img, inv_exp, fwd_img, fwd_exp, st);
+  if (t.ndig == 5) return build_oz_images_s<5>(g, t, inv_img, inv_exp, fwd_img, fwd_exp, st);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_inv_legendre_oz(const ShtGeom& g, const InvSet& s, bool vec, const TcTables& t,

@@ -227,7 +227,11 @@ bool is_pinned_host(const void* p) {
 bool fp64_pipes(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_FP64; }
 // the FP64-accurate tensor-core form: Legendre sums of fixed-point BF16 digits
 // (or, with tc_kernel = 1, the FP64 SIMT sums) and double-float FFTs
-bool oz_form(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_FP64TC; }
+// (also MAGIC_SHT_BF16X5: the same form with five digits per operand)
+bool oz_form(const magic_sht_handle* h) {
+  return h->precision == MAGIC_SHT_FP64TC || h->precision == MAGIC_SHT_BF16X5;
+}
+int oz_digits(const magic_sht_handle* h) { return h->precision == MAGIC_SHT_BF16X5 ? 5 : 7; }
 // FP64 arithmetic in the SIMT Legendre sums and the radial-loop kernels
 bool f64_sums(const magic_sht_handle* h) { return fp64_pipes(h) || oz_form(h); }
 size_t t2_bytes(const magic_sht_handle* h) { return f64_sums(h) ? 16 : 8; }
@@ -820,7 +824,7 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   const int ld = d->nlat_padded > 0 ? d->nlat_padded : N;
   if (ld < N) return set_err(MAGIC_SHT_ERR_SIZE, "nlat_padded=%d < n_theta_max=%d", ld, N);
   if (d->precision != MAGIC_SHT_FP64 && d->precision != MAGIC_SHT_FP32 && d->precision != MAGIC_SHT_BF16X3 &&
-      d->precision != MAGIC_SHT_TF32X2 && d->precision != MAGIC_SHT_FP64TC)
+      d->precision != MAGIC_SHT_TF32X2 && d->precision != MAGIC_SHT_FP64TC && d->precision != MAGIC_SHT_BF16X5)
     return set_err(MAGIC_SHT_ERR_ARG, "unknown precision %d", d->precision);
 
   int dev = d->device;
@@ -913,7 +917,8 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     TcTables& t = h->tct;
     std::vector<long long> ib, fb;
     long long ninv = 0, nfwd = 0;
-    oz_table_layout(g, &t.ntt, &t.nlt, &t.ncj, ib, fb, &ninv, &nfwd);
+    t.ndig = oz_digits(h);
+    oz_table_layout(g, t.ndig, &t.ntt, &t.nlt, &t.ncj, ib, fb, &ninv, &nfwd);
     INIT_CK(cudaMalloc((void**)&h->d_inv_img, (size_t)ninv * 16384));
     INIT_CK(cudaMalloc((void**)&h->d_fwd_img, (size_t)nfwd * 16384));
     INIT_CK(cudaMalloc((void**)&h->d_inv_blk0, sizeof(long long) * n_m));
@@ -2125,7 +2130,7 @@ namespace {
 static_assert(sizeof(ShtGeom) == 10 * 4 + 10 * 8, "ShtGeom holds padding bytes");
 static_assert(sizeof(InvSet) == MAGIC_MAX_FIELDS * sizeof(InvField) + 40, "InvSet holds padding bytes");
 static_assert(sizeof(FwdSet) == MAGIC_MAX_FIELDS * sizeof(FwdField) + 24, "FwdSet holds padding bytes");
-static_assert(sizeof(TcTables) == 12 * 8 + 4 * 4, "TcTables holds padding bytes");
+static_assert(sizeof(TcTables) == 12 * 8 + 6 * 4, "TcTables holds padding bytes");
 static_assert(sizeof(LegInst<InvSet>) == sizeof(ShtGeom) + sizeof(InvSet) + sizeof(TcTables) + 32,
               "LegInst holds padding bytes");
 
@@ -2284,9 +2289,8 @@ int magic_sht_group_create(magic_sht_handle* const* handles, int n, magic_sht_gr
     if (handles[i]->device != handles[0]->device)
       return set_err(MAGIC_SHT_ERR_ARG, "the handles of a group are on one device");
     const int pr = handles[i]->precision;
-    if (pr != MAGIC_SHT_FP64TC && pr != MAGIC_SHT_BF16X3)
-      return set_err(MAGIC_SHT_ERR_UNSUPPORTED,
-                     "group calls need the FP64-accurate or the 3xBF16 tensor-core form (handle %d)", i);
+    if (pr != MAGIC_SHT_FP64TC && pr != MAGIC_SHT_BF16X5 && pr != MAGIC_SHT_BF16X3)
+      return set_err(MAGIC_SHT_ERR_UNSUPPORTED, "group calls need a persistent tensor-core form (handle %d)", i);
     if (pr != handles[0]->precision)
       return set_err(MAGIC_SHT_ERR_ARG, "the handles of a group share one arithmetic form (handle %d)", i);
     for (int k = 0; k < i; ++k)

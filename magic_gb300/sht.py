@@ -738,7 +738,7 @@ class SHT:
 
 class SHTGroup:
     """Several independent instances (SHT handles of different l_max, minc and
-    grids, all precision="fp64tc" or all "bf16x3") transformed together
+    grids, all precision="fp64tc", all "bf16x5" or all "bf16x3") transformed together
     (magic_sht_group_*): the Legendre sums of every instance run as one pack
     and one persistent tensor-core launch per direction and field kind, with
     results equal to the instances' own calls bit for bit.  Spectra and grids

@@ -1,5 +1,6 @@
 """Several independent instances of uneven size in one launch per kind
-(magic_sht_group_*, SHTGroup; FP64-accurate and 3xBF16 tensor-core forms):
+(magic_sht_group_*, SHTGroup; the seven- and five-digit and the 3xBF16
+tensor-core forms):
 the synthesis and analysis sets of every
 instance (rIter.f90:466-712 per instance) with the Legendre sums of all
 instances in one pack + one persistent tensor-core launch per direction and
@@ -49,7 +50,7 @@ def _assert_equal(torch, got, ref, what):
         assert torch.equal(got[k], ref[k]), (what, k, float((got[k] - ref[k]).abs().max()))
 
 
-@pytest.mark.parametrize("precision", ["fp64tc", "bf16x3"])
+@pytest.mark.parametrize("precision", ["fp64tc", "bf16x5", "bf16x3"])
 def test_group_equals_separate_calls(built, torch, precision):
     from magic_gb300 import SHTGroup
     from magic_gb300.workload import FORWARD_FROM_INVERSE
