@@ -541,6 +541,117 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const __grid_cons
   if (tid == 0) tc::bulk_wait<0>();
 }
 
+// The same pack in one pass, for orders of at most two 64-degree chunks per
+// parity (l_max <= 255): warp qg owns complex columns qg and qg + 8 over all
+// degrees of the order (lane kp: degree indices 2 kp, 2 kp + 1 of every
+// chunk), so it loads all of them into registers at once (16 loads in
+// flight per thread), takes each column's scale by a warp reduction and
+// writes the digits from registers: the spectra are read once, with one
+// memory latency per CTA instead of one per pass and chunk.  The digits are
+// those of pack_inv_oz (same scales, same rounding).
+template <bool VEC, bool MULTI, int S>
+__global__ void __launch_bounds__(kPackThreads, 2) pack_inv_oz1(const __grid_constant__ OzInv one,
+                                                             const OzInv* __restrict__ many,
+                                                             const __grid_constant__ InstIndex X) {
+  extern __shared__ unsigned char smem_raw[];
+  OZ_DIGITS(S);
+  unsigned char* buf = align1k(smem_raw);  // two tiles of kTS bytes
+  int ct, mc, c_unused;
+  const OzInv& I = block_inst<MULTI>(one, many, X, ct, mc, c_unused);
+  const ShtGeom& g = I.g;
+  const InvSet& s = I.s;
+  const TcTables& t = I.t;
+  unsigned char* __restrict__ bimg = I.bimg;
+  short* __restrict__ cexp = I.cexp;
+  const int nct = I.nct;
+  const int m = mc * g.minc, n_l = g.l_max - m + 1, lm0 = g.lmoff[mc];
+  const int nch = tc_nch(n_l);  // <= 2
+  const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
+  const int tid = threadIdx.x, kp = tid & 31, qg = tid >> 5;
+  PackCol cols[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) cols[i] = pack_col<VEC>(g, s, ct * (kNC / 2) + qg + 8 * i, ncplx);
+  // v[i][p][c][h]: column i, parity p, chunk c, degree index 64 c + 2 kp + h
+  double2 v[2][2][2][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int loff = p + 2 * (64 * c + 2 * kp + h);
+          const int l = m + loff;
+          v[i][p][c][h] = make_double2(0.0, 0.0);
+          if (cols[i].op.op != OP_ZERO && c < nch && loff < n_l && l <= cols[i].lc)
+            v[i][p][c][h] = oz_operand(cols[i].op, cols[i].r, lm0, loff, l, m, cols[i].or2);
+        }
+  // largest exponent of x 2^k(l) per real column (the spectra divided by the degree weights)
+  int E[2][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    int er = -4096, ei = -4096;
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int k = deg_shift(m + p + 2 * (64 * c + 2 * kp + h));
+          er = max(er, exp_bound(v[i][p][c][h].x) + k);
+          ei = max(ei, exp_bound(v[i][p][c][h].y) + k);
+        }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+      er = max(er, __shfl_xor_sync(0xffffffffu, er, d));
+      ei = max(ei, __shfl_xor_sync(0xffffffffu, ei, d));
+    }
+    E[i][0] = er < -3000 ? 0 : er;
+    E[i][1] = ei < -3000 ? 0 : ei;
+    if (kp == 0) {
+      const int ql = qg + 8 * i;
+      cexp[(long long)mc * nct * kNC + ct * kNC + 2 * ql] = (short)E[i][0];
+      cexp[(long long)mc * nct * kNC + ct * kNC + 2 * ql + 1] = (short)E[i][1];
+    }
+  }
+  int nb = 0;
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      if (c >= nch) continue;
+      unsigned char* B = buf + (nb & 1) * kTS;
+      if (nb >= 2) {  // the bulk store that read this buffer has finished
+        if (tid == 0) tc::bulk_wait_read<1>();
+        __syncthreads();
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int ql = qg + 8 * i;
+        int kw[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) kw[h] = deg_shift(m + p + 2 * (64 * c + 2 * kp + h));
+        float d[2][kS];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) digitsf<S>(fixed_from_double(v[i][p][c][h].x, kFix - E[i][0] + kw[h]), d[h]);
+        store_digit_pairs(B, 2 * ql, 2 * kp, d);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) digitsf<S>(fixed_from_double(v[i][p][c][h].y, kFix - E[i][1] + kw[h]), d[h]);
+        store_digit_pairs(B, 2 * ql + 1, 2 * kp, d);
+      }
+      tc::fence_proxy_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        const long long pc = t.bpc0[mc] + p * nch + c;
+        tc::bulk_s2g(bimg + (pc * nct + ct) * (long long)kTS, B, kTS);
+        tc::bulk_commit();
+      }
+      ++nb;
+    }
+  if (tid == 0) tc::bulk_wait<0>();
+}
+
 // Analysis data of one (column tile ct, order mc): the double-float (ES, EA)
 // half spectra of 16 complex columns over the nh colatitudes.  Exponents per
 // (ES | EA, real column): cexp[mc][2][nct * kNC]; tiles [mc][chunk][ct][ES|EA].
@@ -1185,14 +1296,20 @@ long long oz_fwd_tiles(const ShtGeom& g, const TcTables& t, int nct) { return (l
 
 template <bool VEC, bool MULTI, int S>
 cudaError_t launch_inv_oz_s(const OzInv& one, const OzInv* many, const InstIndex& X, long long nblocks,
-                            long long ntiles, cudaStream_t st) {
+                            long long ntiles, int lmax, cudaStream_t st) {
   constexpr int NT = VEC ? 2 : 1, NA = Rings<VEC, true>::NA, NB = Rings<VEC, true>::NB;
   constexpr uint32_t kTS = tile_bytes(S);
   if (ntiles <= 0) return cudaSuccess;
   const size_t psmem = 1024 + 2 * (size_t)kTS;
-  CUDA_TRY(cudaFuncSetAttribute(pack_inv_oz<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
   const dim3 pgrid = MULTI ? dim3((unsigned)nblocks) : dim3(one.nct, one.g.n_m);
-  pack_inv_oz<VEC, MULTI, S><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
+  // one pass when every order of every instance has at most two chunks per parity
+  if (tc_nch(lmax + 1) > 2) {
+    CUDA_TRY(cudaFuncSetAttribute(pack_inv_oz<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+    pack_inv_oz<VEC, MULTI, S><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
+  } else {
+    CUDA_TRY(cudaFuncSetAttribute(pack_inv_oz1<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+    pack_inv_oz1<VEC, MULTI, S><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
+  }
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * kTS;
   CUDA_TRY(cudaFuncSetAttribute(inv_leg_oz<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1222,11 +1339,12 @@ cudaError_t launch_fwd_oz_s(const OzFwd& one, const OzFwd* many, const InstIndex
 }
 
 // the digit count of the tables (t.ndig: 7 or 5) selects the instantiation
+// lmax: the largest l_max of the launch's instances
 template <bool VEC, bool MULTI>
 cudaError_t launch_inv_oz(const OzInv& one, const OzInv* many, const InstIndex& X, long long nblocks, long long ntiles,
-                          cudaStream_t st) {
-  if (one.t.ndig == 7) return launch_inv_oz_s<VEC, MULTI, 7>(one, many, X, nblocks, ntiles, st);
-  if (one.t.ndig == 5) return launch_inv_oz_s<VEC, MULTI, 5>(one, many, X, nblocks, ntiles, st);
+                          int lmax, cudaStream_t st) {
+  if (one.t.ndig == 7) return launch_inv_oz_s<VEC, MULTI, 7>(one, many, X, nblocks, ntiles, lmax, st);
+  if (one.t.ndig == 5) return launch_inv_oz_s<VEC, MULTI, 5>(one, many, X, nblocks, ntiles, lmax, st);
   return cudaErrorInvalidValue;
 }
 template <bool VEC, bool MULTI>
@@ -1285,8 +1403,8 @@ cudaError_t launch_inv_legendre_oz(const ShtGeom& g, const InvSet& s, bool vec, 
   long long nblocks = 0, ntiles = 0;
   oz_layout_insts(one.data(), 1, vec, &nblocks, &ntiles);
   InstIndex X{};
-  return vec ? launch_inv_oz<true, false>(one[0], nullptr, X, nblocks, ntiles, st)
-             : launch_inv_oz<false, false>(one[0], nullptr, X, nblocks, ntiles, st);
+  return vec ? launch_inv_oz<true, false>(one[0], nullptr, X, nblocks, ntiles, g.l_max, st)
+             : launch_inv_oz<false, false>(one[0], nullptr, X, nblocks, ntiles, g.l_max, st);
 }
 
 cudaError_t launch_fwd_legendre_oz(const ShtGeom& g, const FwdSet& s, bool vec, const TcTables& t,
@@ -1328,8 +1446,10 @@ cudaError_t launch_inv_legendre_oz_multi(const LegInst<InvSet>* inst, const LegI
                                          bool vec, long long nblocks, long long ntiles, cudaStream_t st) {
   if (n < 1 || n > kMaxGroupInst) return cudaErrorInvalidValue;
   const InstIndex X = inst_index(inst, n);
-  return vec ? launch_inv_oz<true, true>(inst[0], d_inst, X, nblocks, ntiles, st)
-             : launch_inv_oz<false, true>(inst[0], d_inst, X, nblocks, ntiles, st);
+  int lmax = 0;
+  for (int i = 0; i < n; ++i) lmax = std::max(lmax, inst[i].g.l_max);
+  return vec ? launch_inv_oz<true, true>(inst[0], d_inst, X, nblocks, ntiles, lmax, st)
+             : launch_inv_oz<false, true>(inst[0], d_inst, X, nblocks, ntiles, lmax, st);
 }
 
 cudaError_t launch_fwd_legendre_oz_multi(const LegInst<FwdSet>* inst, const LegInst<FwdSet>* d_inst, int n,
