@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stage", action="store_true", help="skip the radial-loop stage measurement")
     ap.add_argument("--no-variant", action="store_true", help="skip the other precision forms (3xBF16, 2xTF32)")
-    ap.add_argument("--levels", type=int, default=N_LEVELS, help="radial levels (profiling cases)")
+    ap.add_argument("--levels", type=int, default=N_LEVELS,
+                    help="radial levels (profiling cases; with --instances: the cap of every instance)")
     ap.add_argument("--instances", action="store_true",
                     help="instead of the bench line: sixteen mixed-size instances in one graph (one JSON line)")
     ap.add_argument("--group", action="store_true",
@@ -892,7 +893,7 @@ def instances_measure(form, local, warmup, steps):
     return out
 
 
-def instances_run(form, local, warmup, steps, group=False):
+def instances_run(form, local, warmup, steps, group=False, max_levels=None):
     """Sixteen independent instances of mixed size (l_max in {63, 127, 255},
     minc in {1, 4}, {33, 65, 129} radial levels, n_theta = 3(l_max+1)/2,
     n_phi = 2 n_theta / minc; a fixed seeded list), both transform sets of every
@@ -909,6 +910,8 @@ def instances_run(form, local, warmup, steps, group=False):
         L = int(rng.choice([63, 127, 255]))
         minc = int(rng.choice([1, 4]))
         R = int(rng.choice([33, 65, 129]))
+        if max_levels:  # profiling cases: every instance capped at max_levels levels
+            R = min(R, max_levels)
         N = 3 * (L + 1) // 2
         P = 2 * N // minc
         s = SHT(L, minc, N, P, precision=form, device=local)
@@ -985,7 +988,8 @@ def instances_arm(args):
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
     form = "bf16x3" if args.form == "auto" else args.form
-    r = instances_run(form, local, args.warmup, args.steps, group=args.group)
+    r = instances_run(form, local, args.warmup, args.steps, group=args.group,
+                      max_levels=args.levels if args.levels != N_LEVELS else None)
     if rank == 0:
         print(json.dumps(r), flush=True)
 

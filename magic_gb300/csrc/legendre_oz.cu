@@ -686,25 +686,24 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_oz(const __grid_cons
     const int ql = tid >> 4, li = tid & 15;
     const dfl2* src = src_of(ct * (kNC / 2) + ql);
     float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
+    // only the hi words set the scale: twelve colatitudes per thread in flight
+    // (every colatitude of nh <= 192 in one round), four floats each
     if (src)
-      for (int j0 = li; j0 < g.nh; j0 += 16 * 4) {
-        dfl2 es[4], ea[4];
+      for (int j0 = li; j0 < g.nh; j0 += 16 * 12) {
+        float hw[12][4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < 12; ++u) {
           const int j = j0 + 16 * u;
-          es[u] = {dfl(0), dfl(0)};
-          ea[u] = es[u];
-          if (j < g.nh) {
-            es[u] = src[2 * j];
-            ea[u] = src[2 * j + 1];
-          }
+          const float* q = (const float*)(src + 2 * j);  // es.x.h, es.y.h, ea.x.h, ea.y.h at 0, 2, 4, 6
+#pragma unroll
+          for (int w = 0; w < 4; ++w) hw[u][w] = j < g.nh ? __ldg(q + 2 * w) : 0.f;
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          m0 = fmaxf(m0, fabsf(es[u].x.h));
-          m1 = fmaxf(m1, fabsf(es[u].y.h));
-          m2 = fmaxf(m2, fabsf(ea[u].x.h));
-          m3 = fmaxf(m3, fabsf(ea[u].y.h));
+        for (int u = 0; u < 12; ++u) {
+          m0 = fmaxf(m0, fabsf(hw[u][0]));
+          m1 = fmaxf(m1, fabsf(hw[u][1]));
+          m2 = fmaxf(m2, fabsf(hw[u][2]));
+          m3 = fmaxf(m3, fabsf(hw[u][3]));
         }
       }
 #pragma unroll
@@ -733,26 +732,33 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_oz(const __grid_cons
   const dfl2* srcs[2];
 #pragma unroll
   for (int i = 0; i < 2; ++i) srcs[i] = src_of(ct * (kNC / 2) + qg + 8 * i);
+  // values of chunk c: es / ea [column][colatitude 2 kp + h]; the loads of
+  // chunk c + 1 are issued before chunk c's barrier and bulk store
+  dfl2 es[2][2], ea[2][2];
+  auto load_chunk = [&](int c) {
+    const int j0 = 64 * c + 2 * kp;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        es[i][h] = {dfl(0), dfl(0)};
+        ea[i][h] = es[i][h];
+        if (srcs[i] && c < t.ncj && j0 + h < g.nh) {
+          es[i][h] = srcs[i][2 * (j0 + h)];
+          ea[i][h] = srcs[i][2 * (j0 + h) + 1];
+        }
+      }
+  };
+  load_chunk(0);
   for (int c = 0; c < t.ncj; ++c) {
     unsigned char* B = buf;
     if (c >= 1) {
       if (tid == 0) tc::bulk_wait_read<0>();
       __syncthreads();
     }
-    const int j0 = 64 * c + 2 * kp;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
       const int ql = qg + 8 * i;
-      dfl2 es[2], ea[2];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        es[h] = {dfl(0), dfl(0)};
-        ea[h] = es[h];
-        if (srcs[i] && j0 + h < g.nh) {
-          es[h] = srcs[i][2 * (j0 + h)];
-          ea[h] = srcs[i][2 * (j0 + h) + 1];
-        }
-      }
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const int which = w >> 1, row = 2 * ql + (w & 1);
@@ -760,12 +766,13 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_fwd_oz(const __grid_cons
         float d[2][kS];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const dfl v = w == 0 ? es[h].x : w == 1 ? es[h].y : w == 2 ? ea[h].x : ea[h].y;
+          const dfl v = w == 0 ? es[i][h].x : w == 1 ? es[i][h].y : w == 2 ? ea[i][h].x : ea[i][h].y;
           digitsf<S>(fixed_from_float(v.h, sh) + fixed_from_float(v.l, sh), d[h]);
         }
         store_digit_pairs(B + which * kTS, row, 2 * kp, d);
       }
     }
+    load_chunk(c + 1);
     tc::fence_proxy_async_smem();
     __syncthreads();
     if (tid == 0) {
