@@ -425,10 +425,11 @@ int magic_sht_graph_destroy(magic_sht_graph* graph);
  * every handle must be bound to one stream (magic_sht_set_stream), on which
  * the call is asynchronous and may be captured with magic_sht_graph_begin on
  * the first handle: make the same calls once before capturing (they size the
- * workspaces and upload the per-instance tables the launches read, which the
- * group keeps until magic_sht_group_destroy).  A handle belongs to at most
- * one group call at a time; n_levels, or2, lcut and args are arrays of
- * n_handles entries (or2 / lcut may be NULL for all). */
+ * workspaces and reserve room for the per-instance tables of captured calls,
+ * which the group keeps until magic_sht_group_destroy; uncaptured calls reuse
+ * a fixed device ring for theirs).  A handle belongs to at most one group call
+ * at a time; n_levels, or2, lcut and args are arrays of n_handles entries
+ * (or2 / lcut may be NULL for all). */
 typedef struct magic_sht_group magic_sht_group;
 int magic_sht_group_create(magic_sht_handle* const* handles, int n_handles, magic_sht_group** group);
 int magic_sht_group_destroy(magic_sht_group* group);

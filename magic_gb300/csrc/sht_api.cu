@@ -2108,9 +2108,14 @@ int magic_sht_graph_destroy(magic_sht_graph* gr) {
 struct magic_sht_group {
   std::vector<magic_sht_handle*> h;
   int device = 0;
-  // Device copies of the launches' instance arrays, append-only while the
-  // group lives (a graph captured from a group call reads the copies it was
-  // captured with); an identical array is uploaded once.
+  // Device copies of the launches' instance arrays.  Calls captured into a
+  // graph use the kept copies: append-only while the group lives (the graph
+  // reads the copies it was captured with, from pinned memory that is never
+  // rewritten), an identical array uploaded once.  Other calls take a slot of
+  // a device ring written from pageable memory on the group's stream (the
+  // copy is staged before it returns, and stream order puts it after every
+  // earlier launch that read the slot), so repeated calls with new arrays
+  // reuse the same memory.
   struct Chunk {
     char* host = nullptr;  // pinned: the source of the asynchronous copies
     char* dev = nullptr;
@@ -2123,6 +2128,8 @@ struct magic_sht_group {
     size_t bytes;
   };
   std::vector<Slot> slots;
+  char* ring = nullptr;
+  size_t ring_cap = 0, ring_off = 0;
 };
 
 namespace {
@@ -2134,7 +2141,27 @@ static_assert(sizeof(TcTables) == 12 * 8 + 6 * 4, "TcTables holds padding bytes"
 static_assert(sizeof(LegInst<InvSet>) == sizeof(ShtGeom) + sizeof(InvSet) + sizeof(TcTables) + 32,
               "LegInst holds padding bytes");
 
-constexpr size_t kGroupChunk = 1 << 20;
+constexpr size_t kGroupChunk = 1 << 20;  // kept copies for captured calls
+constexpr size_t kGroupRing = 2 << 20;   // ring of the uncaptured calls (many calls' arrays)
+
+// a kept chunk with `need` free bytes (allocated outside a capture only)
+int group_chunk(magic_sht_group* G, size_t need, bool capturing) {
+  if (!G->chunks.empty() && G->chunks.back().used + need <= G->chunks.back().cap) return MAGIC_SHT_OK;
+  if (capturing)
+    return set_err(MAGIC_SHT_ERR_NOMEM,
+                   "group instance tables for captured calls are full: make a group call outside the capture "
+                   "first (it reserves room for them)");
+  magic_sht_group::Chunk c;
+  c.cap = std::max(kGroupChunk, need);
+  CK(cudaHostAlloc((void**)&c.host, c.cap, cudaHostAllocDefault));
+  if (cudaMalloc((void**)&c.dev, c.cap) != cudaSuccess) {
+    cudaFreeHost(c.host);
+    cudaGetLastError();
+    return set_err(MAGIC_SHT_ERR_NOMEM, "group instance tables: cudaMalloc of %zu bytes failed", c.cap);
+  }
+  G->chunks.push_back(c);
+  return MAGIC_SHT_OK;
+}
 
 int group_upload(magic_sht_group* G, const void* p, size_t bytes, bool capturing, cudaStream_t st,
                  const void** out) {
@@ -2144,20 +2171,29 @@ int group_upload(magic_sht_group* G, const void* p, size_t bytes, bool capturing
       return MAGIC_SHT_OK;
     }
   const size_t need = align256(bytes);
-  if (G->chunks.empty() || G->chunks.back().used + need > G->chunks.back().cap) {
-    if (capturing)
-      return set_err(MAGIC_SHT_ERR_NOMEM,
-                     "group instance tables full during graph capture: make the same calls once before capturing");
-    magic_sht_group::Chunk c;
-    c.cap = std::max(kGroupChunk, need);
-    CK(cudaHostAlloc((void**)&c.host, c.cap, cudaHostAllocDefault));
-    if (cudaMalloc((void**)&c.dev, c.cap) != cudaSuccess) {
-      cudaFreeHost(c.host);
-      cudaGetLastError();
-      return set_err(MAGIC_SHT_ERR_NOMEM, "group instance tables: cudaMalloc of %zu bytes failed", c.cap);
+  if (!capturing) {
+    // room for the kept copies of a capture that may follow
+    TRY(group_chunk(G, 2 * kMaxGroupInst * sizeof(LegInst<InvSet>), false));
+    if (need > G->ring_cap) {
+      if (G->ring) {
+        CK(cudaStreamSynchronize(st));
+        CK(cudaFree(G->ring));
+        G->ring = nullptr;
+        G->ring_cap = 0;
+      }
+      const size_t cap = std::max(kGroupRing, 4 * need);
+      CK(cudaMalloc((void**)&G->ring, cap));
+      G->ring_cap = cap;
+      G->ring_off = 0;
     }
-    G->chunks.push_back(c);
+    if (G->ring_off + need > G->ring_cap) G->ring_off = 0;
+    char* dp = G->ring + G->ring_off;
+    G->ring_off += need;
+    CK(cudaMemcpyAsync(dp, p, bytes, cudaMemcpyHostToDevice, st));  // pageable: staged before it returns
+    *out = dp;
+    return MAGIC_SHT_OK;
   }
+  TRY(group_chunk(G, need, true));
   magic_sht_group::Chunk& c = G->chunks.back();
   char* hp = c.host + c.used;
   char* dp = c.dev + c.used;
@@ -2311,6 +2347,7 @@ int magic_sht_group_destroy(magic_sht_group* G) {
     if (c.dev) cudaFree(c.dev);
     if (c.host) cudaFreeHost(c.host);
   }
+  if (G->ring) cudaFree(G->ring);
   delete G;
   return MAGIC_SHT_OK;
 }

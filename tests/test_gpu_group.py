@@ -76,6 +76,26 @@ def test_group_equals_separate_calls(built, torch, precision):
         s.close()
 
 
+def test_group_many_calls_reuse_the_ring(built, torch):
+    """Uncaptured group calls with new output arrays each time take their
+    instance tables from a fixed device ring (wrapping more than once here):
+    every call stays equal to the instances' own calls."""
+    from magic_gb300 import SHTGroup
+    shts, specs, or2s = _make(torch)
+    ref_g = [s.transform_to_grid_space(sp, or2=o2) for s, sp, o2 in zip(shts, specs, or2s)]
+    torch.cuda.synchronize()
+    G = SHTGroup(shts)
+    for rep in range(160):
+        got_g = G.transform_to_grid_space(specs, or2s=or2s)  # fresh outputs every call
+        if rep % 40 == 39:
+            torch.cuda.synchronize()
+            for i in range(len(shts)):
+                _assert_equal(torch, got_g[i], ref_g[i], ("ring", rep, INSTANCES[i]))
+    G.close()
+    for s in shts:
+        s.close()
+
+
 def test_group_graph_replay(built, torch):
     from magic_gb300 import SHTGroup
     from magic_gb300.workload import FORWARD_FROM_INVERSE
