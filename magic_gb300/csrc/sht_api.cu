@@ -2130,6 +2130,11 @@ struct magic_sht_group {
   std::vector<Slot> slots;
   char* ring = nullptr;
   size_t ring_cap = 0, ring_off = 0;
+  // the FFTs of different instances run on these streams, forked from and
+  // joined back into the call's stream (one event each way per stream)
+  static constexpr int kFftStreams = 4;
+  cudaStream_t fft_st[kFftStreams] = {};
+  cudaEvent_t fork = nullptr, join[kFftStreams] = {};
 };
 
 namespace {
@@ -2253,13 +2258,35 @@ int group_legendre(magic_sht_group* G, const Deferred& D, bool inverse, bool vec
   return MAGIC_SHT_OK;
 }
 
-int group_ffts(const Deferred& D, bool inverse, cudaStream_t st) {
+// The FFT launches of the instances: consecutive instances on different
+// streams forked from `st`, so that the FFTs of small instances overlap the
+// others' (each launch counted in its handle's phase counters, untimed: the
+// phase events are recorded on the handle's stream only).
+int group_ffts(magic_sht_group* G, const Deferred& D, bool inverse, cudaStream_t st) {
+  constexpr int K = magic_sht_group::kFftStreams;
+  int n = 0;
+  for (const auto& f : D.fft) n += f.inverse == inverse;
+  if (n == 0) return MAGIC_SHT_OK;
+  CK(cudaEventRecord(G->fork, st));
+  const int ns = std::min(n, K);
+  for (int k = 0; k < ns; ++k) CK(cudaStreamWaitEvent(G->fft_st[k], G->fork, 0));
+  int i = 0;
+  magic_sht_handle* prev = nullptr;
   for (const auto& f : D.fft) {
     if (f.inverse != inverse) continue;
     magic_sht_handle* h = f.h;
-    PhaseScope ps(h, inverse ? MAGIC_SHT_PHASE_FFT_INV : MAGIC_SHT_PHASE_FFT_FWD);
-    if (inverse) CK(launch_fft_inverse(h->g, f.fs, fft_arith(h), h->fft_rows, st));
-    else CK(launch_fft_forward(h->g, f.fs, fft_arith(h), h->fft_rows, st));
+    if (prev && h != prev) ++i;  // the FFT batches of one instance stay on one stream
+    prev = h;
+    const int ph = inverse ? MAGIC_SHT_PHASE_FFT_INV : MAGIC_SHT_PHASE_FFT_FWD;
+    h->launches++;
+    h->phase_launches[ph]++;
+    cudaStream_t s = G->fft_st[i % ns];
+    if (inverse) CK(launch_fft_inverse(h->g, f.fs, fft_arith(h), h->fft_rows, s));
+    else CK(launch_fft_forward(h->g, f.fs, fft_arith(h), h->fft_rows, s));
+  }
+  for (int k = 0; k < ns; ++k) {
+    CK(cudaEventRecord(G->join[k], G->fft_st[k]));
+    CK(cudaStreamWaitEvent(st, G->join[k], 0));
   }
   return MAGIC_SHT_OK;
 }
@@ -2302,9 +2329,9 @@ int group_call(magic_sht_group* G, bool inverse, const std::vector<const void*>&
     if (inverse) {
       rc = group_legendre<InvSet>(G, D, true, false, capturing, st);
       if (!rc) rc = group_legendre<InvSet>(G, D, true, true, capturing, st);
-      if (!rc) rc = group_ffts(D, true, st);
+      if (!rc) rc = group_ffts(G, D, true, st);
     } else {
-      rc = group_ffts(D, false, st);
+      rc = group_ffts(G, D, false, st);
       if (!rc) rc = group_legendre<FwdSet>(G, D, false, false, capturing, st);
       if (!rc) rc = group_legendre<FwdSet>(G, D, false, true, capturing, st);
     }
@@ -2332,9 +2359,19 @@ int magic_sht_group_create(magic_sht_handle* const* handles, int n, magic_sht_gr
     for (int k = 0; k < i; ++k)
       if (handles[k] == handles[i]) return set_err(MAGIC_SHT_ERR_ARG, "handle %d appears twice in the group", i);
   }
+  DeviceGuard dg(handles[0]->device);
   magic_sht_group* G = new magic_sht_group();
   G->h.assign(handles, handles + n);
   G->device = handles[0]->device;
+  bool ok = cudaEventCreateWithFlags(&G->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; k < magic_sht_group::kFftStreams && ok; ++k)
+    ok = cudaStreamCreateWithFlags(&G->fft_st[k], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&G->join[k], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    magic_sht_group_destroy(G);
+    return set_err(MAGIC_SHT_ERR_CUDA, "group: stream or event creation failed");
+  }
   *out = G;
   return MAGIC_SHT_OK;
 }
@@ -2348,6 +2385,11 @@ int magic_sht_group_destroy(magic_sht_group* G) {
     if (c.host) cudaFreeHost(c.host);
   }
   if (G->ring) cudaFree(G->ring);
+  for (int k = 0; k < magic_sht_group::kFftStreams; ++k) {
+    if (G->fft_st[k]) cudaStreamDestroy(G->fft_st[k]);
+    if (G->join[k]) cudaEventDestroy(G->join[k]);
+  }
+  if (G->fork) cudaEventDestroy(G->fork);
   delete G;
   return MAGIC_SHT_OK;
 }
