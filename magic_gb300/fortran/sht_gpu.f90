@@ -186,11 +186,37 @@ contains
    end subroutine sht_check
 
    subroutine initialize_sht(l_scrambled_theta)
+      ! The plain FP64 form (the drop-in's arithmetic) unless the environment
+      ! variable MAGIC_SHT_PRECISION selects another form of the library:
+      ! fp64tc (FP64-accurate on the tensor cores, the same 1e-12 parity with
+      ! the native transforms), bf16x5, bf16x3, tf32x2 or fp32.
       logical, intent(out) :: l_scrambled_theta
       type(magic_sht_desc) :: d
+      character(len=16) :: form
+      integer :: length, status
       d%l_max = l_max; d%m_max = m_max; d%minc = minc
       d%n_theta_max = n_theta_max; d%n_phi_max = n_phi_max
       d%nlat_padded = nlat_padded; d%precision = 0; d%device = -1
+      call get_environment_variable('MAGIC_SHT_PRECISION', form, length, status)
+      if ( status == 0 .and. length > 0 ) then
+         select case ( trim(form) )
+         case ( 'fp64' )
+            d%precision = 0
+         case ( 'fp32' )
+            d%precision = 1
+         case ( 'bf16x3' )
+            d%precision = 2
+         case ( 'tf32x2' )
+            d%precision = 3
+         case ( 'fp64tc' )
+            d%precision = 4
+         case ( 'bf16x5' )
+            d%precision = 5
+         case default
+            call abortRun('magic_sht: MAGIC_SHT_PRECISION='//trim(form)// &
+                 &        ' is not one of fp64, fp64tc, bf16x5, bf16x3, tf32x2, fp32')
+         end select
+      end if
       call check(c_init(d, handle))
       l_scrambled_theta = .true.
    end subroutine initialize_sht
