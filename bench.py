@@ -293,11 +293,13 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(levels: int):
+def cpu_baseline(levels: int, threads: int = 0):
+    """The oracle's rate on `levels` levels of the set, with `threads` host
+    threads (0: every core)."""
     from oracle import oracle
     from magic_gb300.workload import spectra
     oracle.build_oracle()
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     oracle.set_threads(threads)
     o = oracle.OracleSHT(L_MAX, MINC, N_THETA, N_PHI)
     S = spectra(L_MAX, MINC, 13, seed=99)
@@ -832,6 +834,9 @@ def our_arm(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(args.cpu_levels)
+        # the same on one core (one level), beside the all-core figure
+        one = cpu_baseline(1, threads=1)
+        cpu["one_core"] = {k: one[k] for k in ("value", "unit", "cores", "sample")}
 
     if rank == 0:
         line = {
