@@ -72,3 +72,17 @@ def test_bind_types_match_c_structs():
         assert name in cs, name
         for path, fields in defs:
             assert fields == cs[name], (os.path.basename(path), name, fields, cs[name])
+
+
+def test_precision_switch_matches_header():
+    """MAGIC_SHT_PRECISION in the drop-in's initialize_sht maps each form name
+    to the MAGIC_SHT_* value of the header, and the Python names agree."""
+    from magic_gb300 import _lib
+    hdr = open(HEADER).read()
+    consts = {m.group(1).lower(): int(m.group(2))
+              for m in re.finditer(r"#define MAGIC_SHT_(FP64|FP32|BF16X3|TF32X2|FP64TC|BF16X5)\s+(\d+)", hdr)}
+    src = open(os.path.join(ROOT, "magic_gb300", "fortran", "sht_gpu.f90")).read()
+    cases = {m.group(1): int(m.group(2))
+             for m in re.finditer(r"case \( '(\w+)' \)\s*\n\s*d%precision = (\d+)", src)}
+    assert cases == consts, (cases, consts)
+    assert {k: _lib.PRECISIONS[k] for k in consts} == consts
