@@ -44,7 +44,7 @@ struct InvSet {
   const int* lcut;    // device [nlev] or null (then lcut0 for every level)
   const double* or2;  // device [nlev] or null (then or2_0; only OP_CURLT uses it)
   int lcut0;
-  int pad_;  // no padding bytes: group calls compare descriptors bytewise
+  int pad_;
   double or2_0;
 };
 
@@ -237,8 +237,6 @@ struct BcGrids {
 // of them: tile0 / blk0 are the instance's first tile of the persistent
 // kernel and first block of the pack kernel, and the instances' tiles follow
 // each other in the array's order.
-// (The structs above hold no padding bytes, so that equal descriptors compare
-// equal bytewise.)
 template <class Set>
 struct LegInst {
   ShtGeom g;

@@ -2108,26 +2108,21 @@ int magic_sht_graph_destroy(magic_sht_graph* gr) {
 struct magic_sht_group {
   std::vector<magic_sht_handle*> h;
   int device = 0;
-  // Device copies of the launches' instance arrays.  Calls captured into a
-  // graph use the kept copies: append-only while the group lives (the graph
-  // reads the copies it was captured with, from pinned memory that is never
-  // rewritten), an identical array uploaded once.  Other calls take a slot of
-  // a device ring written from pageable memory on the group's stream (the
-  // copy is staged before it returns, and stream order puts it after every
-  // earlier launch that read the slot), so repeated calls with new arrays
-  // reuse the same memory.
+  // Device copies of the launches' instance arrays.  A call captured into a
+  // graph takes new kept slots: append-only while the group lives, copied by
+  // the graph itself (a memcpy node from pinned memory that is never
+  // rewritten), so every replay reads what was captured and nothing outside
+  // that graph reads them (their device copies exist only once it runs).
+  // Other calls take a slot of a device ring written from pageable memory on
+  // the group's stream (the copy is staged before it returns, and stream
+  // order puts it after every earlier launch that read the slot), so repeated
+  // calls with new arrays reuse the same memory.
   struct Chunk {
     char* host = nullptr;  // pinned: the source of the asynchronous copies
     char* dev = nullptr;
     size_t cap = 0, used = 0;
   };
   std::vector<Chunk> chunks;
-  struct Slot {
-    const char* host;
-    const char* dev;
-    size_t bytes;
-  };
-  std::vector<Slot> slots;
   char* ring = nullptr;
   size_t ring_cap = 0, ring_off = 0;
   // the FFTs of different instances run on these streams, forked from and
@@ -2139,12 +2134,6 @@ struct magic_sht_group {
 
 namespace {
 
-static_assert(sizeof(ShtGeom) == 10 * 4 + 10 * 8, "ShtGeom holds padding bytes");
-static_assert(sizeof(InvSet) == MAGIC_MAX_FIELDS * sizeof(InvField) + 40, "InvSet holds padding bytes");
-static_assert(sizeof(FwdSet) == MAGIC_MAX_FIELDS * sizeof(FwdField) + 24, "FwdSet holds padding bytes");
-static_assert(sizeof(TcTables) == 12 * 8 + 6 * 4, "TcTables holds padding bytes");
-static_assert(sizeof(LegInst<InvSet>) == sizeof(ShtGeom) + sizeof(InvSet) + sizeof(TcTables) + 32,
-              "LegInst holds padding bytes");
 
 constexpr size_t kGroupChunk = 1 << 20;  // kept copies for captured calls
 constexpr size_t kGroupRing = 2 << 20;   // ring of the uncaptured calls (many calls' arrays)
@@ -2170,11 +2159,6 @@ int group_chunk(magic_sht_group* G, size_t need, bool capturing) {
 
 int group_upload(magic_sht_group* G, const void* p, size_t bytes, bool capturing, cudaStream_t st,
                  const void** out) {
-  for (const auto& sl : G->slots)
-    if (sl.bytes == bytes && !memcmp(sl.host, p, bytes)) {
-      *out = sl.dev;
-      return MAGIC_SHT_OK;
-    }
   const size_t need = align256(bytes);
   if (!capturing) {
     // room for the kept copies of a capture that may follow
@@ -2205,7 +2189,6 @@ int group_upload(magic_sht_group* G, const void* p, size_t bytes, bool capturing
   c.used += need;
   memcpy(hp, p, bytes);
   CK(cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, st));
-  G->slots.push_back({hp, dp, bytes});
   *out = dp;
   return MAGIC_SHT_OK;
 }
@@ -2313,10 +2296,10 @@ int group_call(magic_sht_group* G, bool inverse, const std::vector<const void*>&
   const bool capturing = cs == cudaStreamCaptureStatusActive;
   Deferred D;
   std::vector<char> was(G->h.size());
+  for (size_t i = 0; i < G->h.size(); ++i) was[i] = G->h[i]->capturing;
   int rc = MAGIC_SHT_OK;
   for (size_t i = 0; i < G->h.size() && rc == MAGIC_SHT_OK; ++i) {
     magic_sht_handle* h = G->h[i];
-    was[i] = h->capturing;
     h->capturing = h->capturing || capturing;
     h->defer = &D;
     h->defer_bimg = 0;

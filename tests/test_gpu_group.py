@@ -120,7 +120,17 @@ def test_group_graph_replay(built, torch):
             G.transform_to_lm_space(fins, outs=out_l)
         finally:
             gr = shts[0].graph_end()
+        # the same calls outside the graph before its first replay (the
+        # captured instance tables exist only when the graph runs)
+        G.transform_to_grid_space(specs, or2s=or2s, outs=out_g)
+        G.transform_to_lm_space(fins, outs=out_l)
         side.synchronize()
+        for i in range(len(shts)):
+            _assert_equal(torch, out_g[i], ref_g[i], ("eager after capture", INSTANCES[i]))
+            _assert_equal(torch, out_l[i], ref_l[i], ("eager after capture", INSTANCES[i]))
+        for d in out_g + out_l:
+            for v in d.values():
+                v.zero_()
         shts[0].graph_launch(gr)
         side.synchronize()
     for i in range(len(shts)):
