@@ -7,7 +7,7 @@ produced -- for every candidate setting of
 
   tc_kernel   persistent tensor-core kernels or one tile per CTA (3xBF16),
   tc_order    tile order of the persistent kernels (table or data reuse),
-  fft_rows    theta rows per CTA of the FP32 azimuthal FFT (8 or 16),
+  fft_rows    theta rows per CTA of the FP32 / double-float azimuthal FFTs (8 or 16),
   pipe_chunk  levels per chunk of the host-buffer pipeline (host arrays only),
 
 keeps the fastest, applies it to the handle and caches it in a JSON file keyed
@@ -50,7 +50,7 @@ def key(sht, n_levels: int, host: bool, device: str) -> str:
 def candidates(sht, host: bool) -> List[Dict[str, int]]:
     """Settings to try for this handle's precision form."""
     form = sht.precision
-    tc = form in ("bf16x3", "tf32x2")
+    tc = form in ("bf16x3", "tf32x2", "fp64tc", "bf16x5")  # persistent tensor-core kernels: tile order
     kernels = [0, 1] if form == "bf16x3" else [0]
     orders = [0, 1] if tc else [0]
     rows = [8, 16] if form != "fp64" else [0]
