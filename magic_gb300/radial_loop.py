@@ -10,9 +10,13 @@ steps (courant.f90:54-278), the analysis set (transform_to_lm_space), the
 conducting-boundary products (get_br_v_bcs, rIter.f90:263-277) and the
 spectral assembly (get_td with the boundary flags nBc).
 
-Configuration of the device kernels: Boussinesq (rho0 = 1), curl-form
-advection, magnetic field with Lorentz force, heat equation, Coriolis force,
-unit physical constants in get_nl.  Level 0 is the outer boundary (n_r_cmb,
+Configuration of the device kernels: by default Boussinesq (rho0 = 1),
+curl-form advection, magnetic field with Lorentz force, heat equation,
+Coriolis force, unit physical constants in get_nl (magic_sht_get_nl /
+magic_sht_get_td); with ``physics`` the reference's switches, constants and
+radial profiles through the general routines (magic_sht_get_nl_opts /
+magic_sht_get_td_opts): density and temperature profiles, composition,
+double-curl dwdt, the anelastic-liquid dsdt, the physical constants.  Level 0 is the outer boundary (n_r_cmb,
 nBc = ktopv), level n-1 the inner boundary (n_r_icb, nBc = kbotv), as in
 MagIC's radial ordering.  Every array is a CUDA tensor ([level][lm] complex
 spectra, [level][phi][theta] grids) and the stage runs on the current torch
@@ -59,13 +63,26 @@ class RadialLoop:
     omega_ma / omega_ic).  l_vr_cmb / l_vr_icb keep the radial velocity at a
     rigid boundary (special.f90).  The conducting-mantle / inner-core terms
     (get_br_v_bcs) run when l_b_nl_cmb / l_b_nl_icb hold (Namelists.f90:713-729:
-    stress-free and conducting)."""
+    stress-free and conducting).
+
+    ``physics`` (optional) selects the general get_nl / get_td: the
+    keyword arguments of SHT.get_nl_opts (``ViscHeatFac``, ``OhmLossFac``,
+    the profiles ``orho1``, ``beta``, ``otemp1``, ``visc``, ``lam``, the
+    low-conductivity flags ``lcr``, and the switches ``l_conv_nl``,
+    ``l_mag_LF``, ``l_heat_nl``, ``l_chemical_conv``, ``l_mag_nl``; the
+    curl form of the advection and ``l_anel`` off, which the transform set's
+    grids serve: the u.grad u form and the viscous heating need the
+    velocity-derivative grids) and of SHT.get_td_opts (``temp0``, ``epscXi``, ``l_corr``,
+    ``l_double_curl``, ``l_single_matrix``, ``l_anelastic_liquid``);
+    profiles are per level (numpy).  LFfac is the loop's own.  The Courant
+    condition then takes orho1 and orho2 = orho1^2 from the profile."""
 
     def __init__(self, sht: SHT, r, cor_fac: float, courfac: float = 2.5, alffac: float = 1.0,
                  LFfac: float = 1.0, opm: float = 1.0, l_cour_alf_damp: bool = True, lcut=None, epsc=None,
                  ktopv: int = 2, kbotv: int = 2, l_vr_cmb: bool = False, l_vr_icb: bool = False,
                  omega_ma: float = 0.0, omega_ic: float = 0.0, l_rot_ma: bool = False, l_rot_ic: bool = False,
-                 l_cond_ma: bool = False, l_cond_ic: bool = False, BIC: float = 0.0):
+                 l_cond_ma: bool = False, l_cond_ic: bool = False, BIC: float = 0.0,
+                 physics: Optional[dict] = None):
         if ktopv not in (1, 2) or kbotv not in (1, 2):
             raise ValueError("ktopv and kbotv are 1 (stress-free) or 2 (rigid)")
         self.s = sht
@@ -84,7 +101,10 @@ class RadialLoop:
         self.or2 = 1.0 / self.r ** 2
         lc = np.full(n, sht.l_max) if self.lcut is None else self.lcut
         delxr2, delxh2 = delx2(self.r, lc)
-        self.radial = {"orho1": np.ones(n), "orho2": np.ones(n), "or2": self.or2, "or4": self.or2 ** 2,
+        self.physics = self._physics(physics)
+        orho1 = np.ones(n) if self.physics is None or self.physics["profiles"].get("orho1") is None \
+            else self.physics["profiles"]["orho1"]
+        self.radial = {"orho1": orho1, "orho2": orho1 ** 2, "or2": self.or2, "or4": self.or2 ** 2,
                        "delxr2": delxr2, "delxh2": delxh2}
         # rIter.f90:180-187 (Fortran precedence: .and. before .or.)
         self.lMagNlBc = ((ktopv == 1 or l_cond_ma or (ktopv == 2 and l_rot_ma))
@@ -103,6 +123,42 @@ class RadialLoop:
         self.nbc[0], self.nbc[n - 1] = ktopv, kbotv
         self._dev = {}
 
+    NL_FLAGS = ("l_conv_nl", "l_mag_LF", "l_heat_nl", "l_chemical_conv", "l_mag_nl", "l_anel")
+    NL_CONST = ("ViscHeatFac", "OhmLossFac")
+    TD_FLAGS = ("l_corr", "l_double_curl", "l_single_matrix", "l_anelastic_liquid")
+    PROFILES = ("orho1", "beta", "otemp1", "visc", "lam", "temp0")
+
+    def _physics(self, physics: Optional[dict]):
+        """The general routines' arguments, split into switches, constants and
+        per-level profiles (or None for the default configuration)."""
+        if physics is None:
+            return None
+        p = dict(physics)
+        # the velocity-derivative grids of the u.grad u advection and of the
+        # anelastic viscous heating (rIter.f90:527-545) are not in the transform set
+        if not p.pop("l_adv_curl", True):
+            raise ValueError("the transform set serves the curl form of the advection (l_adv_curl)")
+        if p.get("l_anel", False):
+            raise ValueError("l_anel needs the velocity-derivative grids, which the transform set does not produce")
+        known = set(self.NL_FLAGS + self.NL_CONST + self.TD_FLAGS + self.PROFILES + ("lcr", "epscXi"))
+        unknown = set(p) - known
+        if unknown:
+            raise ValueError("unknown physics keys: %s" % sorted(unknown))
+        flags = {k: bool(p.get(k, d)) for k, d in (("l_conv_nl", True), ("l_mag_LF", True), ("l_heat_nl", True),
+                                                  ("l_chemical_conv", False), ("l_mag_nl", True), ("l_anel", False),
+                                                  ("l_corr", True), ("l_double_curl", False),
+                                                  ("l_single_matrix", False), ("l_anelastic_liquid", False))}
+        prof = {}
+        for k in self.PROFILES:
+            if p.get(k) is not None:
+                a = np.ascontiguousarray(p[k], dtype=np.float64)
+                if a.shape != (self.n,):
+                    raise ValueError("%s needs %d levels" % (k, self.n))
+                prof[k] = a
+        lcr = None if p.get("lcr") is None else np.ascontiguousarray(p["lcr"], dtype=np.int32)
+        return {"flags": flags, "const": {k: float(p[k]) for k in self.NL_CONST if k in p},
+                "epscXi": float(p.get("epscXi", 0.0)), "profiles": prof, "lcr": lcr}
+
     def _on(self, device):
         """The per-level arrays as CUDA tensors on `device` (made once): every
         call of the stage then takes device pointers, so none of them waits
@@ -114,6 +170,9 @@ class RadialLoop:
                  "lcut": None if self.lcut is None else f(self.lcut),
                  "epsc": None if self.epsc is None else f(np.asarray(self.epsc, dtype=np.float64)),
                  "radial": {k: f(v) for k, v in self.radial.items()}}
+            if self.physics is not None:
+                d["profiles"] = {k: f(v) for k, v in self.physics["profiles"].items()}
+                d["lcr"] = None if self.physics["lcr"] is None else f(self.physics["lcr"])
             self._dev[device] = d
         return self._dev[device]
 
@@ -143,10 +202,22 @@ class RadialLoop:
                  if spec.get(src[k]) is not None}
         lo, hi = self._lohi()
         out = out or {}
+        if self.physics is None:
+            nl_names, lm_names, td_names = _lib.LM_SPACE_IN, _lib.LM_SPACE_OUT, _lib.TD_OUT
+            nl_alloc = torch.empty
+        else:
+            # the general get_nl / get_td leave what a level does not form
+            # untouched (get_dpdt the l = 0 entry, get_td.f90:311-379):
+            # zero-filled once, those entries stay zero
+            xi = self.physics["flags"]["l_chemical_conv"]
+            nl_names = [k for k in _lib.NLF_OUT if xi or not k.startswith("VXi")]
+            lm_names = _lib.LM_SPACE_OUT + (_lib.LM_SPACE_OUT_XI if xi else [])
+            td_names = self._td_outputs()
+            nl_alloc = torch.zeros
         b = {"device": dev, "grids": grids,
-             "nl": {k: torch.empty((hi - lo, s.n_phi_max, s.nlat_padded), **f64) for k in _lib.LM_SPACE_IN},
-             "lm": {k: torch.empty((n, s.lm_max), **c128) for k in _lib.LM_SPACE_OUT},
-             "td": {k: out[k] if k in out else torch.empty((n, s.lm_max), **c128) for k in _lib.TD_OUT},
+             "nl": {k: nl_alloc((hi - lo, s.n_phi_max, s.nlat_padded), **f64) for k in nl_names},
+             "lm": {k: torch.empty((n, s.lm_max), **c128) for k in lm_names},
+             "td": {k: out[k] if k in out else nl_alloc((n, s.lm_max), **c128) for k in td_names},
              "dtrkc": torch.empty(n, **f64), "dthkc": torch.empty(n, **f64)}
         for flag, key in ((self.l_b_nl_cmb, "cmb"), (self.l_b_nl_icb, "icb")):
             if flag:
@@ -157,6 +228,21 @@ class RadialLoop:
             if flag:
                 b[key] = torch.empty(1, **f64)
         return b
+
+    def _td_outputs(self):
+        """The outputs of the general get_td the switches call for
+        (rIter.f90:410-428: get_dwdt, get_dsdt, get_dxidt, get_dbdt)."""
+        fl = self.physics["flags"]
+        names = []
+        if fl["l_conv_nl"] or fl["l_corr"]:
+            names += ["dwdt", "dzdt"] + (["dVxVhLM"] if fl["l_double_curl"] else ["dpdt"])
+        if fl["l_heat_nl"]:
+            names += ["dsdt", "dVSrLM"]
+        if fl["l_chemical_conv"]:
+            names += ["dxidt", "dVXirLM"]
+        if fl["l_mag_nl"]:
+            names += ["dbdt", "djdt", "dVxBhLM"]
+        return names
 
     def _rigid_kept_vr(self):
         """Boundary levels whose products get_nl forms at all (lMagNlBc) and
@@ -176,6 +262,10 @@ class RadialLoop:
         self._boundary_grids(g, 0, self.ktopv, self.omega_ma, self.l_vr_cmb)
         self._boundary_grids(g, n - 1, self.kbotv, self.omega_ic, self.l_vr_icb)
         lo, hi = self._lohi()
+        if self.physics is not None:
+            self._nl_td_general(spec, b, g, dv, lo, hi)
+            self._boundary_outputs(b, g, dv)
+            return
         nl = s.get_nl({k: v[lo:hi] for k, v in g.items()}, or2=dv["or2"][lo:hi], out=b["nl"])
         # at a rigid boundary the reference forms V x B with vr = vt = 0 (nBc = 2
         # branch of get_nl.f90:391-395: VxBt = or4 vp br, VxBp = 0); where the grid
@@ -199,6 +289,44 @@ class RadialLoop:
                 v[hi:].zero_()
         full["VSrLM"][0].zero_()
         full["VSrLM"][n - 1].zero_()
+        self._boundary_outputs(b, g, dv)
+        tdin = {k: spec[k] for k in ("w", "dw", "z")}
+        tdin.update({k: full[k] for k in ("AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "VxBrLM", "VxBtLM", "VxBpLM")})
+        s.get_td(tdin, dv["r"], self.cor_fac, lcut=dv["lcut"], epsc=dv["epsc"], nbc=dv["nbc"], out=b["td"])
+
+    def _nl_td_general(self, spec: Dict, b: Dict, g: Dict, dv: Dict, lo: int, hi: int):
+        """get_nl, the analysis set and get_td through the general routines:
+        get_nl_opts on the levels lo..hi-1 with their nBc (the boundary forms
+        of V x B at a rigid or stress-free boundary come from the kernel),
+        get_td_opts with the boundary flags of every level."""
+        s, n, ph = self.s, self.n, self.physics
+        fl, prof = ph["flags"], dv["profiles"]
+        sl = lambda t: None if t is None else t[lo:hi]  # noqa: E731
+        nl = s.get_nl_opts({k: v[lo:hi] for k, v in g.items()}, dv["r"][lo:hi], out=b["nl"], LFfac=self.LFfac,
+                           orho1=sl(prof.get("orho1")), beta=sl(prof.get("beta")), otemp1=sl(prof.get("otemp1")),
+                           visc=sl(prof.get("visc")), lam=sl(prof.get("lam")), nbc=dv["nbc"][lo:hi],
+                           lcr=sl(dv["lcr"]), **ph["const"],
+                           **{k: fl[k] for k in self.NL_FLAGS})
+        lc = None if dv["lcut"] is None else dv["lcut"][lo:hi]
+        full = b["lm"]
+        s.transform_to_lm_space(nl, lcut=lc, out={k: v[lo:hi] for k, v in full.items()})
+        for v in full.values():
+            if lo > 0:
+                v[:lo].zero_()
+            if hi < n:
+                v[hi:].zero_()
+        tdin = {k: spec[k] for k in ("w", "dw", "ddw", "z", "dz") if spec.get(k) is not None}
+        tdin.update({k: full[k] for k in ("AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "heatTermsLM", "VXitLM", "VxBrLM",
+                                          "VxBtLM", "VxBpLM") if k in full})
+        s.get_td_opts(tdin, dv["r"], self.cor_fac, outputs=list(b["td"]), out=b["td"], lcut=dv["lcut"],
+                      nbc=dv["nbc"], orho1=prof.get("orho1"), beta=prof.get("beta"), temp0=prof.get("temp0"),
+                      epsc=dv["epsc"], epscXi=ph["epscXi"], l_conv_nl=fl["l_conv_nl"], l_anel=fl["l_anel"],
+                      l_mag_nl=fl["l_mag_nl"], **{k: fl[k] for k in self.TD_FLAGS})
+
+    def _boundary_outputs(self, b: Dict, g: Dict, dv: Dict):
+        """The Courant steps, the Lorentz torques and the conducting-boundary
+        products of the stage."""
+        s, n = self.s, self.n
         b["dtrkc"].fill_(1e10)
         b["dthkc"].fill_(1e10)
         s.courant({k: g[k] for k in ("vrc", "vtc", "vpc", "brc", "btc", "bpc")}, dv["radial"],
@@ -213,9 +341,6 @@ class RadialLoop:
         if self.l_b_nl_icb:
             s.get_br_v_bcs(g["brc"][n - 1], g["vtc"][n - 1], g["vpc"][n - 1], self.omega_ic, self.or2[n - 1], 1.0,
                            out=b["icb"])
-        tdin = {k: spec[k] for k in ("w", "dw", "z")}
-        tdin.update({k: full[k] for k in ("AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "VxBrLM", "VxBtLM", "VxBpLM")})
-        s.get_td(tdin, dv["r"], self.cor_fac, lcut=dv["lcut"], epsc=dv["epsc"], nbc=dv["nbc"], out=b["td"])
 
     @staticmethod
     def _result(b: Dict) -> Dict:

@@ -364,3 +364,82 @@ def test_lorentz_torque_matches_oracle(built, torch, grid):
         assert abs(got_h - exp) <= 1e-12 * scale, (got_h, exp)
         assert got_d == got_h
     s.device_status()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg", [
+    dict(ktopv=2, kbotv=2, omega_ma=0.3, omega_ic=-0.2),
+    dict(ktopv=1, kbotv=2, l_cond_ma=True, omega_ma=0.25),
+    dict(ktopv=2, kbotv=1, l_rot_ma=True, l_cond_ma=True, l_vr_cmb=True, omega_ma=0.3),
+])
+def test_radial_loop_general_physics_default_matches(built, torch, cfg):
+    """The stage through the general get_nl / get_td (physics={}, the
+    reference's defaults) equals the stage through the Boussinesq kernels to
+    rounding, boundaries included (FP64 form)."""
+    from magic_gb300.radial_loop import RadialLoop
+    from magic_gb300.workload import grid_space_inputs
+    from conftest import rel_l2
+    L, minc, N, P, n = 63, 1, 96, 192, 5
+    s = make(L, minc, N, P)
+    r = np.linspace(1.538, 0.538, n)
+    lcut = np.array([L, L, L - 5, L, L], dtype=np.int32)
+    epsc = np.array([0.0, 0.3, 0.1, -0.2, 0.0])
+    spec = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(L, minc, n, seed=8).items()}
+    la = RadialLoop(s, r, cor_fac=50.0, lcut=lcut, epsc=epsc, **cfg)
+    a = la.step(spec)
+    b = RadialLoop(s, r, cor_fac=50.0, lcut=lcut, epsc=epsc, physics={}, **cfg).step(spec)
+    torch.cuda.synchronize()
+    for k in ("dwdt", "dzdt", "dpdt", "dsdt", "dbdt", "djdt", "dVxBhLM"):
+        x, y = a[k].cpu().numpy(), b[k].cpu().numpy()
+        for i in range(n):
+            if la.nbc[i] != 0 and k != "dVxBhLM":  # outputs get_td leaves untouched at a boundary
+                continue
+            # get_dpdt leaves l = 0 (lm = 1, get_td.f90:311-379): zero on the general path
+            xi, yi = (x[i][1:], y[i][1:]) if k == "dpdt" else (x[i], y[i])
+            if k == "dpdt":
+                assert y[i][0] == 0, (k, i)
+            if np.linalg.norm(xi) == 0:
+                assert np.linalg.norm(yi) == 0, (k, i)
+                continue
+            assert rel_l2(yi, xi) < 1e-12, (k, i, rel_l2(yi, xi))
+    np.testing.assert_array_equal(a["dtrkc"], b["dtrkc"])
+    np.testing.assert_array_equal(a["dthkc"], b["dthkc"])
+
+
+@pytest.mark.gpu
+def test_radial_loop_general_physics_composes_the_entry_points(built, torch):
+    """A stage with density and temperature profiles, composition and
+    double-curl dwdt: the loop's general path equals get_nl_opts -> the
+    analysis set -> get_td_opts called directly with the same switches and
+    profiles.  (l_anel needs velocity-derivative grids the transform set does
+    not produce: the loop refuses it.)"""
+    from magic_gb300.radial_loop import RadialLoop
+    from magic_gb300.workload import grid_space_inputs
+    L, minc, N, P, n = 63, 1, 96, 192, 6
+    s = make(L, minc, N, P)
+    r = np.linspace(1.538, 0.538, n)
+    rng = np.random.default_rng(3)
+    prof = {"orho1": 1.0 + 0.3 * rng.random(n), "beta": -0.5 * rng.random(n), "otemp1": 1.0 + 0.2 * rng.random(n),
+            "visc": 1.0 + 0.1 * rng.random(n), "lam": 1.0 + 0.1 * rng.random(n), "temp0": 1.0 + 0.2 * rng.random(n)}
+    physics = dict(prof, ViscHeatFac=0.7, OhmLossFac=0.4, l_chemical_conv=True, l_double_curl=True, epscXi=0.05)
+    with pytest.raises(ValueError):
+        RadialLoop(s, r, cor_fac=40.0, physics=dict(physics, l_anel=True))
+    spec = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(L, minc, n, seed=21).items()}
+    loop = RadialLoop(s, r, cor_fac=40.0, LFfac=0.8, ktopv=1, kbotv=1, physics=physics)
+    got = loop.step(spec)
+    torch.cuda.synchronize()
+    # the same by hand (lMagNlBc holds with stress-free boundaries: every level)
+    g = {k: v.clone() for k, v in got["grids"].items()}
+    nbc = torch.from_numpy(loop.nbc).cuda()
+    nl = s.get_nl_opts(g, r, LFfac=0.8, ViscHeatFac=0.7, OhmLossFac=0.4, nbc=nbc, l_chemical_conv=True,
+                       **{k: prof[k] for k in ("orho1", "beta", "otemp1", "visc", "lam")})
+    lm = s.transform_to_lm_space(nl)
+    tdin = {k: spec[k] for k in ("w", "dw", "ddw", "z", "dz")}
+    tdin.update({k: lm[k] for k in ("AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "heatTermsLM", "VXitLM", "VxBrLM",
+                                    "VxBtLM", "VxBpLM")})
+    outs = ["dwdt", "dzdt", "dVxVhLM", "dsdt", "dVSrLM", "dxidt", "dVXirLM", "dbdt", "djdt", "dVxBhLM"]
+    td = s.get_td_opts(tdin, r, 40.0, outputs=outs, nbc=nbc, orho1=prof["orho1"], beta=prof["beta"],
+                       temp0=prof["temp0"], epscXi=0.05, l_double_curl=True)
+    torch.cuda.synchronize()
+    for k in outs:
+        assert torch.equal(got[k], td[k]), k
