@@ -167,6 +167,12 @@ typedef struct magic_sht_grid_space_args {
   double *vrc, *vtc, *vpc, *cvrc, *cvtc, *cvpc;
   double *brc, *btc, *bpc, *cbrc, *cbtc, *cbpc;
   long long grid_ld;                        /* doubles between levels (>= nlat_padded*n_phi_max) */
+  /* velocity derivatives of the u.grad u advection and the anelastic viscous
+   * heating (rIter.f90:527-545), at grid_ld; NULL skips them:
+   * torpol_to_spat(dw, ddw, dz) -> dvrdrc, dvtdrc, dvpdrc;
+   * pol_to_grad_spat(w) -> dvrdtc, dvrdpc; torpol_to_dphspat(dw, z) -> dvtdpc, dvpdpc.
+   * cvrc alone (without cvtc, cvpc) is pol_to_curlr_spat(z) (rIter.f90:540). */
+  double *dvrdrc, *dvtdrc, *dvpdrc, *dvrdtc, *dvrdpc, *dvtdpc, *dvpdpc;
 } magic_sht_grid_space_args;
 
 typedef struct magic_sht_lm_space_args {

@@ -41,9 +41,14 @@ LM_SPACE_OUT = ["AdvrLM", "AdvtLM", "AdvpLM", "VSrLM", "VStLM", "VSpLM", "VxBrLM
                 "VxBpLM", "heatTermsLM"]
 
 
+# velocity derivatives of the u.grad u advection and the anelastic viscous heating
+GRID_SPACE_OUT_DV = ["dvrdrc", "dvtdrc", "dvpdrc", "dvrdtc", "dvrdpc", "dvtdpc", "dvpdpc"]
+
+
 class GridSpaceArgs(ctypes.Structure):
     _fields_ = ([(n, _V) for n in GRID_SPACE_IN] + [("spec_ld", ctypes.c_longlong)] +
-                [(n, _V) for n in GRID_SPACE_OUT] + [("grid_ld", ctypes.c_longlong)])
+                [(n, _V) for n in GRID_SPACE_OUT] + [("grid_ld", ctypes.c_longlong)] +
+                [(n, _V) for n in GRID_SPACE_OUT_DV])
 
 
 TD_IN = ["w", "dw", "z", "AdvrLM", "AdvtLM", "AdvpLM", "VStLM", "VxBrLM", "VxBtLM", "VxBpLM"]

@@ -1486,21 +1486,25 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
   if (n > h->pipe_chunk && !h->capturing &&
       all_host({a->s, a->p, a->xi, a->w, a->dw, a->ddw, a->z, a->dz, a->b, a->db, a->ddb, a->aj, a->dj,
                 a->sc, a->pc, a->xic, a->vrc, a->vtc, a->vpc, a->cvrc, a->cvtc, a->cvpc, a->brc, a->btc,
-                a->bpc, a->cbrc, a->cbtc, a->cbpc, lcut, or2})) {
+                a->bpc, a->cbrc, a->cbtc, a->cbpc, a->dvrdrc, a->dvtdrc, a->dvpdrc, a->dvrdtc, a->dvrdpc,
+                a->dvtdpc, a->dvpdpc, lcut, or2})) {
     if (lcut)
       for (int i = 0; i < n; ++i)
         if (!is_device_ptr(lcut) && (lcut[i] < 0 || lcut[i] > g.l_max))
           return set_err(MAGIC_SHT_ERR_LCUT, "lcut[%d]=%d outside [0, %d]", i, lcut[i], g.l_max);
     const double* const ins[13] = {a->s, a->p, a->xi, a->w, a->dw, a->ddw, a->z, a->dz,
                                    a->b, a->db, a->ddb, a->aj, a->dj};
-    double* const outs[15] = {a->sc, a->pc, a->xic, a->vrc, a->vtc, a->vpc, a->cvrc, a->cvtc,
-                              a->cvpc, a->brc, a->btc, a->bpc, a->cbrc, a->cbtc, a->cbpc};
+    constexpr int NO = 22;
+    double* const outs[NO] = {a->sc,     a->pc,     a->xic,    a->vrc,    a->vtc,    a->vpc,    a->cvrc,
+                              a->cvtc,   a->cvpc,   a->brc,    a->btc,    a->bpc,    a->cbrc,   a->cbtc,
+                              a->cbpc,   a->dvrdrc, a->dvtdrc, a->dvpdrc, a->dvrdtc, a->dvrdpc, a->dvtdpc,
+                              a->dvpdpc};
     std::vector<PipeArray> arrs;
-    std::vector<int> idx_in(13, -1), idx_out(15, -1);
+    std::vector<int> idx_in(13, -1), idx_out(NO, -1);
     const size_t sb = (size_t)a->spec_ld * 16, gb = (size_t)a->grid_ld * 8;
     for (int i = 0; i < 13; ++i)
       if (ins[i]) { idx_in[i] = (int)arrs.size(); arrs.push_back({ins[i], sb, (size_t)g.lm_max * 16, false, 0}); }
-    for (int i = 0; i < 15; ++i)
+    for (int i = 0; i < NO; ++i)
       if (outs[i]) { idx_out[i] = (int)arrs.size(); arrs.push_back({outs[i], gb, (size_t)g.n_phi * g.ld * 8, true, 0}); }
     if (or2) arrs.push_back({or2, 8, 8, false, 0});
     if (lcut) arrs.push_back({lcut, 4, 4, false, 0});
@@ -1511,10 +1515,12 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
       double** pin[13] = {(double**)&b.s, (double**)&b.p, (double**)&b.xi, (double**)&b.w, (double**)&b.dw,
                           (double**)&b.ddw, (double**)&b.z, (double**)&b.dz, (double**)&b.b, (double**)&b.db,
                           (double**)&b.ddb, (double**)&b.aj, (double**)&b.dj};
-      double** pout[15] = {&b.sc, &b.pc, &b.xic, &b.vrc, &b.vtc, &b.vpc, &b.cvrc, &b.cvtc,
-                           &b.cvpc, &b.brc, &b.btc, &b.bpc, &b.cbrc, &b.cbtc, &b.cbpc};
+      double** pout[NO] = {&b.sc,     &b.pc,     &b.xic,    &b.vrc,    &b.vtc,    &b.vpc,    &b.cvrc,
+                           &b.cvtc,   &b.cvpc,   &b.brc,    &b.btc,    &b.bpc,    &b.cbrc,   &b.cbtc,
+                           &b.cbpc,   &b.dvrdrc, &b.dvtdrc, &b.dvpdrc, &b.dvrdtc, &b.dvrdpc, &b.dvtdpc,
+                           &b.dvpdpc};
       for (int i = 0; i < 13; ++i) *pin[i] = idx_in[i] >= 0 ? (double*)d[idx_in[i]] : nullptr;
-      for (int i = 0; i < 15; ++i) *pout[i] = idx_out[i] >= 0 ? (double*)d[idx_out[i]] : nullptr;
+      for (int i = 0; i < NO; ++i) *pout[i] = idx_out[i] >= 0 ? (double*)d[idx_out[i]] : nullptr;
       (void)r0;
       return magic_sht_transform_to_grid_space(h, nr, i_or2 >= 0 ? (const double*)d[i_or2] : nullptr,
                                                i_lc >= 0 ? (const int*)d[i_lc] : nullptr, &b);
@@ -1548,7 +1554,18 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n, const double* 
   if (iw >= 0 && iddw >= 0 && iz >= 0 && idz >= 0 && a->cvrc && a->cvtc && a->cvpc) {
     sc.push_back({ref(OP_DLH, iz), go(a->cvrc), 0});
     vc.push_back({ref(OP_COPY, idz), ref(OP_CURLT, iw, iddw), go(a->cvtc), go(a->cvpc), 0});
+  } else if (iz >= 0 && a->cvrc && !a->cvtc && !a->cvpc) {
+    sc.push_back({ref(OP_DLH, iz), go(a->cvrc), 0});  // pol_to_curlr_spat(z) of the u.grad u set (:540)
   }
+  // velocity derivatives (rIter.f90:527-545): torpol_to_spat(dw, ddw, dz),
+  // pol_to_grad_spat(w), torpol_to_dphspat(dw, z)
+  if (idw >= 0 && iddw >= 0 && idz >= 0 && a->dvrdrc && a->dvtdrc && a->dvpdrc) {
+    sc.push_back({ref(OP_DLH, idw), go(a->dvrdrc), 0});
+    vc.push_back({ref(OP_COPY, iddw), ref(OP_COPY, idz), go(a->dvtdrc), go(a->dvpdrc), 0});
+  }
+  if (iw >= 0 && a->dvrdtc && a->dvrdpc) vc.push_back({ref(OP_DLH, iw), SpecRef(), go(a->dvrdtc), go(a->dvrdpc), 0});
+  if (idw >= 0 && iz >= 0 && a->dvtdpc && a->dvpdpc)
+    vc.push_back({ref(OP_IM, idw), ref(OP_IM, iz), go(a->dvtdpc), go(a->dvpdpc), FFT_OSIN2});
   // magnetic field and current (rIter.f90:606, 610)
   int ib = -1, idb = -1, iddb = -1, iaj = -1, idj = -1;
   if (a->b) ib = si(a->b);
@@ -2389,7 +2406,10 @@ int magic_sht_group_transform_to_grid_space(magic_sht_group* G, const int* n_lev
                           (const void*)b.dj, (const void*)b.sc, (const void*)b.pc, (const void*)b.xic,
                           (const void*)b.vrc, (const void*)b.vtc, (const void*)b.vpc, (const void*)b.cvrc,
                           (const void*)b.cvtc, (const void*)b.cvpc, (const void*)b.brc, (const void*)b.btc,
-                          (const void*)b.bpc, (const void*)b.cbrc, (const void*)b.cbtc, (const void*)b.cbpc})
+                          (const void*)b.bpc, (const void*)b.cbrc, (const void*)b.cbtc, (const void*)b.cbpc,
+                          (const void*)b.dvrdrc, (const void*)b.dvtdrc, (const void*)b.dvpdrc,
+                          (const void*)b.dvrdtc, (const void*)b.dvrdpc, (const void*)b.dvtdpc,
+                          (const void*)b.dvpdpc})
       arr.push_back(p);
   }
   return group_call(G, true, arr, [&](int i) {

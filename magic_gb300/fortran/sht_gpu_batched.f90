@@ -30,6 +30,7 @@ module sht_gpu_batched
       integer(c_long_long) :: spec_ld
       type(c_ptr) :: sc, pc, xic, vrc, vtc, vpc, cvrc, cvtc, cvpc, brc, btc, bpc, cbrc, cbtc, cbpc
       integer(c_long_long) :: grid_ld
+      type(c_ptr) :: dvrdrc, dvtdrc, dvpdrc, dvrdtc, dvrdpc, dvtdpc, dvpdpc
    end type magic_sht_grid_space_args
 
    type, bind(C) :: magic_sht_lm_space_args
@@ -270,6 +271,8 @@ contains
       a%vpc = c_null_ptr; a%cvrc = c_null_ptr; a%cvtc = c_null_ptr; a%cvpc = c_null_ptr
       a%brc = c_null_ptr; a%btc = c_null_ptr; a%bpc = c_null_ptr; a%cbrc = c_null_ptr
       a%cbtc = c_null_ptr; a%cbpc = c_null_ptr
+      a%dvrdrc = c_null_ptr; a%dvtdrc = c_null_ptr; a%dvpdrc = c_null_ptr; a%dvrdtc = c_null_ptr
+      a%dvrdpc = c_null_ptr; a%dvtdpc = c_null_ptr; a%dvpdpc = c_null_ptr
       a%spec_ld = 0; a%grid_ld = 0
    end subroutine null_grid_args
 

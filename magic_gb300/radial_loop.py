@@ -69,10 +69,10 @@ class RadialLoop:
     keyword arguments of SHT.get_nl_opts (``ViscHeatFac``, ``OhmLossFac``,
     the profiles ``orho1``, ``beta``, ``otemp1``, ``visc``, ``lam``, the
     low-conductivity flags ``lcr``, and the switches ``l_conv_nl``,
-    ``l_mag_LF``, ``l_heat_nl``, ``l_chemical_conv``, ``l_mag_nl``; the
-    curl form of the advection and ``l_anel`` off, which the transform set's
-    grids serve: the u.grad u form and the viscous heating need the
-    velocity-derivative grids) and of SHT.get_td_opts (``temp0``, ``epscXi``, ``l_corr``,
+    ``l_adv_curl``, ``l_mag_LF``, ``l_heat_nl``, ``l_chemical_conv``,
+    ``l_mag_nl``, ``l_anel``; the u.grad u form and the viscous heating
+    take the velocity-derivative grids of the synthesis set,
+    rIter.f90:527-545) and of SHT.get_td_opts (``temp0``, ``epscXi``, ``l_corr``,
     ``l_double_curl``, ``l_single_matrix``, ``l_anelastic_liquid``);
     profiles are per level (numpy).  LFfac is the loop's own.  The Courant
     condition then takes orho1 and orho2 = orho1^2 from the profile."""
@@ -123,7 +123,7 @@ class RadialLoop:
         self.nbc[0], self.nbc[n - 1] = ktopv, kbotv
         self._dev = {}
 
-    NL_FLAGS = ("l_conv_nl", "l_mag_LF", "l_heat_nl", "l_chemical_conv", "l_mag_nl", "l_anel")
+    NL_FLAGS = ("l_conv_nl", "l_adv_curl", "l_mag_LF", "l_heat_nl", "l_chemical_conv", "l_mag_nl", "l_anel")
     NL_CONST = ("ViscHeatFac", "OhmLossFac")
     TD_FLAGS = ("l_corr", "l_double_curl", "l_single_matrix", "l_anelastic_liquid")
     PROFILES = ("orho1", "beta", "otemp1", "visc", "lam", "temp0")
@@ -134,17 +134,12 @@ class RadialLoop:
         if physics is None:
             return None
         p = dict(physics)
-        # the velocity-derivative grids of the u.grad u advection and of the
-        # anelastic viscous heating (rIter.f90:527-545) are not in the transform set
-        if not p.pop("l_adv_curl", True):
-            raise ValueError("the transform set serves the curl form of the advection (l_adv_curl)")
-        if p.get("l_anel", False):
-            raise ValueError("l_anel needs the velocity-derivative grids, which the transform set does not produce")
         known = set(self.NL_FLAGS + self.NL_CONST + self.TD_FLAGS + self.PROFILES + ("lcr", "epscXi"))
         unknown = set(p) - known
         if unknown:
             raise ValueError("unknown physics keys: %s" % sorted(unknown))
-        flags = {k: bool(p.get(k, d)) for k, d in (("l_conv_nl", True), ("l_mag_LF", True), ("l_heat_nl", True),
+        flags = {k: bool(p.get(k, d)) for k, d in (("l_conv_nl", True), ("l_adv_curl", True),
+                                                  ("l_mag_LF", True), ("l_heat_nl", True),
                                                   ("l_chemical_conv", False), ("l_mag_nl", True), ("l_anel", False),
                                                   ("l_corr", True), ("l_double_curl", False),
                                                   ("l_single_matrix", False), ("l_anelastic_liquid", False))}
@@ -181,7 +176,7 @@ class RadialLoop:
             g["vrc"][i].zero_()
         else:          # rigid (rIter.f90:570-592, lDeriv off: cvr untouched)
             self.s.v_rigid_boundary({"vr": g["vrc"][i], "vt": g["vtc"][i], "vp": g["vpc"][i]},
-                                    self.r[i] ** 2, omega, keep_vr)
+                                    self.r[i] ** 2 / self.radial["orho1"][i], omega, keep_vr)
 
     def _lohi(self):
         return (0, self.n) if self.lMagNlBc else (1, self.n - 1)
@@ -200,6 +195,16 @@ class RadialLoop:
                "cvpc": "ddw", "brc": "b", "btc": "b", "bpc": "b", "cbrc": "ddb", "cbtc": "ddb", "cbpc": "ddb"}
         grids = {k: torch.empty((n, s.n_phi_max, s.nlat_padded), **f64) for k in _lib.GRID_SPACE_OUT
                  if spec.get(src[k]) is not None}
+        grid_out = dict(grids)
+        if self._derivatives():
+            # the u.grad u advection and the viscous heating (rIter.f90:527-545);
+            # the u.grad u form takes cvrc alone (pol_to_curlr_spat(z), :540)
+            for k in _lib.GRID_SPACE_OUT_DV:
+                grids[k] = grid_out[k] = torch.empty((n, s.n_phi_max, s.nlat_padded), **f64)
+            if not self.physics["flags"]["l_adv_curl"]:
+                for k in ("cvtc", "cvpc"):
+                    grids.pop(k, None)
+                    grid_out[k] = None
         lo, hi = self._lohi()
         out = out or {}
         if self.physics is None:
@@ -214,7 +219,7 @@ class RadialLoop:
             lm_names = _lib.LM_SPACE_OUT + (_lib.LM_SPACE_OUT_XI if xi else [])
             td_names = self._td_outputs()
             nl_alloc = torch.zeros
-        b = {"device": dev, "grids": grids,
+        b = {"device": dev, "grids": grids, "grid_out": grid_out,
              "nl": {k: nl_alloc((hi - lo, s.n_phi_max, s.nlat_padded), **f64) for k in nl_names},
              "lm": {k: torch.empty((n, s.lm_max), **c128) for k in lm_names},
              "td": {k: out[k] if k in out else nl_alloc((n, s.lm_max), **c128) for k in td_names},
@@ -228,6 +233,14 @@ class RadialLoop:
             if flag:
                 b[key] = torch.empty(1, **f64)
         return b
+
+    def _derivatives(self):
+        """Whether the stage needs the velocity-derivative grids (the u.grad u
+        advection or the anelastic viscous heating)."""
+        if self.physics is None:
+            return False
+        fl = self.physics["flags"]
+        return (fl["l_conv_nl"] and not fl["l_adv_curl"]) or fl["l_anel"]
 
     def _td_outputs(self):
         """The outputs of the general get_td the switches call for
@@ -258,7 +271,7 @@ class RadialLoop:
         allocation and no synchronisation (so it can be captured)."""
         s, n = self.s, self.n
         dv = self._on(b["device"])
-        g = s.transform_to_grid_space(spec, or2=dv["or2"], lcut=dv["lcut"], out=b["grids"])
+        g = s.transform_to_grid_space(spec, or2=dv["or2"], lcut=dv["lcut"], out=b["grid_out"])
         self._boundary_grids(g, 0, self.ktopv, self.omega_ma, self.l_vr_cmb)
         self._boundary_grids(g, n - 1, self.kbotv, self.omega_ic, self.l_vr_icb)
         lo, hi = self._lohi()

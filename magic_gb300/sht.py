@@ -303,7 +303,7 @@ class SHT:
     def _levels(self, arr, n, lcut):
         return _per_level(lcut, np.int32, n, "lcut")
 
-    def _grid_space_call(self, spec: dict, or2, lcut, out):
+    def _grid_space_call(self, spec: dict, or2, lcut, out, derivatives=False):
         """The argument block of one transform_to_grid_space call: (n, args,
         outputs, or2 pointer, lcut pointer, arrays to keep alive)."""
         keys = [k for k in _lib.GRID_SPACE_IN if spec.get(k) is not None]
@@ -323,8 +323,20 @@ class SHT:
             "brc": "b", "btc": "b", "bpc": "b", "cbrc": "ddb", "cbtc": "ddb", "cbpc": "ddb",
         }
         outs = {} if out is None else dict(out)
+        skip = {k for k, v in outs.items() if v is None}  # outputs the caller does not want
+        for k in skip:
+            del outs[k]
         for k in _lib.GRID_SPACE_OUT:
-            if spec.get(produced[k]) is None:
+            if k in skip or (spec.get(produced[k]) is None and k not in outs):
+                continue
+            if k not in outs:
+                outs[k], _ = self._grid(first, n)
+            setattr(a, k, outs[k].data_ptr() if _is_torch(outs[k]) else outs[k].ctypes.data)
+        # velocity derivatives (rIter.f90:527-545) on request or when given in `out`
+        need = {"dvrdrc": ("dw", "ddw", "dz"), "dvtdrc": ("dw", "ddw", "dz"), "dvpdrc": ("dw", "ddw", "dz"),
+                "dvrdtc": ("w",), "dvrdpc": ("w",), "dvtdpc": ("dw", "z"), "dvpdpc": ("dw", "z")}
+        for k in _lib.GRID_SPACE_OUT_DV:
+            if k in skip or (k not in outs and not (derivatives and all(spec.get(x) is not None for x in need[k]))):
                 continue
             if k not in outs:
                 outs[k], _ = self._grid(first, n)
@@ -335,10 +347,16 @@ class SHT:
         keep += [or2_arr, lc_arr]
         return n, a, outs, por2, plc, keep
 
-    def transform_to_grid_space(self, spec: dict, or2=None, lcut=None, out: Optional[dict] = None):
+    def transform_to_grid_space(self, spec: dict, or2=None, lcut=None, out: Optional[dict] = None,
+                                derivatives: bool = False):
         """rIter.f90:466-622 for many radial levels; `spec` maps the names of
-        _lib.GRID_SPACE_IN to (n_levels, lm_max) arrays; returns the grid dict."""
-        n, a, outs, por2, plc, keep = self._grid_space_call(spec, or2, lcut, out)
+        _lib.GRID_SPACE_IN to (n_levels, lm_max) arrays; returns the grid dict.
+        ``derivatives``: also the velocity derivatives of the u.grad u
+        advection and the anelastic viscous heating (``dvrdrc`` ..
+        ``dvpdpc``, rIter.f90:527-545).  An entry None in ``out`` leaves that
+        output out (``cvtc`` and ``cvpc`` None: the u.grad u set's
+        pol_to_curlr_spat(z) alone, rIter.f90:540)."""
+        n, a, outs, por2, plc, keep = self._grid_space_call(spec, or2, lcut, out, derivatives)
         check(self._lib.magic_sht_transform_to_grid_space(self._h, n, por2, plc, ctypes.byref(a)))
         return outs
 

@@ -411,8 +411,7 @@ def test_radial_loop_general_physics_composes_the_entry_points(built, torch):
     """A stage with density and temperature profiles, composition and
     double-curl dwdt: the loop's general path equals get_nl_opts -> the
     analysis set -> get_td_opts called directly with the same switches and
-    profiles.  (l_anel needs velocity-derivative grids the transform set does
-    not produce: the loop refuses it.)"""
+    profiles."""
     from magic_gb300.radial_loop import RadialLoop
     from magic_gb300.workload import grid_space_inputs
     L, minc, N, P, n = 63, 1, 96, 192, 6
@@ -423,7 +422,7 @@ def test_radial_loop_general_physics_composes_the_entry_points(built, torch):
             "visc": 1.0 + 0.1 * rng.random(n), "lam": 1.0 + 0.1 * rng.random(n), "temp0": 1.0 + 0.2 * rng.random(n)}
     physics = dict(prof, ViscHeatFac=0.7, OhmLossFac=0.4, l_chemical_conv=True, l_double_curl=True, epscXi=0.05)
     with pytest.raises(ValueError):
-        RadialLoop(s, r, cor_fac=40.0, physics=dict(physics, l_anel=True))
+        RadialLoop(s, r, cor_fac=40.0, physics=dict(physics, l_anell=True))  # unknown key
     spec = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(L, minc, n, seed=21).items()}
     loop = RadialLoop(s, r, cor_fac=40.0, LFfac=0.8, ktopv=1, kbotv=1, physics=physics)
     got = loop.step(spec)
