@@ -786,14 +786,15 @@ class SHTGroup:
         for s in self.shts:
             s._bind_torch_stream()
 
-    def transform_to_grid_space(self, specs, or2s=None, lcuts=None, outs=None):
-        """specs[i] (and or2s[i], lcuts[i], outs[i]) as
+    def transform_to_grid_space(self, specs, or2s=None, lcuts=None, outs=None, derivatives=False):
+        """specs[i] (and or2s[i], lcuts[i], outs[i], ``derivatives``) as
         SHT.transform_to_grid_space of instance i; returns the list of grid dicts."""
         k = len(self.shts)
         or2s = or2s or [None] * k
         lcuts = lcuts or [None] * k
         outs = outs or [None] * k
-        calls = [s._grid_space_call(specs[i], or2s[i], lcuts[i], outs[i]) for i, s in enumerate(self.shts)]
+        calls = [s._grid_space_call(specs[i], or2s[i], lcuts[i], outs[i], derivatives)
+                 for i, s in enumerate(self.shts)]
         self._bind()
         n = (ctypes.c_int * k)(*[c[0] for c in calls])
         args = (_lib.GridSpaceArgs * k)(*[c[1] for c in calls])

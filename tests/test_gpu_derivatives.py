@@ -68,7 +68,7 @@ def test_derivative_grids_match_oracle(built, oracle_mod, torch, grid, prec):
     s = make(*grid, prec=prec)
     o = oracle_mod.OracleSHT(L, minc, N, P)
     spec_in = grid_space_inputs(L, minc, n, seed=61)
-    lcut = np.array([L, L - 2, max(L - 9, 1), L, L - 1], dtype=np.int32)
+    lcut = np.array([L, 0, max(L - 9, 1), 1, L - 1], dtype=np.int32)  # lcut 0 and 1: the edge degrees
     ref = _derivative_ref(o, spec_in, lcut)
     din = {k: torch.from_numpy(v).cuda() for k, v in spec_in.items()}
     or2 = torch.from_numpy(or2_levels(n)).cuda()

@@ -7,7 +7,8 @@ instances in one pack + one persistent tensor-core launch per direction and
 field kind.  Each tile is computed by the same arithmetic as in the
 instance's own call, so the group's outputs must equal the instances' own
 calls bit for bit; those calls are compared with the oracle for every
-instance size in test_gpu_instances.py.  Also: per-level lcut, a CUDA-graph
+instance size in test_gpu_instances.py.  Also: per-level lcut, the
+velocity-derivative grids, a CUDA-graph
 capture of both group calls replayed, and the argument checks."""
 import numpy as np
 import pytest
@@ -69,6 +70,16 @@ def test_group_equals_separate_calls(built, torch, precision):
         for i in range(len(shts)):
             _assert_equal(torch, got_g[i], ref_g[i], ("grid", rep, INSTANCES[i]))
             _assert_equal(torch, got_l[i], ref_l[i], ("lm", rep, INSTANCES[i]))
+    # with the velocity-derivative grids (and cvrc alone, the u.grad u set)
+    skip = {"cvtc": None, "cvpc": None}
+    ref_d = [s.transform_to_grid_space(sp, or2=o2, lcut=lc, derivatives=True, out=skip)
+             for s, sp, o2, lc in zip(shts, specs, or2s, lcuts)]
+    got_d = G.transform_to_grid_space(specs, or2s=or2s, lcuts=lcuts, outs=[dict(skip) for _ in shts],
+                                      derivatives=True)
+    torch.cuda.synchronize()
+    for i in range(len(shts)):
+        assert "dvrdrc" in got_d[i] and "cvtc" not in got_d[i]
+        _assert_equal(torch, got_d[i], ref_d[i], ("derivatives", INSTANCES[i]))
     for s in shts:
         s.device_status()
     G.close()

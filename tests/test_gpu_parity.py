@@ -253,6 +253,22 @@ def test_graph_replay_matches_direct(built, torch):
     s.graph_destroy(gr)
 
 
+def test_zero_levels_are_no_ops(built, torch):
+    """n_levels = 0 on every batched entry point: status OK, nothing written
+    (host and device arrays)."""
+    from magic_gb300.workload import grid_space_inputs, FORWARD_FROM_INVERSE
+    s = make(31, 1, 48, 96)
+    for dev in (False, True):
+        spec_in = {k: v[:0] for k, v in grid_space_inputs(31, 1, 2, seed=1).items()}
+        if dev:
+            spec_in = {k: torch.from_numpy(v).cuda() for k, v in spec_in.items()}
+        g = s.transform_to_grid_space(spec_in, derivatives=True)
+        assert all(v.shape[0] == 0 for v in g.values()) and "dvrdrc" in g
+        lm = s.transform_to_lm_space({k: g[v] for k, v in FORWARD_FROM_INVERSE.items()})
+        assert all(v.shape[0] == 0 for v in lm.values())
+    s.device_status()
+
+
 def test_error_codes(built, torch):
     from magic_gb300._lib import ShtError
     s = make(31, 1, 48, 96)
