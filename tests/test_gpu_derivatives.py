@@ -181,3 +181,28 @@ def test_radial_loop_derivative_physics_composes_the_entry_points(built, torch, 
     if physics.get("l_anel"):
         assert float(torch.linalg.vector_norm(lm["heatTermsLM"])) > 0
     s.device_status()
+
+
+def test_radial_loop_rigid_boundaries_with_density_profile(built, oracle_mod, torch):
+    """Rigid rotating boundaries under a density profile: v_rigid_boundary
+    takes r^2 rho0 = r^2 / orho1 (nonlinear_bcs.f90:160-172), against the
+    oracle's restatement; the anelastic stage runs to its end."""
+    from magic_gb300.radial_loop import RadialLoop
+    from magic_gb300.workload import grid_space_inputs
+    L, minc, N, P, n = 31, 1, 48, 96, 5
+    s = make(L, minc, N, P)
+    r = np.linspace(1.538, 0.538, n)
+    orho1 = 1.0 + 0.5 * np.linspace(0.0, 1.0, n)
+    spec = {k: torch.from_numpy(v).cuda() for k, v in grid_space_inputs(L, minc, n, seed=29).items()}
+    loop = RadialLoop(s, r, cor_fac=40.0, ktopv=2, kbotv=2, omega_ma=0.3, omega_ic=-0.2,
+                      physics=dict(orho1=orho1, l_anel=True, l_adv_curl=False))
+    got = loop.step(spec)
+    torch.cuda.synchronize()
+    g = got["grids"]
+    for i, om in ((0, 0.3), (n - 1, -0.2)):
+        b = oracle_mod.v_rigid_boundary(N, P, r[i] ** 2 / orho1[i], om, False, np.zeros((P, N)))
+        for k, key in (("vr", "vrc"), ("vt", "vtc"), ("vp", "vpc")):
+            np.testing.assert_allclose(g[key][i].cpu().numpy(), b[k], rtol=0, atol=1e-14 * max(1.0, np.abs(b[k]).max()))
+    for k in loop._td_outputs():
+        assert bool(torch.isfinite(got[k]).all()), k
+    s.device_status()
