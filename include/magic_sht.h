@@ -199,6 +199,45 @@ int magic_sht_transform_to_grid_space(magic_sht_handle* h, int n_levels, const d
 int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n_levels, const int* lcut,
                                     const magic_sht_lm_space_args* a);
 
+/* ---- any facade routines, many radial levels per call ----
+ * Each job is one facade routine of module sht (sht_native.f90:16-20) applied
+ * to every level of its arrays, with the routine's own argument order:
+ * in[] its array inputs, out[] its outputs (spectra complex, spec_ld apart per
+ * level; grids grid_ld doubles apart), unused slots NULL.  All jobs of one call
+ * share one batched Legendre launch per field kind and one FFT launch per
+ * direction.  lcut (per level, NULL = l_max) applies to every job; or2 (per
+ * level) is the or2 argument of torpol_to_curl_spat jobs (required when one is
+ * present).  Inputs may be shared between jobs; outputs must be distinct.
+ * Host pointers are staged (pipelined over chunks of levels when every array
+ * is in host memory); device pointers stay asynchronous.  Errors:
+ * MAGIC_SHT_ERR_ARG for an unknown routine, a job of the other direction, a
+ * missing array, repeated outputs or a curl job without or2. */
+enum {
+  /* synthesis (magic_sht_inv_batch): in[] -> out[] */
+  MAGIC_SHT_JOB_SCAL_TO_SPAT = 1,        /* Slm -> fieldc */
+  MAGIC_SHT_JOB_SCAL_TO_GRAD_SPAT = 2,   /* Slm -> gradtc, gradpc */
+  MAGIC_SHT_JOB_POL_TO_GRAD_SPAT = 3,    /* Slm -> gradtc, gradpc */
+  MAGIC_SHT_JOB_TORPOL_TO_SPAT = 4,      /* Wlm, dWlm, Zlm -> vrc, vtc, vpc */
+  MAGIC_SHT_JOB_SPHTOR_TO_SPAT = 5,      /* dWlm, Zlm -> vtc, vpc */
+  MAGIC_SHT_JOB_TORPOL_TO_CURL_SPAT = 6, /* Blm, ddBlm, Jlm, dJlm -> cvrc, cvtc, cvpc (or2 per level) */
+  MAGIC_SHT_JOB_POL_TO_CURLR_SPAT = 7,   /* Qlm -> cvrc */
+  MAGIC_SHT_JOB_TORPOL_TO_DPHSPAT = 8,   /* dWlm, Zlm -> dvtdp, dvpdp */
+  /* analysis (magic_sht_fwd_batch) */
+  MAGIC_SHT_JOB_SCAL_TO_SH = 101,        /* f -> fLM */
+  MAGIC_SHT_JOB_SPAT_TO_QST = 102,       /* f, g, h -> qLM, sLM, tLM */
+  MAGIC_SHT_JOB_SPAT_TO_SPHERTOR = 103   /* f, g -> fLM, gLM */
+};
+typedef struct magic_sht_job {
+  int routine;                              /* MAGIC_SHT_JOB_* */
+  int pad_;
+  const double *in[4];
+  double *out[3];
+} magic_sht_job;
+int magic_sht_inv_batch(magic_sht_handle* h, int n_levels, const double* or2, const int* lcut,
+                        long long spec_ld, long long grid_ld, const magic_sht_job* jobs, int n_jobs);
+int magic_sht_fwd_batch(magic_sht_handle* h, int n_levels, const int* lcut, long long grid_ld,
+                        long long spec_ld, const magic_sht_job* jobs, int n_jobs);
+
 /* ---- asynchronous host-buffer batches.  With on != 0, a batched call whose
  * arrays are all in host memory and that spans more than 16 levels returns once
  * its chunked copies and kernels are queued (instead of when the host outputs

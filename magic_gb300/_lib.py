@@ -135,6 +135,20 @@ class TdOut(ctypes.Structure):
     _fields_ = [(n, _V) for n in TDF_OUT] + [("spec_ld", ctypes.c_longlong)]
 
 
+# batched facade jobs (magic_sht_inv_batch / magic_sht_fwd_batch): routine
+# name -> (MAGIC_SHT_JOB_* code, number of array inputs, number of outputs)
+JOBS = {
+    "scal_to_spat": (1, 1, 1), "scal_to_grad_spat": (2, 1, 2), "pol_to_grad_spat": (3, 1, 2),
+    "torpol_to_spat": (4, 3, 3), "sphtor_to_spat": (5, 2, 2), "torpol_to_curl_spat": (6, 4, 3),
+    "pol_to_curlr_spat": (7, 1, 1), "torpol_to_dphspat": (8, 2, 2),
+    "scal_to_SH": (101, 1, 1), "spat_to_qst": (102, 3, 3), "spat_to_sphertor": (103, 2, 2),
+}
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("routine", ctypes.c_int), ("pad_", ctypes.c_int), ("in", _V * 4), ("out", _V * 3)]
+
+
 # every entry point of include/magic_sht.h with its argument types
 SIGNATURES = {
     "magic_sht_init": [ctypes.POINTER(Desc), ctypes.POINTER(_V)],
@@ -167,6 +181,10 @@ SIGNATURES = {
     "magic_sht_transform_to_grid_space": [_V, ctypes.c_int, _V, _V,
                                           ctypes.POINTER(GridSpaceArgs)],
     "magic_sht_transform_to_lm_space": [_V, ctypes.c_int, _V, ctypes.POINTER(LmSpaceArgs)],
+    "magic_sht_inv_batch": [_V, ctypes.c_int, _V, _V, ctypes.c_longlong, ctypes.c_longlong, ctypes.POINTER(Job),
+                            ctypes.c_int],
+    "magic_sht_fwd_batch": [_V, ctypes.c_int, _V, ctypes.c_longlong, ctypes.c_longlong, ctypes.POINTER(Job),
+                            ctypes.c_int],
     "magic_sht_set_host_async": [_V, ctypes.c_int],
     "magic_sht_set_tuning": [_V, ctypes.POINTER(Tuning)],
     "magic_sht_get_tuning": [_V, ctypes.POINTER(Tuning)],

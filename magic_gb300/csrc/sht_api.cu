@@ -3,12 +3,14 @@
 // (src/sht_native.f90:16-20) and the batched radial-loop transform set
 // (src/rIter.f90:466-712).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <map>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -1444,7 +1446,7 @@ static int pipelined_levels(magic_sht_handle* h, int n, int chunk, std::vector<P
 }
 
 // the host-buffer pipeline runs when every given array is in host memory
-static bool all_host(std::initializer_list<const void*> ptrs) {
+static bool all_host_v(const std::vector<const void*>& ptrs) {
   bool any = false;
   for (const void* p : ptrs) {
     if (!p) continue;
@@ -1453,7 +1455,7 @@ static bool all_host(std::initializer_list<const void*> ptrs) {
   }
   return any;
 }
-
+static bool all_host(std::initializer_list<const void*> ptrs) { return all_host_v(std::vector<const void*>(ptrs)); }
 
 // ------------------------------------------------------ radial-loop sets
 static int level_ctl(magic_sht_handle* h, CallCtx& cx, int n, const int* lcut, const double* or2,
@@ -2061,6 +2063,201 @@ int magic_sht_transform_to_lm_space(magic_sht_handle* h, int n, const int* lcut,
   TRY(cx.prepare());
   TRY(run_forward(h, cx, lv, sc, vc, hs_sc, hs_vc));
   return cx.finish();
+}
+
+// ------------------------------------------------ batched facade jobs
+// Any facade routines over many levels in one call: each job becomes the
+// scalar / vector jobs its single-level routine builds (above), and all of
+// them go through one run_inverse / run_forward.
+namespace {
+struct JobShape {
+  int n_in, n_out;
+  bool inv;
+};
+bool job_shape(int routine, JobShape& s) {
+  switch (routine) {
+    case MAGIC_SHT_JOB_SCAL_TO_SPAT: s = {1, 1, true}; return true;
+    case MAGIC_SHT_JOB_SCAL_TO_GRAD_SPAT: s = {1, 2, true}; return true;
+    case MAGIC_SHT_JOB_POL_TO_GRAD_SPAT: s = {1, 2, true}; return true;
+    case MAGIC_SHT_JOB_TORPOL_TO_SPAT: s = {3, 3, true}; return true;
+    case MAGIC_SHT_JOB_SPHTOR_TO_SPAT: s = {2, 2, true}; return true;
+    case MAGIC_SHT_JOB_TORPOL_TO_CURL_SPAT: s = {4, 3, true}; return true;
+    case MAGIC_SHT_JOB_POL_TO_CURLR_SPAT: s = {1, 1, true}; return true;
+    case MAGIC_SHT_JOB_TORPOL_TO_DPHSPAT: s = {2, 2, true}; return true;
+    case MAGIC_SHT_JOB_SCAL_TO_SH: s = {1, 1, false}; return true;
+    case MAGIC_SHT_JOB_SPAT_TO_QST: s = {3, 3, false}; return true;
+    case MAGIC_SHT_JOB_SPAT_TO_SPHERTOR: s = {2, 2, false}; return true;
+    default: return false;
+  }
+}
+}  // namespace
+
+static int batch_jobs(magic_sht_handle* h, bool inv, int n, const double* or2, const int* lcut, long long spec_ld,
+                      long long grid_ld, const magic_sht_job* jobs, int n_jobs) {
+  TRY(check_handle(h));
+  if (n < 0 || n_jobs < 0 || (n_jobs > 0 && !jobs)) return set_err(MAGIC_SHT_ERR_ARG, "null jobs or negative counts");
+  if (n == 0 || n_jobs == 0) return MAGIC_SHT_OK;
+  const ShtGeom& g = h->g;
+  if (spec_ld < g.lm_max || grid_ld < (long long)g.n_phi * g.ld)
+    return set_err(MAGIC_SHT_ERR_ARG, "spec_ld/grid_ld smaller than one level");
+  bool curl = false;
+  std::vector<const void*> all;
+  std::vector<const double*> ins, outs;
+  for (int j = 0; j < n_jobs; ++j) {
+    JobShape s;
+    if (!job_shape(jobs[j].routine, s) || s.inv != inv)
+      return set_err(MAGIC_SHT_ERR_ARG, "job %d: routine %d is not a %s routine", j, jobs[j].routine,
+                     inv ? "synthesis" : "analysis");
+    for (int k = 0; k < 4; ++k)
+      if ((k < s.n_in) != (jobs[j].in[k] != nullptr))
+        return set_err(MAGIC_SHT_ERR_ARG, "job %d: input %d %s", j, k, k < s.n_in ? "missing" : "not used (NULL)");
+    for (int k = 0; k < 3; ++k)
+      if ((k < s.n_out) != (jobs[j].out[k] != nullptr))
+        return set_err(MAGIC_SHT_ERR_ARG, "job %d: output %d %s", j, k, k < s.n_out ? "missing" : "not used (NULL)");
+    for (int k = 0; k < s.n_in; ++k) { ins.push_back(jobs[j].in[k]); all.push_back(jobs[j].in[k]); }
+    for (int k = 0; k < s.n_out; ++k) { outs.push_back(jobs[j].out[k]); all.push_back(jobs[j].out[k]); }
+    curl = curl || jobs[j].routine == MAGIC_SHT_JOB_TORPOL_TO_CURL_SPAT;
+  }
+  if (curl && !or2) return set_err(MAGIC_SHT_ERR_ARG, "torpol_to_curl_spat jobs need or2 per level");
+  {
+    std::vector<const double*> o = outs;
+    std::sort(o.begin(), o.end());
+    if (std::adjacent_find(o.begin(), o.end()) != o.end()) return set_err(MAGIC_SHT_ERR_ARG, "repeated output array");
+    for (const double* p : ins)
+      if (std::binary_search(o.begin(), o.end(), p)) return set_err(MAGIC_SHT_ERR_ARG, "an output is also an input");
+  }
+  DeviceGuard dg(h->device);
+  const size_t sb = (size_t)spec_ld * 16, gb = (size_t)grid_ld * 8;
+  const size_t s_last = (size_t)g.lm_max * 16, g_last = (size_t)g.n_phi * g.ld * 8;
+  all.push_back(lcut);
+  all.push_back(or2);
+  if (n > h->pipe_chunk && !h->capturing && all_host_v(all)) {
+    if (lcut)
+      for (int i = 0; i < n; ++i)
+        if (lcut[i] < 0 || lcut[i] > g.l_max)
+          return set_err(MAGIC_SHT_ERR_LCUT, "lcut[%d]=%d outside [0, %d]", i, lcut[i], g.l_max);
+    // one pipelined array per distinct input and per output
+    std::vector<PipeArray> arrs;
+    std::map<const double*, int> seen;
+    std::vector<std::array<int, 4>> iin(n_jobs);
+    std::vector<std::array<int, 3>> iout(n_jobs);
+    for (int j = 0; j < n_jobs; ++j) {
+      JobShape s;
+      job_shape(jobs[j].routine, s);
+      for (int k = 0; k < s.n_in; ++k) {
+        const double* p = jobs[j].in[k];
+        auto it = seen.find(p);
+        if (it == seen.end()) {
+          it = seen.emplace(p, (int)arrs.size()).first;
+          arrs.push_back({p, inv ? sb : gb, inv ? s_last : g_last, false, 0});
+        }
+        iin[j][k] = it->second;
+      }
+      for (int k = 0; k < s.n_out; ++k) {
+        iout[j][k] = (int)arrs.size();
+        arrs.push_back({jobs[j].out[k], inv ? gb : sb, inv ? g_last : s_last, true, 0});
+      }
+    }
+    const int i_or2 = or2 ? (int)arrs.size() : -1;
+    if (or2) arrs.push_back({or2, 8, 8, false, 0});
+    const int i_lc = lcut ? (int)arrs.size() : -1;
+    if (lcut) arrs.push_back({lcut, 4, 4, false, 0});
+    return pipelined_levels(h, n, h->pipe_chunk, arrs, [&](int r0, int nr, const std::vector<char*>& d) {
+      std::vector<magic_sht_job> b(jobs, jobs + n_jobs);
+      for (int j = 0; j < n_jobs; ++j) {
+        JobShape s;
+        job_shape(jobs[j].routine, s);
+        for (int k = 0; k < s.n_in; ++k) b[j].in[k] = (const double*)d[iin[j][k]];
+        for (int k = 0; k < s.n_out; ++k) b[j].out[k] = (double*)d[iout[j][k]];
+      }
+      (void)r0;
+      return batch_jobs(h, inv, nr, i_or2 >= 0 ? (const double*)d[i_or2] : nullptr,
+                        i_lc >= 0 ? (const int*)d[i_lc] : nullptr, spec_ld, grid_ld, b.data(), n_jobs);
+    });
+  }
+  CallCtx cx(h);
+  LevelCtl lv;
+  std::vector<int> lc;
+  TRY(level_ctl(h, cx, n, lcut, or2, lv, lc));
+  lv.spec_ld = spec_ld;
+  lv.grid_ld = grid_ld;
+  std::map<const double*, int> seen;
+  auto in_idx = [&](const double* p) {
+    auto it = seen.find(p);
+    if (it != seen.end()) return it->second;
+    const int i = inv ? cx.spec_in(p, n, spec_ld) : cx.grid_in(p, n, grid_ld);
+    seen.emplace(p, i);
+    return i;
+  };
+  std::vector<int> hs_sc, hs_vc;
+  if (inv) {
+    std::vector<ScalarInv> sc;
+    std::vector<VectorInv> vc;
+    for (int j = 0; j < n_jobs; ++j) {
+      JobShape sh;
+      job_shape(jobs[j].routine, sh);
+      int s[4], o[3];
+      for (int k = 0; k < sh.n_in; ++k) s[k] = in_idx(jobs[j].in[k]);
+      for (int k = 0; k < sh.n_out; ++k) o[k] = cx.grid_out(jobs[j].out[k], n, grid_ld);
+      switch (jobs[j].routine) {  // as the single-level routines above
+        case MAGIC_SHT_JOB_SCAL_TO_SPAT: sc.push_back({ref(OP_COPY, s[0]), o[0], 0}); break;
+        case MAGIC_SHT_JOB_POL_TO_CURLR_SPAT: sc.push_back({ref(OP_DLH, s[0]), o[0], 0}); break;
+        case MAGIC_SHT_JOB_SCAL_TO_GRAD_SPAT: vc.push_back({ref(OP_COPY, s[0]), SpecRef(), o[0], o[1], 0}); break;
+        case MAGIC_SHT_JOB_POL_TO_GRAD_SPAT: vc.push_back({ref(OP_DLH, s[0]), SpecRef(), o[0], o[1], 0}); break;
+        case MAGIC_SHT_JOB_TORPOL_TO_SPAT:
+          sc.push_back({ref(OP_DLH, s[0]), o[0], 0});
+          vc.push_back({ref(OP_COPY, s[1]), ref(OP_COPY, s[2]), o[1], o[2], 0});
+          break;
+        case MAGIC_SHT_JOB_SPHTOR_TO_SPAT: vc.push_back({ref(OP_COPY, s[0]), ref(OP_COPY, s[1]), o[0], o[1], 0}); break;
+        case MAGIC_SHT_JOB_TORPOL_TO_DPHSPAT:
+          vc.push_back({ref(OP_IM, s[0]), ref(OP_IM, s[1]), o[0], o[1], FFT_OSIN2});
+          break;
+        case MAGIC_SHT_JOB_TORPOL_TO_CURL_SPAT:
+          sc.push_back({ref(OP_DLH, s[2]), o[0], 0});
+          vc.push_back({ref(OP_COPY, s[3]), ref(OP_CURLT, s[0], s[1]), o[1], o[2], 0});
+          break;
+        default: break;
+      }
+    }
+    for (size_t i = 0; i < sc.size(); ++i) hs_sc.push_back(cx.tmp(hs_bytes(h, n)));
+    for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_inv_bytes(h, n, true)));
+    TRY(cx.prepare());
+    TRY(run_inverse(h, cx, lv, sc, vc, hs_sc, hs_vc));
+  } else {
+    std::vector<ScalarFwd> sc;
+    std::vector<VectorFwd> vc;
+    for (int j = 0; j < n_jobs; ++j) {
+      JobShape sh;
+      job_shape(jobs[j].routine, sh);
+      int gi[4], so[3];
+      for (int k = 0; k < sh.n_in; ++k) gi[k] = in_idx(jobs[j].in[k]);
+      for (int k = 0; k < sh.n_out; ++k) so[k] = cx.spec_out(jobs[j].out[k], n, spec_ld);
+      switch (jobs[j].routine) {
+        case MAGIC_SHT_JOB_SCAL_TO_SH: sc.push_back({gi[0], so[0]}); break;
+        case MAGIC_SHT_JOB_SPAT_TO_QST:
+          sc.push_back({gi[0], so[0]});
+          vc.push_back({gi[1], gi[2], so[1], so[2]});
+          break;
+        case MAGIC_SHT_JOB_SPAT_TO_SPHERTOR: vc.push_back({gi[0], gi[1], so[0], so[1]}); break;
+        default: break;
+      }
+    }
+    for (size_t i = 0; i < sc.size(); ++i) hs_sc.push_back(cx.tmp(hs_bytes(h, n)));
+    for (size_t i = 0; i < 2 * vc.size(); ++i) hs_vc.push_back(cx.tmp(hs_bytes(h, n)));
+    TRY(cx.prepare());
+    TRY(run_forward(h, cx, lv, sc, vc, hs_sc, hs_vc));
+  }
+  return cx.finish();
+}
+
+int magic_sht_inv_batch(magic_sht_handle* h, int n, const double* or2, const int* lcut, long long spec_ld,
+                        long long grid_ld, const magic_sht_job* jobs, int n_jobs) {
+  return batch_jobs(h, true, n, or2, lcut, spec_ld, grid_ld, jobs, n_jobs);
+}
+
+int magic_sht_fwd_batch(magic_sht_handle* h, int n, const int* lcut, long long grid_ld, long long spec_ld,
+                        const magic_sht_job* jobs, int n_jobs) {
+  return batch_jobs(h, false, n, nullptr, lcut, spec_ld, grid_ld, jobs, n_jobs);
 }
 
 // ------------------------------------------------------------ graphs

@@ -48,6 +48,22 @@ module sht_gpu_batched
       integer(c_long_long) :: spec_ld
    end type magic_sht_td_args
 
+   ! one facade routine over many levels (magic_sht_inv_batch / _fwd_batch):
+   ! in(:) its array inputs, out(:) its outputs in the routine's argument
+   ! order (c_loc of the first level), unused slots c_null_ptr
+   type, bind(C) :: magic_sht_job
+      integer(c_int) :: routine, pad_
+      type(c_ptr) :: in(4)
+      type(c_ptr) :: out(3)
+   end type magic_sht_job
+
+   integer(c_int), parameter, public :: MAGIC_SHT_JOB_SCAL_TO_SPAT = 1, MAGIC_SHT_JOB_SCAL_TO_GRAD_SPAT = 2, &
+        &    MAGIC_SHT_JOB_POL_TO_GRAD_SPAT = 3, MAGIC_SHT_JOB_TORPOL_TO_SPAT = 4,                         &
+        &    MAGIC_SHT_JOB_SPHTOR_TO_SPAT = 5, MAGIC_SHT_JOB_TORPOL_TO_CURL_SPAT = 6,                      &
+        &    MAGIC_SHT_JOB_POL_TO_CURLR_SPAT = 7, MAGIC_SHT_JOB_TORPOL_TO_DPHSPAT = 8,                     &
+        &    MAGIC_SHT_JOB_SCAL_TO_SH = 101, MAGIC_SHT_JOB_SPAT_TO_QST = 102,                               &
+        &    MAGIC_SHT_JOB_SPAT_TO_SPHERTOR = 103
+
    interface
       integer(c_int) function c_to_grid(h, n, or2, lcut, a) bind(C, name='magic_sht_transform_to_grid_space')
          import :: c_int, c_ptr, magic_sht_grid_space_args
@@ -95,36 +111,76 @@ module sht_gpu_batched
          type(c_ptr), value :: h
          integer(c_int), value :: n
       end function
+      integer(c_int) function c_inv_batch(h, n, or2, lcut, spec_ld, grid_ld, jobs, n_jobs) &
+            &        bind(C, name='magic_sht_inv_batch')
+         import :: c_int, c_ptr, c_long_long, magic_sht_job
+         type(c_ptr), value :: h
+         integer(c_int), value :: n
+         type(c_ptr), value :: or2, lcut
+         integer(c_long_long), value :: spec_ld, grid_ld
+         type(magic_sht_job), intent(in) :: jobs(*)
+         integer(c_int), value :: n_jobs
+      end function
+      integer(c_int) function c_fwd_batch(h, n, lcut, grid_ld, spec_ld, jobs, n_jobs) &
+            &        bind(C, name='magic_sht_fwd_batch')
+         import :: c_int, c_ptr, c_long_long, magic_sht_job
+         type(c_ptr), value :: h
+         integer(c_int), value :: n
+         type(c_ptr), value :: lcut
+         integer(c_long_long), value :: grid_ld, spec_ld
+         type(magic_sht_job), intent(in) :: jobs(*)
+         integer(c_int), value :: n_jobs
+      end function
    end interface
 
    public :: transform_to_grid_space_gpu, transform_to_lm_space_gpu, get_nl_gpu, get_td_gpu, &
-        &    dt_courant_gpu, reserve_levels_gpu
+        &    dt_courant_gpu, reserve_levels_gpu, magic_sht_job, inv_batch_gpu, fwd_batch_gpu
 
 contains
 
    subroutine transform_to_grid_space_gpu(or2, lcut, w, dw, ddw, z, dz, vrc, vtc, vpc, cvrc, cvtc, cvpc, &
               &                           s, p, xi, b, db, ddb, aj, dj, sc, pc, xic, brc, btc, bpc,    &
-              &                           cbrc, cbtc, cbpc)
+              &                           cbrc, cbtc, cbpc, dvrdrc, dvtdrc, dvpdrc, dvrdtc, dvrdpc,    &
+              &                           dvtdpc, dvpdpc)
       ! transform_to_grid_space of every level (column) of the spectra at
       ! once: or2(nR) = 1/r^2, lcut(nR) = l_R.  The velocity set is always
       ! transformed; s, p, xi (scalars) and b, db, ddb, aj, dj (magnetic
-      ! field) with their grids only when present.
+      ! field) with their grids only when present.  Without cvtc and cvpc,
+      ! cvrc is pol_to_curlr_spat(z) (the u.grad u set, rIter.f90:540);
+      ! dvrdrc .. dvpdpc, when present, are the velocity derivatives
+      ! (rIter.f90:527-545).
       real(cp),       target, contiguous, intent(in) :: or2(:)
       integer(c_int), target, contiguous, intent(in) :: lcut(:)
       complex(cp), target, contiguous, intent(in) :: w(:,:), dw(:,:), ddw(:,:), z(:,:), dz(:,:)
       real(cp), target, contiguous, intent(out) :: vrc(:,:,:), vtc(:,:,:), vpc(:,:,:)
-      real(cp), target, contiguous, intent(out) :: cvrc(:,:,:), cvtc(:,:,:), cvpc(:,:,:)
+      real(cp), target, contiguous, intent(out) :: cvrc(:,:,:)
+      real(cp), target, contiguous, optional, intent(out) :: cvtc(:,:,:), cvpc(:,:,:)
       complex(cp), target, contiguous, optional, intent(in) :: s(:,:), p(:,:), xi(:,:)
       complex(cp), target, contiguous, optional, intent(in) :: b(:,:), db(:,:), ddb(:,:), aj(:,:), dj(:,:)
       real(cp), target, contiguous, optional, intent(out) :: sc(:,:,:), pc(:,:,:), xic(:,:,:)
       real(cp), target, contiguous, optional, intent(out) :: brc(:,:,:), btc(:,:,:), bpc(:,:,:)
       real(cp), target, contiguous, optional, intent(out) :: cbrc(:,:,:), cbtc(:,:,:), cbpc(:,:,:)
+      real(cp), target, contiguous, optional, intent(out) :: dvrdrc(:,:,:), dvtdrc(:,:,:), dvpdrc(:,:,:)
+      real(cp), target, contiguous, optional, intent(out) :: dvrdtc(:,:,:), dvrdpc(:,:,:)
+      real(cp), target, contiguous, optional, intent(out) :: dvtdpc(:,:,:), dvpdpc(:,:,:)
       type(magic_sht_grid_space_args) :: a
 
       call null_grid_args(a)
       a%w = c_loc(w); a%dw = c_loc(dw); a%ddw = c_loc(ddw); a%z = c_loc(z); a%dz = c_loc(dz)
       a%vrc = c_loc(vrc); a%vtc = c_loc(vtc); a%vpc = c_loc(vpc)
-      a%cvrc = c_loc(cvrc); a%cvtc = c_loc(cvtc); a%cvpc = c_loc(cvpc)
+      a%cvrc = c_loc(cvrc)
+      if ( present(cvtc) .and. present(cvpc) ) then
+         a%cvtc = c_loc(cvtc); a%cvpc = c_loc(cvpc)
+      end if
+      if ( present(dvrdrc) .and. present(dvtdrc) .and. present(dvpdrc) ) then
+         a%dvrdrc = c_loc(dvrdrc); a%dvtdrc = c_loc(dvtdrc); a%dvpdrc = c_loc(dvpdrc)
+      end if
+      if ( present(dvrdtc) .and. present(dvrdpc) ) then
+         a%dvrdtc = c_loc(dvrdtc); a%dvrdpc = c_loc(dvrdpc)
+      end if
+      if ( present(dvtdpc) .and. present(dvpdpc) ) then
+         a%dvtdpc = c_loc(dvtdpc); a%dvpdpc = c_loc(dvpdpc)
+      end if
       if ( present(s) .and. present(sc) ) then
          a%s = c_loc(s); a%sc = c_loc(sc)
       end if
@@ -241,6 +297,41 @@ contains
       call sht_check(c_get_td_nbc(sht_handle(), int(size(w, 2), c_int), c_loc(r), c_loc(lcut), &
            &                      real(cor_fac, c_double), c_loc(epsc), c_loc(nbc), a))
    end subroutine get_td_gpu
+
+   subroutine inv_batch_gpu(n_levels, spec_ld, grid_ld, jobs, or2, lcut)
+      ! synthesis jobs (MAGIC_SHT_JOB_SCAL_TO_SPAT .. _TORPOL_TO_DPHSPAT) over
+      ! n_levels levels in one call: spectra spec_ld complex apart per level,
+      ! grids grid_ld reals apart; or2(nR) for torpol_to_curl_spat jobs,
+      ! lcut(nR) = l_R for all jobs.
+      integer, intent(in) :: n_levels
+      integer(c_long_long), intent(in) :: spec_ld, grid_ld
+      type(magic_sht_job), intent(in) :: jobs(:)
+      real(cp),       target, contiguous, optional, intent(in) :: or2(:)
+      integer(c_int), target, contiguous, optional, intent(in) :: lcut(:)
+      type(c_ptr) :: por2, plc
+
+      por2 = c_null_ptr
+      plc = c_null_ptr
+      if ( present(or2) ) por2 = c_loc(or2)
+      if ( present(lcut) ) plc = c_loc(lcut)
+      call sht_check(c_inv_batch(sht_handle(), int(n_levels, c_int), por2, plc, spec_ld, grid_ld, jobs, &
+           &                     int(size(jobs), c_int)))
+   end subroutine inv_batch_gpu
+
+   subroutine fwd_batch_gpu(n_levels, grid_ld, spec_ld, jobs, lcut)
+      ! analysis jobs (MAGIC_SHT_JOB_SCAL_TO_SH, _SPAT_TO_QST,
+      ! _SPAT_TO_SPHERTOR) over n_levels levels in one call.
+      integer, intent(in) :: n_levels
+      integer(c_long_long), intent(in) :: grid_ld, spec_ld
+      type(magic_sht_job), intent(in) :: jobs(:)
+      integer(c_int), target, contiguous, optional, intent(in) :: lcut(:)
+      type(c_ptr) :: plc
+
+      plc = c_null_ptr
+      if ( present(lcut) ) plc = c_loc(lcut)
+      call sht_check(c_fwd_batch(sht_handle(), int(n_levels, c_int), plc, grid_ld, spec_ld, jobs, &
+           &                     int(size(jobs), c_int)))
+   end subroutine fwd_batch_gpu
 
    subroutine dt_courant_gpu(dtrkc, dthkc, dt, dtMax, l_new_dt, dt_new)
       ! dt_courant without its log lines (host arrays of all levels)

@@ -394,6 +394,62 @@ class SHT:
         check(self._lib.magic_sht_transform_to_lm_space(self._h, n, plc, ctypes.byref(a)))
         return outs
 
+    def _batch(self, jobs, inverse: bool, lcut, or2=None):
+        """(n, Job array, outputs per job, keep-alive list, lcut / or2 pointers)
+        of magic_sht_inv_batch / magic_sht_fwd_batch."""
+        if not jobs:
+            raise ValueError("no jobs")
+        n = None
+        arr = (_lib.Job * len(jobs))()
+        outs, keep = [], []
+        for j, job in enumerate(jobs):
+            name, ins = job[0], job[1:]
+            code, n_in, n_out = _lib.JOBS[name]
+            if (code < 100) != inverse:
+                raise ValueError("%s is not a %s routine" % (name, "synthesis" if inverse else "analysis"))
+            if len(ins) != n_in:
+                raise ValueError("%s takes %d arrays, got %d" % (name, n_in, len(ins)))
+            arr[j].routine = code
+            for k, x in enumerate(ins):
+                t, p = self._spec_in(x) if inverse else self._grid_in(x)
+                if n is None:
+                    n = int(t.shape[0])
+                if int(t.shape[0]) != n:
+                    raise ValueError("every array needs the same number of levels")
+                keep.append(t)
+                getattr(arr[j], "in")[k] = p
+            o = []
+            for k in range(n_out):
+                t, p = self._grid(keep[-1], n) if inverse else self._spec(keep[-1], n)
+                o.append(t)
+                arr[j].out[k] = p
+            outs.append(tuple(o))
+        lc_arr, plc = self._levels(None, n, lcut)
+        or2_arr, por2 = _per_level(or2, np.float64, n, "or2")
+        keep += [lc_arr, or2_arr]
+        return n, arr, outs, keep, plc, por2
+
+    def inv_batch(self, jobs, or2=None, lcut=None):
+        """Facade synthesis routines over many levels in one call
+        (magic_sht_inv_batch): ``jobs`` is a list of (routine name, array
+        inputs...) in the routine's argument order, each input (n_levels,
+        lm_max); ``or2`` per level for torpol_to_curl_spat jobs.  Returns one
+        tuple of (n_levels, n_phi_max, nlat_padded) outputs per job."""
+        n, arr, outs, keep, plc, por2 = self._batch(jobs, True, lcut, or2)
+        check(self._lib.magic_sht_inv_batch(self._h, n, por2, plc, self.lm_max, self.n_phi_max * self.nlat_padded,
+                                            arr, len(jobs)))
+        return outs
+
+    def fwd_batch(self, jobs, lcut=None):
+        """Facade analysis routines over many levels in one call
+        (magic_sht_fwd_batch): ``jobs`` = [(routine name, grids...)], each grid
+        (n_levels, n_phi_max, nlat_padded); returns one tuple of (n_levels,
+        lm_max) spectra per job."""
+        n, arr, outs, keep, plc, _ = self._batch(jobs, False, lcut)
+        check(self._lib.magic_sht_fwd_batch(self._h, n, plc, self.n_phi_max * self.nlat_padded, self.lm_max,
+                                            arr, len(jobs)))
+        return outs
+
     def tuning(self) -> Dict[str, int]:
         """Runtime tuning of this handle (magic_sht_get_tuning): tc_kernel,
         tc_order, pipe_chunk, fft_rows."""

@@ -27,7 +27,8 @@ def c_structs():
             for v in m.group(2).split(","):
                 v = v.strip()
                 kind = "ptr" if v.startswith("*") else {"long long": "i64", "double": "f64", "int": "i32"}[base]
-                fields.append((v.lstrip("*").strip().lower(), kind))
+                # arrays: name[4] in C, name(4) in Fortran
+                fields.append((v.lstrip("*").strip().lower().replace("[", "(").replace("]", ")"), kind))
         out[name] = fields
     return out
 

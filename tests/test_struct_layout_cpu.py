@@ -27,6 +27,7 @@ MIRRORS = {
     "magic_sht_td_out": _lib.TdOut,
     "magic_sht_courant_args": _lib.CourantArgs,
     "magic_sht_rigid_args": _lib.RigidArgs,
+    "magic_sht_job": _lib.Job,
 }
 
 
