@@ -249,8 +249,10 @@ int magic_sht_set_host_async(magic_sht_handle* h, int on);
 
 /* ---- runtime tuning of one handle (magic_gb300/autotune.py searches these
  * per geometry and caches the choice).  Results do not depend on them except
- * tc_kernel, which selects between two kernels of the same arithmetic form;
- * graphs captured earlier keep the settings they were captured with.
+ * tc_kernel, which selects between two kernels of the same arithmetic form,
+ * and fft_rows, whose forward FFT factors its twiddles e^(2 pi i k / n_phi)
+ * differently (spectra differ at FP32 rounding, grids are identical); graphs
+ * captured earlier keep the settings they were captured with.
  *   tc_kernel:  tensor-core forms, 0 persistent kernels, 1 one tile per CTA
  *               (3xBF16) or the FP64 SIMT Legendre sums (FP64TC, with its
  *               double-float FFTs)
@@ -258,7 +260,7 @@ int magic_sht_set_host_async(magic_sht_handle* h, int on);
  *               table blocks, 1 they share the data tiles
  *   pipe_chunk: radial levels per chunk of the host-buffer pipeline (1..1024)
  *   fft_rows:   theta rows per CTA of the FP32 azimuthal FFT, 8 or 16
- *               (0 = by size) */
+ *               (0 = by size; the double-float FFTs keep 16) */
 typedef struct magic_sht_tuning {
   int tc_kernel, tc_order, pipe_chunk, fft_rows;
 } magic_sht_tuning;

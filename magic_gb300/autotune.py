@@ -7,13 +7,15 @@ produced -- for every candidate setting of
 
   tc_kernel   persistent tensor-core kernels or one tile per CTA (3xBF16),
   tc_order    tile order of the persistent kernels (table or data reuse),
-  fft_rows    theta rows per CTA of the FP32 / double-float azimuthal FFTs (8 or 16),
+  fft_rows    theta rows per CTA of the FP32 azimuthal FFTs (8 or 16; the
+              double-float FFTs of the fixed-point forms keep 16),
   pipe_chunk  levels per chunk of the host-buffer pipeline (host arrays only),
 
 keeps the fastest, applies it to the handle and caches it in a JSON file keyed
 by device name and geometry, so later handles of the same geometry pick it up
-without timing.  Only tc_kernel changes arithmetic (two kernels of the same
-3xBF16 form); the other knobs change scheduling only.
+without timing.  tc_kernel changes arithmetic (two kernels of the same
+3xBF16 form), fft_rows the factorisation of the forward FFT's twiddles
+(spectra differ at FP32 rounding); the other knobs change scheduling only.
 """
 from __future__ import annotations
 
@@ -53,7 +55,7 @@ def candidates(sht, host: bool) -> List[Dict[str, int]]:
     tc = form in ("bf16x3", "tf32x2", "fp64tc", "bf16x5")  # persistent tensor-core kernels: tile order
     kernels = [0, 1] if form == "bf16x3" else [0]
     orders = [0, 1] if tc else [0]
-    rows = [8, 16] if form != "fp64" else [0]
+    rows = [8, 16] if form in ("fp32", "bf16x3", "tf32x2") else [0]  # FP32 FFTs only
     chunks = [8, 16, 32] if host else [sht.tuning()["pipe_chunk"]]
     out = []
     for kern, order, row, chunk in itertools.product(kernels if tc else [0], orders, rows, chunks):
