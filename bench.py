@@ -567,17 +567,18 @@ def our_arm(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    def time_steps(s, out_g, out_s, steps):
+    def time_steps(s, out_g, out_s, steps, fn=None):
         """One step (both transform sets over all levels) captured in a CUDA
         graph and replayed `steps` times; CUDA events on the replay stream
         around every replay.  Returns (total ms, kernel launches, per-step ms)."""
+        fn = fn or run_set
         s.reserve(N_LEVELS)
         side = torch.cuda.Stream()
         barrier()
         with torch.cuda.stream(side):
             n0 = s.launch_count()
             s.graph_begin()
-            run_set(s, out_g, out_s)
+            fn(s, out_g, out_s)
             gr = s.graph_end()
             per_step_launches = s.launch_count() - n0
             s.graph_launch(gr)  # warm replay
@@ -680,6 +681,27 @@ def our_arm(args):
             sv.close()
             del gv, lv
             torch.cuda.synchronize()
+
+    # ---- the reference's Boussinesq default analysis set (rIter.f90:682-702): the
+    # composition flux V Xi (spat_to_qst, 3 grids) in place of heatTerms, 12 forward grids
+    bouss = None
+    if not args.no_variant:
+        finx = {k: v for k, v in fin.items() if k != "heatTerms"}
+        finx.update({"VXir": fin["VSr"], "VXit": fin["VSt"], "VXip": fin["VSp"]})
+
+        def run_bouss(s, out_g, out_s):
+            g = s.transform_to_grid_space(spec, or2=or2, out=out_g)
+            return g, s.transform_to_lm_space(finx, out=out_s)
+        gb, lb = run_bouss(sm, gm, None)
+        for _ in range(max(0, args.warmup - 1)):
+            run_bouss(sm, gm, lb)
+        msb, _, perb = time_steps(sm, gm, lb, args.steps, fn=run_bouss)
+        sm.device_status()
+        bouss = {"what": "15 synthesis grids + 12 analysis grids per level (V Xi in place of heatTerms), "
+                         "headline form", "value": world * N_LEVELS * args.steps / (msb * 1e-3),
+                 "unit": "levels/s", "ms_per_step": msb / args.steps, "median_ms_per_step": statistics.median(perb)}
+        del lb, finx
+        torch.cuda.synchronize()
 
     # ---- per-phase kernel timing (CUDA events on the launching stream)
     sm.set_profiling(True)
@@ -862,6 +884,7 @@ def our_arm(args):
             "accuracy_chain": chain,
             "accuracy_checkpoint_spectra": checkpoint,
             "other_forms": others,
+            "boussinesq_default_set": bouss,
             "roofline": roof,
             "phases": phases,
             "peaks": {"fp64_gflops": fp64_peak, "fp32_gflops": fp32_peak, "hbm_gbs": hbm,
