@@ -144,3 +144,48 @@ def test_batch_argument_checks(built, torch):
     assert call([(1, [o1], [o1])]) == _lib.ERR_ARG                     # output aliases an input
     torch.cuda.synchronize()
     s.device_status()
+
+
+def test_batch_small_host_call_and_graph_replay(built, oracle_mod, torch):
+    """Host arrays within one chunk (staged without the pipeline), and a
+    CUDA-graph capture of device-array batch calls replayed on new inputs."""
+    from magic_gb300.workload import grid_space_inputs, or2_levels
+    L, minc, N, P, n = 31, 1, 48, 96, 3
+    s = make(L, minc, N, P)
+    o = oracle_mod.OracleSHT(L, minc, N, P)
+    S = grid_space_inputs(L, minc, n, seed=73)
+    lcut = np.array([L, 5, L - 1], dtype=np.int32)
+    or2 = or2_levels(n)
+    jobs = _inv_jobs(S)
+    got = s.inv_batch(jobs, or2=or2, lcut=lcut)
+    _check_inv(o, jobs, got, lcut, or2, TOL["fp64"], host=True)
+    # capture: the same jobs on device arrays, replayed after the inputs change
+    dS = {k: torch.from_numpy(v).cuda() for k, v in S.items()}
+    djobs = [tuple([j[0]] + [dS[k] for k in names]) for j, names in zip(
+        jobs, [("w",), ("dw",), ("z",), ("w", "dw", "z"), ("dw", "dz"), ("w", "ddw", "z", "dz"), ("dz",), ("dw", "z")])]
+    dor2 = torch.from_numpy(or2).cuda()
+    s.reserve(n)
+    ref = s.inv_batch(djobs, or2=dor2, lcut=lcut)  # eager outputs, reused as the captured call's outputs
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        n_jobs = len(djobs)
+        dlc = torch.from_numpy(lcut).cuda()  # inside a capture every array is a device array
+        nlev, arr, outs, keep, plc, por2 = s._batch(djobs, True, dlc, dor2)
+        for j in range(n_jobs):  # write into the eager call's output arrays
+            for k, t in enumerate(ref[j]):
+                arr[j].out[k] = t.data_ptr()
+        s.graph_begin()
+        try:
+            rc = s._lib.magic_sht_inv_batch(s._h, nlev, por2, plc, s.lm_max, s.n_phi_max * s.nlat_padded, arr, n_jobs)
+        finally:
+            gr = s.graph_end()
+        assert rc == 0
+        S2 = grid_space_inputs(L, minc, n, seed=74)
+        for k, v in dS.items():
+            v.copy_(torch.from_numpy(S2[k]))
+        s.graph_launch(gr)
+        side.synchronize()
+    _check_inv(o, _inv_jobs(S2), ref, lcut, or2, TOL["fp64"])
+    s.graph_destroy(gr)
+    s.device_status()
