@@ -63,6 +63,7 @@ __host__ __device__ constexpr uint32_t tile_bytes(int S) { return (uint32_t)S * 
 constexpr int kThreads = 320;            // 10 warps
 constexpr int kEpiThreads = 256;         // warps 2..9
 constexpr int kPackThreads = 256;
+constexpr int kPack1Threads = 512;       // the one-pass synthesis pack: one complex column per warp
 constexpr int kNTR = 4;                  // tile-index ring
 
 __device__ __forceinline__ unsigned char* align1k(unsigned char* p) {
@@ -550,9 +551,9 @@ __global__ void __launch_bounds__(kPackThreads, 3) pack_inv_oz(const __grid_cons
 // memory latency per CTA instead of one per pass and chunk.  The digits are
 // those of pack_inv_oz (same scales, same rounding).
 template <bool VEC, bool MULTI, int S>
-__global__ void __launch_bounds__(kPackThreads, 2) pack_inv_oz1(const __grid_constant__ OzInv one,
-                                                             const OzInv* __restrict__ many,
-                                                             const __grid_constant__ InstIndex X) {
+__global__ void __launch_bounds__(kPack1Threads, 2) pack_inv_oz1(const __grid_constant__ OzInv one,
+                                                              const OzInv* __restrict__ many,
+                                                              const __grid_constant__ InstIndex X) {
   extern __shared__ unsigned char smem_raw[];
   OZ_DIGITS(S);
   unsigned char* buf = align1k(smem_raw);  // two tiles of kTS bytes
@@ -567,30 +568,26 @@ __global__ void __launch_bounds__(kPackThreads, 2) pack_inv_oz1(const __grid_con
   const int m = mc * g.minc, n_l = g.l_max - m + 1, lm0 = g.lmoff[mc];
   const int nch = tc_nch(n_l);  // <= 2
   const int ncplx = s.nf * s.nlev * (VEC ? 2 : 1);
-  const int tid = threadIdx.x, kp = tid & 31, qg = tid >> 5;
-  PackCol cols[2];
+  // sixteen warps, one complex column (two real rows of the tile) each
+  const int tid = threadIdx.x, kp = tid & 31, ql = tid >> 5;
+  const PackCol col = pack_col<VEC>(g, s, ct * (kNC / 2) + ql, ncplx);
+  // v[p][c][h]: parity p, chunk c, degree index 64 c + 2 kp + h
+  double2 v[2][2][2];
 #pragma unroll
-  for (int i = 0; i < 2; ++i) cols[i] = pack_col<VEC>(g, s, ct * (kNC / 2) + qg + 8 * i, ncplx);
-  // v[i][p][c][h]: column i, parity p, chunk c, degree index 64 c + 2 kp + h
-  double2 v[2][2][2][2];
+  for (int p = 0; p < 2; ++p)
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+    for (int c = 0; c < 2; ++c)
 #pragma unroll
-    for (int p = 0; p < 2; ++p)
-#pragma unroll
-      for (int c = 0; c < 2; ++c)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int loff = p + 2 * (64 * c + 2 * kp + h);
-          const int l = m + loff;
-          v[i][p][c][h] = make_double2(0.0, 0.0);
-          if (cols[i].op.op != OP_ZERO && c < nch && loff < n_l && l <= cols[i].lc)
-            v[i][p][c][h] = oz_operand(cols[i].op, cols[i].r, lm0, loff, l, m, cols[i].or2);
-        }
+      for (int h = 0; h < 2; ++h) {
+        const int loff = p + 2 * (64 * c + 2 * kp + h);
+        const int l = m + loff;
+        v[p][c][h] = make_double2(0.0, 0.0);
+        if (col.op.op != OP_ZERO && c < nch && loff < n_l && l <= col.lc)
+          v[p][c][h] = oz_operand(col.op, col.r, lm0, loff, l, m, col.or2);
+      }
   // largest exponent of x 2^k(l) per real column (the spectra divided by the degree weights)
-  int E[2][2];
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  int E0, E1;
+  {
     int er = -4096, ei = -4096;
 #pragma unroll
     for (int p = 0; p < 2; ++p)
@@ -599,20 +596,19 @@ __global__ void __launch_bounds__(kPackThreads, 2) pack_inv_oz1(const __grid_con
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const int k = deg_shift(m + p + 2 * (64 * c + 2 * kp + h));
-          er = max(er, exp_bound(v[i][p][c][h].x) + k);
-          ei = max(ei, exp_bound(v[i][p][c][h].y) + k);
+          er = max(er, exp_bound(v[p][c][h].x) + k);
+          ei = max(ei, exp_bound(v[p][c][h].y) + k);
         }
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
       er = max(er, __shfl_xor_sync(0xffffffffu, er, d));
       ei = max(ei, __shfl_xor_sync(0xffffffffu, ei, d));
     }
-    E[i][0] = er < -3000 ? 0 : er;
-    E[i][1] = ei < -3000 ? 0 : ei;
+    E0 = er < -3000 ? 0 : er;
+    E1 = ei < -3000 ? 0 : ei;
     if (kp == 0) {
-      const int ql = qg + 8 * i;
-      cexp[(long long)mc * nct * kNC + ct * kNC + 2 * ql] = (short)E[i][0];
-      cexp[(long long)mc * nct * kNC + ct * kNC + 2 * ql + 1] = (short)E[i][1];
+      cexp[(long long)mc * nct * kNC + ct * kNC + 2 * ql] = (short)E0;
+      cexp[(long long)mc * nct * kNC + ct * kNC + 2 * ql + 1] = (short)E1;
     }
   }
   int nb = 0;
@@ -626,20 +622,16 @@ __global__ void __launch_bounds__(kPackThreads, 2) pack_inv_oz1(const __grid_con
         if (tid == 0) tc::bulk_wait_read<1>();
         __syncthreads();
       }
+      int kw[2];
 #pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int ql = qg + 8 * i;
-        int kw[2];
+      for (int h = 0; h < 2; ++h) kw[h] = deg_shift(m + p + 2 * (64 * c + 2 * kp + h));
+      float d[2][kS];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) kw[h] = deg_shift(m + p + 2 * (64 * c + 2 * kp + h));
-        float d[2][kS];
+      for (int h = 0; h < 2; ++h) digitsf<S>(fixed_from_double(v[p][c][h].x, kFix - E0 + kw[h]), d[h]);
+      store_digit_pairs(B, 2 * ql, 2 * kp, d);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) digitsf<S>(fixed_from_double(v[i][p][c][h].x, kFix - E[i][0] + kw[h]), d[h]);
-        store_digit_pairs(B, 2 * ql, 2 * kp, d);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) digitsf<S>(fixed_from_double(v[i][p][c][h].y, kFix - E[i][1] + kw[h]), d[h]);
-        store_digit_pairs(B, 2 * ql + 1, 2 * kp, d);
-      }
+      for (int h = 0; h < 2; ++h) digitsf<S>(fixed_from_double(v[p][c][h].y, kFix - E1 + kw[h]), d[h]);
+      store_digit_pairs(B, 2 * ql + 1, 2 * kp, d);
       tc::fence_proxy_async_smem();
       __syncthreads();
       if (tid == 0) {
@@ -1315,7 +1307,7 @@ cudaError_t launch_inv_oz_s(const OzInv& one, const OzInv* many, const InstIndex
     pack_inv_oz<VEC, MULTI, S><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
   } else {
     CUDA_TRY(cudaFuncSetAttribute(pack_inv_oz1<VEC, MULTI, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-    pack_inv_oz1<VEC, MULTI, S><<<pgrid, kPackThreads, psmem, st>>>(one, many, X);
+    pack_inv_oz1<VEC, MULTI, S><<<pgrid, kPack1Threads, psmem, st>>>(one, many, X);
   }
   CUDA_TRY(cudaGetLastError());
   const size_t smem = 1024 + (size_t)NA * NT * 16384 + (size_t)NB * kTS;
