@@ -120,6 +120,8 @@ struct ShtGeom {
   const double2* tw64;           // device [n_phi]  e^{+2 pi i k/n_phi}
   const float2* tw32;
   const void* twdf;              // device [n_phi]  the same as double-float pairs (hi, lo) x (re, im)
+  const void* twr;               // device: the fast-path twiddle tables of the double-float FFT at 24
+                                 // points per lane (read from L1 instead of shared memory), else null
 };
 
 // Pre-split (3xBF16) and pre-tiled Legendre tables of the tensor-core form.

@@ -33,6 +33,11 @@ template <> struct Tw<dfl> {
   static __device__ __forceinline__ const dfl2* get(const ShtGeom& g) { return (const dfl2*)g.twdf; }
 };
 
+// The double-float rows of 24 points per lane fill 101.5 KB of shared memory
+// per CTA: their twiddle tables (TwTab layout, 15.5 KB) are read from a copy
+// in device memory (through L1) so that two CTAs fit on an SM.
+template <typename T, int S> struct GlobalTw { static constexpr bool v = std::is_same<T, dfl>::value && S >= 24; };
+
 // CTAs per SM of the fast path: FP32 three (two for the longest rows), FP64
 // one, double-float two (its rows are twice the FP32 size, its arithmetic
 // needs the latency hiding of a second CTA)
@@ -164,7 +169,13 @@ __device__ __forceinline__ void reg_fft(T2 (&a)[S], const T2* __restrict__ tw, i
 // transforms).  Outputs of one register are therefore 32 consecutive indices
 // across the warp, which keeps the shared-memory write-back free of bank
 // conflicts.
-__device__ __forceinline__ int brev5(int x) { return __brev(x) >> 27; }
+__host__ __device__ __forceinline__ int brev5(int x) {
+#ifdef __CUDA_ARCH__
+  return __brev(x) >> 27;
+#else
+  return ((x & 1) << 4) | ((x & 2) << 2) | (x & 4) | ((x & 8) >> 2) | ((x & 16) >> 4);
+#endif
+}
 
 // Twiddle tables of the fast path in shared memory, laid out so that every
 // warp-wide read is either 32 consecutive entries (one per lane) or one entry
@@ -179,7 +190,7 @@ struct TwTab {
   static constexpr int kLane = 0, kPost = 128, kRoot = 128 + 32 * S, kLo = kRoot + S, kHi = kLo + S;
   static constexpr int size = kHi + S + 1;
   // index into the table e^{+2 pi i k / P} (k < P) of entry i; KS = order stride of the forward epilogue
-  static __device__ __forceinline__ int src(int i, int KS) {
+  static __host__ __device__ __forceinline__ int src(int i, int KS) {
     constexpr int P = 64 * S;
     if (i < kPost) {
       const int st = i >> 5, l = i & 31, d = 16 >> st;
@@ -356,16 +367,18 @@ __device__ __forceinline__ int pos(int k) { return (k & 31) + ((k >> 4) & 1) + 3
 // batch of NB orders (E at both parities, and F for vector fields), and of
 // the twiddle table, are issued before the first shared-memory store, so that
 // a thread waits for one memory latency per batch.
-template <typename T2, int S, int RT, int NB>
+template <typename T2, int S, int RT, int NB, bool STAGE_TW>
 __device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict__ in, bool in_parity,
                                           bool has_f, bool hs64, long long per_p, const T2* __restrict__ twg, T2* sm,
                                           T2* stw, int rp, int kq, int rowg, bool row_ok) {
   constexpr int KP = 33 * S + 1, KS = 256 / (RT / 2), NT = TwTab<S>::size, NTW = (NT + 255) / 256;
   const int n_m = g.n_m;
   T2 twr[NTW];
+  if constexpr (STAGE_TW) {
 #pragma unroll
-  for (int i = 0; i < NTW; ++i)
-    if (threadIdx.x + 256 * i < NT) twr[i] = twg[TwTab<S>::src(threadIdx.x + 256 * i, KS)];
+    for (int i = 0; i < NTW; ++i)
+      if (threadIdx.x + 256 * i < NT) twr[i] = twg[TwTab<S>::src(threadIdx.x + 256 * i, KS)];
+  }
   for (int kb = 0; kb < n_m; kb += KS * NB) {
     T2 x[NB][4];
 #pragma unroll
@@ -389,7 +402,7 @@ __device__ __forceinline__ void inv_stage(const ShtGeom& g, const T2* __restrict
         }
       }
     }
-    if (kb == 0) {  // n_m >= 1: the first batch always runs
+    if (STAGE_TW && kb == 0) {  // n_m >= 1: the first batch always runs
 #pragma unroll
       for (int i = 0; i < NTW; ++i)
         if (threadIdx.x + 256 * i < NT) stw[threadIdx.x + 256 * i] = twr[i];
@@ -426,7 +439,8 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_inv_fast(const ShtGe
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
   const T2* __restrict__ twg = Tw<T>::get(g);
-  T2* stw = sm + RT * KP;  // twiddle tables (TwTab)
+  T2* stw = sm + RT * KP;  // twiddle tables (TwTab), or their copy in device memory
+  const T2* tab = GlobalTw<T, S>::v ? (const T2*)g.twr : stw;
   const T2* __restrict__ in = (const T2*)fd.in + (long long)r * fd.in_ld;
   const int n_m = g.n_m;
   const bool in_parity = (fd.flags & (FFT_IN_E | FFT_IN_EF)) != 0;
@@ -439,14 +453,14 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_inv_fast(const ShtGe
   const int rowg = row0 + rp;
   const bool row_ok = rowg < g.n_theta;
   const bool hs64 = (fd.flags & FFT_HS_F64) != 0;
-  inv_stage<T2, S, RT, sizeof(T) == 4 ? 4 : 2>(g, in, in_parity, has_f, hs64, per_p, twg, sm, stw, rp, kq, rowg,
-                                               row_ok);
+  inv_stage<T2, S, RT, sizeof(T) == 4 ? 4 : 2, !GlobalTw<T, S>::v>(g, in, in_parity, has_f, hs64, per_p, twg, sm,
+                                                                   stw, rp, kq, rowg, row_ok);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const T2 base = twg[S * lane];  // e^{2 pi i S lane / P}: times lo[q] gives e^{2 pi i k / P}, k = S lane + q
   T2 wq[S];  // the same for both rows of the warp
 #pragma unroll
-  for (int q = 0; q < S; ++q) wq[q] = q == 0 ? base : cmul(base, stw[TwTab<S>::kLo + q]);
+  for (int q = 0; q < S; ++q) wq[q] = q == 0 ? base : cmul(base, tab[TwTab<S>::kLo + q]);
   for (int rr = warp; rr < RT; rr += 8) {
     T2* row = sm + rr * KP;
     T2 a[S];
@@ -466,7 +480,7 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_inv_fast(const ShtGe
       a[q].y = E.y + O.x;
     }
     __syncwarp();
-    warp_fft<T2, S>(a, stw, +1);
+    warp_fft<T2, S>(a, tab, +1);
     const int k1 = brev5(fft_pos<T2, S>(lane));
 #pragma unroll
     for (int k2 = 0; k2 < S; ++k2) row[pos(k1 + 32 * k2)] = a[k2];  // z_j = x_{2j} + i x_{2j+1}
@@ -529,7 +543,9 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_fwd_fast(const ShtGe
   const FftField& fd = s.f[f];
   const int row0 = blockIdx.x * RT;
   const T2* __restrict__ twg = Tw<T>::get(g);
-  T2* stw = sm + RT * KP;  // twiddle tables (TwTab)
+  T2* stw = sm + RT * KP;  // twiddle tables (TwTab), or their copy in device memory
+  constexpr bool kStage = !GlobalTw<T, S>::v;
+  const T2* tab = kStage ? stw : (const T2*)g.twr;
   const double* __restrict__ in = (const double*)fd.in + (long long)r * fd.in_ld;
   // Each thread owns the row pair (rp, rp + 1) and the indices kk = kq + KS j
   // (phi = 2kk, 2kk + 1); the loads of a batch of NB indices, and of the
@@ -540,9 +556,11 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_fwd_fast(const ShtGe
   const bool row_ok = rowg < g.n_theta;
   const bool vec = (g.ld % 2) == 0;
   T2 twr[NTW];
+  if constexpr (kStage) {
 #pragma unroll
-  for (int i = 0; i < NTW; ++i)
-    if (threadIdx.x + 256 * i < NT) twr[i] = twg[TwTab<S>::src(threadIdx.x + 256 * i, KS)];
+    for (int i = 0; i < NTW; ++i)
+      if (threadIdx.x + 256 * i < NT) twr[i] = twg[TwTab<S>::src(threadIdx.x + 256 * i, KS)];
+  }
   for (int kb = 0; kb < n; kb += KS * NB) {
     double2 u[NB], w[NB];  // (row rp | rp+1) at phi 2kk (u) and 2kk+1 (w)
 #pragma unroll
@@ -560,7 +578,7 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_fwd_fast(const ShtGe
         }
       }
     }
-    if (kb == 0) {
+    if (kStage && kb == 0) {
 #pragma unroll
       for (int i = 0; i < NTW; ++i)
         if (threadIdx.x + 256 * i < NT) stw[threadIdx.x + 256 * i] = twr[i];
@@ -585,7 +603,7 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_fwd_fast(const ShtGe
 #pragma unroll
     for (int q = 0; q < S; ++q) a[q] = row[q * 33 + lane];  // = z[S*lane + q]
     __syncwarp();
-    warp_fft<T2, S>(a, stw, -1);
+    warp_fft<T2, S>(a, tab, -1);
     const int k1 = brev5(fft_pos<T2, S>(lane));
 #pragma unroll
     for (int k2 = 0; k2 < S; ++k2) row[pos(k1 + 32 * k2)] = a[k2];
@@ -604,7 +622,7 @@ __global__ void __launch_bounds__(256, FftOcc<T, S>::v) fft_fwd_fast(const ShtGe
   if (fd.flags & FFT_WEIGHT) fac *= from_f64<Tt>(g.wgt[jg]);
   const T2 base = twg[kq];  // e^{2 pi i kq / P}: times hi[j] gives e^{2 pi i k / P}, k = kq + KS j
   for (int k = kq, j = 0; k < g.n_m; k += KS, ++j) {
-    const T2 tk = j == 0 ? base : cmul(base, stw[TwTab<S>::kHi + j]);
+    const T2 tk = j == 0 ? base : cmul(base, tab[TwTab<S>::kHi + j]);
     T2 c[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -844,7 +862,7 @@ template <typename T, int S, int RT>
 cudaError_t launch_rt(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
   typedef typename V2<T>::t T2;
   constexpr int KP = 33 * S + 1;
-  const size_t smem = ((size_t)RT * KP + TwTab<S>::size) * sizeof(T2);
+  const size_t smem = ((size_t)RT * KP + (GlobalTw<T, S>::v ? 0 : TwTab<S>::size)) * sizeof(T2);
   dim3 grid((g.n_theta + RT - 1) / RT, s.nf * s.nlev);
   auto k = inverse ? fft_inv_fast<T, S, RT> : fft_fwd_fast<T, S, RT>;
   CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -910,6 +928,19 @@ cudaError_t launch_any(const ShtGeom& g, const FftSet& s, bool inverse, int rows
 }
 
 }  // namespace
+
+// The twiddle tables the double-float fast path reads from device memory
+// (GlobalTw): TwTab<24> at the order stride of 8-row CTAs, from the
+// double-float table e^{+2 pi i k / P}; empty for the other lengths.
+std::vector<float4> fft_df_global_twiddles(int n_phi, const std::vector<float4>& twdf) {
+  std::vector<float4> out;
+  if (n_phi != 64 * 24 || (int)twdf.size() != n_phi) return out;
+  typedef TwTab<24> TT;
+  constexpr int KS = 256 / (8 / 2);
+  out.resize(TT::size);
+  for (int i = 0; i < TT::size; ++i) out[i] = twdf[TT::src(i, KS)];
+  return out;
+}
 
 bool fft_fast_path(int n_phi) {
   const int n = n_phi / 2;

@@ -15,6 +15,10 @@ cudaError_t launch_fwd_legendre_simt(const ShtGeom& g, const FwdSet& s, bool vec
 // rows: theta rows per CTA of the fast path (8 or 16; 0 = chosen by size)
 // arith: FFT_ARITH_F32 / _F64 / _DF (double-float, working type dfl)
 cudaError_t launch_fft_inverse(const ShtGeom& g, const FftSet& s, int arith, int rows, cudaStream_t st);
+// the double-float fast path's twiddle tables kept in device memory (ShtGeom::twr) for
+// this row length, from the table e^{+2 pi i k / n_phi}; empty when the path keeps them
+// in shared memory
+std::vector<float4> fft_df_global_twiddles(int n_phi, const std::vector<float4>& twdf);
 cudaError_t launch_fft_forward(const ShtGeom& g, const FftSet& s, int arith, int rows, cudaStream_t st);
 bool fft_fast_path(int n_phi);
 

@@ -68,6 +68,7 @@ struct magic_sht_handle {
   double2* d_tw64 = nullptr;
   float2* d_tw32 = nullptr;
   float4* d_twdf = nullptr;  // e^{+2 pi i k/P} as double-float (hi re, lo re, hi im, lo im)
+  float4* d_twr = nullptr;   // the double-float fast path's twiddle tables in device memory (n_phi = 1536)
   short* d_inv_exp = nullptr;  // FP64-accurate tensor-core form: table row exponents
   short* d_fwd_exp = nullptr;
   double* d_cosn2 = nullptr;  // cos / sin^2 of the northern colatitudes (general get_nl)
@@ -899,6 +900,12 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
     INIT_CK(cudaMemcpyAsync(h->d_tw64, tw.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, h->stream));
     INIT_CK(cudaMemcpyAsync(h->d_tw32, tw32.data(), sizeof(float2) * P, cudaMemcpyHostToDevice, h->stream));
     INIT_CK(cudaMemcpyAsync(h->d_twdf, twdf.data(), sizeof(float4) * P, cudaMemcpyHostToDevice, h->stream));
+    const std::vector<float4> twr = fft_df_global_twiddles(P, twdf);
+    if (!twr.empty()) {
+      INIT_CK(cudaMalloc((void**)&h->d_twr, sizeof(float4) * twr.size()));
+      INIT_CK(cudaMemcpyAsync(h->d_twr, twr.data(), sizeof(float4) * twr.size(), cudaMemcpyHostToDevice,
+                              h->stream));
+    }
     INIT_CK(cudaStreamSynchronize(h->stream));
   }
   INIT_CK(build_tables_fp64(L, m_max, minc, N, h->d_lmoff, h->d_theta, h->d_gauss, h->d_P, h->d_dP,
@@ -912,6 +919,7 @@ int magic_sht_init(const magic_sht_desc* d, magic_sht_handle** out) {
   INIT_CK(cudaStreamSynchronize(h->stream));
   g.P64 = h->d_P; g.dP64 = h->d_dP; g.P32 = h->d_P32; g.dP32 = h->d_dP32;
   g.wgt = h->d_wgt; g.osin2 = h->d_osin2; g.tw64 = h->d_tw64; g.tw32 = h->d_tw32; g.twdf = h->d_twdf;
+  g.twr = h->d_twr;
   if (oz_form(h)) {
     if (prop.major != 10)
       return fail(set_err(MAGIC_SHT_ERR_UNSUPPORTED, "the tensor-core form needs tcgen05 (sm_10x)"));
@@ -1008,7 +1016,7 @@ int magic_sht_finalize(magic_sht_handle* h) {
                   h->d_P32, h->d_dP32, h->d_tw64, h->d_tw32, h->ws, h->d_inv_img, h->d_fwd_img,
                   h->d_inv_blk0, h->d_fwd_blk0, h->d_inv_scale, h->d_fwd_scale, h->d_err,
                   h->d_bpc0, h->d_bimg, h->d_tile_ctr, h->d_tdcoef, h->d_tdlq, h->d_twdf,
-                  h->d_inv_exp, h->d_fwd_exp, h->d_cosn2};
+                  h->d_inv_exp, h->d_fwd_exp, h->d_cosn2, h->d_twr};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->pin) cudaFreeHost(h->pin);

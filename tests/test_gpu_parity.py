@@ -496,7 +496,11 @@ def test_radial_step_with_nonlinear_products(built, torch):
 def test_large_config_l511(built, oracle_mod, torch):
     """The large configuration (l_max=511, 768 x 1536 grid): the FP64 form
     against the oracle on one level of the radial set, the 3xBF16 form
-    against the FP64 form on three levels (normwise per call <= 1e-6)."""
+    against the FP64 form on three levels (normwise per call <= 1e-6), and
+    the FP64-accurate tensor-core form (its double-float FFTs at 24 points
+    per lane) against the FP64 form: every call normwise <= 1e-12, every
+    output <= 1e-9 (AdvpLM, the small toroidal part of the advection, sits
+    near 3e-10 as at l_max = 255)."""
     from magic_gb300.workload import grid_space_inputs, or2_levels
     L, minc, N, P, n = 511, 1, 768, 1536, 3
     spec_np = grid_space_inputs(L, minc, n, seed=29)
@@ -523,6 +527,22 @@ def test_large_config_l511(built, oracle_mod, torch):
         num = sum(float(torch.linalg.vector_norm(a[k] - b[k])) ** 2 for k in ks) ** 0.5
         den = sum(float(torch.linalg.vector_norm(b[k])) ** 2 for k in ks) ** 0.5
         assert num / den < 1e-6, (name, num / den)
+    del s16, g16, l16
+    stc = make(L, minc, N, P, prec="fp64tc")
+    gtc = stc.transform_to_grid_space(spec, or2=or2)
+    ltc = stc.transform_to_lm_space(nl)
+    torch.cuda.synchronize()
+    stc.device_status()
+    for a, b in ((gtc, g64), (ltc, l64)):
+        for k in b:
+            e = float(torch.linalg.vector_norm(a[k] - b[k]) / torch.linalg.vector_norm(b[k]))
+            assert e < 1e-9, (k, e)
+    for a, b, ks in ((gtc, g64, ("vrc", "vtc", "vpc")), (gtc, g64, ("cvrc", "cvtc", "cvpc")),
+                     (ltc, l64, ("AdvrLM", "AdvtLM", "AdvpLM")), (ltc, l64, ("VSrLM", "VStLM", "VSpLM")),
+                     (ltc, l64, ("VxBrLM", "VxBtLM", "VxBpLM"))):
+        num = sum(float(torch.linalg.vector_norm(a[k] - b[k])) ** 2 for k in ks) ** 0.5
+        den = sum(float(torch.linalg.vector_norm(b[k])) ** 2 for k in ks) ** 0.5
+        assert num / den < 1e-12, (ks, num / den)
 
 
 @pytest.mark.gpu
