@@ -8,7 +8,7 @@ produced -- for every candidate setting of
   tc_kernel   persistent tensor-core kernels or one tile per CTA (3xBF16),
   tc_order    tile order of the persistent kernels (table or data reuse),
   fft_rows    theta rows per CTA of the FP32 azimuthal FFTs (8 or 16; the
-              double-float FFTs of the fixed-point forms keep 16),
+              double-float FFTs of the fixed-point forms keep their own),
   pipe_chunk  levels per chunk of the host-buffer pipeline (host arrays only),
 
 keeps the fastest, applies it to the handle and caches it in a JSON file keyed
