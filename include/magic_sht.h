@@ -260,8 +260,9 @@ int magic_sht_set_host_async(magic_sht_handle* h, int on);
  *               table blocks, 1 they share the data tiles
  *   pipe_chunk: radial levels per chunk of the host-buffer pipeline (1..1024)
  *   fft_rows:   theta rows per CTA of the FP32 azimuthal FFT, 8 or 16
- *               (0 = by size; the double-float FFTs keep their own: 8 rows
- *               for the forward at n_phi = 768 and 1536, 16 otherwise) */
+ *               (0 = by size; the double-float FFTs choose their own: 8 rows
+ *               where 16 would not fit two CTAs per SM, and for the forward at
+ *               n_phi = 768) */
 typedef struct magic_sht_tuning {
   int tc_kernel, tc_order, pipe_chunk, fft_rows;
 } magic_sht_tuning;
