@@ -543,6 +543,17 @@ def test_large_config_l511(built, oracle_mod, torch):
         num = sum(float(torch.linalg.vector_norm(a[k] - b[k])) ** 2 for k in ks) ** 0.5
         den = sum(float(torch.linalg.vector_norm(b[k])) ** 2 for k in ks) ** 0.5
         assert num / den < 1e-12, (ks, num / den)
+    # the same handle with the FP64 SIMT Legendre sums (tc_kernel 1): FP64 half
+    # spectra into and out of the same double-float FFTs, whose rounding alone
+    # sets AdvpLM's 3e-10 (the same as with the tensor-core sums)
+    stc.set_tuning(tc_kernel=1)
+    g1 = stc.transform_to_grid_space(spec, or2=or2)
+    l1 = stc.transform_to_lm_space(nl)
+    torch.cuda.synchronize()
+    for a, b in ((g1, g64), (l1, l64)):
+        for k in b:
+            e = float(torch.linalg.vector_norm(a[k] - b[k]) / torch.linalg.vector_norm(b[k]))
+            assert e < (1e-9 if k == "AdvpLM" else 1e-12), ("tc_kernel 1", k, e)
 
 
 @pytest.mark.gpu
