@@ -864,6 +864,8 @@ template <typename T, int S, int RT>
 cudaError_t launch_rt(const ShtGeom& g, const FftSet& s, bool inverse, cudaStream_t st) {
   typedef typename V2<T>::t T2;
   constexpr int KP = 33 * S + 1;
+  // the device-memory tables are built for 8-row CTAs (fft_df_global_twiddles)
+  static_assert(!GlobalTw<T, S>::v || (RT == 8 && S == 24), "device-memory twiddle tables: S = 24, 8 rows");
   const size_t smem = ((size_t)RT * KP + (GlobalTw<T, S>::v ? 0 : TwTab<S>::size)) * sizeof(T2);
   dim3 grid((g.n_theta + RT - 1) / RT, s.nf * s.nlev);
   auto k = inverse ? fft_inv_fast<T, S, RT> : fft_fwd_fast<T, S, RT>;
